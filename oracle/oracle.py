@@ -1,0 +1,165 @@
+"""ctypes front-end of the CPU ORACLE (oracle/rt_oracle.c) -- test
+infrastructure.  Only tests/, __graft_entry__.smoke() and the cpu_baseline
+leg of bench.py may use it, always as the checker / baseline, never as the
+product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "librt_oracle.so")
+SOURCES = [os.path.join(HERE, "rt_oracle.c")]
+
+RLK_NCONST = 24
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+
+
+class OracleAtmos(C.Structure):
+    _fields_ = [("ndep", C.c_int), ("muz", C.c_double)] + \
+        [(n, _D) for n in ("height", "T", "ne", "nHtot", "np", "vturb", "vel", "B",
+                           "gamma_B", "chi_B", "line_pops")]
+
+
+class OracleLines(C.Structure):
+    _fields_ = [("nline", C.c_int), ("maxcomp", C.c_int), ("magneto_optical", C.c_int),
+                ("moving", C.c_int), ("vmicro_char", C.c_double), ("c", _D),
+                ("zeeman", _D), ("ncomp", _I)]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (OpenMP for the threaded batch driver)."""
+    newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "rt_oracle.h")])
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
+        return LIB
+    subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-o", LIB] + SOURCES +
+                   ["-lm"], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(LIB)
+        _lib.oracle_lte_synth.restype = C.c_int
+        _lib.oracle_lte_synth_batch.restype = C.c_int
+        _lib.oracle_lte_opacity.restype = C.c_int
+        _lib.oracle_planck.restype = C.c_double
+        _lib.oracle_planck.argtypes = [C.c_double, C.c_double]
+        _lib.oracle_humlicek.argtypes = [C.c_double, C.c_double, _D, _D]
+        _lib.oracle_scalar_bezier3.restype = C.c_double
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(_D)
+
+
+class _Keep:
+    """Holds numpy arrays alive while ctypes structs point into them."""
+
+    def __init__(self):
+        self.arrays = []
+
+    def f64(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self.arrays.append(a)
+        return a
+
+
+def make_lines(line_const, zeeman, zeeman_n, vmicro_char, magneto_optical, moving,
+               keep: _Keep) -> OracleLines:
+    lc = keep.f64(line_const)
+    zm = keep.f64(zeeman)
+    zn = np.ascontiguousarray(zeeman_n, dtype=np.int32)
+    keep.arrays.append(zn)
+    L = OracleLines()
+    L.nline = lc.shape[0]
+    L.maxcomp = zm.shape[-1]
+    L.magneto_optical = int(magneto_optical)
+    L.moving = int(moving)
+    L.vmicro_char = float(vmicro_char)
+    L.c = _p(lc)
+    L.zeeman = _p(zm)
+    L.ncomp = zn.ctypes.data_as(_I)
+    return L
+
+
+def make_atmos(fx: dict, keep: _Keep, mu=None) -> OracleAtmos:
+    A = OracleAtmos()
+    A.ndep = len(fx["T"])
+    A.muz = float(fx["mu"] if mu is None else mu)
+    for n in ("height", "T", "ne", "nHtot", "np", "vturb", "vel", "B", "gamma_B",
+              "chi_B", "line_pops"):
+        setattr(A, n, _p(keep.f64(fx[n])))
+    return A
+
+
+def lte_synth(fx: dict, md_float: bool = True, lam=None, chi_c=None, eta_c=None):
+    """Emergent [4][nlam] Stokes of one atmosphere given as a fixture dict with
+    the keys written by tests/golden/make_golden.py."""
+    keep = _Keep()
+    A = make_atmos(fx, keep)
+    L = make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"], fx["vmicro_char"],
+                   fx["magneto_optical"], fx["moving"], keep)
+    lam = keep.f64(fx["lam"] if lam is None else lam)
+    cc = keep.f64(fx["chi_c"] if chi_c is None else chi_c)
+    ec = keep.f64(fx["eta_c"] if eta_c is None else eta_c)
+    out = np.zeros((4, len(lam)))
+    lib().oracle_lte_synth(C.byref(A), C.byref(L), len(lam), _p(lam), _p(cc), _p(ec),
+                           int(md_float), _p(out))
+    return out
+
+
+def lte_synth_batch(batch: dict, nthreads: int, md_float: bool = True):
+    """Threaded oracle over a batch dict whose per-atmosphere arrays carry a
+    leading atmosphere axis (lam shared)."""
+    keep = _Keep()
+    natm = batch["T"].shape[0]
+    atms = (OracleAtmos * natm)()
+    for p in range(natm):
+        fx = {k: batch[k][p] for k in ("height", "T", "ne", "nHtot", "np", "vturb",
+                                        "vel", "B", "gamma_B", "chi_B", "line_pops")}
+        fx["mu"] = batch["mu"]
+        atms[p] = make_atmos(fx, keep)
+    L = make_lines(batch["line_const"], batch["zeeman"], batch["zeeman_n"],
+                   batch["vmicro_char"], batch["magneto_optical"], batch["moving"], keep)
+    lam = keep.f64(batch["lam"])
+    cc = keep.f64(batch["chi_c"])
+    ec = keep.f64(batch["eta_c"])
+    out = np.zeros((natm, 4, len(lam)))
+    lib().oracle_lte_synth_batch(natm, nthreads, atms, C.byref(L), len(lam), _p(lam),
+                                 _p(cc), _p(ec), int(md_float), _p(out))
+    return out
+
+
+def lte_opacity(fx: dict, k: int, lam: float):
+    keep = _Keep()
+    A = make_atmos(fx, keep)
+    L = make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"], fx["vmicro_char"],
+                   fx["magneto_optical"], fx["moving"], keep)
+    chi = np.zeros(4); eta = np.zeros(4); chip = np.zeros(3)
+    flags = lib().oracle_lte_opacity(C.byref(A), C.byref(L), int(k), C.c_double(lam),
+                                     _p(chi), _p(eta), _p(chip))
+    return flags, chi, eta, chip
+
+
+def humlicek(a: float, v: float):
+    H = C.c_double(); F = C.c_double()
+    lib().oracle_humlicek(a, v, C.byref(H), C.byref(F))
+    return H.value, F.value
+
+
+def output_mask(lam: np.ndarray, lambda_ref: float) -> np.ndarray:
+    """Indices of the spectrum that rhf1d() returns: every wavelength except
+    the one equal to LAMBDA_REF (rh/rhf1d/pyrh_solveray.c:130-150)."""
+    return np.nonzero(lam != lambda_ref)[0]

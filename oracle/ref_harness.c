@@ -1,0 +1,298 @@
+/* ref_harness.c -- TEST INFRASTRUCTURE, compiled only against the reference.
+ *
+ * Thin C harness linked together with the reference's own RH sources into
+ * oracle/_ref/librh_ref.so (recipe: oracle/Makefile.ref).  It is used only to
+ * generate golden vectors in tests/golden/ and never ships with the product.
+ *
+ *  harness_synth     wraps rhf1d() (rh/rhf1d/pyrh_compute1dray.c:112-389) and
+ *                    copies the returned mySpectrum into caller buffers.
+ *  harness_dump_lte  performs the same set-up sequence as rhf1d()
+ *                    (pyrh_compute1dray.c:130-311) and writes the
+ *                    intermediate quantities the formal-solution hot path
+ *                    consumes (continuum, line constants, LTE stage densities,
+ *                    height scale, Zeeman patterns, total background records)
+ *                    as raw little-endian float64/int32 files into a directory.
+ *  harness_dump_nlte performs the whole rhf1d() sequence with one ACTIVE atom
+ *                    and writes the converged populations, the collision
+ *                    matrix, the wavelength grid and the emergent intensity.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+
+#include "rh.h"
+#include "atom.h"
+#include "atmos.h"
+#include "geometry.h"
+#include "spectrum.h"
+#include "background.h"
+#include "inputs.h"
+#include "constant.h"
+#include "error.h"
+#include "pyrh_compute1dray.h"
+
+extern Atmosphere atmos;
+extern Geometry geometry;
+extern Spectrum spectrum;
+extern InputData input;
+extern CommandLine commandline;
+
+void Linear(int Ntable, double *xtable, double *ytable, int N, double *x,
+            double *y, bool_t hunt);
+ZeemanMultiplet *RLKZeeman(RLK_Line *rlk);
+void convertScales(Atmosphere *atmos, Geometry *geometry);
+void getBoundary(Geometry *geometry);
+void MULTIatmos(Atmosphere *atmos, Geometry *geometry, int Nabun,
+                int *atomic_id, double *atomic_abundance);
+void Bproject(void);
+void Background(bool_t write_analyze_output, bool_t equilibria_only);
+
+static int write_f64(const char *dir, const char *name, const double *x, long n)
+{
+  char path[1024];
+  snprintf(path, sizeof(path), "%s/%s.f64", dir, name);
+  FILE *fp = fopen(path, "wb");
+  if (!fp) return -1;
+  long w = (long) fwrite(x, sizeof(double), n, fp);
+  fclose(fp);
+  return (w == n) ? 0 : -1;
+}
+
+static int write_i32(const char *dir, const char *name, const int *x, long n)
+{
+  char path[1024];
+  snprintf(path, sizeof(path), "%s/%s.i32", dir, name);
+  FILE *fp = fopen(path, "wb");
+  if (!fp) return -1;
+  long w = (long) fwrite(x, sizeof(int), n, fp);
+  fclose(fp);
+  return (w == n) ? 0 : -1;
+}
+
+/* Calls rhf1d() on private copies of the nine atmosphere rows (rhf1d mutates
+   its inputs in place, pyrh_compute1dray.c:263-270).  Returns the number of
+   output wavelengths, or -1 if out_cap is too small.  atm is [9][Ndep]. */
+int harness_synth(const char *cwd, double mu, int Ndep, const double *atm,
+                  int atm_scale, int Nwave, const double *lam,
+                  int out_cap, double *out_lam, double *sI, double *sQ,
+                  double *sU, double *sV, int *stokes_flag)
+{
+  double *a = (double *) malloc(9 * Ndep * sizeof(double));
+  double *w = (double *) malloc(Nwave * sizeof(double));
+  memcpy(a, atm, 9 * Ndep * sizeof(double));
+  memcpy(w, lam, Nwave * sizeof(double));
+
+  mySpectrum s = rhf1d((char *) cwd, mu, Ndep,
+                       a + 0 * Ndep, a + 1 * Ndep, a + 2 * Ndep, a + 3 * Ndep,
+                       a + 4 * Ndep, a + 5 * Ndep, a + 6 * Ndep, a + 7 * Ndep,
+                       a + 8 * Ndep, atm_scale, Nwave, w,
+                       0, NULL, NULL, 0, NULL, NULL, 0, NULL, NULL,
+                       0, NULL, NULL, 0, 0, 0, NULL);
+  int n = s.nlw;
+  if (n > out_cap) n = -1;
+  else {
+    for (int i = 0; i < n; i++) {
+      out_lam[i] = s.lam[i];
+      sI[i] = s.sI[i];
+      sQ[i] = s.stokes ? s.sQ[i] : 0.0;
+      sU[i] = s.stokes ? s.sU[i] : 0.0;
+      sV[i] = s.stokes ? s.sV[i] : 0.0;
+    }
+    *stokes_flag = s.stokes;
+  }
+  free(s.lam); free(s.sI); free(s.sQ); free(s.sU); free(s.sV);
+  free(a); free(w);
+  return n;
+}
+
+/* Set-up sequence of rhf1d() up to convertScales(), in the same order as
+   pyrh_compute1dray.c:130-311, followed by a dump of the hot-path inputs. */
+int harness_dump_lte(const char *cwd, double mu, int Ndep, const double *atm,
+                     int Nwave, const double *lam, const char *outdir)
+{
+  char tmp[512];
+  double *a = (double *) malloc(9 * Ndep * sizeof(double));
+  double *w = (double *) malloc(Nwave * sizeof(double));
+  memcpy(a, atm, 9 * Ndep * sizeof(double));
+  memcpy(w, lam, Nwave * sizeof(double));
+
+  snprintf(commandline.keyword_input, sizeof(commandline.keyword_input),
+           "%s/keyword.input", cwd);
+  setOptions(1, NULL);
+  readInput();
+  input.verbose = FALSE;
+  input.get_populations = FALSE;
+  input.pyrhHSE = FALSE;
+  input.get_atomic_rfs = FALSE;
+  input.n_atomic_pars = 0;
+  snprintf(tmp, sizeof(tmp), "%s/%s", cwd, input.atoms_input);
+  strcpy(input.atoms_input, tmp);
+  snprintf(tmp, sizeof(tmp), "%s/%s", cwd, input.molecules_input);
+  strcpy(input.molecules_input, tmp);
+  snprintf(tmp, sizeof(tmp), "%s/%s", cwd, input.KuruczData);
+  strcpy(input.KuruczData, tmp);
+  input.solve_ne = FALSE;
+  spectrum.updateJ = TRUE;
+  input.limit_memory = FALSE;
+  input.solve_NLTE = FALSE;
+  atmos.Nrlk = 0;
+  geometry.Ndep = Ndep;
+
+  MULTIatmos(&atmos, &geometry, 0, NULL, NULL);
+  atmos.active_layer = -1;
+  geometry.scale = TAU500;
+  for (int k = 0; k < Ndep; k++) geometry.tau_ref[k] = POW10(a[k]);
+  atmos.T = a + 1 * Ndep;
+  atmos.ne = a + 2 * Ndep;
+  geometry.vel = a + 3 * Ndep;
+  atmos.vturb = a + 4 * Ndep;
+  atmos.B = a + 5 * Ndep;
+  atmos.gamma_B = a + 6 * Ndep;
+  atmos.chi_B = a + 7 * Ndep;
+  atmos.nHtot = a + 8 * Ndep;
+  atmos.nH = matrix_double(atmos.NHydr, geometry.Ndep);
+  atmos.Stokes = TRUE;
+  atmos.moving = FALSE;
+  for (int k = 0; k < Ndep; k++) {
+    geometry.vel[k] *= KM_TO_M;
+    atmos.vturb[k] *= KM_TO_M;
+    atmos.ne[k] /= CUBE(CM_TO_M);
+    atmos.nHtot[k] /= CUBE(CM_TO_M);
+    atmos.B[k] /= 1e4;
+  }
+  for (int k = 0; k < Ndep; k++)
+    if (fabs(geometry.vel[k]) >= atmos.vmacro_tresh) { atmos.moving = TRUE; break; }
+
+  readAtomicModels();
+  readMolecularModels();
+  atmos.Nrays = geometry.Nrays = 1;
+  geometry.muz[0] = mu;
+  geometry.mux[0] = sqrt(1.0 - SQ(geometry.muz[0]));
+  geometry.muy[0] = 0.0;
+  geometry.wmu[0] = 1.0;
+  Bproject();
+  SortLambda(w, Nwave);
+  getBoundary(&geometry);
+
+  int Nspect = spectrum.Nspect, Nspace = atmos.Nspace;
+
+  /* Pass 1: continuum only.  Background() reads the Kurucz list itself
+     when none is loaded (background.c:288-293), so the list name is set to
+     "none" for this pass (kurucz.c:140). */
+  char kurucz_saved[MAX_LINE_SIZE];
+  strcpy(kurucz_saved, input.KuruczData);
+  strcpy(input.KuruczData, "none");
+  atmos.Nrlk = 0;
+  Background(FALSE, FALSE);
+  strcpy(input.KuruczData, kurucz_saved);
+  double *cont = (double *) malloc(3 * (long) Nspect * Nspace * sizeof(double));
+  int *cflags = (int *) malloc(2 * Nspect * sizeof(int));
+  for (int la = 0; la < Nspect; la++) {
+    memcpy(cont + (0L * Nspect + la) * Nspace, spectrum.chi_c_lam[la], Nspace * sizeof(double));
+    memcpy(cont + (1L * Nspect + la) * Nspace, spectrum.eta_c_lam[la], Nspace * sizeof(double));
+    memcpy(cont + (2L * Nspect + la) * Nspace, spectrum.sca_c_lam[la], Nspace * sizeof(double));
+    cflags[2 * la] = atmos.backgrflags[la].hasline;
+    cflags[2 * la + 1] = atmos.backgrflags[la].ispolarized;
+  }
+  /* Pass 2: with the Kurucz lines, as rhf1d() runs it. */
+  atmos.Nrlk = 0;
+  Background(FALSE, FALSE);
+  convertScales(&atmos, &geometry);
+
+  double *tot_chi = (double *) malloc(4L * Nspect * Nspace * sizeof(double));
+  double *tot_eta = (double *) malloc(4L * Nspect * Nspace * sizeof(double));
+  double *tot_chip = (double *) calloc(3L * Nspect * Nspace, sizeof(double));
+  int *tflags = (int *) malloc(2 * Nspect * sizeof(int));
+  for (int la = 0; la < Nspect; la++) {
+    int nrec = atmos.backgrflags[la].ispolarized ? 4 : 1;
+    for (int i = 0; i < 4 * Nspace; i++) {
+      tot_chi[(long) la * 4 * Nspace + i] = (i < nrec * Nspace) ? spectrum.chi_c_lam[la][i] : 0.0;
+      tot_eta[(long) la * 4 * Nspace + i] = (i < nrec * Nspace) ? spectrum.eta_c_lam[la][i] : 0.0;
+    }
+    if (input.magneto_optical && atmos.backgrflags[la].ispolarized)
+      memcpy(tot_chip + (long) la * 3 * Nspace, spectrum.chip_c_lam[la], 3 * Nspace * sizeof(double));
+    tflags[2 * la] = atmos.backgrflags[la].hasline;
+    tflags[2 * la + 1] = atmos.backgrflags[la].ispolarized;
+  }
+
+  write_f64(outdir, "lambda", spectrum.lambda, Nspect);
+  write_f64(outdir, "cont", cont, 3L * Nspect * Nspace);
+  write_i32(outdir, "cont_flags", cflags, 2 * Nspect);
+  write_f64(outdir, "tot_chi", tot_chi, 4L * Nspect * Nspace);
+  write_f64(outdir, "tot_eta", tot_eta, 4L * Nspect * Nspace);
+  write_f64(outdir, "tot_chip", tot_chip, 3L * Nspect * Nspace);
+  write_i32(outdir, "tot_flags", tflags, 2 * Nspect);
+  write_f64(outdir, "height", geometry.height, Nspace);
+  write_f64(outdir, "T", atmos.T, Nspace);
+  write_f64(outdir, "ne", atmos.ne, Nspace);
+  write_f64(outdir, "nHtot", atmos.nHtot, Nspace);
+  write_f64(outdir, "vturb", atmos.vturb, Nspace);
+  write_f64(outdir, "vel", geometry.vel, Nspace);
+  write_f64(outdir, "B", atmos.B, Nspace);
+  write_f64(outdir, "gamma_B", atmos.gamma_B, Nspace);
+  write_f64(outdir, "chi_B", atmos.chi_B, Nspace);
+  write_f64(outdir, "np", atmos.H->n[atmos.H->Nlevel - 1], Nspace);
+  write_f64(outdir, "cos_gamma", atmos.cos_gamma[0], Nspace);
+  write_f64(outdir, "cos_2chi", atmos.cos_2chi[0], Nspace);
+  write_f64(outdir, "sin_2chi", atmos.sin_2chi[0], Nspace);
+
+  /* Line constants (double[24] per line), Zeeman patterns and stage
+     densities n[stage][k] with log partition function pf[k] as used in
+     rlk_opacity (kurucz.c:662-677). */
+  double *lc = (double *) calloc(24L * atmos.Nrlk, sizeof(double));
+  double *lpop = (double *) calloc(2L * atmos.Nrlk * Nspace, sizeof(double));
+  int maxcomp = 0;
+  for (int n = 0; n < atmos.Nrlk; n++) {
+    RLK_Line *r = &atmos.rlk_lines[n];
+    if (r->polarizable && r->zm == NULL) r->zm = RLKZeeman(r);
+    if (r->zm && r->zm->Ncomponent > maxcomp) maxcomp = r->zm->Ncomponent;
+  }
+  double *zm = (double *) calloc(3L * atmos.Nrlk * (maxcomp > 0 ? maxcomp : 1), sizeof(double));
+  int *zn = (int *) calloc(atmos.Nrlk > 0 ? atmos.Nrlk : 1, sizeof(int));
+  for (int n = 0; n < atmos.Nrlk; n++) {
+    RLK_Line *r = &atmos.rlk_lines[n];
+    Element *el = &atmos.elements[r->pt_index - 1];
+    double *L = lc + 24L * n;
+    L[0] = r->lambda0; L[1] = r->pt_index; L[2] = r->stage; L[3] = r->gi;
+    L[4] = r->gj; L[5] = r->Ei; L[6] = r->Ej; L[7] = r->Aji; L[8] = r->Bji;
+    L[9] = r->Bij; L[10] = r->Grad; L[11] = r->GStark; L[12] = r->GvdWaals;
+    L[13] = r->vdwaals; L[14] = r->cross; L[15] = r->alpha;
+    L[16] = r->isotope_frac; L[17] = r->hyperfine_frac; L[18] = r->polarizable;
+    L[19] = el->weight; L[20] = (r->stage < el->Nstage - 1) && el->abundance_set;
+    L[21] = r->gL_i; L[22] = r->gL_j; L[23] = (el->model != NULL);
+    if (el->n == NULL) {
+      el->n = matrix_double(el->Nstage, Nspace);
+      LTEpops_elem(el);
+    }
+    double *pf = (double *) malloc(Nspace * sizeof(double));
+    Linear(atmos.Npf, atmos.Tpf, el->pf[r->stage], Nspace, atmos.T, pf, TRUE);
+    for (int k = 0; k < Nspace; k++) {
+      lpop[(2L * n + 0) * Nspace + k] = el->n[r->stage][k];
+      lpop[(2L * n + 1) * Nspace + k] = pf[k];
+    }
+    free(pf);
+    if (r->zm) {
+      zn[n] = r->zm->Ncomponent;
+      for (int c = 0; c < r->zm->Ncomponent; c++) {
+        zm[(3L * n + 0) * maxcomp + c] = r->zm->q[c];
+        zm[(3L * n + 1) * maxcomp + c] = r->zm->shift[c];
+        zm[(3L * n + 2) * maxcomp + c] = r->zm->strength[c];
+      }
+    }
+  }
+  write_f64(outdir, "line_const", lc, 24L * atmos.Nrlk);
+  write_f64(outdir, "line_pops", lpop, 2L * atmos.Nrlk * Nspace);
+  write_f64(outdir, "zeeman", zm, 3L * atmos.Nrlk * (maxcomp > 0 ? maxcomp : 1));
+  write_i32(outdir, "zeeman_n", zn, atmos.Nrlk > 0 ? atmos.Nrlk : 1);
+
+  int meta[8] = {Nspect, Nspace, atmos.Nrlk, maxcomp, input.magneto_optical,
+                 atmos.moving, geometry.vboundary[TOP], geometry.vboundary[BOTTOM]};
+  write_i32(outdir, "meta", meta, 8);
+  double fmeta[4] = {atmos.vmicro_char, atmos.lambda_ref, mu, (double) input.StokesMode};
+  write_f64(outdir, "fmeta", fmeta, 4);
+
+  free(cont); free(cflags); free(tot_chi); free(tot_eta); free(tot_chip);
+  free(tflags); free(lc); free(lpop); free(zm); free(zn);
+  return Nspect;
+}

@@ -1,0 +1,264 @@
+"""Runs the compiled REFERENCE (oracle/_ref/librh_ref.so) -- test infrastructure.
+
+Only the golden-vector generator (tests/golden/make_golden.py) and the
+reference arm of the CPU baseline use this module, and only where the
+reference sources were available to build oracle/_ref (never on a machine
+without them).  Every reference call runs in a fresh spawned process because
+the reference keeps process-global state and is not re-entrant
+(rh/rhf1d/pyrh_compute1dray.c:86-92).
+
+Reference entry points driven here:
+  hse()    rh/rhf1d/pyrh_hse.c:67   (ne, nHtot in m^-3 for a T(log tau) model)
+  rhf1d()  rh/rhf1d/pyrh_compute1dray.c:112 via harness_synth
+  set-up of rhf1d() + Background() dump via harness_dump_lte
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import shutil
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_LIB = os.path.join(HERE, "_ref", "librh_ref.so")
+# Same sources built without -DSIMDON: the scalar float 4x4 inverse of
+# rh/bezier_aux.c:235-328 (what the reference compiles to on Arm) instead of
+# the SSE reciprocal-estimate inverse of rh/bezier_aux.c:133-232.
+REF_LIB_PORTABLE = os.path.join(HERE, "_ref", "portable", "librh_ref.so")
+REF_ROOT = os.environ.get("PYRH_REFERENCE_ROOT", "/root/reference")
+
+_P = C.POINTER(C.c_double)
+
+
+def build_ref(ref_root: str = REF_ROOT) -> str:
+    """Compile the reference sources into oracle/_ref/librh_ref.so and the
+    portable variant into oracle/_ref/portable/librh_ref.so."""
+    repo = os.path.dirname(HERE)
+    jobs = f"-j{os.cpu_count() or 4}"
+    subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={ref_root}", jobs],
+                   cwd=repo, check=True)
+    subprocess.run(["make", "-s", "-f", "oracle/Makefile.ref", f"REF={ref_root}",
+                    "OUT=oracle/_ref/portable", "SIMD=", jobs], cwd=repo, check=True)
+    return REF_LIB
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(_P)
+
+
+# ---------------------------------------------------------------- input set --
+
+KEYWORD_TEMPLATE = """\
+  NRAYS = {nrays}
+  ATOMS_FILE = atoms.input
+  MOLECULES_FILE = molecules.input
+  N_MAX_SCATTER = {nmax_scatter}
+  I_SUM = -1
+  N_MAX_ITER = {nmax_iter}
+  ITER_LIMIT = {iter_limit}
+  NG_ORDER  = {ng_order}
+  NG_DELAY  = {ng_delay}
+  NG_PERIOD = {ng_period}
+  PRD_N_MAX_ITER = 1
+  PRD_ITER_LIMIT = 1.0E-2
+  J_FILE          = J.dat
+  STARTING_J      = NEW_J
+  BACKGROUND_FILE = background.dat
+  OLD_BACKGROUND  = FALSE
+  KURUCZ_DATA = {kurucz}
+  SOLVE_NE = NONE
+  RLK_SCATTER = FALSE
+  HYDROGEN_LTE = TRUE
+  VMICRO_CHAR = {vmicro_char}
+  VMACRO_TRESH = 0
+  S_INTERPOLATION = S_BEZIER3
+  S_INTERPOLATION_STOKES = DELO_BEZIER3
+  VACUUM_TO_AIR = FALSE
+  STOKES_MODE = {stokes_mode}
+  MAGNETO_OPTICAL = {magneto_optical}
+  LS_LANDE = FALSE
+  LIMIT_MEMORY = FALSE
+  ALLOW_PASSIVE_BB = FALSE
+  PRINT_CPU = FALSE
+"""
+
+PASSIVE_ATOMS = ["H_6.atom", "He.atom", "C.atom", "N.atom", "O.atom", "S.atom",
+                 "Fe.atom", "Si.atom", "Al.atom", "Na.atom", "Mg.atom"]
+
+
+def write_inputs(workdir: str, kurucz_lines: str | None, atoms=None,
+                 active: str | None = None, **kw) -> None:
+    """Write keyword.input, atoms.input, molecules.input, kurucz.input."""
+    opts = dict(nrays=1, nmax_scatter=0, nmax_iter=1, iter_limit="1.0E-2",
+                ng_order=0, ng_delay=10, ng_period=3, vmicro_char=5.0,
+                stokes_mode="FULL_STOKES", magneto_optical="FALSE",
+                kurucz="kurucz.input" if kurucz_lines else "none")
+    opts.update(kw)
+    with open(os.path.join(workdir, "keyword.input"), "w") as f:
+        f.write(KEYWORD_TEMPLATE.format(**opts))
+    atoms = list(atoms or PASSIVE_ATOMS)
+    with open(os.path.join(workdir, "atoms.input"), "w") as f:
+        f.write(f"{len(atoms)}\n")
+        for a in atoms:
+            mode = "ACTIVE" if a == active else "PASSIVE"
+            f.write(f"  {a}  {mode}  LTE_POPULATIONS  pops.out\n")
+    shutil.copy(os.path.join(REF_ROOT, "tests", "molecules.input"), workdir)
+    if kurucz_lines:
+        path = os.path.join(workdir, "lines.kurucz")
+        with open(path, "w") as f:
+            f.write(kurucz_lines)
+        with open(os.path.join(workdir, "kurucz.input"), "w") as f:
+            f.write(path + "\n")
+
+
+# ------------------------------------------------------------ subprocesses --
+
+def _lib(pyrh_path: str):
+    os.environ["PYRH_PATH"] = pyrh_path
+    return C.CDLL(os.environ.get("PYRH_REF_LIB", REF_LIB))
+
+
+def _hse_job(args):
+    workdir, pyrh_path, logtau, T = args
+    lib = _lib(pyrh_path)
+    n = len(logtau)
+    logtau = np.ascontiguousarray(logtau, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    ne, nH, rho, pg = (np.zeros(n) for _ in range(4))
+    pg[0] = 0.1
+    lib.hse.restype = None
+    lib.hse(workdir.encode(), n, _p(logtau), _p(T), _p(ne), _p(nH), _p(rho),
+            _p(pg), 0, 0, None, None, 0, None, None)
+    return ne, nH
+
+
+def _synth_job(args):
+    workdir, pyrh_path, mu, atm, wave = args
+    lib = _lib(pyrh_path)
+    atm = np.ascontiguousarray(atm, dtype=np.float64)
+    wave = np.ascontiguousarray(wave, dtype=np.float64)
+    cap = len(wave) + 4096
+    out = [np.zeros(cap) for _ in range(5)]
+    flag = C.c_int(0)
+    lib.harness_synth.restype = C.c_int
+    n = lib.harness_synth(workdir.encode(), C.c_double(mu), atm.shape[1],
+                          _p(atm), 0, len(wave), _p(wave), cap,
+                          *[_p(o) for o in out], C.byref(flag))
+    if n < 0:
+        raise RuntimeError("reference output larger than capacity")
+    lam, sI, sQ, sU, sV = (o[:n].copy() for o in out)
+    return lam, np.stack([sI, sQ, sU, sV]), flag.value
+
+
+def _dump_job(args):
+    workdir, pyrh_path, mu, atm, wave, outdir = args
+    lib = _lib(pyrh_path)
+    atm = np.ascontiguousarray(atm, dtype=np.float64)
+    wave = np.ascontiguousarray(wave, dtype=np.float64)
+    os.makedirs(outdir, exist_ok=True)
+    lib.harness_dump_lte.restype = C.c_int
+    return lib.harness_dump_lte(workdir.encode(), C.c_double(mu), atm.shape[1],
+                                _p(atm), len(wave), _p(wave), outdir.encode())
+
+
+def _vac2air_job(args):
+    pyrh_path, lam_vac = args
+    lib = _lib(pyrh_path)
+    lam_vac = np.ascontiguousarray(lam_vac, dtype=np.float64)
+    out = np.zeros_like(lam_vac)
+    lib.vacuum_to_air.restype = None
+    lib.vacuum_to_air(len(lam_vac), _p(lam_vac), _p(out))
+    return out
+
+
+class Reference:
+    """Runs every reference call in a fresh interpreter (subprocess with a
+    time limit), since the reference keeps global state, leaks memory and
+    calls exit() on errors (rh/error.c:45-60)."""
+
+    def __init__(self, pyrh_path: str = REF_ROOT, timeout: float = 600.0,
+                 lib_path: str = REF_LIB):
+        if not (os.path.exists(REF_LIB) and os.path.exists(REF_LIB_PORTABLE)):
+            build_ref()
+        self.pyrh_path = pyrh_path
+        self.timeout = timeout
+        self.lib_path = lib_path
+
+    def _run(self, fn, args):
+        import pickle
+        import sys
+        with tempfile.TemporaryDirectory(prefix="rhjob_") as td:
+            src, dst = os.path.join(td, "in.pkl"), os.path.join(td, "out.pkl")
+            with open(src, "wb") as f:
+                pickle.dump((fn.__name__, args), f)
+            repo = os.path.dirname(HERE)
+            env = dict(os.environ, PYRH_REF_LIB=self.lib_path)
+            r = subprocess.run([sys.executable, "-m", "oracle.ref_runner", src, dst],
+                               cwd=repo, timeout=self.timeout, capture_output=True,
+                               text=True, env=env)
+            if r.returncode != 0 or not os.path.exists(dst):
+                raise RuntimeError(f"reference call {fn.__name__} failed "
+                                   f"(rc={r.returncode}): {r.stderr[-2000:]}"
+                                   f"{r.stdout[-2000:]}")
+            with open(dst, "rb") as f:
+                return pickle.load(f)
+
+    def map(self, fn, arglist, procs=None):
+        from concurrent.futures import ThreadPoolExecutor
+        procs = procs or min(len(arglist), os.cpu_count() or 4)
+        with ThreadPoolExecutor(procs) as ex:
+            return list(ex.map(lambda a: self._run(fn, a), arglist))
+
+    def hse(self, workdir, logtau, T):
+        return self._run(_hse_job, (workdir, self.pyrh_path, logtau, T))
+
+    def synth(self, workdir, mu, atm, wave):
+        return self._run(_synth_job, (workdir, self.pyrh_path, mu, atm, wave))
+
+    def dump_lte(self, workdir, mu, atm, wave, outdir):
+        return self._run(_dump_job, (workdir, self.pyrh_path, mu, atm, wave, outdir))
+
+    def vacuum_to_air(self, lam_vac):
+        return self._run(_vac2air_job, (self.pyrh_path, lam_vac))
+
+
+def read_dump(outdir: str) -> dict:
+    """Load the files written by harness_dump_lte into numpy arrays."""
+    meta = np.fromfile(os.path.join(outdir, "meta.i32"), dtype=np.int32)
+    nspect, nspace, nrlk, maxcomp = (int(x) for x in meta[:4])
+    d = {"meta": meta, "fmeta": np.fromfile(os.path.join(outdir, "fmeta.f64"))}
+    f64 = lambda n: np.fromfile(os.path.join(outdir, n + ".f64"))
+    i32 = lambda n: np.fromfile(os.path.join(outdir, n + ".i32"), dtype=np.int32)
+    d["lambda"] = f64("lambda")
+    d["cont"] = f64("cont").reshape(3, nspect, nspace)
+    d["cont_flags"] = i32("cont_flags").reshape(nspect, 2)
+    d["tot_chi"] = f64("tot_chi").reshape(nspect, 4, nspace)
+    d["tot_eta"] = f64("tot_eta").reshape(nspect, 4, nspace)
+    d["tot_chip"] = f64("tot_chip").reshape(nspect, 3, nspace)
+    d["tot_flags"] = i32("tot_flags").reshape(nspect, 2)
+    for n in ["height", "T", "ne", "nHtot", "vturb", "vel", "B", "gamma_B",
+              "chi_B", "np", "cos_gamma", "cos_2chi", "sin_2chi"]:
+        d[n] = f64(n)
+    d["line_const"] = f64("line_const").reshape(nrlk, 24)
+    d["line_pops"] = f64("line_pops").reshape(nrlk, 2, nspace)
+    mc = max(maxcomp, 1)
+    d["zeeman"] = f64("zeeman").reshape(nrlk, 3, mc)
+    d["zeeman_n"] = i32("zeeman_n")[:nrlk]
+    return d
+
+
+def scratch_dir(prefix="rhref_") -> str:
+    return tempfile.mkdtemp(prefix=prefix)
+
+
+if __name__ == "__main__":
+    import pickle
+    import sys
+    with open(sys.argv[1], "rb") as f:
+        name, args = pickle.load(f)
+    result = globals()[name](args)
+    with open(sys.argv[2], "wb") as f:
+        pickle.dump(result, f)

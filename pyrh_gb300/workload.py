@@ -1,0 +1,148 @@
+"""Synthetic atmospheres, line lists and wavelength grids for the benchmark
+workloads (plain LTE synthesis of one 71-depth atmosphere; the batched form of
+16384 perturbed atmospheres; the NLTE six-level atom cases).
+
+The atmosphere model follows the stated generator: log tau500 uniform from -6
+to +1, T = 5777 (0.75 (tau + 2/3))^0.25 + 2000 exp(-(log tau + 5)^2) K,
+v_mic 1 km/s, B 1000 G, inclination 45 deg, azimuth 30 deg.  Atmosphere rows
+follow pyrh.compute1d (reference pyrh.pyx:621-625): scale, T [K], ne [cm^-3],
+v_los [km/s], v_mic [km/s], B [G], gamma [rad], chi [rad], nH [cm^-3].
+
+Perturbations for the batched workloads: T offsets drawn N(0, 300 K) at the
+nodes log tau = -2, -0.8, 0 and interpolated with a natural cubic spline
+(held constant outside the node range); v_los uniform in [-3, 3] km/s;
+B log-uniform in [10, 3000] G; cos(inclination) uniform in [-1, 1];
+azimuth uniform in [0, pi).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# Physical constants with the values the reference uses (rh/constant.h:28-68).
+CLIGHT = 2.99792458e8
+HPLANCK = 6.6260755e-34
+KBOLTZMANN = 1.380658e-23
+EV = 1.60217733e-19
+CM_TO_M = 1.0e-2
+
+T_NODES = (-2.0, -0.8, 0.0)
+
+# Two Zeeman-split Fe I-like lines: vacuum centre [nm], log gf, chi_low [eV],
+# (J_low, J_up), (gL_low, gL_up) giving g_eff 1.67 and 2.49, terms, damping
+# (log Grad, log GStark, log GvdW), orbital l of (low, up) for ABO broadening.
+FE_LINES = (
+    dict(lam_vac=630.15, loggf=-0.72, chi_low=3.65, J=(2.0, 2.0),
+         gL=(1.835, 1.503), labels=("5Dsp3P z5P", "4s6D5s e5D"),
+         damp=(8.08, -5.42, -7.54), orbital=(1, 0)),
+    dict(lam_vac=630.25, loggf=-1.24, chi_low=3.69, J=(1.0, 0.0),
+         gL=(2.487, 0.000), labels=("5Dsp3P z5P", "4s6D5s e5D"),
+         damp=(8.08, -5.40, -7.54), orbital=(1, 0)),
+)
+
+
+def logtau_grid(ndep: int = 71) -> np.ndarray:
+    return np.linspace(-6.0, 1.0, ndep)
+
+
+def base_temperature(logtau: np.ndarray) -> np.ndarray:
+    tau = 10.0 ** logtau
+    return 5777.0 * (0.75 * (tau + 2.0 / 3.0)) ** 0.25 + \
+        2000.0 * np.exp(-(logtau + 5.0) ** 2)
+
+
+def natural_spline(xn, yn, x):
+    """Natural cubic spline through (xn, yn), constant outside [xn0, xn-1]."""
+    xn = np.asarray(xn, dtype=np.float64)
+    yn = np.asarray(yn, dtype=np.float64)
+    n = len(xn)
+    h = np.diff(xn)
+    A = np.zeros((n, n))
+    r = np.zeros(n)
+    A[0, 0] = A[-1, -1] = 1.0
+    for i in range(1, n - 1):
+        A[i, i - 1] = h[i - 1]
+        A[i, i] = 2.0 * (h[i - 1] + h[i])
+        A[i, i + 1] = h[i]
+        r[i] = 6.0 * ((yn[i + 1] - yn[i]) / h[i] - (yn[i] - yn[i - 1]) / h[i - 1])
+    M = np.linalg.solve(A, r)
+    xc = np.clip(x, xn[0], xn[-1])
+    j = np.clip(np.searchsorted(xn, xc) - 1, 0, n - 2)
+    t0 = xn[j + 1] - xc
+    t1 = xc - xn[j]
+    hj = h[j]
+    return (M[j] * t0 ** 3 + M[j + 1] * t1 ** 3) / (6.0 * hj) + \
+        (yn[j] / hj - M[j] * hj / 6.0) * t0 + (yn[j + 1] / hj - M[j + 1] * hj / 6.0) * t1
+
+
+def perturbations(n: int, seed: int, logtau: np.ndarray) -> dict:
+    """Seeded per-atmosphere perturbations (T offsets, v_los, B, angles)."""
+    rng = np.random.default_rng(seed)
+    dT_nodes = rng.normal(0.0, 300.0, size=(n, len(T_NODES)))
+    dT = np.stack([natural_spline(T_NODES, dT_nodes[i], logtau) for i in range(n)])
+    vlos = rng.uniform(-3.0, 3.0, size=n)
+    B = 10.0 ** rng.uniform(1.0, np.log10(3000.0), size=n)
+    gamma = np.arccos(rng.uniform(-1.0, 1.0, size=n))
+    chi = rng.uniform(0.0, np.pi, size=n)
+    return dict(dT=dT, vlos=vlos, B=B, gamma=gamma, chi=chi)
+
+
+def atmosphere_rows(logtau, T, ne_cm3, nH_cm3, vlos=0.0, vmic=1.0, B=1000.0,
+                    gamma=np.deg2rad(45.0), chi=np.deg2rad(30.0)) -> np.ndarray:
+    nd = len(logtau)
+    atm = np.zeros((9, nd))
+    atm[0] = logtau
+    atm[1] = T
+    atm[2] = ne_cm3
+    atm[3] = vlos
+    atm[4] = vmic
+    atm[5] = B
+    atm[6] = gamma
+    atm[7] = chi
+    atm[8] = nH_cm3
+    return atm
+
+
+def line_wavelengths(n_per_line: int = 201, half_width: float = 0.05,
+                     centres=(630.15, 630.25)) -> np.ndarray:
+    return np.concatenate([np.linspace(c - half_width, c + half_width, n_per_line)
+                           for c in centres])
+
+
+def kurucz_record(lam_air, loggf, code, E_low_cm, J_low, label_low, E_up_cm,
+                  J_up, label_up, damp, gL_low, gL_up, l_low, l_up) -> str:
+    """One line of a Kurucz-format list at the fixed columns that the
+    reference reader uses (rh/kurucz.c:187-373): wavelength, log gf, code and
+    first energy by whitespace, J at +35, labels at +41 and +69, second energy
+    at +53, J at +63, damping at +79, isotope data at +106/+108/+117,
+    hyperfine shifts at +123, Lande factors x1000 at +143, orbital l at +160."""
+    rec = (f"{lam_air:11.4f}{loggf:7.3f}{code:6.2f}{E_low_cm:11.3f}{J_low:5.1f} "
+           f"{label_low:10s}  {E_up_cm:10.3f}{J_up:5.1f} {label_up:10s}"
+           f"{damp[0]:6.2f}{damp[1]:6.2f}{damp[2]:6.2f}"
+           f"{'SYNT':4s} 0 0{0:3d}{0.0:6.3f}{0:3d}{0.0:6.3f}{0:5d}{0:5d}"
+           f"{'':10s}{int(round(gL_low * 1000)):5d}{int(round(gL_up * 1000)):5d}"
+           f"{'':7s}{l_low} {l_up}")
+    assert rec[35:40].strip() and rec[143:153].strip() and len(rec) <= 171
+    return rec
+
+
+def vacuum_to_air(lam_vac: np.ndarray) -> np.ndarray:
+    """Vacuum to air wavelength [nm] with the reference's formula for
+    lambda >= 200 nm (rh/vacuumtoair.c:29-48)."""
+    lam_vac = np.asarray(lam_vac, dtype=np.float64)
+    sq = 1.0 / lam_vac ** 2
+    red = 1.0 + 2.735182e-4 + (1.314182 + 2.76249e4 * sq) * sq
+    return np.where(lam_vac >= 200.0, lam_vac / red, lam_vac)
+
+
+def fe_linelist(lines=FE_LINES) -> str:
+    out = []
+    hc_cm = HPLANCK * CLIGHT / CM_TO_M          # J per cm^-1
+    for L in lines:
+        lam_air = float(vacuum_to_air(np.array([L["lam_vac"]]))[0])
+        E_low = L["chi_low"] * EV / hc_cm
+        E_up = E_low + 1.0e7 / lam_air
+        out.append(kurucz_record(lam_air, L["loggf"], 26.00, E_low, L["J"][0],
+                                 L["labels"][0], E_up, L["J"][1], L["labels"][1],
+                                 L["damp"], L["gL"][0], L["gL"][1],
+                                 L["orbital"][0], L["orbital"][1]))
+    return "\n".join(out) + "\n"

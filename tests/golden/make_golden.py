@@ -1,0 +1,163 @@
+"""Generates the golden fixtures in tests/golden/ from the compiled REFERENCE.
+
+Run in a checkout where the reference sources are available (it builds
+oracle/_ref/librh_ref.so from them with oracle/Makefile.ref):
+
+    python tests/golden/make_golden.py [--only NAME ...]
+
+Every number stored here comes out of the reference's own C code
+(rhf1d(), hse(), Background(), RLKZeeman(), LTEpops_elem()), driven through
+oracle/ref_harness.c.  Nothing in the product reads these files; tests do.
+
+Fixtures (npz, float64):
+  lte_c0          plain LTE polarized synthesis, 71 depths, 2 x 201 lambda,
+                  mu=1 (MAGNETO_OPTICAL = FALSE: with TRUE the reference
+                  writes four records into the three-record chip_c_lam buffer,
+                  rh/readj.c:330 vs rh/sortlambda.c:574, and crashes)
+  lte_edge        mu=0.5, velocity gradient, strong field, lambda points
+                  outside every line window, duplicate and unsorted lambda
+  lte_b0          B = 0 (polarizable lines with no splitting)
+  lte_batch       6 atmospheres of the batched generator (2 x 112 lambda)
+
+stokes_ref comes from the reference as setup.py builds it on x86 (-DSIMDON,
+SSE reciprocal-estimate 4x4 inverse); stokes_ref_portable from the same
+sources without -DSIMDON (scalar float inverse, the Arm build).
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from oracle import ref_runner as rr  # noqa: E402
+from pyrh_gb300 import workload as wl  # noqa: E402
+
+PORTABLE = None
+OPAC_STRIDE = 8      # keep the reference's total background record every 8th lambda
+
+
+def base_c0(ref: rr.Reference, workdir: str, ndep: int = 71):
+    logtau = wl.logtau_grid(ndep)
+    T = wl.base_temperature(logtau)
+    ne, nH = ref.hse(workdir, logtau, T)
+    return logtau, T, ne / 1e6, nH / 1e6
+
+
+def lte_case(ref, name, atm, wave, mu=1.0, magneto_optical="FALSE",
+             extra=None):
+    wd = rr.scratch_dir()
+    rr.write_inputs(wd, wl.fe_linelist(), magneto_optical=magneto_optical)
+    lam_out, stokes, flag = ref.synth(wd, mu, atm, wave)
+    _, stokes_portable, _ = PORTABLE.synth(wd, mu, atm, wave)
+    dd = os.path.join(wd, "dump")
+    ref.dump_lte(wd, mu, atm, wave, dd)
+    d = rr.read_dump(dd)
+    nspect = len(d["lambda"])
+    sel = np.arange(0, nspect, OPAC_STRIDE)
+    out = dict(
+        atm=atm, wave=wave, mu=np.float64(mu),
+        magneto_optical=np.int32(magneto_optical == "TRUE"),
+        vmicro_char=np.float64(d["fmeta"][0]), lambda_ref=np.float64(d["fmeta"][1]),
+        moving=np.int32(d["meta"][5]),
+        lam_out=lam_out, stokes_ref=stokes, stokes_flag=np.int32(flag),
+        stokes_ref_portable=stokes_portable,
+        lam=d["lambda"], chi_c=d["cont"][0], eta_c=d["cont"][1],
+        cont_flags=d["cont_flags"],
+        height=d["height"], T=d["T"], ne=d["ne"], nHtot=d["nHtot"], np=d["np"],
+        vturb=d["vturb"], vel=d["vel"], B=d["B"], gamma_B=d["gamma_B"],
+        chi_B=d["chi_B"], cos_gamma=d["cos_gamma"], cos_2chi=d["cos_2chi"],
+        sin_2chi=d["sin_2chi"],
+        line_const=d["line_const"], line_pops=d["line_pops"],
+        zeeman=d["zeeman"], zeeman_n=d["zeeman_n"],
+        opac_idx=sel, tot_chi=d["tot_chi"][sel], tot_eta=d["tot_eta"][sel],
+        tot_chip=d["tot_chip"][sel], tot_flags=d["tot_flags"],
+    )
+    if extra:
+        out.update(extra)
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    shutil.rmtree(wd, ignore_errors=True)
+    print(f"{name}: {len(lam_out)} lambda, {atm.shape[1]} depths, "
+          f"{os.path.getsize(path) / 1e3:.0f} kB")
+    return out
+
+
+def make_lte_c0(ref, wd):
+    logtau, T, ne, nH = base_c0(ref, wd)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH)
+    wave = wl.line_wavelengths(201, 0.05)
+    lte_case(ref, "lte_c0", atm, wave)
+
+
+def make_lte_edge(ref, wd):
+    logtau, T, ne, nH = base_c0(ref, wd)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH, B=3000.0,
+                             gamma=np.deg2rad(70.0), chi=np.deg2rad(120.0))
+    atm[3] = np.linspace(-2.5, 1.5, len(logtau))      # velocity gradient
+    atm[4] = np.linspace(2.0, 0.5, len(logtau))
+    core = wl.line_wavelengths(21, 0.04)
+    far = np.array([629.70, 629.85, 630.55, 630.80])    # outside 20 v_char/c
+    wave = np.concatenate([core[::-1][:30], far, core[::-1][30:], core[5:8]])
+    lte_case(ref, "lte_edge", atm, wave, mu=0.5)
+
+
+def make_lte_b0(ref, wd):
+    logtau, T, ne, nH = base_c0(ref, wd)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH, B=0.0)
+    wave = wl.line_wavelengths(31, 0.05)
+    lte_case(ref, "lte_b0", atm, wave)
+
+
+def make_lte_batch(ref, wd, n=6, seed=2024):
+    logtau = wl.logtau_grid(71)
+    T0 = wl.base_temperature(logtau)
+    pert = wl.perturbations(n, seed, logtau)
+    wave = wl.line_wavelengths(112, 0.05)
+    jobs = [(wd, ref.pyrh_path, logtau, T0 + pert["dT"][i]) for i in range(n)]
+    hse = ref.map(rr._hse_job, jobs)
+    cases = []
+    for i in range(n):
+        ne, nH = hse[i]
+        atm = wl.atmosphere_rows(logtau, T0 + pert["dT"][i], ne / 1e6, nH / 1e6,
+                                 vlos=pert["vlos"][i], B=pert["B"][i],
+                                 gamma=pert["gamma"][i], chi=pert["chi"][i])
+        cases.append(lte_case(ref, f"_tmp_batch{i}", atm, wave))
+    keys = [k for k in cases[0] if k not in ("opac_idx", "tot_chi", "tot_eta",
+                                              "tot_chip", "tot_flags")]
+    out = {k: np.stack([c[k] for c in cases]) for k in keys}
+    path = os.path.join(HERE, "lte_batch.npz")
+    np.savez_compressed(path, **out)
+    for i in range(n):
+        os.remove(os.path.join(HERE, f"_tmp_batch{i}.npz"))
+    print(f"lte_batch: {n} atmospheres, {os.path.getsize(path) / 1e3:.0f} kB")
+
+
+MAKERS = {"lte_c0": make_lte_c0, "lte_edge": make_lte_edge,
+          "lte_b0": make_lte_b0, "lte_batch": make_lte_batch}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", nargs="*", default=None)
+    args = ap.parse_args()
+    global PORTABLE
+    ref = rr.Reference()
+    PORTABLE = rr.Reference(lib_path=rr.REF_LIB_PORTABLE)
+    wd = rr.scratch_dir()
+    rr.write_inputs(wd, None)
+    for name, fn in MAKERS.items():
+        if args.only and name not in args.only:
+            continue
+        fn(ref, wd)
+    shutil.rmtree(wd, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    main()
