@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""Benchmark of the batched polarized LTE synthesis on GB300.
+
+Workload (the batched precision form): 16384 atmospheres with 71 depth
+points, perturbed from the base model (T nodes +-300 K, v_los, B, angles),
+two Zeeman-split Fe I-like lines with 112 wavelengths each (224 per
+atmosphere), mu = 1, FP32 DELO-Bezier3 Stokes.  One step = one launch of
+pyrh_lte_stokes over the whole batch.  Inputs (continuum 2.1 GB) are larger
+than L2, so no flush is needed between steps.
+
+Prints one JSON line (rank 0).  --impl reference times the CPU path instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = ("pixel·λ·μ formal solutions/s and RF gradients/s vs plain FP64 "
+          "GPU, at 1e-4 rel err")
+UNIT = "pixel*lambda*mu/s"
+WORKLOAD = "batched LTE Stokes synthesis: 16384 atm x 71 depths x 2x112 lambda, mu=1, FP32"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--natm", type=int, default=16384)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--skip-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def config_dict(natm):
+    return {"workload": WORKLOAD, "atmospheres": natm, "depths": 71, "lambda_per_atm": 224,
+            "lines": 2, "zeeman_components": [13, 3], "mu": 1, "solver": "DELO-Bezier3",
+            "magneto_optical": False, "l2": "inputs 2.1 GB > L2, no flush"}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline_port(batch, nthreads, seconds):
+    """Times the CPU oracle (FP64 C port of the reference path, OpenMP over
+    atmospheres) on a bounded sample of the same workload."""
+    from oracle import oracle as O
+    natm = batch["T"].shape[0]
+
+    def sub(n):
+        d = {k: batch[k][:n] for k in ("height", "T", "ne", "nHtot", "np", "vturb", "vel",
+                                        "B", "gamma_B", "chi_B")}
+        d["line_pops"] = batch["line_pops"][:n]
+        d["chi_c"] = np.ascontiguousarray(batch["chi_c"][:n].transpose(0, 2, 1), np.float64)
+        d["eta_c"] = np.ascontiguousarray(batch["eta_c"][:n].transpose(0, 2, 1), np.float64)
+        for k in ("lam", "line_const", "zeeman", "zeeman_n", "vmicro_char", "mu"):
+            d[k] = batch[k]
+        d["magneto_optical"] = 0
+        d["moving"] = 1
+        return d
+
+    n = min(natm, max(nthreads, 8))
+    t0 = time.perf_counter()
+    O.lte_synth_batch(sub(n), nthreads)
+    t = time.perf_counter() - t0
+    n2 = int(min(natm, max(n, n * seconds / max(t, 1e-3))))
+    d = sub(n2)
+    t0 = time.perf_counter()
+    O.lte_synth_batch(d, nthreads)
+    t = time.perf_counter() - t0
+    units = n2 * len(batch["lam"])
+    return {"value": units / t, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{n2} of the {natm} atmospheres x {len(batch['lam'])} lambda, "
+                      f"FP64 oracle (oracle/rt_oracle.c), {t:.1f} s"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from pyrh_gb300 import workload
+    nthreads = os.cpu_count() or 1
+    batch = workload.synthetic_batch(min(args.natm, 4096), seed=1000, dtype=np.float64)
+    vals = []
+    info = None
+    for _ in range(args.warmup):
+        cpu_baseline_port(batch, nthreads, min(args.cpu_seconds, 3.0))
+    for _ in range(args.steps):
+        info = cpu_baseline_port(batch, nthreads, args.cpu_seconds / max(args.steps, 1))
+        vals.append(info["value"])
+    v = statistics.median(vals)
+    info["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(args.natm),
+            "cpu_baseline": info,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference C sources are not available on this machine; the CPU arm runs "
+                    "the oracle port of the same path with all host threads"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from pyrh_gb300 import _lib as L
+    from pyrh_gb300 import lte, workload
+
+    natm = args.natm
+    batch = workload.synthetic_batch(natm, seed=1000 + rank, dtype=np.float32)
+    lines, nline = lte.make_lines(batch["line_const"], batch["zeeman"], batch["zeeman_n"])
+    pk = lte.pack_uniform(batch, nline, L.PYRH_FP32)
+    db = lte.DeviceBatch(pk, lines, nline, device=f"cuda:{local}")
+    cfg = lte.make_config(precision=L.PYRH_FP32, mu=1.0, vmicro_char=batch["vmicro_char"])
+    units = natm * pk.max_nlam
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+
+    for _ in range(max(args.warmup, 3)):
+        db.run(cfg, sp)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing ----
+    clocks = ClockSampler(local)
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches = 0
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(args.steps):
+            db.run(cfg, sp)
+            launches += L.lib().pyrh_last_launch_count()
+        e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = units * world / (ms / 1e3)
+
+    # algorithmic bytes of one launch: every input array once + the output
+    alg_bytes = sum(a.nbytes for a in pk.arrays.values()) + db.out.numel() * db.out.element_size()
+    achieved = alg_bytes / (ms / 1e3) / 1e9
+    peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        peak_src = "measured"
+
+    # ---- end to end through the host-buffer C ABI (pinned host memory) ----
+    pinned = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory()
+              for k, v in pk.arrays.items()}
+    out_h = torch.empty(db.out.numel(), dtype=db.out.dtype).pin_memory()
+    import ctypes as C
+    hb = lte._batch_struct(pk, lambda k: pinned[k].data_ptr())
+    h2d = sum(t.numel() * t.element_size() for t in pinned.values()) + C.sizeof(L.PyrhLine) * nline
+    d2h = out_h.numel() * out_h.element_size()
+
+    def host_call():
+        L.check(L.lib().pyrh_lte_stokes_host(C.byref(hb), lines, nline, C.byref(cfg),
+                                             out_h.data_ptr()))
+
+    for _ in range(max(args.warmup, 3)):
+        host_call()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_call()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": units * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
+           "path": "pyrh_lte_stokes_host (host arrays in, Stokes out)"}
+
+    extra = {}
+    if rank == 0 and not args.skip_fp64:
+        # plain FP64 one-pixel-per-call GPU form (the comparator of the target)
+        b64 = workload.synthetic_batch(64, seed=77, dtype=np.float64)
+        cfg64 = lte.make_config(precision=L.PYRH_FP64, mu=1.0, vmicro_char=b64["vmicro_char"])
+        singles = []
+        for i in range(64):
+            one = {k: (v[i:i + 1] if isinstance(v, np.ndarray) and v.ndim and v.shape[0] == 64
+                       else v) for k, v in b64.items()}
+            p1 = lte.pack_uniform(one, nline, L.PYRH_FP64)
+            singles.append(lte.DeviceBatch(p1, lines, nline, device=f"cuda:{local}"))
+        for s in singles[:4]:
+            s.run(cfg64, sp)
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for s in singles:
+            s.run(cfg64, sp)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        per_call_ms = f0.elapsed_time(f1) / len(singles)
+        fp64_single = pk.max_nlam / (per_call_ms / 1e3)
+        # FP64 batched (same kernel, whole batch, one launch)
+        pk64 = lte.pack_uniform(workload.synthetic_batch(2048, seed=78, dtype=np.float64),
+                                nline, L.PYRH_FP64)
+        db64 = lte.DeviceBatch(pk64, lines, nline, device=f"cuda:{local}")
+        db64.run(cfg64, sp)
+        torch.cuda.synchronize()
+        g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        g0.record(stream)
+        db64.run(cfg64, sp)
+        g1.record(stream)
+        torch.cuda.synchronize()
+        fp64_batched = 2048 * pk64.max_nlam / (g0.elapsed_time(g1) / 1e3)
+        extra = {"fp64_single_pixel_per_call": {"value": fp64_single, "unit": UNIT,
+                                                "ms_per_call": per_call_ms, "sample": "64 calls"},
+                 "fp64_batched": {"value": fp64_batched, "unit": UNIT, "atmospheres": 2048},
+                 "speedup_vs_fp64_single_pixel": value / world / fp64_single}
+        del singles, db64
+
+    cpu = None
+    if rank == 0:
+        batch64 = {k: v for k, v in batch.items()}
+        cpu = cpu_baseline_port(batch64, os.cpu_count() or 1, args.cpu_seconds)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic", "config": config_dict(natm),
+                "clocks": clk, "e2e": e2e, "gpu_launches": launches,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": None,
+                             "peak_source": peak_src, "alg_bytes_per_launch": alg_bytes,
+                             "kernel": "lte_stokes_kernel<float,false>"},
+                "cpu_baseline": cpu}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,159 @@
+/* pyrh_gb300.h -- C ABI of the GB300 radiative-transfer hot path.
+ *
+ * Drop-in boundary for the polarized LTE synthesis that the reference runs
+ * per atmosphere through rhf1d() (rh/rhf1d/pyrh_compute1dray.h:26-36, bound
+ * to Python by pyrh.compute1d, pyrh.pyx:537-668).  The set-up that rhf1d()
+ * does on the host before its hot loop -- reading *.input files, LTE stage
+ * densities, background continuum, tau500 -> height -- is the caller's; this
+ * library takes its results as arrays and runs, on one GB300:
+ *   - the Kurucz-line Zeeman/Voigt opacity of rlk_opacity()/RLKProfile()
+ *     (rh/kurucz.c:511-827, Humlicek 1982 Voigt, rh/humlicek.c:28-118),
+ *   - the formal solution of Formal() (rh/rhf1d/formal.c:44-346): DELO-Bezier3
+ *     Stokes (rh/rhf1d/bezier_1D.c:52-300) where a polarizable line covers the
+ *     wavelength, the scalar Bezier3 solver (bezier_1D.c:306-541) for NO_STOKES,
+ *     and the Feautrier solver (rh/rhf1d/feautrier.c:56-202) where no line
+ *     covers it,
+ * for many atmospheres (pixels) at once.  Only the ray towards the observer
+ * is solved: the emergent Stokes vector does not depend on the other
+ * direction that Formal() also integrates in LTE.
+ *
+ * Conventions
+ *   - All pointers in pyrh_lte_batch and pyrh_line are DEVICE pointers
+ *     (caller-owned, cudaMalloc'd) unless a function says otherwise.
+ *   - Units are SI, as the reference holds them after pyrh_compute1dray.c:
+ *     263-270: height [m], T [K], ne/nHtot/np [m^-3], v [m/s], B [T],
+ *     angles [rad], wavelengths [nm, vacuum].
+ *   - Inputs are never modified (the reference mutates its inputs in place
+ *     during a call, pyrh_compute1dray.c:263-270,351-357; this library does not).
+ *   - Every entry point returns a pyrh_status; none calls exit().
+ */
+#ifndef PYRH_GB300_H
+#define PYRH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PYRH_OK = 0,
+  PYRH_ERR_ARG = 1,          /* bad shape, count, pointer or option */
+  PYRH_ERR_UNSUPPORTED = 2,  /* input outside what the kernels implement */
+  PYRH_ERR_CUDA = 3,         /* a CUDA runtime call failed */
+  PYRH_ERR_NONCONVERGED = 4, /* iteration limit reached before convergence */
+  PYRH_ERR_SINGULAR = 5,     /* singular rate matrix */
+  PYRH_ERR_TIMEOUT = 6       /* device-side iteration budget exhausted */
+} pyrh_status;
+
+typedef enum { PYRH_FP64 = 0, PYRH_FP32 = 1 } pyrh_precision;
+
+/* STOKES_MODE of keyword.input (rh/inputs.h): FULL_STOKES solves I,Q,U,V with
+   DELO-Bezier3; NO_STOKES solves I with the scalar Bezier3 solver (Zeeman
+   broadened profile, formal.c:94-95,225-235). */
+typedef enum { PYRH_NO_STOKES = 0, PYRH_FULL_STOKES = 3 } pyrh_stokes_mode;
+
+/* enum vdWaals of the reference (rh/atom.h:31). */
+typedef enum {
+  PYRH_VDW_UNSOLD = 0, PYRH_VDW_RIDDER = 1, PYRH_VDW_BARKLEM = 2, PYRH_VDW_KURUCZ = 3
+} pyrh_vdw;
+
+#define PYRH_MAX_LINES      16
+#define PYRH_MAX_COMPONENTS 32   /* Zeeman components per line */
+#define PYRH_MAX_DEPTH      512
+
+/* One Kurucz (RLK) line after readKuruczLines()/RLKZeeman() have derived its
+   constants; the fields of RLK_Line (rh/atom.h:156-167) that the opacity uses. */
+typedef struct {
+  double lambda0;          /* vacuum line centre [nm] */
+  double Ei;               /* lower level energy [J] */
+  double gi;               /* lower level statistical weight */
+  double Aji, Bji, Bij;    /* Einstein coefficients (SI, per unit frequency) */
+  double Grad, GStark, GvdWaals;   /* [s^-1], [m^3 s^-1], [m^3 s^-1] */
+  double cross, alpha;     /* Unsold / Barklem cross-section parameters */
+  double isotope_frac, hyperfine_frac;
+  double weight;           /* element atomic weight [amu] */
+  int32_t vdwaals;         /* pyrh_vdw */
+  int32_t contributes;     /* element abundance set and stage < Nstage-1
+                              (kurucz.c:614) and not covered by a model atom */
+  int32_t polarizable;     /* kurucz.c:296,384-387 */
+  int32_t ncomp;           /* Zeeman components (RLKZeeman, kurucz.c:832-920) */
+  int32_t comp_q[PYRH_MAX_COMPONENTS];        /* Ml - Mu in {-1, 0, 1} */
+  double  comp_shift[PYRH_MAX_COMPONENTS];    /* gLl*Ml - gLu*Mu */
+  double  comp_strength[PYRH_MAX_COMPONENTS]; /* normalised per q */
+} pyrh_line;
+
+/* A batch of atmospheres with possibly uneven depth and wavelength counts.
+   Atmosphere p owns depths [depth_off[p], depth_off[p] + ndep[p]) of every
+   per-depth array, wavelengths [lam_off[p], lam_off[p] + nlam[p]) of lambda,
+   continuum entries [cont_off[p], cont_off[p] + ndep[p]*nlam[p]) laid out
+   [depth][lambda] (lambda fastest), and output entries
+   [4*lam_off[p], 4*lam_off[p] + 4*nlam[p]) laid out [stokes][lambda]. */
+typedef struct {
+  int32_t natm;
+  int32_t max_ndep;            /* host value: max over ndep[] */
+  int32_t max_nlam;            /* host value: max over nlam[] */
+  int64_t total_depth;         /* host value: length of the per-depth arrays */
+  const int32_t *ndep;         /* [natm] (3 <= ndep <= PYRH_MAX_DEPTH) */
+  const int64_t *depth_off;    /* [natm] */
+  const int32_t *nlam;         /* [natm] */
+  const int64_t *lam_off;      /* [natm] */
+  const int64_t *cont_off;     /* [natm] */
+  const double *lambda;        /* [sum nlam] vacuum wavelength [nm] */
+  const double *height, *T, *ne, *nHtot, *np, *vturb, *vlos, *B, *gamma_B, *chi_B;
+  const double *line_pops;     /* [nline][2][sum ndep]: n[stage] [m^-3] and
+                                  ln U(T) of the line's ionisation stage,
+                                  as used in kurucz.c:662-677 */
+  const void *chi_c;           /* continuum opacity [m^-1] (float or double,
+                                  following the precision) */
+  const void *eta_c;           /* continuum emissivity [W m^-3 Hz^-1 sr^-1] */
+} pyrh_lte_batch;
+
+typedef struct {
+  int32_t precision;           /* pyrh_precision: FP32 also selects float
+                                  chi_c/eta_c/output */
+  int32_t stokes_mode;         /* pyrh_stokes_mode */
+  int32_t magneto_optical;     /* MAGNETO_OPTICAL */
+  int32_t moving;              /* atmos.moving (pyrh_compute1dray.c:272-278) */
+  double  mu;                  /* cosine of the ray to the observer */
+  double  vmicro_char;         /* VMICRO_CHAR [m/s]: line window 20 v/c */
+  int32_t block_lambda;        /* wavelengths per block; 0 = tuned default */
+  int32_t persistent_blocks;   /* blocks of the persistent grid; 0 = auto */
+} pyrh_lte_config;
+
+/* Emergent Stokes vectors for a batch; replaces the per-atmosphere hot loop
+   of rhf1d() -> Iterate() -> solveSpectrum() -> Formal() with the background
+   line opacity of Background() -> rlk_opacity() (background.c:519-546).
+   stokes_out: [4 * sum nlam], float or double following the precision.
+   lines: device array of nline pyrh_line.  stream: a cudaStream_t or NULL. */
+pyrh_status pyrh_lte_stokes(const pyrh_lte_batch *batch, const pyrh_line *lines,
+                            int32_t nline, const pyrh_lte_config *cfg,
+                            void *stokes_out, void *stream);
+
+/* Validates a HOST copy of a line table (component counts and q values,
+   sort order, polarizable lines only where a Voigt profile is needed).
+   pyrh_lte_stokes does not read its device table back to check it. */
+pyrh_status pyrh_check_lines(const pyrh_line *host_lines, int32_t nline,
+                             int32_t stokes_mode);
+
+/* Same computation with HOST inputs and outputs: copies the batch to the
+   device, runs pyrh_lte_stokes on an internal stream and copies the Stokes
+   vectors back, all inside the call (the shape of a compute1d()-style call,
+   pyrh.pyx:621-642).  Device buffers are cached between calls with the same
+   or smaller sizes.  Not re-entrant (one internal workspace). */
+pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch *host_batch,
+                                 const pyrh_line *host_lines, int32_t nline,
+                                 const pyrh_lte_config *cfg, void *host_stokes_out);
+
+/* Number of kernel launches the last pyrh_lte_stokes call issued. */
+int32_t pyrh_last_launch_count(void);
+
+/* Library version string and the text of the last error on this thread. */
+const char *pyrh_version(void);
+const char *pyrh_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYRH_GB300_H */

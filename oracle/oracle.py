@@ -16,6 +16,8 @@ LIB = os.path.join(HERE, "librt_oracle.so")
 SOURCES = [os.path.join(HERE, "rt_oracle.c")]
 
 RLK_NCONST = 24
+_STACKED = ("mu", "line_const", "zeeman", "zeeman_n", "vmicro_char", "magneto_optical",
+            "moving", "lam")
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
 
@@ -28,7 +30,8 @@ class OracleAtmos(C.Structure):
 
 class OracleLines(C.Structure):
     _fields_ = [("nline", C.c_int), ("maxcomp", C.c_int), ("magneto_optical", C.c_int),
-                ("moving", C.c_int), ("vmicro_char", C.c_double), ("c", _D),
+                ("moving", C.c_int), ("no_stokes", C.c_int), ("vmicro_char", C.c_double),
+                ("c", _D),
                 ("zeeman", _D), ("ncomp", _I)]
 
 
@@ -77,7 +80,7 @@ class _Keep:
 
 
 def make_lines(line_const, zeeman, zeeman_n, vmicro_char, magneto_optical, moving,
-               keep: _Keep) -> OracleLines:
+               keep: _Keep, no_stokes: bool = False) -> OracleLines:
     lc = keep.f64(line_const)
     zm = keep.f64(zeeman)
     zn = np.ascontiguousarray(zeeman_n, dtype=np.int32)
@@ -87,6 +90,7 @@ def make_lines(line_const, zeeman, zeeman_n, vmicro_char, magneto_optical, movin
     L.maxcomp = zm.shape[-1]
     L.magneto_optical = int(magneto_optical)
     L.moving = int(moving)
+    L.no_stokes = int(no_stokes)
     L.vmicro_char = float(vmicro_char)
     L.c = _p(lc)
     L.zeeman = _p(zm)
@@ -104,13 +108,15 @@ def make_atmos(fx: dict, keep: _Keep, mu=None) -> OracleAtmos:
     return A
 
 
-def lte_synth(fx: dict, md_float: bool = True, lam=None, chi_c=None, eta_c=None):
+def lte_synth(fx: dict, md_float: bool = True, lam=None, chi_c=None, eta_c=None,
+              magneto_optical=None, no_stokes: bool = False, mu=None):
     """Emergent [4][nlam] Stokes of one atmosphere given as a fixture dict with
     the keys written by tests/golden/make_golden.py."""
     keep = _Keep()
-    A = make_atmos(fx, keep)
+    A = make_atmos(fx, keep, mu=mu)
+    mo = fx["magneto_optical"] if magneto_optical is None else magneto_optical
     L = make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"], fx["vmicro_char"],
-                   fx["magneto_optical"], fx["moving"], keep)
+                   mo, fx["moving"], keep, no_stokes=no_stokes)
     lam = keep.f64(fx["lam"] if lam is None else lam)
     cc = keep.f64(fx["chi_c"] if chi_c is None else chi_c)
     ec = keep.f64(fx["eta_c"] if eta_c is None else eta_c)
@@ -125,15 +131,21 @@ def lte_synth_batch(batch: dict, nthreads: int, md_float: bool = True):
     leading atmosphere axis (lam shared)."""
     keep = _Keep()
     natm = batch["T"].shape[0]
+
+    def first(k):     # shared quantities may be stacked per atmosphere
+        v = np.asarray(batch[k])
+        return v[0] if v.ndim and v.shape[0] == natm and k in _STACKED else v
+
     atms = (OracleAtmos * natm)()
     for p in range(natm):
         fx = {k: batch[k][p] for k in ("height", "T", "ne", "nHtot", "np", "vturb",
                                         "vel", "B", "gamma_B", "chi_B", "line_pops")}
-        fx["mu"] = batch["mu"]
+        fx["mu"] = float(first("mu"))
         atms[p] = make_atmos(fx, keep)
-    L = make_lines(batch["line_const"], batch["zeeman"], batch["zeeman_n"],
-                   batch["vmicro_char"], batch["magneto_optical"], batch["moving"], keep)
-    lam = keep.f64(batch["lam"])
+    L = make_lines(first("line_const"), first("zeeman"), first("zeeman_n"),
+                   float(first("vmicro_char")), int(first("magneto_optical")),
+                   int(first("moving")), keep)
+    lam = keep.f64(first("lam"))
     cc = keep.f64(batch["chi_c"])
     ec = keep.f64(batch["eta_c"])
     out = np.zeros((natm, 4, len(lam)))

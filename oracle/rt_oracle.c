@@ -661,7 +661,7 @@ int oracle_lte_synth(const OracleAtmos *A, const OracleLines *LN, int nlam,
     }
     double B0 = oracle_planck(A->T[nd - 2], lambda);
     double B1 = oracle_planck(A->T[nd - 1], lambda);
-    if (flags & 2) {
+    if ((flags & 2) && !LN->no_stokes) {
       double I0[4];
       stokes_bezier3(nd, A->height, imu, chi, S, K, B0, B1, md_float, I0);
       for (int s = 0; s < 4; s++) out[(long) s * nlam + la] = I0[s];

@@ -38,6 +38,7 @@ typedef struct {
 
 typedef struct {
   int nline, maxcomp, magneto_optical, moving;
+  int no_stokes;               /* STOKES_MODE = NO_STOKES: scalar solver */
   double vmicro_char;          /* [m/s] */
   const double *c;             /* [nline][RLK_NCONST] */
   const double *zeeman;        /* [nline][3][maxcomp]: q, shift, strength */

@@ -1,0 +1,49 @@
+"""Builds libpyrh_gb300.so in-tree with nvcc for sm_103a (no torch extension
+machinery: the library exposes a plain C ABI, include/pyrh_gb300.h)."""
+from __future__ import annotations
+
+import os
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libpyrh_gb300.so")
+UNITS = ["capi.cu", "lte_stokes.cu"]
+GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC = os.environ.get("NVCC", "nvcc")
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+
+def _sources_mtime() -> float:
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files.append(os.path.join(os.path.dirname(HERE), "include", "pyrh_gb300.h"))
+    return max(os.path.getmtime(f) for f in files)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+
+    def compile_unit(u):
+        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
+        cmd = [NVCC, *GENCODE, *FLAGS, "-c", os.path.join(CSRC, u), "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {u}:\n{r.stderr}")
+        if verbose and r.stderr:
+            print(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(len(UNITS)) as ex:
+        objs = list(ex.map(compile_unit, UNITS))
+    tmp = LIB + ".tmp"
+    subprocess.run([NVCC, *GENCODE, "-shared", "-o", tmp, *objs, "-lcudart"], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force=True, verbose=True))

@@ -1,0 +1,281 @@
+// capi.cu -- extern "C" entry points of libpyrh_gb300.so (include/pyrh_gb300.h).
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "../../include/pyrh_gb300.h"
+#include "lte_stokes.cuh"
+
+namespace {
+
+thread_local char g_err[512] = "";
+int g_last_launches = 0;
+
+pyrh_status fail(pyrh_status s, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return s;
+}
+
+#define CUDA_TRY(x)                                                                   \
+  do {                                                                                \
+    cudaError_t e_ = (x);                                                             \
+    if (e_ != cudaSuccess)                                                            \
+      return fail(PYRH_ERR_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_));        \
+  } while (0)
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+pyrh_status check_lines_host(const pyrh_line* lines, int nline, int stokes_mode) {
+  for (int l = 0; l < nline; ++l) {
+    const pyrh_line& L = lines[l];
+    if (L.ncomp < 0 || L.ncomp > PYRH_MAX_COMPONENTS)
+      return fail(PYRH_ERR_ARG, "line %d: ncomp %d outside [0, %d]", l, L.ncomp,
+                  PYRH_MAX_COMPONENTS);
+    if (!(L.lambda0 > 0.0) || !(L.weight > 0.0) || !(L.Bji > 0.0))
+      return fail(PYRH_ERR_ARG, "line %d: non-positive lambda0, weight or Bji", l);
+    if (L.contributes && !L.polarizable && L.Grad != 0.0)
+      return fail(PYRH_ERR_UNSUPPORTED,
+                  "line %d is not polarizable: the reference evaluates it with "
+                  "Armstrong's Voigt function (kurucz.c:824), not implemented", l);
+    for (int c = 0; c < L.ncomp; ++c)
+      if (L.comp_q[c] < -1 || L.comp_q[c] > 1)
+        return fail(PYRH_ERR_ARG, "line %d component %d: q = %d", l, c, L.comp_q[c]);
+    if (l > 0 && lines[l].lambda0 < lines[l - 1].lambda0)
+      return fail(PYRH_ERR_ARG, "lines must be sorted by lambda0 (background.c:293)");
+  }
+  (void)stokes_mode;
+  return PYRH_OK;
+}
+
+pyrh_status check_cfg(const pyrh_lte_config* cfg) {
+  if (!cfg) return fail(PYRH_ERR_ARG, "cfg is NULL");
+  if (cfg->precision != PYRH_FP64 && cfg->precision != PYRH_FP32)
+    return fail(PYRH_ERR_ARG, "precision %d", cfg->precision);
+  if (cfg->stokes_mode != PYRH_FULL_STOKES && cfg->stokes_mode != PYRH_NO_STOKES)
+    return fail(PYRH_ERR_ARG, "stokes_mode %d", cfg->stokes_mode);
+  if (!(cfg->mu > 0.0 && cfg->mu <= 1.0)) return fail(PYRH_ERR_ARG, "mu %g outside (0, 1]", cfg->mu);
+  if (!(cfg->vmicro_char >= 0.0)) return fail(PYRH_ERR_ARG, "vmicro_char %g", cfg->vmicro_char);
+  if (cfg->block_lambda < 0 || cfg->block_lambda > 256 || (cfg->block_lambda % 32))
+    return fail(PYRH_ERR_ARG, "block_lambda %d must be 0 or a multiple of 32 <= 256",
+                cfg->block_lambda);
+  return PYRH_OK;
+}
+
+pyrh_status check_batch_shape(const pyrh_lte_batch* b, int nline) {
+  if (!b) return fail(PYRH_ERR_ARG, "batch is NULL");
+  if (b->natm < 1) return fail(PYRH_ERR_ARG, "natm %d", b->natm);
+  if (b->max_ndep < 3 || b->max_ndep > PYRH_MAX_DEPTH)
+    return fail(PYRH_ERR_ARG, "max_ndep %d outside [3, %d]", b->max_ndep, PYRH_MAX_DEPTH);
+  if (b->max_nlam < 1) return fail(PYRH_ERR_ARG, "max_nlam %d", b->max_nlam);
+  if (b->total_depth < b->max_ndep) return fail(PYRH_ERR_ARG, "total_depth %lld", (long long)b->total_depth);
+  if (nline < 0 || nline > PYRH_MAX_LINES)
+    return fail(PYRH_ERR_ARG, "nline %d outside [0, %d]", nline, PYRH_MAX_LINES);
+  const void* ptrs[] = {b->ndep, b->depth_off, b->nlam, b->lam_off, b->cont_off, b->lambda,
+                        b->height, b->T, b->ne, b->nHtot, b->np, b->vturb, b->vlos, b->B,
+                        b->gamma_B, b->chi_B, b->chi_c, b->eta_c};
+  for (const void* p : ptrs)
+    if (!p) return fail(PYRH_ERR_ARG, "a batch array pointer is NULL");
+  if (nline > 0 && !b->line_pops) return fail(PYRH_ERR_ARG, "line_pops is NULL");
+  return PYRH_OK;
+}
+
+pyrh::LteArgs make_args(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nline,
+                        const pyrh_lte_config* cfg, void* out, int block) {
+  pyrh::LteArgs a;
+  a.natm = b->natm;
+  a.tiles = (b->max_nlam + block - 1) / block;
+  a.maxd = b->max_ndep;
+  a.nline = nline;
+  a.precision = cfg->precision;
+  a.stokes_mode = cfg->stokes_mode;
+  a.magneto_optical = cfg->magneto_optical ? 1 : 0;
+  a.moving = cfg->moving ? 1 : 0;
+  a.mu = cfg->mu;
+  a.vmicro_char = cfg->vmicro_char;
+  a.total_depth = b->total_depth;
+  a.ndep = b->ndep; a.nlam = b->nlam;
+  a.depth_off = b->depth_off; a.lam_off = b->lam_off; a.cont_off = b->cont_off;
+  a.lambda = b->lambda; a.height = b->height; a.T = b->T; a.ne = b->ne;
+  a.nHtot = b->nHtot; a.np = b->np; a.vturb = b->vturb; a.vlos = b->vlos; a.B = b->B;
+  a.gamma_B = b->gamma_B; a.chi_B = b->chi_B; a.line_pops = b->line_pops;
+  a.chi_c = b->chi_c; a.eta_c = b->eta_c;
+  a.lines = d_lines;
+  a.out = out;
+  return a;
+}
+
+int default_block(int max_nlam, int requested) {
+  if (requested > 0) return requested;
+  int b = round_up(max_nlam, 32);
+  if (b > 256) {
+    // split into equal tiles of at most 256 wavelengths
+    int tiles = (max_nlam + 255) / 256;
+    b = round_up((max_nlam + tiles - 1) / tiles, 32);
+  }
+  return b < 32 ? 32 : b;
+}
+
+pyrh_status launch(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nline,
+                   const pyrh_lte_config* cfg, void* out, cudaStream_t st) {
+  const int block = default_block(b->max_nlam, cfg->block_lambda);
+  pyrh::LteArgs a = make_args(b, d_lines, nline, cfg, out, block);
+  const size_t smem = pyrh::lte_smem_bytes(cfg->precision, nline, a.maxd);
+  if (smem > 200 * 1024)
+    return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
+                nline, a.maxd);
+  const long long work = (long long)a.natm * a.tiles;
+  int grid = cfg->persistent_blocks;
+  if (grid <= 0) {
+    // persistent grid: every SM filled to its resident-block limit
+    int per_sm = pyrh::lte_blocks_per_sm(cfg->precision, a.magneto_optical, block, smem);
+    if (per_sm < 1) per_sm = 1;
+    grid = sm_count() * per_sm;
+  }
+  if (grid > work) grid = (int)work;
+  cudaError_t e = pyrh::launch_lte_stokes(a, block, grid, st);
+  if (e != cudaSuccess) return fail(PYRH_ERR_CUDA, "lte_stokes launch: %s", cudaGetErrorString(e));
+  g_last_launches = 1;
+  return PYRH_OK;
+}
+
+// Workspace of the host-buffer entry point.
+struct HostWs {
+  std::mutex mu;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> bufs;
+  std::vector<size_t> caps;
+  void* get(int slot, size_t bytes, cudaError_t* err) {
+    if ((int)bufs.size() <= slot) { bufs.resize(slot + 1, nullptr); caps.resize(slot + 1, 0); }
+    if (caps[slot] < bytes) {
+      if (bufs[slot]) cudaFree(bufs[slot]);
+      bufs[slot] = nullptr;
+      caps[slot] = 0;
+      *err = cudaMalloc(&bufs[slot], bytes);
+      if (*err != cudaSuccess) return nullptr;
+      caps[slot] = bytes;
+    }
+    return bufs[slot];
+  }
+};
+HostWs g_ws;
+
+}  // namespace
+
+extern "C" {
+
+const char* pyrh_version(void) { return "pyrh_gb300 0.1 (sm_103a)"; }
+const char* pyrh_last_error(void) { return g_err; }
+int32_t pyrh_last_launch_count(void) { return g_last_launches; }
+
+pyrh_status pyrh_lte_stokes(const pyrh_lte_batch* batch, const pyrh_line* lines, int32_t nline,
+                            const pyrh_lte_config* cfg, void* stokes_out, void* stream) {
+  g_last_launches = 0;
+  pyrh_status s = check_cfg(cfg);
+  if (s != PYRH_OK) return s;
+  s = check_batch_shape(batch, nline);
+  if (s != PYRH_OK) return s;
+  if (!stokes_out) return fail(PYRH_ERR_ARG, "stokes_out is NULL");
+  if (nline > 0 && !lines) return fail(PYRH_ERR_ARG, "lines is NULL");
+  // The line table lives in device memory and is not read back here (that
+  // would synchronise the stream); pyrh_check_lines validates a host copy,
+  // and the kernel clamps component counts to PYRH_MAX_COMPONENTS.
+  return launch(batch, lines, nline, cfg, stokes_out, (cudaStream_t)stream);
+}
+
+pyrh_status pyrh_check_lines(const pyrh_line* host_lines, int32_t nline, int32_t stokes_mode) {
+  if (nline < 0 || nline > PYRH_MAX_LINES)
+    return fail(PYRH_ERR_ARG, "nline %d outside [0, %d]", nline, PYRH_MAX_LINES);
+  if (nline > 0 && !host_lines) return fail(PYRH_ERR_ARG, "host_lines is NULL");
+  return check_lines_host(host_lines, nline, stokes_mode);
+}
+
+pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host_lines,
+                                 int32_t nline, const pyrh_lte_config* cfg,
+                                 void* host_stokes_out) {
+  g_last_launches = 0;
+  pyrh_status s = check_cfg(cfg);
+  if (s != PYRH_OK) return s;
+  s = check_batch_shape(hb, nline);
+  if (s != PYRH_OK) return s;
+  if (!host_stokes_out) return fail(PYRH_ERR_ARG, "host_stokes_out is NULL");
+  if (nline > 0) {
+    if (!host_lines) return fail(PYRH_ERR_ARG, "host_lines is NULL");
+    s = check_lines_host(host_lines, nline, cfg->stokes_mode);
+    if (s != PYRH_OK) return s;
+  }
+  std::lock_guard<std::mutex> lock(g_ws.mu);
+  if (!g_ws.stream) CUDA_TRY(cudaStreamCreateWithFlags(&g_ws.stream, cudaStreamNonBlocking));
+  const int natm = hb->natm;
+  long long nlam_tot = 0, cont_tot = 0;
+  for (int p = 0; p < natm; ++p) {
+    const long long e = hb->lam_off[p] + hb->nlam[p];
+    if (e > nlam_tot) nlam_tot = e;
+    const long long c = hb->cont_off[p] + (long long)hb->ndep[p] * hb->nlam[p];
+    if (c > cont_tot) cont_tot = c;
+    if (hb->ndep[p] < 3 || hb->ndep[p] > hb->max_ndep || hb->nlam[p] < 1 ||
+        hb->nlam[p] > hb->max_nlam || hb->depth_off[p] + hb->ndep[p] > hb->total_depth)
+      return fail(PYRH_ERR_ARG, "atmosphere %d: inconsistent ndep/nlam/offsets", p);
+  }
+  const size_t real = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
+  const size_t D = sizeof(double) * hb->total_depth;
+  cudaError_t err = cudaSuccess;
+  pyrh_lte_batch db = *hb;
+  int slot = 0;
+  auto up = [&](const void* src, size_t bytes) -> void* {
+    void* d = g_ws.get(slot++, bytes, &err);
+    if (!d) return nullptr;
+    err = cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, g_ws.stream);
+    return err == cudaSuccess ? d : nullptr;
+  };
+#define UP(field, bytes)                                                       \
+  do {                                                                         \
+    db.field = (decltype(db.field))up(hb->field, bytes);                       \
+    if (!db.field) return fail(PYRH_ERR_CUDA, "upload %s: %s", #field,         \
+                               cudaGetErrorString(err));                       \
+  } while (0)
+  UP(ndep, sizeof(int32_t) * natm);
+  UP(depth_off, sizeof(int64_t) * natm);
+  UP(nlam, sizeof(int32_t) * natm);
+  UP(lam_off, sizeof(int64_t) * natm);
+  UP(cont_off, sizeof(int64_t) * natm);
+  UP(lambda, sizeof(double) * nlam_tot);
+  UP(height, D); UP(T, D); UP(ne, D); UP(nHtot, D); UP(np, D);
+  UP(vturb, D); UP(vlos, D); UP(B, D); UP(gamma_B, D); UP(chi_B, D);
+  if (nline > 0) UP(line_pops, D * 2 * nline);
+  UP(chi_c, real * cont_tot);
+  UP(eta_c, real * cont_tot);
+#undef UP
+  pyrh_line* d_lines = nullptr;
+  if (nline > 0) {
+    d_lines = (pyrh_line*)up(host_lines, sizeof(pyrh_line) * nline);
+    if (!d_lines) return fail(PYRH_ERR_CUDA, "upload lines: %s", cudaGetErrorString(err));
+  }
+  const size_t out_bytes = real * 4 * nlam_tot;
+  void* d_out = g_ws.get(slot++, out_bytes, &err);
+  if (!d_out) return fail(PYRH_ERR_CUDA, "output buffer: %s", cudaGetErrorString(err));
+  s = launch(&db, d_lines, nline, cfg, d_out, g_ws.stream);
+  if (s != PYRH_OK) return s;
+  CUDA_TRY(cudaMemcpyAsync(host_stokes_out, d_out, out_bytes, cudaMemcpyDeviceToHost, g_ws.stream));
+  CUDA_TRY(cudaStreamSynchronize(g_ws.stream));
+  return PYRH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,29 @@
+// lte_stokes.cuh -- launch interface of the fused LTE Stokes kernel.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pyrh_gb300.h"
+
+namespace pyrh {
+
+struct LteArgs {
+  int natm, tiles, maxd, nline;
+  int precision, stokes_mode, magneto_optical, moving;
+  double mu, vmicro_char;
+  int64_t total_depth;
+  const int32_t *ndep, *nlam;
+  const int64_t *depth_off, *lam_off, *cont_off;
+  const double *lambda, *height, *T, *ne, *nHtot, *np, *vturb, *vlos, *B, *gamma_B, *chi_B;
+  const double *line_pops;
+  const void *chi_c, *eta_c;
+  const pyrh_line *lines;
+  void *out;
+};
+
+size_t lte_smem_bytes(int precision, int nline, int maxd);
+int lte_blocks_per_sm(int precision, int magneto_optical, int block, size_t smem);
+cudaError_t launch_lte_stokes(const LteArgs &a, int block, int grid, cudaStream_t st);
+
+}  // namespace pyrh

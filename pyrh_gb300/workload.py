@@ -146,3 +146,71 @@ def fe_linelist(lines=FE_LINES) -> str:
                                  L["damp"], L["gL"][0], L["gL"][1],
                                  L["orbital"][0], L["orbital"][1]))
     return "\n".join(out) + "\n"
+
+
+# ------------------------------------------------------------------------
+# Batched synthetic workload built on the base atmosphere's hot-path inputs
+# (continuum, stage densities, height scale from the reference's set-up for
+# the base model, stored in pyrh_gb300/data/base_atmosphere.npz).  The
+# temperature perturbations rescale the inputs that depend on T:
+#   continuum opacity  ~ n(H-)   ~ T^-3/2 exp(0.754 eV / kT)  (Saha, H- bf)
+#   continuum emission = opacity x Planck(T)                 (LTE)
+#   Fe I stage density ~ T^-3/2 exp(7.87 eV / kT)            (Saha, minority)
+# with ne, nH, height held fixed.  The result has the shapes and value
+# distributions of the batched form; its spectra are not reference spectra.
+# ------------------------------------------------------------------------
+
+import os as _os
+
+E_HMINUS = 0.754 * EV
+E_FE_ION = 7.87 * EV
+DATA = _os.path.join(_os.path.dirname(_os.path.abspath(__file__)), "data")
+
+
+def load_base() -> dict:
+    with np.load(_os.path.join(DATA, "base_atmosphere.npz")) as f:
+        return {k: f[k] for k in f.files}
+
+
+def planck_lambda(T, lam_nm):
+    """Planck function B_nu(T) at wavelength lam [nm] (rh/planck.c:38-63)."""
+    l = lam_nm * 1e-9
+    x = HPLANCK * CLIGHT / (KBOLTZMANN * l * T)
+    return (2.0 * HPLANCK * CLIGHT / l ** 3) / np.expm1(x)
+
+
+def synthetic_batch(natm: int, seed: int = 2024, n_per_line: int = 112,
+                    half_width: float = 0.05, dtype=np.float32) -> dict:
+    """natm perturbed copies of the base atmosphere on the 2 x n_per_line
+    grid.  Arrays carry a leading atmosphere axis; continuum is
+    [natm, ndep, nlam] (lambda fastest) in `dtype`."""
+    base = load_base()
+    lam = line_wavelengths(n_per_line, half_width)
+    nd = len(base["T"])
+    T0 = base["T"]
+    # continuum of the base model interpolated to the new grid (it varies by
+    # ~1e-4 across 0.2 nm)
+    chi0 = np.stack([np.interp(lam, base["lam"][1:], base["chi_c"][1:, k]) for k in range(nd)])
+    logtau = base["atm"][0]
+    pert = perturbations(natm, seed, logtau)
+    T = T0[None, :] + pert["dT"]
+    T = np.maximum(T, 2500.0)
+    r = T0[None, :] / T
+    f_cont = r ** 1.5 * np.exp(E_HMINUS / KBOLTZMANN * (1.0 / T - 1.0 / T0[None, :]))
+    f_fe = r ** 1.5 * np.exp(E_FE_ION / KBOLTZMANN * (1.0 / T - 1.0 / T0[None, :]))
+    chi_c = (chi0[None, :, :] * f_cont[:, :, None]).astype(dtype)
+    eta_c = (chi_c * planck_lambda(T[:, :, None], lam[None, None, :])).astype(dtype)
+    ones = np.ones((natm, nd))
+    out = dict(
+        lam=lam, T=T, ne=ones * base["ne"], nHtot=ones * base["nHtot"], np=ones * base["np"],
+        height=ones * base["height"], vturb=ones * base["vturb"],
+        vel=ones * (pert["vlos"][:, None] * 1e3), B=ones * (pert["B"][:, None] * 1e-4),
+        gamma_B=ones * pert["gamma"][:, None], chi_B=ones * pert["chi"][:, None],
+        chi_c=chi_c, eta_c=eta_c,
+        line_const=base["line_const"], zeeman=base["zeeman"], zeeman_n=base["zeeman_n"],
+        vmicro_char=float(base["vmicro_char"]), mu=1.0,
+    )
+    lp = np.repeat(base["line_pops"][None], natm, axis=0)    # [natm, nline, 2, nd]
+    lp[:, :, 0, :] *= f_fe[:, None, :]
+    out["line_pops"] = lp
+    return out

@@ -96,6 +96,20 @@ def make_lte_c0(ref, wd):
     lte_case(ref, "lte_c0", atm, wave)
 
 
+def make_base_model(ref, wd):
+    """Package data for the synthetic batched workloads: the reference's
+    hot-path inputs for the base 71-depth atmosphere (continuum on the
+    2 x 201 lambda grid, height scale, stage densities, line table)."""
+    fx = np.load(os.path.join(HERE, "lte_c0.npz"))
+    keep = ["atm", "lam", "chi_c", "eta_c", "height", "T", "ne", "nHtot", "np", "vturb",
+            "vel", "B", "gamma_B", "chi_B", "line_const", "line_pops", "zeeman", "zeeman_n",
+            "vmicro_char", "lambda_ref", "moving", "mu"]
+    path = os.path.join(REPO, "pyrh_gb300", "data", "base_atmosphere.npz")
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    np.savez_compressed(path, **{k: fx[k] for k in keep})
+    print(f"base_atmosphere: {os.path.getsize(path) / 1e3:.0f} kB")
+
+
 def make_lte_edge(ref, wd):
     logtau, T, ne, nH = base_c0(ref, wd)
     atm = wl.atmosphere_rows(logtau, T, ne, nH, B=3000.0,
@@ -139,7 +153,7 @@ def make_lte_batch(ref, wd, n=6, seed=2024):
     print(f"lte_batch: {n} atmospheres, {os.path.getsize(path) / 1e3:.0f} kB")
 
 
-MAKERS = {"lte_c0": make_lte_c0, "lte_edge": make_lte_edge,
+MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch}
 
 

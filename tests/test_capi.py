@@ -1,0 +1,79 @@
+"""The C ABI library loads and exports every entry point that
+include/pyrh_gb300.h declares; argument checks run without a GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+from pyrh_gb300 import _lib as L
+from pyrh_gb300 import lte
+
+
+def _declared():
+    names = set()
+    for f in os.listdir(os.path.join(REPO, "include")):
+        if f.endswith(".h"):
+            src = open(os.path.join(REPO, "include", f)).read()
+            names |= set(re.findall(r"^\s*(?:pyrh_status|int32_t|const char \*)\s*(pyrh_\w+)\s*\(",
+                                    src, re.M))
+    return names
+
+
+def test_library_exports_all_declared_symbols():
+    lib = L.lib()
+    declared = _declared()
+    assert declared, "no declarations parsed"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(L.EXPORTED) <= declared
+    assert b"sm_103a" in lib.pyrh_version()
+
+
+def test_struct_sizes_match_header_layout():
+    # 14 doubles + 4 int32 + 32 int32 + 64 doubles
+    assert C.sizeof(L.PyrhLine) == 14 * 8 + 4 * 4 + 32 * 4 + 64 * 8
+    assert C.sizeof(L.PyrhLteConfig) == 4 * 4 + 2 * 8 + 2 * 4
+
+
+def test_config_validation_without_gpu(golden):
+    fx = golden("lte_c0")
+    lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
+    pk = lte.pack([fx], n)
+    for bad in (dict(mu=0.0), dict(mu=1.5), dict(precision=7), dict(block_lambda=48),
+                dict(stokes_mode=1)):
+        cfg = lte.make_config(**bad)
+        with pytest.raises(L.PyrhError) as e:
+            lte.synth_host(pk, lines, n, cfg)
+        assert e.value.status == L.PYRH_ERR_ARG
+
+
+def test_line_checks(golden):
+    fx = golden("lte_c0")
+    lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
+    lib = L.lib()
+    assert lib.pyrh_check_lines(lines, n, L.PYRH_FULL_STOKES) == L.PYRH_OK
+    bad, _ = lte.make_lines(fx["line_const"][::-1].copy(), fx["zeeman"][::-1].copy(),
+                            fx["zeeman_n"][::-1].copy())
+    assert lib.pyrh_check_lines(bad, n, L.PYRH_FULL_STOKES) == L.PYRH_ERR_ARG
+    lc = fx["line_const"].copy()
+    lc[0, 18] = 0   # not polarizable -> Armstrong Voigt in the reference
+    unp, _ = lte.make_lines(lc, fx["zeeman"], fx["zeeman_n"])
+    assert lib.pyrh_check_lines(unp, n, L.PYRH_FULL_STOKES) == L.PYRH_ERR_UNSUPPORTED
+    assert lib.pyrh_check_lines(lines, L.PYRH_MAX_LINES + 1, 3) == L.PYRH_ERR_ARG
+
+
+def test_pack_layout(golden):
+    fx = golden("lte_c0")
+    b = golden("lte_batch")
+    from conftest import batch_member
+    atms = [fx, batch_member(b, 0)]
+    pk = lte.pack(atms, 2)
+    a = pk.arrays
+    assert list(a["ndep"]) == [71, 71]
+    assert list(a["nlam"]) == [len(fx["lam"]), len(b["lam"][0])]
+    assert a["cont_off"][1] == 71 * len(fx["lam"])
+    # continuum is [depth][lambda] per atmosphere
+    assert a["chi_c"][5 * len(fx["lam"]) + 7] == fx["chi_c"][7, 5]

@@ -1,0 +1,174 @@
+"""GPU parity of the fused LTE Stokes kernel (libpyrh_gb300.so, called through
+its C ABI) against the compiled reference's golden vectors and the CPU oracle.
+
+Tolerances, relative to the continuum intensity I_c = max(I) of a spectrum:
+  FP64 kernel vs reference (x86 SSE build)   1e-5   (stated parity bar)
+  FP64 kernel vs reference (portable build)  2e-6
+  FP64 kernel vs FP64 oracle                 1e-8
+  FP32 kernel vs FP64 oracle                 1e-4   (stated FP32 bar)
+"""
+import numpy as np
+import pytest
+
+from conftest import batch_member
+from oracle import oracle as O
+from pyrh_gb300 import _lib as L
+from pyrh_gb300 import lte
+
+pytestmark = pytest.mark.gpu
+
+FP64, FP32 = L.PYRH_FP64, L.PYRH_FP32
+
+
+def _err(mine, ref):
+    return np.abs(mine - ref).max(axis=1) / ref[0].max()
+
+
+def run(atms, precision, mu=1.0, api="host", **cfgkw):
+    fx = atms[0]
+    lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
+    pk = lte.pack(atms, n, precision)
+    cfg = lte.make_config(precision=precision, mu=mu, vmicro_char=float(fx["vmicro_char"]),
+                          moving=bool(fx["moving"]), **cfgkw)
+    if api == "host":
+        out = lte.synth_host(pk, lines, n, cfg)
+    else:
+        import torch
+        db = lte.DeviceBatch(pk, lines, n)
+        db.run(cfg)
+        torch.cuda.synchronize()
+        out = db.out.cpu().numpy()
+    assert L.lib().pyrh_last_launch_count() == 1
+    return [o.astype(np.float64) for o in lte.split_output(pk, out)]
+
+
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0"])
+def test_fp64_vs_reference(golden, name):
+    fx = golden(name)
+    m = O.output_mask(fx["lam"], fx["lambda_ref"])
+    out = run([fx], FP64, mu=float(fx["mu"]))[0][:, m]
+    assert _err(out, fx["stokes_ref"]).max() < 1e-5
+    assert _err(out, fx["stokes_ref_portable"]).max() < 2e-6
+    assert np.all(out[1:, fx["tot_flags"][m][:, 1] == 0] == 0.0)
+
+
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0"])
+def test_fp64_vs_oracle(golden, name):
+    fx = golden(name)
+    out = run([fx], FP64, mu=float(fx["mu"]))[0]
+    ref = O.lte_synth(fx, md_float=False)
+    assert _err(out, ref).max() < 1e-8
+
+
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0"])
+def test_fp32_vs_oracle(golden, name):
+    fx = golden(name)
+    out = run([fx], FP32, mu=float(fx["mu"]))[0]
+    ref = O.lte_synth(fx, md_float=False)
+    assert _err(out, ref).max() < 1e-4
+    m = O.output_mask(fx["lam"], fx["lambda_ref"])
+    assert _err(out[:, m], fx["stokes_ref"]).max() < 1e-4
+
+
+@pytest.mark.parametrize("precision,tol", [(FP64, 1e-8), (FP32, 1e-4)])
+def test_magneto_optical_vs_oracle(golden, precision, tol):
+    """MAGNETO_OPTICAL = TRUE crashes the reference (rh/readj.c:330 writes
+    four records into the three-record chip_c_lam buffer of
+    rh/sortlambda.c:574), so the magneto-optical terms are checked against
+    the oracle only."""
+    fx = golden("lte_c0")
+    out = run([fx], precision, magneto_optical=True)[0]
+    ref = O.lte_synth(fx, md_float=False, magneto_optical=True)
+    assert _err(out, ref).max() < tol
+    # the Faraday terms change Q and U visibly at 1000 G
+    plain = O.lte_synth(fx, md_float=False)
+    assert np.abs(ref[1] - plain[1]).max() > 1e-3 * ref[0].max()
+
+
+@pytest.mark.parametrize("precision,tol", [(FP64, 1e-8), (FP32, 1e-4)])
+def test_no_stokes_mode(golden, precision, tol):
+    fx = golden("lte_c0")
+    out = run([fx], precision, stokes_mode=L.PYRH_NO_STOKES)[0]
+    ref = O.lte_synth(fx, md_float=False, no_stokes=True)
+    assert _err(out[:1], ref[:1]).max() < tol
+    assert np.all(out[1:] == 0.0)
+
+
+def test_batch_fixture_fp64_and_fp32(golden):
+    b = golden("lte_batch")
+    atms = [batch_member(b, i) for i in range(b["T"].shape[0])]
+    o64 = run(atms, FP64)
+    o32 = run(atms, FP32)
+    for fx, a, c in zip(atms, o64, o32):
+        m = O.output_mask(fx["lam"], fx["lambda_ref"])
+        assert _err(a[:, m], fx["stokes_ref"]).max() < 1e-5
+        assert _err(c, O.lte_synth(fx, md_float=False)).max() < 1e-4
+
+
+def test_ragged_batch_equals_single(golden):
+    """Uneven depth and wavelength counts in one launch give the same spectra
+    as one-atmosphere launches."""
+    c0 = golden("lte_c0")
+    b = golden("lte_batch")
+    short = dict(c0)
+    for k in ("height", "T", "ne", "nHtot", "np", "vturb", "vel", "B", "gamma_B", "chi_B"):
+        short[k] = c0[k][:50]
+    short["line_pops"] = c0["line_pops"][:, :, :50]
+    short["chi_c"] = c0["chi_c"][:, :50]
+    short["eta_c"] = c0["eta_c"][:, :50]
+    sub = batch_member(b, 3)
+    sub["lam"] = sub["lam"][::3]
+    sub["chi_c"] = sub["chi_c"][::3]
+    sub["eta_c"] = sub["eta_c"][::3]
+    atms = [c0, short, sub, batch_member(b, 1)]
+    for prec in (FP64, FP32):
+        together = run(atms, prec)
+        for fx, t in zip(atms, together):
+            alone = run([fx], prec)[0]
+            assert np.array_equal(t, alone)
+    o = run([short], FP64)[0]
+    assert _err(o, O.lte_synth(short, md_float=False)).max() < 1e-8
+
+
+def test_host_and_device_api_agree(golden):
+    fx = golden("lte_c0")
+    for prec in (FP64, FP32):
+        a = run([fx], prec, api="host")[0]
+        d = run([fx], prec, api="device")[0]
+        assert np.array_equal(a, d)
+
+
+@pytest.mark.parametrize("block", [32, 64, 128, 256])
+def test_tile_shapes_agree(golden, block):
+    b = golden("lte_batch")
+    atms = [batch_member(b, i) for i in range(3)]
+    base = run(atms, FP32)
+    other = run(atms, FP32, block_lambda=block, persistent_blocks=7)
+    for x, y in zip(base, other):
+        assert np.array_equal(x, y)
+
+
+def test_field_reversal_symmetry_large_batch(golden):
+    """Size-independent property on 512 atmospheres: reversing the field
+    (gamma -> pi - gamma) flips Stokes V and keeps I, Q, U; rotating the
+    azimuth by pi/2 flips Q and U."""
+    b = golden("lte_batch")
+    rng = np.random.default_rng(7)
+    atms, flipped, rotated = [], [], []
+    for i in range(512):
+        fx = batch_member(b, i % b["T"].shape[0])
+        fx = dict(fx)
+        fx["gamma_B"] = np.full_like(fx["gamma_B"], rng.uniform(0.1, 1.4))
+        fx["chi_B"] = np.full_like(fx["chi_B"], rng.uniform(0.0, 1.5))
+        g = dict(fx); g["gamma_B"] = np.pi - fx["gamma_B"]
+        r = dict(fx); r["chi_B"] = fx["chi_B"] + np.pi / 2
+        atms.append(fx); flipped.append(g); rotated.append(r)
+    base = run(atms, FP32)
+    fl = run(flipped, FP32)
+    ro = run(rotated, FP32)
+    for x, y, z in zip(base, fl, ro):
+        ic = x[0].max()
+        assert np.abs(x[0] - y[0]).max() / ic < 1e-5
+        assert np.abs(x[3] + y[3]).max() / ic < 1e-5
+        assert np.abs(x[1] + z[1]).max() / ic < 1e-5
+        assert np.abs(x[2] + z[2]).max() / ic < 1e-5
