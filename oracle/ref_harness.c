@@ -296,3 +296,217 @@ int harness_dump_lte(const char *cwd, double mu, int Ndep, const double *atm,
   free(tflags); free(lc); free(lpop); free(zm); free(zn);
   return Nspect;
 }
+
+/* ------------------------------------------------------------------ NLTE */
+
+void Damping(AtomicLine *line, double *adamp);
+double solveSpectrum(bool_t eval_operator, bool_t redistribute);
+void statEquil(Atom *atom, int isum);
+void initGammaAtom(Atom *atom);
+void initSolution(bool_t pyrh_io_flag);
+void initScatter(void);
+void getProfiles(void);
+void Iterate(int NmaxIter, double iterLimit);
+void _solveray(double muz, mySpectrum *spec);
+
+/* Set-up of rhf1d() with an ACTIVE atom, up to initScatter()
+   (pyrh_compute1dray.c:130-323). */
+static void nlte_setup(const char *cwd, double mu, int Ndep, double *a, int Nwave,
+                       double *w)
+{
+  char tmp[512];
+  snprintf(commandline.keyword_input, sizeof(commandline.keyword_input),
+           "%s/keyword.input", cwd);
+  setOptions(1, NULL);
+  readInput();
+  input.verbose = FALSE;
+  input.get_populations = FALSE;
+  input.pyrhHSE = FALSE;
+  input.get_atomic_rfs = FALSE;
+  input.n_atomic_pars = 0;
+  snprintf(tmp, sizeof(tmp), "%s/%s", cwd, input.atoms_input);
+  strcpy(input.atoms_input, tmp);
+  snprintf(tmp, sizeof(tmp), "%s/%s", cwd, input.molecules_input);
+  strcpy(input.molecules_input, tmp);
+  if (strcmp(input.KuruczData, "none")) {
+    snprintf(tmp, sizeof(tmp), "%s/%s", cwd, input.KuruczData);
+    strcpy(input.KuruczData, tmp);
+  }
+  input.solve_ne = FALSE;
+  spectrum.updateJ = TRUE;
+  input.limit_memory = FALSE;
+  input.solve_NLTE = FALSE;
+  atmos.Nrlk = 0;
+  geometry.Ndep = Ndep;
+  MULTIatmos(&atmos, &geometry, 0, NULL, NULL);
+  atmos.active_layer = -1;
+  geometry.scale = TAU500;
+  for (int k = 0; k < Ndep; k++) geometry.tau_ref[k] = POW10(a[k]);
+  atmos.T = a + 1 * Ndep;
+  atmos.ne = a + 2 * Ndep;
+  geometry.vel = a + 3 * Ndep;
+  atmos.vturb = a + 4 * Ndep;
+  atmos.B = a + 5 * Ndep;
+  atmos.gamma_B = a + 6 * Ndep;
+  atmos.chi_B = a + 7 * Ndep;
+  atmos.nHtot = a + 8 * Ndep;
+  atmos.nH = matrix_double(atmos.NHydr, geometry.Ndep);
+  atmos.Stokes = TRUE;
+  atmos.moving = FALSE;
+  for (int k = 0; k < Ndep; k++) {
+    geometry.vel[k] *= KM_TO_M;
+    atmos.vturb[k] *= KM_TO_M;
+    atmos.ne[k] /= CUBE(CM_TO_M);
+    atmos.nHtot[k] /= CUBE(CM_TO_M);
+    atmos.B[k] /= 1e4;
+  }
+  for (int k = 0; k < Ndep; k++)
+    if (fabs(geometry.vel[k]) >= atmos.vmacro_tresh) { atmos.moving = TRUE; break; }
+  readAtomicModels();
+  readMolecularModels();
+  for (int n = 0; n < atmos.Natom; n++)
+    if (atmos.atoms[n].active) { input.solve_NLTE = TRUE; break; }
+  if (atmos.Stokes) Bproject();
+  SortLambda(w, Nwave);
+  getBoundary(&geometry);
+  Background(FALSE, FALSE);
+  convertScales(&atmos, &geometry);
+  if (input.solve_NLTE) getProfiles();
+  initSolution(FALSE);
+  if (input.solve_NLTE) initScatter();
+}
+
+static void dump_matrix(const char *dir, const char *name, double **m, int n1, int n2)
+{
+  double *buf = (double *) malloc((long) n1 * n2 * sizeof(double));
+  for (int i = 0; i < n1; i++) memcpy(buf + (long) i * n2, m[i], n2 * sizeof(double));
+  write_f64(dir, name, buf, (long) n1 * n2);
+  free(buf);
+}
+
+/* mode 0: dump the set-up, run one iteration by hand (Gamma, J, statEquil)
+   and dump it.  mode 1: run Iterate() and _solveray() and dump the
+   converged populations and the emergent intensity. */
+int harness_nlte(const char *cwd, double mu, int Ndep, const double *atm, int Nwave,
+                 const double *lam, const char *outdir, int mode)
+{
+  double *a = (double *) malloc(9 * Ndep * sizeof(double));
+  double *w = (double *) malloc(Nwave * sizeof(double));
+  memcpy(a, atm, 9 * Ndep * sizeof(double));
+  memcpy(w, lam, Nwave * sizeof(double));
+  nlte_setup(cwd, mu, Ndep, a, Nwave, w);
+  if (atmos.Nactiveatom != 1) return -1;
+  Atom *atom = atmos.activeatoms[0];
+  int Nspect = spectrum.Nspect, Nspace = atmos.Nspace, Nl = atom->Nlevel;
+
+  if (mode == 0) {
+    int mi[16] = {Nspect, Nspace, atmos.Nrays, Nl, atom->Nline, atom->Ncont,
+                  input.NmaxIter, input.Ngdelay, input.Ngorder, input.Ngperiod,
+                  input.isum, input.NmaxScatter, atmos.moving,
+                  geometry.vboundary[TOP], geometry.vboundary[BOTTOM], 0};
+    write_i32(outdir, "meta", mi, 16);
+    double mf[4] = {input.iterLimit, atmos.lambda_ref, mu, atmos.totalAbund};
+    write_f64(outdir, "fmeta", mf, 4);
+    write_f64(outdir, "lambda", spectrum.lambda, Nspect);
+    write_f64(outdir, "muz", geometry.muz, atmos.Nrays);
+    write_f64(outdir, "wmu", geometry.wmu, atmos.Nrays);
+    write_f64(outdir, "T", atmos.T, Nspace);
+    write_f64(outdir, "ne", atmos.ne, Nspace);
+    write_f64(outdir, "nHtot", atmos.nHtot, Nspace);
+    write_f64(outdir, "vel", geometry.vel, Nspace);
+    write_f64(outdir, "vturb", atmos.vturb, Nspace);
+    write_f64(outdir, "height", geometry.height, Nspace);
+    double *bg = (double *) malloc(3L * Nspect * Nspace * sizeof(double));
+    int *hl = (int *) malloc(Nspect * sizeof(int));
+    for (int la = 0; la < Nspect; la++) {
+      memcpy(bg + (0L * Nspect + la) * Nspace, spectrum.chi_c_lam[la], Nspace * sizeof(double));
+      memcpy(bg + (1L * Nspect + la) * Nspace, spectrum.eta_c_lam[la], Nspace * sizeof(double));
+      memcpy(bg + (2L * Nspect + la) * Nspace, spectrum.sca_c_lam[la], Nspace * sizeof(double));
+      hl[la] = atmos.backgrflags[la].hasline | (atmos.backgrflags[la].ispolarized << 1);
+    }
+    write_f64(outdir, "background", bg, 3L * Nspect * Nspace);
+    write_i32(outdir, "bgflags", hl, Nspect);
+    free(bg); free(hl);
+    dump_matrix(outdir, "J0", spectrum.J, Nspect, Nspace);
+    write_f64(outdir, "g", atom->g, Nl);
+    write_f64(outdir, "E", atom->E, Nl);
+    write_i32(outdir, "stage", atom->stage, Nl);
+    dump_matrix(outdir, "nstar", atom->nstar, Nl, Nspace);
+    dump_matrix(outdir, "n0", atom->n, Nl, Nspace);
+    write_f64(outdir, "ntotal", atom->ntotal, Nspace);
+    dump_matrix(outdir, "C", atom->C, Nl * Nl, Nspace);
+    write_f64(outdir, "vbroad", atom->vbroad, Nspace);
+    /* lines: [i, j, lambda0, Aji, Bji, Bij, isotope_frac, Nblue, Nlambda,
+               symmetric, Ncomponent, c_shift0, c_fraction0, Voigt, PRD, 0] */
+    double *lr = (double *) calloc(16L * atom->Nline, sizeof(double));
+    double *ad = (double *) calloc((long) atom->Nline * Nspace, sizeof(double));
+    double *wp = (double *) calloc((long) atom->Nline * Nspace, sizeof(double));
+    double *ph = (double *) calloc((long) atom->Nline * 5 * 2 * atmos.Nrays * Nspace, sizeof(double));
+    int *phla = (int *) calloc(atom->Nline * 5, sizeof(int));
+    for (int kr = 0; kr < atom->Nline; kr++) {
+      AtomicLine *l = &atom->line[kr];
+      double *r = lr + 16L * kr;
+      r[0] = l->i; r[1] = l->j; r[2] = l->lambda0; r[3] = l->Aji; r[4] = l->Bji;
+      r[5] = l->Bij; r[6] = l->isotope_frac; r[7] = l->Nblue; r[8] = l->Nlambda;
+      r[9] = l->symmetric; r[10] = l->Ncomponent;
+      r[11] = l->Ncomponent > 0 ? l->c_shift[0] : 0.0;
+      r[12] = l->Ncomponent > 0 ? l->c_fraction[0] : 1.0;
+      r[13] = l->Voigt; r[14] = l->PRD;
+      if (l->Voigt) Damping(l, ad + (long) kr * Nspace);
+      memcpy(wp + (long) kr * Nspace, l->wphi, Nspace * sizeof(double));
+      int sel[5] = {0, l->Nlambda / 4, l->Nlambda / 2, (3 * l->Nlambda) / 4, l->Nlambda - 1};
+      for (int s = 0; s < 5; s++) {
+        phla[kr * 5 + s] = sel[s];
+        for (int q = 0; q < 2 * atmos.Nrays; q++) {
+          int lamu = 2 * atmos.Nrays * sel[s] + q;
+          memcpy(ph + (((long) kr * 5 + s) * 2 * atmos.Nrays + q) * Nspace, l->phi[lamu],
+                 Nspace * sizeof(double));
+        }
+      }
+    }
+    write_f64(outdir, "lines", lr, 16L * atom->Nline);
+    write_f64(outdir, "adamp", ad, (long) atom->Nline * Nspace);
+    write_f64(outdir, "wphi", wp, (long) atom->Nline * Nspace);
+    write_f64(outdir, "phi_sample", ph, (long) atom->Nline * 5 * 2 * atmos.Nrays * Nspace);
+    write_i32(outdir, "phi_sample_la", phla, atom->Nline * 5);
+    free(lr); free(ad); free(wp); free(ph); free(phla);
+    /* continua: [i, j, Nblue, Nlambda, lambda0, hydrogenic] + alpha */
+    int na = 0;
+    for (int kr = 0; kr < atom->Ncont; kr++) na += atom->continuum[kr].Nlambda;
+    double *cr = (double *) calloc(8L * atom->Ncont, sizeof(double));
+    double *al = (double *) calloc(na > 0 ? na : 1, sizeof(double));
+    int off = 0;
+    for (int kr = 0; kr < atom->Ncont; kr++) {
+      AtomicContinuum *c = &atom->continuum[kr];
+      double *r = cr + 8L * kr;
+      r[0] = c->i; r[1] = c->j; r[2] = c->Nblue; r[3] = c->Nlambda; r[4] = c->lambda0;
+      r[5] = c->hydrogenic; r[6] = off;
+      memcpy(al + off, c->alpha, c->Nlambda * sizeof(double));
+      off += c->Nlambda;
+    }
+    write_f64(outdir, "continua", cr, 8L * atom->Ncont);
+    write_f64(outdir, "alpha", al, na > 0 ? na : 1);
+    free(cr); free(al);
+
+    /* one iteration by hand: Gamma = C + radiative (Iterate, iterate.c:86-97) */
+    initGammaAtom(atom);
+    solveSpectrum(TRUE, FALSE);
+    dump_matrix(outdir, "Gamma1", atom->Gamma, Nl * Nl, Nspace);
+    dump_matrix(outdir, "J1", spectrum.J, Nspect, Nspace);
+    statEquil(atom, input.isum);
+    dump_matrix(outdir, "n1", atom->n, Nl, Nspace);
+  } else {
+    Iterate(input.NmaxIter, input.iterLimit);
+    dump_matrix(outdir, "n_final", atom->n, Nl, Nspace);
+    dump_matrix(outdir, "J_final", spectrum.J, Nspect, Nspace);
+    mySpectrum spec;
+    spec.nlw = spectrum.Nspect;
+    spec.Nrays = atmos.Nrays;
+    _solveray(mu, &spec);
+    write_f64(outdir, "lam_out", spec.lam, spec.nlw);
+    write_f64(outdir, "I_out", spec.sI, spec.nlw);
+    int mo[2] = {spec.nlw, 0};
+    write_i32(outdir, "out_meta", mo, 2);
+  }
+  return Nspect;
+}

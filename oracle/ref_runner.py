@@ -83,7 +83,7 @@ KEYWORD_TEMPLATE = """\
   LIMIT_MEMORY = FALSE
   ALLOW_PASSIVE_BB = FALSE
   PRINT_CPU = FALSE
-"""
+{extra}"""
 
 PASSIVE_ATOMS = ["H_6.atom", "He.atom", "C.atom", "N.atom", "O.atom", "S.atom",
                  "Fe.atom", "Si.atom", "Al.atom", "Na.atom", "Mg.atom"]
@@ -95,7 +95,7 @@ def write_inputs(workdir: str, kurucz_lines: str | None, atoms=None,
     opts = dict(nrays=1, nmax_scatter=0, nmax_iter=1, iter_limit="1.0E-2",
                 ng_order=0, ng_delay=10, ng_period=3, vmicro_char=5.0,
                 stokes_mode="FULL_STOKES", magneto_optical="FALSE",
-                kurucz="kurucz.input" if kurucz_lines else "none")
+                kurucz="kurucz.input" if kurucz_lines else "none", extra="")
     opts.update(kw)
     with open(os.path.join(workdir, "keyword.input"), "w") as f:
         f.write(KEYWORD_TEMPLATE.format(**opts))
@@ -221,6 +221,9 @@ class Reference:
     def dump_lte(self, workdir, mu, atm, wave, outdir):
         return self._run(_dump_job, (workdir, self.pyrh_path, mu, atm, wave, outdir))
 
+    def nlte(self, workdir, mu, atm, wave, outdir, mode):
+        return self._run(_nlte_job, (workdir, self.pyrh_path, mu, atm, wave, outdir, mode))
+
     def vacuum_to_air(self, lam_vac):
         return self._run(_vac2air_job, (self.pyrh_path, lam_vac))
 
@@ -252,6 +255,76 @@ def read_dump(outdir: str) -> dict:
 
 def scratch_dir(prefix="rhref_") -> str:
     return tempfile.mkdtemp(prefix=prefix)
+
+
+
+# ------------------------------------------------------------------ NLTE --
+
+def make_pyrh_root(atom_name: str, atom_text: str, ref_root: str = REF_ROOT) -> str:
+    """Scratch PYRH_PATH: the reference looks model atoms up under
+    $PYRH_PATH/rh/Atoms (rh/readatom.c:839-842), so the reference's data files
+    are linked there next to the generated model atom."""
+    root = tempfile.mkdtemp(prefix="pyrh_root_")
+    atoms = os.path.join(root, "rh", "Atoms")
+    os.makedirs(atoms)
+    src = os.path.join(ref_root, "rh", "Atoms")
+    for f in os.listdir(src):
+        os.symlink(os.path.join(src, f), os.path.join(atoms, f))
+    os.symlink(os.path.join(ref_root, "rh", "Molecules"), os.path.join(root, "rh", "Molecules"))
+    with open(os.path.join(atoms, atom_name), "w") as f:
+        f.write(atom_text)
+    return root
+
+
+def _nlte_job(args):
+    workdir, pyrh_path, mu, atm, wave, outdir, mode = args
+    lib = _lib(pyrh_path)
+    atm = np.ascontiguousarray(atm, dtype=np.float64)
+    wave = np.ascontiguousarray(wave, dtype=np.float64)
+    os.makedirs(outdir, exist_ok=True)
+    lib.harness_nlte.restype = C.c_int
+    return lib.harness_nlte(workdir.encode(), C.c_double(mu), atm.shape[1], _p(atm),
+                            len(wave), _p(wave), outdir.encode(), int(mode))
+
+
+def read_nlte_dump(outdir: str) -> dict:
+    f64 = lambda n: np.fromfile(os.path.join(outdir, n + ".f64"))
+    i32 = lambda n: np.fromfile(os.path.join(outdir, n + ".i32"), dtype=np.int32)
+    ex = lambda n, s: os.path.exists(os.path.join(outdir, n + s))
+    d = {}
+    if ex("meta", ".i32"):
+        m = i32("meta")
+        ns, nd, nr, nl, nline, ncont = (int(x) for x in m[:6])
+        d["meta"] = m
+        d["fmeta"] = f64("fmeta")
+        d["lambda"] = f64("lambda")
+        for k in ("muz", "wmu", "T", "ne", "nHtot", "vel", "vturb", "height", "g", "E",
+                  "ntotal", "vbroad"):
+            d[k] = f64(k)
+        d["stage"] = i32("stage")
+        d["background"] = f64("background").reshape(3, ns, nd)
+        d["bgflags"] = i32("bgflags")
+        d["J0"] = f64("J0").reshape(ns, nd)
+        d["nstar"] = f64("nstar").reshape(nl, nd)
+        d["n0"] = f64("n0").reshape(nl, nd)
+        d["C"] = f64("C").reshape(nl * nl, nd)
+        d["lines"] = f64("lines").reshape(nline, 16)
+        d["adamp"] = f64("adamp").reshape(nline, nd)
+        d["wphi"] = f64("wphi").reshape(nline, nd)
+        d["phi_sample"] = f64("phi_sample").reshape(nline, 5, 2 * nr, nd)
+        d["phi_sample_la"] = i32("phi_sample_la").reshape(nline, 5)
+        d["continua"] = f64("continua").reshape(ncont, 8)
+        d["alpha"] = f64("alpha")
+        d["Gamma1"] = f64("Gamma1").reshape(nl * nl, nd)
+        d["J1"] = f64("J1").reshape(ns, nd)
+        d["n1"] = f64("n1").reshape(nl, nd)
+    if ex("n_final", ".f64"):
+        nl = len(f64("g")) if ex("g", ".f64") else None
+        d["n_final"] = f64("n_final")
+        d["J_final"] = f64("J_final")
+        d["lam_out"] = f64("lam_out")
+        d["I_out"] = f64("I_out")
+    return d
 
 
 if __name__ == "__main__":

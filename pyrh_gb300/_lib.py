@@ -5,7 +5,7 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libpyrh_gb300.so")
+LIB_PATH = os.environ.get("PYRH_GB300_LIB", os.path.join(HERE, "libpyrh_gb300.so"))
 
 PYRH_OK = 0
 PYRH_ERR_ARG = 1

@@ -22,14 +22,20 @@ def _sources_mtime() -> float:
     return max(os.path.getmtime(f) for f in files)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _sources_mtime():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, out: str | None = None,
+          defines: tuple = ()) -> str:
+    """Compile the library; `out` and `defines` (e.g. "PYRH_LTE_MIN_BLOCKS=3")
+    build a variant next to the default one (used for tile/occupancy sweeps)."""
+    target = out or LIB
+    if not force and os.path.exists(target) and os.path.getmtime(target) >= _sources_mtime():
+        return target
+    bdir = BUILD if out is None else os.path.join(BUILD, os.path.basename(out) + ".d")
+    os.makedirs(bdir, exist_ok=True)
+    dflags = [f"-D{d}" for d in defines]
 
     def compile_unit(u):
-        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
-        cmd = [NVCC, *GENCODE, *FLAGS, "-c", os.path.join(CSRC, u), "-o", obj]
+        obj = os.path.join(bdir, u.replace(".cu", ".o"))
+        cmd = [NVCC, *GENCODE, *FLAGS, *dflags, "-c", os.path.join(CSRC, u), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {u}:\n{r.stderr}")
@@ -39,10 +45,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     with ThreadPoolExecutor(len(UNITS)) as ex:
         objs = list(ex.map(compile_unit, UNITS))
-    tmp = LIB + ".tmp"
+    tmp = target + ".tmp"
     subprocess.run([NVCC, *GENCODE, "-shared", "-o", tmp, *objs, "-lcudart"], check=True)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, target)
+    return target
 
 
 if __name__ == "__main__":

@@ -137,13 +137,14 @@ struct Opacity {
     }
     const size_t ci = (size_t)k * nl;
     chi = chi_c[ci] + cI;
-    const R rchi = R(1) / chi;
+    const R rchi = fdiv(R(1), chi);
     S[0] = (eta_c[ci] + eI) * rchi;
     S[1] = eQ * rchi;
     S[2] = eU * rchi;
     S[3] = eV * rchi;
     K6[0] = cQ * rchi; K6[1] = cU * rchi; K6[2] = cV * rchi;
-    K6[3] = pQ * rchi; K6[4] = pU * rchi; K6[5] = pV * rchi;
+    if (MO) { K6[3] = pQ * rchi; K6[4] = pU * rchi; K6[5] = pV * rchi; }
+    else { K6[3] = K6[4] = K6[5] = R(0); }
   }
 };
 
@@ -162,65 +163,55 @@ __device__ __forceinline__ void build_K(const R k6[6], R K[4][4]) {
   }
 }
 
-// DELO-Bezier3 along the ray to the observer; bezier_1D.c:52-300 with
-// to_obs = TRUE (k_start = Ndep-1, k_end = 0, dk = -1).
+// One DELO-Bezier3 step (bezier_1D.c:207-247): with the interval weights,
+// the K' parameters and derivatives at the upwind (u) and central (0) points
+// and the source vectors, returns the new Stokes vector in I (in place).
+// Without magneto-optical terms K' has non-zeros only in row/column 0, so
+//   Md = [[1 + c|k|^2, b^T], [b, I + c k k^T]],  c = gamma*dt/3,
+// which is solved with the Schur complement of its 3x3 block and the
+// Sherman-Morrison inverse of I + c k k^T (about 60 flops instead of a 4x4
+// factorisation); the magneto-optical case keeps the general 4x4 algebra.
 template <typename R, bool MO>
-__device__ void solve_stokes(const Opacity<R, MO>& op, const R* ds, int nd, double B0,
-                             double B1, R out[4]) {
-  // pipeline: u = k+1, c = k, d = k-1, dd = k-2
-  R chi_u, chi_c, chi_d, chi_dd;
-  R S_u[4], S_c[4], S_d[4], S_dd[4];
-  R k_u[6], k_c[6], k_d[6], k_dd[6];
-  op(nd - 1, chi_u, S_u, k_u);
-  op(nd - 2, chi_c, S_c, k_c);
-  chi_d = chi_c;
-  if (nd >= 3) op(nd - 3, chi_d, S_d, k_d);
-
-  R I[4];
-  {
-    const double dtau0 = 0.5 * ((double)chi_u + (double)chi_c) * (double)ds[nd - 1];
-    I[0] = R(B1 - (B0 - B1) / dtau0);
-    I[1] = I[2] = I[3] = R(0);
-  }
-  int k = nd - 2;
-  R dsup = ds[k + 1], dsdn = (k >= 1) ? ds[k] : ds[k + 1];
-  R dchi_up = (chi_c - chi_u) / dsup;
-  R dchi_c = cent_deriv<R>(dsup, dsdn, chi_u, chi_c, chi_d);
-  R c2 = fmax(chi_c - (dsup / R(3)) * dchi_c, R(0));
-  R c1 = fmax(chi_u + (dsup / R(3)) * dchi_up, R(0));
-  R dtau_uw = R(0.25) * dsup * (chi_c + chi_u + c1 + c2);
-  R dSu[4], dKu6[6];
-  for (int n = 0; n < 4; ++n) dSu[n] = (S_c[n] - S_u[n]) / dtau_uw;
-  for (int n = 0; n < 6; ++n) dKu6[n] = (k_c[n] - k_u[n]) / dtau_uw;
-
-  for (k = nd - 2; k >= 1; --k) {
-    // downwind derivative of chi needs depth k-2
-    R dchi_dn;
-    dsdn = ds[k];
-    if (k > 1) {
-      op(k - 2, chi_dd, S_dd, k_dd);
-      const R dsdn2 = ds[k - 1];
-      dchi_dn = cent_deriv<R>(dsdn, dsdn2, chi_c, chi_d, chi_dd);
-    } else {
-      dchi_dn = (chi_d - chi_c) / dsdn;
-    }
-    c2 = fmax(chi_c + (dsdn / R(3)) * dchi_c, R(0));
-    c1 = fmax(chi_d - (dsdn / R(3)) * dchi_dn, R(0));
-    const R dtau_dw = R(0.25) * dsdn * (chi_c + chi_d + c1 + c2);
-    const R dt = dtau_uw, dt03 = dt / R(3);
-    R alpha, beta, gamma, theta, eps;
-    bezier3_coeffs(dt, alpha, beta, gamma, theta, eps);
-
-    R dK06[6], dS0[4];
-    for (int n = 0; n < 6; ++n) dK06[n] = cent_deriv<R>(dtau_uw, dtau_dw, k_u[n], k_c[n], k_d[n]);
-    for (int n = 0; n < 4; ++n) dS0[n] = cent_deriv<R>(dtau_uw, dtau_dw, S_u[n], S_c[n], S_d[n]);
-
+__device__ __forceinline__ void delo_step(R alpha, R beta, R gamma, R theta, R eps, R dt03,
+                                          const R ku[6], const R k0[6], const R dku[6],
+                                          const R dk0[6], const R Su[4], const R S0[4],
+                                          const R dSu[4], const R dS0[4], R I[4]) {
+  if (!MO) {
+    const R c = gamma * dt03, pK = alpha + gamma * (R(1) + dt03);
+    const R ca = theta * dt03, pa = -beta - theta + theta * dt03;
+    const R bt = beta + theta, ag = alpha + gamma, tdt = theta * dt03, gdt = gamma * dt03;
+    const R kuIv = ku[0] * I[1] + ku[1] * I[2] + ku[2] * I[3];
+    const R ku2 = ku[0] * ku[0] + ku[1] * ku[1] + ku[2] * ku[2];
+    R V[4];
+    V[0] = (eps + ca * ku2) * I[0] + (pa * ku[0] + ca * dku[0]) * I[1] +
+           (pa * ku[1] + ca * dku[1]) * I[2] + (pa * ku[2] + ca * dku[2]) * I[3] +
+           bt * Su[0] - tdt * (ku[0] * Su[1] + ku[1] * Su[2] + ku[2] * Su[3]) + ag * S0[0] +
+           gdt * (k0[0] * S0[1] + k0[1] * S0[2] + k0[2] * S0[3]) +
+           dt03 * (gamma * dS0[0] - theta * dSu[0]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      V[j + 1] = (pa * ku[j] + ca * dku[j]) * I[0] + eps * I[j + 1] + ca * ku[j] * kuIv -
+                 tdt * ku[j] * Su[0] + bt * Su[j + 1] + gdt * k0[j] * S0[0] + ag * S0[j + 1] +
+                 dt03 * (gamma * dS0[j + 1] - theta * dSu[j + 1]);
+    // solve Md x = V
+    const R b0 = pK * k0[0] + c * dk0[0], b1 = pK * k0[1] + c * dk0[1], b2 = pK * k0[2] + c * dk0[2];
+    const R sig = R(1) + c * (k0[0] * k0[0] + k0[1] * k0[1] + k0[2] * k0[2]);
+    const R f = fdiv(c, sig);
+    const R kb = k0[0] * b0 + k0[1] * b1 + k0[2] * b2;
+    const R kv = k0[0] * V[1] + k0[1] * V[2] + k0[2] * V[3];
+    const R w0 = b0 - f * kb * k0[0], w1 = b1 - f * kb * k0[1], w2 = b2 - f * kb * k0[2];
+    const R z0 = V[1] - f * kv * k0[0], z1 = V[2] - f * kv * k0[1], z2 = V[3] - f * kv * k0[2];
+    const R x0 = fdiv(V[0] - (b0 * z0 + b1 * z1 + b2 * z2), sig - (b0 * w0 + b1 * w1 + b2 * w2));
+    I[0] = x0;
+    I[1] = z0 - x0 * w0;
+    I[2] = z1 - x0 * w1;
+    I[3] = z2 - x0 * w2;
+  } else {
     R Ku[4][4], K0[4][4], dKu[4][4], dK0[4][4];
-    build_K<R, MO>(k_u, Ku);
-    build_K<R, MO>(k_c, K0);
-    build_K<R, MO>(dKu6, dKu);
-    build_K<R, MO>(dK06, dK0);
-
+    build_K<R, MO>(ku, Ku);
+    build_K<R, MO>(k0, K0);
+    build_K<R, MO>(dku, dKu);
+    build_K<R, MO>(dk0, dK0);
     R Md[4][4], V0[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
@@ -238,32 +229,41 @@ __device__ void solve_stokes(const Opacity<R, MO>& op, const R* ds, int nd, doub
         const R ma = eps * id - beta * Ku[j][i] + theta * (dt03 * (kku + dKu[j][i] + Ku[j][i]) - Ku[j][i]);
         const R mb = beta * id + theta * (id - dt03 * Ku[j][i]);
         const R mc = alpha * id + gamma * (id + dt03 * K0[j][i]);
-        v += ma * I[i] + mb * S_u[i] + mc * S_c[i];
+        v += ma * I[i] + mb * Su[i] + mc * S0[i];
       }
       V0[j] = v + dt03 * (gamma * dS0[j] - theta * dSu[j]);
     }
     solve4<R>(Md, V0, I);
-
-    // shift the window one depth up
-    for (int n = 0; n < 4; ++n) { S_u[n] = S_c[n]; S_c[n] = S_d[n]; S_d[n] = S_dd[n]; dSu[n] = dS0[n]; }
-    for (int n = 0; n < 6; ++n) { k_u[n] = k_c[n]; k_c[n] = k_d[n]; k_d[n] = k_dd[n]; dKu6[n] = dK06[n]; }
-    chi_u = chi_c; chi_c = chi_d; chi_d = chi_dd;
-    dtau_uw = dtau_dw;
-    dchi_c = dchi_dn;
   }
-  // Linear last interval (bezier_1D.c:266-299); chi_c/S_c/k_c = depth 0,
-  // chi_u/S_u/k_u = depth 1.
-  {
-    const double dtau = 0.5 * ((double)chi_c + (double)chi_u) * (double)ds[1];
-    double w[3];
-    w3(dtau, w);
-    const R w0 = R(w[0]), wd = R(w[1] / dtau), w1 = R(w[1]);
+}
+
+// Linear last interval (bezier_1D.c:266-299).
+template <typename R, bool MO>
+__device__ __forceinline__ void delo_last(R w0, R w1, R wd, const R ku[6], const R k0[6],
+                                          const R S0[4], const R dSu[4], R I[4], R out[4]) {
+  if (!MO) {
+    // A = (1-w0) I - wd Ku (off-diagonal); Md = I + (w0 - wd) K0 (off-diagonal)
+    R V[4];
+    V[0] = w0 * S0[0] - w1 * dSu[0] + (R(1) - w0) * I[0] -
+           wd * (ku[0] * I[1] + ku[1] * I[2] + ku[2] * I[3]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      V[j + 1] = w0 * S0[j + 1] - w1 * dSu[j + 1] + (R(1) - w0) * I[j + 1] - wd * ku[j] * I[0];
+    const R g = w0 - wd;
+    const R b0 = g * k0[0], b1 = g * k0[1], b2 = g * k0[2];
+    const R x0 = fdiv(V[0] - (b0 * V[1] + b1 * V[2] + b2 * V[3]),
+                      R(1) - (b0 * b0 + b1 * b1 + b2 * b2));
+    out[0] = x0;
+    out[1] = V[1] - x0 * b0;
+    out[2] = V[2] - x0 * b1;
+    out[3] = V[3] - x0 * b2;
+  } else {
     R Ku[4][4], K0[4][4], Md[4][4], V0[4];
-    build_K<R, MO>(k_u, Ku);
-    build_K<R, MO>(k_c, K0);
+    build_K<R, MO>(ku, Ku);
+    build_K<R, MO>(k0, K0);
 #pragma unroll
     for (int n = 0; n < 4; ++n) {
-      R v = w0 * S_c[n] + w1 * -dSu[n];
+      R v = w0 * S0[n] + w1 * -dSu[n];
 #pragma unroll
       for (int m = 0; m < 4; ++m) {
         const R A = (n == m) ? (R(1) - w0) : (-wd * Ku[n][m]);
@@ -274,6 +274,88 @@ __device__ void solve_stokes(const Opacity<R, MO>& op, const R* ds, int nd, doub
     }
     solve4<R>(Md, V0, out);
   }
+}
+
+// DELO-Bezier3 along the ray to the observer; bezier_1D.c:52-300 with
+// to_obs = TRUE (k_start = Ndep-1, k_end = 0, dk = -1).
+template <typename R, bool MO>
+__device__ void solve_stokes(const Opacity<R, MO>& op, const R* ds, int nd, double B0,
+                             double B1, R out[4]) {
+  constexpr int NK = MO ? 6 : 3;
+  // pipeline: u = k+1, c = k, d = k-1, dd = k-2
+  R chi_u, chi_c, chi_d, chi_dd;
+  R S_u[4], S_c[4], S_d[4], S_dd[4];
+  R k_u[6], k_c[6], k_d[6], k_dd[6];
+  op(nd - 1, chi_u, S_u, k_u);
+  op(nd - 2, chi_c, S_c, k_c);
+  op(nd - 3, chi_d, S_d, k_d);
+
+  R I[4];
+  {
+    const double dtau0 = 0.5 * ((double)chi_u + (double)chi_c) * (double)ds[nd - 1];
+    I[0] = R(B1 - (B0 - B1) / dtau0);
+    I[1] = I[2] = I[3] = R(0);
+  }
+  int k = nd - 2;
+  R dsup = ds[k + 1], dsdn = ds[k];
+  R dchi_up = fdiv(chi_c - chi_u, dsup);
+  R dchi_c = cent_deriv<R>(dsup, dsdn, chi_u, chi_c, chi_d);
+  R c2 = fmax(chi_c - (dsup / R(3)) * dchi_c, R(0));
+  R c1 = fmax(chi_u + (dsup / R(3)) * dchi_up, R(0));
+  R dtau_uw = R(0.25) * dsup * (chi_c + chi_u + c1 + c2);
+  R dSu[4], dKu6[6];
+  {
+    const R r = fdiv(R(1), dtau_uw);
+#pragma unroll
+    for (int n = 0; n < 4; ++n) dSu[n] = (S_c[n] - S_u[n]) * r;
+#pragma unroll
+    for (int n = 0; n < 6; ++n) dKu6[n] = (n < NK) ? (k_c[n] - k_u[n]) * r : R(0);
+  }
+
+  for (k = nd - 2; k >= 1; --k) {
+    // downwind derivative of chi needs depth k-2
+    R dchi_dn;
+    dsdn = ds[k];
+    if (k > 1) {
+      op(k - 2, chi_dd, S_dd, k_dd);
+      dchi_dn = cent_deriv<R>(dsdn, ds[k - 1], chi_c, chi_d, chi_dd);
+    } else {
+      dchi_dn = fdiv(chi_d - chi_c, dsdn);
+    }
+    c2 = fmax(chi_c + (dsdn / R(3)) * dchi_c, R(0));
+    c1 = fmax(chi_d - (dsdn / R(3)) * dchi_dn, R(0));
+    const R dtau_dw = R(0.25) * dsdn * (chi_c + chi_d + c1 + c2);
+    const R dt = dtau_uw, dt03 = dt / R(3);
+    R alpha, beta, gamma, theta, eps;
+    bezier3_coeffs(dt, alpha, beta, gamma, theta, eps);
+
+    // derivatives at the central point share 1/dtau and the weight
+    const R rup = fdiv(R(1), dtau_uw), rdn = fdiv(R(1), dtau_dw);
+    const R aw = R(0.333333333333333333333333) * (R(1) + fdiv(dtau_dw, dtau_dw + dtau_uw));
+    R dK06[6], dS0[4];
+#pragma unroll
+    for (int n = 0; n < 6; ++n)
+      dK06[n] = (n < NK) ? cent_deriv_w<R>(rup, rdn, aw, k_u[n], k_c[n], k_d[n]) : R(0);
+#pragma unroll
+    for (int n = 0; n < 4; ++n) dS0[n] = cent_deriv_w<R>(rup, rdn, aw, S_u[n], S_c[n], S_d[n]);
+
+    delo_step<R, MO>(alpha, beta, gamma, theta, eps, dt03, k_u, k_c, dKu6, dK06, S_u, S_c, dSu,
+                     dS0, I);
+
+    // shift the window one depth up
+#pragma unroll
+    for (int n = 0; n < 4; ++n) { S_u[n] = S_c[n]; S_c[n] = S_d[n]; S_d[n] = S_dd[n]; dSu[n] = dS0[n]; }
+#pragma unroll
+    for (int n = 0; n < 6; ++n) { k_u[n] = k_c[n]; k_c[n] = k_d[n]; k_d[n] = k_dd[n]; dKu6[n] = dK06[n]; }
+    chi_u = chi_c; chi_c = chi_d; chi_d = chi_dd;
+    dtau_uw = dtau_dw;
+    dchi_c = dchi_dn;
+  }
+  // chi_c/S_c/k_c = depth 0, chi_u/S_u/k_u = depth 1.
+  const double dtau = 0.5 * ((double)chi_c + (double)chi_u) * (double)ds[1];
+  double w[3];
+  w3(dtau, w);
+  delo_last<R, MO>(R(w[0]), R(w[1]), R(w[1] / dtau), k_u, k_c, S_c, dSu, I, out);
 }
 
 // Scalar Bezier3 along the ray to the observer (bezier_1D.c:306-541).
@@ -361,8 +443,14 @@ __device__ R solve_feautrier(const Opacity<R, MO>& op, const R* ds, int nd, doub
   return R(2) * P0;
 }
 
+// Resident blocks per SM the FP32 kernel is compiled for (register cap
+// 65536 / (256 * N)); the FP64 kernel is compiled without a cap.
+#ifndef PYRH_LTE_MIN_BLOCKS
+#define PYRH_LTE_MIN_BLOCKS 4
+#endif
+
 template <typename R, bool MO>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, (sizeof(R) == 4 ? PYRH_LTE_MIN_BLOCKS : 1))
 lte_stokes_kernel(LteArgs args) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nline = args.nline < PYRH_MAX_LINES ? args.nline : PYRH_MAX_LINES;

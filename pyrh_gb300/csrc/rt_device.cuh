@@ -37,16 +37,23 @@ template <typename R>
 __device__ __forceinline__ Cx<R> cmul(Cx<R> a, Cx<R> b) {
   return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r};
 }
+// Division: IEEE in FP64; in FP32 the fast reciprocal-based division
+// (__fdividef, 2 ulp), which the FP32 accuracy budget (1e-4) allows.
+__device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+
 template <typename R>
 __device__ __forceinline__ Cx<R> cdiv(Cx<R> a, Cx<R> b) {
-  R d = b.r * b.r + b.i * b.i;
-  return {(a.r * b.r + a.i * b.i) / d, (a.i * b.r - a.r * b.i) / d};
+  R inv = fdiv(R(1), b.r * b.r + b.i * b.i);
+  return {(a.r * b.r + a.i * b.i) * inv, (a.i * b.r - a.r * b.i) * inv};
 }
 
 __device__ __forceinline__ double dev_exp(double x) { return exp(x); }
-__device__ __forceinline__ float dev_exp(float x) { return expf(x); }
+__device__ __forceinline__ float dev_exp(float x) { return __expf(x); }
 __device__ __forceinline__ void dev_sincos(double x, double* s, double* c) { sincos(x, s, c); }
-__device__ __forceinline__ void dev_sincos(float x, float* s, float* c) { sincosf(x, s, c); }
+// |x| <= 2 a |v| stays below ~11 in Humlicek region IV; the hardware sine /
+// cosine keeps an absolute error near 1e-6 there, far inside the budget.
+__device__ __forceinline__ void dev_sincos(float x, float* s, float* c) { __sincosf(x, s, c); }
 
 // Humlicek W4: returns H = Re W, F = Im W for t = a - i v.
 template <typename R>
@@ -107,11 +114,20 @@ __device__ __forceinline__ void humlicek(R a, R v, R& H, R& F) {
 
 template <typename R>
 __device__ __forceinline__ R cent_deriv(R dsup, R dsdn, R up, R c, R dn) {
-  R fim1 = (c - up) / dsup, fi = (dn - c) / dsdn;
+  R fim1 = fdiv(c - up, dsup), fi = fdiv(dn - c, dsdn);
   if (fim1 * fi > R(0)) {
-    R alpha = R(0.333333333333333333333333) * (R(1) + dsdn / (dsdn + dsup));
-    return (fim1 * fi) / ((R(1) - alpha) * fim1 + alpha * fi);
+    R alpha = R(0.333333333333333333333333) * (R(1) + fdiv(dsdn, dsdn + dsup));
+    return fdiv(fim1 * fi, (R(1) - alpha) * fim1 + alpha * fi);
   }
+  return R(0);
+}
+
+// cent_deriv with the path lengths' reciprocals and the weight alpha
+// precomputed (shared by all entries of one depth).
+template <typename R>
+__device__ __forceinline__ R cent_deriv_w(R rdsup, R rdsdn, R alpha, R up, R c, R dn) {
+  R fim1 = (c - up) * rdsup, fi = (dn - c) * rdsdn;
+  if (fim1 * fi > R(0)) return fdiv(fim1 * fi, (R(1) - alpha) * fim1 + alpha * fi);
   return R(0);
 }
 

@@ -214,3 +214,68 @@ def synthetic_batch(natm: int, seed: int = 2024, n_per_line: int = 112,
     lp[:, :, 0, :] *= f_fe[:, None, :]
     out["line_pops"] = lp
     return out
+
+
+# ------------------------------------------------------------------------
+# Six-level Ca II-like model atom in RH .atom format (5 bound levels plus
+# the continuum, 5 bound-bound CRD Voigt lines, 5 hydrogenic bound-free
+# edges, electron-impact collisions tabulated on TEMP).  Level energies,
+# log gf and collision strengths are drawn from a seeded table around Ca II
+# like values (energies 0-11.9 eV, log gf in [-1.5, 0.2]).  Field layout as
+# the reference reader expects it (rh/readatom.c:108-470).
+# ------------------------------------------------------------------------
+
+_CAII_LEVELS = (  # E [cm^-1], g, label, stage
+    (0.0, 2.0, "CA II 3P6 4S 2SE"),
+    (13650.0, 4.0, "CA II 3P6 3D 2DE 3"),
+    (13711.0, 6.0, "CA II 3P6 3D 2DE 5"),
+    (25192.0, 2.0, "CA II 3P6 4P 2PO 1"),
+    (25414.0, 4.0, "CA II 3P6 4P 2PO 3"),
+    (95752.0, 1.0, "CA III 3P6 1SE"),
+)
+# (upper, lower, Nlambda, qcore, qwing) of the five lines
+_CAII_LINES = ((3, 0, 150, 15.0, 600.0), (4, 0, 150, 15.0, 600.0),
+               (3, 1, 110, 4.0, 150.0), (4, 1, 110, 4.0, 150.0), (4, 2, 120, 4.0, 200.0))
+
+
+def caii_like_atom(seed: int = 11, nlambda_scale: float = 1.0) -> str:
+    rng = np.random.default_rng(seed)
+    E = [lv[0] for lv in _CAII_LEVELS]
+    # jitter bound excited levels by +-1 %, keep ordering
+    for i in range(1, 5):
+        E[i] *= 1.0 + rng.uniform(-0.01, 0.01)
+    E[1], E[2] = sorted(E[1:3])
+    E[3], E[4] = sorted(E[3:5])
+    out = ["# Ca II-like six-level model atom (seeded synthetic table)",
+           "  CA", "", "    6   5   5   0", ""]
+    for i, (e, (_, g, lab)) in enumerate(zip(E, _CAII_LEVELS)):
+        stage = 2 if i == 5 else 1
+        out.append(f"  {e:12.3f}   {g:4.1f}   '{lab:<20s}'   {stage:d}   {i:d}")
+    out.append("")
+    for (j, i, nl, qc, qw) in _CAII_LINES:
+        loggf = rng.uniform(-1.5, 0.2)
+        f = 10.0 ** loggf / _CAII_LEVELS[i][1]
+        nl = max(21, int(round(nl * nlambda_scale)) | 1)
+        out.append(f"  {j:d}  {i:d}  {f:10.4E}   VOIGT  {nl:4d}   ASYMM  {qc:6.1f}  {qw:7.1f}"
+                   f"  UNSOLD   1.00   0.00   1.00   0.00   1.50E+08   1.0E-00")
+    out.append("")
+    for i in range(5):
+        alpha0 = 10.0 ** rng.uniform(-23.0, -21.2)
+        edge_nm = 1.0e7 / (E[5] - E[i])
+        out.append(f"  5  {i:d}  {alpha0:11.4E}  {max(9, int(round(30 * nlambda_scale))):4d}"
+                   f"  HYDROGENIC  {0.35 * edge_nm:9.3f}")
+    out.append("")
+    temps = (3000.0, 5000.0, 7000.0, 15000.0, 50000.0, 100000.0)
+    out.append(" TEMP    6   " + "".join(f"{t:11.1f}" for t in temps))
+    out.append("")
+    for j in range(1, 5):
+        for i in range(j):
+            om = 10.0 ** rng.uniform(0.0, 1.4) * np.linspace(0.9, 1.3, 6)
+            out.append(f" OMEGA   {j:d}  {i:d}  " + "".join(f"{v:11.3E}" for v in om))
+    out.append("")
+    for i in range(5):
+        ci = 10.0 ** rng.uniform(-17.5, -15.7)
+        out.append(f" CI      {i:d}  5  " + "".join(f"{ci:11.3E}" for _ in temps))
+    out.append("")
+    out.append(" END")
+    return "\n".join(out) + "\n"
