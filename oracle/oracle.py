@@ -13,7 +13,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "librt_oracle.so")
-SOURCES = [os.path.join(HERE, "rt_oracle.c")]
+SOURCES = [os.path.join(HERE, "rt_oracle.c"), os.path.join(HERE, "nlte_oracle.c")]
 
 RLK_NCONST = 24
 _STACKED = ("mu", "line_const", "zeeman", "zeeman_n", "vmicro_char", "magneto_optical",
@@ -37,7 +37,8 @@ class OracleLines(C.Structure):
 
 def build(force: bool = False) -> str:
     """Compile the oracle with gcc (OpenMP for the threaded batch driver)."""
-    newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "rt_oracle.h")])
+    newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "rt_oracle.h"),
+                                                         os.path.join(HERE, "nlte_oracle.h")])
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
     subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-o", LIB] + SOURCES +
@@ -175,3 +176,115 @@ def output_mask(lam: np.ndarray, lambda_ref: float) -> np.ndarray:
     """Indices of the spectrum that rhf1d() returns: every wavelength except
     the one equal to LAMBDA_REF (rh/rhf1d/pyrh_solveray.c:130-150)."""
     return np.nonzero(lam != lambda_ref)[0]
+
+
+# ------------------------------------------------------------------ NLTE --
+
+class NlteProblem(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("ndep", "nspect", "nrays", "nlevel", "nline",
+                                       "ncont", "moving")] + \
+        [(n, _D) for n in ("lambda_", "muz", "wmu", "height", "T", "vel", "vbroad", "chi_c",
+                           "eta_c", "sca_c")] + [("bgline", _I)] + \
+        [(n, _D) for n in ("nstar", "ntotal", "C", "lines", "adamp", "cont", "alpha")] + \
+        [(n, C.c_int) for n in ("ng_delay", "ng_order", "ng_period", "isum", "nmax_iter")] + \
+        [("iter_limit", C.c_double)]
+
+
+def nlte_problem(fx: dict, keep: _Keep) -> NlteProblem:
+    """NlteProblem from an nlte fixture dict (tests/golden/make_golden.py)."""
+    P = NlteProblem()
+    m = fx["meta"]
+    P.nspect, P.ndep, P.nrays, P.nlevel, P.nline, P.ncont = (int(x) for x in m[:6])
+    P.nmax_iter, P.ng_delay, P.ng_order, P.ng_period, P.isum = (int(x) for x in m[6:11])
+    P.moving = int(m[12])
+    P.iter_limit = float(fx["fmeta"][0])
+    P.lambda_ = _p(keep.f64(fx["lambda"]))
+    for k in ("muz", "wmu", "height", "T", "vel", "vbroad", "nstar", "ntotal", "C",
+              "lines", "adamp", "alpha"):
+        setattr(P, k, _p(keep.f64(fx[k])))
+    P.cont = _p(keep.f64(fx["continua"]))
+    bg = keep.f64(fx["background"])
+    P.chi_c = _p(keep.f64(bg[0]))
+    P.eta_c = _p(keep.f64(bg[1]))
+    P.sca_c = _p(keep.f64(bg[2]))
+    fl = np.ascontiguousarray(fx["bgflags"] & 1, dtype=np.int32)
+    keep.arrays.append(fl)
+    P.bgline = fl.ctypes.data_as(_I)
+    return P
+
+
+def nlte_J0(fx: dict) -> np.ndarray:
+    """Mean intensity before the first iteration (zero when N_MAX_SCATTER = 0,
+    which the fixtures use)."""
+    if "J0" in fx:
+        return fx["J0"]
+    return np.zeros((len(fx["lambda"]), len(fx["T"])))
+
+
+def _nlte_lib():
+    L = lib()
+    L.oracle_voigt_armstrong.restype = C.c_double
+    L.oracle_voigt_armstrong.argtypes = [C.c_double, C.c_double]
+    L.oracle_nlte_iterate.restype = C.c_int
+    L.oracle_stat_equil.restype = C.c_int
+    return L
+
+
+def voigt_armstrong(a, v):
+    return _nlte_lib().oracle_voigt_armstrong(a, v)
+
+
+def nlte_profiles(fx: dict, nrays=None, muz=None, wmu=None):
+    """phi per line ([Nlambda, 2*nrays, ndep]) and wphi [nline, ndep]."""
+    keep = _Keep()
+    P = nlte_problem(fx, keep)
+    muz = keep.f64(fx["muz"] if muz is None else muz)
+    wmu = keep.f64(fx["wmu"] if wmu is None else wmu)
+    nrays = len(muz)
+    phis = [np.zeros((int(l[8]), 2 * nrays, P.ndep)) for l in fx["lines"]]
+    arr = (_D * max(len(phis), 1))(*[_p(x) for x in phis])
+    wphi = np.zeros((P.nline, P.ndep))
+    _nlte_lib().oracle_nlte_profiles(C.byref(P), nrays, _p(muz), _p(wmu), arr, _p(wphi))
+    return phis, wphi
+
+
+def nlte_first_iteration(fx: dict):
+    """Gamma and J after one formal pass with the starting populations and
+    J, and the populations after one statEquil (no acceleration)."""
+    keep = _Keep()
+    P = nlte_problem(fx, keep)
+    phis, wphi = nlte_profiles(fx)
+    arr = (_D * max(len(phis), 1))(*[_p(x) for x in phis])
+    n = np.array(fx["n0"], dtype=np.float64)
+    J0 = keep.f64(nlte_J0(fx))
+    J = np.zeros_like(J0)
+    G = np.zeros((P.nlevel * P.nlevel, P.ndep))
+    L = _nlte_lib()
+    L.oracle_nlte_spectrum(C.byref(P), _p(n), _p(J0), _p(J), _p(G), arr, _p(wphi))
+    n1 = n.copy()
+    L.oracle_stat_equil(C.byref(P), _p(G), _p(n1))
+    return G, J, n1
+
+
+def nlte_solve(fx: dict):
+    """Converged populations, final J, iteration count and dpops history."""
+    keep = _Keep()
+    P = nlte_problem(fx, keep)
+    n = np.array(fx["n0"], dtype=np.float64)
+    J = np.array(nlte_J0(fx), dtype=np.float64)
+    dp = np.zeros(P.nmax_iter)
+    acc = np.zeros(P.nmax_iter, dtype=np.int32)
+    it = _nlte_lib().oracle_nlte_iterate(C.byref(P), _p(n), _p(J), _p(dp),
+                                         acc.ctypes.data_as(_I))
+    return n, J, it, dp[:it], acc[:it]
+
+
+def nlte_emergent(fx: dict, n, J, mu_out=None):
+    keep = _Keep()
+    P = nlte_problem(fx, keep)
+    n = keep.f64(n)
+    J = keep.f64(J)
+    out = np.zeros(P.nspect)
+    mu = float(fx["fmeta"][2] if mu_out is None else mu_out)
+    _nlte_lib().oracle_nlte_emergent(C.byref(P), C.c_double(mu), _p(n), _p(J), _p(out))
+    return out

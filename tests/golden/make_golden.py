@@ -18,6 +18,9 @@ Fixtures (npz, float64):
                   outside every line window, duplicate and unsorted lambda
   lte_b0          B = 0 (polarizable lines with no splitting)
   lte_batch       6 atmospheres of the batched generator (2 x 112 lambda)
+  nlte_c1         six-level Ca II-like atom ACTIVE, 82 depths, 5 rays
+  nlte_c4_50/120  the same atom on perturbed 50- and 120-depth atmospheres
+                  with velocity fields and other wavelength counts
 
 stokes_ref comes from the reference as setup.py builds it on x86 (-DSIMDON,
 SSE reciprocal-estimate 4x4 inverse); stokes_ref_portable from the same
@@ -153,8 +156,57 @@ def make_lte_batch(ref, wd, n=6, seed=2024):
     print(f"lte_batch: {n} atmospheres, {os.path.getsize(path) / 1e3:.0f} kB")
 
 
+NLTE_ATOM = "CaII_synth.atom"
+
+
+def nlte_case(name, ndep=82, nlambda_scale=1.0, atom_seed=11, dT=None, vlos=0.0,
+              mu_out=1.0, nrays=5):
+    """NLTE MALI with the six-level Ca II-like atom ACTIVE: the reference's
+    set-up state, one hand-made iteration (Gamma, J, statEquil), and the
+    converged populations and emergent intensity (N_MAX_SCATTER = 0, Ng
+    order 2 / delay 5 / period 5, ITER_LIMIT 1e-4, I_SUM = -1)."""
+    root = rr.make_pyrh_root(NLTE_ATOM, wl.caii_like_atom(atom_seed, nlambda_scale))
+    ref = rr.Reference(pyrh_path=root)
+    wd = rr.scratch_dir()
+    rr.write_inputs(wd, None, atoms=list(rr.PASSIVE_ATOMS) + [NLTE_ATOM], active=NLTE_ATOM,
+                    nrays=nrays, nmax_iter=200, iter_limit="1.0E-4", ng_order=2, ng_delay=5,
+                    ng_period=5, stokes_mode="NO_STOKES", nmax_scatter=0)
+    lt = wl.logtau_grid(ndep)
+    T = wl.base_temperature(lt) + (0.0 if dT is None else dT)
+    ne, nH = ref.hse(wd, lt, T)
+    atm = wl.atmosphere_rows(lt, T, ne / 1e6, nH / 1e6, vlos=vlos, B=0.0)
+    wave = np.array([393.4])
+    ref.nlte(wd, mu_out, atm, wave, os.path.join(wd, "d0"), 0)
+    ref.nlte(wd, mu_out, atm, wave, os.path.join(wd, "d1"), 1)
+    d = rr.read_nlte_dump(os.path.join(wd, "d0"))
+    d1 = rr.read_nlte_dump(os.path.join(wd, "d1"))
+    nl = len(d["g"])
+    out = {k: v for k, v in d.items() if k not in ("J0",)}
+    assert not np.any(d["J0"]), "N_MAX_SCATTER = 0 leaves J = 0 before the first iteration"
+    out.update(atm=atm, wave=wave, atom_text=np.array(wl.caii_like_atom(atom_seed, nlambda_scale)),
+               n_final=d1["n_final"].reshape(nl, -1), J_final=d1["J_final"].reshape(d["J1"].shape),
+               lam_out=d1["lam_out"], I_out=d1["I_out"])
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **out)
+    shutil.rmtree(wd, ignore_errors=True)
+    shutil.rmtree(root, ignore_errors=True)
+    print(f"{name}: {len(d['lambda'])} lambda, {ndep} depths, "
+          f"{os.path.getsize(path) / 1e3:.0f} kB")
+
+
+def make_nlte(ref, wd):
+    nlte_case("nlte_c1", ndep=82)
+    lt50 = wl.logtau_grid(50)
+    pert = wl.perturbations(2, 99, lt50)
+    nlte_case("nlte_c4_50", ndep=50, nlambda_scale=0.8, dT=pert["dT"][0], vlos=1.5,
+              mu_out=0.7)
+    lt120 = wl.logtau_grid(120)
+    pert = wl.perturbations(2, 98, lt120)
+    nlte_case("nlte_c4_120", ndep=120, nlambda_scale=1.25, dT=pert["dT"][1], vlos=-2.0)
+
+
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
-          "lte_b0": make_lte_b0, "lte_batch": make_lte_batch}
+          "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "nlte": make_nlte}
 
 
 def main():

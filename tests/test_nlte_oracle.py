@@ -1,0 +1,52 @@
+"""The NLTE CPU oracle (oracle/nlte_oracle.c) against the compiled
+reference's golden vectors: profiles, the rate matrix after one formal pass,
+one statistical-equilibrium solve, the converged populations at the same
+convergence criterion, and the emergent intensity."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+CASES = ["nlte_c1", "nlte_c4_50", "nlte_c4_120"]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_profiles(golden, name):
+    fx = golden(name)
+    phis, wphi = O.nlte_profiles(fx)
+    assert np.abs(wphi / fx["wphi"] - 1).max() < 1e-12
+    for kr, ph in enumerate(phis):
+        for s, la in enumerate(fx["phi_sample_la"][kr]):
+            ref = fx["phi_sample"][kr, s]
+            assert np.abs(ph[la] - ref).max() <= 1e-10 * np.abs(ref).max()   # GH nodes: 10 vs 17 digits
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_first_iteration(golden, name):
+    fx = golden(name)
+    G, J, n1 = O.nlte_first_iteration(fx)
+    g = fx["Gamma1"]
+    assert np.abs(G - g).max() <= 1e-12 * np.abs(g).max()
+    assert np.abs(J - fx["J1"]).max() <= 1e-10 * np.abs(fx["J1"]).max()
+    assert np.abs(n1 / fx["n1"] - 1).max() < 1e-7
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_converged_populations_and_emergent(golden, name):
+    fx = golden(name)
+    n, J, it, dp, acc = O.nlte_solve(fx)
+    assert dp[-1] < fx["fmeta"][0] <= dp[-2]
+    assert acc.sum() >= 1                       # Ng acceleration was exercised
+    assert np.abs(n / fx["n_final"] - 1).max() < 1e-6
+    Iem = O.nlte_emergent(fx, n, J)
+    m = O.output_mask(fx["lambda"], fx["fmeta"][1])
+    assert np.array_equal(fx["lambda"][m], fx["lam_out"])
+    assert np.abs(Iem[m] / fx["I_out"] - 1).max() < 1e-6
+
+
+def test_armstrong_voigt_limits():
+    # H(0, v) = exp(-v^2); Lorentz wings H ~ a / (sqrt(pi) v^2)
+    for v in (0.0, 0.5, 1.7, 3.9):
+        assert abs(O.voigt_armstrong(0.0, v) - np.exp(-v * v)) < 1e-12
+    a, v = 0.01, 40.0
+    assert abs(O.voigt_armstrong(a, v) / (a / (np.sqrt(np.pi) * v * v)) - 1) < 1e-3
