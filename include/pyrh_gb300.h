@@ -146,7 +146,97 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch *host_batch,
                                  const pyrh_line *host_lines, int32_t nline,
                                  const pyrh_lte_config *cfg, void *host_stokes_out);
 
-/* Number of kernel launches the last pyrh_lte_stokes call issued. */
+/* ------------------------------------------------------------------ NLTE
+ * MALI lambda iteration for one active atom per atmosphere, replacing the
+ * reference's Iterate() (rh/iterate.c:48-143) with its solveSpectrum() /
+ * Formal() passes (profiles, rh/profile.c:67-371; opacity, rh/opacity.c:
+ * 64-300; Gamma and cross-coupling, rh/fillgamma.c:82-332), statEquil()
+ * (rh/statequil.c:40-102, LU of rh/ludcmp.c:36-177), Ng acceleration
+ * (rh/accelerate.c:34-146) and MaxChange() (rh/maxchange.c:32-50), and the
+ * emergent intensity of _solveray() (rh/rhf1d/pyrh_solveray.c:82-150).
+ * The caller supplies the state that the reference's set-up leaves behind
+ * (LTE populations, collision matrix, background, damping, cross-sections).
+ */
+#define PYRH_NLTE_MAX_LEVELS  8
+#define PYRH_NLTE_MAX_ACTIVE  16   /* transitions active at one wavelength */
+#define PYRH_NLTE_MAX_RAYS    8
+#define PYRH_NLTE_MAX_DEPTH   160
+#define PYRH_NLTE_MAX_NG      4
+
+/* One radiative transition of the active atom of one atmosphere. */
+typedef struct {
+  int32_t type;          /* 0 = bound-bound line, 1 = bound-free continuum */
+  int32_t i, j;          /* lower and upper level */
+  int32_t nblue;         /* first spectrum index (rh/sortlambda.c:296-355) */
+  int32_t nlambda;       /* number of spectrum points covered */
+  int32_t symmetric;     /* line->symmetric (getlambda.c:194) */
+  int32_t voigt;         /* line->Voigt (damping used) */
+  int32_t line_index;    /* row of adamp for lines */
+  int64_t phi_off;       /* line profile block offset in the workspace */
+  int64_t alpha_off;     /* continua: first cross-section in alpha[] */
+  double lambda0, Aji, Bji, Bij, isotope_frac, c_shift, c_fraction;
+} pyrh_nlte_transition;
+
+/* A batch of atmospheres, each with the same number of atomic levels and
+   its own depth grid, spectrum and transition table.  Arrays indexed by
+   depth use depth_off[p] + k; spectral arrays lam_off[p] + la; per
+   (lambda, depth) arrays cont_off[p] + k*nspect[p] + la (lambda fastest);
+   per (level, depth) arrays (i*total_depth + depth_off[p] + k); the rate
+   matrix C ((i*nlevel + j)*total_depth + depth_off[p] + k). */
+typedef struct {
+  int32_t natm, nlevel, max_ndep, max_nspect, max_nline;
+  int64_t total_depth, total_lambda, total_cont;
+  const int32_t *ndep, *nspect, *ntrans;          /* [natm] */
+  const int64_t *depth_off, *lam_off, *cont_off, *trans_off, *adamp_off;  /* [natm] */
+  const double *lambda;                           /* [total_lambda] nm */
+  const double *height, *T, *vel, *vbroad, *ntotal;   /* [total_depth] SI */
+  const double *nstar;                            /* [nlevel][total_depth] */
+  const double *C;                                /* [nlevel^2][total_depth] */
+  const double *chi_c, *eta_c, *sca_c;            /* [total_cont] */
+  const int32_t *bgline;                          /* [total_lambda] */
+  const pyrh_nlte_transition *trans;              /* [sum ntrans] */
+  const double *alpha;                            /* continuum cross-sections */
+  const double *adamp;                            /* [sum nline*ndep] */
+  double *n;        /* [nlevel][total_depth]: start populations, then result */
+  double *J;        /* [total_cont]: start mean intensity, then the last one */
+} pyrh_nlte_batch;
+
+typedef struct {
+  int32_t precision;      /* formal solution: PYRH_FP64 or PYRH_FP32; rates,
+                             LU, Ng and convergence are always FP64 */
+  int32_t nrays;
+  double  muz[PYRH_NLTE_MAX_RAYS], wmu[PYRH_NLTE_MAX_RAYS];
+  int32_t moving;         /* atmos.moving */
+  int32_t isum;           /* I_SUM (-1: eliminate the most populated level) */
+  int32_t ng_order, ng_delay, ng_period;
+  int32_t nmax_iter;
+  double  iter_limit;
+} pyrh_nlte_config;
+
+/* Bytes of device workspace pyrh_nlte_solve / pyrh_nlte_emergent need:
+   the line profiles (phi_elems values: sum over atmospheres and lines of
+   nlambda * 2 * nrays * ndep, addressed by the transitions' phi_off), their
+   normalisation, a second mean-intensity buffer, the rate matrices, the Ng
+   history and per-atmosphere iteration state. */
+size_t pyrh_nlte_workspace_bytes(const pyrh_nlte_batch *batch, const pyrh_nlte_config *cfg,
+                                 int64_t phi_elems);
+
+/* Solves the batch; iterations[p] (device, int32) and dpops[p] (device,
+   double) receive each atmosphere's iteration count and last convergence
+   metric.  Returns PYRH_ERR_NONCONVERGED if an atmosphere reached nmax_iter
+   above iter_limit. */
+pyrh_status pyrh_nlte_solve(const pyrh_nlte_batch *batch, const pyrh_nlte_config *cfg,
+                            void *workspace, size_t workspace_bytes,
+                            int32_t *iterations, double *dpops, void *stream);
+
+/* Emergent intensity at mu_out for every spectrum point with the batch's
+   populations n and mean intensity J (pyrh_solveray.c:82-150); I_out is
+   [total_lambda] (FP64). */
+pyrh_status pyrh_nlte_emergent(const pyrh_nlte_batch *batch, const pyrh_nlte_config *cfg,
+                               double mu_out, void *workspace, size_t workspace_bytes,
+                               double *I_out, void *stream);
+
+/* Number of kernel launches the last pyrh_lte_stokes / pyrh_nlte_* call issued. */
 int32_t pyrh_last_launch_count(void);
 
 /* Library version string and the text of the last error on this thread. */

@@ -179,6 +179,16 @@ HostWs g_ws;
 
 }  // namespace
 
+namespace pyrh {
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+void set_launches(int n) { g_last_launches = n; }
+}  // namespace pyrh
+
 extern "C" {
 
 const char* pyrh_version(void) { return "pyrh_gb300 0.1 (sm_103a)"; }

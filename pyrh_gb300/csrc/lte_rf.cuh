@@ -1,0 +1,844 @@
+// lte_rf.cuh -- response functions of the polarized LTE synthesis.
+//
+// Depth-resolved response functions dS_s(lambda)/dx(k) of the emergent
+// Stokes vector to x = (T, v_los, v_mic, B, gamma, chi) at every depth, and
+// the gradient of a weighted chi^2, for the same path as lte_stokes.cu
+// (DELO-Bezier3 without magneto-optical terms, ray to the observer).
+//
+// Method, per (atmosphere, wavelength):
+//  1. forward sweep of the DELO-Bezier3 recurrence (bezier_1D.c:52-300),
+//     recording the per-depth optical quantities q_k = (chi, S_I..S_V,
+//     K'_Q, K'_U, K'_V) and the per-step state on a thread-private tape;
+//  2. hand-written reverse (adjoint) sweep of that recurrence, giving
+//     dS_s(0)/dq_k for every depth (seeds: the four Stokes outputs, or the
+//     chi^2 weights);
+//  3. q_k depends only on the parameters of depth k, so the local Jacobian
+//     dq_k/dx_k (forward-mode dual numbers through the Zeeman/Voigt opacity
+//     of kurucz.c:729-827 and the line strength of kurucz.c:638-680, with
+//     the exact derivative of each Humlicek region) closes the chain.
+// The continuum (chi_c, eta_c), stage densities and the height scale are
+// inputs of the hot path and are held fixed.  The reference has no
+// analytical response functions for these parameters; its definition is
+// finite differences of the whole synthesis (rf_ray.c:205-293).
+#pragma once
+
+#include "rt_device.cuh"
+
+namespace pyrh {
+
+constexpr int kNX = 6;  // T, v_los, v_mic, B, gamma, chi
+
+// ------------------------------------------------------------- duals -----
+template <typename R>
+struct D6 {
+  R v;
+  R d[kNX];
+};
+
+template <typename R>
+PYRH_HD D6<R> dconst(R v) {
+  D6<R> r;
+  r.v = v;
+  for (int i = 0; i < kNX; ++i) r.d[i] = R(0);
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> dvar(R v, int i) {
+  D6<R> r = dconst(v);
+  r.d[i] = R(1);
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> operator+(const D6<R>& a, const D6<R>& b) {
+  D6<R> r;
+  r.v = a.v + b.v;
+  for (int i = 0; i < kNX; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> operator-(const D6<R>& a, const D6<R>& b) {
+  D6<R> r;
+  r.v = a.v - b.v;
+  for (int i = 0; i < kNX; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> operator*(const D6<R>& a, const D6<R>& b) {
+  D6<R> r;
+  r.v = a.v * b.v;
+  for (int i = 0; i < kNX; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> operator*(R s, const D6<R>& a) {
+  D6<R> r;
+  r.v = s * a.v;
+  for (int i = 0; i < kNX; ++i) r.d[i] = s * a.d[i];
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> operator/(const D6<R>& a, const D6<R>& b) {
+  D6<R> r;
+  const R ib = R(1) / b.v;
+  r.v = a.v * ib;
+  for (int i = 0; i < kNX; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> dsqrt(const D6<R>& a) {
+  D6<R> r;
+  r.v = sqrt(a.v);
+  const R h = R(0.5) / r.v;
+  for (int i = 0; i < kNX; ++i) r.d[i] = h * a.d[i];
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> dexp(const D6<R>& a) {
+  D6<R> r;
+  r.v = exp(a.v);
+  for (int i = 0; i < kNX; ++i) r.d[i] = r.v * a.d[i];
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> dpow(const D6<R>& a, R p) {
+  D6<R> r;
+  r.v = pow(a.v, p);
+  const R f = p * r.v / a.v;
+  for (int i = 0; i < kNX; ++i) r.d[i] = f * a.d[i];
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> dcos(const D6<R>& a) {
+  D6<R> r;
+  r.v = cos(a.v);
+  const R f = -sin(a.v);
+  for (int i = 0; i < kNX; ++i) r.d[i] = f * a.d[i];
+  return r;
+}
+template <typename R>
+PYRH_HD D6<R> dsin(const D6<R>& a) {
+  D6<R> r;
+  r.v = sin(a.v);
+  const R f = cos(a.v);
+  for (int i = 0; i < kNX; ++i) r.d[i] = f * a.d[i];
+  return r;
+}
+
+// ---------------------------------------------- Humlicek with derivative --
+// W(t) and dW/dt for t = a - i v, differentiating each region's rational
+// approximation exactly (so the derivative is that of the forward model).
+template <typename R>
+PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
+  const Cx<R> t = {a, -v};
+  const R s = fabs(v) + a;
+  if (s >= R(15.0)) {
+    // W = c t / (t^2 + 1/2);  W' = c (1/2 - t^2) / (t^2 + 1/2)^2
+    const R c0 = R(0.5641896);
+    Cx<R> t2 = cmul(t, t);
+    Cx<R> den = {t2.r + R(0.5), t2.i};
+    W = cdiv(Cx<R>{c0 * t.r, c0 * t.i}, den);
+    dW = cdiv(Cx<R>{c0 * (R(0.5) - t2.r), -c0 * t2.i}, cmul(den, den));
+  } else if (s >= R(5.5)) {
+    // W = t (c1 u + c2) / (u (u + 3) + 3/4), u = t^2
+    const R c1 = R(0.5641896), c2 = R(1.410474);
+    Cx<R> u = cmul(t, t);
+    Cx<R> g = {c1 * u.r + c2, c1 * u.i};
+    Cx<R> N = cmul(t, g);
+    Cx<R> dN = {g.r + R(2) * c1 * u.r, g.i + R(2) * c1 * u.i};  // g + t * c1 * 2t
+    Cx<R> D = cmul(u, Cx<R>{u.r + R(3), u.i});
+    D.r += R(0.75);
+    Cx<R> dD = cmul(Cx<R>{R(2) * u.r + R(3), R(2) * u.i}, Cx<R>{R(2) * t.r, R(2) * t.i});
+    W = cdiv(N, D);
+    Cx<R> num = cmul(dN, D), nd = cmul(N, dD);
+    dW = cdiv(Cx<R>{num.r - nd.r, num.i - nd.i}, cmul(D, D));
+  } else if (a >= R(0.195) * fabs(v) - R(0.176)) {
+    const R A[5] = {R(0.5642236), R(3.778987), R(11.96482), R(20.20933), R(16.4955)};
+    const R B[5] = {R(6.699398), R(21.69274), R(39.27121), R(38.82363), R(16.4955)};
+    Cx<R> P = {A[0], R(0)}, dP = {R(0), R(0)};
+    Cx<R> Q = {t.r + B[0], t.i}, dQ = {R(1), R(0)};
+    for (int n = 1; n < 5; ++n) {
+      dP = cmul(dP, t); dP.r += P.r; dP.i += P.i;
+      P = cmul(P, t); P.r += A[n];
+      dQ = cmul(dQ, t); dQ.r += Q.r; dQ.i += Q.i;
+      Q = cmul(Q, t); Q.r += B[n];
+    }
+    W = cdiv(P, Q);
+    Cx<R> x1 = cmul(dP, Q), x2 = cmul(P, dQ);
+    dW = cdiv(Cx<R>{x1.r - x2.r, x1.i - x2.i}, cmul(Q, Q));
+  } else {
+    // W = exp(t^2) - t P(u) / Q(u), u = -t^2
+    const R A[7] = {R(0.56419), R(1.320522), R(35.7668), R(219.031), R(1540.787), R(3321.99), R(36183.31)};
+    const R B[7] = {R(1.841439), R(61.57037), R(364.2191), R(2186.181), R(9022.228), R(24322.84), R(32066.6)};
+    Cx<R> u = {-(t.r * t.r - t.i * t.i), -(R(2) * t.r * t.i)};
+    Cx<R> P = {A[0], R(0)}, dP = {R(0), R(0)};           // derivatives w.r.t. u
+    Cx<R> Q = {u.r + B[0], u.i}, dQ = {R(1), R(0)};
+    for (int n = 1; n < 7; ++n) {
+      dP = cmul(dP, u); dP.r += P.r; dP.i += P.i;
+      P = cmul(u, P); P.r += A[n];
+      dQ = cmul(dQ, u); dQ.r += Q.r; dQ.i += Q.i;
+      Q = cmul(u, Q); Q.r += B[n];
+    }
+    R e = dev_exp(-u.r), sn, cs;
+    dev_sincos(-u.i, &sn, &cs);
+    Cx<R> E = {e * cs, e * sn};                             // exp(t^2)
+    Cx<R> r = cdiv(P, Q);
+    Cx<R> tr = cmul(t, r);
+    W = {E.r - tr.r, E.i - tr.i};
+    // d/dt [t P/Q] = P/Q + t (P'Q - PQ')/Q^2 * du/dt,  du/dt = -2t
+    Cx<R> x1 = cmul(dP, Q), x2 = cmul(P, dQ);
+    Cx<R> dr = cdiv(Cx<R>{x1.r - x2.r, x1.i - x2.i}, cmul(Q, Q));
+    Cx<R> tdr = cmul(cmul(t, dr), Cx<R>{R(-2) * t.r, R(-2) * t.i});
+    Cx<R> dE = cmul(E, Cx<R>{R(2) * t.r, R(2) * t.i});
+    dW = {dE.r - r.r - tdr.r, dE.i - r.i - tdr.i};
+  }
+}
+
+// ------------------------------------------- per-(line, depth) quantities --
+// Value and derivatives w.r.t. (T, v_los, v_mic, B, gamma, chi) of the
+// line quantities of one depth (kurucz.c:638-680, 745-783).
+template <typename R>
+struct LineDepth {
+  D6<R> inv_vb, vshift, adamp, vB, chil, etal;
+  bool gauss;  // Grad == 0
+};
+
+struct LineConstD {
+  double lambda0, Ei, gi, Aji, Bji, Bij, Grad, GStark, GvdWaals, cross, alpha, isotope_frac,
+      hyperfine_frac, weight;
+  int vdwaals;
+};
+
+template <typename R>
+PYRH_HD LineDepth<R> line_depth(const LineConstD& L, R T, R vel, R vturb, R B, R ne, R nHtot,
+                                R np, R nstage, R lnU, R muz, bool moving) {
+  LineDepth<R> o;
+  const D6<R> dT = dvar(T, 0), dv = dvar(vel, 1), dvt = dvar(vturb, 2), dB = dvar(B, 3);
+  const R vtherm = R(2.0 * kKBOLTZMANN / (kAMU * L.weight));
+  const D6<R> vb = dsqrt(vtherm * dT + dvt * dvt);
+  const D6<R> one = dconst(R(1));
+  o.inv_vb = R(kCLIGHT / L.lambda0) * (one / vb);
+  o.vshift = moving ? muz * (dv / vb) : dconst(R(0));
+  const D6<R> sv = R(1.0 / kSQRTPI) * (one / vb);
+  o.gauss = (L.Grad == 0.0);
+  if (!o.gauss) {
+    D6<R> GvdW;
+    if (L.vdwaals == 0) GvdW = R(L.cross) * dpow(dT, R(0.3));
+    else if (L.vdwaals == 2) GvdW = R(L.cross) * dpow(dT, R((1.0 - L.alpha) / 2.0));
+    else GvdW = dconst(R(L.GvdWaals));
+    const D6<R> G = dconst(R(L.Grad + L.GStark * ne)) + (nHtot - np) * GvdW;
+    o.adamp = R(L.lambda0 * kNM_TO_M / (4.0 * kPI)) * (G / vb);
+  } else {
+    o.adamp = dconst(R(-1));
+  }
+  o.vB = R(kLARMOR * L.lambda0) * (dB / vb);
+  const R hc = R(kHPLANCK * kCLIGHT);
+  const R hc_la = R(kHPLANCK * kCLIGHT / (L.lambda0 * kNM_TO_M));
+  const R B4 = R(kHPLANCK * kCLIGHT / (4.0 * kPI) * L.Bij * L.isotope_frac * L.hyperfine_frac * L.gi);
+  const R tw = R(L.Aji / L.Bji);
+  const D6<R> kT = one / (R(kKBOLTZMANN) * dT);
+  const D6<R> ni = nstage * dexp(dconst(-lnU) - R(L.Ei) * kT);
+  const D6<R> nj = ni * dexp(dconst(R(0)) - hc_la * kT);
+  o.chil = (B4 * (ni - nj)) * sv;
+  o.etal = ((B4 * tw) * nj) * sv;
+  (void)hc;
+  return o;
+}
+
+// Projected field geometry (project.c:38-79) with derivatives w.r.t. gamma
+// (slot 4) and chi (slot 5): sin^2(g) cos(2c), sin^2(g) sin(2c), cos(g), sin^2(g).
+template <typename R>
+struct GeoD {
+  D6<R> gQ, gU, gV, s2g;
+};
+
+template <typename R>
+PYRH_HD GeoD<R> geometry_d(R gam, R chb, R muz) {
+  const D6<R> g = dvar(gam, 4), c = dvar(chb, 5);
+  D6<R> cg, c2c, s2c;
+  if (muz == R(1)) {
+    cg = dcos(g);
+    c2c = dcos(R(2) * c);
+    s2c = dsin(R(2) * c);
+  } else {
+    const R mux = sqrt(R(1) - muz * muz), csc = R(1) / sqrt(R(1) - muz * muz);
+    const D6<R> sg = dsin(g);
+    const D6<R> bx = sg * dcos(c), by = sg * dsin(c), bz = dcos(g);
+    const D6<R> b3 = mux * bx + muz * bz;
+    const D6<R> b1 = csc * (bz - muz * b3);
+    const D6<R> b2 = (-csc * mux) * by;
+    const D6<R> den = dconst(R(1)) - b3 * b3;
+    cg = b3;
+    c2c = (b1 * b1 - b2 * b2) / den;
+    s2c = (R(2) * (b1 * b2)) / den;
+  }
+  GeoD<R> o;
+  o.s2g = dconst(R(1)) - cg * cg;
+  o.gQ = o.s2g * c2c;
+  o.gU = o.s2g * s2c;
+  o.gV = cg;
+  return o;
+}
+
+// Local optical quantities q = (chi, S0..S3, k1..k3) and their Jacobian
+// dq/dx at one depth for one wavelength (kurucz.c:669-715, formal.c:178-208,
+// stokesopac.c:47-79), MAGNETO_OPTICAL off.  comp_* are the Zeeman tables
+// of each line (q index 0..2 for Ml - Mu = -1, 0, +1).
+template <typename R>
+PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, const GeoD<R>& geo, const R* dlam,
+                         unsigned inwin, const int* ncomp, const R* cshift, const R* cweight,
+                         const int* cq, int maxcomp, R chi_c, R eta_c, R q[8], R J[8][kNX]) {
+  D6<R> cI = dconst(R(0)), cQ = cI, cU = cI, cV = cI, eI = cI, eQ = cI, eU = cI, eV = cI;
+  for (int l = 0; l < nline; ++l) {
+    if (!((inwin >> l) & 1u)) continue;
+    const LineDepth<R>& L = ld[l];
+    const D6<R> v = dlam[l] * L.inv_vb + L.vshift;
+    if (L.gauss) {
+      const D6<R> phi = (fabs(v.v) <= R(kMAX_GAUSS_DOPPLER)) ? dexp(dconst(R(0)) - v * v) : dconst(R(0));
+      cI = cI + L.chil * phi;
+      eI = eI + L.etal * phi;
+      continue;
+    }
+    D6<R> ph[3] = {dconst(R(0)), dconst(R(0)), dconst(R(0))};
+    for (int c = 0; c < ncomp[l]; ++c) {
+      const R sh = cshift[l * maxcomp + c], w = cweight[l * maxcomp + c];
+      Cx<R> W, dW;
+      const R vv = v.v - sh * L.vB.v;
+      humlicek_d<R>(L.adamp.v, vv, W, dW);
+      // t = a - i (v - sh vB): dt = da - i (dv - sh dvB); dH = Re(W' dt)
+      D6<R> H;
+      H.v = W.r;
+      for (int i = 0; i < kNX; ++i) {
+        const R dre = L.adamp.d[i], dim = -(v.d[i] - sh * L.vB.d[i]);
+        H.d[i] = dW.r * dre - dW.i * dim;
+      }
+      const int qi = cq[l * maxcomp + c] + 1;
+      ph[qi < 0 ? 0 : (qi > 2 ? 2 : qi)] = ph[qi < 0 ? 0 : (qi > 2 ? 2 : qi)] + w * H;
+    }
+    const D6<R> sig = ph[2] + ph[0];
+    const D6<R> del = R(0.5) * ph[1] - R(0.25) * sig;
+    const D6<R> phiI = del * geo.s2g + R(0.5) * sig;
+    const D6<R> phiQ = del * geo.gQ, phiU = del * geo.gU, phiV = R(0.5) * ((ph[2] - ph[0]) * geo.gV);
+    cI = cI + L.chil * phiI; eI = eI + L.etal * phiI;
+    cQ = cQ + L.chil * phiQ; eQ = eQ + L.etal * phiQ;
+    cU = cU + L.chil * phiU; eU = eU + L.etal * phiU;
+    cV = cV + L.chil * phiV; eV = eV + L.etal * phiV;
+  }
+  const D6<R> chi = dconst(chi_c) + cI;
+  const D6<R> out[8] = {chi,
+                        (dconst(eta_c) + eI) / chi, eQ / chi, eU / chi, eV / chi,
+                        cQ / chi, cU / chi, cV / chi};
+  for (int n = 0; n < 8; ++n) {
+    q[n] = out[n].v;
+    for (int i = 0; i < kNX; ++i) J[n][i] = out[n].d[i];
+  }
+}
+
+// ------------------------------------------------- coefficient derivatives --
+template <typename R>
+PYRH_HD void bezier3_coeffs_d(R dt, R c[5], R dc[5]) {
+  // c = (alpha, beta, gamma, theta, eps), dc = d/d(dt)
+  bezier3_coeffs(dt, c[0], c[1], c[2], c[3], c[4]);
+  const R thr = sizeof(R) == 8 ? R(5.e-2) : R(1.5);
+  if (dt >= thr) {
+    const R e = c[4], t = dt, t3 = t * t * t;
+    dc[0] = (R(6) - R(6) * t + R(3) * t * t - R(6) * e) / t3 - R(3) * c[0] / t;
+    dc[1] = e - R(3) * c[1] / t;
+    dc[2] = R(3) * (R(-4) + R(2) * t + (R(4) + R(2) * t) * e) / t3 - R(3) * c[2] / t;
+    dc[3] = R(3) * (e * (R(-2) - R(2) * t - t * t) + R(2)) / t3 - R(3) * c[3] / t;
+    dc[4] = -e;
+  } else if (sizeof(R) == 8) {
+    const R t = dt, t2 = t * t, t3 = t2 * t;
+    dc[4] = R(-1) + t - R(0.5) * t2 + t3 / R(6);
+    dc[0] = R(0.25) - R(0.1) * t + t2 / R(40) - t3 / R(210);
+    dc[1] = R(0.25) - R(0.4) * t + t2 / R(4) - R(2) * t3 / R(21);
+    dc[2] = R(0.25) - R(0.2) * t + R(0.075) * t2 - R(4) * t3 / R(210);
+    dc[3] = R(0.25) - R(0.3) * t + R(0.15) * t2 - t3 / R(21);
+  } else {
+    // derivative of the 11-term series of the single-precision form
+    const R ca[11] = {R(0.25), R(-0.05), R(8.333333333e-3), R(-1.190476190e-3), R(1.488095238e-4),
+                      R(-1.653439153e-5), R(1.653439153e-6), R(-1.503126503e-7),
+                      R(1.252605419e-8), R(-9.635426302e-10), R(6.882447359e-11)};
+    const R cb[11] = {R(0.25), R(-0.2), R(8.333333333e-2), R(-2.380952381e-2), R(5.208333333e-3),
+                      R(-9.259259259e-4), R(1.388888889e-4), R(-1.803751804e-5),
+                      R(2.066798942e-6), R(-2.119793786e-7), R(1.968379945e-8)};
+    const R cg[11] = {R(0.25), R(-0.1), R(0.025), R(-4.761904762e-3), R(7.440476190e-4),
+                      R(-9.920634921e-5), R(1.157407407e-5), R(-1.202501203e-6),
+                      R(1.127344877e-7), R(-9.635426302e-9), R(7.570692095e-10)};
+    const R ct[11] = {R(0.25), R(-0.15), R(0.05), R(-1.190476190e-2), R(2.232142857e-3),
+                      R(-3.472222222e-4), R(4.629629630e-5), R(-5.411255411e-6),
+                      R(5.636724387e-7), R(-5.299484466e-8), R(4.542415257e-9)};
+    const R* cs[4] = {ca, cb, cg, ct};
+    for (int m = 0; m < 4; ++m) {
+      R s = R(11) * cs[m][10];
+      for (int i = 9; i >= 0; --i) s = s * dt + R(i + 1) * cs[m][i];
+      dc[m] = s;
+    }
+    dc[4] = -c[4];
+  }
+}
+
+// --------------------------------------------------------- cent_deriv VJP --
+// w = cent_deriv(dsup, dsdn, a, b, c); accumulates adjoints of all five args.
+template <typename R>
+PYRH_HD void cent_deriv_vjp(R dsup, R dsdn, R a, R b, R c, R wbar, R& dsupb, R& dsdnb, R& ab,
+                            R& bb, R& cb) {
+  const R fim1 = (b - a) / dsup, fi = (c - b) / dsdn;
+  if (!(fim1 * fi > R(0)) || wbar == R(0)) return;
+  const R s = dsdn + dsup;
+  const R al = R(0.333333333333333333333333) * (R(1) + dsdn / s);
+  const R D = (R(1) - al) * fim1 + al * fi, N = fim1 * fi;
+  const R Nb = wbar / D, Db = -wbar * N / (D * D);
+  const R f1b = Nb * fi + Db * (R(1) - al);
+  const R f2b = Nb * fim1 + Db * al;
+  const R alb = Db * (fi - fim1);
+  dsdnb += alb * R(0.333333333333333333333333) * dsup / (s * s);
+  dsupb -= alb * R(0.333333333333333333333333) * dsdn / (s * s);
+  ab -= f1b / dsup;
+  bb += f1b / dsup - f2b / dsdn;
+  cb += f2b / dsdn;
+  dsupb -= f1b * fim1 / dsup;
+  dsdnb -= f2b * fi / dsdn;
+}
+
+// ----------------------------------------------------------- DELO step ---
+// Structured DELO-Bezier3 step without magneto-optical terms (see
+// delo_step in lte_stokes.cu).  k vectors hold (K'_Q, K'_U, K'_V).
+template <typename R>
+struct StepIn {
+  R al, be, ga, th, ep, dt03;
+  R ku[3], k0[3], dku[3], dk0[3];
+  R Su[4], S0[4], dSu[4], dS0[4];
+  R Iu[4];
+};
+
+template <typename R>
+PYRH_HD void md_solve(R c, const R b[3], const R k0[3], const R V[4], R x[4]) {
+  const R sig = R(1) + c * (k0[0] * k0[0] + k0[1] * k0[1] + k0[2] * k0[2]);
+  const R f = c / sig;
+  const R kb = k0[0] * b[0] + k0[1] * b[1] + k0[2] * b[2];
+  const R kv = k0[0] * V[1] + k0[1] * V[2] + k0[2] * V[3];
+  R w[3], z[3];
+  for (int j = 0; j < 3; ++j) {
+    w[j] = b[j] - f * kb * k0[j];
+    z[j] = V[j + 1] - f * kv * k0[j];
+  }
+  const R x0 = (V[0] - (b[0] * z[0] + b[1] * z[1] + b[2] * z[2])) /
+               (sig - (b[0] * w[0] + b[1] * w[1] + b[2] * w[2]));
+  x[0] = x0;
+  for (int j = 0; j < 3; ++j) x[j + 1] = z[j] - x0 * w[j];
+}
+
+template <typename R>
+PYRH_HD void step_fwd(const StepIn<R>& s, R x[4], R V[4], R b[3], R& c) {
+  c = s.ga * s.dt03;
+  const R pK = s.al + s.ga * (R(1) + s.dt03);
+  const R ca = s.th * s.dt03, pa = -s.be - s.th + s.th * s.dt03;
+  const R bt = s.be + s.th, ag = s.al + s.ga, tdt = s.th * s.dt03, gdt = s.ga * s.dt03;
+  const R kuIv = s.ku[0] * s.Iu[1] + s.ku[1] * s.Iu[2] + s.ku[2] * s.Iu[3];
+  const R ku2 = s.ku[0] * s.ku[0] + s.ku[1] * s.ku[1] + s.ku[2] * s.ku[2];
+  R h[3];
+  for (int j = 0; j < 3; ++j) h[j] = pa * s.ku[j] + ca * s.dku[j];
+  V[0] = (s.ep + ca * ku2) * s.Iu[0] + h[0] * s.Iu[1] + h[1] * s.Iu[2] + h[2] * s.Iu[3] +
+         bt * s.Su[0] - tdt * (s.ku[0] * s.Su[1] + s.ku[1] * s.Su[2] + s.ku[2] * s.Su[3]) +
+         ag * s.S0[0] + gdt * (s.k0[0] * s.S0[1] + s.k0[1] * s.S0[2] + s.k0[2] * s.S0[3]) +
+         s.dt03 * (s.ga * s.dS0[0] - s.th * s.dSu[0]);
+  for (int j = 0; j < 3; ++j)
+    V[j + 1] = h[j] * s.Iu[0] + s.ep * s.Iu[j + 1] + ca * s.ku[j] * kuIv - tdt * s.ku[j] * s.Su[0] +
+               bt * s.Su[j + 1] + gdt * s.k0[j] * s.S0[0] + ag * s.S0[j + 1] +
+               s.dt03 * (s.ga * s.dS0[j + 1] - s.th * s.dSu[j + 1]);
+  for (int j = 0; j < 3; ++j) b[j] = pK * s.k0[j] + c * s.dk0[j];
+  md_solve(c, b, s.k0, V, x);
+}
+
+// Reverse of step_fwd: given xb = dL/dx, accumulate into sb (same layout).
+template <typename R>
+PYRH_HD void step_vjp(const StepIn<R>& s, const R xb[4], StepIn<R>& sb) {
+  R x[4], V[4], b[3], c;
+  step_fwd(s, x, V, b, c);
+  const R pK = s.al + s.ga * (R(1) + s.dt03);
+  const R ca = s.th * s.dt03, pa = -s.be - s.th + s.th * s.dt03;
+  const R bt = s.be + s.th, ag = s.al + s.ga, tdt = s.th * s.dt03, gdt = s.ga * s.dt03;
+  // Md is symmetric: Vb = Md^-1 xb
+  R Vb[4];
+  md_solve(c, b, s.k0, xb, Vb);
+  // Md entries: Md00 = 1 + c|k0|^2, Md0j = Mdj0 = b_j, Mdij = d_ij + c k0_i k0_j
+  const R xk = x[1] * s.k0[0] + x[2] * s.k0[1] + x[3] * s.k0[2];
+  const R vk = Vb[1] * s.k0[0] + Vb[2] * s.k0[1] + Vb[3] * s.k0[2];
+  const R k02 = s.k0[0] * s.k0[0] + s.k0[1] * s.k0[1] + s.k0[2] * s.k0[2];
+  const R sigb = -Vb[0] * x[0];
+  R cb = -vk * xk + sigb * k02, bb[3], k0b[3];
+  for (int j = 0; j < 3; ++j) {
+    bb[j] = -(Vb[0] * x[j + 1] + Vb[j + 1] * x[0]);
+    k0b[j] = -c * (Vb[j + 1] * xk + vk * x[j + 1]) + sigb * R(2) * c * s.k0[j];
+  }
+  R pKb = 0, cab = 0, pab = 0, btb = 0, agb = 0, tdtb = 0, gdtb = 0;
+  for (int j = 0; j < 3; ++j) {
+    pKb += bb[j] * s.k0[j];
+    k0b[j] += pK * bb[j];
+    cb += bb[j] * s.dk0[j];
+    sb.dk0[j] += c * bb[j];
+  }
+  // V0
+  const R ku2 = s.ku[0] * s.ku[0] + s.ku[1] * s.ku[1] + s.ku[2] * s.ku[2];
+  const R kuIv = s.ku[0] * s.Iu[1] + s.ku[1] * s.Iu[2] + s.ku[2] * s.Iu[3];
+  const R kuSv = s.ku[0] * s.Su[1] + s.ku[1] * s.Su[2] + s.ku[2] * s.Su[3];
+  const R k0S0v = s.k0[0] * s.S0[1] + s.k0[1] * s.S0[2] + s.k0[2] * s.S0[3];
+  R hb[3] = {0, 0, 0}, h[3];
+  for (int j = 0; j < 3; ++j) h[j] = pa * s.ku[j] + ca * s.dku[j];
+  {
+    const R v = Vb[0];
+    sb.ep += v * s.Iu[0];
+    cab += v * ku2 * s.Iu[0];
+    for (int j = 0; j < 3; ++j) sb.ku[j] += v * ca * s.Iu[0] * R(2) * s.ku[j];
+    sb.Iu[0] += v * (s.ep + ca * ku2);
+    for (int j = 0; j < 3; ++j) { hb[j] += v * s.Iu[j + 1]; sb.Iu[j + 1] += v * h[j]; }
+    btb += v * s.Su[0]; sb.Su[0] += v * bt;
+    tdtb -= v * kuSv;
+    for (int j = 0; j < 3; ++j) { sb.ku[j] -= v * tdt * s.Su[j + 1]; sb.Su[j + 1] -= v * tdt * s.ku[j]; }
+    agb += v * s.S0[0]; sb.S0[0] += v * ag;
+    gdtb += v * k0S0v;
+    for (int j = 0; j < 3; ++j) { k0b[j] += v * gdt * s.S0[j + 1]; sb.S0[j + 1] += v * gdt * s.k0[j]; }
+    sb.dt03 += v * (s.ga * s.dS0[0] - s.th * s.dSu[0]);
+    sb.ga += v * s.dt03 * s.dS0[0]; sb.dS0[0] += v * s.dt03 * s.ga;
+    sb.th -= v * s.dt03 * s.dSu[0]; sb.dSu[0] -= v * s.dt03 * s.th;
+  }
+  for (int j = 0; j < 3; ++j) {
+    const R v = Vb[j + 1];
+    hb[j] += v * s.Iu[0]; sb.Iu[0] += v * h[j];
+    sb.ep += v * s.Iu[j + 1]; sb.Iu[j + 1] += v * s.ep;
+    cab += v * s.ku[j] * kuIv;
+    sb.ku[j] += v * ca * kuIv;
+    for (int m = 0; m < 3; ++m) {
+      sb.ku[m] += v * ca * s.ku[j] * s.Iu[m + 1];
+      sb.Iu[m + 1] += v * ca * s.ku[j] * s.ku[m];
+    }
+    tdtb -= v * s.ku[j] * s.Su[0]; sb.ku[j] -= v * tdt * s.Su[0]; sb.Su[0] -= v * tdt * s.ku[j];
+    btb += v * s.Su[j + 1]; sb.Su[j + 1] += v * bt;
+    gdtb += v * s.k0[j] * s.S0[0]; k0b[j] += v * gdt * s.S0[0]; sb.S0[0] += v * gdt * s.k0[j];
+    agb += v * s.S0[j + 1]; sb.S0[j + 1] += v * ag;
+    sb.dt03 += v * (s.ga * s.dS0[j + 1] - s.th * s.dSu[j + 1]);
+    sb.ga += v * s.dt03 * s.dS0[j + 1]; sb.dS0[j + 1] += v * s.dt03 * s.ga;
+    sb.th -= v * s.dt03 * s.dSu[j + 1]; sb.dSu[j + 1] -= v * s.dt03 * s.th;
+  }
+  for (int j = 0; j < 3; ++j) {
+    pab += hb[j] * s.ku[j]; sb.ku[j] += hb[j] * pa;
+    cab += hb[j] * s.dku[j]; sb.dku[j] += hb[j] * ca;
+    sb.k0[j] += k0b[j];
+  }
+  // scalars back to the coefficients
+  sb.ga += cb * s.dt03; sb.dt03 += cb * s.ga;
+  sb.al += pKb; sb.ga += pKb * (R(1) + s.dt03); sb.dt03 += pKb * s.ga;
+  sb.th += cab * s.dt03; sb.dt03 += cab * s.th;
+  sb.be -= pab; sb.th += pab * (s.dt03 - R(1)); sb.dt03 += pab * s.th;
+  sb.be += btb; sb.th += btb;
+  sb.al += agb; sb.ga += agb;
+  sb.th += tdtb * s.dt03; sb.dt03 += tdtb * s.th;
+  sb.ga += gdtb * s.dt03; sb.dt03 += gdtb * s.ga;
+}
+
+// ------------------------------------------------------ forward with tape --
+template <typename R>
+struct Tape {
+  R q[PYRH_MAX_DEPTH_RF][8];   // chi, S[4], k[3] per depth
+  R I[PYRH_MAX_DEPTH_RF][4];   // I_k
+  R T[PYRH_MAX_DEPTH_RF];      // dtau_uw of step k (T_k), and T[0] = dtau_dw of step 1
+  R dchi[PYRH_MAX_DEPTH_RF];   // dchi_c used by step k (dchi_dn of step k+1)
+  R dS0[PYRH_MAX_DEPTH_RF][4]; // dS0_k (dSu of step k-1); index nd-1 holds the initial dSu
+  R dK0[PYRH_MAX_DEPTH_RF][3];
+  R dchi_up0;                  // initial dchi_up
+};
+
+template <typename R>
+PYRH_HD void delo_forward(Tape<R>& tp, const R* ds, int nd, double B0, double B1, R out[4]) {
+  // depth index j; ds[j] = path length between j-1 and j
+  const int N = nd;
+  const double dtau0 = 0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * (double)ds[N - 1];
+  tp.I[N - 1][0] = R(B1 - (B0 - B1) / dtau0);
+  tp.I[N - 1][1] = tp.I[N - 1][2] = tp.I[N - 1][3] = R(0);
+  {
+    const int k = N - 2;
+    const R dsup = ds[k + 1], dsdn = ds[k];
+    const R cu = tp.q[k + 1][0], cc = tp.q[k][0], cd = tp.q[k - 1][0];
+    const R dchi_up = (cc - cu) / dsup;
+    const R dchi_c = cent_deriv<R>(dsup, dsdn, cu, cc, cd);
+    const R c2 = fmax(cc - (dsup / R(3)) * dchi_c, R(0));
+    const R c1 = fmax(cu + (dsup / R(3)) * dchi_up, R(0));
+    tp.T[k] = R(0.25) * dsup * (cc + cu + c1 + c2);
+    tp.dchi[k] = dchi_c;
+    tp.dchi_up0 = dchi_up;
+    for (int n = 0; n < 4; ++n) tp.dS0[N - 1][n] = (tp.q[k][1 + n] - tp.q[k + 1][1 + n]) / tp.T[k];
+    for (int n = 0; n < 3; ++n) tp.dK0[N - 1][n] = (tp.q[k][5 + n] - tp.q[k + 1][5 + n]) / tp.T[k];
+  }
+  for (int k = N - 2; k >= 1; --k) {
+    const R dsdn = ds[k];
+    R dchi_dn;
+    if (k > 1) dchi_dn = cent_deriv<R>(dsdn, ds[k - 1], tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0]);
+    else dchi_dn = (tp.q[k - 1][0] - tp.q[k][0]) / dsdn;
+    const R c2 = fmax(tp.q[k][0] + (dsdn / R(3)) * tp.dchi[k], R(0));
+    const R c1 = fmax(tp.q[k - 1][0] - (dsdn / R(3)) * dchi_dn, R(0));
+    const R Tdw = R(0.25) * dsdn * (tp.q[k][0] + tp.q[k - 1][0] + c1 + c2);
+    tp.T[k - 1] = Tdw;
+    tp.dchi[k - 1] = dchi_dn;
+    StepIn<R> s;
+    R cf[5];
+    bezier3_coeffs(tp.T[k], cf[0], cf[1], cf[2], cf[3], cf[4]);
+    s.al = cf[0]; s.be = cf[1]; s.ga = cf[2]; s.th = cf[3]; s.ep = cf[4];
+    s.dt03 = tp.T[k] / R(3);
+    for (int n = 0; n < 3; ++n) {
+      s.ku[n] = tp.q[k + 1][5 + n];
+      s.k0[n] = tp.q[k][5 + n];
+      s.dku[n] = tp.dK0[k + 1 == N - 1 ? N - 1 : k + 1][n];
+      s.dk0[n] = cent_deriv<R>(tp.T[k], Tdw, tp.q[k + 1][5 + n], tp.q[k][5 + n], tp.q[k - 1][5 + n]);
+      tp.dK0[k][n] = s.dk0[n];
+    }
+    for (int n = 0; n < 4; ++n) {
+      s.Su[n] = tp.q[k + 1][1 + n];
+      s.S0[n] = tp.q[k][1 + n];
+      s.dSu[n] = tp.dS0[k + 1 == N - 1 ? N - 1 : k + 1][n];
+      s.dS0[n] = cent_deriv<R>(tp.T[k], Tdw, tp.q[k + 1][1 + n], tp.q[k][1 + n], tp.q[k - 1][1 + n]);
+      tp.dS0[k][n] = s.dS0[n];
+      s.Iu[n] = tp.I[k + 1][n];
+    }
+    R x[4], V[4], b[3], c;
+    step_fwd(s, x, V, b, c);
+    for (int n = 0; n < 4; ++n) tp.I[k][n] = x[n];
+  }
+  // last interval
+  const double dtau = 0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * (double)ds[1];
+  double w[3];
+  w3(dtau, w);
+  const R w0 = R(w[0]), w1 = R(w[1]), wd = R(w[1] / dtau);
+  const R* ku = &tp.q[1][5];
+  const R* k0 = &tp.q[0][5];
+  const R* dSu = tp.dS0[1];
+  R V[4];
+  V[0] = w0 * tp.q[0][1] - w1 * dSu[0] + (R(1) - w0) * tp.I[1][0] -
+         wd * (ku[0] * tp.I[1][1] + ku[1] * tp.I[1][2] + ku[2] * tp.I[1][3]);
+  for (int j = 0; j < 3; ++j)
+    V[j + 1] = w0 * tp.q[0][2 + j] - w1 * dSu[j + 1] + (R(1) - w0) * tp.I[1][j + 1] -
+               wd * ku[j] * tp.I[1][0];
+  const R g = w0 - wd;
+  const R bv[3] = {g * k0[0], g * k0[1], g * k0[2]};
+  const R x0 = (V[0] - (bv[0] * V[1] + bv[1] * V[2] + bv[2] * V[3])) /
+               (R(1) - (bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2]));
+  out[0] = x0;
+  for (int j = 0; j < 3; ++j) out[j + 1] = V[j + 1] - x0 * bv[j];
+  for (int n = 0; n < 4; ++n) tp.I[0][n] = out[n];
+}
+
+// w3 derivatives (w3.c:44-63)
+PYRH_HD void w3_d(double dtau, double w[3], double dw[2]) {
+  w3(dtau, w);
+  if (dtau < 5.0E-4) {
+    dw[0] = 1.0 - dtau;
+    dw[1] = dtau - dtau * dtau;
+  } else if (dtau > 50.0) {
+    dw[0] = dw[1] = 0.0;
+  } else {
+    const double e = exp(-dtau);
+    dw[0] = e;
+    dw[1] = dtau * e;
+  }
+}
+
+// Reverse sweep for NS seeds.  seed[s][4] = dL_s/dI_0.  Accumulates
+// qb[j][s][8] = dL_s/dq_j and Bb[s][2] = dL_s/d(B0, B1).
+template <typename R, int NS>
+PYRH_HD void delo_reverse(const Tape<R>& tp, const R* ds, int nd, double B0, double B1,
+                          const R seed[NS][4], R (*qb)[NS][8], R Bb[NS][2]) {
+  const int N = nd;
+  for (int j = 0; j < N; ++j)
+    for (int s = 0; s < NS; ++s)
+      for (int n = 0; n < 8; ++n) qb[j][s][n] = R(0);
+  for (int s = 0; s < NS; ++s) {
+    R Ib[4];   // adjoint of I_k being carried
+    R dSb[4];  // adjoint of dS0 of the step above (dSu of the current)
+    R dKb[3];
+    R dchib = R(0), Tb = R(0);
+    // ---- last interval ----
+    {
+      const double dtau = 0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * (double)ds[1];
+      double w[3], dw[2];
+      w3_d(dtau, w, dw);
+      const R w0 = R(w[0]), w1 = R(w[1]), wd = R(w[1] / dtau);
+      const R* ku = &tp.q[1][5];
+      const R* k0 = &tp.q[0][5];
+      const R* dSu = tp.dS0[1];
+      const R* I1 = tp.I[1];
+      R V[4];
+      V[0] = w0 * tp.q[0][1] - w1 * dSu[0] + (R(1) - w0) * I1[0] -
+             wd * (ku[0] * I1[1] + ku[1] * I1[2] + ku[2] * I1[3]);
+      for (int j = 0; j < 3; ++j)
+        V[j + 1] = w0 * tp.q[0][2 + j] - w1 * dSu[j + 1] + (R(1) - w0) * I1[j + 1] - wd * ku[j] * I1[0];
+      const R g = w0 - wd;
+      const R bv[3] = {g * k0[0], g * k0[1], g * k0[2]};
+      const R Dn = R(1) - (bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2]);
+      const R x0 = (V[0] - (bv[0] * V[1] + bv[1] * V[2] + bv[2] * V[3])) / Dn;
+      R Vb[4] = {0, 0, 0, 0}, bb[3] = {0, 0, 0};
+      R x0b = seed[s][0];
+      for (int j = 0; j < 3; ++j) {
+        Vb[j + 1] += seed[s][j + 1];
+        x0b -= bv[j] * seed[s][j + 1];
+        bb[j] -= x0 * seed[s][j + 1];
+      }
+      Vb[0] += x0b / Dn;
+      for (int j = 0; j < 3; ++j) {
+        Vb[j + 1] -= x0b / Dn * bv[j];
+        bb[j] -= x0b / Dn * V[j + 1];
+      }
+      const R Dnb = -x0b * x0 / Dn;
+      for (int j = 0; j < 3; ++j) bb[j] += Dnb * R(-2) * bv[j];
+      R gb = 0, w0b = 0, w1b = 0, wdb = 0;
+      for (int j = 0; j < 3; ++j) { gb += bb[j] * k0[j]; qb[0][s][5 + j] += g * bb[j]; }
+      w0b += gb; wdb -= gb;
+      for (int n = 0; n < 4; ++n) { Ib[n] = R(0); dSb[n] = R(0); }
+      // V0
+      w0b += Vb[0] * (tp.q[0][1] - I1[0]);
+      qb[0][s][1] += Vb[0] * w0;
+      dSb[0] -= Vb[0] * w1;
+      w1b -= Vb[0] * dSu[0];
+      Ib[0] += Vb[0] * (R(1) - w0);
+      wdb -= Vb[0] * (ku[0] * I1[1] + ku[1] * I1[2] + ku[2] * I1[3]);
+      for (int j = 0; j < 3; ++j) {
+        qb[1][s][5 + j] -= Vb[0] * wd * I1[j + 1];
+        Ib[j + 1] -= Vb[0] * wd * ku[j];
+      }
+      for (int j = 0; j < 3; ++j) {
+        const R v = Vb[j + 1];
+        w0b += v * (tp.q[0][2 + j] - I1[j + 1]);
+        qb[0][s][2 + j] += v * w0;
+        dSb[j + 1] -= v * w1;
+        w1b -= v * dSu[j + 1];
+        Ib[j + 1] += v * (R(1) - w0);
+        wdb -= v * ku[j] * I1[0];
+        qb[1][s][5 + j] -= v * wd * I1[0];
+        Ib[0] -= v * wd * ku[j];
+      }
+      w1b += wdb / R(dtau);
+      const double dtb = (double)w0b * dw[0] + (double)w1b * dw[1] - (double)wdb * w[1] / (dtau * dtau);
+      qb[0][s][0] += R(0.5 * (double)ds[1] * dtb);
+      qb[1][s][0] += R(0.5 * (double)ds[1] * dtb);
+      for (int n = 0; n < 3; ++n) dKb[n] = R(0);
+      dchib = R(0);
+      Tb = R(0);
+    }
+    // ---- steps k = 1 .. N-2 (reverse order) ----
+    for (int k = 1; k <= N - 2; ++k) {
+      const R Tk = tp.T[k], Tdw = tp.T[k - 1];
+      StepIn<R> st, sb;
+      R cf[5], dcf[5];
+      bezier3_coeffs_d(Tk, cf, dcf);
+      st.al = cf[0]; st.be = cf[1]; st.ga = cf[2]; st.th = cf[3]; st.ep = cf[4];
+      st.dt03 = Tk / R(3);
+      const int kup = (k + 1 == N - 1) ? N - 1 : k + 1;
+      for (int n = 0; n < 3; ++n) {
+        st.ku[n] = tp.q[k + 1][5 + n]; st.k0[n] = tp.q[k][5 + n];
+        st.dku[n] = tp.dK0[kup][n]; st.dk0[n] = tp.dK0[k][n];
+      }
+      for (int n = 0; n < 4; ++n) {
+        st.Su[n] = tp.q[k + 1][1 + n]; st.S0[n] = tp.q[k][1 + n];
+        st.dSu[n] = tp.dS0[kup][n]; st.dS0[n] = tp.dS0[k][n];
+        st.Iu[n] = tp.I[k + 1][n];
+      }
+      // zero the adjoint struct
+      sb.al = sb.be = sb.ga = sb.th = sb.ep = sb.dt03 = R(0);
+      for (int n = 0; n < 3; ++n) sb.ku[n] = sb.k0[n] = sb.dku[n] = sb.dk0[n] = R(0);
+      for (int n = 0; n < 4; ++n) sb.Su[n] = sb.S0[n] = sb.dSu[n] = sb.dS0[n] = sb.Iu[n] = R(0);
+      step_vjp(st, Ib, sb);
+      // carried adjoints of dS0_k, dK0_k add to the step's own
+      for (int n = 0; n < 4; ++n) sb.dS0[n] += dSb[n];
+      for (int n = 0; n < 3; ++n) sb.dk0[n] += dKb[n];
+      // cent_deriv VJPs of dK0_k and dS0_k
+      R Tkb = R(0), Tdwb = Tb;
+      for (int n = 0; n < 3; ++n)
+        cent_deriv_vjp<R>(Tk, Tdw, tp.q[k + 1][5 + n], tp.q[k][5 + n], tp.q[k - 1][5 + n], sb.dk0[n],
+                          Tkb, Tdwb, qb[k + 1][s][5 + n], qb[k][s][5 + n], qb[k - 1][s][5 + n]);
+      for (int n = 0; n < 4; ++n)
+        cent_deriv_vjp<R>(Tk, Tdw, tp.q[k + 1][1 + n], tp.q[k][1 + n], tp.q[k - 1][1 + n], sb.dS0[n],
+                          Tkb, Tdwb, qb[k + 1][s][1 + n], qb[k][s][1 + n], qb[k - 1][s][1 + n]);
+      // coefficients
+      Tkb += sb.al * dcf[0] + sb.be * dcf[1] + sb.ga * dcf[2] + sb.th * dcf[3] + sb.ep * dcf[4] +
+             sb.dt03 / R(3);
+      for (int n = 0; n < 3; ++n) { qb[k + 1][s][5 + n] += sb.ku[n]; qb[k][s][5 + n] += sb.k0[n]; }
+      for (int n = 0; n < 4; ++n) { qb[k + 1][s][1 + n] += sb.Su[n]; qb[k][s][1 + n] += sb.S0[n]; }
+      // T_{k-1} = 0.25 ds[k] (chi_k + chi_{k-1} + c1 + c2)
+      const R dsdn = ds[k];
+      const R dchi_c = tp.dchi[k], dchi_dn = tp.dchi[k - 1];
+      R dchi_cb = R(0), dchi_dnb = dchib;
+      {
+        const R a = R(0.25) * dsdn * Tdwb;
+        qb[k][s][0] += a;
+        qb[k - 1][s][0] += a;
+        const R c2 = tp.q[k][0] + (dsdn / R(3)) * dchi_c;
+        const R c1 = tp.q[k - 1][0] - (dsdn / R(3)) * dchi_dn;
+        if (c2 > R(0)) { qb[k][s][0] += a; dchi_cb += (dsdn / R(3)) * a; }
+        if (c1 > R(0)) { qb[k - 1][s][0] += a; dchi_dnb -= (dsdn / R(3)) * a; }
+      }
+      // dchi_dn_k
+      if (k > 1) {
+        R d1 = 0, d2 = 0;
+        cent_deriv_vjp<R>(dsdn, ds[k - 1], tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0], dchi_dnb, d1, d2,
+                          qb[k][s][0], qb[k - 1][s][0], qb[k - 2][s][0]);
+      } else {
+        qb[k - 1][s][0] += dchi_dnb / dsdn;
+        qb[k][s][0] -= dchi_dnb / dsdn;
+      }
+      // carry up
+      for (int n = 0; n < 4; ++n) { Ib[n] = sb.Iu[n]; dSb[n] = sb.dSu[n]; }
+      for (int n = 0; n < 3; ++n) dKb[n] = sb.dku[n];
+      dchib = dchi_cb;
+      Tb = Tkb;
+    }
+    // ---- initial values (k = N-2 set-up and the bottom boundary) ----
+    {
+      const int k = N - 2;
+      const R T = tp.T[k];
+      const R dsup = ds[k + 1], dsdn = ds[k];
+      // dSu = (S_k - S_{k+1}) / T, dKu = (k_k - k_{k+1}) / T
+      for (int n = 0; n < 4; ++n) {
+        qb[k][s][1 + n] += dSb[n] / T;
+        qb[k + 1][s][1 + n] -= dSb[n] / T;
+        Tb -= dSb[n] * tp.dS0[N - 1][n] / T;
+      }
+      for (int n = 0; n < 3; ++n) {
+        qb[k][s][5 + n] += dKb[n] / T;
+        qb[k + 1][s][5 + n] -= dKb[n] / T;
+        Tb -= dKb[n] * tp.dK0[N - 1][n] / T;
+      }
+      const R cu = tp.q[k + 1][0], cc = tp.q[k][0];
+      const R dchi_c = tp.dchi[k], dchi_up = tp.dchi_up0;
+      const R a = R(0.25) * dsup * Tb;
+      qb[k][s][0] += a;
+      qb[k + 1][s][0] += a;
+      R dchi_cb = dchib, dchi_upb = R(0);
+      if (cc - (dsup / R(3)) * dchi_c > R(0)) { qb[k][s][0] += a; dchi_cb -= (dsup / R(3)) * a; }
+      if (cu + (dsup / R(3)) * dchi_up > R(0)) { qb[k + 1][s][0] += a; dchi_upb += (dsup / R(3)) * a; }
+      qb[k][s][0] += dchi_upb / dsup;
+      qb[k + 1][s][0] -= dchi_upb / dsup;
+      R d1 = 0, d2 = 0;
+      cent_deriv_vjp<R>(dsup, dsdn, cu, cc, tp.q[k - 1][0], dchi_cb, d1, d2, qb[k + 1][s][0],
+                        qb[k][s][0], qb[k - 1][s][0]);
+      // I_{N-1} = B1 - (B0 - B1) / dtau0
+      const double dtau0 = 0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * (double)ds[N - 1];
+      const double ib = (double)Ib[0];
+      Bb[s][1] = R(ib * (1.0 + 1.0 / dtau0));
+      Bb[s][0] = R(-ib / dtau0);
+      const double dtb = ib * (B0 - B1) / (dtau0 * dtau0);
+      qb[N - 1][s][0] += R(0.5 * (double)ds[N - 1] * dtb);
+      qb[N - 2][s][0] += R(0.5 * (double)ds[N - 1] * dtb);
+    }
+  }
+}
+
+// dB_nu/dT of planck() (planck.c:38-63)
+PYRH_HD double planck_dT(double T, double lambda) {
+  const double hc_kla = (kHPLANCK * kCLIGHT) / (kKBOLTZMANN * kNM_TO_M * lambda);
+  const double x = hc_kla / T;
+  if (x > 150.0) return 0.0;
+  const double l = kNM_TO_M * lambda;
+  const double twohnu3_c2 = (2.0 * kHPLANCK * kCLIGHT) / (l * l * l);
+  const double ex = exp(x);
+  return twohnu3_c2 * ex * x / (T * (ex - 1.0) * (ex - 1.0));
+}
+
+}  // namespace pyrh

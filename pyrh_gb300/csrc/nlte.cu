@@ -1,0 +1,852 @@
+// nlte.cu -- MALI lambda iteration for one active atom, batched over
+// atmospheres.
+//
+// Per iteration (rh/iterate.c:48-143):
+//   gamma_init    Gamma = C, new J = 0                  (fillgamma.c:44-54)
+//   formal        every (atmosphere, wavelength, ray): active-atom opacity
+//                 (opacity.c:64-300), formal solution with the diagonal
+//                 operator for both directions (bezier_1D.c:306-541) or
+//                 Feautrier where no line is active (feautrier.c:56-202),
+//                 cross-coupling (fillgamma.c:251-332) and the Gamma / J
+//                 quadrature (fillgamma.c:82-246, formal.c:247-256)
+//   stateq        per depth: statEquil with Crout LU + one improvement
+//                 (statequil.c:40-102, ludcmp.c:36-177), FP64
+//   ng            per atmosphere: Ng acceleration and MaxChange
+//                 (accelerate.c:68-146, maxchange.c:32-50), FP64;
+//                 converged atmospheres drop out of later launches
+// Line profiles (profile.c:67-371, Armstrong Voigt of voigt.c:126-243) are
+// computed once in FP64 and kept in the workspace in the formal-solution
+// precision.  The Gamma quadrature of a block of 32 wavelengths x all rays
+// is reduced in shared memory (FP64) before one global atomic per entry.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pyrh_gb300.h"
+#include "nlte.cuh"
+#include "rt_device.cuh"
+
+namespace pyrh {
+
+// ------------------------------------------------------- Armstrong Voigt --
+// Chebyshev coefficients of Dawson(5x) in odd T_{2n+1}(x) on [0,1] and the
+// 20-point Gauss-Hermite rule (positive half), both from their definitions.
+__constant__ double kDawsonCheb[34] = {
+    0.1999999999972224, -0.18400000000299979, 0.15583999999650247, -0.12166400000439881,
+    0.087708159994039123, -0.058514124808690643, 0.036215730162391359, -0.020849765439803627,
+    0.011196011634627011, -0.0056231896167108913, 0.0026487634172264554, -0.0011732670757704463,
+    0.00048995199780883401, -0.00019336308015277829, 7.2287744678832942e-05, -2.565551249788587e-05,
+    8.6620736840759859e-06, -2.7876379719252641e-06, 8.5668736268524721e-07, -2.5184337837693224e-07,
+    7.0936022149218665e-08, -1.917322572749502e-08, 4.9801256466357896e-09, -1.2447733996061773e-09,
+    2.9977766411656295e-10, -6.9644956269250685e-11, 1.5626242538020159e-11, -3.3896879080452118e-12,
+    7.1161574262122503e-13, -1.4472012169242576e-13, 2.8536768232975401e-14, -5.4606927155058021e-15,
+    1.0148769468261627e-15, -1.8333259200975614e-16};
+__constant__ double kGhT[10] = {
+    0.24534070830090124, 0.73747372854539439, 1.2340762153953231, 1.7385377121165861,
+    2.2549740020892757, 2.7888060584281305, 3.3478545673832163, 3.9447640401156252,
+    4.6036824495507442, 5.3874808900112328};
+__constant__ double kGhW[10] = {
+    0.46224366960061009, 0.28667550536283415, 0.10901720602002329, 0.024810520887463643,
+    0.0032437733422378567, 0.00022833863601635365, 7.8025564785320599e-06,
+    1.0860693707692782e-07, 4.3993409922731747e-10, 2.2293936455341447e-13};
+
+__device__ double voigt_armstrong(double a, double v) {
+  if (v < 0.0) v = -v;
+  if ((a < 1.0 && v < 4.0) || (a < 1.8 / (v + 1.0))) {
+    const double a2 = a * a, v2 = v * v;
+    double u1 = ((v2 - a2) > 70.0) ? 0.0 : exp(a2 - v2) * cos(2.0 * v * a);
+    double dn01, dn02;
+    if (v > 5.0) {
+      const double r = 1.0 / v2;
+      dn01 = -r * (0.5 + r * (0.75 + r * (1.875 + r * (6.5625 + r * (29.53125 +
+             r * (1162.4218 + r * 1055.7421))))));
+      dn02 = (1.0 - dn01) / (2.0 * v);
+    } else {
+      double b1 = 0.0, b2 = 0.0, b = 0.0;
+      const double x = v / 5.0, coef = 4.0 * x * x - 2.0;
+      for (int n = 33; n >= 0; --n) {
+        b = coef * b1 - b2 + kDawsonCheb[n];
+        b2 = b1;
+        b1 = b;
+      }
+      dn02 = x * (b - b2);
+      dn01 = 1.0 - 2.0 * v * dn02;
+    }
+    double funct = a * dn01;
+    if (a > 1.0e-8) {
+      double q = 1.0, an = a;
+      for (int n = 2; n <= 50; ++n) {
+        const double dn = (v * dn01 + dn02) * (-2.0 / n);
+        dn02 = dn01;
+        dn01 = dn;
+        if (n % 2) {
+          q = -q;
+          an *= a2;
+          const double g = dn * an;
+          funct += q * g;
+          if (fabs(g / funct) <= 1.0e-8) return u1 - 1.12837917 * funct;
+        }
+      }
+    }
+    return u1 - 1.12837917 * funct;
+  }
+  if (a < 2.5 && v < 4.0) {
+    double g = 0.0;
+    const double a2 = a * a;
+    for (int n = 0; n < 10; ++n) {
+      const double r = kGhT[n] - v, s = kGhT[n] + v;
+      g += (4.0 * kGhT[n] * kGhT[n] - 2.0) *
+           (r * atan(r / a) + s * atan(s / a) - 0.5 * a * (log(a2 + r * r) + log(a2 + s * s))) *
+           kGhW[n];
+    }
+    return g / kPI;
+  }
+  double g = 0.0;
+  const double a2 = a * a;
+  for (int n = 0; n < 10; ++n)
+    g += (1.0 / ((v - kGhT[n]) * (v - kGhT[n]) + a2) + 1.0 / ((v + kGhT[n]) * (v + kGhT[n]) + a2)) *
+         kGhW[n];
+  return (a * g) / kPI;
+}
+
+// ------------------------------------------------------------ helpers ----
+
+__device__ __forceinline__ double wlambda_line(const double* lam, const pyrh_nlte_transition& t,
+                                               int la) {
+  double Dw = kCLIGHT / t.lambda0;
+  if (t.symmetric) Dw *= 2.0;
+  const int nl = t.nlambda;
+  double w;
+  if (la == 0) w = 0.5 * (lam[1] - lam[0]);
+  else if (la == nl - 1) w = 0.5 * (lam[la] - lam[la - 1]);
+  else w = 0.5 * (lam[la + 1] - lam[la - 1]);
+  return w * Dw;
+}
+
+__device__ __forceinline__ double wlambda_cont(const double* lam, const pyrh_nlte_transition& t,
+                                               int la) {
+  const int nl = t.nlambda;
+  if (la == 0) return 0.5 * (lam[1] - lam[0]);
+  if (la == nl - 1) return 0.5 * (lam[la] - lam[la - 1]);
+  return 0.5 * (lam[la + 1] - lam[la - 1]);
+}
+
+// ---------------------------------------------------------- profiles -----
+// phi block of a line: [k][2*nrays][nlambda], lambda fastest.
+
+template <typename R>
+__global__ void nlte_profile_kernel(NlteArgs A) {
+  const int p = blockIdx.y;
+  const pyrh_nlte_batch& b = A.b;
+  const int nd = b.ndep[p], nt = b.ntrans[p], nq = 2 * A.nrays;
+  const pyrh_nlte_transition* tr = b.trans + b.trans_off[p];
+  const int64_t doff = b.depth_off[p];
+  const double* lam = b.lambda + b.lam_off[p];
+  int64_t total = 0;
+  for (int t = 0; t < nt; ++t)
+    if (tr[t].type == 0) total += (int64_t)tr[t].nlambda * nq * nd;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = e;
+    int t = 0;
+    for (; t < nt; ++t) {
+      if (tr[t].type != 0) continue;
+      const int64_t sz = (int64_t)tr[t].nlambda * nq * nd;
+      if (r < sz) break;
+      r -= sz;
+    }
+    const pyrh_nlte_transition& L = tr[t];
+    const int la = (int)(r % L.nlambda);
+    const int q = (int)((r / L.nlambda) % nq);
+    const int k = (int)(r / ((int64_t)L.nlambda * nq));
+    const int mu = q / 2, to_obs = q % 2;
+    const double vb = b.vbroad[doff + k];
+    double v = (lam[L.nblue + la] - L.lambda0 - L.c_shift) * kCLIGHT / (vb * L.lambda0);
+    if (A.moving) v += (to_obs ? 1.0 : -1.0) * A.muz[mu] * b.vel[doff + k] / vb;
+    const double a = L.voigt ? b.adamp[b.adamp_off[p] + (int64_t)L.line_index * nd + k] : 0.0;
+    const int64_t idx = L.phi_off + r;
+    if (idx < A.phi_cap)
+      static_cast<R*>(A.phi)[idx] = R(voigt_armstrong(a, v) * L.c_fraction / (kSQRTPI * vb));
+    else
+      atomicOr(A.err, 1);
+  }
+}
+
+// wphi = 1 / sum_{la, mu, dir} phi * wlambda * wmu / 2   (profile.c:210-364)
+template <typename R>
+__global__ void nlte_wphi_kernel(NlteArgs A) {
+  const int p = blockIdx.y;
+  const pyrh_nlte_batch& b = A.b;
+  const int nd = b.ndep[p], nt = b.ntrans[p], nq = 2 * A.nrays;
+  const pyrh_nlte_transition* tr = b.trans + b.trans_off[p];
+  const double* lam = b.lambda + b.lam_off[p];
+  for (int e = threadIdx.x + blockIdx.x * blockDim.x; e < nt * nd; e += blockDim.x * gridDim.x) {
+    const int t = e / nd, k = e % nd;
+    const pyrh_nlte_transition& L = tr[t];
+    if (L.type != 0) continue;
+    if (L.phi_off + (int64_t)(k + 1) * nq * L.nlambda > A.phi_cap) {
+      atomicOr(A.err, 1);
+      continue;
+    }
+    const R* ph = static_cast<const R*>(A.phi) + L.phi_off + (int64_t)k * nq * L.nlambda;
+    double s = 0.0;
+    for (int la = 0; la < L.nlambda; ++la) {
+      const double wl = wlambda_line(lam + L.nblue, L, la);
+      for (int mu = 0; mu < A.nrays; ++mu) {
+        const double wlamu = wl * 0.5 * A.wmu[mu];
+        for (int to = 0; to <= 1; ++to) s += (double)ph[(2 * mu + to) * L.nlambda + la] * wlamu;
+      }
+    }
+    A.wphi[b.adamp_off[p] + (int64_t)L.line_index * nd + k] = 1.0 / s;
+  }
+}
+
+// Gamma = C and the new J = 0 for atmospheres still iterating.
+__global__ void nlte_gamma_init_kernel(NlteArgs A) {
+  const pyrh_nlte_batch& b = A.b;
+  const int p = blockIdx.y;
+  if (!A.active[p]) return;
+  const int nd = b.ndep[p], nl2 = b.nlevel * b.nlevel;
+  const int64_t doff = b.depth_off[p];
+  for (int e = threadIdx.x + blockIdx.x * blockDim.x; e < nl2 * nd; e += blockDim.x * gridDim.x) {
+    const int ij = e / nd, k = e % nd;
+    const int64_t g = (int64_t)ij * b.total_depth + doff + k;
+    A.Gamma[g] = b.C[g];
+  }
+  const int64_t coff = b.cont_off[p], ncont = (int64_t)nd * b.nspect[p];
+  for (int64_t e = threadIdx.x + (int64_t)blockIdx.x * blockDim.x; e < ncont;
+       e += (int64_t)blockDim.x * gridDim.x)
+    A.Jnew[coff + e] = 0.0;
+}
+
+// ------------------------------------------------------------ formal -----
+
+struct ActiveSet {
+  int n;
+  int t[PYRH_NLTE_MAX_ACTIVE];   // transition index
+  int la[PYRH_NLTE_MAX_ACTIVE];  // wavelength index within the transition
+  bool bb;
+};
+
+template <typename R>
+struct NlteOpacity {
+  const NlteArgs* A;
+  const pyrh_nlte_transition* tr;
+  const ActiveSet* as;
+  const double* n_s;      // shared [nlevel][nd]
+  const double* nstar_s;  // shared [nlevel][nd]
+  int nd, nl, ns, la, q, nlev;
+  int64_t doff, coff;
+  double lam;
+  const double* lamp;     // spectrum of this atmosphere
+
+  // total opacity and source function at depth k, plus the atom's emissivity
+  __device__ __forceinline__ void operator()(int k, R& chi, R& S, double& eta_atom,
+                                             double Jold) const {
+    const pyrh_nlte_batch& b = A->b;
+    double chi_a = 0.0, eta_a = 0.0;
+    for (int m = 0; m < as->n; ++m) {
+      const pyrh_nlte_transition& t = tr[as->t[m]];
+      double V, g, tw;
+      if (t.type == 0) {
+        const int64_t pi = t.phi_off + ((int64_t)k * 2 * A->nrays + q) * t.nlambda + as->la[m];
+        const double phv = pi < A->phi_cap ? (double)static_cast<const R*>(A->phi)[pi] : 0.0;
+        V = kHPLANCK * kCLIGHT / (4.0 * kPI) * t.Bij * t.isotope_frac * phv;
+        g = t.Bji / t.Bij;
+        tw = t.Aji / t.Bji;
+      } else {
+        V = b.alpha[t.alpha_off + as->la[m]];
+        g = nstar_s[t.i * nd + k] / nstar_s[t.j * nd + k] *
+            exp(-(kHPLANCK * kCLIGHT / (kKBOLTZMANN * kNM_TO_M)) / (lam * b.T[doff + k]));
+        tw = 2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M) / (lam * lam * lam);
+      }
+      chi_a += V * (n_s[t.i * nd + k] - g * n_s[t.j * nd + k]);
+      eta_a += tw * g * V * n_s[t.j * nd + k];
+    }
+    const int64_t c = coff + (int64_t)k * ns + la;
+    const double ct = chi_a + b.chi_c[c];
+    chi = R(ct);
+    S = R((eta_a + b.eta_c[c] + b.sca_c[c] * Jold) / ct);
+    eta_atom = eta_a;
+  }
+};
+
+// Scalar Bezier3 with the diagonal operator along one direction; stores
+// I[k] and Psi[k] for every depth (bezier_1D.c:306-541).
+// Mean intensity of one wavelength at depth k ([depth][lambda] storage).
+struct JRow {
+  const double* base;
+  int stride;
+  __device__ __forceinline__ double operator[](int k) const { return base[(int64_t)k * stride]; }
+};
+
+template <typename R, typename Op>
+__device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, double B0, double B1,
+                            const JRow& Jold, R* I, R* Psi) {
+  const int dk = to_obs ? -1 : 1, k_start = to_obs ? nd - 1 : 0, k_end = to_obs ? 0 : nd - 1;
+  double ea;
+  R chi_u, chi_c, chi_d, chi_dd, S_u, S_c, S_d, S_dd = 0;
+  op(k_start, chi_u, S_u, ea, Jold[k_start]);
+  op(k_start + dk, chi_c, S_c, ea, Jold[k_start + dk]);
+  op(k_start + 2 * dk, chi_d, S_d, ea, Jold[k_start + 2 * dk]);
+  // interval path length between depth a and a+1 is ds[a+1]
+  auto dsi = [&](int a, int b2) { return ds[a > b2 ? a : b2]; };
+  const R dtau0 = R(0.5) * (chi_u + chi_c) * dsi(k_start, k_start + dk);
+  R I_upw = to_obs ? R(B1 - (B0 - B1) / (double)dtau0) : R(0);
+  I[k_start] = I_upw;
+  Psi[k_start] = R(0);
+  int k = k_start + dk;
+  R dsup = dsi(k, k - dk), dsdn = dsi(k + dk, k);
+  R dchi_up = (chi_c - chi_u) / dsup;
+  R dchi_c = cent_deriv<R>(dsup, dsdn, chi_u, chi_c, chi_d);
+  R c1 = fmax(chi_c - (dsup / R(3)) * dchi_c, R(0));
+  R c2 = fmax(chi_u + (dsup / R(3)) * dchi_up, R(0));
+  R dtau_uw = dsup * (chi_c + chi_u + c1 + c2) * R(0.25);
+  R dS_up = (S_c - S_u) / dtau_uw;
+  for (k = k_start + dk; k != k_end; k += dk) {
+    dsdn = dsi(k + dk, k);
+    R dchi_dn;
+    if (abs(k - k_end) > 1) {
+      op(k + 2 * dk, chi_dd, S_dd, ea, Jold[k + 2 * dk]);
+      dchi_dn = cent_deriv<R>(dsdn, dsi(k + 2 * dk, k + dk), chi_c, chi_d, chi_dd);
+    } else {
+      dchi_dn = (chi_d - chi_c) / dsdn;
+    }
+    c1 = fmax(chi_c + (dsdn / R(3)) * dchi_c, R(0));
+    c2 = fmax(chi_d - (dsdn / R(3)) * dchi_dn, R(0));
+    const R dtau_dw = dsdn * (chi_c + chi_d + c1 + c2) * R(0.25);
+    const R dt03 = dtau_uw / R(3);
+    R alpha, beta, gamma, theta, eps;
+    bezier3_coeffs(dtau_uw, alpha, beta, gamma, theta, eps);
+    const R dS_c = cent_deriv<R>(dtau_uw, dtau_dw, S_u, S_c, S_d);
+    c1 = fmax(S_c - dt03 * dS_c, R(0));
+    c2 = fmax(S_u + dt03 * dS_up, R(0));
+    I_upw = I_upw * eps + alpha * S_c + beta * S_u + gamma * c1 + theta * c2;
+    I[k] = I_upw;
+    Psi[k] = alpha + gamma;
+    S_u = S_c; S_c = S_d; S_d = S_dd;
+    chi_u = chi_c; chi_c = chi_d; chi_d = chi_dd;
+    dchi_c = dchi_dn;
+    dtau_uw = dtau_dw;
+    dS_up = dS_c;
+  }
+  k = k_end;
+  const double dtau = 0.5 * ((double)chi_c + (double)chi_u) * (double)dsi(k, k - dk);
+  double w[3];
+  w3(dtau, w);
+  const R dS_uw = -(S_c - S_u) / R(dtau);
+  I[k] = (R(1) - R(w[0])) * I_upw + R(w[0]) * S_c + R(w[1]) * dS_uw;
+  Psi[k] = R(w[0] - w[1] / dtau);
+}
+
+// Feautrier (feautrier.c:56-202) with P and Psi at every depth; chi and S
+// are stored in I/Psi first and overwritten.
+template <typename R>
+__device__ R feautrier_full(const R* chi, const R* S, const R* ds, int nd, double muz,
+                            double B0, double B1, R* P, R* Psi, R* F, R* zt) {
+  // dtau[k] = 0.5 (chi[k] + chi[k+1]) ds[k+1] for k = 0..nd-2 (ds already / mu)
+  auto dtau = [&](int kk) { return R(0.5) * (chi[kk] + chi[kk + 1]) * ds[kk + 1]; };
+  const R hN = R(B1 - (B0 - B1) / (double)dtau(nd - 2));
+  // rows: A1, C1, abc, St
+  const R d0 = dtau(0);
+  R abc0 = R(1) + R(2) / d0, C10 = R(2) / (d0 * d0);
+  F[0] = abc0 / C10;
+  zt[0] = S[0] / (abc0 + C10);
+  for (int k = 1; k < nd - 1; ++k) {
+    const R dm = dtau(k - 1), dp = dtau(k), dmid = R(0.5) * (dp + dm);
+    const R A1 = R(1) / (dmid * dm), C1 = R(1) / (dmid * dp);
+    F[k] = (R(1) + A1 * F[k - 1] / (R(1) + F[k - 1])) / C1;
+    zt[k] = (S[k] + A1 * zt[k - 1]) / (C1 * (R(1) + F[k]));
+  }
+  const R dN = dtau(nd - 2);
+  const R abcN = R(1) + R(2) / dN, A1N = R(2) / (dN * dN), StN = S[nd - 1] + R(2) * hN / dN;
+  R Pk = (StN + A1N * zt[nd - 2]) / (abcN + A1N * (F[nd - 2] / (R(1) + F[nd - 2])));
+  // Psi by the upward G recurrence needs F[k-1]; compute P and Psi together
+  R G = abcN / A1N;
+  Psi[nd - 1] = R(1) / (abcN + A1N * F[nd - 2] / (R(1) + F[nd - 2]));
+  P[nd - 1] = Pk;
+  for (int k = nd - 2; k >= 0; --k) {
+    Pk = Pk / (R(1) + F[k]) + zt[k];
+    P[k] = Pk;
+  }
+  for (int k = nd - 2; k >= 1; --k) {
+    const R dm = dtau(k - 1), dp = dtau(k), dmid = R(0.5) * (dp + dm);
+    const R A1 = R(1) / (dmid * dm), C1 = R(1) / (dmid * dp);
+    Psi[k] = R(1) / (R(1) + A1 * F[k - 1] / (R(1) + F[k - 1]) + C1 * G / (R(1) + G));
+    G = (R(1) + C1 * G / (R(1) + G)) / A1;
+  }
+  Psi[0] = R(1) / (abc0 + C10 * G / (R(1) + G));
+  (void)muz;
+  return R(2) * P[0];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(256)
+nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const pyrh_nlte_batch& b = A.b;
+  const int p = blockIdx.y;
+  if (!emergent_only && !A.active[p]) return;
+  const int nd = b.ndep[p], ns = b.nspect[p], nlev = b.nlevel, nt = b.ntrans[p];
+  const int la0 = blockIdx.x * 32;
+  if (la0 >= ns) return;
+  if (nd < 3 || nd > b.max_ndep || nd > PYRH_NLTE_MAX_DEPTH) {   // uniform per block
+    if (threadIdx.x == 0) atomicOr(A.err, 2);
+    return;
+  }
+  const int64_t doff = b.depth_off[p], coff = b.cont_off[p];
+  const pyrh_nlte_transition* tr = b.trans + b.trans_off[p];
+  const double* lamp = b.lambda + b.lam_off[p];
+  double* Gs = reinterpret_cast<double*>(smem_raw);                 // [nlev^2][nd]
+  double* Js = Gs + (size_t)nlev * nlev * nd;                        // [nd][32]
+  double* n_s = Js + (size_t)nd * 32;                                // [nlev][nd]
+  double* nst_s = n_s + (size_t)nlev * nd;                           // [nlev][nd]
+  const int nthr = blockDim.x;
+  for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) Gs[e] = 0.0;
+  for (int e = threadIdx.x; e < nd * 32; e += nthr) Js[e] = 0.0;
+  for (int e = threadIdx.x; e < nlev * nd; e += nthr) {
+    const int i = e / nd, k = e % nd;
+    n_s[e] = b.n[(int64_t)i * b.total_depth + doff + k];
+    nst_s[e] = b.nstar[(int64_t)i * b.total_depth + doff + k];
+  }
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31, ray = threadIdx.x >> 5;
+  const int la = la0 + lane;
+  const bool live = (la < ns) && (ray < A.nrays);
+  if (live) {
+    const double muz = A.muz[ray], imu = 1.0 / muz;
+    // path lengths of this ray (thread-private copy in local memory)
+    R dsl[PYRH_NLTE_MAX_DEPTH];
+    dsl[0] = R(0);
+    for (int k = 1; k < nd; ++k) dsl[k] = R(fabs(b.height[doff + k] - b.height[doff + k - 1]) * imu);
+    ActiveSet as;
+    as.n = 0;
+    as.bb = false;
+    for (int pass = 1; pass >= 0; --pass)       // continua (type 1) first, then lines
+      for (int t = 0; t < nt; ++t) {
+        const pyrh_nlte_transition& T = tr[t];
+        if (T.type != pass) continue;
+        if (la >= T.nblue && la < T.nblue + T.nlambda && as.n < PYRH_NLTE_MAX_ACTIVE) {
+          as.t[as.n] = t;
+          as.la[as.n] = la - T.nblue;
+          ++as.n;
+          if (T.type == 0) as.bb = true;
+        }
+      }
+    const double lam = lamp[la];
+    const double B0 = planck(b.T[doff + nd - 2], lam), B1 = planck(b.T[doff + nd - 1], lam);
+    const JRow Jold{b.J + coff + la, ns};
+    const bool angle_dep = A.moving && (as.bb || b.bgline[b.lam_off[p] + la]);
+    R I[PYRH_NLTE_MAX_DEPTH], Psi[PYRH_NLTE_MAX_DEPTH];
+    NlteOpacity<R> op;
+    op.A = &A; op.tr = tr; op.as = &as; op.n_s = n_s; op.nstar_s = nst_s;
+    op.nd = nd; op.ns = ns; op.la = la; op.nlev = nlev; op.doff = doff; op.coff = coff;
+    op.lam = lam; op.lamp = lamp;
+    const int ndir = angle_dep ? 2 : 1;
+    for (int dir = 0; dir < ndir; ++dir) {
+      const int to_obs = angle_dep ? dir : 0;
+      op.q = 2 * ray + to_obs;
+      double wdir;
+      R emergent;
+      if (angle_dep) {
+        if (emergent_only && !to_obs) continue;
+        bezier_full<R>(op, dsl, nd, to_obs, B0, B1, Jold, I, Psi);
+        wdir = 0.5 * A.wmu[ray];
+        emergent = I[0];
+      } else {
+        R chi[PYRH_NLTE_MAX_DEPTH], S[PYRH_NLTE_MAX_DEPTH];
+        double ea;
+        for (int k = 0; k < nd; ++k) op(k, chi[k], S[k], ea, Jold[k]);
+        R F[PYRH_NLTE_MAX_DEPTH], zt[PYRH_NLTE_MAX_DEPTH];
+        emergent = feautrier_full<R>(chi, S, dsl, nd, muz, B0, B1, I, Psi, F, zt);
+        wdir = A.wmu[ray];
+      }
+      if (emergent_only) {
+        I_out[b.lam_off[p] + la] = (double)emergent;
+        continue;
+      }
+      // Gamma, coupling and J at every depth (fillgamma.c:82-332, formal.c:247-256)
+      for (int k = 0; k < nd; ++k) {
+        R chi_k, S_k;
+        double eta_atom;
+        op(k, chi_k, S_k, eta_atom, Jold[k]);
+        atomicAdd(&Js[k * 32 + lane], wdir * (double)I[k]);
+        if (!eval_operator) continue;
+        const double psi = (double)Psi[k] / (double)chi_k;
+        const double Ieff = (double)I[k] - psi * eta_atom;
+        double V[PYRH_NLTE_MAX_ACTIVE], G[PYRH_NLTE_MAX_ACTIVE], W[PYRH_NLTE_MAX_ACTIVE],
+            TW[PYRH_NLTE_MAX_ACTIVE];
+        for (int m = 0; m < as.n; ++m) {
+          const pyrh_nlte_transition& t = tr[as.t[m]];
+          if (t.type == 0) {
+            const int64_t pi =
+                t.phi_off + ((int64_t)k * 2 * A.nrays + op.q) * t.nlambda + as.la[m];
+            const double phv = pi < A.phi_cap ? (double)static_cast<const R*>(A.phi)[pi] : 0.0;
+            V[m] = kHPLANCK * kCLIGHT / (4.0 * kPI) * t.Bij * t.isotope_frac * phv;
+            G[m] = t.Bji / t.Bij;
+            TW[m] = t.Aji / t.Bji;
+            W[m] = wlambda_line(lamp + t.nblue, t, as.la[m]) *
+                   A.wphi[b.adamp_off[p] + (int64_t)t.line_index * nd + k] /
+                   (kHPLANCK * kCLIGHT / (4.0 * kPI));
+          } else {
+            V[m] = b.alpha[t.alpha_off + as.la[m]];
+            G[m] = nst_s[t.i * nd + k] / nst_s[t.j * nd + k] *
+                   exp(-(kHPLANCK * kCLIGHT / (kKBOLTZMANN * kNM_TO_M)) / (lam * b.T[doff + k]));
+            TW[m] = 2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M) / (lam * lam * lam);
+            W[m] = 4.0 * kPI / kHPLANCK * (wlambda_cont(lamp + t.nblue, t, as.la[m]) / lam);
+          }
+        }
+        for (int m = 0; m < as.n; ++m) {
+          const pyrh_nlte_transition& t = tr[as.t[m]];
+          const int i = t.i, j = t.j;
+          // cross-coupling sums over the active set (addtoCoupling)
+          double chi_up_i = 0.0, chi_down_j = 0.0, U_down_j = 0.0, U_down_i = 0.0;
+          bool i_is_upper = false;
+          for (int q = 0; q < as.n; ++q) {
+            const pyrh_nlte_transition& u = tr[as.t[q]];
+            const double chicc = V[q] * W[q] * (n_s[u.i * nd + k] - G[q] * n_s[u.j * nd + k]);
+            if (u.i == i) chi_up_i += chicc;
+            if (u.j == j) { chi_down_j += chicc; U_down_j += TW[q] * G[q] * V[q]; }
+            if (u.j == i) { U_down_i += TW[q] * G[q] * V[q]; i_is_upper = true; }
+          }
+          const double wlamu = V[m] * W[m] * wdir;
+          double gji = Ieff * wlamu;
+          double gij = (TW[m] + Ieff) * G[m] * wlamu - chi_up_i * psi * U_down_j * wdir;
+          if (i_is_upper) {
+            // one term per active transition whose upper level is i
+            int cnt = 0;
+            for (int q = 0; q < as.n; ++q) cnt += (tr[as.t[q]].j == i);
+            gji += cnt * chi_down_j * psi * U_down_i * wdir;
+          }
+          atomicAdd(&Gs[(i * nlev + j) * nd + k], gij);
+          atomicAdd(&Gs[(j * nlev + i) * nd + k], gji);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (emergent_only) return;
+  for (int e = threadIdx.x; e < nd * 32; e += nthr) {
+    const int k = e / 32, l = e % 32;
+    if (la0 + l < ns) A.Jnew[coff + (int64_t)k * ns + la0 + l] = Js[e];
+  }
+  if (eval_operator)
+    for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) {
+      const int ij = e / nd, k = e % nd;
+      const double v = Gs[e];
+      if (v != 0.0) atomicAdd(&A.Gamma[(int64_t)ij * b.total_depth + doff + k], v);
+    }
+}
+
+// J <- new J for atmospheres still iterating (each wavelength replaces its
+// own mean intensity, formal.c:128-139).
+__global__ void nlte_jcopy_kernel(NlteArgs A) {
+  const pyrh_nlte_batch& b = A.b;
+  const int p = blockIdx.y;
+  if (!A.active[p]) return;
+  const int64_t coff = b.cont_off[p], ncont = (int64_t)b.ndep[p] * b.nspect[p];
+  for (int64_t e = threadIdx.x + (int64_t)blockIdx.x * blockDim.x; e < ncont;
+       e += (int64_t)blockDim.x * gridDim.x)
+    b.J[coff + e] = A.Jnew[coff + e];
+}
+
+// ------------------------------------------------ statistical equilibrium --
+
+__device__ void lu_solve(int n, double* A, double* bvec) {
+  double Ac[PYRH_NLTE_MAX_LEVELS * PYRH_NLTE_MAX_LEVELS], bc[PYRH_NLTE_MAX_LEVELS];
+  double vv[PYRH_NLTE_MAX_LEVELS], res[PYRH_NLTE_MAX_LEVELS];
+  int index[PYRH_NLTE_MAX_LEVELS];
+  for (int i = 0; i < n * n; ++i) Ac[i] = A[i];
+  for (int i = 0; i < n; ++i) bc[i] = bvec[i];
+  for (int i = 0; i < n; ++i) {
+    double big = 0.0;
+    for (int j = 0; j < n; ++j) big = fmax(big, fabs(A[i * n + j]));
+    vv[i] = (big == 0.0) ? 0.0 : 1.0 / big;
+  }
+  for (int j = 0; j < n; ++j) {
+    int imax = 0;
+    for (int i = 0; i < j; ++i) {
+      double sum = A[i * n + j];
+      for (int k = 0; k < i; ++k) sum -= A[i * n + k] * A[k * n + j];
+      A[i * n + j] = sum;
+    }
+    double big = 0.0;
+    for (int i = j; i < n; ++i) {
+      double sum = A[i * n + j];
+      for (int k = 0; k < j; ++k) sum -= A[i * n + k] * A[k * n + j];
+      A[i * n + j] = sum;
+      const double dum = vv[i] * fabs(sum);
+      if (dum >= big) { big = dum; imax = i; }
+    }
+    if (j != imax) {
+      for (int k = 0; k < n; ++k) {
+        const double t = A[imax * n + k];
+        A[imax * n + k] = A[j * n + k];
+        A[j * n + k] = t;
+      }
+      vv[imax] = vv[j];
+    }
+    index[j] = imax;
+    if (A[j * n + j] == 0.0) A[j * n + j] = 1.0e-20;
+    const double dum = 1.0 / A[j * n + j];
+    for (int i = j + 1; i < n; ++i) A[i * n + j] *= dum;
+  }
+  for (int pass = 0; pass < 2; ++pass) {
+    double* x = pass ? res : bvec;
+    if (pass)
+      for (int i = 0; i < n; ++i) {
+        res[i] = bc[i];
+        for (int j = 0; j < n; ++j) res[i] -= Ac[i * n + j] * bvec[j];
+      }
+    int ii = -1;
+    for (int i = 0; i < n; ++i) {
+      const int ip = index[i];
+      double sum = x[ip];
+      x[ip] = x[i];
+      if (ii >= 0) for (int j = ii; j < i; ++j) sum -= A[i * n + j] * x[j];
+      else if (sum != 0.0) ii = i;
+      x[i] = sum;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double sum = x[i];
+      for (int j = i + 1; j < n; ++j) sum -= A[i * n + j] * x[j];
+      x[i] = sum / A[i * n + i];
+    }
+  }
+  for (int i = 0; i < n; ++i) bvec[i] += res[i];
+}
+
+__global__ void nlte_stateq_kernel(NlteArgs A) {
+  const pyrh_nlte_batch& b = A.b;
+  const int p = blockIdx.y;
+  if (!A.active[p]) return;
+  const int nd = b.ndep[p], nl = b.nlevel;
+  const int64_t doff = b.depth_off[p];
+  for (int k = threadIdx.x + blockIdx.x * blockDim.x; k < nd; k += blockDim.x * gridDim.x) {
+    double M[PYRH_NLTE_MAX_LEVELS * PYRH_NLTE_MAX_LEVELS], x[PYRH_NLTE_MAX_LEVELS];
+    int ie = 0;
+    if (A.isum == -1) {
+      double nmax = 0.0;
+      for (int i = 0; i < nl; ++i) {
+        const double v = b.n[(int64_t)i * b.total_depth + doff + k];
+        if (v > nmax) { nmax = v; ie = i; }
+      }
+    } else {
+      ie = A.isum;
+    }
+    for (int i = 0; i < nl; ++i)
+      for (int j = 0; j < nl; ++j)
+        M[i * nl + j] = A.Gamma[(int64_t)(i * nl + j) * b.total_depth + doff + k];
+    for (int i = 0; i < nl; ++i) {
+      double d = 0.0;
+      M[i * nl + i] = 0.0;
+      x[i] = 0.0;
+      for (int j = 0; j < nl; ++j) d += M[j * nl + i];
+      M[i * nl + i] = -d;
+    }
+    x[ie] = b.ntotal[doff + k];
+    for (int j = 0; j < nl; ++j) M[ie * nl + j] = 1.0;
+    lu_solve(nl, M, x);
+    for (int i = 0; i < nl; ++i) b.n[(int64_t)i * b.total_depth + doff + k] = x[i];
+  }
+}
+
+// --------------------------------------------------------- Ng + MaxChange --
+// One block per atmosphere; history prev[(order+2)][nlevel*ndep] per atmosphere.
+
+__device__ double block_sum(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+  __syncthreads();
+  if (threadIdx.x == 0) red[0] = s;
+  __syncthreads();
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__device__ double block_max(double v, double* red) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s = fmax(s, red[i]);
+    red[0] = s;
+  }
+  __syncthreads();
+  const double r = red[0];
+  __syncthreads();
+  return r;
+}
+
+__global__ void nlte_ng_kernel(NlteArgs A, int init) {
+  __shared__ double red[32];
+  __shared__ double Ab[PYRH_NLTE_MAX_NG * PYRH_NLTE_MAX_NG + PYRH_NLTE_MAX_NG];
+  const pyrh_nlte_batch& b = A.b;
+  const int p = blockIdx.x;
+  if (!init && !A.active[p]) return;
+  const int nd = b.ndep[p], nl = b.nlevel, N = nl * nd, No = A.ng_order, np2 = No + 2;
+  const int64_t doff = b.depth_off[p];
+  double* prev = A.ngprev + (int64_t)np2 * nl * doff;   // [np2][N]
+  auto sol = [&](int e) -> double& {
+    return b.n[(int64_t)(e / nd) * b.total_depth + doff + (e % nd)];
+  };
+  if (init) {                                     // NgInit (accelerate.c:34-63)
+    for (int e = threadIdx.x; e < N; e += blockDim.x) prev[e] = sol(e);
+    if (threadIdx.x == 0) { A.count[p] = 1; A.iters[p] = 0; A.dpops[p] = 0.0; A.active[p] = 1; }
+    return;
+  }
+  const int count0 = A.count[p];
+  const int slot = count0 % np2;
+  for (int e = threadIdx.x; e < N; e += blockDim.x) prev[(int64_t)slot * N + e] = sol(e);
+  const int count = count0 + 1;
+  const int Ndelay = A.ng_delay > No + 2 ? A.ng_delay : No + 2;
+  bool accel = (No > 0) && (count >= Ndelay) && !((count - Ndelay) % A.ng_period);
+  __syncthreads();
+  if (accel) {
+    // A[i][j], b[j] over the weighted differences (accelerate.c:87-118)
+    for (int j = 0; j < No; ++j) {
+      const int ip0 = (count - 1) % np2, ipp0 = (count - 2) % np2;
+      const int ipj = (count - 2 - j) % np2, ippj = (count - 3 - j) % np2;
+      double sb = 0.0;
+      for (int e = threadIdx.x; e < N; e += blockDim.x) {
+        const double w = 1.0 / fabs(sol(e));
+        const double d0 = prev[(int64_t)ip0 * N + e] - prev[(int64_t)ipp0 * N + e];
+        const double dj = prev[(int64_t)ipj * N + e] - prev[(int64_t)ippj * N + e];
+        sb += w * d0 * (d0 - dj);
+      }
+      sb = block_sum(sb, red);
+      if (threadIdx.x == 0) Ab[No * No + j] = sb;
+      for (int i = 0; i < No; ++i) {
+        const int ipi = (count - 2 - i) % np2, ippi = (count - 3 - i) % np2;
+        double sa = 0.0;
+        for (int e = threadIdx.x; e < N; e += blockDim.x) {
+          const double w = 1.0 / fabs(sol(e));
+          const double d0 = prev[(int64_t)ip0 * N + e] - prev[(int64_t)ipp0 * N + e];
+          const double dj = prev[(int64_t)ipj * N + e] - prev[(int64_t)ippj * N + e];
+          const double di = prev[(int64_t)ipi * N + e] - prev[(int64_t)ippi * N + e];
+          sa += w * (dj - d0) * (di - d0);
+        }
+        sa = block_sum(sa, red);
+        if (threadIdx.x == 0) Ab[i * No + j] = sa;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) lu_solve(No, Ab, Ab + No * No);
+    __syncthreads();
+    const int i0 = (count - 1) % np2;
+    for (int e = threadIdx.x; e < N; e += blockDim.x) {
+      double s = sol(e);
+      for (int q = 0; q < No; ++q) {
+        const int ip = (count - 2 - q) % np2;
+        s += Ab[No * No + q] * (prev[(int64_t)ip * N + e] - prev[(int64_t)i0 * N + e]);
+      }
+      sol(e) = s;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < N; e += blockDim.x) prev[(int64_t)i0 * N + e] = sol(e);
+    __syncthreads();
+  }
+  // MaxChange (maxchange.c:32-50)
+  const int io = (count - 2) % np2, in = (count - 1) % np2;
+  double dm = 0.0;
+  for (int e = threadIdx.x; e < N; e += blockDim.x) {
+    const double nw = prev[(int64_t)in * N + e], ol = prev[(int64_t)io * N + e];
+    if (nw != 0.0) dm = fmax(dm, fabs((nw - ol) / nw));
+  }
+  dm = block_max(dm, red);
+  if (threadIdx.x == 0) {
+    A.count[p] = count;
+    A.iters[p] += 1;
+    A.dpops[p] = dm;
+    if (dm < A.iter_limit || A.iters[p] >= A.nmax_iter) A.active[p] = 0;
+  }
+}
+
+// ----------------------------------------------------------- launching ---
+
+size_t nlte_formal_smem(int nlevel, int maxd, int precision) {
+  const size_t r = precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
+  (void)r;
+  return sizeof(double) * ((size_t)nlevel * nlevel * maxd + (size_t)maxd * 32 +
+                           2 * (size_t)nlevel * maxd) + 64;
+}
+
+template <typename R>
+static cudaError_t launch_profiles_t(const NlteArgs& A, int natm, int64_t max_elems,
+                                     cudaStream_t st) {
+  int64_t gx = (max_elems + 255) / 256;
+  const int64_t cap = natm >= 4096 ? 1 : 4096 / natm;
+  if (gx > cap) gx = cap;
+  if (gx < 1) gx = 1;
+  dim3 g((unsigned)gx, natm);
+  nlte_profile_kernel<R><<<g, 256, 0, st>>>(A);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  dim3 g2(8, natm);
+  nlte_wphi_kernel<R><<<g2, 128, 0, st>>>(A);
+  return cudaGetLastError();
+}
+
+cudaError_t nlte_launch_profiles(const NlteArgs& A, int natm, int64_t max_elems, int precision,
+                                 cudaStream_t st) {
+  return precision == PYRH_FP32 ? launch_profiles_t<float>(A, natm, max_elems, st)
+                                : launch_profiles_t<double>(A, natm, max_elems, st);
+}
+
+template <typename R>
+static cudaError_t launch_formal_t(const NlteArgs& A, int natm, int max_nspect, int maxd,
+                                   int eval_operator, int emergent_only, double* I_out,
+                                   cudaStream_t st) {
+  const size_t smem = nlte_formal_smem(A.b.nlevel, maxd, sizeof(R) == 4 ? PYRH_FP32 : PYRH_FP64);
+  cudaError_t e = cudaFuncSetAttribute(nlte_formal_kernel<R>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 g((max_nspect + 31) / 32, natm);
+  nlte_formal_kernel<R><<<g, 32 * A.nrays, smem, st>>>(A, eval_operator, emergent_only, I_out);
+  return cudaGetLastError();
+}
+
+cudaError_t nlte_launch_iteration(const NlteArgs& A, int natm, int max_nspect, int maxd,
+                                  int precision, cudaStream_t st) {
+  dim3 gi(8, natm);
+  nlte_gamma_init_kernel<<<gi, 256, 0, st>>>(A);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  e = precision == PYRH_FP32
+          ? launch_formal_t<float>(A, natm, max_nspect, maxd, 1, 0, nullptr, st)
+          : launch_formal_t<double>(A, natm, max_nspect, maxd, 1, 0, nullptr, st);
+  if (e != cudaSuccess) return e;
+  nlte_jcopy_kernel<<<gi, 256, 0, st>>>(A);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  dim3 gs((maxd + 127) / 128, natm);
+  nlte_stateq_kernel<<<gs, 128, 0, st>>>(A);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  nlte_ng_kernel<<<natm, 256, 0, st>>>(A, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t nlte_launch_ng_init(const NlteArgs& A, int natm, cudaStream_t st) {
+  nlte_ng_kernel<<<natm, 256, 0, st>>>(A, 1);
+  return cudaGetLastError();
+}
+
+cudaError_t nlte_launch_emergent(const NlteArgs& A, int natm, int max_nspect, int maxd,
+                                 int precision, double* I_out, cudaStream_t st) {
+  return precision == PYRH_FP32
+             ? launch_formal_t<float>(A, natm, max_nspect, maxd, 0, 1, I_out, st)
+             : launch_formal_t<double>(A, natm, max_nspect, maxd, 0, 1, I_out, st);
+}
+
+}  // namespace pyrh

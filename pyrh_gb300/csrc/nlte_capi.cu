@@ -1,0 +1,226 @@
+// nlte_capi.cu -- extern "C" entry points of the NLTE solver.
+#include <cuda_runtime.h>
+#include <stdio.h>
+
+#include <vector>
+
+#include "../../include/pyrh_gb300.h"
+#include "nlte.cuh"
+
+namespace pyrh {
+void set_error(const char* fmt, ...);
+void set_launches(int n);
+}  // namespace pyrh
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct Layout {
+  size_t wphi, Jnew, Gamma, ngprev, count, active, iters, err, dpops, phi, fixed;
+};
+
+Layout layout(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg) {
+  Layout L;
+  size_t off = 0;
+  const int nlev = b->nlevel, natm = b->natm;
+  L.wphi = off; off = align256(off + sizeof(double) * (size_t)(b->max_nline > 0 ? b->max_nline : 1) * b->total_depth);
+  L.Jnew = off; off = align256(off + sizeof(double) * (size_t)b->total_cont);
+  L.Gamma = off; off = align256(off + sizeof(double) * (size_t)nlev * nlev * b->total_depth);
+  L.ngprev = off; off = align256(off + sizeof(double) * (size_t)(cfg->ng_order + 2) * nlev * b->total_depth);
+  L.count = off; off = align256(off + sizeof(int32_t) * natm);
+  L.active = off; off = align256(off + sizeof(int32_t) * natm);
+  L.iters = off; off = align256(off + sizeof(int32_t) * natm);
+  L.err = off; off = align256(off + sizeof(int32_t));
+  L.dpops = off; off = align256(off + sizeof(double) * natm);
+  L.phi = off;
+  L.fixed = off;
+  return L;
+}
+
+pyrh_status check(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg) {
+  if (!b || !cfg) { pyrh::set_error("batch or cfg is NULL"); return PYRH_ERR_ARG; }
+  if (b->natm < 1 || b->nlevel < 2 || b->nlevel > PYRH_NLTE_MAX_LEVELS) {
+    pyrh::set_error("natm %d / nlevel %d outside limits", b->natm, b->nlevel);
+    return PYRH_ERR_ARG;
+  }
+  if (b->max_ndep < 3 || b->max_ndep > PYRH_NLTE_MAX_DEPTH) {
+    pyrh::set_error("max_ndep %d outside [3, %d]", b->max_ndep, PYRH_NLTE_MAX_DEPTH);
+    return PYRH_ERR_ARG;
+  }
+  if (cfg->nrays < 1 || cfg->nrays > PYRH_NLTE_MAX_RAYS) {
+    pyrh::set_error("nrays %d outside [1, %d]", cfg->nrays, PYRH_NLTE_MAX_RAYS);
+    return PYRH_ERR_ARG;
+  }
+  if (cfg->ng_order < 0 || cfg->ng_order > PYRH_NLTE_MAX_NG || (cfg->ng_order > 0 && cfg->ng_period < 1)) {
+    pyrh::set_error("ng_order %d / ng_period %d", cfg->ng_order, cfg->ng_period);
+    return PYRH_ERR_ARG;
+  }
+  if (cfg->precision != PYRH_FP32 && cfg->precision != PYRH_FP64) {
+    pyrh::set_error("precision %d", cfg->precision);
+    return PYRH_ERR_ARG;
+  }
+  if (cfg->isum < -1 || cfg->isum >= b->nlevel || cfg->nmax_iter < 1) {
+    pyrh::set_error("isum %d / nmax_iter %d", cfg->isum, cfg->nmax_iter);
+    return PYRH_ERR_ARG;
+  }
+  const void* ptrs[] = {b->ndep, b->nspect, b->ntrans, b->depth_off, b->lam_off, b->cont_off,
+                        b->trans_off, b->adamp_off, b->lambda, b->height, b->T, b->vel,
+                        b->vbroad, b->ntotal, b->nstar, b->C, b->chi_c, b->eta_c, b->sca_c,
+                        b->bgline, b->trans, b->n, b->J};
+  for (const void* p : ptrs)
+    if (!p) { pyrh::set_error("a batch array pointer is NULL"); return PYRH_ERR_ARG; }
+  return PYRH_OK;
+}
+
+pyrh::NlteArgs make_args(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg, void* ws,
+                         size_t ws_bytes, const Layout& L) {
+  pyrh::NlteArgs A;
+  A.b = *b;
+  A.nrays = cfg->nrays;
+  for (int m = 0; m < PYRH_NLTE_MAX_RAYS; ++m) {
+    A.muz[m] = m < cfg->nrays ? cfg->muz[m] : 1.0;
+    A.wmu[m] = m < cfg->nrays ? cfg->wmu[m] : 0.0;
+  }
+  A.moving = cfg->moving;
+  A.isum = cfg->isum;
+  A.ng_order = cfg->ng_order;
+  A.ng_delay = cfg->ng_delay;
+  A.ng_period = cfg->ng_period > 0 ? cfg->ng_period : 1;
+  A.nmax_iter = cfg->nmax_iter;
+  A.iter_limit = cfg->iter_limit;
+  char* w = static_cast<char*>(ws);
+  A.wphi = reinterpret_cast<double*>(w + L.wphi);
+  A.Jnew = reinterpret_cast<double*>(w + L.Jnew);
+  A.Gamma = reinterpret_cast<double*>(w + L.Gamma);
+  A.ngprev = reinterpret_cast<double*>(w + L.ngprev);
+  A.count = reinterpret_cast<int32_t*>(w + L.count);
+  A.active = reinterpret_cast<int32_t*>(w + L.active);
+  A.iters = reinterpret_cast<int32_t*>(w + L.iters);
+  A.err = reinterpret_cast<int32_t*>(w + L.err);
+  A.dpops = reinterpret_cast<double*>(w + L.dpops);
+  A.phi = w + L.phi;
+  const size_t r = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
+  A.phi_cap = (int64_t)((ws_bytes - L.phi) / r);
+  return A;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t pyrh_nlte_workspace_bytes(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg,
+                                 int64_t phi_elems) {
+  if (!b || !cfg) return 0;
+  const Layout L = layout(b, cfg);
+  const size_t r = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
+  return L.fixed + r * (size_t)(phi_elems > 0 ? phi_elems : 1);
+}
+
+pyrh_status pyrh_nlte_solve(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg, void* ws,
+                            size_t ws_bytes, int32_t* iterations, double* dpops, void* stream) {
+  pyrh::set_launches(0);
+  pyrh_status s = check(b, cfg);
+  if (s != PYRH_OK) return s;
+  const Layout L = layout(b, cfg);
+  if (!ws || ws_bytes <= L.fixed) {
+    pyrh::set_error("workspace of %zu bytes is smaller than %zu", ws_bytes, L.fixed);
+    return PYRH_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  pyrh::NlteArgs A = make_args(b, cfg, ws, ws_bytes, L);
+  const size_t smem = pyrh::nlte_formal_smem(b->nlevel, b->max_ndep, cfg->precision);
+  if (smem > 220 * 1024) {
+    pyrh::set_error("shared memory %zu B for %d levels x %d depths", smem, b->nlevel, b->max_ndep);
+    return PYRH_ERR_UNSUPPORTED;
+  }
+  cudaError_t e = cudaMemsetAsync(A.err, 0, sizeof(int32_t), st);
+  int launches = 1;
+  if (e == cudaSuccess) e = pyrh::nlte_launch_ng_init(A, b->natm, st), ++launches;
+  const int64_t max_elems = (int64_t)b->max_nspect * 2 * cfg->nrays * b->max_ndep;
+  if (e == cudaSuccess)
+    e = pyrh::nlte_launch_profiles(A, b->natm, max_elems, cfg->precision, st), launches += 2;
+  std::vector<int32_t> active(b->natm, 1);
+  int it = 0;
+  for (; e == cudaSuccess && it < cfg->nmax_iter; ++it) {
+    e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision, st);
+    launches += 5;
+    if (e != cudaSuccess) break;
+    e = cudaMemcpyAsync(active.data(), A.active, sizeof(int32_t) * b->natm,
+                        cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    bool any = false;
+    for (int p = 0; p < b->natm; ++p) any |= active[p] != 0;
+    if (!any) { ++it; break; }
+  }
+  int32_t err = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&err, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && iterations)
+    e = cudaMemcpyAsync(iterations, A.iters, sizeof(int32_t) * b->natm, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess && dpops)
+    e = cudaMemcpyAsync(dpops, A.dpops, sizeof(double) * b->natm, cudaMemcpyDeviceToDevice, st);
+  std::vector<double> dp(b->natm);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dp.data(), A.dpops, sizeof(double) * b->natm, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  pyrh::set_launches(launches);
+  if (e != cudaSuccess) {
+    pyrh::set_error("NLTE solve: %s", cudaGetErrorString(e));
+    return PYRH_ERR_CUDA;
+  }
+  if (err) {
+    pyrh::set_error(err & 2 ? "an atmosphere's ndep exceeds max_ndep or the depth limit"
+                            : "line profiles do not fit the workspace (phi_off beyond capacity)");
+    return PYRH_ERR_ARG;
+  }
+  for (int p = 0; p < b->natm; ++p)
+    if (!(dp[p] < cfg->iter_limit)) {
+      pyrh::set_error("atmosphere %d not converged after %d iterations (dpops %g)", p,
+                      cfg->nmax_iter, dp[p]);
+      return PYRH_ERR_NONCONVERGED;
+    }
+  return PYRH_OK;
+}
+
+pyrh_status pyrh_nlte_emergent(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg,
+                               double mu_out, void* ws, size_t ws_bytes, double* I_out,
+                               void* stream) {
+  pyrh::set_launches(0);
+  pyrh_status s = check(b, cfg);
+  if (s != PYRH_OK) return s;
+  if (!(mu_out > 0.0 && mu_out <= 1.0) || !I_out) {
+    pyrh::set_error("mu_out %g or I_out", mu_out);
+    return PYRH_ERR_ARG;
+  }
+  pyrh_nlte_config one = *cfg;
+  one.nrays = 1;
+  one.muz[0] = mu_out;
+  one.wmu[0] = 1.0;
+  const Layout L = layout(b, &one);
+  if (!ws || ws_bytes <= L.fixed) {
+    pyrh::set_error("workspace of %zu bytes is smaller than %zu", ws_bytes, L.fixed);
+    return PYRH_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  pyrh::NlteArgs A = make_args(b, &one, ws, ws_bytes, L);
+  cudaError_t e = cudaMemsetAsync(A.err, 0, sizeof(int32_t), st);
+  const int64_t max_elems = (int64_t)b->max_nspect * 2 * b->max_ndep;
+  if (e == cudaSuccess) e = pyrh::nlte_launch_profiles(A, b->natm, max_elems, one.precision, st);
+  if (e == cudaSuccess)
+    e = pyrh::nlte_launch_emergent(A, b->natm, b->max_nspect, b->max_ndep, one.precision, I_out, st);
+  int32_t err = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&err, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  pyrh::set_launches(3);
+  if (e != cudaSuccess) {
+    pyrh::set_error("NLTE emergent: %s", cudaGetErrorString(e));
+    return PYRH_ERR_CUDA;
+  }
+  if (err) {
+    pyrh::set_error("line profiles do not fit the workspace");
+    return PYRH_ERR_ARG;
+  }
+  return PYRH_OK;
+}
+
+}  // extern "C"

@@ -15,6 +15,10 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+// Functions here are host-and-device so the same math is unit-testable on
+// the CPU (FP64); single-precision hardware intrinsics are device-only.
+#define PYRH_HD __host__ __device__ __forceinline__
+
 namespace pyrh {
 
 // Physical constants with the values of the reference (rh/constant.h:28-68).
@@ -34,30 +38,56 @@ constexpr double kMAX_GAUSS_DOPPLER = 7.0;
 template <typename R> struct Cx { R r, i; };
 
 template <typename R>
-__device__ __forceinline__ Cx<R> cmul(Cx<R> a, Cx<R> b) {
+PYRH_HD Cx<R> cmul(Cx<R> a, Cx<R> b) {
   return {a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r};
 }
 // Division: IEEE in FP64; in FP32 the fast reciprocal-based division
 // (__fdividef, 2 ulp), which the FP32 accuracy budget (1e-4) allows.
-__device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
-__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+PYRH_HD double fdiv(double a, double b) { return a / b; }
+PYRH_HD float fdiv(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
 
 template <typename R>
-__device__ __forceinline__ Cx<R> cdiv(Cx<R> a, Cx<R> b) {
+PYRH_HD Cx<R> cdiv(Cx<R> a, Cx<R> b) {
   R inv = fdiv(R(1), b.r * b.r + b.i * b.i);
   return {(a.r * b.r + a.i * b.i) * inv, (a.i * b.r - a.r * b.i) * inv};
 }
 
-__device__ __forceinline__ double dev_exp(double x) { return exp(x); }
-__device__ __forceinline__ float dev_exp(float x) { return __expf(x); }
-__device__ __forceinline__ void dev_sincos(double x, double* s, double* c) { sincos(x, s, c); }
+PYRH_HD double dev_exp(double x) { return exp(x); }
+PYRH_HD float dev_exp(float x) {
+#ifdef __CUDA_ARCH__
+  return __expf(x);
+#else
+  return expf(x);
+#endif
+}
+PYRH_HD void dev_sincos(double x, double* s, double* c) {
+#ifdef __CUDA_ARCH__
+  sincos(x, s, c);
+#else
+  *s = ::sin(x);
+  *c = ::cos(x);
+#endif
+}
 // |x| <= 2 a |v| stays below ~11 in Humlicek region IV; the hardware sine /
 // cosine keeps an absolute error near 1e-6 there, far inside the budget.
-__device__ __forceinline__ void dev_sincos(float x, float* s, float* c) { __sincosf(x, s, c); }
+PYRH_HD void dev_sincos(float x, float* s, float* c) {
+#ifdef __CUDA_ARCH__
+  __sincosf(x, s, c);
+#else
+  *s = ::sinf(x);
+  *c = ::cosf(x);
+#endif
+}
 
 // Humlicek W4: returns H = Re W, F = Im W for t = a - i v.
 template <typename R>
-__device__ __forceinline__ void humlicek(R a, R v, R& H, R& F) {
+PYRH_HD void humlicek(R a, R v, R& H, R& F) {
   const Cx<R> t = {a, -v};
   const R s = fabs(v) + a;
   Cx<R> W;
@@ -113,7 +143,7 @@ __device__ __forceinline__ void humlicek(R a, R v, R& H, R& F) {
 }
 
 template <typename R>
-__device__ __forceinline__ R cent_deriv(R dsup, R dsdn, R up, R c, R dn) {
+PYRH_HD R cent_deriv(R dsup, R dsdn, R up, R c, R dn) {
   R fim1 = fdiv(c - up, dsup), fi = fdiv(dn - c, dsdn);
   if (fim1 * fi > R(0)) {
     R alpha = R(0.333333333333333333333333) * (R(1) + fdiv(dsdn, dsdn + dsup));
@@ -125,7 +155,7 @@ __device__ __forceinline__ R cent_deriv(R dsup, R dsdn, R up, R c, R dn) {
 // cent_deriv with the path lengths' reciprocals and the weight alpha
 // precomputed (shared by all entries of one depth).
 template <typename R>
-__device__ __forceinline__ R cent_deriv_w(R rdsup, R rdsdn, R alpha, R up, R c, R dn) {
+PYRH_HD R cent_deriv_w(R rdsup, R rdsdn, R alpha, R up, R c, R dn) {
   R fim1 = (c - up) * rdsup, fi = (dn - c) * rdsdn;
   if (fim1 * fi > R(0)) return fdiv(fim1 * fi, (R(1) - alpha) * fim1 + alpha * fi);
   return R(0);
@@ -134,7 +164,7 @@ __device__ __forceinline__ R cent_deriv_w(R rdsup, R rdsdn, R alpha, R up, R c, 
 struct BezierW { double a, b, g, t, e; };
 
 // Reference branches (FP64 mode).
-__device__ __forceinline__ void bezier3_coeffs(double dt, double& alpha, double& beta,
+PYRH_HD void bezier3_coeffs(double dt, double& alpha, double& beta,
                                                double& gamma, double& theta, double& eps) {
   double dt2 = dt * dt, dt3 = dt2 * dt;
   if (dt >= 5.e-2) {
@@ -158,14 +188,14 @@ __device__ __forceinline__ void bezier3_coeffs(double dt, double& alpha, double&
 // FP32 mode: Taylor series (x^1..x^11) of the same weights for dt < 1.5,
 // the closed form above it; the series coefficients are the exact Taylor
 // coefficients of the closed forms (alternating tails of exp(-x)).
-__device__ __forceinline__ float horner11(float x, const float* c) {
+PYRH_HD float horner11(float x, const float* c) {
   float s = c[10];
 #pragma unroll
   for (int i = 9; i >= 0; --i) s = fmaf(s, x, c[i]);
   return s * x;
 }
 
-__device__ __forceinline__ void bezier3_coeffs(float dt, float& alpha, float& beta,
+PYRH_HD void bezier3_coeffs(float dt, float& alpha, float& beta,
                                                float& gamma, float& theta, float& eps) {
   eps = expf(-dt);
   if (dt >= 1.5f) {
@@ -194,7 +224,7 @@ __device__ __forceinline__ void bezier3_coeffs(float dt, float& alpha, float& be
   }
 }
 
-__device__ __forceinline__ void w3(double dtau, double* w) {
+PYRH_HD void w3(double dtau, double* w) {
   if (dtau < 5.0E-4) {
     w[0] = dtau * (1.0 - 0.5 * dtau);
     double d2 = dtau * dtau;
@@ -211,7 +241,7 @@ __device__ __forceinline__ void w3(double dtau, double* w) {
   }
 }
 
-__device__ __forceinline__ double planck(double T, double lambda) {
+PYRH_HD double planck(double T, double lambda) {
   double hc_kla = (kHPLANCK * kCLIGHT) / (kKBOLTZMANN * kNM_TO_M * lambda);
   double l = kNM_TO_M * lambda;
   double twohnu3_c2 = (2.0 * kHPLANCK * kCLIGHT) / (l * l * l);
@@ -223,7 +253,7 @@ __device__ __forceinline__ double planck(double T, double lambda) {
 // matrices are unit-diagonal-dominated; the reference inverts them by
 // cofactors, rh/bezier_aux.c:133-329).  All indices are compile-time.
 template <typename R>
-__device__ __forceinline__ void solve4(R M[4][4], const R b[4], R x[4]) {
+PYRH_HD void solve4(R M[4][4], const R b[4], R x[4]) {
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     R inv = R(1) / M[c][c];

@@ -77,3 +77,23 @@ def test_pack_layout(golden):
     assert a["cont_off"][1] == 71 * len(fx["lam"])
     # continuum is [depth][lambda] per atmosphere
     assert a["chi_c"][5 * len(fx["lam"]) + 7] == fx["chi_c"][7, 5]
+
+
+def test_nlte_structs_and_workspace_without_gpu(golden):
+    import ctypes as C
+    from pyrh_gb300 import nlte
+    assert C.sizeof(nlte.PyrhNlteTransition) == 8 * 4 + 2 * 8 + 7 * 8
+    fx = golden("nlte_c1")
+    cfg = nlte.make_config(fx)
+    pk = nlte.pack([fx], cfg.nrays)
+    b = nlte.PyrhNlteBatch()
+    b.natm, b.nlevel = pk.natm, pk.nlevel
+    for k, v in pk.shape.items():
+        setattr(b, k, v)
+    n = nlte._lib().pyrh_nlte_workspace_bytes(C.byref(b), C.byref(cfg), pk.phi_elems)
+    # profiles dominate: 663 line wavelengths x 10 ray-directions x 82 depths
+    assert n >= 8 * pk.phi_elems
+    assert pk.phi_elems == sum(int(l[8]) for l in fx["lines"]) * 10 * 82
+    # transitions: continua first, then lines, as the active sets are built
+    types = [pk.trans[i].type for i in range(pk.ntrans_total)]
+    assert types == [1] * len(fx["continua"]) + [0] * len(fx["lines"])
