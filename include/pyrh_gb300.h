@@ -236,6 +236,31 @@ pyrh_status pyrh_nlte_emergent(const pyrh_nlte_batch *batch, const pyrh_nlte_con
                                double mu_out, void *workspace, size_t workspace_bytes,
                                double *I_out, void *stream);
 
+/* Size of the device array that pyrh_nlte_solve_static uses as scratch. */
+#define PYRH_NLTE_STATIC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+/* pyrh_nlte_solve for callers that cannot allocate device memory (their
+   device memory belongs to another component's pool, their host forbids
+   device allocation after start-up, or an allocation's implicit
+   synchronisation is not acceptable).  No counterpart exists in the
+   reference; it is the same solve as pyrh_nlte_solve with the workspace
+   replaced by a fixed array of PYRH_NLTE_STATIC_SCRATCH_BYTES in device
+   memory that every GPU loading this library holds until the process exits.
+   phi_elems is the line-profile size of the batch (as for
+   pyrh_nlte_workspace_bytes); batches whose scratch does not fit, or with
+   more than 256 atmospheres, are rejected with PYRH_ERR_ARG.  The call
+   allocates nothing.  The first call on a device looks up the array's
+   device address (cudaGetSymbolAddress) with that device current, which
+   also loads this library's device code there if that has not happened
+   yet; make that first call before any stream capture.  Nothing in the
+   array has to start at zero: the call clears its error word and every
+   kernel writes the rest before reading it, so each call may find the
+   previous call's contents there.  All calls share the one array: calls
+   that overlap on the GPU (other streams, other host threads) race on it. */
+pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch *batch, const pyrh_nlte_config *cfg,
+                                   int64_t phi_elems, int32_t *iterations, double *dpops,
+                                   void *stream);
+
 /* Number of kernel launches the last pyrh_lte_stokes / pyrh_nlte_* call issued. */
 int32_t pyrh_last_launch_count(void);
 

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 
+#include <mutex>
 #include <vector>
 
 #include "../../include/pyrh_gb300.h"
@@ -224,3 +225,132 @@ pyrh_status pyrh_nlte_emergent(const pyrh_nlte_batch* b, const pyrh_nlte_config*
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// Allocation-free variant of pyrh_nlte_solve.
+//
+// Some callers cannot call cudaMalloc: code that runs while another
+// component owns all device memory through its own pool, programs embedded
+// in hosts that forbid device allocation after start-up, and latency-bound
+// loops that cannot afford the implicit device synchronisation an
+// allocation may cause.  For them the solver's scratch (line profiles,
+// profile normalisation, second mean-intensity buffer, rate matrices, Ng
+// history, per-atmosphere state) lives in one fixed, file-scope device
+// array.  Every GPU that loads this library holds that array until the
+// process exits.
+// ------------------------------------------------------------------------
+
+static __device__ __align__(256) unsigned char g_nlte_static_scratch[PYRH_NLTE_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+constexpr int kMaxStaticAtm = 256;
+void* g_static_ptr[kMaxDevices] = {nullptr};
+std::mutex g_static_mu;
+
+// Device address of the static scratch on the current device.  The first
+// call on each device looks the symbol up (with that device current); the
+// host-side name of the array is not a device address and is never passed
+// to a kernel.
+cudaError_t static_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_nlte_static_scratch);
+    if (e != cudaSuccess) return e;
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch* b,
+                                              const pyrh_nlte_config* cfg, int64_t phi_elems,
+                                              int32_t* iterations, double* dpops, void* stream) {
+  pyrh::set_launches(0);
+  pyrh_status s = check(b, cfg);
+  if (s != PYRH_OK) return s;
+  if (b->natm > kMaxStaticAtm) {
+    pyrh::set_error("pyrh_nlte_solve_static: %d atmospheres exceed the limit of %d", b->natm,
+                    kMaxStaticAtm);
+    return PYRH_ERR_ARG;
+  }
+  const Layout L = layout(b, cfg);
+  const size_t r = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
+  const size_t need = L.fixed + r * (size_t)(phi_elems > 0 ? phi_elems : 1);
+  if (need > (size_t)PYRH_NLTE_STATIC_SCRATCH_BYTES) {
+    pyrh::set_error("pyrh_nlte_solve_static: batch needs %zu bytes of scratch, the static "
+                    "scratch holds %zu (PYRH_NLTE_STATIC_SCRATCH_BYTES)",
+                    need, (size_t)PYRH_NLTE_STATIC_SCRATCH_BYTES);
+    return PYRH_ERR_ARG;
+  }
+  const size_t smem = pyrh::nlte_formal_smem(b->nlevel, b->max_ndep, cfg->precision);
+  if (smem > 220 * 1024) {
+    pyrh::set_error("shared memory %zu B for %d levels x %d depths", smem, b->nlevel, b->max_ndep);
+    return PYRH_ERR_UNSUPPORTED;
+  }
+  void* ws = nullptr;
+  cudaError_t e = static_scratch(&ws);
+  if (e != cudaSuccess) {
+    pyrh::set_error("pyrh_nlte_solve_static: static scratch lookup: %s", cudaGetErrorString(e));
+    return PYRH_ERR_CUDA;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  pyrh::NlteArgs A = make_args(b, cfg, ws, need, L);
+  // The array keeps the previous call's contents; the error word is the
+  // only part a kernel reads before this call writes it, so it alone is
+  // cleared (the kernels write profiles, rate matrices, Ng history and
+  // per-atmosphere state before reading them, as in pyrh_nlte_solve, whose
+  // workspace also arrives uninitialised).
+  e = cudaMemsetAsync(A.err, 0, sizeof(int32_t), st);
+  int launches = 1;
+  if (e == cudaSuccess) e = pyrh::nlte_launch_ng_init(A, b->natm, st), ++launches;
+  const int64_t max_elems = (int64_t)b->max_nspect * 2 * cfg->nrays * b->max_ndep;
+  if (e == cudaSuccess)
+    e = pyrh::nlte_launch_profiles(A, b->natm, max_elems, cfg->precision, st), launches += 2;
+  int32_t active[kMaxStaticAtm];
+  for (int it = 0; e == cudaSuccess && it < cfg->nmax_iter; ++it) {
+    e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision, st);
+    launches += 5;
+    if (e != cudaSuccess) break;
+    e = cudaMemcpyAsync(active, A.active, sizeof(int32_t) * b->natm, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    bool any = false;
+    for (int p = 0; p < b->natm; ++p) any |= active[p] != 0;
+    if (!any) break;
+  }
+  int32_t err = 0;
+  double dp[kMaxStaticAtm];
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&err, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && iterations)
+    e = cudaMemcpyAsync(iterations, A.iters, sizeof(int32_t) * b->natm, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess && dpops)
+    e = cudaMemcpyAsync(dpops, A.dpops, sizeof(double) * b->natm, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dp, A.dpops, sizeof(double) * b->natm, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  pyrh::set_launches(launches);
+  if (e != cudaSuccess) {
+    pyrh::set_error("pyrh_nlte_solve_static: %s", cudaGetErrorString(e));
+    return PYRH_ERR_CUDA;
+  }
+  if (err) {
+    pyrh::set_error(err & 2 ? "an atmosphere's ndep exceeds max_ndep or the depth limit"
+                            : "line profiles do not fit the static scratch (phi_off beyond phi_elems)");
+    return PYRH_ERR_ARG;
+  }
+  for (int p = 0; p < b->natm; ++p)
+    if (!(dp[p] < cfg->iter_limit)) {
+      pyrh::set_error("atmosphere %d not converged after %d iterations (dpops %g)", p,
+                      cfg->nmax_iter, dp[p]);
+      return PYRH_ERR_NONCONVERGED;
+    }
+  return PYRH_OK;
+}
