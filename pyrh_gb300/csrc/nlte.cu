@@ -239,8 +239,9 @@ struct NlteOpacity {
   double lam;
   const double* lamp;     // spectrum of this atmosphere
 
-  // total opacity and source function at depth k, plus the atom's emissivity
-  __device__ __forceinline__ void operator()(int k, R& chi, R& S, double& eta_atom,
+  // Total opacity, source function and the background part of the source
+  // function (eta_c + sca_c J) / chi at depth k, plus the atom's emissivity.
+  __device__ __forceinline__ void operator()(int k, R& chi, R& S, R& S_bg, double& eta_atom,
                                              double Jold) const {
     const pyrh_nlte_batch& b = A->b;
     double chi_a = 0.0, eta_a = 0.0;
@@ -264,9 +265,17 @@ struct NlteOpacity {
     }
     const int64_t c = coff + (int64_t)k * ns + la;
     const double ct = chi_a + b.chi_c[c];
+    const double eta_bg = b.eta_c[c] + b.sca_c[c] * Jold;
     chi = R(ct);
-    S = R((eta_a + b.eta_c[c] + b.sca_c[c] * Jold) / ct);
+    S = R((eta_a + eta_bg) / ct);
+    S_bg = R(eta_bg / ct);
     eta_atom = eta_a;
+  }
+
+  __device__ __forceinline__ void operator()(int k, R& chi, R& S, double& eta_atom,
+                                             double Jold) const {
+    R S_bg;
+    (*this)(k, chi, S, S_bg, eta_atom, Jold);
   }
 };
 
@@ -281,19 +290,27 @@ struct JRow {
 
 template <typename R, typename Op>
 __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, double B0, double B1,
-                            const JRow& Jold, R* I, R* Psi) {
+                            const JRow& Jold, R* I, R* Psi, R* Ieff) {
+  // Ieff[k] = I[k] - Psi[k] * S_atom[k], the effective intensity of the
+  // MALI rates (fillgamma.c:121-134), is built term by term in the same
+  // recurrence: the local source enters through S_bg = S - S_atom only, so
+  // no difference of two nearly equal intensities is ever formed.  In
+  // optically thick line cores I and Psi*S_atom agree to many digits, and
+  // forming their difference from single-precision I and Psi would lose
+  // all of them.
   const int dk = to_obs ? -1 : 1, k_start = to_obs ? nd - 1 : 0, k_end = to_obs ? 0 : nd - 1;
   double ea;
-  R chi_u, chi_c, chi_d, chi_dd, S_u, S_c, S_d, S_dd = 0;
-  op(k_start, chi_u, S_u, ea, Jold[k_start]);
-  op(k_start + dk, chi_c, S_c, ea, Jold[k_start + dk]);
-  op(k_start + 2 * dk, chi_d, S_d, ea, Jold[k_start + 2 * dk]);
+  R chi_u, chi_c, chi_d, chi_dd, S_u, S_c, S_d, S_dd = 0, Sb_u, Sb_c, Sb_d, Sb_dd = 0;
+  op(k_start, chi_u, S_u, Sb_u, ea, Jold[k_start]);
+  op(k_start + dk, chi_c, S_c, Sb_c, ea, Jold[k_start + dk]);
+  op(k_start + 2 * dk, chi_d, S_d, Sb_d, ea, Jold[k_start + 2 * dk]);
   // interval path length between depth a and a+1 is ds[a+1]
   auto dsi = [&](int a, int b2) { return ds[a > b2 ? a : b2]; };
   const R dtau0 = R(0.5) * (chi_u + chi_c) * dsi(k_start, k_start + dk);
   R I_upw = to_obs ? R(B1 - (B0 - B1) / (double)dtau0) : R(0);
   I[k_start] = I_upw;
   Psi[k_start] = R(0);
+  Ieff[k_start] = I_upw;
   int k = k_start + dk;
   R dsup = dsi(k, k - dk), dsdn = dsi(k + dk, k);
   R dchi_up = (chi_c - chi_u) / dsup;
@@ -306,7 +323,7 @@ __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, doubl
     dsdn = dsi(k + dk, k);
     R dchi_dn;
     if (abs(k - k_end) > 1) {
-      op(k + 2 * dk, chi_dd, S_dd, ea, Jold[k + 2 * dk]);
+      op(k + 2 * dk, chi_dd, S_dd, Sb_dd, ea, Jold[k + 2 * dk]);
       dchi_dn = cent_deriv<R>(dsdn, dsi(k + 2 * dk, k + dk), chi_c, chi_d, chi_dd);
     } else {
       dchi_dn = (chi_d - chi_c) / dsdn;
@@ -318,12 +335,18 @@ __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, doubl
     R alpha, beta, gamma, theta, eps;
     bezier3_coeffs(dtau_uw, alpha, beta, gamma, theta, eps);
     const R dS_c = cent_deriv<R>(dtau_uw, dtau_dw, S_u, S_c, S_d);
-    c1 = fmax(S_c - dt03 * dS_c, R(0));
+    const R c1_raw = S_c - dt03 * dS_c;
+    c1 = fmax(c1_raw, R(0));
     c2 = fmax(S_u + dt03 * dS_up, R(0));
-    I_upw = I_upw * eps + alpha * S_c + beta * S_u + gamma * c1 + theta * c2;
+    // control point minus S_atom: S_bg - dt03 dS_c, or -S_atom where it clips
+    const R c1_eff = c1_raw > R(0) ? Sb_c - dt03 * dS_c : Sb_c - S_c;
+    const R upw = I_upw * eps + beta * S_u + theta * c2;
+    Ieff[k] = upw + alpha * Sb_c + gamma * c1_eff;
+    I_upw = upw + alpha * S_c + gamma * c1;
     I[k] = I_upw;
     Psi[k] = alpha + gamma;
     S_u = S_c; S_c = S_d; S_d = S_dd;
+    Sb_u = Sb_c; Sb_c = Sb_d; Sb_d = Sb_dd;
     chi_u = chi_c; chi_c = chi_d; chi_d = chi_dd;
     dchi_c = dchi_dn;
     dtau_uw = dtau_dw;
@@ -336,6 +359,7 @@ __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, doubl
   const R dS_uw = -(S_c - S_u) / R(dtau);
   I[k] = (R(1) - R(w[0])) * I_upw + R(w[0]) * S_c + R(w[1]) * dS_uw;
   Psi[k] = R(w[0] - w[1] / dtau);
+  Ieff[k] = (R(1) - R(w[0])) * I_upw + R(w[0]) * Sb_c + R(w[1]) * ((S_u - Sb_c) / R(dtau));
 }
 
 // Feautrier (feautrier.c:56-202) with P and Psi at every depth; chi and S
@@ -437,7 +461,7 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
     const double B0 = planck(b.T[doff + nd - 2], lam), B1 = planck(b.T[doff + nd - 1], lam);
     const JRow Jold{b.J + coff + la, ns};
     const bool angle_dep = A.moving && (as.bb || b.bgline[b.lam_off[p] + la]);
-    R I[PYRH_NLTE_MAX_DEPTH], Psi[PYRH_NLTE_MAX_DEPTH];
+    R I[PYRH_NLTE_MAX_DEPTH], Psi[PYRH_NLTE_MAX_DEPTH], Ieff[PYRH_NLTE_MAX_DEPTH];
     NlteOpacity<R> op;
     op.A = &A; op.tr = tr; op.as = &as; op.n_s = n_s; op.nstar_s = nst_s;
     op.nd = nd; op.ns = ns; op.la = la; op.nlev = nlev; op.doff = doff; op.coff = coff;
@@ -450,7 +474,7 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
       R emergent;
       if (angle_dep) {
         if (emergent_only && !to_obs) continue;
-        bezier_full<R>(op, dsl, nd, to_obs, B0, B1, Jold, I, Psi);
+        bezier_full<R>(op, dsl, nd, to_obs, B0, B1, Jold, I, Psi, Ieff);
         wdir = 0.5 * A.wmu[ray];
         emergent = I[0];
       } else {
@@ -473,7 +497,7 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
         atomicAdd(&Js[k * 32 + lane], wdir * (double)I[k]);
         if (!eval_operator) continue;
         const double psi = (double)Psi[k] / (double)chi_k;
-        const double Ieff = (double)I[k] - psi * eta_atom;
+        const double Ieff_k = angle_dep ? (double)Ieff[k] : (double)I[k] - psi * eta_atom;
         double V[PYRH_NLTE_MAX_ACTIVE], G[PYRH_NLTE_MAX_ACTIVE], W[PYRH_NLTE_MAX_ACTIVE],
             TW[PYRH_NLTE_MAX_ACTIVE];
         for (int m = 0; m < as.n; ++m) {
@@ -510,8 +534,8 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
             if (u.j == i) { U_down_i += TW[q] * G[q] * V[q]; i_is_upper = true; }
           }
           const double wlamu = V[m] * W[m] * wdir;
-          double gji = Ieff * wlamu;
-          double gij = (TW[m] + Ieff) * G[m] * wlamu - chi_up_i * psi * U_down_j * wdir;
+          double gji = Ieff_k * wlamu;
+          double gij = (TW[m] + Ieff_k) * G[m] * wlamu - chi_up_i * psi * U_down_j * wdir;
           if (i_is_upper) {
             // one term per active transition whose upper level is i
             int cnt = 0;

@@ -4,11 +4,15 @@ golden populations and emergent intensities.
 
 Tolerances (relative, element-wise):
   FP64: populations and emergent intensity vs reference   1e-6
-  FP32 formal solution (FP64 rates, LU, Ng):               2e-3
-The FP32 bound is measured, not designed: the MALI effective intensity
-I - Psi*eta of fillgamma.c:121-134 cancels to a small difference in
-optically thick line cores, so single-precision I and Psi (relative error
-~1e-6) move the rates there by up to ~1e-3.  FP64 is the parity mode.
+  FP32 formal solution (FP64 rates, LU, Ng):               1e-3
+The FP32 bound is measured, not designed: single-precision I and Psi change
+the path of the iteration (a few more or fewer iterations, a different Ng
+extrapolation), so the FP32 run stops at a different point inside the same
+convergence limit of 1e-4; measured errors of the converged populations are
+0.8e-4 to 3.5e-4 on these atmospheres.  The MALI effective intensity
+I - Psi*eta of fillgamma.c:121-134 is formed without cancellation inside the
+Bezier recurrence; formed as a difference it cost up to 2e-3 in optically
+thick line cores.  FP64 is the parity mode.
 """
 import numpy as np
 import pytest
@@ -64,10 +68,10 @@ def test_converged_fp32(golden):
     fx = golden("nlte_c1")
     dev, cfg, st = _solve([fx], L.PYRH_FP32)
     assert st == L.PYRH_OK, L.lib().pyrh_last_error()
-    assert _rel(dev.populations()[0], fx["n_final"]) < 2e-3
+    assert _rel(dev.populations()[0], fx["n_final"]) < 1e-3
     assert dev.emergent(cfg, float(fx["fmeta"][2])) == L.PYRH_OK
     m = O.output_mask(fx["lambda"], fx["fmeta"][1])
-    assert _rel(dev.emergent_spectra()[0][m], fx["I_out"]) < 2e-3
+    assert _rel(dev.emergent_spectra()[0][m], fx["I_out"]) < 1e-3
 
 
 def test_ragged_batch_fp64(golden):

@@ -10,10 +10,9 @@ and Ng acceleration amplifies those last-digit differences (FP64 runs differ
 by ~1e-8 relative in the populations).  So the comparison uses the solver's
 own parity tolerances: FP64 populations and J within 1e-6 relative of the
 workspace solve and of the reference's converged populations, with identical
-iteration counts; FP32 populations and J within 2e-3 (single-precision I and
-Psi move the rates in optically thick line cores by up to ~1e-3, and the
-iteration count there depends on where that noise crosses the convergence
-limit).  The file name sorts last so that the static array is first touched
+iteration counts; FP32 populations and J within 1e-3 (single-precision I and
+Psi change the iteration's path, so two FP32 runs may stop at different
+iterations inside the same convergence limit).  The file name sorts last so that the static array is first touched
 after every other test's allocations."""
 import ctypes as C
 
@@ -26,7 +25,7 @@ from pyrh_gb300 import nlte
 pytestmark = pytest.mark.gpu
 
 STATIC_BYTES = 32 * 1024 * 1024
-TOL = {L.PYRH_FP64: 1e-6, L.PYRH_FP32: 2e-3}
+TOL = {L.PYRH_FP64: 1e-6, L.PYRH_FP32: 1e-3}
 
 
 def _bind():
