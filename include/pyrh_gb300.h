@@ -146,6 +146,49 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch *host_batch,
                                  const pyrh_line *host_lines, int32_t nline,
                                  const pyrh_lte_config *cfg, void *host_stokes_out);
 
+/* ------------------------------------------------------- response functions
+ * Depth-resolved response functions of the emergent Stokes vector of
+ * pyrh_lte_stokes to the atmosphere at every depth, and the gradient of a
+ * weighted chi^2, by a hand-written adjoint of the DELO-Bezier3 recurrence
+ * and of the Zeeman/Voigt opacity.  The reference computes the same
+ * derivatives by finite differences of whole syntheses (rh/rhf1d/
+ * rf_ray.c:205-293, perturbing T, v, v_turb, B, gamma, chi per depth); its
+ * only analytical response functions are for log gf (rh/rhf1d/
+ * bezier_1D.c:416-490).  Parameters, in this order and in the units of
+ * pyrh_lte_batch: T [K], v_los [m/s], v_mic [m/s], B [T], gamma_B [rad],
+ * chi_B [rad].  The continuum (chi_c, eta_c), stage densities and the
+ * height scale are held fixed.  Every wavelength is solved with
+ * DELO-Bezier3 (the reference's solver wherever a polarizable line covers
+ * the wavelength); FULL_STOKES without magneto-optical terms only. */
+#define PYRH_RF_NPARAM    6
+#define PYRH_RF_MAX_DEPTH 160
+
+/* rf_out (float or double following the precision): for atmosphere p,
+   entries [24 * cont_off[p], 24 * (cont_off[p] + ndep[p] * nlam[p])) laid
+   out [stokes][param][depth][lambda] (lambda fastest): dS_s(lambda)/dx(k).
+   stokes_out receives the emergent Stokes vectors as for pyrh_lte_stokes. */
+pyrh_status pyrh_lte_rf(const pyrh_lte_batch *batch, const pyrh_line *lines, int32_t nline,
+                        const pyrh_lte_config *cfg, void *stokes_out, void *rf_out,
+                        void *stream);
+
+/* chi2[p] = sum over lambda and s of weights * (S_s(lambda) - obs)^2, with
+   obs and weights laid out like stokes_out; grad_out is [6][total_depth]
+   (d chi2[p] / d x(k) at param * total_depth + depth_off[p] + k).  chi2_out
+   ([natm]) and grad_out are overwritten. */
+pyrh_status pyrh_lte_chi2_grad(const pyrh_lte_batch *batch, const pyrh_line *lines,
+                               int32_t nline, const pyrh_lte_config *cfg, const void *obs,
+                               const void *weights, void *stokes_out, void *chi2_out,
+                               void *grad_out, void *stream);
+
+/* Vector-Jacobian product: grad_out[x * total_depth + depth_off[p] + k] =
+   sum over lambda and s of dL_dstokes * dS_s(lambda)/dx(k), with dL_dstokes
+   laid out like stokes_out (the adjoint a reverse-mode framework calls with
+   the upstream gradient).  grad_out is overwritten. */
+pyrh_status pyrh_lte_stokes_vjp(const pyrh_lte_batch *batch, const pyrh_line *lines,
+                                int32_t nline, const pyrh_lte_config *cfg,
+                                const void *dL_dstokes, void *stokes_out, void *grad_out,
+                                void *stream);
+
 /* ------------------------------------------------------------------ NLTE
  * MALI lambda iteration for one active atom per atmosphere, replacing the
  * reference's Iterate() (rh/iterate.c:48-143) with its solveSpectrum() /

@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpyrh_gb300.so")
-UNITS = ["capi.cu", "lte_stokes.cu", "nlte.cu", "nlte_capi.cu"]
+UNITS = ["capi.cu", "lte_stokes.cu", "lte_rf.cu", "nlte.cu", "nlte_capi.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

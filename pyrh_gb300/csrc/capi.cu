@@ -156,6 +156,54 @@ pyrh_status launch(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nline,
   return PYRH_OK;
 }
 
+pyrh_status check_rf(const pyrh_lte_batch* b, const pyrh_lte_config* cfg, int nline,
+                     const pyrh_line* lines) {
+  pyrh_status s = check_cfg(cfg);
+  if (s != PYRH_OK) return s;
+  s = check_batch_shape(b, nline);
+  if (s != PYRH_OK) return s;
+  if (nline > 0 && !lines) return fail(PYRH_ERR_ARG, "lines is NULL");
+  if (cfg->stokes_mode != PYRH_FULL_STOKES || cfg->magneto_optical)
+    return fail(PYRH_ERR_UNSUPPORTED,
+                "response functions need FULL_STOKES without magneto-optical terms");
+  if (b->max_ndep > PYRH_RF_MAX_DEPTH)
+    return fail(PYRH_ERR_UNSUPPORTED, "max_ndep %d above PYRH_RF_MAX_DEPTH %d", b->max_ndep,
+                PYRH_RF_MAX_DEPTH);
+  if (cfg->block_lambda > 128)
+    return fail(PYRH_ERR_ARG, "block_lambda %d above 128 for response functions",
+                cfg->block_lambda);
+  return PYRH_OK;
+}
+
+pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nline,
+                      const pyrh_lte_config* cfg, int mode, const void* obs, const void* weights,
+                      void* stokes_out, void* rf, void* chi2, void* grad, cudaStream_t st) {
+  const int block = cfg->block_lambda > 0 ? cfg->block_lambda : 128;
+  pyrh::RfArgs ra;
+  ra.lte = make_args(b, d_lines, nline, cfg, stokes_out, block);
+  ra.mode = mode;
+  ra.obs = obs;
+  ra.weights = weights;
+  ra.rf = rf;
+  ra.chi2 = chi2;
+  ra.grad = grad;
+  const size_t smem = pyrh::rf_smem_bytes(cfg->precision, nline, ra.lte.maxd);
+  if (smem > 200 * 1024)
+    return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
+                nline, ra.lte.maxd);
+  const long long work = (long long)ra.lte.natm * ra.lte.tiles;
+  int grid = cfg->persistent_blocks;
+  if (grid <= 0) {
+    int per_sm = pyrh::rf_blocks_per_sm(cfg->precision, mode, block, smem);
+    if (per_sm < 1) per_sm = 1;
+    grid = sm_count() * per_sm;
+  }
+  if (grid > work) grid = (int)work;
+  cudaError_t e = pyrh::launch_lte_rf(ra, block, grid, st);
+  if (e != cudaSuccess) return fail(PYRH_ERR_CUDA, "lte_rf launch: %s", cudaGetErrorString(e));
+  return PYRH_OK;
+}
+
 // Workspace of the host-buffer entry point.
 struct HostWs {
   std::mutex mu;
@@ -208,6 +256,56 @@ pyrh_status pyrh_lte_stokes(const pyrh_lte_batch* batch, const pyrh_line* lines,
   // would synchronise the stream); pyrh_check_lines validates a host copy,
   // and the kernel clamps component counts to PYRH_MAX_COMPONENTS.
   return launch(batch, lines, nline, cfg, stokes_out, (cudaStream_t)stream);
+}
+
+pyrh_status pyrh_lte_rf(const pyrh_lte_batch* batch, const pyrh_line* lines, int32_t nline,
+                        const pyrh_lte_config* cfg, void* stokes_out, void* rf_out,
+                        void* stream) {
+  g_last_launches = 0;
+  pyrh_status s = check_rf(batch, cfg, nline, lines);
+  if (s != PYRH_OK) return s;
+  if (!stokes_out || !rf_out) return fail(PYRH_ERR_ARG, "stokes_out or rf_out is NULL");
+  s = launch_rf(batch, lines, nline, cfg, 0, nullptr, nullptr, stokes_out, rf_out, nullptr,
+                nullptr, (cudaStream_t)stream);
+  if (s == PYRH_OK) g_last_launches = 1;
+  return s;
+}
+
+pyrh_status pyrh_lte_chi2_grad(const pyrh_lte_batch* batch, const pyrh_line* lines,
+                               int32_t nline, const pyrh_lte_config* cfg, const void* obs,
+                               const void* weights, void* stokes_out, void* chi2_out,
+                               void* grad_out, void* stream) {
+  g_last_launches = 0;
+  pyrh_status s = check_rf(batch, cfg, nline, lines);
+  if (s != PYRH_OK) return s;
+  if (!obs || !weights || !stokes_out || !chi2_out || !grad_out)
+    return fail(PYRH_ERR_ARG, "obs, weights, stokes_out, chi2_out or grad_out is NULL");
+  const size_t real = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(cudaMemsetAsync(chi2_out, 0, real * batch->natm, st));
+  CUDA_TRY(cudaMemsetAsync(grad_out, 0, real * PYRH_RF_NPARAM * batch->total_depth, st));
+  s = launch_rf(batch, lines, nline, cfg, 1, obs, weights, stokes_out, nullptr, chi2_out, grad_out,
+                st);
+  if (s == PYRH_OK) g_last_launches = 1;
+  return s;
+}
+
+pyrh_status pyrh_lte_stokes_vjp(const pyrh_lte_batch* batch, const pyrh_line* lines,
+                                int32_t nline, const pyrh_lte_config* cfg,
+                                const void* dL_dstokes, void* stokes_out, void* grad_out,
+                                void* stream) {
+  g_last_launches = 0;
+  pyrh_status s = check_rf(batch, cfg, nline, lines);
+  if (s != PYRH_OK) return s;
+  if (!dL_dstokes || !stokes_out || !grad_out)
+    return fail(PYRH_ERR_ARG, "dL_dstokes, stokes_out or grad_out is NULL");
+  const size_t real = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
+  cudaStream_t st = (cudaStream_t)stream;
+  CUDA_TRY(cudaMemsetAsync(grad_out, 0, real * PYRH_RF_NPARAM * batch->total_depth, st));
+  s = launch_rf(batch, lines, nline, cfg, 2, nullptr, dL_dstokes, stokes_out, nullptr, nullptr,
+                grad_out, st);
+  if (s == PYRH_OK) g_last_launches = 1;
+  return s;
 }
 
 pyrh_status pyrh_check_lines(const pyrh_line* host_lines, int32_t nline, int32_t stokes_mode) {

@@ -1,0 +1,326 @@
+// lte_rf.cu -- response functions and chi^2 gradient of the LTE Stokes
+// synthesis on the GPU.
+//
+// One thread owns one (atmosphere, wavelength) pair, as in lte_stokes.cu.
+// Per block (one atmosphere, one tile of wavelengths) the per-(line, depth)
+// quantities and the projected field geometry are computed once, with their
+// derivatives with respect to (T, v_los, v_mic, B, gamma, chi) of the same
+// depth, into shared memory (forward-mode dual numbers, lte_rf.cuh).  Each
+// thread then
+//   1. evaluates the optical quantities q_k = (chi, S_I..S_V, K'_Q..K'_V) of
+//      its wavelength at every depth and runs the DELO-Bezier3 recurrence
+//      (bezier_1D.c:52-300) to the surface, keeping the recurrence state on a
+//      thread-private tape (local memory; depth-major, so the tape words of a
+//      warp's threads are interleaved and coalesce);
+//   2. runs the hand-written adjoint of that recurrence back down
+//      (delo_reverse_stream), which hands over dL/dq_k as soon as depth k is
+//      final;
+//   3. at each handed-over depth, re-evaluates q_k with its dual numbers to
+//      get dq_k/dx_k and writes dL/dx_k: for response functions the four
+//      Stokes seeds give RF[s][x][k] (written wavelength-fastest, coalesced);
+//      for the chi^2 gradient the single seed 2 w (S - obs), and for a
+//      vector-Jacobian product the caller's dL/dS, give one value per
+//      (x, k), summed over the block's wavelengths in shared memory and then
+//      added to the atmosphere's gradient in HBM.
+// The local Jacobian is recomputed, not stored, so the tape holds 21 values
+// per depth; four depths of adjoints are live at a time.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pyrh_gb300.h"
+#include "lte_rf.cuh"
+#include "lte_stokes.cuh"
+
+namespace pyrh {
+
+namespace {
+
+template <typename R>
+struct RfSmem {
+  LineDepth<R>* ld;   // [nline][maxd]
+  GeoD<R>* geo;       // [maxd]
+  R* ds;              // [maxd]
+  R* cshift;          // [nline][PYRH_MAX_COMPONENTS]
+  R* cweight;
+  int* cq;
+  int* ncomp;         // [nline]
+  int* contrib;       // [nline]
+  int* polar;         // [nline]
+  double* lam0;       // [nline]
+  R* grad;            // [kNX][maxd] (chi^2 mode)
+  R* chi2;            // [1]
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+template <typename R>
+__host__ __device__ size_t rf_smem_t(int nline, int maxd, RfSmem<R>* s, unsigned char* base) {
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char* p = base ? base + off : nullptr;
+    off = align16(off + bytes);
+    return p;
+  };
+  unsigned char* p;
+  p = take(sizeof(LineDepth<R>) * nline * maxd); if (s) s->ld = reinterpret_cast<LineDepth<R>*>(p);
+  p = take(sizeof(GeoD<R>) * maxd);              if (s) s->geo = reinterpret_cast<GeoD<R>*>(p);
+  p = take(sizeof(R) * maxd);                    if (s) s->ds = reinterpret_cast<R*>(p);
+  p = take(sizeof(R) * nline * PYRH_MAX_COMPONENTS);   if (s) s->cshift = reinterpret_cast<R*>(p);
+  p = take(sizeof(R) * nline * PYRH_MAX_COMPONENTS);   if (s) s->cweight = reinterpret_cast<R*>(p);
+  p = take(sizeof(int) * nline * PYRH_MAX_COMPONENTS); if (s) s->cq = reinterpret_cast<int*>(p);
+  p = take(sizeof(int) * nline);                 if (s) s->ncomp = reinterpret_cast<int*>(p);
+  p = take(sizeof(int) * nline);                 if (s) s->contrib = reinterpret_cast<int*>(p);
+  p = take(sizeof(int) * nline);                 if (s) s->polar = reinterpret_cast<int*>(p);
+  p = take(sizeof(double) * nline);              if (s) s->lam0 = reinterpret_cast<double*>(p);
+  p = take(sizeof(R) * kNX * maxd);              if (s) s->grad = reinterpret_cast<R*>(p);
+  p = take(sizeof(R) * 4);                       if (s) s->chi2 = reinterpret_cast<R*>(p);
+  return off;
+}
+
+template <typename R>
+__device__ D6<R> to_r(const D6<double>& a) {
+  D6<R> o;
+  o.v = R(a.v);
+#pragma unroll
+  for (int i = 0; i < kNX; ++i) o.d[i] = R(a.d[i]);
+  return o;
+}
+
+// What one thread needs to evaluate q and dq/dx at any depth.
+template <typename R>
+struct Local {
+  const RfSmem<R>* sm;
+  int nline, maxd, nl;
+  unsigned inwin;
+  R dlam[PYRH_MAX_LINES];
+  const R* chi_c;   // continuum of this (atmosphere, wavelength): index k * nl
+  const R* eta_c;
+};
+
+template <typename R, int MODE>
+struct Emit {
+  const Local<R>* loc;
+  const double* T;   // temperatures of this atmosphere
+  double lam;
+  int nd, nl, la;
+  R* rf;             // mode 0: rf_out + 24 * cont_off + la
+  __device__ void operator()(int k, const R* qb, const R* bpl) const {
+    constexpr int NS = MODE == 0 ? 4 : 1;
+    const RfSmem<R>& sm = *loc->sm;
+    R q[8], J[8][kNX];
+    local_q_jac<R>(loc->nline, sm.ld + k, loc->maxd, sm.geo[k], loc->dlam, loc->inwin, sm.ncomp,
+                   sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS, loc->chi_c[(int64_t)k * nl],
+                   loc->eta_c[(int64_t)k * nl], q, J);
+    const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lam)) : R(0);
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+#pragma unroll
+      for (int x = 0; x < kNX; ++x) {
+        R v = 0;
+#pragma unroll
+        for (int n = 0; n < 8; ++n) v += qb[s * 8 + n] * J[n][x];
+        if (x == 0) v += bpl[s] * dB;
+        if (MODE == 0) rf[((int64_t)(s * kNX + x) * nd + k) * nl] = v;
+        else atomicAdd(&sm.grad[x * loc->maxd + k], v);   // modes 1 and 2
+      }
+    }
+  }
+};
+
+template <typename R, int MODE>
+__global__ void __launch_bounds__(128) lte_rf_kernel(RfArgs ra) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const LteArgs& args = ra.lte;
+  const int nline = args.nline < PYRH_MAX_LINES ? args.nline : PYRH_MAX_LINES;
+  RfSmem<R> sm;
+  rf_smem_t<R>(nline, args.maxd, &sm, smem_raw);
+  const int BL = blockDim.x;
+
+  for (int i = threadIdx.x; i < nline * PYRH_MAX_COMPONENTS; i += BL) {
+    const int l = i / PYRH_MAX_COMPONENTS, c = i % PYRH_MAX_COMPONENTS;
+    const pyrh_line& L = args.lines[l];
+    sm.cshift[i] = R(L.comp_shift[c]);
+    sm.cweight[i] = R(L.comp_strength[c]);
+    sm.cq[i] = L.comp_q[c];
+  }
+  for (int l = threadIdx.x; l < nline; l += BL) {
+    const pyrh_line& L = args.lines[l];
+    const int nc = L.ncomp < 0 ? 0 : (L.ncomp > PYRH_MAX_COMPONENTS ? PYRH_MAX_COMPONENTS : L.ncomp);
+    sm.ncomp[l] = L.polarizable ? nc : 0;
+    sm.polar[l] = L.polarizable;
+    sm.contrib[l] = L.contributes;
+    sm.lam0[l] = L.lambda0;
+  }
+
+  const double muz = args.mu, imu = 1.0 / args.mu;
+  const int64_t total = (int64_t)args.natm * args.tiles;
+  for (int64_t w = blockIdx.x; w < total; w += gridDim.x) {
+    const int p = (int)(w / args.tiles);
+    const int tile = (int)(w % args.tiles);
+    const int nl = args.nlam[p];
+    const int la0 = tile * BL;
+    if (la0 >= nl) continue;                 // uniform across the block
+    const int nd = args.ndep[p];
+    if (nd < 3 || nd > args.maxd) continue;  // uniform across the block
+    const int64_t doff = args.depth_off[p];
+    __syncthreads();  // shared tables of the previous work item are consumed
+
+    // ---- per-depth and per-(line, depth) values with derivatives ----
+    for (int k = threadIdx.x; k < nd; k += BL) {
+      const int64_t d = doff + k;
+      sm.ds[k] = (k >= 1) ? R(fabs(args.height[d] - args.height[d - 1]) * imu) : R(0);
+      const GeoD<double> g = geometry_d<double>(args.gamma_B[d], args.chi_B[d], muz);
+      GeoD<R> gr;
+      gr.gQ = to_r<R>(g.gQ); gr.gU = to_r<R>(g.gU); gr.gV = to_r<R>(g.gV); gr.s2g = to_r<R>(g.s2g);
+      sm.geo[k] = gr;
+      if (MODE != 0)
+        for (int x = 0; x < kNX; ++x) sm.grad[x * args.maxd + k] = R(0);
+    }
+    if (MODE == 1 && threadIdx.x == 0) sm.chi2[0] = R(0);
+    for (int i = threadIdx.x; i < nline * nd; i += BL) {
+      const int l = i / nd, k = i % nd;
+      const int64_t d = doff + k;
+      const pyrh_line& L = args.lines[l];
+      const LineConstD c = {L.lambda0, L.Ei, L.gi, L.Aji, L.Bji, L.Bij, L.Grad, L.GStark,
+                            L.GvdWaals, L.cross, L.alpha, L.isotope_frac, L.hyperfine_frac,
+                            L.weight, L.vdwaals};
+      const LineDepth<double> ld = line_depth<double>(
+          c, args.T[d], args.vlos[d], args.vturb[d], args.B[d], args.ne[d], args.nHtot[d],
+          args.np[d], args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d],
+          args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d], muz, args.moving != 0);
+      LineDepth<R> o;
+      o.inv_vb = to_r<R>(ld.inv_vb); o.vshift = to_r<R>(ld.vshift); o.adamp = to_r<R>(ld.adamp);
+      o.vB = to_r<R>(ld.vB); o.chil = to_r<R>(ld.chil); o.etal = to_r<R>(ld.etal);
+      o.gauss = ld.gauss;
+      sm.ld[l * args.maxd + k] = o;
+    }
+    __syncthreads();
+
+    const int la = la0 + threadIdx.x;
+    if (la < nl) {
+      const int64_t loff = args.lam_off[p];
+      const double lam = args.lambda[loff + la];
+      const double dlc = lam * kQ_WING * (args.vmicro_char / kCLIGHT);
+      Local<R> loc;
+      loc.sm = &sm;
+      loc.nline = nline;
+      loc.maxd = args.maxd;
+      loc.nl = nl;
+      loc.inwin = 0u;
+      for (int l = 0; l < nline; ++l) {
+        loc.dlam[l] = R(lam - sm.lam0[l]);
+        if (fabs(sm.lam0[l] - lam) <= dlc && sm.contrib[l]) loc.inwin |= 1u << l;
+      }
+      loc.chi_c = static_cast<const R*>(args.chi_c) + args.cont_off[p] + la;
+      loc.eta_c = static_cast<const R*>(args.eta_c) + args.cont_off[p] + la;
+
+      Tape<R> tp;
+      for (int k = 0; k < nd; ++k)
+        local_q<R>(nline, sm.ld + k, args.maxd, sm.geo[k], loc.dlam, loc.inwin, sm.ncomp,
+                   sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS,
+                   loc.chi_c[(int64_t)k * nl], loc.eta_c[(int64_t)k * nl], tp.q[k]);
+      const double B0 = planck(args.T[doff + nd - 2], lam);
+      const double B1 = planck(args.T[doff + nd - 1], lam);
+      R st[4];
+      delo_forward<R>(tp, sm.ds, nd, B0, B1, st);
+      R* out = static_cast<R*>(args.out) + 4 * loff;
+#pragma unroll
+      for (int s = 0; s < 4; ++s) out[(int64_t)s * nl + la] = st[s];
+
+      Emit<R, MODE> em;
+      em.loc = &loc;
+      em.T = args.T + doff;
+      em.lam = lam;
+      em.nd = nd;
+      em.nl = nl;
+      em.la = la;
+      if (MODE == 0) {
+        em.rf = static_cast<R*>(ra.rf) + 24 * args.cont_off[p] + la;
+        const R seed[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+        delo_reverse_stream<R, 4>(tp, sm.ds, nd, B0, B1, seed, em);
+      } else if (MODE == 2) {
+        em.rf = nullptr;
+        const R* dL = static_cast<const R*>(ra.weights) + 4 * loff;
+        R seed[1][4];
+#pragma unroll
+        for (int s = 0; s < 4; ++s) seed[0][s] = dL[(int64_t)s * nl + la];
+        delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
+      } else {
+        em.rf = nullptr;
+        const R* obs = static_cast<const R*>(ra.obs) + 4 * loff;
+        const R* wt = static_cast<const R*>(ra.weights) + 4 * loff;
+        R seed[1][4];
+        R c2 = 0;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+          const R wv = wt[(int64_t)s * nl + la];
+          const R r = st[s] - obs[(int64_t)s * nl + la];
+          seed[0][s] = R(2) * wv * r;
+          c2 += wv * r * r;
+        }
+        atomicAdd(sm.chi2, c2);
+        delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
+      }
+    }
+    if (MODE != 0) {
+      __syncthreads();
+      R* grad = static_cast<R*>(ra.grad);
+      for (int i = threadIdx.x; i < kNX * nd; i += BL) {
+        const int x = i / nd, k = i % nd;
+        atomicAdd(&grad[(int64_t)x * args.total_depth + doff + k], sm.grad[x * args.maxd + k]);
+      }
+      if (MODE == 1 && threadIdx.x == 0) atomicAdd(static_cast<R*>(ra.chi2) + p, sm.chi2[0]);
+    }
+  }
+}
+
+template <typename R, int MODE>
+cudaError_t launch_mode(const RfArgs& a, int block, int grid, size_t smem, cudaStream_t st) {
+  auto k = lte_rf_kernel<R, MODE>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k<<<grid, block, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename R, int MODE>
+int per_sm_mode(int block, size_t smem) {
+  int n = 0;
+  cudaFuncSetAttribute(lte_rf_kernel<R, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lte_rf_kernel<R, MODE>, block, smem);
+  return n;
+}
+
+}  // namespace
+
+size_t rf_smem_bytes(int precision, int nline, int maxd) {
+  return precision == PYRH_FP32 ? rf_smem_t<float>(nline, maxd, nullptr, nullptr)
+                                : rf_smem_t<double>(nline, maxd, nullptr, nullptr);
+}
+
+template <typename R>
+int per_sm_t(int mode, int block, size_t smem) {
+  if (mode == 0) return per_sm_mode<R, 0>(block, smem);
+  if (mode == 1) return per_sm_mode<R, 1>(block, smem);
+  return per_sm_mode<R, 2>(block, smem);
+}
+
+template <typename R>
+cudaError_t launch_t(const RfArgs& a, int block, int grid, size_t smem, cudaStream_t st) {
+  if (a.mode == 0) return launch_mode<R, 0>(a, block, grid, smem, st);
+  if (a.mode == 1) return launch_mode<R, 1>(a, block, grid, smem, st);
+  return launch_mode<R, 2>(a, block, grid, smem, st);
+}
+
+int rf_blocks_per_sm(int precision, int mode, int block, size_t smem) {
+  return precision == PYRH_FP32 ? per_sm_t<float>(mode, block, smem)
+                                : per_sm_t<double>(mode, block, smem);
+}
+
+cudaError_t launch_lte_rf(const RfArgs& a, int block, int grid, cudaStream_t st) {
+  const size_t smem = rf_smem_bytes(a.lte.precision, a.lte.nline, a.lte.maxd);
+  return a.lte.precision == PYRH_FP32 ? launch_t<float>(a, block, grid, smem, st)
+                                      : launch_t<double>(a, block, grid, smem, st);
+}
+
+}  // namespace pyrh

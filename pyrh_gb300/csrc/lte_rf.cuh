@@ -22,7 +22,12 @@
 // finite differences of the whole synthesis (rf_ray.c:205-293).
 #pragma once
 
+#include "../../include/pyrh_gb300.h"
 #include "rt_device.cuh"
+
+#ifndef PYRH_MAX_DEPTH_RF
+#define PYRH_MAX_DEPTH_RF PYRH_RF_MAX_DEPTH
+#endif
 
 namespace pyrh {
 
@@ -127,6 +132,9 @@ PYRH_HD D6<R> dsin(const D6<R>& a) {
 // ---------------------------------------------- Humlicek with derivative --
 // W(t) and dW/dt for t = a - i v, differentiating each region's rational
 // approximation exactly (so the derivative is that of the forward model).
+// Quotients of the form x / Q^2 divide by Q twice: |Q|^2 of the region-4
+// denominator reaches 1e21 near |v| = 5.5, and cdiv's |Q^2|^2 would
+// overflow single precision.
 template <typename R>
 PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
   const Cx<R> t = {a, -v};
@@ -137,7 +145,7 @@ PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
     Cx<R> t2 = cmul(t, t);
     Cx<R> den = {t2.r + R(0.5), t2.i};
     W = cdiv(Cx<R>{c0 * t.r, c0 * t.i}, den);
-    dW = cdiv(Cx<R>{c0 * (R(0.5) - t2.r), -c0 * t2.i}, cmul(den, den));
+    dW = cdiv(cdiv(Cx<R>{c0 * (R(0.5) - t2.r), -c0 * t2.i}, den), den);
   } else if (s >= R(5.5)) {
     // W = t (c1 u + c2) / (u (u + 3) + 3/4), u = t^2
     const R c1 = R(0.5641896), c2 = R(1.410474);
@@ -150,7 +158,7 @@ PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
     Cx<R> dD = cmul(Cx<R>{R(2) * u.r + R(3), R(2) * u.i}, Cx<R>{R(2) * t.r, R(2) * t.i});
     W = cdiv(N, D);
     Cx<R> num = cmul(dN, D), nd = cmul(N, dD);
-    dW = cdiv(Cx<R>{num.r - nd.r, num.i - nd.i}, cmul(D, D));
+    dW = cdiv(cdiv(Cx<R>{num.r - nd.r, num.i - nd.i}, D), D);
   } else if (a >= R(0.195) * fabs(v) - R(0.176)) {
     const R A[5] = {R(0.5642236), R(3.778987), R(11.96482), R(20.20933), R(16.4955)};
     const R B[5] = {R(6.699398), R(21.69274), R(39.27121), R(38.82363), R(16.4955)};
@@ -164,7 +172,7 @@ PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
     }
     W = cdiv(P, Q);
     Cx<R> x1 = cmul(dP, Q), x2 = cmul(P, dQ);
-    dW = cdiv(Cx<R>{x1.r - x2.r, x1.i - x2.i}, cmul(Q, Q));
+    dW = cdiv(cdiv(Cx<R>{x1.r - x2.r, x1.i - x2.i}, Q), Q);
   } else {
     // W = exp(t^2) - t P(u) / Q(u), u = -t^2
     const R A[7] = {R(0.56419), R(1.320522), R(35.7668), R(219.031), R(1540.787), R(3321.99), R(36183.31)};
@@ -186,7 +194,7 @@ PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
     W = {E.r - tr.r, E.i - tr.i};
     // d/dt [t P/Q] = P/Q + t (P'Q - PQ')/Q^2 * du/dt,  du/dt = -2t
     Cx<R> x1 = cmul(dP, Q), x2 = cmul(P, dQ);
-    Cx<R> dr = cdiv(Cx<R>{x1.r - x2.r, x1.i - x2.i}, cmul(Q, Q));
+    Cx<R> dr = cdiv(cdiv(Cx<R>{x1.r - x2.r, x1.i - x2.i}, Q), Q);
     Cx<R> tdr = cmul(cmul(t, dr), Cx<R>{R(-2) * t.r, R(-2) * t.i});
     Cx<R> dE = cmul(E, Cx<R>{R(2) * t.r, R(2) * t.i});
     dW = {dE.r - r.r - tdr.r, dE.i - r.i - tdr.i};
@@ -283,14 +291,16 @@ PYRH_HD GeoD<R> geometry_d(R gam, R chb, R muz) {
 // dq/dx at one depth for one wavelength (kurucz.c:669-715, formal.c:178-208,
 // stokesopac.c:47-79), MAGNETO_OPTICAL off.  comp_* are the Zeeman tables
 // of each line (q index 0..2 for Ml - Mu = -1, 0, +1).
+// Line l's quantities at this depth are ld[l * ld_stride].
 template <typename R>
-PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, const GeoD<R>& geo, const R* dlam,
-                         unsigned inwin, const int* ncomp, const R* cshift, const R* cweight,
-                         const int* cq, int maxcomp, R chi_c, R eta_c, R q[8], R J[8][kNX]) {
+PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
+                         const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
+                         const R* cweight, const int* cq, int maxcomp, R chi_c, R eta_c, R q[8],
+                         R J[8][kNX]) {
   D6<R> cI = dconst(R(0)), cQ = cI, cU = cI, cV = cI, eI = cI, eQ = cI, eU = cI, eV = cI;
   for (int l = 0; l < nline; ++l) {
     if (!((inwin >> l) & 1u)) continue;
-    const LineDepth<R>& L = ld[l];
+    const LineDepth<R>& L = ld[l * ld_stride];
     const D6<R> v = dlam[l] * L.inv_vb + L.vshift;
     if (L.gauss) {
       const D6<R> phi = (fabs(v.v) <= R(kMAX_GAUSS_DOPPLER)) ? dexp(dconst(R(0)) - v * v) : dconst(R(0));
@@ -331,6 +341,51 @@ PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, const GeoD<R>& geo, 
     q[n] = out[n].v;
     for (int i = 0; i < kNX; ++i) J[n][i] = out[n].d[i];
   }
+}
+
+// Values of q only (the forward sweep): the same sums as local_q_jac on the
+// value parts, with the single-precision fast Humlicek where R is float.
+template <typename R>
+PYRH_HD void local_q(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
+                     const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
+                     const R* cweight, const int* cq, int maxcomp, R chi_c, R eta_c, R q[8]) {
+  R cI = 0, cQ = 0, cU = 0, cV = 0, eI = 0, eQ = 0, eU = 0, eV = 0;
+  for (int l = 0; l < nline; ++l) {
+    if (!((inwin >> l) & 1u)) continue;
+    const LineDepth<R>& L = ld[l * ld_stride];
+    const R v = dlam[l] * L.inv_vb.v + L.vshift.v;
+    if (L.gauss) {
+      const R phi = (fabs(v) <= R(kMAX_GAUSS_DOPPLER)) ? dev_exp(-v * v) : R(0);
+      cI += L.chil.v * phi;
+      eI += L.etal.v * phi;
+      continue;
+    }
+    R ph[3] = {0, 0, 0};
+    for (int c = 0; c < ncomp[l]; ++c) {
+      R H, F;
+      humlicek<R>(L.adamp.v, v - cshift[l * maxcomp + c] * L.vB.v, H, F);
+      const int qi = cq[l * maxcomp + c] + 1;
+      ph[qi < 0 ? 0 : (qi > 2 ? 2 : qi)] += cweight[l * maxcomp + c] * H;
+    }
+    const R sig = ph[2] + ph[0];
+    const R del = R(0.5) * ph[1] - R(0.25) * sig;
+    const R phiI = del * geo.s2g.v + R(0.5) * sig;
+    const R phiQ = del * geo.gQ.v, phiU = del * geo.gU.v, phiV = R(0.5) * ((ph[2] - ph[0]) * geo.gV.v);
+    cI += L.chil.v * phiI; eI += L.etal.v * phiI;
+    cQ += L.chil.v * phiQ; eQ += L.etal.v * phiQ;
+    cU += L.chil.v * phiU; eU += L.etal.v * phiU;
+    cV += L.chil.v * phiV; eV += L.etal.v * phiV;
+  }
+  const R chi = chi_c + cI;
+  const R rchi = fdiv(R(1), chi);
+  q[0] = chi;
+  q[1] = (eta_c + eI) * rchi;
+  q[2] = eQ * rchi;
+  q[3] = eU * rchi;
+  q[4] = eV * rchi;
+  q[5] = cQ * rchi;
+  q[6] = cU * rchi;
+  q[7] = cV * rchi;
 }
 
 // ------------------------------------------------- coefficient derivatives --
@@ -451,10 +506,10 @@ PYRH_HD void step_fwd(const StepIn<R>& s, R x[4], R V[4], R b[3], R& c) {
 }
 
 // Reverse of step_fwd: given xb = dL/dx, accumulate into sb (same layout).
+// x, b and c are the step's forward results (step_fwd).
 template <typename R>
-PYRH_HD void step_vjp(const StepIn<R>& s, const R xb[4], StepIn<R>& sb) {
-  R x[4], V[4], b[3], c;
-  step_fwd(s, x, V, b, c);
+PYRH_HD void step_vjp(const StepIn<R>& s, const R x[4], const R b[3], R c, const R xb[4],
+                      StepIn<R>& sb) {
   const R pK = s.al + s.ga * (R(1) + s.dt03);
   const R ca = s.th * s.dt03, pa = -s.be - s.th + s.th * s.dt03;
   const R bt = s.be + s.th, ag = s.al + s.ga, tdt = s.th * s.dt03, gdt = s.ga * s.dt03;
@@ -641,39 +696,46 @@ PYRH_HD void w3_d(double dtau, double w[3], double dw[2]) {
   }
 }
 
-// Reverse sweep for NS seeds.  seed[s][4] = dL_s/dI_0.  Accumulates
-// qb[j][s][8] = dL_s/dq_j and Bb[s][2] = dL_s/d(B0, B1).
-template <typename R, int NS>
-PYRH_HD void delo_reverse(const Tape<R>& tp, const R* ds, int nd, double B0, double B1,
-                          const R seed[NS][4], R (*qb)[NS][8], R Bb[NS][2]) {
+// Reverse (adjoint) sweep of delo_forward for NS seeds (seed[s][4] =
+// dL_s/dI_0).  dL/dq_j is handed to emit(j, qb_j, bpl) as soon as no later
+// step can add to it (step k reaches depths k-2 .. k+1), so only four depths
+// of adjoints are live at a time instead of all of them.  qb_j is
+// R[NS][8]; bpl[s] is dL_s/dB for the Planck function of depth j (non-zero
+// only for the two bottom depths, whose temperatures set the boundary
+// condition I = B1 - (B0 - B1)/dtau).  The steps are shared by the seeds.
+template <typename R, int NS, typename Emit>
+PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double B0, double B1,
+                                 const R seed[NS][4], Emit&& emit) {
   const int N = nd;
-  for (int j = 0; j < N; ++j)
+  R ring[4][NS][8];
+  for (int a = 0; a < 4; ++a)
     for (int s = 0; s < NS; ++s)
-      for (int n = 0; n < 8; ++n) qb[j][s][n] = R(0);
-  for (int s = 0; s < NS; ++s) {
-    R Ib[4];   // adjoint of I_k being carried
-    R dSb[4];  // adjoint of dS0 of the step above (dSu of the current)
-    R dKb[3];
-    R dchib = R(0), Tb = R(0);
-    // ---- last interval ----
-    {
-      const double dtau = 0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * (double)ds[1];
-      double w[3], dw[2];
-      w3_d(dtau, w, dw);
-      const R w0 = R(w[0]), w1 = R(w[1]), wd = R(w[1] / dtau);
-      const R* ku = &tp.q[1][5];
-      const R* k0 = &tp.q[0][5];
-      const R* dSu = tp.dS0[1];
-      const R* I1 = tp.I[1];
-      R V[4];
-      V[0] = w0 * tp.q[0][1] - w1 * dSu[0] + (R(1) - w0) * I1[0] -
-             wd * (ku[0] * I1[1] + ku[1] * I1[2] + ku[2] * I1[3]);
-      for (int j = 0; j < 3; ++j)
-        V[j + 1] = w0 * tp.q[0][2 + j] - w1 * dSu[j + 1] + (R(1) - w0) * I1[j + 1] - wd * ku[j] * I1[0];
-      const R g = w0 - wd;
-      const R bv[3] = {g * k0[0], g * k0[1], g * k0[2]};
-      const R Dn = R(1) - (bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2]);
-      const R x0 = (V[0] - (bv[0] * V[1] + bv[1] * V[2] + bv[2] * V[3])) / Dn;
+      for (int n = 0; n < 8; ++n) ring[a][s][n] = R(0);
+  R zero_b[NS];
+  for (int s = 0; s < NS; ++s) zero_b[s] = R(0);
+  R Ib[NS][4], dSb[NS][4], dKb[NS][3], dchib[NS], Tb[NS];
+  // ---- last interval ----
+  {
+    const double dtau = 0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * (double)ds[1];
+    double w[3], dw[2];
+    w3_d(dtau, w, dw);
+    const R w0 = R(w[0]), w1 = R(w[1]), wd = R(w[1] / dtau);
+    const R* ku = &tp.q[1][5];
+    const R* k0 = &tp.q[0][5];
+    const R* dSu = tp.dS0[1];
+    const R* I1 = tp.I[1];
+    R V[4];
+    V[0] = w0 * tp.q[0][1] - w1 * dSu[0] + (R(1) - w0) * I1[0] -
+           wd * (ku[0] * I1[1] + ku[1] * I1[2] + ku[2] * I1[3]);
+    for (int j = 0; j < 3; ++j)
+      V[j + 1] = w0 * tp.q[0][2 + j] - w1 * dSu[j + 1] + (R(1) - w0) * I1[j + 1] - wd * ku[j] * I1[0];
+    const R g = w0 - wd;
+    const R bv[3] = {g * k0[0], g * k0[1], g * k0[2]};
+    const R Dn = R(1) - (bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2]);
+    const R x0 = (V[0] - (bv[0] * V[1] + bv[1] * V[2] + bv[2] * V[3])) / Dn;
+    R(&q0)[NS][8] = ring[0];
+    R(&q1)[NS][8] = ring[1];
+    for (int s = 0; s < NS; ++s) {
       R Vb[4] = {0, 0, 0, 0}, bb[3] = {0, 0, 0};
       R x0b = seed[s][0];
       for (int j = 0; j < 3; ++j) {
@@ -689,145 +751,156 @@ PYRH_HD void delo_reverse(const Tape<R>& tp, const R* ds, int nd, double B0, dou
       const R Dnb = -x0b * x0 / Dn;
       for (int j = 0; j < 3; ++j) bb[j] += Dnb * R(-2) * bv[j];
       R gb = 0, w0b = 0, w1b = 0, wdb = 0;
-      for (int j = 0; j < 3; ++j) { gb += bb[j] * k0[j]; qb[0][s][5 + j] += g * bb[j]; }
+      for (int j = 0; j < 3; ++j) { gb += bb[j] * k0[j]; q0[s][5 + j] += g * bb[j]; }
       w0b += gb; wdb -= gb;
-      for (int n = 0; n < 4; ++n) { Ib[n] = R(0); dSb[n] = R(0); }
-      // V0
+      for (int n = 0; n < 4; ++n) { Ib[s][n] = R(0); dSb[s][n] = R(0); }
       w0b += Vb[0] * (tp.q[0][1] - I1[0]);
-      qb[0][s][1] += Vb[0] * w0;
-      dSb[0] -= Vb[0] * w1;
+      q0[s][1] += Vb[0] * w0;
+      dSb[s][0] -= Vb[0] * w1;
       w1b -= Vb[0] * dSu[0];
-      Ib[0] += Vb[0] * (R(1) - w0);
+      Ib[s][0] += Vb[0] * (R(1) - w0);
       wdb -= Vb[0] * (ku[0] * I1[1] + ku[1] * I1[2] + ku[2] * I1[3]);
       for (int j = 0; j < 3; ++j) {
-        qb[1][s][5 + j] -= Vb[0] * wd * I1[j + 1];
-        Ib[j + 1] -= Vb[0] * wd * ku[j];
+        q1[s][5 + j] -= Vb[0] * wd * I1[j + 1];
+        Ib[s][j + 1] -= Vb[0] * wd * ku[j];
       }
       for (int j = 0; j < 3; ++j) {
         const R v = Vb[j + 1];
         w0b += v * (tp.q[0][2 + j] - I1[j + 1]);
-        qb[0][s][2 + j] += v * w0;
-        dSb[j + 1] -= v * w1;
+        q0[s][2 + j] += v * w0;
+        dSb[s][j + 1] -= v * w1;
         w1b -= v * dSu[j + 1];
-        Ib[j + 1] += v * (R(1) - w0);
+        Ib[s][j + 1] += v * (R(1) - w0);
         wdb -= v * ku[j] * I1[0];
-        qb[1][s][5 + j] -= v * wd * I1[0];
-        Ib[0] -= v * wd * ku[j];
+        q1[s][5 + j] -= v * wd * I1[0];
+        Ib[s][0] -= v * wd * ku[j];
       }
       w1b += wdb / R(dtau);
       const double dtb = (double)w0b * dw[0] + (double)w1b * dw[1] - (double)wdb * w[1] / (dtau * dtau);
-      qb[0][s][0] += R(0.5 * (double)ds[1] * dtb);
-      qb[1][s][0] += R(0.5 * (double)ds[1] * dtb);
-      for (int n = 0; n < 3; ++n) dKb[n] = R(0);
-      dchib = R(0);
-      Tb = R(0);
+      q0[s][0] += R(0.5 * (double)ds[1] * dtb);
+      q1[s][0] += R(0.5 * (double)ds[1] * dtb);
+      for (int n = 0; n < 3; ++n) dKb[s][n] = R(0);
+      dchib[s] = R(0);
+      Tb[s] = R(0);
     }
-    // ---- steps k = 1 .. N-2 (reverse order) ----
-    for (int k = 1; k <= N - 2; ++k) {
-      const R Tk = tp.T[k], Tdw = tp.T[k - 1];
-      StepIn<R> st, sb;
-      R cf[5], dcf[5];
-      bezier3_coeffs_d(Tk, cf, dcf);
-      st.al = cf[0]; st.be = cf[1]; st.ga = cf[2]; st.th = cf[3]; st.ep = cf[4];
-      st.dt03 = Tk / R(3);
-      const int kup = (k + 1 == N - 1) ? N - 1 : k + 1;
-      for (int n = 0; n < 3; ++n) {
-        st.ku[n] = tp.q[k + 1][5 + n]; st.k0[n] = tp.q[k][5 + n];
-        st.dku[n] = tp.dK0[kup][n]; st.dk0[n] = tp.dK0[k][n];
-      }
-      for (int n = 0; n < 4; ++n) {
-        st.Su[n] = tp.q[k + 1][1 + n]; st.S0[n] = tp.q[k][1 + n];
-        st.dSu[n] = tp.dS0[kup][n]; st.dS0[n] = tp.dS0[k][n];
-        st.Iu[n] = tp.I[k + 1][n];
-      }
-      // zero the adjoint struct
+  }
+  // ---- steps k = 1 .. N-2 (reverse order of the forward sweep) ----
+  for (int k = 1; k <= N - 2; ++k) {
+    R(&qu)[NS][8] = ring[(k + 1) & 3];
+    R(&qc)[NS][8] = ring[k & 3];
+    R(&qd)[NS][8] = ring[(k - 1) & 3];
+    for (int s = 0; s < NS; ++s)
+      for (int n = 0; n < 8; ++n) qu[s][n] = R(0);   // depth k+1 is first reached here
+    const R Tk = tp.T[k], Tdw = tp.T[k - 1];
+    StepIn<R> st;
+    R cf[5], dcf[5];
+    bezier3_coeffs_d(Tk, cf, dcf);
+    st.al = cf[0]; st.be = cf[1]; st.ga = cf[2]; st.th = cf[3]; st.ep = cf[4];
+    st.dt03 = Tk / R(3);
+    const int kup = (k + 1 == N - 1) ? N - 1 : k + 1;
+    for (int n = 0; n < 3; ++n) {
+      st.ku[n] = tp.q[k + 1][5 + n]; st.k0[n] = tp.q[k][5 + n];
+      st.dku[n] = tp.dK0[kup][n]; st.dk0[n] = tp.dK0[k][n];
+    }
+    for (int n = 0; n < 4; ++n) {
+      st.Su[n] = tp.q[k + 1][1 + n]; st.S0[n] = tp.q[k][1 + n];
+      st.dSu[n] = tp.dS0[kup][n]; st.dS0[n] = tp.dS0[k][n];
+      st.Iu[n] = tp.I[k + 1][n];
+    }
+    R x[4], V[4], bvec[3], c;
+    step_fwd(st, x, V, bvec, c);
+    const R dsdn = ds[k];
+    const R dchi_c = tp.dchi[k], dchi_dn = tp.dchi[k - 1];
+    const bool c2pos = tp.q[k][0] + (dsdn / R(3)) * dchi_c > R(0);
+    const bool c1pos = tp.q[k - 1][0] - (dsdn / R(3)) * dchi_dn > R(0);
+    for (int s = 0; s < NS; ++s) {
+      StepIn<R> sb;
       sb.al = sb.be = sb.ga = sb.th = sb.ep = sb.dt03 = R(0);
       for (int n = 0; n < 3; ++n) sb.ku[n] = sb.k0[n] = sb.dku[n] = sb.dk0[n] = R(0);
       for (int n = 0; n < 4; ++n) sb.Su[n] = sb.S0[n] = sb.dSu[n] = sb.dS0[n] = sb.Iu[n] = R(0);
-      step_vjp(st, Ib, sb);
-      // carried adjoints of dS0_k, dK0_k add to the step's own
-      for (int n = 0; n < 4; ++n) sb.dS0[n] += dSb[n];
-      for (int n = 0; n < 3; ++n) sb.dk0[n] += dKb[n];
-      // cent_deriv VJPs of dK0_k and dS0_k
-      R Tkb = R(0), Tdwb = Tb;
+      step_vjp(st, x, bvec, c, Ib[s], sb);
+      for (int n = 0; n < 4; ++n) sb.dS0[n] += dSb[s][n];
+      for (int n = 0; n < 3; ++n) sb.dk0[n] += dKb[s][n];
+      R Tkb = R(0), Tdwb = Tb[s];
       for (int n = 0; n < 3; ++n)
         cent_deriv_vjp<R>(Tk, Tdw, tp.q[k + 1][5 + n], tp.q[k][5 + n], tp.q[k - 1][5 + n], sb.dk0[n],
-                          Tkb, Tdwb, qb[k + 1][s][5 + n], qb[k][s][5 + n], qb[k - 1][s][5 + n]);
+                          Tkb, Tdwb, qu[s][5 + n], qc[s][5 + n], qd[s][5 + n]);
       for (int n = 0; n < 4; ++n)
         cent_deriv_vjp<R>(Tk, Tdw, tp.q[k + 1][1 + n], tp.q[k][1 + n], tp.q[k - 1][1 + n], sb.dS0[n],
-                          Tkb, Tdwb, qb[k + 1][s][1 + n], qb[k][s][1 + n], qb[k - 1][s][1 + n]);
-      // coefficients
+                          Tkb, Tdwb, qu[s][1 + n], qc[s][1 + n], qd[s][1 + n]);
       Tkb += sb.al * dcf[0] + sb.be * dcf[1] + sb.ga * dcf[2] + sb.th * dcf[3] + sb.ep * dcf[4] +
              sb.dt03 / R(3);
-      for (int n = 0; n < 3; ++n) { qb[k + 1][s][5 + n] += sb.ku[n]; qb[k][s][5 + n] += sb.k0[n]; }
-      for (int n = 0; n < 4; ++n) { qb[k + 1][s][1 + n] += sb.Su[n]; qb[k][s][1 + n] += sb.S0[n]; }
-      // T_{k-1} = 0.25 ds[k] (chi_k + chi_{k-1} + c1 + c2)
-      const R dsdn = ds[k];
-      const R dchi_c = tp.dchi[k], dchi_dn = tp.dchi[k - 1];
-      R dchi_cb = R(0), dchi_dnb = dchib;
+      for (int n = 0; n < 3; ++n) { qu[s][5 + n] += sb.ku[n]; qc[s][5 + n] += sb.k0[n]; }
+      for (int n = 0; n < 4; ++n) { qu[s][1 + n] += sb.Su[n]; qc[s][1 + n] += sb.S0[n]; }
+      R dchi_cb = R(0), dchi_dnb = dchib[s];
       {
         const R a = R(0.25) * dsdn * Tdwb;
-        qb[k][s][0] += a;
-        qb[k - 1][s][0] += a;
-        const R c2 = tp.q[k][0] + (dsdn / R(3)) * dchi_c;
-        const R c1 = tp.q[k - 1][0] - (dsdn / R(3)) * dchi_dn;
-        if (c2 > R(0)) { qb[k][s][0] += a; dchi_cb += (dsdn / R(3)) * a; }
-        if (c1 > R(0)) { qb[k - 1][s][0] += a; dchi_dnb -= (dsdn / R(3)) * a; }
+        qc[s][0] += a;
+        qd[s][0] += a;
+        if (c2pos) { qc[s][0] += a; dchi_cb += (dsdn / R(3)) * a; }
+        if (c1pos) { qd[s][0] += a; dchi_dnb -= (dsdn / R(3)) * a; }
       }
-      // dchi_dn_k
       if (k > 1) {
         R d1 = 0, d2 = 0;
-        cent_deriv_vjp<R>(dsdn, ds[k - 1], tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0], dchi_dnb, d1, d2,
-                          qb[k][s][0], qb[k - 1][s][0], qb[k - 2][s][0]);
+        cent_deriv_vjp<R>(dsdn, ds[k - 1], tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0], dchi_dnb, d1,
+                          d2, qc[s][0], qd[s][0], ring[(k - 2) & 3][s][0]);
       } else {
-        qb[k - 1][s][0] += dchi_dnb / dsdn;
-        qb[k][s][0] -= dchi_dnb / dsdn;
+        qd[s][0] += dchi_dnb / dsdn;
+        qc[s][0] -= dchi_dnb / dsdn;
       }
-      // carry up
-      for (int n = 0; n < 4; ++n) { Ib[n] = sb.Iu[n]; dSb[n] = sb.dSu[n]; }
-      for (int n = 0; n < 3; ++n) dKb[n] = sb.dku[n];
-      dchib = dchi_cb;
-      Tb = Tkb;
+      for (int n = 0; n < 4; ++n) { Ib[s][n] = sb.Iu[n]; dSb[s][n] = sb.dSu[n]; }
+      for (int n = 0; n < 3; ++n) dKb[s][n] = sb.dku[n];
+      dchib[s] = dchi_cb;
+      Tb[s] = Tkb;
     }
-    // ---- initial values (k = N-2 set-up and the bottom boundary) ----
-    {
-      const int k = N - 2;
-      const R T = tp.T[k];
-      const R dsup = ds[k + 1], dsdn = ds[k];
-      // dSu = (S_k - S_{k+1}) / T, dKu = (k_k - k_{k+1}) / T
+    // depth k-2 received its last term from this step's chi derivative
+    if (k >= 2 && k - 2 <= N - 4) emit(k - 2, &ring[(k - 2) & 3][0][0], zero_b);
+  }
+  // ---- initial values (k = N-2 set-up and the bottom boundary) ----
+  R bpl[2][NS];
+  {
+    const int k = N - 2;
+    const R T = tp.T[k];
+    const R dsup = ds[k + 1], dsdn = ds[k];
+    const R cu = tp.q[k + 1][0], cc = tp.q[k][0];
+    const R dchi_c = tp.dchi[k], dchi_up = tp.dchi_up0;
+    const double dtau0 = 0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * (double)ds[N - 1];
+    R(&qu)[NS][8] = ring[(k + 1) & 3];
+    R(&qc)[NS][8] = ring[k & 3];
+    R(&qd)[NS][8] = ring[(k - 1) & 3];
+    for (int s = 0; s < NS; ++s) {
       for (int n = 0; n < 4; ++n) {
-        qb[k][s][1 + n] += dSb[n] / T;
-        qb[k + 1][s][1 + n] -= dSb[n] / T;
-        Tb -= dSb[n] * tp.dS0[N - 1][n] / T;
+        qc[s][1 + n] += dSb[s][n] / T;
+        qu[s][1 + n] -= dSb[s][n] / T;
+        Tb[s] -= dSb[s][n] * tp.dS0[N - 1][n] / T;
       }
       for (int n = 0; n < 3; ++n) {
-        qb[k][s][5 + n] += dKb[n] / T;
-        qb[k + 1][s][5 + n] -= dKb[n] / T;
-        Tb -= dKb[n] * tp.dK0[N - 1][n] / T;
+        qc[s][5 + n] += dKb[s][n] / T;
+        qu[s][5 + n] -= dKb[s][n] / T;
+        Tb[s] -= dKb[s][n] * tp.dK0[N - 1][n] / T;
       }
-      const R cu = tp.q[k + 1][0], cc = tp.q[k][0];
-      const R dchi_c = tp.dchi[k], dchi_up = tp.dchi_up0;
-      const R a = R(0.25) * dsup * Tb;
-      qb[k][s][0] += a;
-      qb[k + 1][s][0] += a;
-      R dchi_cb = dchib, dchi_upb = R(0);
-      if (cc - (dsup / R(3)) * dchi_c > R(0)) { qb[k][s][0] += a; dchi_cb -= (dsup / R(3)) * a; }
-      if (cu + (dsup / R(3)) * dchi_up > R(0)) { qb[k + 1][s][0] += a; dchi_upb += (dsup / R(3)) * a; }
-      qb[k][s][0] += dchi_upb / dsup;
-      qb[k + 1][s][0] -= dchi_upb / dsup;
+      const R a = R(0.25) * dsup * Tb[s];
+      qc[s][0] += a;
+      qu[s][0] += a;
+      R dchi_cb = dchib[s], dchi_upb = R(0);
+      if (cc - (dsup / R(3)) * dchi_c > R(0)) { qc[s][0] += a; dchi_cb -= (dsup / R(3)) * a; }
+      if (cu + (dsup / R(3)) * dchi_up > R(0)) { qu[s][0] += a; dchi_upb += (dsup / R(3)) * a; }
+      qc[s][0] += dchi_upb / dsup;
+      qu[s][0] -= dchi_upb / dsup;
       R d1 = 0, d2 = 0;
-      cent_deriv_vjp<R>(dsup, dsdn, cu, cc, tp.q[k - 1][0], dchi_cb, d1, d2, qb[k + 1][s][0],
-                        qb[k][s][0], qb[k - 1][s][0]);
-      // I_{N-1} = B1 - (B0 - B1) / dtau0
-      const double dtau0 = 0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * (double)ds[N - 1];
-      const double ib = (double)Ib[0];
-      Bb[s][1] = R(ib * (1.0 + 1.0 / dtau0));
-      Bb[s][0] = R(-ib / dtau0);
+      cent_deriv_vjp<R>(dsup, dsdn, cu, cc, tp.q[k - 1][0], dchi_cb, d1, d2, qu[s][0], qc[s][0],
+                        qd[s][0]);
+      const double ib = (double)Ib[s][0];
+      bpl[1][s] = R(ib * (1.0 + 1.0 / dtau0));
+      bpl[0][s] = R(-ib / dtau0);
       const double dtb = ib * (B0 - B1) / (dtau0 * dtau0);
-      qb[N - 1][s][0] += R(0.5 * (double)ds[N - 1] * dtb);
-      qb[N - 2][s][0] += R(0.5 * (double)ds[N - 1] * dtb);
+      qu[s][0] += R(0.5 * (double)ds[N - 1] * dtb);
+      qc[s][0] += R(0.5 * (double)ds[N - 1] * dtb);
     }
   }
+  emit(N - 3, &ring[(N - 3) & 3][0][0], zero_b);
+  emit(N - 2, &ring[(N - 2) & 3][0][0], bpl[0]);
+  emit(N - 1, &ring[(N - 1) & 3][0][0], bpl[1]);
 }
 
 // dB_nu/dT of planck() (planck.c:38-63)

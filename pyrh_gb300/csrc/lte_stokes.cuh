@@ -22,6 +22,20 @@ struct LteArgs {
   void *out;
 };
 
+// Response-function / gradient launch (lte_rf.cu).  mode 0 writes rf;
+// mode 1 accumulates chi2 and grad (zeroed by the caller) with obs and
+// weights; mode 2 accumulates grad with dL/dS passed in `weights`.
+struct RfArgs {
+  LteArgs lte;
+  int mode;
+  const void *obs, *weights;
+  void *rf, *chi2, *grad;
+};
+
+size_t rf_smem_bytes(int precision, int nline, int maxd);
+int rf_blocks_per_sm(int precision, int mode, int block, size_t smem);
+cudaError_t launch_lte_rf(const RfArgs &a, int block, int grid, cudaStream_t st);
+
 size_t lte_smem_bytes(int precision, int nline, int maxd);
 int lte_blocks_per_sm(int precision, int magneto_optical, int block, size_t smem);
 cudaError_t launch_lte_stokes(const LteArgs &a, int block, int grid, cudaStream_t st);

@@ -1,0 +1,150 @@
+"""Response functions and gradients of the batched LTE Stokes synthesis.
+
+Host side of pyrh_lte_rf, pyrh_lte_chi2_grad and pyrh_lte_stokes_vjp
+(include/pyrh_gb300.h) and a torch.autograd.Function around the synthesis.
+The derivatives are taken with respect to the six atmosphere parameters of
+every depth, in this order and in SI units:
+    T [K], v_los [m/s], v_mic [m/s], B [T], gamma_B [rad], chi_B [rad]
+(the depth-resolved quantities the reference perturbs for its finite-
+difference response functions, rh/rhf1d/rf_ray.c:205-235).  The continuum
+opacity and emissivity, stage densities and height scale are held fixed.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .lte import DeviceBatch, Packed
+
+PARAMS = ("T", "vel", "vturb", "B", "gamma_B", "chi_B")
+NPARAM = len(PARAMS)
+
+_bound = None
+
+
+def _lib():
+    global _bound
+    lib = L.lib()
+    if _bound is not lib:
+        B, P, I32, V = C.POINTER(L.PyrhLteBatch), C.POINTER(L.PyrhLteConfig), C.c_int32, C.c_void_p
+        lib.pyrh_lte_rf.restype = C.c_int
+        lib.pyrh_lte_rf.argtypes = [B, V, I32, P, V, V, V]
+        lib.pyrh_lte_chi2_grad.restype = C.c_int
+        lib.pyrh_lte_chi2_grad.argtypes = [B, V, I32, P, V, V, V, V, V, V]
+        lib.pyrh_lte_stokes_vjp.restype = C.c_int
+        lib.pyrh_lte_stokes_vjp.argtypes = [B, V, I32, P, V, V, V, V]
+        _bound = lib
+    return lib
+
+
+def _real(dev: DeviceBatch):
+    import torch
+    return torch.float32 if dev.pk.precision == L.PYRH_FP32 else torch.float64
+
+
+def rf_size(pk: Packed) -> int:
+    """Length of the flat response-function array of a batch."""
+    last = pk.natm - 1
+    cont = int(pk.arrays["cont_off"][last] + int(pk.arrays["ndep"][last]) * int(pk.arrays["nlam"][last]))
+    return 4 * NPARAM * cont
+
+
+def response_functions(dev: DeviceBatch, cfg: L.PyrhLteConfig, stream_ptr: int = 0):
+    """Runs pyrh_lte_rf; returns the flat RF tensor (layout of the header)
+    and leaves the emergent Stokes vectors in dev.out."""
+    import torch
+    rf = torch.empty(rf_size(dev.pk), dtype=_real(dev), device=dev.out.device)
+    L.check(_lib().pyrh_lte_rf(C.byref(dev.struct), dev.lines_t.data_ptr(), dev.nline,
+                               C.byref(cfg), dev.out.data_ptr(), rf.data_ptr(), stream_ptr))
+    return rf
+
+
+def split_rf(pk: Packed, rf) -> list:
+    """Per-atmosphere [4, 6, ndep, nlam] views of a flat RF array."""
+    out = []
+    for p in range(pk.natm):
+        o = int(pk.arrays["cont_off"][p])
+        nd, nl = int(pk.arrays["ndep"][p]), int(pk.arrays["nlam"][p])
+        out.append(rf[4 * NPARAM * o: 4 * NPARAM * (o + nd * nl)].reshape(4, NPARAM, nd, nl))
+    return out
+
+
+def chi2_grad(dev: DeviceBatch, cfg: L.PyrhLteConfig, obs, weights, stream_ptr: int = 0):
+    """chi2[p] = sum w (S - obs)^2 and its gradient [6, total_depth] in one
+    forward + adjoint pass (obs, weights: flat tensors laid out like dev.out)."""
+    import torch
+    real = _real(dev)
+    obs = obs.to(device=dev.out.device, dtype=real).contiguous()
+    weights = weights.to(device=dev.out.device, dtype=real).contiguous()
+    chi2 = torch.empty(dev.pk.natm, dtype=real, device=dev.out.device)
+    grad = torch.empty(NPARAM * dev.pk.total_depth, dtype=real, device=dev.out.device)
+    L.check(_lib().pyrh_lte_chi2_grad(C.byref(dev.struct), dev.lines_t.data_ptr(), dev.nline,
+                                      C.byref(cfg), obs.data_ptr(), weights.data_ptr(),
+                                      dev.out.data_ptr(), chi2.data_ptr(), grad.data_ptr(),
+                                      stream_ptr))
+    return chi2, grad.view(NPARAM, dev.pk.total_depth)
+
+
+def vjp(dev: DeviceBatch, cfg: L.PyrhLteConfig, dL_dstokes, stream_ptr: int = 0):
+    """sum over wavelengths and Stokes of dL/dS * dS/dx: [6, total_depth]."""
+    import torch
+    real = _real(dev)
+    g = dL_dstokes.to(device=dev.out.device, dtype=real).contiguous()
+    grad = torch.empty(NPARAM * dev.pk.total_depth, dtype=real, device=dev.out.device)
+    L.check(_lib().pyrh_lte_stokes_vjp(C.byref(dev.struct), dev.lines_t.data_ptr(), dev.nline,
+                                       C.byref(cfg), g.data_ptr(), dev.out.data_ptr(),
+                                       grad.data_ptr(), stream_ptr))
+    return grad.view(NPARAM, dev.pk.total_depth)
+
+
+def set_params(dev: DeviceBatch, params) -> None:
+    """Writes a [6, total_depth] float64 tensor into the batch's per-depth
+    arrays (T, v_los, v_mic, B, gamma_B, chi_B)."""
+    for i, k in enumerate(PARAMS):
+        dev.t[k].copy_(params[i])
+
+
+def get_params(dev: DeviceBatch):
+    import torch
+    return torch.stack([dev.t[k] for k in PARAMS])
+
+
+def _autograd_function():
+    import torch
+
+    class LteStokes(torch.autograd.Function):
+        """Emergent Stokes vectors of a resident batch as a function of the
+        [6, total_depth] atmosphere parameters; backward is the hand-written
+        adjoint (pyrh_lte_stokes_vjp), which recomputes the forward sweep per
+        pixel instead of storing it."""
+
+        @staticmethod
+        def forward(ctx, params, dev, cfg):
+            set_params(dev, params.detach())
+            dev.run(cfg)
+            ctx.dev, ctx.cfg = dev, cfg
+            ctx.save_for_backward(params.detach().clone())
+            return dev.out.clone()
+
+        @staticmethod
+        def backward(ctx, g):
+            (params,) = ctx.saved_tensors
+            set_params(ctx.dev, params)
+            grad = vjp(ctx.dev, ctx.cfg, g)
+            return grad.to(params.dtype), None, None
+
+    return LteStokes
+
+
+_fn = None
+
+
+def synthesize(dev: DeviceBatch, cfg: L.PyrhLteConfig, params):
+    """Differentiable synthesis: Stokes (flat, like dev.out) from params
+    [6, total_depth] (float64, on the device of dev)."""
+    global _fn
+    if _fn is None:
+        _fn = _autograd_function()
+    return _fn.apply(params, dev, cfg)

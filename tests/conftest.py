@@ -1,4 +1,7 @@
+import ctypes as C
 import os
+import shutil
+import subprocess
 import sys
 
 import numpy as np
@@ -33,3 +36,56 @@ def golden():
             cache[name] = load_golden(name)
         return cache[name]
     return get
+
+
+@pytest.fixture(scope="session")
+def rf_harness(tmp_path_factory):
+    """tests/native/rf_host.cu compiled for the host: the response-function
+    math of pyrh_gb300/csrc/lte_rf.cuh evaluated on the CPU in FP64."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    out = str(tmp_path_factory.mktemp("rf") / "librf_host.so")
+    src = os.path.join(REPO, "tests", "native", "rf_host.cu")
+    subprocess.run([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-shared",
+                    "-diag-suppress", "20011,20013", "-x", "cu", src, "-o", out], check=True)
+    return C.CDLL(out)
+
+
+def rf_eval(lib, fx, sel, single=False):
+    """Stokes [nsel, 4] and response functions [nsel, 4, 6, ndep] of one
+    atmosphere at the wavelengths fx["lam"][sel] (CPU harness, FP64 or, with
+    single=True, FP32)."""
+    from pyrh_gb300 import lte
+    D = C.POINTER(C.c_double)
+    keep = []
+
+    def arr(a):
+        a = np.ascontiguousarray(a, np.float64)
+        keep.append(a)
+        return a.ctypes.data_as(D)
+
+    lam = fx["lam"][sel]
+    nd = len(fx["T"])
+    lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
+    st = np.zeros((len(sel), 4))
+    rf = np.zeros((len(sel), 4, 6, nd))
+    fn = lib.rf_eval_f32 if single else lib.rf_eval
+    r = fn(nd, arr(fx["height"]), arr(fx["T"]), arr(fx["ne"]), arr(fx["nHtot"]),
+                    arr(fx["np"]), arr(fx["vturb"]), arr(fx["vel"]), arr(fx["B"]),
+                    arr(fx["gamma_B"]), arr(fx["chi_B"]), arr(fx["line_pops"]), n, lines,
+                    len(sel), arr(lam), arr(fx["chi_c"][sel]), arr(fx["eta_c"][sel]),
+                    C.c_double(float(fx["mu"])), C.c_double(float(fx["vmicro_char"])),
+                    st.ctypes.data_as(D), rf.ctypes.data_as(D))
+    assert r == 0
+    return st, rf
+
+
+def delo_wavelengths(fx) -> np.ndarray:
+    """Indices of the wavelengths where a contributing line is inside its
+    window (20 VMICRO_CHAR / c, kurucz.c:593-602): the DELO-Bezier3 ones."""
+    lam = fx["lam"]
+    win = np.zeros(len(lam), bool)
+    for l0 in fx["line_const"][:, 0]:
+        win |= np.abs(lam - l0) <= lam * 20 * fx["vmicro_char"] / 2.99792458e8
+    return np.nonzero(win)[0]

@@ -1,0 +1,199 @@
+"""GPU response functions, chi^2 gradients and vector-Jacobian products
+(pyrh_lte_rf, pyrh_lte_chi2_grad, pyrh_lte_stokes_vjp through the C ABI).
+
+Checked against
+  * the same adjoint evaluated on the CPU in FP64 (tests/native/rf_host.cu),
+    which tests/test_rf_host.py pins to central finite differences of the
+    oracle's synthesis, the reference's definition of response functions
+    (rh/rhf1d/rf_ray.c:205-293);
+  * central finite differences of the GPU's own FP64 synthesis
+    (pyrh_lte_stokes), at the five steps of tests/test_rf_host.py;
+  * each other: chi^2 gradient and VJP equal the contraction of the RFs.
+Tolerances are relative to the largest |RF| of each parameter:
+  FP64 kernel vs CPU adjoint (FP64)   1e-8 (fused multiply-adds on the GPU)
+  FP32 kernel vs CPU adjoint (FP64)   1e-4 at the 99.9th percentile, 1e-3 at
+                                      most (isolated limiter-branch flips next
+                                      to sign changes of S_Q, S_U; see
+                                      test_rf_host)
+  GPU FD (FP64) vs FP64 kernel        1e-4, per element the closest of five
+                                      steps (Humlicek region jumps, FP64
+                                      noise of the synthesis)
+  chi^2 gradient and VJP vs contracted RFs: 1e-10 (FP64); 1e-3 (FP32, two
+  single-precision evaluations of one quantity, relative to the sum of the
+  magnitudes of the contracted terms)
+"""
+import numpy as np
+import pytest
+
+from conftest import batch_member, delo_wavelengths, rf_eval
+from pyrh_gb300 import _lib as L
+from pyrh_gb300 import lte, rf as RF
+
+pytestmark = pytest.mark.gpu
+
+FP64, FP32 = L.PYRH_FP64, L.PYRH_FP32
+PARAMS = RF.PARAMS
+
+
+def device_batch(atms, precision):
+    fx = atms[0]
+    lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
+    pk = lte.pack(atms, n, precision)
+    cfg = lte.make_config(precision=precision, mu=float(fx["mu"]),
+                          vmicro_char=float(fx["vmicro_char"]), moving=bool(fx["moving"]))
+    return lte.DeviceBatch(pk, lines, n), cfg
+
+
+def gpu_rf(atms, precision):
+    import torch
+    dev, cfg = device_batch(atms, precision)
+    rf = RF.response_functions(dev, cfg)
+    torch.cuda.synchronize()
+    assert L.lib().pyrh_last_launch_count() == 1
+    rfs = [r.astype(np.float64) for r in RF.split_rf(dev.pk, rf.cpu().numpy())]
+    st = [s.astype(np.float64) for s in lte.split_output(dev.pk, dev.out.cpu().numpy())]
+    return dev, cfg, st, rfs
+
+
+def rel_err(mine, ref):
+    """max |mine - ref| per parameter over the largest |ref| of that
+    parameter; arrays [4, 6, depth, lambda]."""
+    scale = np.abs(ref).max(axis=(0, 2, 3))
+    return (np.abs(mine - ref).max(axis=(0, 2, 3)) / np.where(scale > 0, scale, 1.0)).max()
+
+
+def contract_err(got, seed, rf):
+    """got [6, depth] against sum over (s, lambda) of seed * rf, relative to
+    the sum of the magnitudes of the terms (the rounding scale of the sum)."""
+    want = np.einsum("sl,sxkl->xk", seed, rf)
+    scale = np.einsum("sl,sxkl->xk", np.abs(seed), np.abs(rf)).max(axis=1)
+    return (np.abs(got - want).max(axis=1) / np.where(scale > 0, scale, 1.0)).max()
+
+
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge"])
+@pytest.mark.parametrize("precision", [FP64, FP32])
+def test_rf_matches_cpu_adjoint(rf_harness, golden, name, precision):
+    fx = golden(name)
+    _, _, st, rfs = gpu_rf([fx], precision)
+    win = delo_wavelengths(fx)
+    st_h, rf_h = rf_eval(rf_harness, fx, win)
+    ref = rf_h.transpose(1, 2, 3, 0)                  # [4, 6, nd, nsel]
+    mine = rfs[0][..., win]
+    if precision == FP64:
+        assert rel_err(mine, ref) < 1e-8
+    else:
+        for x in range(6):
+            e = np.abs(mine[:, x] - ref[:, x]) / np.abs(ref[:, x]).max()
+            assert np.percentile(e, 99.9) < 1e-4 and e.max() < 1e-3, (PARAMS[x], e.max())
+    assert np.abs(st[0][:, win] - st_h.T).max() <= (1e-10 if precision == FP64 else 1e-5) * \
+        st_h[:, 0].max()
+
+
+@pytest.mark.parametrize("precision,tol", [(FP64, 1e-9), (FP32, 1e-5)])
+def test_rf_stokes_equal_forward_kernel(golden, precision, tol):
+    """The RF kernel's forward sweep gives the synthesis kernel's spectra at
+    every DELO-Bezier3 wavelength."""
+    b = golden("lte_batch")
+    atms = [batch_member(b, i) for i in range(b["T"].shape[0])]
+    dev, cfg, st, _ = gpu_rf(atms, precision)
+    dev.run(cfg)
+    fwd = lte.split_output(dev.pk, dev.out.cpu().numpy())
+    for p, fx in enumerate(atms):
+        win = delo_wavelengths(fx)
+        assert np.abs(st[p][:, win] - fwd[p][:, win]).max() <= tol * fwd[p][0].max()
+
+
+def test_rf_ragged_batch_equals_single(golden):
+    """Atmospheres of different depth and wavelength counts in one launch
+    give the response functions each gives alone."""
+    a, c = golden("lte_c0"), golden("lte_edge")
+    c = dict(c)
+    c["mu"] = a["mu"]                     # one ray per batch
+    _, _, _, both = gpu_rf([a, c], FP64)
+    for i, fx in enumerate((a, c)):
+        _, _, _, one = gpu_rf([fx], FP64)
+        assert np.abs(both[i] - one[0]).max() <= 1e-12 * np.abs(one[0]).max()
+
+
+@pytest.mark.parametrize("precision,tol,ctol", [(FP64, 1e-12, 1e-10), (FP32, 1e-3, 1e-3)])
+def test_chi2_grad_and_vjp_contract_rf(golden, precision, tol, ctol):
+    import torch
+    b = golden("lte_batch")
+    atms = [batch_member(b, i) for i in range(b["T"].shape[0])]
+    dev, cfg, st, rfs = gpu_rf(atms, precision)
+    rng = np.random.default_rng(7)
+    S = dev.out.cpu().numpy().astype(np.float64)
+    obs = S * (1 + 1e-2 * rng.standard_normal(S.shape))
+    w = rng.uniform(0.5, 2.0, S.shape) / np.abs(S).max() ** 2
+    real = np.float32 if precision == FP32 else np.float64
+    obs, w = obs.astype(real).astype(np.float64), w.astype(real).astype(np.float64)
+    chi2, grad = RF.chi2_grad(dev, cfg, torch.from_numpy(obs), torch.from_numpy(w))
+    g = (rng.standard_normal(S.shape) / np.abs(S).max()).astype(real).astype(np.float64)
+    gv = RF.vjp(dev, cfg, torch.from_numpy(g))
+    torch.cuda.synchronize()
+    chi2, grad, gv = (x.cpu().numpy().astype(np.float64) for x in (chi2, grad, gv))
+    pk = dev.pk
+    for p in range(pk.natm):
+        o, nl = int(pk.arrays["lam_off"][p]), int(pk.arrays["nlam"][p])
+        d0, nd = int(pk.arrays["depth_off"][p]), int(pk.arrays["ndep"][p])
+        sl = slice(4 * o, 4 * o + 4 * nl)
+        Sp, Op, Wp, Gp = (x[sl].reshape(4, nl) for x in (S, obs, w, g))
+        assert abs(chi2[p] - (Wp * (Sp - Op) ** 2).sum()) <= ctol * chi2[p]
+        assert contract_err(grad[:, d0:d0 + nd], 2 * Wp * (Sp - Op), rfs[p]) < ctol
+        assert contract_err(gv[:, d0:d0 + nd], Gp, rfs[p]) < tol
+
+
+def test_autograd_function_uses_adjoint(golden):
+    import torch
+    b = golden("lte_batch")
+    atms = [batch_member(b, i) for i in range(3)]
+    dev, cfg = device_batch(atms, FP64)
+    params = RF.get_params(dev).clone().requires_grad_(True)
+    S = RF.synthesize(dev, cfg, params)
+    g = torch.randn_like(S) / S.detach().abs().max()
+    (S * g).sum().backward()
+    want = RF.vjp(dev, cfg, g)
+    torch.cuda.synchronize()
+    assert torch.allclose(params.grad, want, rtol=1e-12, atol=1e-12 * want.abs().max().item())
+
+
+def test_rf_matches_gpu_finite_differences(golden):
+    """Central differences of pyrh_lte_stokes (FP64) at selected depths for
+    all six parameters of two perturbed atmospheres at once."""
+    import torch
+    b = golden("lte_batch")
+    atms = [batch_member(b, i) for i in range(2)]
+    dev, cfg, _, rfs = gpu_rf(atms, FP64)
+    base = RF.get_params(dev).clone()
+    pk = dev.pk
+    nd = int(pk.arrays["ndep"][0])
+    worst = 0.0
+    for x, key in enumerate(PARAMS):
+        for k in (5, nd // 2, (2 * nd) // 3, nd - 2):
+            errs = [[] for _ in range(pk.natm)]
+            for rel in (1e-3, 1e-4, 1e-5, 1e-6, 1e-7):
+                hs, outs = [], []
+                for sgn in (1, -1):
+                    pp = base.clone()
+                    h = []
+                    for p in range(pk.natm):
+                        d = int(pk.arrays["depth_off"][p]) + k
+                        v = base[x, d].item()
+                        h.append(rel * 1e3 if key == "vel" else rel if key in ("gamma_B", "chi_B")
+                                 else rel * max(abs(v), 0.1) if key == "B" else rel * abs(v))
+                        pp[x, d] = v + sgn * h[-1]
+                    hs = h
+                    RF.set_params(dev, pp)
+                    dev.run(cfg)
+                    torch.cuda.synchronize()
+                    outs.append(dev.out.cpu().numpy().copy())
+                for p in range(pk.natm):
+                    o, nl = int(pk.arrays["lam_off"][p]), int(pk.arrays["nlam"][p])
+                    fd = (outs[0] - outs[1])[4 * o:4 * o + 4 * nl].reshape(4, nl) / (2 * hs[p])
+                    win = delo_wavelengths(atms[p])
+                    errs[p].append(np.abs(fd[:, win] - rfs[p][:, x, k][:, win]))
+            for p in range(pk.natm):
+                scale = np.abs(rfs[p][:, x]).max()
+                worst = max(worst, np.min(errs[p], axis=0).max() / scale)
+    RF.set_params(dev, base)
+    assert worst < 1e-4, worst

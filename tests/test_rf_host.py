@@ -1,0 +1,102 @@
+"""The response-function math of pyrh_gb300/csrc/lte_rf.cuh (hand-written
+adjoint of DELO-Bezier3 plus dual-number Jacobians of the Zeeman/Voigt
+opacity), evaluated on the CPU through tests/native/rf_host.cu, against
+central finite differences of the oracle's synthesis.
+
+Central differences of the whole synthesis are the reference's definition of
+depth-resolved response functions (rh/rhf1d/rf_ray.c:205-293: perturb one
+parameter at one depth, difference the emergent spectra).  The synthesis is
+only piecewise smooth: Humlicek's approximation switches region on
+|v| + a thresholds (humlicek.c:28-118) and its regions do not join exactly,
+so the spectrum jumps where a Zeeman component crosses a boundary; the
+centred derivative of bezier_aux.c switches to zero where successive slopes
+change sign.  A central difference that straddles such a point is wrong by
+the jump over the step, so every element (wavelength, Stokes) is compared at
+five steps and the closest one counts.  Errors are relative to the largest
+|RF| of that parameter over depth, wavelength and Stokes.
+
+FP32: the same math in single precision against FP64.  Apart from isolated
+elements next to a sign change of S_Q or S_U, where the two precisions take
+different branches of the centred-derivative limiter, the FP32 response
+functions agree to 1e-4; the bound is on the 99.9th percentile, with 1e-3 on
+the maximum.
+"""
+import numpy as np
+import pytest
+
+from conftest import batch_member, delo_wavelengths, rf_eval
+from oracle import oracle as O
+
+PARAMS = ["T", "vel", "vturb", "B", "gamma_B", "chi_B"]
+TOL = 1e-4
+
+
+def fd(fx, key, k, h, sel):
+    kw = dict(md_float=False, lam=fx["lam"][sel], chi_c=fx["chi_c"][sel],
+              eta_c=fx["eta_c"][sel])
+    fp, fm = dict(fx), dict(fx)
+    a = fx[key].copy(); a[k] += h; fp[key] = a
+    b = fx[key].copy(); b[k] -= h; fm[key] = b
+    return (O.lte_synth(fp, **kw) - O.lte_synth(fm, **kw)) / (2 * h)
+
+
+STEPS = (1e-3, 1e-4, 1e-5, 1e-6, 1e-7)
+
+
+def step(fx, key, k, rel):
+    """Central-difference step relative to the parameter's scale (1 km/s for
+    v_los, 1 rad for the angles, at least 0.1 T for B).  Two errors bound
+    the usable steps from either side: the FP64 synthesis carries ~1e-11
+    relative noise (the closed-form Bezier weights just above their Taylor
+    threshold lose digits), which small steps amplify, and Humlicek region
+    jumps can sit within 1e-6 of a parameter's scale, which large steps
+    straddle; so five steps over four decades are tried per element."""
+    base = fx[key][k]
+    if key == "vel":
+        return rel * 1e3
+    if key in ("gamma_B", "chi_B"):
+        return rel
+    if key == "B":
+        return rel * max(abs(base), 0.1)
+    return rel * abs(base)
+
+
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_batch:0", "lte_batch:1"])
+def test_adjoint_matches_finite_differences(rf_harness, golden, name):
+    if ":" in name:
+        n, i = name.split(":")
+        fx = batch_member(golden(n), int(i))
+    else:
+        fx = golden(name)
+    win = delo_wavelengths(fx)
+    sel = win[::9] if len(win) > 40 else win
+    st, rf = rf_eval(rf_harness, fx, sel)
+    ref = O.lte_synth(fx, md_float=False, lam=fx["lam"][sel], chi_c=fx["chi_c"][sel],
+                      eta_c=fx["eta_c"][sel])
+    assert np.abs(st.T - ref).max() <= 1e-9 * ref[0].max()
+    nd = len(fx["T"])
+    depths = sorted({2, nd // 4, nd // 2, (2 * nd) // 3, nd - 6, nd - 2, nd - 1})
+    worst = {}
+    for x, key in enumerate(PARAMS):
+        scale = np.abs(rf[:, :, x, :]).max()
+        if scale == 0.0:
+            continue
+        for k in depths:
+            ad = rf[:, :, x, k].T
+            errs = [np.abs(ad - fd(fx, key, k, step(fx, key, k, r), sel))
+                    for r in STEPS]
+            worst[(key, k)] = np.min(errs, axis=0).max() / scale
+    bad = {k: v for k, v in worst.items() if v > TOL}
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge"])
+def test_single_precision_adjoint(rf_harness, golden, name):
+    fx = golden(name)
+    win = delo_wavelengths(fx)
+    _, rf64 = rf_eval(rf_harness, fx, win)
+    _, rf32 = rf_eval(rf_harness, fx, win, single=True)
+    for x in range(6):
+        scale = np.abs(rf64[:, :, x]).max()
+        e = np.abs(rf32[:, :, x] - rf64[:, :, x]) / scale
+        assert np.percentile(e, 99.9) < 1e-4 and e.max() < 1e-3, (PARAMS[x], e.max())
