@@ -29,6 +29,9 @@ METRIC = ("pixel·λ·μ formal solutions/s and RF gradients/s vs plain FP64 "
           "GPU, at 1e-4 rel err")
 UNIT = "pixel*lambda*mu/s"
 WORKLOAD = "batched LTE Stokes synthesis: 16384 atm x 71 depths x 2x112 lambda, mu=1, FP32"
+# DRAM bytes (read + write) per atmosphere of one lte_stokes_kernel launch:
+# ncu, 2048 atmospheres, 285.6 MB + 76.5 MB (profiles/lte_stokes_kernel_batched_16384x224.md).
+TRAFFIC_PER_ATM = (285.631488e6 + 76.459520e6) / 2048
 
 
 def parse():
@@ -40,6 +43,10 @@ def parse():
     ap.add_argument("--natm", type=int, default=16384)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-rf", action="store_true")
+    ap.add_argument("--skip-nlte", action="store_true")
+    ap.add_argument("--rf-natm", type=int, default=4096)
+    ap.add_argument("--nlte-natm", type=int, default=1024)
     return ap.parse_args()
 
 
@@ -122,6 +129,101 @@ def cpu_baseline_port(batch, nthreads, seconds):
     return {"value": units / t, "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": f"{n2} of the {natm} atmospheres x {len(batch['lam'])} lambda, "
                       f"FP64 oracle (oracle/rt_oracle.c), {t:.1f} s"}
+
+
+def _events_ms(fn, stream, n):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(n):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / n
+
+
+def rf_measure(natm, local, stream, steps, warmup):
+    """Adjoint of the batched synthesis: chi^2 against noisy targets
+    synthesised from perturbed copies (sigma = 1e-3 I_c), its gradient with
+    respect to T, v_los, v_mic, B, gamma, chi at every depth, and the full
+    depth-resolved response functions, for natm atmospheres (FP32)."""
+    import torch
+    from pyrh_gb300 import _lib as L
+    from pyrh_gb300 import lte, rf as RF, workload
+    batch = workload.synthetic_batch(natm, seed=3000 + local, dtype=np.float32)
+    pert = workload.synthetic_batch(natm, seed=4000 + local, dtype=np.float32)
+    lines, nline = lte.make_lines(batch["line_const"], batch["zeeman"], batch["zeeman_n"])
+    dev = lte.DeviceBatch(lte.pack_uniform(batch, nline, L.PYRH_FP32), lines, nline,
+                          device=f"cuda:{local}")
+    tgt = lte.DeviceBatch(lte.pack_uniform(pert, nline, L.PYRH_FP32), lines, nline,
+                          device=f"cuda:{local}")
+    cfg = lte.make_config(precision=L.PYRH_FP32, mu=1.0, vmicro_char=batch["vmicro_char"])
+    sp = stream.cuda_stream
+    tgt.run(cfg, sp)
+    torch.cuda.synchronize()
+    nl = dev.pk.max_nlam
+    S = tgt.out.view(natm, 4, nl)
+    ic = S[:, 0].max(dim=1).values[:, None, None]
+    gen = torch.Generator(device=S.device).manual_seed(5)
+    sigma = 1e-3 * ic
+    obs = (S + sigma * torch.randn(S.shape, device=S.device, generator=gen)).reshape(-1)
+    w = (1.0 / sigma ** 2).expand(natm, 4, nl).reshape(-1).contiguous()
+    with torch.cuda.stream(stream):
+        for _ in range(max(warmup, 3)):
+            dev.run(cfg, sp)
+            RF.chi2_grad(dev, cfg, obs, w, sp)
+        fwd_ms = _events_ms(lambda: dev.run(cfg, sp), stream, steps)
+        grad_ms = _events_ms(lambda: RF.chi2_grad(dev, cfg, obs, w, sp), stream, steps)
+        RF.response_functions(dev, cfg, sp)
+        rf_ms = _events_ms(lambda: RF.response_functions(dev, cfg, sp), stream, 2)
+    units = natm * nl
+    return {"workload": f"chi^2 gradient and response functions: {natm} atm x 71 depths x "
+                        f"{nl} lambda, FP32, targets from perturbed copies + noise 1e-3 I_c",
+            "gradients_per_s": {"value": units / (grad_ms / 1e3), "unit": UNIT},
+            "ms_forward": fwd_ms, "ms_chi2_gradient": grad_ms,
+            "gradient_cost_vs_forward": grad_ms / fwd_ms,
+            "ms_response_functions": rf_ms,
+            "rf_bytes_written": int(4 * 6 * 71 * units * 4)}
+
+
+def nlte_measure(natm, local):
+    """Batched NLTE MALI (C4 shapes): natm atmospheres cycled from the three
+    reference fixtures (82, 50 and 120 depths; 787, 629 and 989 wavelengths;
+    five rays; Ng order 2 every 5 iterations after 5), each solved
+    independently in one batch.  Converged atmospheres per second and the
+    largest population error against the reference's converged populations
+    at the same convergence limit."""
+    import torch
+    from pyrh_gb300 import _lib as L
+    from pyrh_gb300 import nlte
+    names = ["nlte_c1", "nlte_c4_50", "nlte_c4_120"]
+    gold = [dict(np.load(os.path.join(HERE, "tests", "golden", n + ".npz"))) for n in names]
+    atms = [gold[i % 3] for i in range(natm)]
+    src = [i % 3 for i in range(natm)]
+    out = {"workload": f"batched NLTE: {natm} atmospheres (50/82/120 depths, 629-989 lambda, "
+                       "5 rays, 6-level atom), formal solution FP32, rates/LU/Ng FP64"}
+    for prec, tag in ((L.PYRH_FP32, "fp32"), (L.PYRH_FP64, "fp64")):
+        cfg = nlte.make_config(gold[0], prec)
+        pk = nlte.pack(atms, cfg.nrays)
+        dev = nlte.DeviceNlte(pk, cfg, device=f"cuda:{local}")
+        st = dev.solve(cfg)                      # warm-up (first-touch of the workspace)
+        dev.reset()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = dev.solve(cfg)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        its = dev.iterations.cpu().numpy()
+        pops = dev.populations()
+        err = max(float(np.abs(pops[i] / gold[src[i]]["n_final"] - 1).max()) for i in range(natm))
+        out[tag] = {"status": int(st), "seconds": t, "converged_atm_per_s": natm / t,
+                    "iterations_min_max": [int(its.min()), int(its.max())],
+                    "max_population_rel_err_vs_reference": err,
+                    "launches": int(L.lib().pyrh_last_launch_count())}
+        del dev
+        torch.cuda.empty_cache()
+    return out
 
 
 def reference_arm(args):
@@ -288,6 +390,16 @@ def main():
                  "speedup_vs_fp64_single_pixel": value / world / fp64_single}
         del singles, db64
 
+    del db
+    torch.cuda.empty_cache()
+    if rank == 0 and not args.skip_rf:
+        extra["rf"] = rf_measure(args.rf_natm, local, stream, max(2, min(args.steps, 5)),
+                                 args.warmup)
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.skip_nlte:
+        extra["nlte"] = nlte_measure(args.nlte_natm, local)
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0:
         batch64 = {k: v for k, v in batch.items()}
@@ -300,9 +412,15 @@ def main():
                 "dtype": "f32", "data": "synthetic", "config": config_dict(natm),
                 "clocks": clk, "e2e": e2e, "gpu_launches": launches,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": None,
+                             "frac": achieved / peak,
+                             "traffic": TRAFFIC_PER_ATM * natm,
+                             "traffic_source": "ncu dram__bytes_read+write of one launch at "
+                                               "2048 atmospheres, scaled by atmospheres "
+                                               "(profiles/lte_stokes_kernel_batched_16384x224.md)",
                              "peak_source": peak_src, "alg_bytes_per_launch": alg_bytes,
-                             "kernel": "lte_stokes_kernel<float,false>"},
+                             "kernel": "lte_stokes_kernel<float,false>",
+                             "note": "FP32-pipe bound (ncu: 70 % issue, 45 % FMA pipe); "
+                                     "the HBM fraction is small by construction"},
                 "cpu_baseline": cpu}
         line.update(extra)
         print(json.dumps(line), flush=True)

@@ -119,7 +119,9 @@ typedef struct {
   double  mu;                  /* cosine of the ray to the observer */
   double  vmicro_char;         /* VMICRO_CHAR [m/s]: line window 20 v/c */
   int32_t block_lambda;        /* wavelengths per block; 0 = tuned default */
-  int32_t persistent_blocks;   /* blocks of the persistent grid; 0 = auto */
+  int32_t persistent_blocks;   /* 0: one block per (atmosphere, wavelength
+                                  tile); > 0: at most this many blocks, each
+                                  looping over tiles */
 } pyrh_lte_config;
 
 /* Emergent Stokes vectors for a batch; replaces the per-atmosphere hot loop

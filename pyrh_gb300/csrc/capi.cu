@@ -30,17 +30,6 @@ pyrh_status fail(pyrh_status s, const char* fmt, ...) {
       return fail(PYRH_ERR_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_));        \
   } while (0)
 
-int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
-  return n;
-}
-
 int round_up(int x, int m) { return (x + m - 1) / m * m; }
 
 pyrh_status check_lines_host(const pyrh_line* lines, int nline, int stokes_mode) {
@@ -141,16 +130,16 @@ pyrh_status launch(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nline,
   if (smem > 200 * 1024)
     return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
                 nline, a.maxd);
+  // One block per (atmosphere, wavelength tile) by default: a block that
+  // finishes early frees its SM slot for the next one, where a persistent
+  // grid would make its warps wait at the next work item's barrier
+  // (measured 18.9 ms against 22.2 ms for 16384 atmospheres x 224 lambda).
+  // persistent_blocks > 0 caps the grid; blocks then loop over work items.
   const long long work = (long long)a.natm * a.tiles;
-  int grid = cfg->persistent_blocks;
-  if (grid <= 0) {
-    // persistent grid: every SM filled to its resident-block limit
-    int per_sm = pyrh::lte_blocks_per_sm(cfg->precision, a.magneto_optical, block, smem);
-    if (per_sm < 1) per_sm = 1;
-    grid = sm_count() * per_sm;
-  }
-  if (grid > work) grid = (int)work;
-  cudaError_t e = pyrh::launch_lte_stokes(a, block, grid, st);
+  long long grid = cfg->persistent_blocks > 0 ? cfg->persistent_blocks : work;
+  if (grid > work) grid = work;
+  if (grid > 0x7fffffffLL) grid = 0x7fffffffLL;
+  cudaError_t e = pyrh::launch_lte_stokes(a, block, (int)grid, st);
   if (e != cudaSuccess) return fail(PYRH_ERR_CUDA, "lte_stokes launch: %s", cudaGetErrorString(e));
   g_last_launches = 1;
   return PYRH_OK;
@@ -192,14 +181,10 @@ pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nli
     return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
                 nline, ra.lte.maxd);
   const long long work = (long long)ra.lte.natm * ra.lte.tiles;
-  int grid = cfg->persistent_blocks;
-  if (grid <= 0) {
-    int per_sm = pyrh::rf_blocks_per_sm(cfg->precision, mode, block, smem);
-    if (per_sm < 1) per_sm = 1;
-    grid = sm_count() * per_sm;
-  }
-  if (grid > work) grid = (int)work;
-  cudaError_t e = pyrh::launch_lte_rf(ra, block, grid, st);
+  long long grid = cfg->persistent_blocks > 0 ? cfg->persistent_blocks : work;
+  if (grid > work) grid = work;
+  if (grid > 0x7fffffffLL) grid = 0x7fffffffLL;
+  cudaError_t e = pyrh::launch_lte_rf(ra, block, (int)grid, st);
   if (e != cudaSuccess) return fail(PYRH_ERR_CUDA, "lte_rf launch: %s", cudaGetErrorString(e));
   return PYRH_OK;
 }

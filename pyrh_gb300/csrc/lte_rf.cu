@@ -3,10 +3,10 @@
 //
 // One thread owns one (atmosphere, wavelength) pair, as in lte_stokes.cu.
 // Per block (one atmosphere, one tile of wavelengths) the per-(line, depth)
-// quantities and the projected field geometry are computed once, with their
-// derivatives with respect to (T, v_los, v_mic, B, gamma, chi) of the same
-// depth, into shared memory (forward-mode dual numbers, lte_rf.cuh).  Each
-// thread then
+// quantities and the projected field geometry are computed once, in the
+// working precision, with their derivatives with respect to (T, v_los,
+// v_mic, B, gamma, chi) of the same depth, into shared memory (forward-mode
+// dual numbers, lte_rf.cuh).  Each thread then
 //   1. evaluates the optical quantities q_k = (chi, S_I..S_V, K'_Q..K'_V) of
 //      its wavelength at every depth and runs the DELO-Bezier3 recurrence
 //      (bezier_1D.c:52-300) to the surface, keeping the recurrence state on a
@@ -15,15 +15,18 @@
 //   2. runs the hand-written adjoint of that recurrence back down
 //      (delo_reverse_stream), which hands over dL/dq_k as soon as depth k is
 //      final;
-//   3. at each handed-over depth, re-evaluates q_k with its dual numbers to
-//      get dq_k/dx_k and writes dL/dx_k: for response functions the four
+//   3. at each handed-over depth, carries dL/dq_k backwards through the
+//      opacity of that depth (local_q_vjp: through the line sums and Zeeman
+//      components to the per-line primitives, whose derivatives with respect
+//      to the parameters are the dual parts in shared memory) and writes
+//      dL/dx_k: for response functions the four
 //      Stokes seeds give RF[s][x][k] (written wavelength-fastest, coalesced);
 //      for the chi^2 gradient the single seed 2 w (S - obs), and for a
 //      vector-Jacobian product the caller's dL/dS, give one value per
 //      (x, k), summed over the block's wavelengths in shared memory and then
 //      added to the atmosphere's gradient in HBM.
-// The local Jacobian is recomputed, not stored, so the tape holds 21 values
-// per depth; four depths of adjoints are live at a time.
+// The opacity derivatives are recomputed at each depth, not stored, so the
+// tape holds 21 values per depth; four depths of adjoints are live at a time.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -77,15 +80,6 @@ __host__ __device__ size_t rf_smem_t(int nline, int maxd, RfSmem<R>* s, unsigned
   return off;
 }
 
-template <typename R>
-__device__ D6<R> to_r(const D6<double>& a) {
-  D6<R> o;
-  o.v = R(a.v);
-#pragma unroll
-  for (int i = 0; i < kNX; ++i) o.d[i] = R(a.d[i]);
-  return o;
-}
-
 // What one thread needs to evaluate q and dq/dx at any depth.
 template <typename R>
 struct Local {
@@ -104,21 +98,24 @@ struct Emit {
   double lam;
   int nd, nl, la;
   R* rf;             // mode 0: rf_out + 24 * cont_off + la
+  const Tape<R>* tp;
   __device__ void operator()(int k, const R* qb, const R* bpl) const {
     constexpr int NS = MODE == 0 ? 4 : 1;
     const RfSmem<R>& sm = *loc->sm;
-    R q[8], J[8][kNX];
-    local_q_jac<R>(loc->nline, sm.ld + k, loc->maxd, sm.geo[k], loc->dlam, loc->inwin, sm.ncomp,
-                   sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS, loc->chi_c[(int64_t)k * nl],
-                   loc->eta_c[(int64_t)k * nl], q, J);
+    R g[NS][kNX];
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+#pragma unroll
+      for (int x = 0; x < kNX; ++x) g[s][x] = R(0);
+    local_q_vjp<R, NS>(loc->nline, sm.ld + k, loc->maxd, sm.geo[k], loc->dlam, loc->inwin,
+                       sm.ncomp, sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS, tp->q[k], qb,
+                       g);
     const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lam)) : R(0);
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
 #pragma unroll
       for (int x = 0; x < kNX; ++x) {
-        R v = 0;
-#pragma unroll
-        for (int n = 0; n < 8; ++n) v += qb[s * 8 + n] * J[n][x];
+        R v = g[s][x];
         if (x == 0) v += bpl[s] * dB;
         if (MODE == 0) rf[((int64_t)(s * kNX + x) * nd + k) * nl] = v;
         else atomicAdd(&sm.grad[x * loc->maxd + k], v);   // modes 1 and 2
@@ -169,10 +166,7 @@ __global__ void __launch_bounds__(128) lte_rf_kernel(RfArgs ra) {
     for (int k = threadIdx.x; k < nd; k += BL) {
       const int64_t d = doff + k;
       sm.ds[k] = (k >= 1) ? R(fabs(args.height[d] - args.height[d - 1]) * imu) : R(0);
-      const GeoD<double> g = geometry_d<double>(args.gamma_B[d], args.chi_B[d], muz);
-      GeoD<R> gr;
-      gr.gQ = to_r<R>(g.gQ); gr.gU = to_r<R>(g.gU); gr.gV = to_r<R>(g.gV); gr.s2g = to_r<R>(g.s2g);
-      sm.geo[k] = gr;
+      sm.geo[k] = geometry_d<R>(R(args.gamma_B[d]), R(args.chi_B[d]), R(muz));
       if (MODE != 0)
         for (int x = 0; x < kNX; ++x) sm.grad[x * args.maxd + k] = R(0);
     }
@@ -184,15 +178,12 @@ __global__ void __launch_bounds__(128) lte_rf_kernel(RfArgs ra) {
       const LineConstD c = {L.lambda0, L.Ei, L.gi, L.Aji, L.Bji, L.Bij, L.Grad, L.GStark,
                             L.GvdWaals, L.cross, L.alpha, L.isotope_frac, L.hyperfine_frac,
                             L.weight, L.vdwaals};
-      const LineDepth<double> ld = line_depth<double>(
-          c, args.T[d], args.vlos[d], args.vturb[d], args.B[d], args.ne[d], args.nHtot[d],
-          args.np[d], args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d],
-          args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d], muz, args.moving != 0);
-      LineDepth<R> o;
-      o.inv_vb = to_r<R>(ld.inv_vb); o.vshift = to_r<R>(ld.vshift); o.adamp = to_r<R>(ld.adamp);
-      o.vB = to_r<R>(ld.vB); o.chil = to_r<R>(ld.chil); o.etal = to_r<R>(ld.etal);
-      o.gauss = ld.gauss;
-      sm.ld[l * args.maxd + k] = o;
+      sm.ld[l * args.maxd + k] = line_depth<R>(
+          c, R(args.T[d]), R(args.vlos[d]), R(args.vturb[d]), R(args.B[d]), R(args.ne[d]),
+          R(args.nHtot[d]), R(args.np[d]),
+          R(args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d]),
+          R(args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d]), R(muz),
+          args.moving != 0);
     }
     __syncthreads();
 
@@ -229,6 +220,7 @@ __global__ void __launch_bounds__(128) lte_rf_kernel(RfArgs ra) {
 
       Emit<R, MODE> em;
       em.loc = &loc;
+      em.tp = &tp;
       em.T = args.T + doff;
       em.lam = lam;
       em.nd = nd;
@@ -283,14 +275,6 @@ cudaError_t launch_mode(const RfArgs& a, int block, int grid, size_t smem, cudaS
   return cudaGetLastError();
 }
 
-template <typename R, int MODE>
-int per_sm_mode(int block, size_t smem) {
-  int n = 0;
-  cudaFuncSetAttribute(lte_rf_kernel<R, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lte_rf_kernel<R, MODE>, block, smem);
-  return n;
-}
-
 }  // namespace
 
 size_t rf_smem_bytes(int precision, int nline, int maxd) {
@@ -299,22 +283,10 @@ size_t rf_smem_bytes(int precision, int nline, int maxd) {
 }
 
 template <typename R>
-int per_sm_t(int mode, int block, size_t smem) {
-  if (mode == 0) return per_sm_mode<R, 0>(block, smem);
-  if (mode == 1) return per_sm_mode<R, 1>(block, smem);
-  return per_sm_mode<R, 2>(block, smem);
-}
-
-template <typename R>
 cudaError_t launch_t(const RfArgs& a, int block, int grid, size_t smem, cudaStream_t st) {
   if (a.mode == 0) return launch_mode<R, 0>(a, block, grid, smem, st);
   if (a.mode == 1) return launch_mode<R, 1>(a, block, grid, smem, st);
   return launch_mode<R, 2>(a, block, grid, smem, st);
-}
-
-int rf_blocks_per_sm(int precision, int mode, int block, size_t smem) {
-  return precision == PYRH_FP32 ? per_sm_t<float>(mode, block, smem)
-                                : per_sm_t<double>(mode, block, smem);
 }
 
 cudaError_t launch_lte_rf(const RfArgs& a, int block, int grid, cudaStream_t st) {

@@ -343,6 +343,106 @@ PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, int ld_stride, const
   }
 }
 
+// Reverse-mode contraction of the local opacity: for NS adjoint vectors
+// qb[s][8] = dL_s/dq (q as in local_q_jac), accumulates
+// out[s][x] += sum_n qb[s][n] dq_n/dx for the six parameters of this depth.
+// Instead of carrying six derivative directions through every profile sum
+// (local_q_jac), the adjoints run backwards from q through the line sums and
+// the Zeeman components to the per-line primitives (a, v, v_B, chi_l, eta_l)
+// and the field geometry, and only those are multiplied by their
+// derivatives with respect to the parameters (the .d parts of LineDepth and
+// GeoD).  q holds the forward values of this depth (the tape).
+template <typename R, int NS>
+PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
+                         const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
+                         const R* cweight, const int* cq, int maxcomp, const R q[8],
+                         const R* qb, R out[NS][kNX]) {
+  const R ichi = R(1) / q[0];
+  R eb[NS][4], cb[NS][4];
+  R gb[NS][4];   // adjoints of s2g, gQ, gU, gV
+  for (int s = 0; s < NS; ++s) {
+    const R* a = qb + s * 8;
+    R chib = a[0];
+    for (int n = 1; n < 8; ++n) chib -= a[n] * q[n] * ichi;
+    cb[s][0] = chib;
+    for (int j = 0; j < 3; ++j) cb[s][j + 1] = a[5 + j] * ichi;
+    for (int j = 0; j < 4; ++j) eb[s][j] = a[1 + j] * ichi;
+    for (int j = 0; j < 4; ++j) gb[s][j] = R(0);
+  }
+  for (int l = 0; l < nline; ++l) {
+    if (!((inwin >> l) & 1u)) continue;
+    const LineDepth<R>& L = ld[l * ld_stride];
+    const R v = dlam[l] * L.inv_vb.v + L.vshift.v;
+    R ab[NS], vb[NS], vBb[NS], chilb[NS], etalb[NS];
+    if (L.gauss) {
+      const R phi = (fabs(v) <= R(kMAX_GAUSS_DOPPLER)) ? dev_exp(-v * v) : R(0);
+      for (int s = 0; s < NS; ++s) {
+        const R phib = cb[s][0] * L.chil.v + eb[s][0] * L.etal.v;
+        chilb[s] = cb[s][0] * phi;
+        etalb[s] = eb[s][0] * phi;
+        vb[s] = phib * (R(-2) * v * phi);
+        ab[s] = vBb[s] = R(0);
+      }
+    } else {
+      R phb[NS][3];
+      for (int s = 0; s < NS; ++s) {
+        R fI = cb[s][0] * L.chil.v + eb[s][0] * L.etal.v;
+        R fQ = cb[s][1] * L.chil.v + eb[s][1] * L.etal.v;
+        R fU = cb[s][2] * L.chil.v + eb[s][2] * L.etal.v;
+        R fV = cb[s][3] * L.chil.v + eb[s][3] * L.etal.v;
+        const R delb = fI * geo.s2g.v + fQ * geo.gQ.v + fU * geo.gU.v;
+        const R sigb = R(0.5) * fI - R(0.25) * delb;
+        phb[s][1] = R(0.5) * delb;
+        phb[s][2] = sigb + R(0.5) * fV * geo.gV.v;
+        phb[s][0] = sigb - R(0.5) * fV * geo.gV.v;
+        ab[s] = vb[s] = vBb[s] = R(0);
+      }
+      R ph[3] = {0, 0, 0};
+      for (int c = 0; c < ncomp[l]; ++c) {
+        const R sh = cshift[l * maxcomp + c], w = cweight[l * maxcomp + c];
+        Cx<R> W, dW;
+        humlicek_d<R>(L.adamp.v, v - sh * L.vB.v, W, dW);
+        const int qi0 = cq[l * maxcomp + c] + 1;
+        const int qi = qi0 < 0 ? 0 : (qi0 > 2 ? 2 : qi0);
+        ph[qi] += w * W.r;
+        for (int s = 0; s < NS; ++s) {
+          const R hb = w * phb[s][qi];
+          const R xb = hb * dW.i;   // dH/dx = Im W' (t = a - i x)
+          ab[s] += hb * dW.r;       // dH/da = Re W'
+          vb[s] += xb;
+          vBb[s] -= sh * xb;
+        }
+      }
+      const R sig = ph[2] + ph[0];
+      const R del = R(0.5) * ph[1] - R(0.25) * sig;
+      const R phiI = del * geo.s2g.v + R(0.5) * sig;
+      const R phiQ = del * geo.gQ.v, phiU = del * geo.gU.v;
+      const R dV = R(0.5) * (ph[2] - ph[0]);
+      const R phiV = dV * geo.gV.v;
+      for (int s = 0; s < NS; ++s) {
+        chilb[s] = cb[s][0] * phiI + cb[s][1] * phiQ + cb[s][2] * phiU + cb[s][3] * phiV;
+        etalb[s] = eb[s][0] * phiI + eb[s][1] * phiQ + eb[s][2] * phiU + eb[s][3] * phiV;
+        const R fI = cb[s][0] * L.chil.v + eb[s][0] * L.etal.v;
+        const R fQ = cb[s][1] * L.chil.v + eb[s][1] * L.etal.v;
+        const R fU = cb[s][2] * L.chil.v + eb[s][2] * L.etal.v;
+        const R fV = cb[s][3] * L.chil.v + eb[s][3] * L.etal.v;
+        gb[s][0] += fI * del;
+        gb[s][1] += fQ * del;
+        gb[s][2] += fU * del;
+        gb[s][3] += fV * dV;
+      }
+    }
+    for (int s = 0; s < NS; ++s)
+      for (int x = 0; x < kNX; ++x)
+        out[s][x] += ab[s] * L.adamp.d[x] + vb[s] * (dlam[l] * L.inv_vb.d[x] + L.vshift.d[x]) +
+                     vBb[s] * L.vB.d[x] + chilb[s] * L.chil.d[x] + etalb[s] * L.etal.d[x];
+  }
+  for (int s = 0; s < NS; ++s)
+    for (int x = 0; x < kNX; ++x)
+      out[s][x] += gb[s][0] * geo.s2g.d[x] + gb[s][1] * geo.gQ.d[x] + gb[s][2] * geo.gU.d[x] +
+                   gb[s][3] * geo.gV.d[x];
+}
+
 // Values of q only (the forward sweep): the same sums as local_q_jac on the
 // value parts, with the single-precision fast Humlicek where R is float.
 template <typename R>
@@ -707,10 +807,12 @@ template <typename R, int NS, typename Emit>
 PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double B0, double B1,
                                  const R seed[NS][4], Emit&& emit) {
   const int N = nd;
-  R ring[4][NS][8];
-  for (int a = 0; a < 4; ++a)
-    for (int s = 0; s < NS; ++s)
-      for (int n = 0; n < 8; ++n) ring[a][s][n] = R(0);
+  // Adjoints of the four live depths, named by their place relative to the
+  // step being reversed (k+1, k, k-1, k-2) and rotated after each step, so
+  // every index is known at compile time and the arrays stay in registers.
+  R qu[NS][8], qc[NS][8], qd[NS][8], qdd[NS][8];
+  for (int s = 0; s < NS; ++s)
+    for (int n = 0; n < 8; ++n) qu[s][n] = qc[s][n] = qd[s][n] = qdd[s][n] = R(0);
   R zero_b[NS];
   for (int s = 0; s < NS; ++s) zero_b[s] = R(0);
   R Ib[NS][4], dSb[NS][4], dKb[NS][3], dchib[NS], Tb[NS];
@@ -733,8 +835,8 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
     const R bv[3] = {g * k0[0], g * k0[1], g * k0[2]};
     const R Dn = R(1) - (bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2]);
     const R x0 = (V[0] - (bv[0] * V[1] + bv[1] * V[2] + bv[2] * V[3])) / Dn;
-    R(&q0)[NS][8] = ring[0];
-    R(&q1)[NS][8] = ring[1];
+    R(&q0)[NS][8] = qd;   // depth 0 is k-1 of the first step
+    R(&q1)[NS][8] = qc;   // depth 1 is its k
     for (int s = 0; s < NS; ++s) {
       R Vb[4] = {0, 0, 0, 0}, bb[3] = {0, 0, 0};
       R x0b = seed[s][0];
@@ -786,11 +888,6 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
   }
   // ---- steps k = 1 .. N-2 (reverse order of the forward sweep) ----
   for (int k = 1; k <= N - 2; ++k) {
-    R(&qu)[NS][8] = ring[(k + 1) & 3];
-    R(&qc)[NS][8] = ring[k & 3];
-    R(&qd)[NS][8] = ring[(k - 1) & 3];
-    for (int s = 0; s < NS; ++s)
-      for (int n = 0; n < 8; ++n) qu[s][n] = R(0);   // depth k+1 is first reached here
     const R Tk = tp.T[k], Tdw = tp.T[k - 1];
     StepIn<R> st;
     R cf[5], dcf[5];
@@ -807,8 +904,11 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       st.dSu[n] = tp.dS0[kup][n]; st.dS0[n] = tp.dS0[k][n];
       st.Iu[n] = tp.I[k + 1][n];
     }
-    R x[4], V[4], bvec[3], c;
-    step_fwd(st, x, V, bvec, c);
+    // the step's solution is I_k on the tape; b and c of its matrix are cheap
+    const R c = st.ga * st.dt03, pK = st.al + st.ga * (R(1) + st.dt03);
+    R bvec[3];
+    for (int n = 0; n < 3; ++n) bvec[n] = pK * st.k0[n] + c * st.dk0[n];
+    const R* x = tp.I[k];
     const R dsdn = ds[k];
     const R dchi_c = tp.dchi[k], dchi_dn = tp.dchi[k - 1];
     const bool c2pos = tp.q[k][0] + (dsdn / R(3)) * dchi_c > R(0);
@@ -843,7 +943,7 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       if (k > 1) {
         R d1 = 0, d2 = 0;
         cent_deriv_vjp<R>(dsdn, ds[k - 1], tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0], dchi_dnb, d1,
-                          d2, qc[s][0], qd[s][0], ring[(k - 2) & 3][s][0]);
+                          d2, qc[s][0], qd[s][0], qdd[s][0]);
       } else {
         qd[s][0] += dchi_dnb / dsdn;
         qc[s][0] -= dchi_dnb / dsdn;
@@ -854,7 +954,15 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       Tb[s] = Tkb;
     }
     // depth k-2 received its last term from this step's chi derivative
-    if (k >= 2 && k - 2 <= N - 4) emit(k - 2, &ring[(k - 2) & 3][0][0], zero_b);
+    if (k >= 2) emit(k - 2, &qdd[0][0], zero_b);
+    // rotate: depth k+2 (first reached by the next step) starts at zero
+    for (int s = 0; s < NS; ++s)
+      for (int n = 0; n < 8; ++n) {
+        qdd[s][n] = qd[s][n];
+        qd[s][n] = qc[s][n];
+        qc[s][n] = qu[s][n];
+        qu[s][n] = R(0);
+      }
   }
   // ---- initial values (k = N-2 set-up and the bottom boundary) ----
   R bpl[2][NS];
@@ -865,42 +973,44 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
     const R cu = tp.q[k + 1][0], cc = tp.q[k][0];
     const R dchi_c = tp.dchi[k], dchi_up = tp.dchi_up0;
     const double dtau0 = 0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * (double)ds[N - 1];
-    R(&qu)[NS][8] = ring[(k + 1) & 3];
-    R(&qc)[NS][8] = ring[k & 3];
-    R(&qd)[NS][8] = ring[(k - 1) & 3];
+    // after the last rotation depth N-1 is in qc, N-2 in qd and N-3 in qdd;
+    // this set-up step reaches exactly those three (eu, ec, ed below)
+    R(&eu)[NS][8] = qc;
+    R(&ec)[NS][8] = qd;
+    R(&ed)[NS][8] = qdd;
     for (int s = 0; s < NS; ++s) {
       for (int n = 0; n < 4; ++n) {
-        qc[s][1 + n] += dSb[s][n] / T;
-        qu[s][1 + n] -= dSb[s][n] / T;
+        ec[s][1 + n] += dSb[s][n] / T;
+        eu[s][1 + n] -= dSb[s][n] / T;
         Tb[s] -= dSb[s][n] * tp.dS0[N - 1][n] / T;
       }
       for (int n = 0; n < 3; ++n) {
-        qc[s][5 + n] += dKb[s][n] / T;
-        qu[s][5 + n] -= dKb[s][n] / T;
+        ec[s][5 + n] += dKb[s][n] / T;
+        eu[s][5 + n] -= dKb[s][n] / T;
         Tb[s] -= dKb[s][n] * tp.dK0[N - 1][n] / T;
       }
       const R a = R(0.25) * dsup * Tb[s];
-      qc[s][0] += a;
-      qu[s][0] += a;
+      ec[s][0] += a;
+      eu[s][0] += a;
       R dchi_cb = dchib[s], dchi_upb = R(0);
-      if (cc - (dsup / R(3)) * dchi_c > R(0)) { qc[s][0] += a; dchi_cb -= (dsup / R(3)) * a; }
-      if (cu + (dsup / R(3)) * dchi_up > R(0)) { qu[s][0] += a; dchi_upb += (dsup / R(3)) * a; }
-      qc[s][0] += dchi_upb / dsup;
-      qu[s][0] -= dchi_upb / dsup;
+      if (cc - (dsup / R(3)) * dchi_c > R(0)) { ec[s][0] += a; dchi_cb -= (dsup / R(3)) * a; }
+      if (cu + (dsup / R(3)) * dchi_up > R(0)) { eu[s][0] += a; dchi_upb += (dsup / R(3)) * a; }
+      ec[s][0] += dchi_upb / dsup;
+      eu[s][0] -= dchi_upb / dsup;
       R d1 = 0, d2 = 0;
-      cent_deriv_vjp<R>(dsup, dsdn, cu, cc, tp.q[k - 1][0], dchi_cb, d1, d2, qu[s][0], qc[s][0],
-                        qd[s][0]);
+      cent_deriv_vjp<R>(dsup, dsdn, cu, cc, tp.q[k - 1][0], dchi_cb, d1, d2, eu[s][0], ec[s][0],
+                        ed[s][0]);
       const double ib = (double)Ib[s][0];
       bpl[1][s] = R(ib * (1.0 + 1.0 / dtau0));
       bpl[0][s] = R(-ib / dtau0);
       const double dtb = ib * (B0 - B1) / (dtau0 * dtau0);
-      qu[s][0] += R(0.5 * (double)ds[N - 1] * dtb);
-      qc[s][0] += R(0.5 * (double)ds[N - 1] * dtb);
+      eu[s][0] += R(0.5 * (double)ds[N - 1] * dtb);
+      ec[s][0] += R(0.5 * (double)ds[N - 1] * dtb);
     }
   }
-  emit(N - 3, &ring[(N - 3) & 3][0][0], zero_b);
-  emit(N - 2, &ring[(N - 2) & 3][0][0], bpl[0]);
-  emit(N - 1, &ring[(N - 1) & 3][0][0], bpl[1]);
+  emit(N - 3, &qdd[0][0], zero_b);
+  emit(N - 2, &qd[0][0], bpl[0]);
+  emit(N - 1, &qc[0][0], bpl[1]);
 }
 
 // dB_nu/dT of planck() (planck.c:38-63)

@@ -609,24 +609,6 @@ static cudaError_t launch_t(const LteArgs& a, int block, int grid, cudaStream_t 
   return cudaGetLastError();
 }
 
-template <typename R>
-static int blocks_per_sm_t(int mo, int block, size_t smem) {
-  int n = 0;
-  if (mo) {
-    cudaFuncSetAttribute(lte_stokes_kernel<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lte_stokes_kernel<R, true>, block, smem);
-  } else {
-    cudaFuncSetAttribute(lte_stokes_kernel<R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lte_stokes_kernel<R, false>, block, smem);
-  }
-  return n;
-}
-
-int lte_blocks_per_sm(int precision, int magneto_optical, int block, size_t smem) {
-  return precision == PYRH_FP32 ? blocks_per_sm_t<float>(magneto_optical, block, smem)
-                                : blocks_per_sm_t<double>(magneto_optical, block, smem);
-}
-
 size_t lte_smem_bytes(int precision, int nline, int maxd) {
   return precision == PYRH_FP32 ? smem_bytes<float>(nline, maxd) : smem_bytes<double>(nline, maxd);
 }

@@ -33,11 +33,9 @@ struct RfArgs {
 };
 
 size_t rf_smem_bytes(int precision, int nline, int maxd);
-int rf_blocks_per_sm(int precision, int mode, int block, size_t smem);
 cudaError_t launch_lte_rf(const RfArgs &a, int block, int grid, cudaStream_t st);
 
 size_t lte_smem_bytes(int precision, int nline, int maxd);
-int lte_blocks_per_sm(int precision, int magneto_optical, int block, size_t smem);
 cudaError_t launch_lte_stokes(const LteArgs &a, int block, int grid, cudaStream_t st);
 
 }  // namespace pyrh

@@ -52,10 +52,11 @@ def rf_harness(tmp_path_factory):
     return C.CDLL(out)
 
 
-def rf_eval(lib, fx, sel, single=False):
+def rf_eval(lib, fx, sel, single=False, jac=False):
     """Stokes [nsel, 4] and response functions [nsel, 4, 6, ndep] of one
     atmosphere at the wavelengths fx["lam"][sel] (CPU harness, FP64 or, with
-    single=True, FP32)."""
+    single=True, FP32; jac=True takes the opacity derivatives in forward
+    mode)."""
     from pyrh_gb300 import lte
     D = C.POINTER(C.c_double)
     keep = []
@@ -70,7 +71,7 @@ def rf_eval(lib, fx, sel, single=False):
     lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
     st = np.zeros((len(sel), 4))
     rf = np.zeros((len(sel), 4, 6, nd))
-    fn = lib.rf_eval_f32 if single else lib.rf_eval
+    fn = lib.rf_eval_f32 if single else (lib.rf_eval_jac if jac else lib.rf_eval)
     r = fn(nd, arr(fx["height"]), arr(fx["T"]), arr(fx["ne"]), arr(fx["nHtot"]),
                     arr(fx["np"]), arr(fx["vturb"]), arr(fx["vel"]), arr(fx["B"]),
                     arr(fx["gamma_B"]), arr(fx["chi_B"]), arr(fx["line_pops"]), n, lines,

@@ -1,10 +1,13 @@
 // rf_host.cu -- TEST HARNESS: evaluates the response-function math of
 // pyrh_gb300/csrc/lte_rf.cuh on the CPU for one atmosphere, in the same
-// order as the GPU kernel (per-depth quantities and their derivatives in
-// FP64, then converted to the working precision; forward sweep on the
-// values; reverse sweep; local Jacobians at each handed-over depth), so the
-// adjoint can be compared with finite differences of the CPU oracle and with
-// the GPU.  rf_eval works in FP64, rf_eval_f32 in FP32.
+// order as the GPU kernel (per-depth quantities and their derivatives in the
+// working precision; forward sweep on the values; reverse sweep; reverse-mode
+// contraction through the opacity at each handed-over depth), so the adjoint
+// can be compared with finite differences of the CPU oracle and with the
+// GPU.  rf_eval works in FP64, rf_eval_f32 in FP32; rf_eval_jac is rf_eval
+// with the opacity derivatives taken in forward mode instead (six dual
+// directions through every sum, local_q_jac), an independent check of the
+// reverse-mode contraction.
 // Built by tests/conftest.py (rf_harness) with nvcc, host code only.
 #include <stdint.h>
 #include <string.h>
@@ -14,15 +17,7 @@
 
 using namespace pyrh;
 
-template <typename R>
-static D6<R> to_r(const D6<double>& a) {
-  D6<R> o;
-  o.v = R(a.v);
-  for (int i = 0; i < kNX; ++i) o.d[i] = R(a.d[i]);
-  return o;
-}
-
-template <typename R>
+template <typename R, bool JAC>
 struct Emit {
   int nd;
   const double* T;
@@ -37,24 +32,34 @@ struct Emit {
   const R *cs, *cw;
   const int* cq;
   const R *chi_c, *eta_c;   // [depth] at this wavelength
+  const Tape<R>* tp;
   void operator()(int k, const R* qb, const R* bpl) const {
-    R q[8], J[8][kNX];
-    local_q_jac<R>(nline, ld + k, PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
-                   PYRH_MAX_COMPONENTS, chi_c[k], eta_c[k], q, J);
+    R g[4][kNX];
+    if (JAC) {
+      R q[8], J[8][kNX];
+      local_q_jac<R>(nline, ld + k, PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
+                     PYRH_MAX_COMPONENTS, chi_c[k], eta_c[k], q, J);
+      for (int s = 0; s < 4; ++s)
+        for (int x = 0; x < kNX; ++x) {
+          g[s][x] = 0;
+          for (int n = 0; n < 8; ++n) g[s][x] += qb[s * 8 + n] * J[n][x];
+        }
+    } else {
+      for (int s = 0; s < 4; ++s)
+        for (int x = 0; x < kNX; ++x) g[s][x] = 0;
+      local_q_vjp<R, 4>(nline, ld + k, PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
+                        PYRH_MAX_COMPONENTS, tp->q[k], qb, g);
+    }
     const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lm)) : R(0);
     for (int s = 0; s < 4; ++s)
-      for (int x = 0; x < kNX; ++x) {
-        R v = 0;
-        for (int n = 0; n < 8; ++n) v += qb[s * 8 + n] * J[n][x];
-        if (x == 0) v += bpl[s] * dB;
-        rfl[(s * kNX + x) * nd + k] = double(v);
-      }
+      for (int x = 0; x < kNX; ++x)
+        rfl[(s * kNX + x) * nd + k] = double(g[s][x] + (x == 0 ? bpl[s] * dB : R(0)));
   }
 };
 
 // atmosphere arrays SI [nd]; line_pops [nline][2][nd]; lines: pyrh_line[nline];
 // chi_c, eta_c [nlam][nd]; out: stokes [nlam][4], rf [nlam][4][6][nd]
-template <typename R>
+template <typename R, bool JAC>
 static int rf_eval_t(int nd, const double* height, const double* T, const double* ne,
                      const double* nHtot, const double* np, const double* vturb,
                      const double* vel, const double* B, const double* gam, const double* chb,
@@ -77,21 +82,12 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
       cs[l * PYRH_MAX_COMPONENTS + m] = R(L.comp_shift[m]);
       cw[l * PYRH_MAX_COMPONENTS + m] = R(L.comp_strength[m]);
     }
-    for (int k = 0; k < nd; ++k) {
-      const LineDepth<double> d = line_depth<double>(
-          c, T[k], vel[k], vturb[k], B[k], ne[k], nHtot[k], np[k], line_pops[(l * 2 + 0) * nd + k],
-          line_pops[(l * 2 + 1) * nd + k], mu, true);
-      LineDepth<R>& o = ld[l][k];
-      o.inv_vb = to_r<R>(d.inv_vb); o.vshift = to_r<R>(d.vshift); o.adamp = to_r<R>(d.adamp);
-      o.vB = to_r<R>(d.vB); o.chil = to_r<R>(d.chil); o.etal = to_r<R>(d.etal);
-      o.gauss = d.gauss;
-    }
+    for (int k = 0; k < nd; ++k)
+      ld[l][k] = line_depth<R>(c, R(T[k]), R(vel[k]), R(vturb[k]), R(B[k]), R(ne[k]), R(nHtot[k]),
+                               R(np[k]), R(line_pops[(l * 2 + 0) * nd + k]),
+                               R(line_pops[(l * 2 + 1) * nd + k]), R(mu), true);
   }
-  for (int k = 0; k < nd; ++k) {
-    const GeoD<double> g = geometry_d<double>(gam[k], chb[k], mu);
-    geo[k].gQ = to_r<R>(g.gQ); geo[k].gU = to_r<R>(g.gU);
-    geo[k].gV = to_r<R>(g.gV); geo[k].s2g = to_r<R>(g.s2g);
-  }
+  for (int k = 0; k < nd; ++k) geo[k] = geometry_d<R>(R(gam[k]), R(chb[k]), R(mu));
   R ds[PYRH_MAX_DEPTH_RF];
   ds[0] = 0;
   for (int k = 1; k < nd; ++k) ds[k] = R(fabs(height[k] - height[k - 1]) / mu);
@@ -123,7 +119,8 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     delo_forward<R>(tape, ds, nd, B0, B1, out);
     for (int s = 0; s < 4; ++s) stokes[la * 4 + s] = double(out[s]);
     const R seed[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
-    Emit<R> emit{nd, T, lm, rfl, nline, &ld[0][0], geo, dlam, inwin, ncomp, cs, cw, cq, cc, ec};
+    Emit<R, JAC> emit{nd, T, lm, rfl, nline, &ld[0][0], geo, dlam, inwin, ncomp, cs, cw, cq, cc, ec,
+                      &tape};
     delo_reverse_stream<R, 4>(tape, ds, nd, B0, B1, seed, emit);
   }
   return 0;
@@ -139,5 +136,6 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
   nd, height, T, ne, nHtot, np, vturb, vel, B, gam, chb, line_pops, nline, lines, nlam, lam,  \
       chi_c, eta_c, mu, vmicro_char, stokes, rf
 
-extern "C" int rf_eval(RF_ARGS) { return rf_eval_t<double>(RF_PASS); }
-extern "C" int rf_eval_f32(RF_ARGS) { return rf_eval_t<float>(RF_PASS); }
+extern "C" int rf_eval(RF_ARGS) { return rf_eval_t<double, false>(RF_PASS); }
+extern "C" int rf_eval_f32(RF_ARGS) { return rf_eval_t<float, false>(RF_PASS); }
+extern "C" int rf_eval_jac(RF_ARGS) { return rf_eval_t<double, true>(RF_PASS); }

@@ -11,10 +11,9 @@ Checked against
   * each other: chi^2 gradient and VJP equal the contraction of the RFs.
 Tolerances are relative to the largest |RF| of each parameter:
   FP64 kernel vs CPU adjoint (FP64)   1e-8 (fused multiply-adds on the GPU)
-  FP32 kernel vs CPU adjoint (FP64)   1e-4 at the 99.9th percentile, 1e-3 at
-                                      most (isolated limiter-branch flips next
-                                      to sign changes of S_Q, S_U; see
-                                      test_rf_host)
+  FP32 kernel vs CPU adjoint (FP64)   2e-4 at the 99.9th percentile, 1e-3 at
+                                      most (polarized terms and isolated
+                                      limiter-branch flips; see test_rf_host)
   GPU FD (FP64) vs FP64 kernel        1e-4, per element the closest of five
                                       steps (Humlicek region jumps, FP64
                                       noise of the synthesis)
@@ -84,7 +83,7 @@ def test_rf_matches_cpu_adjoint(rf_harness, golden, name, precision):
     else:
         for x in range(6):
             e = np.abs(mine[:, x] - ref[:, x]) / np.abs(ref[:, x]).max()
-            assert np.percentile(e, 99.9) < 1e-4 and e.max() < 1e-3, (PARAMS[x], e.max())
+            assert np.percentile(e, 99.9) < 2e-4 and e.max() < 1e-3, (PARAMS[x], e.max())
     assert np.abs(st[0][:, win] - st_h.T).max() <= (1e-10 if precision == FP64 else 1e-5) * \
         st_h[:, 0].max()
 

