@@ -16,8 +16,11 @@
 //                 converged atmospheres drop out of later launches
 // Line profiles (profile.c:67-371, Armstrong Voigt of voigt.c:126-243) are
 // computed once in FP64 and kept in the workspace in the formal-solution
-// precision.  The Gamma quadrature of a block of 32 wavelengths x all rays
-// is reduced in shared memory (FP64) before one global atomic per entry.
+// precision.  The per-(wavelength, depth) opacity and rate contributions run
+// in the formal-solution precision; the Gamma quadrature of a block of 32
+// wavelengths x all rays is summed in shared memory in that precision before
+// one FP64 global atomic per entry (in FP32 mode the FP64 units, a small
+// fraction of the FP32 rate on this GPU, stay out of the inner loops).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -220,59 +223,78 @@ __global__ void nlte_gamma_init_kernel(NlteArgs A) {
 
 // ------------------------------------------------------------ formal -----
 
+// The transitions active at one wavelength and their wavelength-only
+// constants, in the formal-solution precision R.  Line quantities are kept
+// without the factor h c / (4 pi) where products would leave the single-
+// precision range (V W reaches 1e15 and W alone 1e33).
+template <typename R>
 struct ActiveSet {
   int n;
   int t[PYRH_NLTE_MAX_ACTIVE];   // transition index
   int la[PYRH_NLTE_MAX_ACTIVE];  // wavelength index within the transition
   bool bb;
+  R vb[PYRH_NLTE_MAX_ACTIVE];    // lines: B_ij isotope_frac; continua: alpha(lambda)
+  R gl[PYRH_NLTE_MAX_ACTIVE];    // lines: B_ji / B_ij
+  R tw[PYRH_NLTE_MAX_ACTIVE];    // lines: A_ji / B_ji; continua: 2 h c / lambda^3
+  R wl[PYRH_NLTE_MAX_ACTIVE];    // lines: wlambda (Hz); continua: 4 pi wlambda / (h lambda)
+  R hckl;                        // h c / (k_B lambda)
+};
+
+// Per-block staging of the quantities every thread reads at every depth.
+template <typename R>
+struct NlteShared {
+  R* Gs;      // [nlev^2][nd] Gamma of this block's wavelengths
+  R* Js;      // [nd][32] new J of this block's wavelengths
+  R* n;       // [nlev][nd] populations
+  R* lnst;    // [nlev][nd] log of the LTE populations
+  R* iT;      // [nd] 1 / T
+  R* ds;      // [nrays][nd] path lengths of each ray
+  R* wphi;    // [nline][nd] line profile normalisation
 };
 
 template <typename R>
 struct NlteOpacity {
   const NlteArgs* A;
   const pyrh_nlte_transition* tr;
-  const ActiveSet* as;
-  const double* n_s;      // shared [nlevel][nd]
-  const double* nstar_s;  // shared [nlevel][nd]
-  int nd, nl, ns, la, q, nlev;
-  int64_t doff, coff;
-  double lam;
-  const double* lamp;     // spectrum of this atmosphere
+  const ActiveSet<R>* as;
+  const NlteShared<R>* sh;
+  int nd, ns, la, q;
+  int64_t coff;
 
   // Total opacity, source function and the background part of the source
-  // function (eta_c + sca_c J) / chi at depth k, plus the atom's emissivity.
-  __device__ __forceinline__ void operator()(int k, R& chi, R& S, R& S_bg, double& eta_atom,
+  // function (eta_c + sca_c J) / chi at depth k, plus the atom's emissivity
+  // (opacity.c:64-300 for the active atom).
+  __device__ __forceinline__ void operator()(int k, R& chi, R& S, R& S_bg, R& eta_atom,
                                              double Jold) const {
     const pyrh_nlte_batch& b = A->b;
-    double chi_a = 0.0, eta_a = 0.0;
+    R chi_a = 0, eta_a = 0;
     for (int m = 0; m < as->n; ++m) {
       const pyrh_nlte_transition& t = tr[as->t[m]];
-      double V, g, tw;
+      const R ni = sh->n[t.i * nd + k], nj = sh->n[t.j * nd + k];
       if (t.type == 0) {
         const int64_t pi = t.phi_off + ((int64_t)k * 2 * A->nrays + q) * t.nlambda + as->la[m];
-        const double phv = pi < A->phi_cap ? (double)static_cast<const R*>(A->phi)[pi] : 0.0;
-        V = kHPLANCK * kCLIGHT / (4.0 * kPI) * t.Bij * t.isotope_frac * phv;
-        g = t.Bji / t.Bij;
-        tw = t.Aji / t.Bji;
+        const R phv = pi < A->phi_cap ? static_cast<const R*>(A->phi)[pi] : R(0);
+        const R V = R(kHPLANCK * kCLIGHT / (4.0 * kPI)) * (as->vb[m] * phv);
+        chi_a += V * (ni - as->gl[m] * nj);
+        eta_a += (as->tw[m] * as->gl[m]) * (V * nj);
       } else {
-        V = b.alpha[t.alpha_off + as->la[m]];
-        g = nstar_s[t.i * nd + k] / nstar_s[t.j * nd + k] *
-            exp(-(kHPLANCK * kCLIGHT / (kKBOLTZMANN * kNM_TO_M)) / (lam * b.T[doff + k]));
-        tw = 2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M) / (lam * lam * lam);
+        const R g = dev_exp(sh->lnst[t.i * nd + k] - sh->lnst[t.j * nd + k] -
+                            as->hckl * sh->iT[k]);
+        const R V = as->vb[m];
+        chi_a += V * (ni - g * nj);
+        eta_a += (as->tw[m] * g) * (V * nj);
       }
-      chi_a += V * (n_s[t.i * nd + k] - g * n_s[t.j * nd + k]);
-      eta_a += tw * g * V * n_s[t.j * nd + k];
     }
     const int64_t c = coff + (int64_t)k * ns + la;
-    const double ct = chi_a + b.chi_c[c];
-    const double eta_bg = b.eta_c[c] + b.sca_c[c] * Jold;
-    chi = R(ct);
-    S = R((eta_a + eta_bg) / ct);
-    S_bg = R(eta_bg / ct);
+    const R ct = chi_a + R(b.chi_c[c]);
+    const R eta_bg = R(b.eta_c[c]) + R(b.sca_c[c]) * R(Jold);
+    chi = ct;
+    S = (eta_a + eta_bg) / ct;
+    S_bg = eta_bg / ct;
     eta_atom = eta_a;
   }
 
-  __device__ __forceinline__ void operator()(int k, R& chi, R& S, double& eta_atom,
+  __device__ __forceinline__ void operator()(int k, R& chi, R& S, R& eta_atom,
                                              double Jold) const {
     R S_bg;
     (*this)(k, chi, S, S_bg, eta_atom, Jold);
@@ -290,7 +312,7 @@ struct JRow {
 
 template <typename R, typename Op>
 __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, double B0, double B1,
-                            const JRow& Jold, R* I, R* Psi, R* Ieff) {
+                            const JRow& Jold, R* I, R* Psi, R* Ieff, R* chi_out) {
   // Ieff[k] = I[k] - Psi[k] * S_atom[k], the effective intensity of the
   // MALI rates (fillgamma.c:121-134), is built term by term in the same
   // recurrence: the local source enters through S_bg = S - S_atom only, so
@@ -299,11 +321,14 @@ __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, doubl
   // forming their difference from single-precision I and Psi would lose
   // all of them.
   const int dk = to_obs ? -1 : 1, k_start = to_obs ? nd - 1 : 0, k_end = to_obs ? 0 : nd - 1;
-  double ea;
-  R chi_u, chi_c, chi_d, chi_dd, S_u, S_c, S_d, S_dd = 0, Sb_u, Sb_c, Sb_d, Sb_dd = 0;
+  R ea;
+  R chi_u, chi_c, chi_d, chi_dd = 0, S_u, S_c, S_d, S_dd = 0, Sb_u, Sb_c, Sb_d, Sb_dd = 0;
   op(k_start, chi_u, S_u, Sb_u, ea, Jold[k_start]);
   op(k_start + dk, chi_c, S_c, Sb_c, ea, Jold[k_start + dk]);
   op(k_start + 2 * dk, chi_d, S_d, Sb_d, ea, Jold[k_start + 2 * dk]);
+  chi_out[k_start] = chi_u;
+  chi_out[k_start + dk] = chi_c;
+  chi_out[k_start + 2 * dk] = chi_d;
   // interval path length between depth a and a+1 is ds[a+1]
   auto dsi = [&](int a, int b2) { return ds[a > b2 ? a : b2]; };
   const R dtau0 = R(0.5) * (chi_u + chi_c) * dsi(k_start, k_start + dk);
@@ -324,6 +349,7 @@ __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, doubl
     R dchi_dn;
     if (abs(k - k_end) > 1) {
       op(k + 2 * dk, chi_dd, S_dd, Sb_dd, ea, Jold[k + 2 * dk]);
+      chi_out[k + 2 * dk] = chi_dd;
       dchi_dn = cent_deriv<R>(dsdn, dsi(k + 2 * dk, k + dk), chi_c, chi_d, chi_dd);
     } else {
       dchi_dn = (chi_d - chi_c) / dsdn;
@@ -404,6 +430,26 @@ __device__ R feautrier_full(const R* chi, const R* S, const R* ds, int nd, doubl
 }
 
 template <typename R>
+__host__ __device__ inline size_t formal_smem_layout(int nlev, int nd, int nrays, int nline,
+                                                     NlteShared<R>* sh, unsigned char* base) {
+  size_t off = 0;
+  auto take = [&](size_t count) {
+    R* p = base ? reinterpret_cast<R*>(base + off) : nullptr;
+    off += ((sizeof(R) * count + 15) / 16) * 16;
+    return p;
+  };
+  R* Gs = take((size_t)nlev * nlev * nd);
+  R* Js = take((size_t)nd * 32);
+  R* n = take((size_t)nlev * nd);
+  R* lnst = take((size_t)nlev * nd);
+  R* iT = take((size_t)nd);
+  R* ds = take((size_t)nrays * nd);
+  R* wphi = take((size_t)(nline > 0 ? nline : 1) * nd);
+  if (sh) *sh = NlteShared<R>{Gs, Js, n, lnst, iT, ds, wphi};
+  return off;
+}
+
+template <typename R>
 __global__ void __launch_bounds__(256)
 nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -420,70 +466,90 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
   const int64_t doff = b.depth_off[p], coff = b.cont_off[p];
   const pyrh_nlte_transition* tr = b.trans + b.trans_off[p];
   const double* lamp = b.lambda + b.lam_off[p];
-  double* Gs = reinterpret_cast<double*>(smem_raw);                 // [nlev^2][nd]
-  double* Js = Gs + (size_t)nlev * nlev * nd;                        // [nd][32]
-  double* n_s = Js + (size_t)nd * 32;                                // [nlev][nd]
-  double* nst_s = n_s + (size_t)nlev * nd;                           // [nlev][nd]
+  NlteShared<R> sh;
+  formal_smem_layout<R>(nlev, b.max_ndep, A.nrays, b.max_nline, &sh, smem_raw);
   const int nthr = blockDim.x;
-  for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) Gs[e] = 0.0;
-  for (int e = threadIdx.x; e < nd * 32; e += nthr) Js[e] = 0.0;
+  for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) sh.Gs[e] = R(0);
+  for (int e = threadIdx.x; e < nd * 32; e += nthr) sh.Js[e] = R(0);
   for (int e = threadIdx.x; e < nlev * nd; e += nthr) {
     const int i = e / nd, k = e % nd;
-    n_s[e] = b.n[(int64_t)i * b.total_depth + doff + k];
-    nst_s[e] = b.nstar[(int64_t)i * b.total_depth + doff + k];
+    sh.n[e] = R(b.n[(int64_t)i * b.total_depth + doff + k]);
+    sh.lnst[e] = R(log(b.nstar[(int64_t)i * b.total_depth + doff + k]));
   }
+  for (int k = threadIdx.x; k < nd; k += nthr) sh.iT[k] = R(1.0 / b.T[doff + k]);
+  for (int e = threadIdx.x; e < A.nrays * nd; e += nthr) {
+    const int m = e / nd, k = e % nd;
+    sh.ds[e] = k ? R(fabs(b.height[doff + k] - b.height[doff + k - 1]) / A.muz[m]) : R(0);
+  }
+  int nline = 0;
+  for (int t = 0; t < nt; ++t) nline += (tr[t].type == 0);
+  for (int e = threadIdx.x; e < nline * nd; e += nthr)
+    sh.wphi[e] = R(A.wphi[b.adamp_off[p] + e]);
   __syncthreads();
 
   const int lane = threadIdx.x & 31, ray = threadIdx.x >> 5;
   const int la = la0 + lane;
   const bool live = (la < ns) && (ray < A.nrays);
   if (live) {
-    const double muz = A.muz[ray], imu = 1.0 / muz;
-    // path lengths of this ray (thread-private copy in local memory)
-    R dsl[PYRH_NLTE_MAX_DEPTH];
-    dsl[0] = R(0);
-    for (int k = 1; k < nd; ++k) dsl[k] = R(fabs(b.height[doff + k] - b.height[doff + k - 1]) * imu);
-    ActiveSet as;
+    const double muz = A.muz[ray];
+    const R* dsl = sh.ds + ray * nd;
+    const double lam = lamp[la];
+    ActiveSet<R> as;
     as.n = 0;
     as.bb = false;
+    as.hckl = R((kHPLANCK * kCLIGHT / (kKBOLTZMANN * kNM_TO_M)) / lam);
     for (int pass = 1; pass >= 0; --pass)       // continua (type 1) first, then lines
       for (int t = 0; t < nt; ++t) {
         const pyrh_nlte_transition& T = tr[t];
         if (T.type != pass) continue;
         if (la >= T.nblue && la < T.nblue + T.nlambda && as.n < PYRH_NLTE_MAX_ACTIVE) {
-          as.t[as.n] = t;
-          as.la[as.n] = la - T.nblue;
-          ++as.n;
-          if (T.type == 0) as.bb = true;
+          const int m = as.n++;
+          as.t[m] = t;
+          as.la[m] = la - T.nblue;
+          if (T.type == 0) {
+            as.bb = true;
+            as.vb[m] = R(T.Bij * T.isotope_frac);
+            as.gl[m] = R(T.Bji / T.Bij);
+            as.tw[m] = R(T.Aji / T.Bji);
+            as.wl[m] = R(wlambda_line(lamp + T.nblue, T, as.la[m]));
+          } else {
+            as.vb[m] = R(b.alpha[T.alpha_off + as.la[m]]);
+            as.gl[m] = R(0);
+            as.tw[m] = R(2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M) /
+                         (lam * lam * lam));
+            as.wl[m] = R(4.0 * kPI / kHPLANCK * (wlambda_cont(lamp + T.nblue, T, as.la[m]) / lam));
+          }
         }
       }
-    const double lam = lamp[la];
     const double B0 = planck(b.T[doff + nd - 2], lam), B1 = planck(b.T[doff + nd - 1], lam);
     const JRow Jold{b.J + coff + la, ns};
     const bool angle_dep = A.moving && (as.bb || b.bgline[b.lam_off[p] + la]);
-    R I[PYRH_NLTE_MAX_DEPTH], Psi[PYRH_NLTE_MAX_DEPTH], Ieff[PYRH_NLTE_MAX_DEPTH];
+    R I[PYRH_NLTE_MAX_DEPTH], Psi[PYRH_NLTE_MAX_DEPTH], Ieff[PYRH_NLTE_MAX_DEPTH],
+        chis[PYRH_NLTE_MAX_DEPTH];
     NlteOpacity<R> op;
-    op.A = &A; op.tr = tr; op.as = &as; op.n_s = n_s; op.nstar_s = nst_s;
-    op.nd = nd; op.ns = ns; op.la = la; op.nlev = nlev; op.doff = doff; op.coff = coff;
-    op.lam = lam; op.lamp = lamp;
+    op.A = &A; op.tr = tr; op.as = &as; op.sh = &sh;
+    op.nd = nd; op.ns = ns; op.la = la; op.coff = coff;
     const int ndir = angle_dep ? 2 : 1;
     for (int dir = 0; dir < ndir; ++dir) {
       const int to_obs = angle_dep ? dir : 0;
       op.q = 2 * ray + to_obs;
-      double wdir;
+      R wdir;
       R emergent;
       if (angle_dep) {
         if (emergent_only && !to_obs) continue;
-        bezier_full<R>(op, dsl, nd, to_obs, B0, B1, Jold, I, Psi, Ieff);
-        wdir = 0.5 * A.wmu[ray];
+        bezier_full<R>(op, dsl, nd, to_obs, B0, B1, Jold, I, Psi, Ieff, chis);
+        wdir = R(0.5 * A.wmu[ray]);
         emergent = I[0];
       } else {
-        R chi[PYRH_NLTE_MAX_DEPTH], S[PYRH_NLTE_MAX_DEPTH];
-        double ea;
-        for (int k = 0; k < nd; ++k) op(k, chi[k], S[k], ea, Jold[k]);
+        R S[PYRH_NLTE_MAX_DEPTH];
+        for (int k = 0; k < nd; ++k) {
+          R ea;
+          op(k, chis[k], S[k], ea, Jold[k]);
+          Ieff[k] = ea;   // the atom's emissivity, for I - Psi eta below
+        }
         R F[PYRH_NLTE_MAX_DEPTH], zt[PYRH_NLTE_MAX_DEPTH];
-        emergent = feautrier_full<R>(chi, S, dsl, nd, muz, B0, B1, I, Psi, F, zt);
-        wdir = A.wmu[ray];
+        emergent = feautrier_full<R>(chis, S, dsl, nd, muz, B0, B1, I, Psi, F, zt);
+        wdir = R(A.wmu[ray]);
       }
       if (emergent_only) {
         I_out[b.lam_off[p] + la] = (double)emergent;
@@ -491,59 +557,49 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
       }
       // Gamma, coupling and J at every depth (fillgamma.c:82-332, formal.c:247-256)
       for (int k = 0; k < nd; ++k) {
-        R chi_k, S_k;
-        double eta_atom;
-        op(k, chi_k, S_k, eta_atom, Jold[k]);
-        atomicAdd(&Js[k * 32 + lane], wdir * (double)I[k]);
+        atomicAdd(&sh.Js[k * 32 + lane], wdir * I[k]);
         if (!eval_operator) continue;
-        const double psi = (double)Psi[k] / (double)chi_k;
-        const double Ieff_k = angle_dep ? (double)Ieff[k] : (double)I[k] - psi * eta_atom;
-        double V[PYRH_NLTE_MAX_ACTIVE], G[PYRH_NLTE_MAX_ACTIVE], W[PYRH_NLTE_MAX_ACTIVE],
-            TW[PYRH_NLTE_MAX_ACTIVE];
+        const R psi = Psi[k] / chis[k];
+        const R Ieff_k = angle_dep ? Ieff[k] : I[k] - psi * Ieff[k];
+        // per transition: V W (product formed without the h c / 4 pi that
+        // cancels in it), U = TW G V and the stimulated-emission factor G
+        R VW[PYRH_NLTE_MAX_ACTIVE], U[PYRH_NLTE_MAX_ACTIVE], G[PYRH_NLTE_MAX_ACTIVE];
         for (int m = 0; m < as.n; ++m) {
           const pyrh_nlte_transition& t = tr[as.t[m]];
           if (t.type == 0) {
             const int64_t pi =
                 t.phi_off + ((int64_t)k * 2 * A.nrays + op.q) * t.nlambda + as.la[m];
-            const double phv = pi < A.phi_cap ? (double)static_cast<const R*>(A.phi)[pi] : 0.0;
-            V[m] = kHPLANCK * kCLIGHT / (4.0 * kPI) * t.Bij * t.isotope_frac * phv;
-            G[m] = t.Bji / t.Bij;
-            TW[m] = t.Aji / t.Bji;
-            W[m] = wlambda_line(lamp + t.nblue, t, as.la[m]) *
-                   A.wphi[b.adamp_off[p] + (int64_t)t.line_index * nd + k] /
-                   (kHPLANCK * kCLIGHT / (4.0 * kPI));
+            const R phv = pi < A.phi_cap ? static_cast<const R*>(A.phi)[pi] : R(0);
+            const R vph = as.vb[m] * phv;
+            G[m] = as.gl[m];
+            VW[m] = vph * (as.wl[m] * sh.wphi[t.line_index * nd + k]);
+            U[m] = (as.tw[m] * G[m]) * (R(kHPLANCK * kCLIGHT / (4.0 * kPI)) * vph);
           } else {
-            V[m] = b.alpha[t.alpha_off + as.la[m]];
-            G[m] = nst_s[t.i * nd + k] / nst_s[t.j * nd + k] *
-                   exp(-(kHPLANCK * kCLIGHT / (kKBOLTZMANN * kNM_TO_M)) / (lam * b.T[doff + k]));
-            TW[m] = 2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M) / (lam * lam * lam);
-            W[m] = 4.0 * kPI / kHPLANCK * (wlambda_cont(lamp + t.nblue, t, as.la[m]) / lam);
+            G[m] = dev_exp(sh.lnst[t.i * nd + k] - sh.lnst[t.j * nd + k] - as.hckl * sh.iT[k]);
+            VW[m] = as.vb[m] * as.wl[m];
+            U[m] = (as.tw[m] * G[m]) * as.vb[m];
           }
         }
         for (int m = 0; m < as.n; ++m) {
           const pyrh_nlte_transition& t = tr[as.t[m]];
           const int i = t.i, j = t.j;
           // cross-coupling sums over the active set (addtoCoupling)
-          double chi_up_i = 0.0, chi_down_j = 0.0, U_down_j = 0.0, U_down_i = 0.0;
-          bool i_is_upper = false;
+          R chi_up_i = 0, chi_down_j = 0, U_down_j = 0, U_down_i = 0;
+          int cnt = 0;
           for (int q = 0; q < as.n; ++q) {
             const pyrh_nlte_transition& u = tr[as.t[q]];
-            const double chicc = V[q] * W[q] * (n_s[u.i * nd + k] - G[q] * n_s[u.j * nd + k]);
+            const R chicc = VW[q] * (sh.n[u.i * nd + k] - G[q] * sh.n[u.j * nd + k]);
             if (u.i == i) chi_up_i += chicc;
-            if (u.j == j) { chi_down_j += chicc; U_down_j += TW[q] * G[q] * V[q]; }
-            if (u.j == i) { U_down_i += TW[q] * G[q] * V[q]; i_is_upper = true; }
+            if (u.j == j) { chi_down_j += chicc; U_down_j += U[q]; }
+            if (u.j == i) { U_down_i += U[q]; ++cnt; }
           }
-          const double wlamu = V[m] * W[m] * wdir;
-          double gji = Ieff_k * wlamu;
-          double gij = (TW[m] + Ieff_k) * G[m] * wlamu - chi_up_i * psi * U_down_j * wdir;
-          if (i_is_upper) {
-            // one term per active transition whose upper level is i
-            int cnt = 0;
-            for (int q = 0; q < as.n; ++q) cnt += (tr[as.t[q]].j == i);
-            gji += cnt * chi_down_j * psi * U_down_i * wdir;
-          }
-          atomicAdd(&Gs[(i * nlev + j) * nd + k], gij);
-          atomicAdd(&Gs[(j * nlev + i) * nd + k], gji);
+          const R wlamu = VW[m] * wdir;
+          R gji = Ieff_k * wlamu;
+          R gij = (as.tw[m] + Ieff_k) * G[m] * wlamu - chi_up_i * (psi * U_down_j) * wdir;
+          // one term per active transition whose upper level is i
+          if (cnt) gji += R(cnt) * chi_down_j * (psi * U_down_i) * wdir;
+          atomicAdd(&sh.Gs[(i * nlev + j) * nd + k], gij);
+          atomicAdd(&sh.Gs[(j * nlev + i) * nd + k], gji);
         }
       }
     }
@@ -552,12 +608,12 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
   if (emergent_only) return;
   for (int e = threadIdx.x; e < nd * 32; e += nthr) {
     const int k = e / 32, l = e % 32;
-    if (la0 + l < ns) A.Jnew[coff + (int64_t)k * ns + la0 + l] = Js[e];
+    if (la0 + l < ns) A.Jnew[coff + (int64_t)k * ns + la0 + l] = (double)sh.Js[e];
   }
   if (eval_operator)
     for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) {
       const int ij = e / nd, k = e % nd;
-      const double v = Gs[e];
+      const double v = (double)sh.Gs[e];
       if (v != 0.0) atomicAdd(&A.Gamma[(int64_t)ij * b.total_depth + doff + k], v);
     }
 }
@@ -798,11 +854,10 @@ __global__ void nlte_ng_kernel(NlteArgs A, int init) {
 
 // ----------------------------------------------------------- launching ---
 
-size_t nlte_formal_smem(int nlevel, int maxd, int precision) {
-  const size_t r = precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
-  (void)r;
-  return sizeof(double) * ((size_t)nlevel * nlevel * maxd + (size_t)maxd * 32 +
-                           2 * (size_t)nlevel * maxd) + 64;
+size_t nlte_formal_smem(int nlevel, int maxd, int nrays, int max_nline, int precision) {
+  return precision == PYRH_FP32
+             ? formal_smem_layout<float>(nlevel, maxd, nrays, max_nline, nullptr, nullptr)
+             : formal_smem_layout<double>(nlevel, maxd, nrays, max_nline, nullptr, nullptr);
 }
 
 template <typename R>
@@ -831,7 +886,8 @@ template <typename R>
 static cudaError_t launch_formal_t(const NlteArgs& A, int natm, int max_nspect, int maxd,
                                    int eval_operator, int emergent_only, double* I_out,
                                    cudaStream_t st) {
-  const size_t smem = nlte_formal_smem(A.b.nlevel, maxd, sizeof(R) == 4 ? PYRH_FP32 : PYRH_FP64);
+  const size_t smem = nlte_formal_smem(A.b.nlevel, maxd, A.nrays, A.b.max_nline,
+                                       sizeof(R) == 4 ? PYRH_FP32 : PYRH_FP64);
   cudaError_t e = cudaFuncSetAttribute(nlte_formal_kernel<R>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;

@@ -21,7 +21,7 @@ struct NlteArgs {
   int32_t *count, *active, *iters, *err;
 };
 
-size_t nlte_formal_smem(int nlevel, int maxd, int precision);
+size_t nlte_formal_smem(int nlevel, int maxd, int nrays, int max_nline, int precision);
 cudaError_t nlte_launch_profiles(const NlteArgs &A, int natm, int64_t max_elems, int precision,
                                  cudaStream_t st);
 cudaError_t nlte_launch_ng_init(const NlteArgs &A, int natm, cudaStream_t st);

@@ -130,7 +130,7 @@ pyrh_status pyrh_nlte_solve(const pyrh_nlte_batch* b, const pyrh_nlte_config* cf
   }
   cudaStream_t st = (cudaStream_t)stream;
   pyrh::NlteArgs A = make_args(b, cfg, ws, ws_bytes, L);
-  const size_t smem = pyrh::nlte_formal_smem(b->nlevel, b->max_ndep, cfg->precision);
+  const size_t smem = pyrh::nlte_formal_smem(b->nlevel, b->max_ndep, cfg->nrays, b->max_nline, cfg->precision);
   if (smem > 220 * 1024) {
     pyrh::set_error("shared memory %zu B for %d levels x %d depths", smem, b->nlevel, b->max_ndep);
     return PYRH_ERR_UNSUPPORTED;
@@ -291,7 +291,7 @@ extern "C" pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch* b,
                     need, (size_t)PYRH_NLTE_STATIC_SCRATCH_BYTES);
     return PYRH_ERR_ARG;
   }
-  const size_t smem = pyrh::nlte_formal_smem(b->nlevel, b->max_ndep, cfg->precision);
+  const size_t smem = pyrh::nlte_formal_smem(b->nlevel, b->max_ndep, cfg->nrays, b->max_nline, cfg->precision);
   if (smem > 220 * 1024) {
     pyrh::set_error("shared memory %zu B for %d levels x %d depths", smem, b->nlevel, b->max_ndep);
     return PYRH_ERR_UNSUPPORTED;
