@@ -148,6 +148,27 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch *host_batch,
                                  const pyrh_line *host_lines, int32_t nline,
                                  const pyrh_lte_config *cfg, void *host_stokes_out);
 
+/* A launch plan for one resident batch: pyrh_lte_plan_create times every
+   wavelength tile (block_lambda, multiples of 32 up to 256 and up to the
+   batch's widest spectrum) on the caller's buffers, keeps the fastest, and
+   records one launch of pyrh_lte_stokes with it as a CUDA graph bound to
+   those buffers (batch arrays, lines, stokes_out).  pyrh_lte_plan_launch
+   replays the graph on any stream; the buffers' contents may change between
+   launches, their addresses and the batch shape may not.  cfg->block_lambda
+   is ignored (tuned); cfg->persistent_blocks is kept.  stream: a
+   cudaStream_t (NULL uses an internal stream for the tuning launches and
+   the capture).  The reference has no counterpart: it makes one call per
+   atmosphere. */
+typedef struct pyrh_lte_plan_s *pyrh_lte_plan;
+pyrh_status pyrh_lte_plan_create(const pyrh_lte_batch *batch, const pyrh_line *lines,
+                                 int32_t nline, const pyrh_lte_config *cfg, void *stokes_out,
+                                 void *stream, pyrh_lte_plan *plan_out);
+pyrh_status pyrh_lte_plan_launch(pyrh_lte_plan plan, void *stream);
+/* The tuned tile and its measured time per launch [ms]. */
+int32_t pyrh_lte_plan_block(pyrh_lte_plan plan);
+double pyrh_lte_plan_ms(pyrh_lte_plan plan);
+void pyrh_lte_plan_destroy(pyrh_lte_plan plan);
+
 /* ------------------------------------------------------- response functions
  * Depth-resolved response functions of the emergent Stokes vector of
  * pyrh_lte_stokes to the atmosphere at every depth, and the gradient of a

@@ -293,6 +293,106 @@ pyrh_status pyrh_lte_stokes_vjp(const pyrh_lte_batch* batch, const pyrh_line* li
   return s;
 }
 
+struct pyrh_lte_plan_s {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int block = 0;
+  double ms = 0.0;
+};
+
+pyrh_status pyrh_lte_plan_create(const pyrh_lte_batch* batch, const pyrh_line* lines,
+                                 int32_t nline, const pyrh_lte_config* cfg, void* stokes_out,
+                                 void* stream, pyrh_lte_plan* plan_out) {
+  g_last_launches = 0;
+  if (!plan_out) return fail(PYRH_ERR_ARG, "plan_out is NULL");
+  *plan_out = nullptr;
+  pyrh_status s = check_cfg(cfg);
+  if (s != PYRH_OK) return s;
+  s = check_batch_shape(batch, nline);
+  if (s != PYRH_OK) return s;
+  if (!stokes_out) return fail(PYRH_ERR_ARG, "stokes_out is NULL");
+  if (nline > 0 && !lines) return fail(PYRH_ERR_ARG, "lines is NULL");
+  cudaStream_t own = nullptr;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (!st) {
+    CUDA_TRY(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+    st = own;
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  pyrh_lte_config c = *cfg;
+  auto cleanup = [&]() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (own) cudaStreamDestroy(own);
+  };
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cleanup();
+    return fail(PYRH_ERR_CUDA, "event creation failed");
+  }
+  // ---- tune the wavelength tile on the caller's buffers ----
+  const int widest = round_up(batch->max_nlam, 32);
+  int best = 0;
+  double best_ms = 0.0;
+  for (int blk = 32; blk <= 256 && blk <= (widest < 32 ? 32 : widest); blk += 32) {
+    c.block_lambda = blk;
+    s = launch(batch, lines, nline, &c, stokes_out, st);   // first launch sets up the kernel
+    if (s != PYRH_OK) { cleanup(); return s; }
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 3; ++r) {
+      s = launch(batch, lines, nline, &c, stokes_out, st);
+      if (s != PYRH_OK) { cleanup(); return s; }
+    }
+    cudaEventRecord(e1, st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess) {
+      cleanup();
+      return fail(PYRH_ERR_CUDA, "tuning: %s", cudaGetErrorString(e));
+    }
+    if (!best || ms / 3.0 < best_ms) { best = blk; best_ms = ms / 3.0; }
+  }
+  // ---- record the tuned launch as a graph ----
+  c.block_lambda = best;
+  pyrh_lte_plan plan = new pyrh_lte_plan_s;
+  plan->block = best;
+  plan->ms = best_ms;
+  cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    s = launch(batch, lines, nline, &c, stokes_out, st);
+    cudaError_t e2 = cudaStreamEndCapture(st, &plan->graph);
+    if (s == PYRH_OK && e2 != cudaSuccess) e = e2;
+  }
+  if (e == cudaSuccess && s == PYRH_OK) e = cudaGraphInstantiate(&plan->exec, plan->graph, 0);
+  cleanup();
+  if (e != cudaSuccess || s != PYRH_OK) {
+    pyrh_lte_plan_destroy(plan);
+    if (s != PYRH_OK) return s;
+    return fail(PYRH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  }
+  g_last_launches = 1;
+  *plan_out = plan;
+  return PYRH_OK;
+}
+
+pyrh_status pyrh_lte_plan_launch(pyrh_lte_plan plan, void* stream) {
+  g_last_launches = 0;
+  if (!plan || !plan->exec) return fail(PYRH_ERR_ARG, "plan is NULL");
+  CUDA_TRY(cudaGraphLaunch(plan->exec, (cudaStream_t)stream));
+  g_last_launches = 1;
+  return PYRH_OK;
+}
+
+int32_t pyrh_lte_plan_block(pyrh_lte_plan plan) { return plan ? plan->block : 0; }
+double pyrh_lte_plan_ms(pyrh_lte_plan plan) { return plan ? plan->ms : 0.0; }
+
+void pyrh_lte_plan_destroy(pyrh_lte_plan plan) {
+  if (!plan) return;
+  if (plan->exec) cudaGraphExecDestroy(plan->exec);
+  if (plan->graph) cudaGraphDestroy(plan->graph);
+  delete plan;
+}
+
 pyrh_status pyrh_check_lines(const pyrh_line* host_lines, int32_t nline, int32_t stokes_mode) {
   if (nline < 0 || nline > PYRH_MAX_LINES)
     return fail(PYRH_ERR_ARG, "nline %d outside [0, %d]", nline, PYRH_MAX_LINES);

@@ -97,6 +97,7 @@ struct Emit {
   const double* T;   // temperatures of this atmosphere
   double lam;
   int nd, nl, la;
+  bool act;          // this lane holds a wavelength (writes and seeds)
   R* rf;             // mode 0: rf_out + 24 * cont_off + la
   const Tape<R>* tp;
   __device__ void operator()(int k, const R* qb, const R* bpl) const {
@@ -117,8 +118,13 @@ struct Emit {
       for (int x = 0; x < kNX; ++x) {
         R v = g[s][x];
         if (x == 0) v += bpl[s] * dB;
-        if (MODE == 0) rf[((int64_t)(s * kNX + x) * nd + k) * nl] = v;
-        else atomicAdd(&sm.grad[x * loc->maxd + k], v);   // modes 1 and 2
+        if (MODE == 0) {
+          if (act) rf[((int64_t)(s * kNX + x) * nd + k) * nl] = v;
+        } else {   // modes 1 and 2: sum over the warp's wavelengths first
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          if ((threadIdx.x & 31u) == 0) atomicAdd(&sm.grad[x * loc->maxd + k], v);
+        }
       }
     }
   }
@@ -187,8 +193,13 @@ __global__ void __launch_bounds__(128) lte_rf_kernel(RfArgs ra) {
     }
     __syncthreads();
 
-    const int la = la0 + threadIdx.x;
-    if (la < nl) {
+    // Every lane of a warp that holds at least one wavelength runs the sweep
+    // (lanes past the spectrum repeat its last wavelength with zero seeds and
+    // write nothing), so the per-depth gradient sums can use full-warp
+    // shuffles before one shared atomic per warp.
+    const bool act = la0 + (int)threadIdx.x < nl;
+    const int la = act ? la0 + (int)threadIdx.x : nl - 1;
+    if (la0 + (int)(threadIdx.x & ~31u) < nl) {
       const int64_t loff = args.lam_off[p];
       const double lam = args.lambda[loff + la];
       const double dlc = lam * kQ_WING * (args.vmicro_char / kCLIGHT);
@@ -215,8 +226,9 @@ __global__ void __launch_bounds__(128) lte_rf_kernel(RfArgs ra) {
       R st[4];
       delo_forward<R>(tp, sm.ds, nd, B0, B1, st);
       R* out = static_cast<R*>(args.out) + 4 * loff;
+      if (act)
 #pragma unroll
-      for (int s = 0; s < 4; ++s) out[(int64_t)s * nl + la] = st[s];
+        for (int s = 0; s < 4; ++s) out[(int64_t)s * nl + la] = st[s];
 
       Emit<R, MODE> em;
       em.loc = &loc;
@@ -226,6 +238,7 @@ __global__ void __launch_bounds__(128) lte_rf_kernel(RfArgs ra) {
       em.nd = nd;
       em.nl = nl;
       em.la = la;
+      em.act = act;
       if (MODE == 0) {
         em.rf = static_cast<R*>(ra.rf) + 24 * args.cont_off[p] + la;
         const R seed[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
@@ -235,7 +248,7 @@ __global__ void __launch_bounds__(128) lte_rf_kernel(RfArgs ra) {
         const R* dL = static_cast<const R*>(ra.weights) + 4 * loff;
         R seed[1][4];
 #pragma unroll
-        for (int s = 0; s < 4; ++s) seed[0][s] = dL[(int64_t)s * nl + la];
+        for (int s = 0; s < 4; ++s) seed[0][s] = act ? dL[(int64_t)s * nl + la] : R(0);
         delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
       } else {
         em.rf = nullptr;
@@ -245,12 +258,14 @@ __global__ void __launch_bounds__(128) lte_rf_kernel(RfArgs ra) {
         R c2 = 0;
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-          const R wv = wt[(int64_t)s * nl + la];
+          const R wv = act ? wt[(int64_t)s * nl + la] : R(0);
           const R r = st[s] - obs[(int64_t)s * nl + la];
           seed[0][s] = R(2) * wv * r;
           c2 += wv * r * r;
         }
-        atomicAdd(sm.chi2, c2);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+        if ((threadIdx.x & 31u) == 0) atomicAdd(sm.chi2, c2);
         delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
       }
     }

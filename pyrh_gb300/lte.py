@@ -169,6 +169,42 @@ class DeviceBatch:
                                         stream_ptr))
 
 
+class Plan:
+    """pyrh_lte_plan for a resident batch: the wavelength tile tuned on the
+    batch's own buffers and one launch recorded as a CUDA graph."""
+
+    def __init__(self, dev: DeviceBatch, cfg: L.PyrhLteConfig, stream_ptr: int = 0):
+        lib = L.lib()
+        lib.pyrh_lte_plan_create.restype = C.c_int
+        lib.pyrh_lte_plan_create.argtypes = [C.POINTER(L.PyrhLteBatch), C.c_void_p, C.c_int32,
+                                             C.POINTER(L.PyrhLteConfig), C.c_void_p, C.c_void_p,
+                                             C.POINTER(C.c_void_p)]
+        lib.pyrh_lte_plan_launch.restype = C.c_int
+        lib.pyrh_lte_plan_launch.argtypes = [C.c_void_p, C.c_void_p]
+        lib.pyrh_lte_plan_block.restype = C.c_int32
+        lib.pyrh_lte_plan_block.argtypes = [C.c_void_p]
+        lib.pyrh_lte_plan_ms.restype = C.c_double
+        lib.pyrh_lte_plan_ms.argtypes = [C.c_void_p]
+        lib.pyrh_lte_plan_destroy.restype = None
+        lib.pyrh_lte_plan_destroy.argtypes = [C.c_void_p]
+        self.lib = lib
+        self.dev = dev                      # keeps the bound buffers alive
+        self.handle = C.c_void_p()
+        L.check(lib.pyrh_lte_plan_create(C.byref(dev.struct), dev.lines_t.data_ptr(), dev.nline,
+                                         C.byref(cfg), dev.out.data_ptr(), stream_ptr,
+                                         C.byref(self.handle)))
+        self.block = int(lib.pyrh_lte_plan_block(self.handle))
+        self.tuned_ms = float(lib.pyrh_lte_plan_ms(self.handle))
+
+    def launch(self, stream_ptr: int = 0) -> None:
+        L.check(self.lib.pyrh_lte_plan_launch(self.handle, stream_ptr))
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            self.lib.pyrh_lte_plan_destroy(self.handle)
+            self.handle = None
+
+
 def pack_uniform(batch: dict, nline: int, precision: int = L.PYRH_FP32) -> Packed:
     """Vectorised pack of a batch whose atmospheres share ndep and the
     wavelength grid (arrays with a leading atmosphere axis; continuum

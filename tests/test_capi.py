@@ -17,7 +17,7 @@ def _declared():
     for f in os.listdir(os.path.join(REPO, "include")):
         if f.endswith(".h"):
             src = open(os.path.join(REPO, "include", f)).read()
-            names |= set(re.findall(r"^\s*(?:pyrh_status|int32_t|size_t|const char \*)\s*(pyrh_\w+)\s*\(",
+            names |= set(re.findall(r"^\s*(?:pyrh_status|int32_t|size_t|double|void|const char \*)\s*(pyrh_\w+)\s*\(",
                                     src, re.M))
     return names
 

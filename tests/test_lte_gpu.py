@@ -172,3 +172,28 @@ def test_field_reversal_symmetry_large_batch(golden):
         assert np.abs(x[3] + y[3]).max() / ic < 1e-5
         assert np.abs(x[1] + z[1]).max() / ic < 1e-5
         assert np.abs(x[2] + z[2]).max() / ic < 1e-5
+
+
+def test_plan_tunes_and_replays_graph(golden):
+    """pyrh_lte_plan: the tuned tile is one of the candidates, and replaying
+    the captured graph gives exactly the spectra of a direct launch (the
+    tile only decides which block computes which wavelength)."""
+    import torch
+    b = golden("lte_batch")
+    atms = [batch_member(b, i) for i in range(b["T"].shape[0])]
+    fx = atms[0]
+    lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
+    pk = lte.pack(atms, n, FP32)
+    cfg = lte.make_config(precision=FP32, mu=1.0, vmicro_char=float(fx["vmicro_char"]),
+                          moving=bool(fx["moving"]))
+    db = lte.DeviceBatch(pk, lines, n)
+    db.run(cfg)
+    torch.cuda.synchronize()
+    direct = db.out.cpu().numpy().copy()
+    plan = lte.Plan(db, cfg)
+    assert plan.block % 32 == 0 and 32 <= plan.block <= 256 and plan.tuned_ms > 0
+    for _ in range(2):
+        db.out.zero_()
+        plan.launch()
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(db.out.cpu().numpy(), direct)
