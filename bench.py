@@ -273,7 +273,9 @@ def main():
     from pyrh_gb300 import lte, workload
 
     natm = args.natm
-    batch = workload.synthetic_batch(natm, seed=1000 + rank, dtype=np.float32)
+    from pyrh_gb300.shard import max_over_ranks, rank_seed
+    # weak scaling: every rank synthesises its own natm atmospheres
+    batch = workload.synthetic_batch(natm, seed=rank_seed(1000, rank), dtype=np.float32)
     lines, nline = lte.make_lines(batch["line_const"], batch["zeeman"], batch["zeeman_n"])
     pk = lte.pack_uniform(batch, nline, L.PYRH_FP32)
     db = lte.DeviceBatch(pk, lines, nline, device=f"cuda:{local}")
@@ -305,10 +307,7 @@ def main():
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
     clk = clocks.stop()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist)
     value = units * world / (ms / 1e3)
 
     # algorithmic bytes of one launch: every input array once + the output
@@ -344,10 +343,7 @@ def main():
         host_call()
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dist)
     e2e = {"value": units * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
            "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3,
            "path": "pyrh_lte_stokes_host (host arrays in, Stokes out)"}
