@@ -132,9 +132,9 @@ PYRH_HD D6<R> dsin(const D6<R>& a) {
 // ---------------------------------------------- Humlicek with derivative --
 // W(t) and dW/dt for t = a - i v, differentiating each region's rational
 // approximation exactly (so the derivative is that of the forward model).
-// Quotients of the form x / Q^2 divide by Q twice: |Q|^2 of the region-4
-// denominator reaches 1e21 near |v| = 5.5, and cdiv's |Q^2|^2 would
-// overflow single precision.
+// Derivatives of the rational forms as (P' - W Q') / Q with W = P / Q
+// already known: one complex division, and no Q^2, whose |Q^2|^2 would
+// overflow single precision near |v| = 5.5 (|Q|^2 reaches 1e21 there).
 template <typename R>
 PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
   const Cx<R> t = {a, -v};
@@ -157,8 +157,9 @@ PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
     D.r += R(0.75);
     Cx<R> dD = cmul(Cx<R>{R(2) * u.r + R(3), R(2) * u.i}, Cx<R>{R(2) * t.r, R(2) * t.i});
     W = cdiv(N, D);
-    Cx<R> num = cmul(dN, D), nd = cmul(N, dD);
-    dW = cdiv(cdiv(Cx<R>{num.r - nd.r, num.i - nd.i}, D), D);
+    // (N/D)' = (N' - W D') / D
+    const Cx<R> wd = cmul(W, dD);
+    dW = cdiv(Cx<R>{dN.r - wd.r, dN.i - wd.i}, D);
   } else if (a >= R(0.195) * fabs(v) - R(0.176)) {
     const R A[5] = {R(0.5642236), R(3.778987), R(11.96482), R(20.20933), R(16.4955)};
     const R B[5] = {R(6.699398), R(21.69274), R(39.27121), R(38.82363), R(16.4955)};
@@ -171,8 +172,8 @@ PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
       Q = cmul(Q, t); Q.r += B[n];
     }
     W = cdiv(P, Q);
-    Cx<R> x1 = cmul(dP, Q), x2 = cmul(P, dQ);
-    dW = cdiv(cdiv(Cx<R>{x1.r - x2.r, x1.i - x2.i}, Q), Q);
+    const Cx<R> wq = cmul(W, dQ);
+    dW = cdiv(Cx<R>{dP.r - wq.r, dP.i - wq.i}, Q);
   } else {
     // W = exp(t^2) - t P(u) / Q(u), u = -t^2
     const R A[7] = {R(0.56419), R(1.320522), R(35.7668), R(219.031), R(1540.787), R(3321.99), R(36183.31)};
@@ -192,9 +193,9 @@ PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
     Cx<R> r = cdiv(P, Q);
     Cx<R> tr = cmul(t, r);
     W = {E.r - tr.r, E.i - tr.i};
-    // d/dt [t P/Q] = P/Q + t (P'Q - PQ')/Q^2 * du/dt,  du/dt = -2t
-    Cx<R> x1 = cmul(dP, Q), x2 = cmul(P, dQ);
-    Cx<R> dr = cdiv(cdiv(Cx<R>{x1.r - x2.r, x1.i - x2.i}, Q), Q);
+    // d/dt [t P/Q] = P/Q + t (P' - r Q')/Q * du/dt,  du/dt = -2t
+    const Cx<R> rq = cmul(r, dQ);
+    Cx<R> dr = cdiv(Cx<R>{dP.r - rq.r, dP.i - rq.i}, Q);
     Cx<R> tdr = cmul(cmul(t, dr), Cx<R>{R(-2) * t.r, R(-2) * t.i});
     Cx<R> dE = cmul(E, Cx<R>{R(2) * t.r, R(2) * t.i});
     dW = {dE.r - r.r - tdr.r, dE.i - r.i - tdr.i};
@@ -357,7 +358,7 @@ PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const
                          const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
                          const R* cweight, const int* cq, int maxcomp, const R q[8],
                          const R* qb, R out[NS][kNX]) {
-  const R ichi = R(1) / q[0];
+  const R ichi = fdiv(R(1), q[0]);
   R eb[NS][4], cb[NS][4];
   R gb[NS][4];   // adjoints of s2g, gQ, gU, gV
   for (int s = 0; s < NS; ++s) {
@@ -495,11 +496,11 @@ PYRH_HD void bezier3_coeffs_d(R dt, R c[5], R dc[5]) {
   bezier3_coeffs(dt, c[0], c[1], c[2], c[3], c[4]);
   const R thr = sizeof(R) == 8 ? R(5.e-2) : R(1.5);
   if (dt >= thr) {
-    const R e = c[4], t = dt, t3 = t * t * t;
-    dc[0] = (R(6) - R(6) * t + R(3) * t * t - R(6) * e) / t3 - R(3) * c[0] / t;
-    dc[1] = e - R(3) * c[1] / t;
-    dc[2] = R(3) * (R(-4) + R(2) * t + (R(4) + R(2) * t) * e) / t3 - R(3) * c[2] / t;
-    dc[3] = R(3) * (e * (R(-2) - R(2) * t - t * t) + R(2)) / t3 - R(3) * c[3] / t;
+    const R e = c[4], t = dt, rt = fdiv(R(1), t), rt3 = rt * rt * rt;
+    dc[0] = (R(6) - R(6) * t + R(3) * t * t - R(6) * e) * rt3 - R(3) * c[0] * rt;
+    dc[1] = e - R(3) * c[1] * rt;
+    dc[2] = R(3) * (R(-4) + R(2) * t + (R(4) + R(2) * t) * e) * rt3 - R(3) * c[2] * rt;
+    dc[3] = R(3) * (e * (R(-2) - R(2) * t - t * t) + R(2)) * rt3 - R(3) * c[3] * rt;
     dc[4] = -e;
   } else if (sizeof(R) == 8) {
     const R t = dt, t2 = t * t, t3 = t2 * t;
@@ -534,25 +535,44 @@ PYRH_HD void bezier3_coeffs_d(R dt, R c[5], R dc[5]) {
 
 // --------------------------------------------------------- cent_deriv VJP --
 // w = cent_deriv(dsup, dsdn, a, b, c); accumulates adjoints of all five args.
+// The quantities that depend only on the two intervals are computed once per
+// interval pair (CdW) and shared by the entries of one depth.
 template <typename R>
-PYRH_HD void cent_deriv_vjp(R dsup, R dsdn, R a, R b, R c, R wbar, R& dsupb, R& dsdnb, R& ab,
+struct CdW {
+  R rsup, rsdn, al, dal_dsup, dal_dsdn;
+};
+
+template <typename R>
+PYRH_HD CdW<R> cd_weights(R dsup, R dsdn) {
+  CdW<R> w;
+  w.rsup = fdiv(R(1), dsup);
+  w.rsdn = fdiv(R(1), dsdn);
+  const R rs = fdiv(R(1), dsdn + dsup);
+  const R third = R(0.333333333333333333333333);
+  w.al = third * (R(1) + dsdn * rs);
+  w.dal_dsdn = third * dsup * rs * rs;
+  w.dal_dsup = -third * dsdn * rs * rs;
+  return w;
+}
+
+template <typename R>
+PYRH_HD void cent_deriv_vjp(const CdW<R>& w, R a, R b, R c, R wbar, R& dsupb, R& dsdnb, R& ab,
                             R& bb, R& cb) {
-  const R fim1 = (b - a) / dsup, fi = (c - b) / dsdn;
+  const R fim1 = (b - a) * w.rsup, fi = (c - b) * w.rsdn;
   if (!(fim1 * fi > R(0)) || wbar == R(0)) return;
-  const R s = dsdn + dsup;
-  const R al = R(0.333333333333333333333333) * (R(1) + dsdn / s);
-  const R D = (R(1) - al) * fim1 + al * fi, N = fim1 * fi;
-  const R Nb = wbar / D, Db = -wbar * N / (D * D);
-  const R f1b = Nb * fi + Db * (R(1) - al);
-  const R f2b = Nb * fim1 + Db * al;
+  const R D = (R(1) - w.al) * fim1 + w.al * fi, N = fim1 * fi;
+  const R rD = fdiv(R(1), D);
+  const R Nb = wbar * rD, Db = -Nb * N * rD;
+  const R f1b = Nb * fi + Db * (R(1) - w.al);
+  const R f2b = Nb * fim1 + Db * w.al;
   const R alb = Db * (fi - fim1);
-  dsdnb += alb * R(0.333333333333333333333333) * dsup / (s * s);
-  dsupb -= alb * R(0.333333333333333333333333) * dsdn / (s * s);
-  ab -= f1b / dsup;
-  bb += f1b / dsup - f2b / dsdn;
-  cb += f2b / dsdn;
-  dsupb -= f1b * fim1 / dsup;
-  dsdnb -= f2b * fi / dsdn;
+  dsdnb += alb * w.dal_dsdn;
+  dsupb += alb * w.dal_dsup;
+  ab -= f1b * w.rsup;
+  bb += f1b * w.rsup - f2b * w.rsdn;
+  cb += f2b * w.rsdn;
+  dsupb -= f1b * fim1 * w.rsup;
+  dsdnb -= f2b * fi * w.rsdn;
 }
 
 // ----------------------------------------------------------- DELO step ---
@@ -569,7 +589,7 @@ struct StepIn {
 template <typename R>
 PYRH_HD void md_solve(R c, const R b[3], const R k0[3], const R V[4], R x[4]) {
   const R sig = R(1) + c * (k0[0] * k0[0] + k0[1] * k0[1] + k0[2] * k0[2]);
-  const R f = c / sig;
+  const R f = fdiv(c, sig);
   const R kb = k0[0] * b[0] + k0[1] * b[1] + k0[2] * b[2];
   const R kv = k0[0] * V[1] + k0[1] * V[2] + k0[2] * V[3];
   R w[3], z[3];
@@ -577,8 +597,8 @@ PYRH_HD void md_solve(R c, const R b[3], const R k0[3], const R V[4], R x[4]) {
     w[j] = b[j] - f * kb * k0[j];
     z[j] = V[j + 1] - f * kv * k0[j];
   }
-  const R x0 = (V[0] - (b[0] * z[0] + b[1] * z[1] + b[2] * z[2])) /
-               (sig - (b[0] * w[0] + b[1] * w[1] + b[2] * w[2]));
+  const R x0 = fdiv(V[0] - (b[0] * z[0] + b[1] * z[1] + b[2] * z[2]),
+                    sig - (b[0] * w[0] + b[1] * w[1] + b[2] * w[2]));
   x[0] = x0;
   for (int j = 0; j < 3; ++j) x[j + 1] = z[j] - x0 * w[j];
 }
@@ -703,79 +723,107 @@ struct Tape {
   R dchi_up0;                  // initial dchi_up
 };
 
-template <typename R>
-PYRH_HD void delo_forward(Tape<R>& tp, const R* ds, int nd, double B0, double B1, R out[4]) {
-  // depth index j; ds[j] = path length between j-1 and j
+// Forward DELO-Bezier3 sweep from the bottom boundary to the surface
+// (bezier_1D.c:52-300), writing the tape.  qop(k, q) returns the optical
+// quantities of depth k; they are computed once, two depths ahead of the
+// step that first needs them, kept in a three-depth register window and
+// written to the tape (never read back here).
+template <typename R, typename QOp>
+PYRH_HD void delo_forward(Tape<R>& tp, const R* ds, int nd, double B0, double B1, R out[4],
+                          const QOp& qop) {
   const int N = nd;
-  const double dtau0 = 0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * (double)ds[N - 1];
-  tp.I[N - 1][0] = R(B1 - (B0 - B1) / dtau0);
-  tp.I[N - 1][1] = tp.I[N - 1][2] = tp.I[N - 1][3] = R(0);
+  R qa[8], qb[8], qc[8];   // depths k+1, k, k-1 of the step being taken
+  qop(N - 1, qa);
+  qop(N - 2, qb);
+  qop(N - 3, qc);
+  for (int n = 0; n < 8; ++n) {
+    tp.q[N - 1][n] = qa[n];
+    tp.q[N - 2][n] = qb[n];
+    tp.q[N - 3][n] = qc[n];
+  }
+  const double dtau0 = 0.5 * ((double)qa[0] + (double)qb[0]) * (double)ds[N - 1];
+  R Iu[4] = {R(B1 - (B0 - B1) / dtau0), R(0), R(0), R(0)};
+  for (int n = 0; n < 4; ++n) tp.I[N - 1][n] = Iu[n];
+  R dSu[4], dKu[3], dchi_c, Tk;
   {
     const int k = N - 2;
     const R dsup = ds[k + 1], dsdn = ds[k];
-    const R cu = tp.q[k + 1][0], cc = tp.q[k][0], cd = tp.q[k - 1][0];
-    const R dchi_up = (cc - cu) / dsup;
-    const R dchi_c = cent_deriv<R>(dsup, dsdn, cu, cc, cd);
+    const R cu = qa[0], cc = qb[0], cd = qc[0];
+    const R dchi_up = fdiv(cc - cu, dsup);
+    dchi_c = cent_deriv<R>(dsup, dsdn, cu, cc, cd);
     const R c2 = fmax(cc - (dsup / R(3)) * dchi_c, R(0));
     const R c1 = fmax(cu + (dsup / R(3)) * dchi_up, R(0));
-    tp.T[k] = R(0.25) * dsup * (cc + cu + c1 + c2);
+    Tk = R(0.25) * dsup * (cc + cu + c1 + c2);
+    tp.T[k] = Tk;
     tp.dchi[k] = dchi_c;
     tp.dchi_up0 = dchi_up;
-    for (int n = 0; n < 4; ++n) tp.dS0[N - 1][n] = (tp.q[k][1 + n] - tp.q[k + 1][1 + n]) / tp.T[k];
-    for (int n = 0; n < 3; ++n) tp.dK0[N - 1][n] = (tp.q[k][5 + n] - tp.q[k + 1][5 + n]) / tp.T[k];
+    for (int n = 0; n < 4; ++n) dSu[n] = tp.dS0[N - 1][n] = (qb[1 + n] - qa[1 + n]) / Tk;
+    for (int n = 0; n < 3; ++n) dKu[n] = tp.dK0[N - 1][n] = (qb[5 + n] - qa[5 + n]) / Tk;
   }
   for (int k = N - 2; k >= 1; --k) {
+    // q[k-2] enters this step's chi derivative and the next step's window
+    R qd[8];
+    if (k > 1) {
+      qop(k - 2, qd);
+      for (int n = 0; n < 8; ++n) tp.q[k - 2][n] = qd[n];
+    }
     const R dsdn = ds[k];
-    R dchi_dn;
-    if (k > 1) dchi_dn = cent_deriv<R>(dsdn, ds[k - 1], tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0]);
-    else dchi_dn = (tp.q[k - 1][0] - tp.q[k][0]) / dsdn;
-    const R c2 = fmax(tp.q[k][0] + (dsdn / R(3)) * tp.dchi[k], R(0));
-    const R c1 = fmax(tp.q[k - 1][0] - (dsdn / R(3)) * dchi_dn, R(0));
-    const R Tdw = R(0.25) * dsdn * (tp.q[k][0] + tp.q[k - 1][0] + c1 + c2);
+    const R dchi_dn = (k > 1) ? cent_deriv<R>(dsdn, ds[k - 1], qb[0], qc[0], qd[0])
+                              : fdiv(qc[0] - qb[0], dsdn);
+    const R c2 = fmax(qb[0] + (dsdn / R(3)) * dchi_c, R(0));
+    const R c1 = fmax(qc[0] - (dsdn / R(3)) * dchi_dn, R(0));
+    const R Tdw = R(0.25) * dsdn * (qb[0] + qc[0] + c1 + c2);
     tp.T[k - 1] = Tdw;
     tp.dchi[k - 1] = dchi_dn;
-    StepIn<R> s;
+    StepIn<R> st;
     R cf[5];
-    bezier3_coeffs(tp.T[k], cf[0], cf[1], cf[2], cf[3], cf[4]);
-    s.al = cf[0]; s.be = cf[1]; s.ga = cf[2]; s.th = cf[3]; s.ep = cf[4];
-    s.dt03 = tp.T[k] / R(3);
+    bezier3_coeffs(Tk, cf[0], cf[1], cf[2], cf[3], cf[4]);
+    st.al = cf[0]; st.be = cf[1]; st.ga = cf[2]; st.th = cf[3]; st.ep = cf[4];
+    st.dt03 = Tk / R(3);
     for (int n = 0; n < 3; ++n) {
-      s.ku[n] = tp.q[k + 1][5 + n];
-      s.k0[n] = tp.q[k][5 + n];
-      s.dku[n] = tp.dK0[k + 1 == N - 1 ? N - 1 : k + 1][n];
-      s.dk0[n] = cent_deriv<R>(tp.T[k], Tdw, tp.q[k + 1][5 + n], tp.q[k][5 + n], tp.q[k - 1][5 + n]);
-      tp.dK0[k][n] = s.dk0[n];
+      st.ku[n] = qa[5 + n];
+      st.k0[n] = qb[5 + n];
+      st.dku[n] = dKu[n];
+      st.dk0[n] = cent_deriv<R>(Tk, Tdw, qa[5 + n], qb[5 + n], qc[5 + n]);
+      tp.dK0[k][n] = st.dk0[n];
     }
     for (int n = 0; n < 4; ++n) {
-      s.Su[n] = tp.q[k + 1][1 + n];
-      s.S0[n] = tp.q[k][1 + n];
-      s.dSu[n] = tp.dS0[k + 1 == N - 1 ? N - 1 : k + 1][n];
-      s.dS0[n] = cent_deriv<R>(tp.T[k], Tdw, tp.q[k + 1][1 + n], tp.q[k][1 + n], tp.q[k - 1][1 + n]);
-      tp.dS0[k][n] = s.dS0[n];
-      s.Iu[n] = tp.I[k + 1][n];
+      st.Su[n] = qa[1 + n];
+      st.S0[n] = qb[1 + n];
+      st.dSu[n] = dSu[n];
+      st.dS0[n] = cent_deriv<R>(Tk, Tdw, qa[1 + n], qb[1 + n], qc[1 + n]);
+      tp.dS0[k][n] = st.dS0[n];
+      st.Iu[n] = Iu[n];
     }
-    R x[4], V[4], b[3], c;
-    step_fwd(s, x, V, b, c);
-    for (int n = 0; n < 4; ++n) tp.I[k][n] = x[n];
+    R x[4], V[4], bv[3], c;
+    step_fwd(st, x, V, bv, c);
+    for (int n = 0; n < 4; ++n) tp.I[k][n] = Iu[n] = x[n];
+    for (int n = 0; n < 4; ++n) dSu[n] = st.dS0[n];
+    for (int n = 0; n < 3; ++n) dKu[n] = st.dk0[n];
+    dchi_c = dchi_dn;
+    Tk = Tdw;
+    for (int n = 0; n < 8; ++n) {
+      qa[n] = qb[n];
+      qb[n] = qc[n];
+      if (k > 1) qc[n] = qd[n];
+    }
   }
-  // last interval
-  const double dtau = 0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * (double)ds[1];
+  // last interval: now qa = q[1], qb = q[0]
+  const double dtau = 0.5 * ((double)qb[0] + (double)qa[0]) * (double)ds[1];
   double w[3];
   w3(dtau, w);
   const R w0 = R(w[0]), w1 = R(w[1]), wd = R(w[1] / dtau);
-  const R* ku = &tp.q[1][5];
-  const R* k0 = &tp.q[0][5];
-  const R* dSu = tp.dS0[1];
+  const R* ku = &qa[5];
+  const R* k0 = &qb[5];
   R V[4];
-  V[0] = w0 * tp.q[0][1] - w1 * dSu[0] + (R(1) - w0) * tp.I[1][0] -
-         wd * (ku[0] * tp.I[1][1] + ku[1] * tp.I[1][2] + ku[2] * tp.I[1][3]);
+  V[0] = w0 * qb[1] - w1 * dSu[0] + (R(1) - w0) * Iu[0] -
+         wd * (ku[0] * Iu[1] + ku[1] * Iu[2] + ku[2] * Iu[3]);
   for (int j = 0; j < 3; ++j)
-    V[j + 1] = w0 * tp.q[0][2 + j] - w1 * dSu[j + 1] + (R(1) - w0) * tp.I[1][j + 1] -
-               wd * ku[j] * tp.I[1][0];
+    V[j + 1] = w0 * qb[2 + j] - w1 * dSu[j + 1] + (R(1) - w0) * Iu[j + 1] - wd * ku[j] * Iu[0];
   const R g = w0 - wd;
   const R bv[3] = {g * k0[0], g * k0[1], g * k0[2]};
-  const R x0 = (V[0] - (bv[0] * V[1] + bv[1] * V[2] + bv[2] * V[3])) /
-               (R(1) - (bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2]));
+  const R x0 = fdiv(V[0] - (bv[0] * V[1] + bv[1] * V[2] + bv[2] * V[3]),
+                    R(1) - (bv[0] * bv[0] + bv[1] * bv[1] + bv[2] * bv[2]));
   out[0] = x0;
   for (int j = 0; j < 3; ++j) out[j + 1] = V[j + 1] - x0 * bv[j];
   for (int n = 0; n < 4; ++n) tp.I[0][n] = out[n];
@@ -910,6 +958,10 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
     for (int n = 0; n < 3; ++n) bvec[n] = pK * st.k0[n] + c * st.dk0[n];
     const R* x = tp.I[k];
     const R dsdn = ds[k];
+    const R rdsdn = fdiv(R(1), dsdn);
+    const CdW<R> wT = cd_weights<R>(Tk, Tdw);
+    CdW<R> wchi;
+    if (k > 1) wchi = cd_weights<R>(dsdn, ds[k - 1]);
     const R dchi_c = tp.dchi[k], dchi_dn = tp.dchi[k - 1];
     const bool c2pos = tp.q[k][0] + (dsdn / R(3)) * dchi_c > R(0);
     const bool c1pos = tp.q[k - 1][0] - (dsdn / R(3)) * dchi_dn > R(0);
@@ -923,10 +975,10 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       for (int n = 0; n < 3; ++n) sb.dk0[n] += dKb[s][n];
       R Tkb = R(0), Tdwb = Tb[s];
       for (int n = 0; n < 3; ++n)
-        cent_deriv_vjp<R>(Tk, Tdw, tp.q[k + 1][5 + n], tp.q[k][5 + n], tp.q[k - 1][5 + n], sb.dk0[n],
+        cent_deriv_vjp<R>(wT, tp.q[k + 1][5 + n], tp.q[k][5 + n], tp.q[k - 1][5 + n], sb.dk0[n],
                           Tkb, Tdwb, qu[s][5 + n], qc[s][5 + n], qd[s][5 + n]);
       for (int n = 0; n < 4; ++n)
-        cent_deriv_vjp<R>(Tk, Tdw, tp.q[k + 1][1 + n], tp.q[k][1 + n], tp.q[k - 1][1 + n], sb.dS0[n],
+        cent_deriv_vjp<R>(wT, tp.q[k + 1][1 + n], tp.q[k][1 + n], tp.q[k - 1][1 + n], sb.dS0[n],
                           Tkb, Tdwb, qu[s][1 + n], qc[s][1 + n], qd[s][1 + n]);
       Tkb += sb.al * dcf[0] + sb.be * dcf[1] + sb.ga * dcf[2] + sb.th * dcf[3] + sb.ep * dcf[4] +
              sb.dt03 / R(3);
@@ -942,11 +994,11 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       }
       if (k > 1) {
         R d1 = 0, d2 = 0;
-        cent_deriv_vjp<R>(dsdn, ds[k - 1], tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0], dchi_dnb, d1,
-                          d2, qc[s][0], qd[s][0], qdd[s][0]);
+        cent_deriv_vjp<R>(wchi, tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0], dchi_dnb, d1, d2,
+                          qc[s][0], qd[s][0], qdd[s][0]);
       } else {
-        qd[s][0] += dchi_dnb / dsdn;
-        qc[s][0] -= dchi_dnb / dsdn;
+        qd[s][0] += dchi_dnb * rdsdn;
+        qc[s][0] -= dchi_dnb * rdsdn;
       }
       for (int n = 0; n < 4; ++n) { Ib[s][n] = sb.Iu[n]; dSb[s][n] = sb.dSu[n]; }
       for (int n = 0; n < 3; ++n) dKb[s][n] = sb.dku[n];
@@ -998,8 +1050,8 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       ec[s][0] += dchi_upb / dsup;
       eu[s][0] -= dchi_upb / dsup;
       R d1 = 0, d2 = 0;
-      cent_deriv_vjp<R>(dsup, dsdn, cu, cc, tp.q[k - 1][0], dchi_cb, d1, d2, eu[s][0], ec[s][0],
-                        ed[s][0]);
+      cent_deriv_vjp<R>(cd_weights<R>(dsup, dsdn), cu, cc, tp.q[k - 1][0], dchi_cb, d1, d2,
+                        eu[s][0], ec[s][0], ed[s][0]);
       const double ib = (double)Ib[s][0];
       bpl[1][s] = R(ib * (1.0 + 1.0 / dtau0));
       bpl[0][s] = R(-ib / dtau0);

@@ -240,11 +240,29 @@ struct ActiveSet {
   R hckl;                        // h c / (k_B lambda)
 };
 
+// Shared-memory accumulation.  FP64: atomicAdd.  FP32: compensated -- the
+// atomic returns the value it added to, the rounding error of that one
+// addition follows exactly from it (Knuth's TwoSum), and the errors are summed
+// in a second array that is added back in FP64 when the block flushes.  The
+// quadrature then carries ~FP64 accuracy at FP32 atomic cost.
+__device__ __forceinline__ void acc_add(double* hi, double* lo, double v) {
+  (void)lo;
+  atomicAdd(hi, v);
+}
+__device__ __forceinline__ void acc_add(float* hi, float* lo, float v) {
+  const float old = atomicAdd(hi, v);
+  const float s = old + v;
+  const float bv = s - old;
+  atomicAdd(lo, (old - (s - bv)) + (v - bv));
+}
+
 // Per-block staging of the quantities every thread reads at every depth.
 template <typename R>
 struct NlteShared {
   R* Gs;      // [nlev^2][nd] Gamma of this block's wavelengths
+  R* Gl;      // [nlev^2][nd] compensation terms of Gs (FP32 mode)
   R* Js;      // [nd][32] new J of this block's wavelengths
+  R* Jl;      // [nd][32] compensation terms of Js (FP32 mode)
   R* n;       // [nlev][nd] populations
   R* lnst;    // [nlev][nd] log of the LTE populations
   R* iT;      // [nd] 1 / T
@@ -438,14 +456,17 @@ __host__ __device__ inline size_t formal_smem_layout(int nlev, int nd, int nrays
     off += ((sizeof(R) * count + 15) / 16) * 16;
     return p;
   };
+  const bool comp = sizeof(R) == 4;
   R* Gs = take((size_t)nlev * nlev * nd);
+  R* Gl = take(comp ? (size_t)nlev * nlev * nd : 0);
   R* Js = take((size_t)nd * 32);
+  R* Jl = take(comp ? (size_t)nd * 32 : 0);
   R* n = take((size_t)nlev * nd);
   R* lnst = take((size_t)nlev * nd);
   R* iT = take((size_t)nd);
   R* ds = take((size_t)nrays * nd);
   R* wphi = take((size_t)(nline > 0 ? nline : 1) * nd);
-  if (sh) *sh = NlteShared<R>{Gs, Js, n, lnst, iT, ds, wphi};
+  if (sh) *sh = NlteShared<R>{Gs, Gl, Js, Jl, n, lnst, iT, ds, wphi};
   return off;
 }
 
@@ -469,8 +490,15 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
   NlteShared<R> sh;
   formal_smem_layout<R>(nlev, b.max_ndep, A.nrays, b.max_nline, &sh, smem_raw);
   const int nthr = blockDim.x;
-  for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) sh.Gs[e] = R(0);
-  for (int e = threadIdx.x; e < nd * 32; e += nthr) sh.Js[e] = R(0);
+  const bool comp = sizeof(R) == 4;
+  for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) {
+    sh.Gs[e] = R(0);
+    if (comp) sh.Gl[e] = R(0);
+  }
+  for (int e = threadIdx.x; e < nd * 32; e += nthr) {
+    sh.Js[e] = R(0);
+    if (comp) sh.Jl[e] = R(0);
+  }
   for (int e = threadIdx.x; e < nlev * nd; e += nthr) {
     const int i = e / nd, k = e % nd;
     sh.n[e] = R(b.n[(int64_t)i * b.total_depth + doff + k]);
@@ -490,6 +518,13 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
   const int lane = threadIdx.x & 31, ray = threadIdx.x >> 5;
   const int la = la0 + lane;
   const bool live = (la < ns) && (ray < A.nrays);
+  // A warp is 32 wavelengths of one ray.  Where all its lanes are live they
+  // run the depth and transition loops in step and sum each Gamma
+  // contribution over the warp with a shuffle tree before one shared-memory
+  // addition (lanes almost always share their transitions); elsewhere every
+  // lane adds its own.
+  const unsigned full = 0xffffffffu;
+  const bool coll = __ballot_sync(full, live) == full;
   if (live) {
     const double muz = A.muz[ray];
     const R* dsl = sh.ds + ray * nd;
@@ -530,12 +565,17 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
     op.A = &A; op.tr = tr; op.as = &as; op.sh = &sh;
     op.nd = nd; op.ns = ns; op.la = la; op.coff = coff;
     const int ndir = angle_dep ? 2 : 1;
-    for (int dir = 0; dir < ndir; ++dir) {
+    // in a collective warp every lane runs the largest direction count, the
+    // extra pass contributing nothing
+    const int ndir_loop = coll ? __reduce_max_sync(full, ndir) : ndir;
+    for (int dir = 0; dir < ndir_loop; ++dir) {
+      const bool mine = dir < ndir;
       const int to_obs = angle_dep ? dir : 0;
       op.q = 2 * ray + to_obs;
-      R wdir;
-      R emergent;
-      if (angle_dep) {
+      R wdir = R(0);
+      R emergent = R(0);
+      if (!mine) {
+      } else if (angle_dep) {
         if (emergent_only && !to_obs) continue;
         bezier_full<R>(op, dsl, nd, to_obs, B0, B1, Jold, I, Psi, Ieff, chis);
         wdir = R(0.5 * A.wmu[ray]);
@@ -552,19 +592,21 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
         wdir = R(A.wmu[ray]);
       }
       if (emergent_only) {
-        I_out[b.lam_off[p] + la] = (double)emergent;
+        if (mine) I_out[b.lam_off[p] + la] = (double)emergent;
         continue;
       }
+      const int nact = mine ? as.n : 0;
+      const int nm = coll ? __reduce_max_sync(full, nact) : nact;
       // Gamma, coupling and J at every depth (fillgamma.c:82-332, formal.c:247-256)
       for (int k = 0; k < nd; ++k) {
-        atomicAdd(&sh.Js[k * 32 + lane], wdir * I[k]);
+        if (mine) acc_add(&sh.Js[k * 32 + lane], &sh.Jl[k * 32 + lane], wdir * I[k]);
         if (!eval_operator) continue;
-        const R psi = Psi[k] / chis[k];
-        const R Ieff_k = angle_dep ? Ieff[k] : I[k] - psi * Ieff[k];
+        const R psi = mine ? Psi[k] / chis[k] : R(0);
+        const R Ieff_k = !mine ? R(0) : angle_dep ? Ieff[k] : I[k] - psi * Ieff[k];
         // per transition: V W (product formed without the h c / 4 pi that
         // cancels in it), U = TW G V and the stimulated-emission factor G
         R VW[PYRH_NLTE_MAX_ACTIVE], U[PYRH_NLTE_MAX_ACTIVE], G[PYRH_NLTE_MAX_ACTIVE];
-        for (int m = 0; m < as.n; ++m) {
+        for (int m = 0; m < nact; ++m) {
           const pyrh_nlte_transition& t = tr[as.t[m]];
           if (t.type == 0) {
             const int64_t pi =
@@ -580,26 +622,42 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
             U[m] = (as.tw[m] * G[m]) * as.vb[m];
           }
         }
-        for (int m = 0; m < as.n; ++m) {
-          const pyrh_nlte_transition& t = tr[as.t[m]];
-          const int i = t.i, j = t.j;
-          // cross-coupling sums over the active set (addtoCoupling)
-          R chi_up_i = 0, chi_down_j = 0, U_down_j = 0, U_down_i = 0;
-          int cnt = 0;
-          for (int q = 0; q < as.n; ++q) {
-            const pyrh_nlte_transition& u = tr[as.t[q]];
-            const R chicc = VW[q] * (sh.n[u.i * nd + k] - G[q] * sh.n[u.j * nd + k]);
-            if (u.i == i) chi_up_i += chicc;
-            if (u.j == j) { chi_down_j += chicc; U_down_j += U[q]; }
-            if (u.j == i) { U_down_i += U[q]; ++cnt; }
+        for (int m = 0; m < nm; ++m) {
+          int key = -1;
+          R gij = 0, gji = 0;
+          if (m < nact) {
+            const pyrh_nlte_transition& t = tr[as.t[m]];
+            const int i = t.i, j = t.j;
+            key = i * nlev + j;
+            // cross-coupling sums over the active set (addtoCoupling)
+            R chi_up_i = 0, chi_down_j = 0, U_down_j = 0, U_down_i = 0;
+            int cnt = 0;
+            for (int q = 0; q < nact; ++q) {
+              const pyrh_nlte_transition& u = tr[as.t[q]];
+              const R chicc = VW[q] * (sh.n[u.i * nd + k] - G[q] * sh.n[u.j * nd + k]);
+              if (u.i == i) chi_up_i += chicc;
+              if (u.j == j) { chi_down_j += chicc; U_down_j += U[q]; }
+              if (u.j == i) { U_down_i += U[q]; ++cnt; }
+            }
+            const R wlamu = VW[m] * wdir;
+            gji = Ieff_k * wlamu;
+            gij = (as.tw[m] + Ieff_k) * G[m] * wlamu - chi_up_i * (psi * U_down_j) * wdir;
+            // one term per active transition whose upper level is i
+            if (cnt) gji += R(cnt) * chi_down_j * (psi * U_down_i) * wdir;
           }
-          const R wlamu = VW[m] * wdir;
-          R gji = Ieff_k * wlamu;
-          R gij = (as.tw[m] + Ieff_k) * G[m] * wlamu - chi_up_i * (psi * U_down_j) * wdir;
-          // one term per active transition whose upper level is i
-          if (cnt) gji += R(cnt) * chi_down_j * (psi * U_down_i) * wdir;
-          atomicAdd(&sh.Gs[(i * nlev + j) * nd + k], gij);
-          atomicAdd(&sh.Gs[(j * nlev + i) * nd + k], gji);
+          // one match per lane and iteration, from this single site
+          const unsigned peers = coll ? __match_any_sync(full, key) : 0u;
+          if (peers == full && key >= 0) {   // the whole warp adds to one entry
+            for (int o = 16; o > 0; o >>= 1) {
+              gij += __shfl_xor_sync(full, gij, o);
+              gji += __shfl_xor_sync(full, gji, o);
+            }
+            if (lane != 0) continue;
+          }
+          if (key < 0) continue;
+          const int i = key / nlev, j = key % nlev;
+          acc_add(&sh.Gs[(i * nlev + j) * nd + k], &sh.Gl[(i * nlev + j) * nd + k], gij);
+          acc_add(&sh.Gs[(j * nlev + i) * nd + k], &sh.Gl[(j * nlev + i) * nd + k], gji);
         }
       }
     }
@@ -608,12 +666,13 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
   if (emergent_only) return;
   for (int e = threadIdx.x; e < nd * 32; e += nthr) {
     const int k = e / 32, l = e % 32;
-    if (la0 + l < ns) A.Jnew[coff + (int64_t)k * ns + la0 + l] = (double)sh.Js[e];
+    if (la0 + l < ns)
+      A.Jnew[coff + (int64_t)k * ns + la0 + l] = (double)sh.Js[e] + (comp ? (double)sh.Jl[e] : 0.0);
   }
   if (eval_operator)
     for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) {
       const int ij = e / nd, k = e % nd;
-      const double v = (double)sh.Gs[e];
+      const double v = (double)sh.Gs[e] + (comp ? (double)sh.Gl[e] : 0.0);
       if (v != 0.0) atomicAdd(&A.Gamma[(int64_t)ij * b.total_depth + doff + k], v);
     }
 }

@@ -48,7 +48,7 @@ def rf_harness(tmp_path_factory):
     out = str(tmp_path_factory.mktemp("rf") / "librf_host.so")
     src = os.path.join(REPO, "tests", "native", "rf_host.cu")
     subprocess.run([nvcc, "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-shared",
-                    "-diag-suppress", "20011,20013", "-x", "cu", src, "-o", out], check=True)
+                    "-diag-suppress", "20011,20013,20015", "-x", "cu", src, "-o", out], check=True)
     return C.CDLL(out)
 
 

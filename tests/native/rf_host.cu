@@ -111,12 +111,14 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     for (int k = 0; k < nd; ++k) {
       cc[k] = R(chi_c[(int64_t)la * nd + k]);
       ec[k] = R(eta_c[(int64_t)la * nd + k]);
-      local_q<R>(nline, &ld[0][k], PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
-                 PYRH_MAX_COMPONENTS, cc[k], ec[k], tape.q[k]);
     }
+    auto qop = [&](int k, R* q) {
+      local_q<R>(nline, &ld[0][k], PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
+                 PYRH_MAX_COMPONENTS, cc[k], ec[k], q);
+    };
     const double B0 = planck(T[nd - 2], lm), B1 = planck(T[nd - 1], lm);
     R out[4];
-    delo_forward<R>(tape, ds, nd, B0, B1, out);
+    delo_forward<R>(tape, ds, nd, B0, B1, out, qop);
     for (int s = 0; s < 4; ++s) stokes[la * 4 + s] = double(out[s]);
     const R seed[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
     Emit<R, JAC> emit{nd, T, lm, rfl, nline, &ld[0][0], geo, dlam, inwin, ncomp, cs, cw, cq, cc, ec,
