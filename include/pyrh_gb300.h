@@ -189,28 +189,35 @@ void pyrh_lte_plan_destroy(pyrh_lte_plan plan);
 /* rf_out (float or double following the precision): for atmosphere p,
    entries [24 * cont_off[p], 24 * (cont_off[p] + ndep[p] * nlam[p])) laid
    out [stokes][param][depth][lambda] (lambda fastest): dS_s(lambda)/dx(k).
+   rf_loggf_out (optional, NULL to skip): dS_s(lambda)/d log10(gf) of every
+   line, entries [4 * nline * lam_off[p], 4 * nline * (lam_off[p] + nlam[p]))
+   laid out [line][stokes][lambda] -- the atomic-parameter response functions
+   of compute1d(..., get_atomic_rfs=True) (pyrh.pyx:537-668), there for
+   Stokes I of NO_STOKES syntheses only.
    stokes_out receives the emergent Stokes vectors as for pyrh_lte_stokes. */
 pyrh_status pyrh_lte_rf(const pyrh_lte_batch *batch, const pyrh_line *lines, int32_t nline,
                         const pyrh_lte_config *cfg, void *stokes_out, void *rf_out,
-                        void *stream);
+                        void *rf_loggf_out, void *stream);
 
 /* chi2[p] = sum over lambda and s of weights * (S_s(lambda) - obs)^2, with
    obs and weights laid out like stokes_out; grad_out is [6][total_depth]
-   (d chi2[p] / d x(k) at param * total_depth + depth_off[p] + k).  chi2_out
-   ([natm]) and grad_out are overwritten. */
+   (d chi2[p] / d x(k) at param * total_depth + depth_off[p] + k);
+   grad_loggf_out (optional) is [natm][nline], d chi2[p] / d log10(gf_l).
+   The outputs are overwritten. */
 pyrh_status pyrh_lte_chi2_grad(const pyrh_lte_batch *batch, const pyrh_line *lines,
                                int32_t nline, const pyrh_lte_config *cfg, const void *obs,
                                const void *weights, void *stokes_out, void *chi2_out,
-                               void *grad_out, void *stream);
+                               void *grad_out, void *grad_loggf_out, void *stream);
 
 /* Vector-Jacobian product: grad_out[x * total_depth + depth_off[p] + k] =
    sum over lambda and s of dL_dstokes * dS_s(lambda)/dx(k), with dL_dstokes
    laid out like stokes_out (the adjoint a reverse-mode framework calls with
-   the upstream gradient).  grad_out is overwritten. */
+   the upstream gradient); grad_loggf_out (optional) [natm][nline] as for
+   pyrh_lte_chi2_grad.  The outputs are overwritten. */
 pyrh_status pyrh_lte_stokes_vjp(const pyrh_lte_batch *batch, const pyrh_line *lines,
                                 int32_t nline, const pyrh_lte_config *cfg,
                                 const void *dL_dstokes, void *stokes_out, void *grad_out,
-                                void *stream);
+                                void *grad_loggf_out, void *stream);
 
 /* ------------------------------------------------------------------ NLTE
  * MALI lambda iteration for one active atom per atmosphere, replacing the

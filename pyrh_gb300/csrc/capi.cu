@@ -166,7 +166,8 @@ pyrh_status check_rf(const pyrh_lte_batch* b, const pyrh_lte_config* cfg, int nl
 
 pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nline,
                       const pyrh_lte_config* cfg, int mode, const void* obs, const void* weights,
-                      void* stokes_out, void* rf, void* chi2, void* grad, cudaStream_t st) {
+                      void* stokes_out, void* rf, void* chi2, void* grad, void* rf_gf,
+                      void* grad_gf, cudaStream_t st) {
   const int block = cfg->block_lambda > 0 ? cfg->block_lambda : 128;
   pyrh::RfArgs ra;
   ra.lte = make_args(b, d_lines, nline, cfg, stokes_out, block);
@@ -176,6 +177,8 @@ pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nli
   ra.rf = rf;
   ra.chi2 = chi2;
   ra.grad = grad;
+  ra.rf_gf = rf_gf;
+  ra.grad_gf = grad_gf;
   const size_t smem = pyrh::rf_smem_bytes(cfg->precision, nline, ra.lte.maxd);
   if (smem > 200 * 1024)
     return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
@@ -245,13 +248,13 @@ pyrh_status pyrh_lte_stokes(const pyrh_lte_batch* batch, const pyrh_line* lines,
 
 pyrh_status pyrh_lte_rf(const pyrh_lte_batch* batch, const pyrh_line* lines, int32_t nline,
                         const pyrh_lte_config* cfg, void* stokes_out, void* rf_out,
-                        void* stream) {
+                        void* rf_loggf_out, void* stream) {
   g_last_launches = 0;
   pyrh_status s = check_rf(batch, cfg, nline, lines);
   if (s != PYRH_OK) return s;
   if (!stokes_out || !rf_out) return fail(PYRH_ERR_ARG, "stokes_out or rf_out is NULL");
   s = launch_rf(batch, lines, nline, cfg, 0, nullptr, nullptr, stokes_out, rf_out, nullptr,
-                nullptr, (cudaStream_t)stream);
+                nullptr, rf_loggf_out, nullptr, (cudaStream_t)stream);
   if (s == PYRH_OK) g_last_launches = 1;
   return s;
 }
@@ -259,7 +262,7 @@ pyrh_status pyrh_lte_rf(const pyrh_lte_batch* batch, const pyrh_line* lines, int
 pyrh_status pyrh_lte_chi2_grad(const pyrh_lte_batch* batch, const pyrh_line* lines,
                                int32_t nline, const pyrh_lte_config* cfg, const void* obs,
                                const void* weights, void* stokes_out, void* chi2_out,
-                               void* grad_out, void* stream) {
+                               void* grad_out, void* grad_loggf_out, void* stream) {
   g_last_launches = 0;
   pyrh_status s = check_rf(batch, cfg, nline, lines);
   if (s != PYRH_OK) return s;
@@ -269,8 +272,9 @@ pyrh_status pyrh_lte_chi2_grad(const pyrh_lte_batch* batch, const pyrh_line* lin
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(cudaMemsetAsync(chi2_out, 0, real * batch->natm, st));
   CUDA_TRY(cudaMemsetAsync(grad_out, 0, real * PYRH_RF_NPARAM * batch->total_depth, st));
+  if (grad_loggf_out) CUDA_TRY(cudaMemsetAsync(grad_loggf_out, 0, real * batch->natm * nline, st));
   s = launch_rf(batch, lines, nline, cfg, 1, obs, weights, stokes_out, nullptr, chi2_out, grad_out,
-                st);
+                nullptr, grad_loggf_out, st);
   if (s == PYRH_OK) g_last_launches = 1;
   return s;
 }
@@ -278,7 +282,7 @@ pyrh_status pyrh_lte_chi2_grad(const pyrh_lte_batch* batch, const pyrh_line* lin
 pyrh_status pyrh_lte_stokes_vjp(const pyrh_lte_batch* batch, const pyrh_line* lines,
                                 int32_t nline, const pyrh_lte_config* cfg,
                                 const void* dL_dstokes, void* stokes_out, void* grad_out,
-                                void* stream) {
+                                void* grad_loggf_out, void* stream) {
   g_last_launches = 0;
   pyrh_status s = check_rf(batch, cfg, nline, lines);
   if (s != PYRH_OK) return s;
@@ -287,8 +291,9 @@ pyrh_status pyrh_lte_stokes_vjp(const pyrh_lte_batch* batch, const pyrh_line* li
   const size_t real = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
   cudaStream_t st = (cudaStream_t)stream;
   CUDA_TRY(cudaMemsetAsync(grad_out, 0, real * PYRH_RF_NPARAM * batch->total_depth, st));
+  if (grad_loggf_out) CUDA_TRY(cudaMemsetAsync(grad_loggf_out, 0, real * batch->natm * nline, st));
   s = launch_rf(batch, lines, nline, cfg, 2, nullptr, dL_dstokes, stokes_out, nullptr, nullptr,
-                grad_out, st);
+                grad_out, nullptr, grad_loggf_out, st);
   if (s == PYRH_OK) g_last_launches = 1;
   return s;
 }

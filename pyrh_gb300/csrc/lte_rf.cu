@@ -52,6 +52,7 @@ struct RfSmem {
   double* lam0;       // [nline]
   R* grad;            // [kNX][maxd] (chi^2 mode)
   R* chi2;            // [1]
+  R* gfs;             // [nline] log gf gradient of the block (modes 1-2)
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -77,6 +78,7 @@ __host__ __device__ size_t rf_smem_t(int nline, int maxd, RfSmem<R>* s, unsigned
   p = take(sizeof(double) * nline);              if (s) s->lam0 = reinterpret_cast<double*>(p);
   p = take(sizeof(R) * kNX * maxd);              if (s) s->grad = reinterpret_cast<R*>(p);
   p = take(sizeof(R) * 4);                       if (s) s->chi2 = reinterpret_cast<R*>(p);
+  p = take(sizeof(R) * (nline > 0 ? nline : 1)); if (s) s->gfs = reinterpret_cast<R*>(p);
   return off;
 }
 
@@ -91,6 +93,18 @@ struct Local {
   const R* eta_c;
 };
 
+// Sum of every thread's per-line log gf gradient over the warp (shuffles)
+// and the block (one shared atomic per warp and line).
+template <typename R>
+__device__ void gf_block_sum(const R* gfacc, int nline, R* gfs) {
+  for (int l = 0; l < nline; ++l) {
+    R v = gfacc[l];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31u) == 0) atomicAdd(&gfs[l], v);
+  }
+}
+
 template <typename R, int MODE>
 struct Emit {
   const Local<R>* loc;
@@ -99,6 +113,7 @@ struct Emit {
   int nd, nl, la;
   bool act;          // this lane holds a wavelength (writes and seeds)
   R* rf;             // mode 0: rf_out + 24 * cont_off + la
+  R* gf;             // per-thread log gf accumulators [NS][PYRH_MAX_LINES] or nullptr
   const Tape<R>* tp;
   __device__ void operator()(int k, const R* qb, const R* bpl) const {
     constexpr int NS = MODE == 0 ? 4 : 1;
@@ -110,7 +125,7 @@ struct Emit {
       for (int x = 0; x < kNX; ++x) g[s][x] = R(0);
     local_q_vjp<R, NS>(loc->nline, sm.ld + k, loc->maxd, sm.geo[k], loc->dlam, loc->inwin,
                        sm.ncomp, sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS, tp->q[k], qb,
-                       g);
+                       g, gf);
     const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lam)) : R(0);
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
@@ -181,6 +196,8 @@ lte_rf_kernel(RfArgs ra) {
         for (int x = 0; x < kNX; ++x) sm.grad[x * args.maxd + k] = R(0);
     }
     if (MODE == 1 && threadIdx.x == 0) sm.chi2[0] = R(0);
+    if (MODE != 0)
+      for (int l = threadIdx.x; l < nline; l += BL) sm.gfs[l] = R(0);
     for (int i = threadIdx.x; i < nline * nd; i += BL) {
       const int l = i / nd, k = i % nd;
       const int64_t d = doff + k;
@@ -235,9 +252,15 @@ lte_rf_kernel(RfArgs ra) {
 #pragma unroll
         for (int s = 0; s < 4; ++s) out[(int64_t)s * nl + la] = st[s];
 
+      constexpr int NSG = MODE == 0 ? 4 : 1;
+      const bool want_gf = MODE == 0 ? ra.rf_gf != nullptr : ra.grad_gf != nullptr;
+      R gfacc[NSG * PYRH_MAX_LINES];
+      if (want_gf)
+        for (int e = 0; e < NSG * PYRH_MAX_LINES; ++e) gfacc[e] = R(0);
       Emit<R, MODE> em;
       em.loc = &loc;
       em.tp = &tp;
+      em.gf = want_gf ? gfacc : nullptr;
       em.T = args.T + doff;
       em.lam = lam;
       em.nd = nd;
@@ -248,6 +271,12 @@ lte_rf_kernel(RfArgs ra) {
         em.rf = static_cast<R*>(ra.rf) + 24 * args.cont_off[p] + la;
         const R seed[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
         delo_reverse_stream<R, 4>(tp, sm.ds, nd, B0, B1, seed, em);
+        if (want_gf && act) {
+          R* o = static_cast<R*>(ra.rf_gf) + (int64_t)4 * nline * loff + la;
+          for (int l = 0; l < nline; ++l)
+            for (int s = 0; s < 4; ++s)
+              o[(int64_t)(l * 4 + s) * nl] = gfacc[s * PYRH_MAX_LINES + l];
+        }
       } else if (MODE == 2) {
         em.rf = nullptr;
         const R* dL = static_cast<const R*>(ra.weights) + 4 * loff;
@@ -255,6 +284,7 @@ lte_rf_kernel(RfArgs ra) {
 #pragma unroll
         for (int s = 0; s < 4; ++s) seed[0][s] = act ? dL[(int64_t)s * nl + la] : R(0);
         delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
+        if (want_gf) gf_block_sum(gfacc, nline, sm.gfs);
       } else {
         em.rf = nullptr;
         const R* obs = static_cast<const R*>(ra.obs) + 4 * loff;
@@ -272,6 +302,7 @@ lte_rf_kernel(RfArgs ra) {
         for (int o = 16; o > 0; o >>= 1) c2 += __shfl_xor_sync(0xffffffffu, c2, o);
         if ((threadIdx.x & 31u) == 0) atomicAdd(sm.chi2, c2);
         delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
+        if (want_gf) gf_block_sum(gfacc, nline, sm.gfs);
       }
     }
     if (MODE != 0) {
@@ -282,6 +313,9 @@ lte_rf_kernel(RfArgs ra) {
         atomicAdd(&grad[(int64_t)x * args.total_depth + doff + k], sm.grad[x * args.maxd + k]);
       }
       if (MODE == 1 && threadIdx.x == 0) atomicAdd(static_cast<R*>(ra.chi2) + p, sm.chi2[0]);
+      if (ra.grad_gf)
+        for (int l = threadIdx.x; l < nline; l += BL)
+          atomicAdd(static_cast<R*>(ra.grad_gf) + (int64_t)p * nline + l, sm.gfs[l]);
     }
   }
 }

@@ -353,11 +353,15 @@ PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, int ld_stride, const
 // and the field geometry, and only those are multiplied by their
 // derivatives with respect to the parameters (the .d parts of LineDepth and
 // GeoD).  q holds the forward values of this depth (the tape).
+// With gf != nullptr, also accumulates gf[s * PYRH_MAX_LINES + l] += dL_s /
+// d log10(gf_l) of this depth: the line's opacity and emissivity are both
+// proportional to its gf (kurucz.c:638-680), so the derivative is
+// ln 10 (chi_l-bar chi_l + eta_l-bar eta_l).
 template <typename R, int NS>
 PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
                          const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
                          const R* cweight, const int* cq, int maxcomp, const R q[8],
-                         const R* qb, R out[NS][kNX]) {
+                         const R* qb, R out[NS][kNX], R* gf = nullptr) {
   const R ichi = fdiv(R(1), q[0]);
   R eb[NS][4], cb[NS][4];
   R gb[NS][4];   // adjoints of s2g, gQ, gU, gV
@@ -437,6 +441,10 @@ PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const
       for (int x = 0; x < kNX; ++x)
         out[s][x] += ab[s] * L.adamp.d[x] + vb[s] * (dlam[l] * L.inv_vb.d[x] + L.vshift.d[x]) +
                      vBb[s] * L.vB.d[x] + chilb[s] * L.chil.d[x] + etalb[s] * L.etal.d[x];
+    if (gf)
+      for (int s = 0; s < NS; ++s)
+        gf[s * PYRH_MAX_LINES + l] +=
+            R(2.302585092994045684) * (chilb[s] * L.chil.v + etalb[s] * L.etal.v);
   }
   for (int s = 0; s < NS; ++s)
     for (int x = 0; x < kNX; ++x)

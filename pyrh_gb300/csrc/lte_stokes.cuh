@@ -24,12 +24,15 @@ struct LteArgs {
 
 // Response-function / gradient launch (lte_rf.cu).  mode 0 writes rf;
 // mode 1 accumulates chi2 and grad (zeroed by the caller) with obs and
-// weights; mode 2 accumulates grad with dL/dS passed in `weights`.
+// weights; mode 2 accumulates grad with dL/dS passed in `weights`.  The
+// log gf outputs are written or accumulated (zeroed by the caller) when set.
 struct RfArgs {
   LteArgs lte;
   int mode;
   const void *obs, *weights;
   void *rf, *chi2, *grad;
+  void *rf_gf;    // mode 0, optional: dS/dlog10(gf) [nline][4][lambda] per atmosphere
+  void *grad_gf;  // modes 1-2, optional: dL/dlog10(gf) [natm][nline]
 };
 
 size_t rf_smem_bytes(int precision, int nline, int maxd);

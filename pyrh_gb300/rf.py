@@ -30,11 +30,11 @@ def _lib():
     if _bound is not lib:
         B, P, I32, V = C.POINTER(L.PyrhLteBatch), C.POINTER(L.PyrhLteConfig), C.c_int32, C.c_void_p
         lib.pyrh_lte_rf.restype = C.c_int
-        lib.pyrh_lte_rf.argtypes = [B, V, I32, P, V, V, V]
+        lib.pyrh_lte_rf.argtypes = [B, V, I32, P, V, V, V, V]
         lib.pyrh_lte_chi2_grad.restype = C.c_int
-        lib.pyrh_lte_chi2_grad.argtypes = [B, V, I32, P, V, V, V, V, V, V]
+        lib.pyrh_lte_chi2_grad.argtypes = [B, V, I32, P, V, V, V, V, V, V, V]
         lib.pyrh_lte_stokes_vjp.restype = C.c_int
-        lib.pyrh_lte_stokes_vjp.argtypes = [B, V, I32, P, V, V, V, V]
+        lib.pyrh_lte_stokes_vjp.argtypes = [B, V, I32, P, V, V, V, V, V]
         _bound = lib
     return lib
 
@@ -51,14 +51,28 @@ def rf_size(pk: Packed) -> int:
     return 4 * NPARAM * cont
 
 
-def response_functions(dev: DeviceBatch, cfg: L.PyrhLteConfig, stream_ptr: int = 0):
-    """Runs pyrh_lte_rf; returns the flat RF tensor (layout of the header)
-    and leaves the emergent Stokes vectors in dev.out."""
+def response_functions(dev: DeviceBatch, cfg: L.PyrhLteConfig, stream_ptr: int = 0,
+                       loggf: bool = False):
+    """Runs pyrh_lte_rf; returns the flat RF tensor (layout of the header),
+    with loggf=True also the flat log gf RFs ([line][stokes][lambda] per
+    atmosphere), and leaves the emergent Stokes vectors in dev.out."""
     import torch
     rf = torch.empty(rf_size(dev.pk), dtype=_real(dev), device=dev.out.device)
+    gf = (torch.empty(4 * dev.nline * dev.pk.nlam_total, dtype=_real(dev), device=dev.out.device)
+          if loggf else None)
     L.check(_lib().pyrh_lte_rf(C.byref(dev.struct), dev.lines_t.data_ptr(), dev.nline,
-                               C.byref(cfg), dev.out.data_ptr(), rf.data_ptr(), stream_ptr))
-    return rf
+                               C.byref(cfg), dev.out.data_ptr(), rf.data_ptr(),
+                               gf.data_ptr() if loggf else None, stream_ptr))
+    return (rf, gf) if loggf else rf
+
+
+def split_loggf_rf(pk: Packed, nline: int, gf) -> list:
+    """Per-atmosphere [nline, 4, nlam] views of the flat log gf RFs."""
+    out = []
+    for p in range(pk.natm):
+        o, nl = int(pk.arrays["lam_off"][p]), int(pk.arrays["nlam"][p])
+        out.append(gf[4 * nline * o: 4 * nline * (o + nl)].reshape(nline, 4, nl))
+    return out
 
 
 def split_rf(pk: Packed, rf) -> list:
@@ -71,32 +85,41 @@ def split_rf(pk: Packed, rf) -> list:
     return out
 
 
-def chi2_grad(dev: DeviceBatch, cfg: L.PyrhLteConfig, obs, weights, stream_ptr: int = 0):
+def chi2_grad(dev: DeviceBatch, cfg: L.PyrhLteConfig, obs, weights, stream_ptr: int = 0,
+              loggf: bool = False):
     """chi2[p] = sum w (S - obs)^2 and its gradient [6, total_depth] in one
-    forward + adjoint pass (obs, weights: flat tensors laid out like dev.out)."""
+    forward + adjoint pass (obs, weights: flat tensors laid out like dev.out);
+    with loggf=True also d chi2 / d log10(gf) [natm, nline]."""
     import torch
     real = _real(dev)
     obs = obs.to(device=dev.out.device, dtype=real).contiguous()
     weights = weights.to(device=dev.out.device, dtype=real).contiguous()
     chi2 = torch.empty(dev.pk.natm, dtype=real, device=dev.out.device)
     grad = torch.empty(NPARAM * dev.pk.total_depth, dtype=real, device=dev.out.device)
+    gf = torch.empty(dev.pk.natm * dev.nline, dtype=real, device=dev.out.device) if loggf else None
     L.check(_lib().pyrh_lte_chi2_grad(C.byref(dev.struct), dev.lines_t.data_ptr(), dev.nline,
                                       C.byref(cfg), obs.data_ptr(), weights.data_ptr(),
                                       dev.out.data_ptr(), chi2.data_ptr(), grad.data_ptr(),
-                                      stream_ptr))
-    return chi2, grad.view(NPARAM, dev.pk.total_depth)
+                                      gf.data_ptr() if loggf else None, stream_ptr))
+    g = grad.view(NPARAM, dev.pk.total_depth)
+    return (chi2, g, gf.view(dev.pk.natm, dev.nline)) if loggf else (chi2, g)
 
 
-def vjp(dev: DeviceBatch, cfg: L.PyrhLteConfig, dL_dstokes, stream_ptr: int = 0):
-    """sum over wavelengths and Stokes of dL/dS * dS/dx: [6, total_depth]."""
+def vjp(dev: DeviceBatch, cfg: L.PyrhLteConfig, dL_dstokes, stream_ptr: int = 0,
+        loggf: bool = False):
+    """sum over wavelengths and Stokes of dL/dS * dS/dx: [6, total_depth]
+    (and with loggf=True the same for log10(gf) of every line: [natm, nline])."""
     import torch
     real = _real(dev)
     g = dL_dstokes.to(device=dev.out.device, dtype=real).contiguous()
     grad = torch.empty(NPARAM * dev.pk.total_depth, dtype=real, device=dev.out.device)
+    gf = torch.empty(dev.pk.natm * dev.nline, dtype=real, device=dev.out.device) if loggf else None
     L.check(_lib().pyrh_lte_stokes_vjp(C.byref(dev.struct), dev.lines_t.data_ptr(), dev.nline,
                                        C.byref(cfg), g.data_ptr(), dev.out.data_ptr(),
-                                       grad.data_ptr(), stream_ptr))
-    return grad.view(NPARAM, dev.pk.total_depth)
+                                       grad.data_ptr(), gf.data_ptr() if loggf else None,
+                                       stream_ptr))
+    out = grad.view(NPARAM, dev.pk.total_depth)
+    return (out, gf.view(dev.pk.natm, dev.nline)) if loggf else out
 
 
 def set_params(dev: DeviceBatch, params) -> None:

@@ -52,11 +52,11 @@ def rf_harness(tmp_path_factory):
     return C.CDLL(out)
 
 
-def rf_eval(lib, fx, sel, single=False, jac=False):
+def rf_eval(lib, fx, sel, single=False, jac=False, loggf=False):
     """Stokes [nsel, 4] and response functions [nsel, 4, 6, ndep] of one
     atmosphere at the wavelengths fx["lam"][sel] (CPU harness, FP64 or, with
     single=True, FP32; jac=True takes the opacity derivatives in forward
-    mode)."""
+    mode); loggf=True also returns dS/dlog10(gf) [nsel, 4, nline]."""
     from pyrh_gb300 import lte
     D = C.POINTER(C.c_double)
     keep = []
@@ -71,15 +71,16 @@ def rf_eval(lib, fx, sel, single=False, jac=False):
     lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
     st = np.zeros((len(sel), 4))
     rf = np.zeros((len(sel), 4, 6, nd))
+    gf = np.zeros((len(sel), 4, max(n, 1)))
     fn = lib.rf_eval_f32 if single else (lib.rf_eval_jac if jac else lib.rf_eval)
     r = fn(nd, arr(fx["height"]), arr(fx["T"]), arr(fx["ne"]), arr(fx["nHtot"]),
                     arr(fx["np"]), arr(fx["vturb"]), arr(fx["vel"]), arr(fx["B"]),
                     arr(fx["gamma_B"]), arr(fx["chi_B"]), arr(fx["line_pops"]), n, lines,
                     len(sel), arr(lam), arr(fx["chi_c"][sel]), arr(fx["eta_c"][sel]),
                     C.c_double(float(fx["mu"])), C.c_double(float(fx["vmicro_char"])),
-                    st.ctypes.data_as(D), rf.ctypes.data_as(D))
+                    st.ctypes.data_as(D), rf.ctypes.data_as(D), gf.ctypes.data_as(D))
     assert r == 0
-    return st, rf
+    return (st, rf, gf) if loggf else (st, rf)
 
 
 def delo_wavelengths(fx) -> np.ndarray:

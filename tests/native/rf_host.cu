@@ -33,6 +33,7 @@ struct Emit {
   const int* cq;
   const R *chi_c, *eta_c;   // [depth] at this wavelength
   const Tape<R>* tp;
+  R* gf;                    // [4][PYRH_MAX_LINES] log gf accumulators
   void operator()(int k, const R* qb, const R* bpl) const {
     R g[4][kNX];
     if (JAC) {
@@ -48,7 +49,7 @@ struct Emit {
       for (int s = 0; s < 4; ++s)
         for (int x = 0; x < kNX; ++x) g[s][x] = 0;
       local_q_vjp<R, 4>(nline, ld + k, PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
-                        PYRH_MAX_COMPONENTS, tp->q[k], qb, g);
+                        PYRH_MAX_COMPONENTS, tp->q[k], qb, g, gf);
     }
     const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lm)) : R(0);
     for (int s = 0; s < 4; ++s)
@@ -58,14 +59,15 @@ struct Emit {
 };
 
 // atmosphere arrays SI [nd]; line_pops [nline][2][nd]; lines: pyrh_line[nline];
-// chi_c, eta_c [nlam][nd]; out: stokes [nlam][4], rf [nlam][4][6][nd]
+// chi_c, eta_c [nlam][nd]; out: stokes [nlam][4], rf [nlam][4][6][nd],
+// rf_gf [nlam][4][nline] (dS/dlog10 gf; the forward-mode variant leaves it 0)
 template <typename R, bool JAC>
 static int rf_eval_t(int nd, const double* height, const double* T, const double* ne,
                      const double* nHtot, const double* np, const double* vturb,
                      const double* vel, const double* B, const double* gam, const double* chb,
                      const double* line_pops, int nline, const pyrh_line* lines, int nlam,
                      const double* lam, const double* chi_c, const double* eta_c, double mu,
-                     double vmicro_char, double* stokes, double* rf) {
+                     double vmicro_char, double* stokes, double* rf, double* rf_gf) {
   if (nd < 3 || nd > PYRH_MAX_DEPTH_RF || nline > PYRH_MAX_LINES) return -1;
   static LineDepth<R> ld[PYRH_MAX_LINES][PYRH_MAX_DEPTH_RF];
   static GeoD<R> geo[PYRH_MAX_DEPTH_RF];
@@ -107,6 +109,8 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     }
     double* rfl = rf + (int64_t)la * 4 * kNX * nd;
     memset(rfl, 0, sizeof(double) * 4 * kNX * nd);
+    double* gfl = rf_gf + (int64_t)la * 4 * nline;
+    for (int e = 0; e < 4 * nline; ++e) gfl[e] = 0.0;
     if (!pol) { for (int s = 0; s < 4; ++s) stokes[la * 4 + s] = 0.0; continue; }
     for (int k = 0; k < nd; ++k) {
       cc[k] = R(chi_c[(int64_t)la * nd + k]);
@@ -121,9 +125,13 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     delo_forward<R>(tape, ds, nd, B0, B1, out, qop);
     for (int s = 0; s < 4; ++s) stokes[la * 4 + s] = double(out[s]);
     const R seed[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+    R gfa[4 * PYRH_MAX_LINES];
+    for (int e = 0; e < 4 * PYRH_MAX_LINES; ++e) gfa[e] = R(0);
     Emit<R, JAC> emit{nd, T, lm, rfl, nline, &ld[0][0], geo, dlam, inwin, ncomp, cs, cw, cq, cc, ec,
-                      &tape};
+                      &tape, gfa};
     delo_reverse_stream<R, 4>(tape, ds, nd, B0, B1, seed, emit);
+    for (int s = 0; s < 4; ++s)
+      for (int l = 0; l < nline; ++l) gfl[s * nline + l] = double(gfa[s * PYRH_MAX_LINES + l]);
   }
   return 0;
 }
@@ -133,10 +141,11 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
       const double *np, const double *vturb, const double *vel, const double *B,              \
       const double *gam, const double *chb, const double *line_pops, int nline,               \
       const pyrh_line *lines, int nlam, const double *lam, const double *chi_c,               \
-      const double *eta_c, double mu, double vmicro_char, double *stokes, double *rf
+      const double *eta_c, double mu, double vmicro_char, double *stokes, double *rf,        \
+      double *rf_gf
 #define RF_PASS                                                                              \
   nd, height, T, ne, nHtot, np, vturb, vel, B, gam, chb, line_pops, nline, lines, nlam, lam,  \
-      chi_c, eta_c, mu, vmicro_char, stokes, rf
+      chi_c, eta_c, mu, vmicro_char, stokes, rf, rf_gf
 
 extern "C" int rf_eval(RF_ARGS) { return rf_eval_t<double, false>(RF_PASS); }
 extern "C" int rf_eval_f32(RF_ARGS) { return rf_eval_t<float, false>(RF_PASS); }

@@ -253,3 +253,34 @@ def test_rf_matches_gpu_finite_differences(golden):
                 worst = max(worst, np.min(errs[p], axis=0).max() / scale)
     RF.set_params(dev, base)
     assert worst < 1e-4, worst
+
+
+@pytest.mark.parametrize("precision,tol", [(FP64, 1e-8), (FP32, 1e-3)])
+def test_loggf_rf_matches_cpu_adjoint(rf_harness, golden, precision, tol):
+    """dS/dlog10(gf) per line from pyrh_lte_rf against the CPU adjoint, and
+    the chi^2 and VJP log gf gradients against their contraction."""
+    import torch
+    fx = golden("lte_c0")
+    dev, cfg = device_batch([fx], precision)
+    rf, gf = RF.response_functions(dev, cfg, loggf=True)
+    torch.cuda.synchronize()
+    nline = dev.nline
+    gfs = RF.split_loggf_rf(dev.pk, nline, gf.cpu().numpy().astype(np.float64))[0]
+    win = delo_wavelengths(fx)
+    _, _, gf_h = rf_eval(rf_harness, fx, win, loggf=True)
+    ref = gf_h.transpose(2, 1, 0)                       # [nline, 4, nsel]
+    assert np.abs(gfs[..., win] - ref).max() <= tol * np.abs(ref).max()
+    S = dev.out.cpu().numpy().astype(np.float64)
+    rng = np.random.default_rng(3)
+    g = rng.standard_normal(S.shape) / np.abs(S).max()
+    _, gl = RF.vjp(dev, cfg, torch.from_numpy(g), loggf=True)
+    want = np.einsum("sl,nsl->n", g.reshape(4, -1), gfs)
+    scale = np.einsum("sl,nsl->n", np.abs(g.reshape(4, -1)), np.abs(gfs))
+    assert np.all(np.abs(gl.cpu().numpy()[0] - want) <= (1e-10 if precision == FP64 else 1e-4) * scale)
+    obs = S * (1 + 1e-2 * rng.standard_normal(S.shape))
+    w = np.ones_like(S) / np.abs(S).max() ** 2
+    _, _, gc = RF.chi2_grad(dev, cfg, torch.from_numpy(obs), torch.from_numpy(w), loggf=True)
+    seed = (2 * w * (S - obs)).reshape(4, -1)
+    want = np.einsum("sl,nsl->n", seed, gfs)
+    scale = np.einsum("sl,nsl->n", np.abs(seed), np.abs(gfs))
+    assert np.all(np.abs(gc.cpu().numpy()[0] - want) <= (1e-10 if precision == FP64 else 1e-3) * scale)

@@ -120,3 +120,33 @@ def test_reverse_mode_opacity_contraction_equals_forward_mode(rf_harness, golden
     for x in range(6):
         scale = np.abs(rf_fwd[:, :, x]).max()
         assert np.abs(rf_rev[:, :, x] - rf_fwd[:, :, x]).max() <= 1e-12 * scale, PARAMS[x]
+
+
+def fd_loggf(fx, line, h, sel):
+    """Central difference in log10(gf) of one line: A_ji, B_ji and B_ij all
+    scale with gf (kurucz.c:250-330)."""
+    kw = dict(md_float=False, lam=fx["lam"][sel], chi_c=fx["chi_c"][sel],
+              eta_c=fx["eta_c"][sel])
+    out = []
+    for sgn in (1, -1):
+        f = dict(fx)
+        lc = fx["line_const"].copy()
+        lc[line, 7:10] *= 10.0 ** (sgn * h)
+        f["line_const"] = lc
+        out.append(O.lte_synth(f, **kw))
+    return (out[0] - out[1]) / (2 * h)
+
+
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge"])
+def test_loggf_response_matches_finite_differences(rf_harness, golden, name):
+    """dS/dlog10(gf) of each line (the atomic-parameter response functions of
+    compute1d(..., get_atomic_rfs=True), here for all four Stokes parameters)
+    against central differences of the oracle's synthesis."""
+    fx = golden(name)
+    win = delo_wavelengths(fx)
+    _, _, gf = rf_eval(rf_harness, fx, win, loggf=True)
+    for line in range(fx["line_const"].shape[0]):
+        ad = gf[:, :, line].T                        # [4, nsel]
+        scale = np.abs(ad).max()
+        errs = [np.abs(ad - fd_loggf(fx, line, h, win)) for h in (1e-3, 1e-4, 1e-5)]
+        assert np.min(errs, axis=0).max() <= 1e-5 * scale, line
