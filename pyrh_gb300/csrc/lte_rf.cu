@@ -16,9 +16,10 @@
 //      (delo_reverse_stream), which hands over dL/dq_k as soon as depth k is
 //      final;
 //   3. at each handed-over depth, carries dL/dq_k backwards through the
-//      opacity of that depth (local_q_vjp: through the line sums and Zeeman
-//      components to the per-line primitives, whose derivatives with respect
-//      to the parameters are the dual parts in shared memory) and writes
+//      opacity of that depth (local_q_vjp: through the line sums to the
+//      per-line primitives, whose derivatives with respect to the parameters
+//      are the dual parts in shared memory; the Zeeman profile sums and their
+//      derivatives were evaluated once by the forward sweep and taped) and writes
 //      dL/dx_k: for response functions the four
 //      Stokes seeds give RF[s][x][k] (written wavelength-fastest, coalesced);
 //      for the chi^2 gradient the single seed 2 w (S - obs), and for a
@@ -125,7 +126,7 @@ struct Emit {
       for (int x = 0; x < kNX; ++x) g[s][x] = R(0);
     local_q_vjp<R, NS>(loc->nline, sm.ld + k, loc->maxd, sm.geo[k], loc->dlam, loc->inwin,
                        sm.ncomp, sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS, tp->q[k], qb,
-                       g, gf);
+                       g, gf, tp->z[k]);
     const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lam)) : R(0);
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
@@ -239,9 +240,9 @@ lte_rf_kernel(RfArgs ra) {
 
       Tape<R> tp;
       auto qop = [&](int k, R* q) {
-        local_q<R>(nline, sm.ld + k, args.maxd, sm.geo[k], loc.dlam, loc.inwin, sm.ncomp,
-                   sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS,
-                   loc.chi_c[(int64_t)k * nl], loc.eta_c[(int64_t)k * nl], q);
+        local_q<R, true>(nline, sm.ld + k, args.maxd, sm.geo[k], loc.dlam, loc.inwin, sm.ncomp,
+                         sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS,
+                         loc.chi_c[(int64_t)k * nl], loc.eta_c[(int64_t)k * nl], q, tp.z[k]);
       };
       const double B0 = planck(args.T[doff + nd - 2], lam);
       const double B1 = planck(args.T[doff + nd - 1], lam);

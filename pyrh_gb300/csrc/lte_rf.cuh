@@ -344,6 +344,91 @@ PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, int ld_stride, const
   }
 }
 
+// Lines whose Zeeman profile sums are kept per depth (on the tape) for the
+// reverse sweep: the first kZLines lines inside their windows at a
+// wavelength, in list order.  Per line kZ values: the three profile sums
+// ph_q = sum_{c in q} w_c H(x_c) (q = sigma-, pi, sigma+) and their
+// derivatives with respect to the damping a, the reduced frequency x and the
+// Zeeman splitting v_B:  sum w Re W',  sum w Im W',  -sum w sh Im W'
+// (W' = dW/dt, t = a - i x; dH/da = Re W', dH/dx = Im W').  Gaussian lines
+// keep phi and dphi/dx in the first two slots.
+constexpr int kZLines = 2;
+constexpr int kZ = 12;
+
+// q of one depth (the forward sweep): the same sums as local_q_jac on the
+// value parts, with the single-precision fast Humlicek where R is float.
+// With SUMS, the Humlicek derivative is evaluated as well and the profile
+// sums of the first kZLines in-window lines are stored in z.
+template <typename R, bool SUMS = false>
+PYRH_HD void local_q(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
+                     const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
+                     const R* cweight, const int* cq, int maxcomp, R chi_c, R eta_c, R q[8],
+                     R (*z)[kZ] = nullptr) {
+  R cI = 0, cQ = 0, cU = 0, cV = 0, eI = 0, eQ = 0, eU = 0, eV = 0;
+  int slot = 0;
+  for (int l = 0; l < nline; ++l) {
+    if (!((inwin >> l) & 1u)) continue;
+    const LineDepth<R>& L = ld[l * ld_stride];
+    const R v = dlam[l] * L.inv_vb.v + L.vshift.v;
+    const bool keep = SUMS && slot < kZLines;
+    if (L.gauss) {
+      const R phi = (fabs(v) <= R(kMAX_GAUSS_DOPPLER)) ? dev_exp(-v * v) : R(0);
+      cI += L.chil.v * phi;
+      eI += L.etal.v * phi;
+      if (keep) {
+        z[slot][0] = phi;
+        z[slot][1] = R(-2) * v * phi;
+      }
+      slot += SUMS ? 1 : 0;
+      continue;
+    }
+    R ph[3] = {0, 0, 0}, pa[3] = {0, 0, 0}, px[3] = {0, 0, 0}, pv[3] = {0, 0, 0};
+    for (int c = 0; c < ncomp[l]; ++c) {
+      const R sh = cshift[l * maxcomp + c], w = cweight[l * maxcomp + c];
+      const int qi0 = cq[l * maxcomp + c] + 1;
+      const int qi = qi0 < 0 ? 0 : (qi0 > 2 ? 2 : qi0);
+      if (SUMS) {
+        Cx<R> W, dW;
+        humlicek_d<R>(L.adamp.v, v - sh * L.vB.v, W, dW);
+        ph[qi] += w * W.r;
+        pa[qi] += w * dW.r;
+        px[qi] += w * dW.i;
+        pv[qi] -= w * sh * dW.i;
+      } else {
+        R H, F;
+        humlicek<R>(L.adamp.v, v - sh * L.vB.v, H, F);
+        ph[qi] += w * H;
+      }
+    }
+    if (keep)
+      for (int g = 0; g < 3; ++g) {
+        z[slot][g] = ph[g];
+        z[slot][3 + g] = pa[g];
+        z[slot][6 + g] = px[g];
+        z[slot][9 + g] = pv[g];
+      }
+    slot += SUMS ? 1 : 0;
+    const R sig = ph[2] + ph[0];
+    const R del = R(0.5) * ph[1] - R(0.25) * sig;
+    const R phiI = del * geo.s2g.v + R(0.5) * sig;
+    const R phiQ = del * geo.gQ.v, phiU = del * geo.gU.v, phiV = R(0.5) * ((ph[2] - ph[0]) * geo.gV.v);
+    cI += L.chil.v * phiI; eI += L.etal.v * phiI;
+    cQ += L.chil.v * phiQ; eQ += L.etal.v * phiQ;
+    cU += L.chil.v * phiU; eU += L.etal.v * phiU;
+    cV += L.chil.v * phiV; eV += L.etal.v * phiV;
+  }
+  const R chi = chi_c + cI;
+  const R rchi = fdiv(R(1), chi);
+  q[0] = chi;
+  q[1] = (eta_c + eI) * rchi;
+  q[2] = eQ * rchi;
+  q[3] = eU * rchi;
+  q[4] = eV * rchi;
+  q[5] = cQ * rchi;
+  q[6] = cU * rchi;
+  q[7] = cV * rchi;
+}
+
 // Reverse-mode contraction of the local opacity: for NS adjoint vectors
 // qb[s][8] = dL_s/dq (q as in local_q_jac), accumulates
 // out[s][x] += sum_n qb[s][n] dq_n/dx for the six parameters of this depth.
@@ -357,11 +442,16 @@ PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, int ld_stride, const
 // d log10(gf_l) of this depth: the line's opacity and emissivity are both
 // proportional to its gf (kurucz.c:638-680), so the derivative is
 // ln 10 (chi_l-bar chi_l + eta_l-bar eta_l).
+// With z (the profile sums local_q<R, true> stored for this depth), the
+// first kZLines in-window lines take their profile sums and derivatives from
+// z instead of re-evaluating the Zeeman components.
 template <typename R, int NS>
 PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
                          const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
                          const R* cweight, const int* cq, int maxcomp, const R q[8],
-                         const R* qb, R out[NS][kNX], R* gf = nullptr) {
+                         const R* qb, R out[NS][kNX], R* gf = nullptr,
+                         const R (*z)[kZ] = nullptr) {
+  int slot = 0;
   const R ichi = fdiv(R(1), q[0]);
   R eb[NS][4], cb[NS][4];
   R gb[NS][4];   // adjoints of s2g, gQ, gU, gV
@@ -378,14 +468,17 @@ PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const
     if (!((inwin >> l) & 1u)) continue;
     const LineDepth<R>& L = ld[l * ld_stride];
     const R v = dlam[l] * L.inv_vb.v + L.vshift.v;
+    const R* zl = (z && slot < kZLines) ? z[slot] : nullptr;
+    ++slot;
     R ab[NS], vb[NS], vBb[NS], chilb[NS], etalb[NS];
     if (L.gauss) {
-      const R phi = (fabs(v) <= R(kMAX_GAUSS_DOPPLER)) ? dev_exp(-v * v) : R(0);
+      const R phi = zl ? zl[0] : ((fabs(v) <= R(kMAX_GAUSS_DOPPLER)) ? dev_exp(-v * v) : R(0));
+      const R dphi = zl ? zl[1] : R(-2) * v * phi;
       for (int s = 0; s < NS; ++s) {
         const R phib = cb[s][0] * L.chil.v + eb[s][0] * L.etal.v;
         chilb[s] = cb[s][0] * phi;
         etalb[s] = eb[s][0] * phi;
-        vb[s] = phib * (R(-2) * v * phi);
+        vb[s] = phib * dphi;
         ab[s] = vBb[s] = R(0);
       }
     } else {
@@ -403,19 +496,30 @@ PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const
         ab[s] = vb[s] = vBb[s] = R(0);
       }
       R ph[3] = {0, 0, 0};
-      for (int c = 0; c < ncomp[l]; ++c) {
-        const R sh = cshift[l * maxcomp + c], w = cweight[l * maxcomp + c];
-        Cx<R> W, dW;
-        humlicek_d<R>(L.adamp.v, v - sh * L.vB.v, W, dW);
-        const int qi0 = cq[l * maxcomp + c] + 1;
-        const int qi = qi0 < 0 ? 0 : (qi0 > 2 ? 2 : qi0);
-        ph[qi] += w * W.r;
-        for (int s = 0; s < NS; ++s) {
-          const R hb = w * phb[s][qi];
-          const R xb = hb * dW.i;   // dH/dx = Im W' (t = a - i x)
-          ab[s] += hb * dW.r;       // dH/da = Re W'
-          vb[s] += xb;
-          vBb[s] -= sh * xb;
+      if (zl) {
+        for (int g = 0; g < 3; ++g) {
+          ph[g] = zl[g];
+          for (int s = 0; s < NS; ++s) {
+            ab[s] += phb[s][g] * zl[3 + g];
+            vb[s] += phb[s][g] * zl[6 + g];
+            vBb[s] += phb[s][g] * zl[9 + g];
+          }
+        }
+      } else {
+        for (int c = 0; c < ncomp[l]; ++c) {
+          const R sh = cshift[l * maxcomp + c], w = cweight[l * maxcomp + c];
+          Cx<R> W, dW;
+          humlicek_d<R>(L.adamp.v, v - sh * L.vB.v, W, dW);
+          const int qi0 = cq[l * maxcomp + c] + 1;
+          const int qi = qi0 < 0 ? 0 : (qi0 > 2 ? 2 : qi0);
+          ph[qi] += w * W.r;
+          for (int s = 0; s < NS; ++s) {
+            const R hb = w * phb[s][qi];
+            const R xb = hb * dW.i;   // dH/dx = Im W' (t = a - i x)
+            ab[s] += hb * dW.r;       // dH/da = Re W'
+            vb[s] += xb;
+            vBb[s] -= sh * xb;
+          }
         }
       }
       const R sig = ph[2] + ph[0];
@@ -450,51 +554,6 @@ PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const
     for (int x = 0; x < kNX; ++x)
       out[s][x] += gb[s][0] * geo.s2g.d[x] + gb[s][1] * geo.gQ.d[x] + gb[s][2] * geo.gU.d[x] +
                    gb[s][3] * geo.gV.d[x];
-}
-
-// Values of q only (the forward sweep): the same sums as local_q_jac on the
-// value parts, with the single-precision fast Humlicek where R is float.
-template <typename R>
-PYRH_HD void local_q(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
-                     const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
-                     const R* cweight, const int* cq, int maxcomp, R chi_c, R eta_c, R q[8]) {
-  R cI = 0, cQ = 0, cU = 0, cV = 0, eI = 0, eQ = 0, eU = 0, eV = 0;
-  for (int l = 0; l < nline; ++l) {
-    if (!((inwin >> l) & 1u)) continue;
-    const LineDepth<R>& L = ld[l * ld_stride];
-    const R v = dlam[l] * L.inv_vb.v + L.vshift.v;
-    if (L.gauss) {
-      const R phi = (fabs(v) <= R(kMAX_GAUSS_DOPPLER)) ? dev_exp(-v * v) : R(0);
-      cI += L.chil.v * phi;
-      eI += L.etal.v * phi;
-      continue;
-    }
-    R ph[3] = {0, 0, 0};
-    for (int c = 0; c < ncomp[l]; ++c) {
-      R H, F;
-      humlicek<R>(L.adamp.v, v - cshift[l * maxcomp + c] * L.vB.v, H, F);
-      const int qi = cq[l * maxcomp + c] + 1;
-      ph[qi < 0 ? 0 : (qi > 2 ? 2 : qi)] += cweight[l * maxcomp + c] * H;
-    }
-    const R sig = ph[2] + ph[0];
-    const R del = R(0.5) * ph[1] - R(0.25) * sig;
-    const R phiI = del * geo.s2g.v + R(0.5) * sig;
-    const R phiQ = del * geo.gQ.v, phiU = del * geo.gU.v, phiV = R(0.5) * ((ph[2] - ph[0]) * geo.gV.v);
-    cI += L.chil.v * phiI; eI += L.etal.v * phiI;
-    cQ += L.chil.v * phiQ; eQ += L.etal.v * phiQ;
-    cU += L.chil.v * phiU; eU += L.etal.v * phiU;
-    cV += L.chil.v * phiV; eV += L.etal.v * phiV;
-  }
-  const R chi = chi_c + cI;
-  const R rchi = fdiv(R(1), chi);
-  q[0] = chi;
-  q[1] = (eta_c + eI) * rchi;
-  q[2] = eQ * rchi;
-  q[3] = eU * rchi;
-  q[4] = eV * rchi;
-  q[5] = cQ * rchi;
-  q[6] = cU * rchi;
-  q[7] = cV * rchi;
 }
 
 // ------------------------------------------------- coefficient derivatives --
@@ -729,6 +788,7 @@ struct Tape {
   R dS0[PYRH_MAX_DEPTH_RF][4]; // dS0_k (dSu of step k-1); index nd-1 holds the initial dSu
   R dK0[PYRH_MAX_DEPTH_RF][3];
   R dchi_up0;                  // initial dchi_up
+  R z[PYRH_MAX_DEPTH_RF][kZLines][kZ];   // profile sums of local_q<R, true>
 };
 
 // Forward DELO-Bezier3 sweep from the bottom boundary to the surface

@@ -49,7 +49,7 @@ struct Emit {
       for (int s = 0; s < 4; ++s)
         for (int x = 0; x < kNX; ++x) g[s][x] = 0;
       local_q_vjp<R, 4>(nline, ld + k, PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
-                        PYRH_MAX_COMPONENTS, tp->q[k], qb, g, gf);
+                        PYRH_MAX_COMPONENTS, tp->q[k], qb, g, gf, tp->z[k]);
     }
     const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lm)) : R(0);
     for (int s = 0; s < 4; ++s)
@@ -117,8 +117,8 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
       ec[k] = R(eta_c[(int64_t)la * nd + k]);
     }
     auto qop = [&](int k, R* q) {
-      local_q<R>(nline, &ld[0][k], PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
-                 PYRH_MAX_COMPONENTS, cc[k], ec[k], q);
+      local_q<R, true>(nline, &ld[0][k], PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
+                       PYRH_MAX_COMPONENTS, cc[k], ec[k], q, tape.z[k]);
     };
     const double B0 = planck(T[nd - 2], lm), B1 = planck(T[nd - 1], lm);
     R out[4];

@@ -17,7 +17,7 @@ Tolerances are relative to the largest |RF| of each parameter:
   GPU FD (FP64) vs FP64 kernel        1e-4, per element the closest of five
                                       steps (Humlicek region jumps, FP64
                                       noise of the synthesis)
-  chi^2 gradient and VJP vs contracted RFs (FP64)   1e-10
+  chi^2 gradient and VJP vs contracted RFs (FP64)   1e-9
   FP32 VJP vs FP64                                   1e-3 per parameter
   FP32 chi^2 gradient vs FP32 VJP of its seeds       1e-4 per parameter
 """
@@ -117,7 +117,11 @@ def test_rf_ragged_batch_equals_single(golden):
 
 def test_chi2_grad_and_vjp_contract_rf(golden):
     """FP64: chi^2, its gradient and a VJP equal the contraction of the
-    response functions (the same linear map, evaluated three ways)."""
+    response functions (the same linear map, evaluated three ways), to 1e-9
+    of the sum of the magnitudes of the contracted terms: the Q and U of the
+    15-50 G atmospheres are ~v_B^2 ~ 1e-5 of their profiles, so even FP64
+    leaves them ~1e-11 relative rounding, independently in the three
+    evaluations."""
     import torch
     b = golden("lte_batch")
     atms = [batch_member(b, i) for i in range(b["T"].shape[0])]
@@ -138,8 +142,8 @@ def test_chi2_grad_and_vjp_contract_rf(golden):
         sl = slice(4 * o, 4 * o + 4 * nl)
         Sp, Op, Wp, Gp = (x[sl].reshape(4, nl) for x in (S, obs, w, g))
         assert abs(chi2[p] - (Wp * (Sp - Op) ** 2).sum()) <= 1e-10 * chi2[p]
-        assert np.all(contract_err(grad[:, d0:d0 + nd], 2 * Wp * (Sp - Op), rfs[p]) < 1e-10), p
-        assert np.all(contract_err(gv[:, d0:d0 + nd], Gp, rfs[p]) < 1e-10), p
+        assert np.all(contract_err(grad[:, d0:d0 + nd], 2 * Wp * (Sp - Op), rfs[p]) < 1e-9), p
+        assert np.all(contract_err(gv[:, d0:d0 + nd], Gp, rfs[p]) < 1e-9), p
 
 
 def test_fp32_gradients_vs_fp64(golden):
