@@ -151,7 +151,7 @@ def rf_measure(natm, local, stream, steps, warmup):
     import torch
     from pyrh_gb300 import _lib as L
     from pyrh_gb300 import lte, rf as RF, workload
-    batch = workload.synthetic_batch(natm, seed=3000 + local, dtype=np.float32)
+    batch = workload.synthetic_batch(natm, seed=3000 + local, dtype=np.float32, setup_dT=True)
     pert = workload.synthetic_batch(natm, seed=4000 + local, dtype=np.float32)
     lines, nline = lte.make_lines(batch["line_const"], batch["zeeman"], batch["zeeman_n"])
     dev = lte.DeviceBatch(lte.pack_uniform(batch, nline, L.PYRH_FP32), lines, nline,
@@ -177,12 +177,21 @@ def rf_measure(natm, local, stream, steps, warmup):
         grad_ms = _events_ms(lambda: RF.chi2_grad(dev, cfg, obs, w, sp), stream, steps)
         RF.response_functions(dev, cfg, sp)
         rf_ms = _events_ms(lambda: RF.response_functions(dev, cfg, sp), stream, 2)
+        # the same gradient with the set-up held fixed (partial T derivative)
+        held = dev.struct.setup_dT
+        dev.struct.setup_dT = None
+        RF.chi2_grad(dev, cfg, obs, w, sp)
+        fixed_ms = _events_ms(lambda: RF.chi2_grad(dev, cfg, obs, w, sp), stream, steps)
+        dev.struct.setup_dT = held
     units = natm * nl
     return {"workload": f"chi^2 gradient and response functions: {natm} atm x 71 depths x "
-                        f"{nl} lambda, FP32, targets from perturbed copies + noise 1e-3 I_c",
+                        f"{nl} lambda, FP32, targets from perturbed copies + noise 1e-3 I_c; "
+                        "the temperature derivative follows T through the set-up (continuum "
+                        "and stage densities) as the reference's finite differences do",
             "gradients_per_s": {"value": units / (grad_ms / 1e3), "unit": UNIT},
             "ms_forward": fwd_ms, "ms_chi2_gradient": grad_ms,
             "gradient_cost_vs_forward": grad_ms / fwd_ms,
+            "ms_chi2_gradient_setup_fixed": fixed_ms,
             "ms_response_functions": rf_ms,
             "rf_bytes_written": int(4 * 6 * 71 * units * 4)}
 

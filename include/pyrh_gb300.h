@@ -84,6 +84,31 @@ typedef struct {
   double  comp_strength[PYRH_MAX_COMPONENTS]; /* normalised per q */
 } pyrh_line;
 
+/* Temperature derivatives of the set-up quantities, for response functions
+   and gradients that follow the temperature through the set-up.  The
+   reference's response functions are finite differences of its whole
+   synthesis (rh/rhf1d/rf_ray.c:205-293): every perturbed temperature re-runs
+   Background() (continuum, LTE stage densities, proton density) and
+   convertScales() (the height scale from tau_500,
+   rh/rhf1d/multiatmos.c:126-138), so its temperature response includes how
+   those inputs move with T.  Given these derivatives, pyrh_lte_rf,
+   pyrh_lte_chi2_grad and pyrh_lte_stokes_vjp add the same terms.  Each
+   pointer may be NULL, which holds that input fixed.  The set-up is local in
+   depth: every derivative is with respect to the temperature of the same
+   depth, except the interval lengths, which depend on the temperatures at
+   both ends of their interval.  Device pointers, laid out like the batch
+   arrays they differentiate. */
+typedef struct {
+  const void *dchi_c;          /* d chi_c / dT: layout and type of chi_c */
+  const void *deta_c;          /* d eta_c / dT */
+  const double *dline_pops;    /* [nline][2][sum ndep]: d n_stage/dT, d ln U/dT */
+  const double *dnp;           /* [sum ndep]: d n_p / dT */
+  const double *dlen_up;       /* [sum ndep]: entry k >= 1 of an atmosphere,
+                                  d|height[k] - height[k-1]| / dT[k-1] */
+  const double *dlen_dn;       /* [sum ndep]: entry k >= 1,
+                                  d|height[k] - height[k-1]| / dT[k] */
+} pyrh_lte_setup_dT;
+
 /* A batch of atmospheres with possibly uneven depth and wavelength counts.
    Atmosphere p owns depths [depth_off[p], depth_off[p] + ndep[p]) of every
    per-depth array, wavelengths [lam_off[p], lam_off[p] + nlam[p]) of lambda,
@@ -108,6 +133,9 @@ typedef struct {
   const void *chi_c;           /* continuum opacity [m^-1] (float or double,
                                   following the precision) */
   const void *eta_c;           /* continuum emissivity [W m^-3 Hz^-1 sr^-1] */
+  const pyrh_lte_setup_dT *setup_dT;  /* optional HOST pointer (NULL: the
+                                  set-up is held fixed); read only by the
+                                  response-function entry points */
 } pyrh_lte_batch;
 
 typedef struct {
@@ -140,10 +168,16 @@ pyrh_status pyrh_check_lines(const pyrh_line *host_lines, int32_t nline,
                              int32_t stokes_mode);
 
 /* Same computation with HOST inputs and outputs: copies the batch to the
-   device, runs pyrh_lte_stokes on an internal stream and copies the Stokes
-   vectors back, all inside the call (the shape of a compute1d()-style call,
-   pyrh.pyx:621-642).  Device buffers are cached between calls with the same
-   or smaller sizes.  Not re-entrant (one internal workspace). */
+   device, runs pyrh_lte_stokes and copies the Stokes vectors back, all
+   inside the call (the shape of a compute1d()-style call,
+   pyrh.pyx:621-642).  When the atmospheres' continuum and spectra follow one
+   another in memory, the continuum (the bulk of the bytes) is uploaded in
+   chunks of about 128 MB of atmospheres, each synthesised on a second
+   internal stream while the next uploads, and its spectra copied back on a
+   third; pyrh_last_launch_count() then reports one launch per chunk.  Host
+   buffers in page-locked memory let the copies run at full speed.  Device
+   buffers are cached between calls with the same or smaller sizes.  Not
+   re-entrant (one internal workspace). */
 pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch *host_batch,
                                  const pyrh_line *host_lines, int32_t nline,
                                  const pyrh_lte_config *cfg, void *host_stokes_out);

@@ -45,7 +45,13 @@ class PyrhLteBatch(C.Structure):
                 ("ndep", C.c_void_p), ("depth_off", C.c_void_p), ("nlam", C.c_void_p),
                 ("lam_off", C.c_void_p), ("cont_off", C.c_void_p), ("lambda_", C.c_void_p)] + \
         [(n, C.c_void_p) for n in ("height", "T", "ne", "nHtot", "np", "vturb", "vlos", "B",
-                                   "gamma_B", "chi_B", "line_pops", "chi_c", "eta_c")]
+                                   "gamma_B", "chi_B", "line_pops", "chi_c", "eta_c",
+                                   "setup_dT")]
+
+
+class PyrhLteSetupDT(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("dchi_c", "deta_c", "dline_pops", "dnp", "dlen_up",
+                                          "dlen_dn")]
 
 
 class PyrhLteConfig(C.Structure):

@@ -179,6 +179,8 @@ pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nli
   ra.grad = grad;
   ra.rf_gf = rf_gf;
   ra.grad_gf = grad_gf;
+  if (b->setup_dT) ra.dT = *b->setup_dT;
+  else memset(&ra.dT, 0, sizeof(ra.dT));
   const size_t smem = pyrh::rf_smem_bytes(cfg->precision, nline, ra.lte.maxd);
   if (smem > 200 * 1024)
     return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
@@ -192,12 +194,30 @@ pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nli
   return PYRH_OK;
 }
 
-// Workspace of the host-buffer entry point.
+// Workspace of the host-buffer entry point: device buffers cached between
+// calls, and four streams (host-to-device copies, two for kernels,
+// device-to-host copies) with per-chunk events for the pipelined upload.
 struct HostWs {
   std::mutex mu;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // host-to-device copies
+  cudaStream_t kstream[2] = {};       // kernels of even and odd chunks
+  cudaStream_t ostream = nullptr;     // device-to-host copies
+  std::vector<cudaEvent_t> ev_in, ev_k;
   std::vector<void*> bufs;
   std::vector<size_t> caps;
+  cudaError_t init(int nchunk) {
+    cudaError_t e = cudaSuccess;
+    for (cudaStream_t* s : {&stream, &kstream[0], &kstream[1], &ostream})
+      if (!*s && (e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking)) != cudaSuccess) return e;
+    while ((int)ev_in.size() < nchunk) {
+      cudaEvent_t a, b;
+      if ((e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming)) != cudaSuccess) return e;
+      if ((e = cudaEventCreateWithFlags(&b, cudaEventDisableTiming)) != cudaSuccess) return e;
+      ev_in.push_back(a);
+      ev_k.push_back(b);
+    }
+    return e;
+  }
   void* get(int slot, size_t bytes, cudaError_t* err) {
     if ((int)bufs.size() <= slot) { bufs.resize(slot + 1, nullptr); caps.resize(slot + 1, 0); }
     if (caps[slot] < bytes) {
@@ -419,10 +439,11 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host
     s = check_lines_host(host_lines, nline, cfg->stokes_mode);
     if (s != PYRH_OK) return s;
   }
-  std::lock_guard<std::mutex> lock(g_ws.mu);
-  if (!g_ws.stream) CUDA_TRY(cudaStreamCreateWithFlags(&g_ws.stream, cudaStreamNonBlocking));
   const int natm = hb->natm;
   long long nlam_tot = 0, cont_tot = 0;
+  // atmospheres whose continuum and spectrum follow each other in memory
+  // can be uploaded and synthesised in chunks that overlap
+  bool ordered = true;
   for (int p = 0; p < natm; ++p) {
     const long long e = hb->lam_off[p] + hb->nlam[p];
     if (e > nlam_tot) nlam_tot = e;
@@ -431,11 +452,23 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host
     if (hb->ndep[p] < 3 || hb->ndep[p] > hb->max_ndep || hb->nlam[p] < 1 ||
         hb->nlam[p] > hb->max_nlam || hb->depth_off[p] + hb->ndep[p] > hb->total_depth)
       return fail(PYRH_ERR_ARG, "atmosphere %d: inconsistent ndep/nlam/offsets", p);
+    if (p > 0 && (hb->cont_off[p] < hb->cont_off[p - 1] + (long long)hb->ndep[p - 1] * hb->nlam[p - 1] ||
+                  hb->lam_off[p] < hb->lam_off[p - 1] + hb->nlam[p - 1]))
+      ordered = false;
   }
   const size_t real = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
   const size_t D = sizeof(double) * hb->total_depth;
+  // about 128 MB of continuum per chunk, at most 16 chunks
+  const long long cont_bytes = 2LL * (long long)real * cont_tot;
+  int nchunk = ordered ? (int)(cont_bytes / (128LL << 20)) : 1;
+  if (nchunk > 16) nchunk = 16;
+  if (nchunk > natm) nchunk = natm;
+  if (nchunk < 1) nchunk = 1;
+  std::lock_guard<std::mutex> lock(g_ws.mu);
+  CUDA_TRY(g_ws.init(nchunk));
   cudaError_t err = cudaSuccess;
   pyrh_lte_batch db = *hb;
+  db.setup_dT = nullptr;   // the forward synthesis does not read it
   int slot = 0;
   auto up = [&](const void* src, size_t bytes) -> void* {
     void* d = g_ws.get(slot++, bytes, &err);
@@ -458,21 +491,68 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host
   UP(height, D); UP(T, D); UP(ne, D); UP(nHtot, D); UP(np, D);
   UP(vturb, D); UP(vlos, D); UP(B, D); UP(gamma_B, D); UP(chi_B, D);
   if (nline > 0) UP(line_pops, D * 2 * nline);
-  UP(chi_c, real * cont_tot);
-  UP(eta_c, real * cont_tot);
 #undef UP
   pyrh_line* d_lines = nullptr;
   if (nline > 0) {
     d_lines = (pyrh_line*)up(host_lines, sizeof(pyrh_line) * nline);
     if (!d_lines) return fail(PYRH_ERR_CUDA, "upload lines: %s", cudaGetErrorString(err));
   }
+  unsigned char* d_chi = (unsigned char*)g_ws.get(slot++, real * cont_tot, &err);
+  unsigned char* d_eta = d_chi ? (unsigned char*)g_ws.get(slot++, real * cont_tot, &err) : nullptr;
+  if (!d_eta) return fail(PYRH_ERR_CUDA, "continuum buffers: %s", cudaGetErrorString(err));
+  db.chi_c = d_chi;
+  db.eta_c = d_eta;
   const size_t out_bytes = real * 4 * nlam_tot;
-  void* d_out = g_ws.get(slot++, out_bytes, &err);
+  unsigned char* d_out = (unsigned char*)g_ws.get(slot++, out_bytes, &err);
   if (!d_out) return fail(PYRH_ERR_CUDA, "output buffer: %s", cudaGetErrorString(err));
-  s = launch(&db, d_lines, nline, cfg, d_out, g_ws.stream);
-  if (s != PYRH_OK) return s;
-  CUDA_TRY(cudaMemcpyAsync(host_stokes_out, d_out, out_bytes, cudaMemcpyDeviceToHost, g_ws.stream));
+  // Chunk c: upload its continuum (copy stream), synthesise its atmospheres
+  // once the upload is done (kernel stream c % 2), copy its spectra back
+  // (output stream).  Chunk c+1's upload runs under chunk c's kernel, and
+  // with two kernel streams chunk c+1's blocks fill the SMs that chunk c's
+  // last, partial wave leaves idle.
+  const unsigned char* h_chi = (const unsigned char*)hb->chi_c;
+  const unsigned char* h_eta = (const unsigned char*)hb->eta_c;
+  for (int c = 0; c < nchunk; ++c) {
+    const int p0 = (int)((long long)natm * c / nchunk);
+    const int p1 = (int)((long long)natm * (c + 1) / nchunk);
+    long long c0 = nchunk == 1 ? 0 : hb->cont_off[p0];
+    long long c1 = nchunk == 1 ? cont_tot
+                               : hb->cont_off[p1 - 1] + (long long)hb->ndep[p1 - 1] * hb->nlam[p1 - 1];
+    CUDA_TRY(cudaMemcpyAsync(d_chi + real * c0, h_chi + real * c0, real * (c1 - c0),
+                             cudaMemcpyHostToDevice, g_ws.stream));
+    CUDA_TRY(cudaMemcpyAsync(d_eta + real * c0, h_eta + real * c0, real * (c1 - c0),
+                             cudaMemcpyHostToDevice, g_ws.stream));
+    CUDA_TRY(cudaEventRecord(g_ws.ev_in[c], g_ws.stream));
+    cudaStream_t ks = g_ws.kstream[c & 1];
+    CUDA_TRY(cudaStreamWaitEvent(ks, g_ws.ev_in[c], 0));
+    pyrh_lte_batch cb = db;   // atmospheres [p0, p1): offsets stay absolute
+    cb.natm = p1 - p0;
+    cb.ndep = db.ndep + p0;
+    cb.depth_off = db.depth_off + p0;
+    cb.nlam = db.nlam + p0;
+    cb.lam_off = db.lam_off + p0;
+    cb.cont_off = db.cont_off + p0;
+    s = launch(&cb, d_lines, nline, cfg, d_out, ks);
+    if (s != PYRH_OK) return s;
+    CUDA_TRY(cudaEventRecord(g_ws.ev_k[c], ks));
+    CUDA_TRY(cudaStreamWaitEvent(g_ws.ostream, g_ws.ev_k[c], 0));
+    const long long l0 = nchunk == 1 ? 0 : hb->lam_off[p0];
+    const long long l1 = nchunk == 1 ? nlam_tot : hb->lam_off[p1 - 1] + hb->nlam[p1 - 1];
+    if (nchunk == 1) {
+      CUDA_TRY(cudaMemcpyAsync(host_stokes_out, d_out, out_bytes, cudaMemcpyDeviceToHost,
+                               g_ws.ostream));
+    } else {
+      // Stokes of atmosphere p occupy [4 lam_off[p], 4 lam_off[p] + 4 nlam[p])
+      CUDA_TRY(cudaMemcpyAsync((unsigned char*)host_stokes_out + real * 4 * l0,
+                               d_out + real * 4 * l0, real * 4 * (l1 - l0),
+                               cudaMemcpyDeviceToHost, g_ws.ostream));
+    }
+  }
+  CUDA_TRY(cudaStreamSynchronize(g_ws.ostream));
+  CUDA_TRY(cudaStreamSynchronize(g_ws.kstream[0]));
+  CUDA_TRY(cudaStreamSynchronize(g_ws.kstream[1]));
   CUDA_TRY(cudaStreamSynchronize(g_ws.stream));
+  g_last_launches = nchunk;
   return PYRH_OK;
 }
 

@@ -26,8 +26,12 @@
 //      vector-Jacobian product the caller's dL/dS, give one value per
 //      (x, k), summed over the block's wavelengths in shared memory and then
 //      added to the atmosphere's gradient in HBM.
-// The opacity derivatives are recomputed at each depth, not stored, so the
-// tape holds 21 values per depth; four depths of adjoints are live at a time.
+// With the set-up's temperature derivatives (RfArgs::dT), the temperature
+// slot also collects the continuum, population and path-length terms (the
+// reference's finite-difference response functions re-run the set-up for
+// every perturbed temperature, rf_ray.c:257-283).
+// The tape holds 21 values per depth plus the Zeeman profile sums of the
+// first kZLines lines; four depths of adjoints are live at a time.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -52,6 +56,8 @@ struct RfSmem {
   int* polar;         // [nline]
   double* lam0;       // [nline]
   R* grad;            // [kNX][maxd] (chi^2 mode)
+  R* len_up;          // [maxd] d ds_k/dT_{k-1} (k >= 1; ds includes 1/mu), or zeros
+  R* len_dn;          // [maxd] d ds_k/dT_k
   R* chi2;            // [1]
   R* gfs;             // [nline] log gf gradient of the block (modes 1-2)
 };
@@ -78,6 +84,8 @@ __host__ __device__ size_t rf_smem_t(int nline, int maxd, RfSmem<R>* s, unsigned
   p = take(sizeof(int) * nline);                 if (s) s->polar = reinterpret_cast<int*>(p);
   p = take(sizeof(double) * nline);              if (s) s->lam0 = reinterpret_cast<double*>(p);
   p = take(sizeof(R) * kNX * maxd);              if (s) s->grad = reinterpret_cast<R*>(p);
+  p = take(sizeof(R) * maxd);                    if (s) s->len_up = reinterpret_cast<R*>(p);
+  p = take(sizeof(R) * maxd);                    if (s) s->len_dn = reinterpret_cast<R*>(p);
   p = take(sizeof(R) * 4);                       if (s) s->chi2 = reinterpret_cast<R*>(p);
   p = take(sizeof(R) * (nline > 0 ? nline : 1)); if (s) s->gfs = reinterpret_cast<R*>(p);
   return off;
@@ -92,6 +100,8 @@ struct Local {
   R dlam[PYRH_MAX_LINES];
   const R* chi_c;   // continuum of this (atmosphere, wavelength): index k * nl
   const R* eta_c;
+  const R* dchi_c;  // their temperature derivatives, or nullptr (held fixed)
+  const R* deta_c;
 };
 
 // Sum of every thread's per-line log gf gradient over the warp (shuffles)
@@ -116,7 +126,10 @@ struct Emit {
   R* rf;             // mode 0: rf_out + 24 * cont_off + la
   R* gf;             // per-thread log gf accumulators [NS][PYRH_MAX_LINES] or nullptr
   const Tape<R>* tp;
-  __device__ void operator()(int k, const R* qb, const R* bpl) const {
+  // k: the depth handed over; qb: dL_s/dq_k; bpl: dL_s/dB_k of the Planck
+  // boundary; sdn, sup: dL_s/d ds_k and dL_s/d ds_{k+1} (path lengths)
+  __device__ void operator()(int k, const R* qb, const R* bpl, const R* sdn,
+                             const R* sup) const {
     constexpr int NS = MODE == 0 ? 4 : 1;
     const RfSmem<R>& sm = *loc->sm;
     R g[NS][kNX];
@@ -126,14 +139,16 @@ struct Emit {
       for (int x = 0; x < kNX; ++x) g[s][x] = R(0);
     local_q_vjp<R, NS>(loc->nline, sm.ld + k, loc->maxd, sm.geo[k], loc->dlam, loc->inwin,
                        sm.ncomp, sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS, tp->q[k], qb,
-                       g, gf, tp->z[k]);
+                       g, gf, tp->z[k], loc->dchi_c ? loc->dchi_c[(int64_t)k * nl] : R(0),
+                       loc->deta_c ? loc->deta_c[(int64_t)k * nl] : R(0));
     const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lam)) : R(0);
+    const R ldn = sm.len_dn[k], lup = (k + 1 < nd) ? sm.len_up[k + 1] : R(0);
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
 #pragma unroll
       for (int x = 0; x < kNX; ++x) {
         R v = g[s][x];
-        if (x == 0) v += bpl[s] * dB;
+        if (x == 0) v += bpl[s] * dB + sdn[s] * ldn + sup[s] * lup;
         if (MODE == 0) {
           if (act) rf[((int64_t)(s * kNX + x) * nd + k) * nl] = v;
         } else {   // modes 1 and 2: sum over the warp's wavelengths first
@@ -193,6 +208,8 @@ lte_rf_kernel(RfArgs ra) {
       const int64_t d = doff + k;
       sm.ds[k] = (k >= 1) ? R(fabs(args.height[d] - args.height[d - 1]) * imu) : R(0);
       sm.geo[k] = geometry_d<R>(R(args.gamma_B[d]), R(args.chi_B[d]), R(muz));
+      sm.len_up[k] = (k >= 1 && ra.dT.dlen_up) ? R(ra.dT.dlen_up[d] * imu) : R(0);
+      sm.len_dn[k] = (k >= 1 && ra.dT.dlen_dn) ? R(ra.dT.dlen_dn[d] * imu) : R(0);
       if (MODE != 0)
         for (int x = 0; x < kNX; ++x) sm.grad[x * args.maxd + k] = R(0);
     }
@@ -206,12 +223,15 @@ lte_rf_kernel(RfArgs ra) {
       const LineConstD c = {L.lambda0, L.Ei, L.gi, L.Aji, L.Bji, L.Bij, L.Grad, L.GStark,
                             L.GvdWaals, L.cross, L.alpha, L.isotope_frac, L.hyperfine_frac,
                             L.weight, L.vdwaals};
+      const double* dp = ra.dT.dline_pops;
       sm.ld[l * args.maxd + k] = line_depth<R>(
           c, R(args.T[d]), R(args.vlos[d]), R(args.vturb[d]), R(args.B[d]), R(args.ne[d]),
           R(args.nHtot[d]), R(args.np[d]),
           R(args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d]),
           R(args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d]), R(muz),
-          args.moving != 0);
+          args.moving != 0, dp ? R(dp[((int64_t)l * 2 + 0) * args.total_depth + d]) : R(0),
+          dp ? R(dp[((int64_t)l * 2 + 1) * args.total_depth + d]) : R(0),
+          ra.dT.dnp ? R(ra.dT.dnp[d]) : R(0));
     }
     __syncthreads();
 
@@ -237,6 +257,10 @@ lte_rf_kernel(RfArgs ra) {
       }
       loc.chi_c = static_cast<const R*>(args.chi_c) + args.cont_off[p] + la;
       loc.eta_c = static_cast<const R*>(args.eta_c) + args.cont_off[p] + la;
+      loc.dchi_c = ra.dT.dchi_c ? static_cast<const R*>(ra.dT.dchi_c) + args.cont_off[p] + la
+                                : nullptr;
+      loc.deta_c = ra.dT.deta_c ? static_cast<const R*>(ra.dT.deta_c) + args.cont_off[p] + la
+                                : nullptr;
 
       Tape<R> tp;
       auto qop = [&](int k, R* q) {

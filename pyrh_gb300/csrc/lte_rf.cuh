@@ -16,10 +16,16 @@
 //     dq_k/dx_k (forward-mode dual numbers through the Zeeman/Voigt opacity
 //     of kurucz.c:729-827 and the line strength of kurucz.c:638-680, with
 //     the exact derivative of each Humlicek region) closes the chain.
-// The continuum (chi_c, eta_c), stage densities and the height scale are
-// inputs of the hot path and are held fixed.  The reference has no
-// analytical response functions for these parameters; its definition is
-// finite differences of the whole synthesis (rf_ray.c:205-293).
+// The reference has no analytical response functions for these parameters;
+// its definition is finite differences of the whole synthesis
+// (rf_ray.c:205-293), which re-runs the set-up for every perturbation.  The
+// set-up's outputs are inputs here (continuum chi_c and eta_c, stage
+// densities, proton density, path lengths); where the caller passes their
+// temperature derivatives (pyrh_lte_setup_dT) the temperature response
+// carries them too: the continuum terms through dL/dchi_c and dL/deta_c
+// (local_q_vjp), the populations through the line quantities (line_depth),
+// and the path lengths through their own adjoints in the reverse sweep.
+// Without them the set-up is held fixed.
 #pragma once
 
 #include "../../include/pyrh_gb300.h"
@@ -217,11 +223,22 @@ struct LineConstD {
   int vdwaals;
 };
 
+// dn_dT, dlnU_dT, dnp_dT: derivatives of the set-up's stage density, log
+// partition function and proton density with respect to the temperature of
+// the same depth (zero: held fixed).  The reference's finite-difference
+// response functions re-run the LTE populations for every perturbed T
+// (rf_ray.c:257-283 -> Background() -> LTEpops), so its temperature
+// response carries these terms.
 template <typename R>
 PYRH_HD LineDepth<R> line_depth(const LineConstD& L, R T, R vel, R vturb, R B, R ne, R nHtot,
-                                R np, R nstage, R lnU, R muz, bool moving) {
+                                R np, R nstage, R lnU, R muz, bool moving, R dn_dT = R(0),
+                                R dlnU_dT = R(0), R dnp_dT = R(0)) {
   LineDepth<R> o;
   const D6<R> dT = dvar(T, 0), dv = dvar(vel, 1), dvt = dvar(vturb, 2), dB = dvar(B, 3);
+  D6<R> nst = dconst(nstage), lnUd = dconst(lnU), npd = dconst(np);
+  nst.d[0] = dn_dT;
+  lnUd.d[0] = dlnU_dT;
+  npd.d[0] = dnp_dT;
   const R vtherm = R(2.0 * kKBOLTZMANN / (kAMU * L.weight));
   const D6<R> vb = dsqrt(vtherm * dT + dvt * dvt);
   const D6<R> one = dconst(R(1));
@@ -234,7 +251,7 @@ PYRH_HD LineDepth<R> line_depth(const LineConstD& L, R T, R vel, R vturb, R B, R
     if (L.vdwaals == 0) GvdW = R(L.cross) * dpow(dT, R(0.3));
     else if (L.vdwaals == 2) GvdW = R(L.cross) * dpow(dT, R((1.0 - L.alpha) / 2.0));
     else GvdW = dconst(R(L.GvdWaals));
-    const D6<R> G = dconst(R(L.Grad + L.GStark * ne)) + (nHtot - np) * GvdW;
+    const D6<R> G = dconst(R(L.Grad + L.GStark * ne)) + (dconst(nHtot) - npd) * GvdW;
     o.adamp = R(L.lambda0 * kNM_TO_M / (4.0 * kPI)) * (G / vb);
   } else {
     o.adamp = dconst(R(-1));
@@ -245,7 +262,7 @@ PYRH_HD LineDepth<R> line_depth(const LineConstD& L, R T, R vel, R vturb, R B, R
   const R B4 = R(kHPLANCK * kCLIGHT / (4.0 * kPI) * L.Bij * L.isotope_frac * L.hyperfine_frac * L.gi);
   const R tw = R(L.Aji / L.Bji);
   const D6<R> kT = one / (R(kKBOLTZMANN) * dT);
-  const D6<R> ni = nstage * dexp(dconst(-lnU) - R(L.Ei) * kT);
+  const D6<R> ni = nst * dexp(dconst(R(0)) - lnUd - R(L.Ei) * kT);
   const D6<R> nj = ni * dexp(dconst(R(0)) - hc_la * kT);
   o.chil = (B4 * (ni - nj)) * sv;
   o.etal = ((B4 * tw) * nj) * sv;
@@ -445,12 +462,14 @@ PYRH_HD void local_q(int nline, const LineDepth<R>* ld, int ld_stride, const Geo
 // With z (the profile sums local_q<R, true> stored for this depth), the
 // first kZLines in-window lines take their profile sums and derivatives from
 // z instead of re-evaluating the Zeeman components.
+// dchic_dT, detac_dT: temperature derivatives of the continuum opacity and
+// emissivity of this (depth, wavelength) from the set-up (zero: held fixed).
 template <typename R, int NS>
 PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
                          const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
                          const R* cweight, const int* cq, int maxcomp, const R q[8],
                          const R* qb, R out[NS][kNX], R* gf = nullptr,
-                         const R (*z)[kZ] = nullptr) {
+                         const R (*z)[kZ] = nullptr, R dchic_dT = R(0), R detac_dT = R(0)) {
   int slot = 0;
   const R ichi = fdiv(R(1), q[0]);
   R eb[NS][4], cb[NS][4];
@@ -554,6 +573,9 @@ PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const
     for (int x = 0; x < kNX; ++x)
       out[s][x] += gb[s][0] * geo.s2g.d[x] + gb[s][1] * geo.gQ.d[x] + gb[s][2] * geo.gU.d[x] +
                    gb[s][3] * geo.gV.d[x];
+  // continuum: chi = chi_c + lines and S = (eta_c + lines) / chi, so
+  // dL/dchi_c = cb[s][0] and dL/deta_c = eb[s][0]
+  for (int s = 0; s < NS; ++s) out[s][0] += cb[s][0] * dchic_dT + eb[s][0] * detac_dT;
 }
 
 // ------------------------------------------------- coefficient derivatives --
@@ -913,12 +935,15 @@ PYRH_HD void w3_d(double dtau, double w[3], double dw[2]) {
 }
 
 // Reverse (adjoint) sweep of delo_forward for NS seeds (seed[s][4] =
-// dL_s/dI_0).  dL/dq_j is handed to emit(j, qb_j, bpl) as soon as no later
-// step can add to it (step k reaches depths k-2 .. k+1), so only four depths
-// of adjoints are live at a time instead of all of them.  qb_j is
-// R[NS][8]; bpl[s] is dL_s/dB for the Planck function of depth j (non-zero
-// only for the two bottom depths, whose temperatures set the boundary
-// condition I = B1 - (B0 - B1)/dtau).  The steps are shared by the seeds.
+// dL_s/dI_0).  dL/dq_j is handed to emit(j, qb_j, bpl, sdn, sup) as soon as
+// no later step can add to it (step k reaches depths k-2 .. k+1), so only
+// four depths of adjoints are live at a time instead of all of them.  qb_j
+// is R[NS][8]; bpl[s] is dL_s/dB for the Planck function of depth j
+// (non-zero only for the two bottom depths, whose temperatures set the
+// boundary condition I = B1 - (B0 - B1)/dtau); sdn[s] and sup[s] are dL_s/d
+// ds_j and dL_s/d ds_{j+1}, the adjoints of the path lengths of the two
+// intervals that meet at depth j (zero where there is none), final by the
+// time depth j is handed over.  The steps are shared by the seeds.
 template <typename R, int NS, typename Emit>
 PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double B0, double B1,
                                  const R seed[NS][4], Emit&& emit) {
@@ -932,6 +957,10 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
   R zero_b[NS];
   for (int s = 0; s < NS; ++s) zero_b[s] = R(0);
   R Ib[NS][4], dSb[NS][4], dKb[NS][3], dchib[NS], Tb[NS];
+  // path-length adjoints of the intervals ending at depths k, k-1, k-2 of
+  // the step being reversed (ds_k, ds_{k-1}, ds_{k-2}), rotated like qc..qdd
+  R sc[NS], sd[NS], sdd[NS];
+  for (int s = 0; s < NS; ++s) sc[s] = sd[s] = sdd[s] = R(0);
   // ---- last interval ----
   {
     const double dtau = 0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * (double)ds[1];
@@ -997,6 +1026,7 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       const double dtb = (double)w0b * dw[0] + (double)w1b * dw[1] - (double)wdb * w[1] / (dtau * dtau);
       q0[s][0] += R(0.5 * (double)ds[1] * dtb);
       q1[s][0] += R(0.5 * (double)ds[1] * dtb);
+      sc[s] = R(0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * dtb);   // ds_1
       for (int n = 0; n < 3; ++n) dKb[s][n] = R(0);
       dchib[s] = R(0);
       Tb[s] = R(0);
@@ -1054,35 +1084,43 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       for (int n = 0; n < 4; ++n) { qu[s][1 + n] += sb.Su[n]; qc[s][1 + n] += sb.S0[n]; }
       R dchi_cb = R(0), dchi_dnb = dchib[s];
       {
+        // Tdw = ds_k/4 (chi_k + chi_{k-1} + c1 + c2), c2 = chi_k + ds_k/3
+        // dchi_c, c1 = chi_{k-1} - ds_k/3 dchi_dn (each clipped at zero)
         const R a = R(0.25) * dsdn * Tdwb;
         qc[s][0] += a;
         qd[s][0] += a;
-        if (c2pos) { qc[s][0] += a; dchi_cb += (dsdn / R(3)) * a; }
-        if (c1pos) { qd[s][0] += a; dchi_dnb -= (dsdn / R(3)) * a; }
+        sc[s] += Tdwb * Tdw * rdsdn;
+        if (c2pos) { qc[s][0] += a; dchi_cb += (dsdn / R(3)) * a; sc[s] += a * dchi_c / R(3); }
+        if (c1pos) { qd[s][0] += a; dchi_dnb -= (dsdn / R(3)) * a; sc[s] -= a * dchi_dn / R(3); }
       }
       if (k > 1) {
-        R d1 = 0, d2 = 0;
-        cent_deriv_vjp<R>(wchi, tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0], dchi_dnb, d1, d2,
+        cent_deriv_vjp<R>(wchi, tp.q[k][0], tp.q[k - 1][0], tp.q[k - 2][0], dchi_dnb, sc[s], sd[s],
                           qc[s][0], qd[s][0], qdd[s][0]);
       } else {
         qd[s][0] += dchi_dnb * rdsdn;
         qc[s][0] -= dchi_dnb * rdsdn;
+        sc[s] -= dchi_dnb * dchi_dn * rdsdn;
       }
       for (int n = 0; n < 4; ++n) { Ib[s][n] = sb.Iu[n]; dSb[s][n] = sb.dSu[n]; }
       for (int n = 0; n < 3; ++n) dKb[s][n] = sb.dku[n];
       dchib[s] = dchi_cb;
       Tb[s] = Tkb;
     }
-    // depth k-2 received its last term from this step's chi derivative
-    if (k >= 2) emit(k - 2, &qdd[0][0], zero_b);
+    // depth k-2 received its last term from this step's chi derivative, and
+    // ds_{k-1} its last from this step's
+    if (k >= 2) emit(k - 2, &qdd[0][0], zero_b, sdd, sd);
     // rotate: depth k+2 (first reached by the next step) starts at zero
-    for (int s = 0; s < NS; ++s)
+    for (int s = 0; s < NS; ++s) {
       for (int n = 0; n < 8; ++n) {
         qdd[s][n] = qd[s][n];
         qd[s][n] = qc[s][n];
         qc[s][n] = qu[s][n];
         qu[s][n] = R(0);
       }
+      sdd[s] = sd[s];
+      sd[s] = sc[s];
+      sc[s] = R(0);
+    }
   }
   // ---- initial values (k = N-2 set-up and the bottom boundary) ----
   R bpl[2][NS];
@@ -1098,6 +1136,7 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
     R(&eu)[NS][8] = qc;
     R(&ec)[NS][8] = qd;
     R(&ed)[NS][8] = qdd;
+    // and the path lengths ds_{N-1} in sc, ds_{N-2} in sd, ds_{N-3} in sdd
     for (int s = 0; s < NS; ++s) {
       for (int n = 0; n < 4; ++n) {
         ec[s][1 + n] += dSb[s][n] / T;
@@ -1112,13 +1151,22 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       const R a = R(0.25) * dsup * Tb[s];
       ec[s][0] += a;
       eu[s][0] += a;
+      sc[s] += Tb[s] * T / dsup;
       R dchi_cb = dchib[s], dchi_upb = R(0);
-      if (cc - (dsup / R(3)) * dchi_c > R(0)) { ec[s][0] += a; dchi_cb -= (dsup / R(3)) * a; }
-      if (cu + (dsup / R(3)) * dchi_up > R(0)) { eu[s][0] += a; dchi_upb += (dsup / R(3)) * a; }
+      if (cc - (dsup / R(3)) * dchi_c > R(0)) {
+        ec[s][0] += a;
+        dchi_cb -= (dsup / R(3)) * a;
+        sc[s] -= a * dchi_c / R(3);
+      }
+      if (cu + (dsup / R(3)) * dchi_up > R(0)) {
+        eu[s][0] += a;
+        dchi_upb += (dsup / R(3)) * a;
+        sc[s] += a * dchi_up / R(3);
+      }
       ec[s][0] += dchi_upb / dsup;
       eu[s][0] -= dchi_upb / dsup;
-      R d1 = 0, d2 = 0;
-      cent_deriv_vjp<R>(cd_weights<R>(dsup, dsdn), cu, cc, tp.q[k - 1][0], dchi_cb, d1, d2,
+      sc[s] -= dchi_upb * dchi_up / dsup;
+      cent_deriv_vjp<R>(cd_weights<R>(dsup, dsdn), cu, cc, tp.q[k - 1][0], dchi_cb, sc[s], sd[s],
                         eu[s][0], ec[s][0], ed[s][0]);
       const double ib = (double)Ib[s][0];
       bpl[1][s] = R(ib * (1.0 + 1.0 / dtau0));
@@ -1126,11 +1174,12 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
       const double dtb = ib * (B0 - B1) / (dtau0 * dtau0);
       eu[s][0] += R(0.5 * (double)ds[N - 1] * dtb);
       ec[s][0] += R(0.5 * (double)ds[N - 1] * dtb);
+      sc[s] += R(0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * dtb);
     }
   }
-  emit(N - 3, &qdd[0][0], zero_b);
-  emit(N - 2, &qd[0][0], bpl[0]);
-  emit(N - 1, &qc[0][0], bpl[1]);
+  emit(N - 3, &qdd[0][0], zero_b, sdd, sd);
+  emit(N - 2, &qd[0][0], bpl[0], sd, sc);
+  emit(N - 1, &qc[0][0], bpl[1], sc, zero_b);
 }
 
 // dB_nu/dT of planck() (planck.c:38-63)

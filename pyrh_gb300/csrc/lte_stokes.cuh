@@ -33,6 +33,7 @@ struct RfArgs {
   void *rf, *chi2, *grad;
   void *rf_gf;    // mode 0, optional: dS/dlog10(gf) [nline][4][lambda] per atmosphere
   void *grad_gf;  // modes 1-2, optional: dL/dlog10(gf) [natm][nline]
+  pyrh_lte_setup_dT dT;   // set-up temperature derivatives (NULL members: held fixed)
 };
 
 size_t rf_smem_bytes(int precision, int nline, int maxd);

@@ -9,6 +9,14 @@ internal units after rh/rhf1d/pyrh_compute1dray.c:263-270):
   chi_c, eta_c [nlam, ndep]    (continuum opacity / emissivity, as the
                                 reference stores them per wavelength,
                                 rh/readj.c:284-354)
+Optional temperature derivatives of those set-up inputs, used by the
+response functions and gradients (pyrh_lte_setup_dT; a missing key holds
+that input fixed):
+  dT_chi_c, dT_eta_c [nlam, ndep]   d chi_c/dT, d eta_c/dT of the same depth
+  dT_line_pops [nline, 2, ndep]     d n_stage/dT, d ln U/dT
+  dT_np [ndep]                      d n_p/dT
+  dT_len_up, dT_len_dn [ndep]       entry k >= 1: d|h_k - h_{k-1}|/dT_{k-1},
+                                    d|h_k - h_{k-1}|/dT_k
 """
 from __future__ import annotations
 
@@ -90,7 +98,22 @@ def pack(atms: list[dict], nline: int, precision: int = L.PYRH_FP64) -> Packed:
     # continuum [depth][lambda] per atmosphere
     arrays["chi_c"] = np.concatenate([np.asarray(a["chi_c"], real).T.ravel() for a in atms])
     arrays["eta_c"] = np.concatenate([np.asarray(a["eta_c"], real).T.ravel() for a in atms])
+    # set-up temperature derivatives where every atmosphere has them
+    have = lambda k: all(k in a for a in atms)
+    for k in ("dT_chi_c", "dT_eta_c"):
+        if have(k):
+            arrays[k] = np.concatenate([np.asarray(a[k], real).T.ravel() for a in atms])
+    if have("dT_line_pops") and nline:
+        arrays["dT_line_pops"] = np.concatenate(
+            [np.asarray(a["dT_line_pops"], np.float64) for a in atms], axis=2)
+    for k in ("dT_np", "dT_len_up", "dT_len_dn"):
+        if have(k):
+            arrays[k] = np.concatenate([np.asarray(a[k], np.float64) for a in atms])
     return Packed(natm, int(ndep.max()), int(nlam.max()), total_depth, arrays, precision)
+
+
+SETUP_DT_FIELDS = {"dT_chi_c": "dchi_c", "dT_eta_c": "deta_c", "dT_line_pops": "dline_pops",
+                   "dT_np": "dnp", "dT_len_up": "dlen_up", "dT_len_dn": "dlen_dn"}
 
 
 def _batch_struct(pk: Packed, ptr) -> L.PyrhLteBatch:
@@ -105,6 +128,12 @@ def _batch_struct(pk: Packed, ptr) -> L.PyrhLteBatch:
     b.line_pops = ptr("line_pops")
     b.chi_c = ptr("chi_c")
     b.eta_c = ptr("eta_c")
+    if any(k in pk.arrays for k in SETUP_DT_FIELDS):
+        sd = L.PyrhLteSetupDT()
+        for k, f in SETUP_DT_FIELDS.items():
+            setattr(sd, f, ptr(k) if k in pk.arrays else None)
+        b._setup_dT = sd                 # keeps the struct alive with the batch
+        b.setup_dT = C.addressof(sd)
     return b
 
 
@@ -225,4 +254,13 @@ def pack_uniform(batch: dict, nline: int, precision: int = L.PYRH_FP32) -> Packe
     arrays["line_pops"] = np.ascontiguousarray(lp.transpose(1, 2, 0, 3)).reshape(nline, 2, -1)
     arrays["chi_c"] = np.ascontiguousarray(batch["chi_c"], real).reshape(-1)
     arrays["eta_c"] = np.ascontiguousarray(batch["eta_c"], real).reshape(-1)
+    for k in ("dT_chi_c", "dT_eta_c"):
+        if k in batch:
+            arrays[k] = np.ascontiguousarray(batch[k], real).reshape(-1)
+    if "dT_line_pops" in batch:
+        dlp = np.asarray(batch["dT_line_pops"], np.float64)
+        arrays["dT_line_pops"] = np.ascontiguousarray(dlp.transpose(1, 2, 0, 3)).reshape(nline, 2, -1)
+    for k in ("dT_np", "dT_len_up", "dT_len_dn"):
+        if k in batch:
+            arrays[k] = np.ascontiguousarray(batch[k], np.float64).reshape(-1)
     return Packed(natm, nd, nl, natm * nd, arrays, precision)

@@ -6,8 +6,15 @@ The derivatives are taken with respect to the six atmosphere parameters of
 every depth, in this order and in SI units:
     T [K], v_los [m/s], v_mic [m/s], B [T], gamma_B [rad], chi_B [rad]
 (the depth-resolved quantities the reference perturbs for its finite-
-difference response functions, rh/rhf1d/rf_ray.c:205-235).  The continuum
-opacity and emissivity, stage densities and height scale are held fixed.
+difference response functions, rh/rhf1d/rf_ray.c:205-235).
+
+The reference re-runs its set-up for every perturbed temperature
+(Background() and convertScales(), rf_ray.c:257-283), so its temperature
+response also moves the continuum, the stage densities, the proton density
+and, on a tau_500 depth scale, the interval lengths.  A batch packed with the
+dT_* keys of pyrh_gb300.lte (pyrh_lte_setup_dT) gets those terms as well;
+without them the set-up is held fixed and the temperature derivative is the
+partial one at fixed continuum, populations and heights.
 """
 from __future__ import annotations
 
@@ -42,6 +49,24 @@ def _lib():
 def _real(dev: DeviceBatch):
     import torch
     return torch.float32 if dev.pk.precision == L.PYRH_FP32 else torch.float64
+
+
+def tau500_interval_dT(height, chi_ref, dchi_ref_dT):
+    """Temperature derivatives of the interval lengths |h_k - h_{k-1}| of a
+    height scale built from tau_500 (convertScales, TAU500 branch,
+    rh/rhf1d/multiatmos.c:126-138: h_k = h_{k-1} - 2 (tau_k - tau_{k-1}) /
+    (chi_ref_{k-1} + chi_ref_k), chi_ref the continuum opacity at
+    LAMBDA_REF).  Returns (dT_len_up, dT_len_dn) [ndep]: entry k >= 1 is
+    the derivative with respect to T_{k-1} and T_k; entry 0 is zero."""
+    h = np.asarray(height, np.float64)
+    c = np.asarray(chi_ref, np.float64)
+    dc = np.asarray(dchi_ref_dT, np.float64)
+    up, dn = np.zeros(len(h)), np.zeros(len(h))
+    length = np.abs(h[1:] - h[:-1])
+    den = c[:-1] + c[1:]
+    up[1:] = -length * dc[:-1] / den
+    dn[1:] = -length * dc[1:] / den
+    return up, dn
 
 
 def rf_size(pk: Packed) -> int:

@@ -180,10 +180,14 @@ def planck_lambda(T, lam_nm):
 
 
 def synthetic_batch(natm: int, seed: int = 2024, n_per_line: int = 112,
-                    half_width: float = 0.05, dtype=np.float32) -> dict:
+                    half_width: float = 0.05, dtype=np.float32, setup_dT: bool = False) -> dict:
     """natm perturbed copies of the base atmosphere on the 2 x n_per_line
     grid.  Arrays carry a leading atmosphere axis; continuum is
-    [natm, ndep, nlam] (lambda fastest) in `dtype`."""
+    [natm, ndep, nlam] (lambda fastest) in `dtype`.  With setup_dT, also the
+    temperature derivatives of this set-up (dT_chi_c, dT_eta_c [natm, ndep,
+    nlam]; dT_line_pops [natm, nline, 2, ndep]) for response functions that
+    follow T through it; ne, nH, the proton density and the heights do not
+    depend on T here."""
     base = load_base()
     lam = line_wavelengths(n_per_line, half_width)
     nd = len(base["T"])
@@ -213,6 +217,18 @@ def synthetic_batch(natm: int, seed: int = 2024, n_per_line: int = 112,
     lp = np.repeat(base["line_pops"][None], natm, axis=0)    # [natm, nline, 2, nd]
     lp[:, :, 0, :] *= f_fe[:, None, :]
     out["line_pops"] = lp
+    if setup_dT:
+        # d ln f / dT of the Saha factors above; d B / dT = B x e^x / ((e^x - 1) T)
+        g_cont = -1.5 / T - E_HMINUS / (KBOLTZMANN * T * T)
+        g_fe = -1.5 / T - E_FE_ION / (KBOLTZMANN * T * T)
+        x = HPLANCK * CLIGHT / (KBOLTZMANN * lam[None, None, :] * 1e-9 * T[:, :, None])
+        dlnB = x / (-np.expm1(-x) * T[:, :, None])
+        dchi = chi_c.astype(np.float64) * g_cont[:, :, None]
+        out["dT_chi_c"] = dchi.astype(dtype)
+        out["dT_eta_c"] = (eta_c.astype(np.float64) * (g_cont[:, :, None] + dlnB)).astype(dtype)
+        dlp = np.zeros_like(lp)
+        dlp[:, :, 0, :] = lp[:, :, 0, :] * g_fe[:, None, :]
+        out["dT_line_pops"] = dlp
     return out
 
 

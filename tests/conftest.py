@@ -52,11 +52,14 @@ def rf_harness(tmp_path_factory):
     return C.CDLL(out)
 
 
-def rf_eval(lib, fx, sel, single=False, jac=False, loggf=False):
+def rf_eval(lib, fx, sel, single=False, jac=False, loggf=False, setup_dT=None):
     """Stokes [nsel, 4] and response functions [nsel, 4, 6, ndep] of one
     atmosphere at the wavelengths fx["lam"][sel] (CPU harness, FP64 or, with
     single=True, FP32; jac=True takes the opacity derivatives in forward
-    mode); loggf=True also returns dS/dlog10(gf) [nsel, 4, nline]."""
+    mode); loggf=True also returns dS/dlog10(gf) [nsel, 4, nline].
+    setup_dT: optional dict of the set-up's temperature derivatives
+    (dchi_c, deta_c [lambda][depth]; dline_pops [line][2][depth]; dnp,
+    dlen_up, dlen_dn [depth]); missing keys are held fixed."""
     from pyrh_gb300 import lte
     D = C.POINTER(C.c_double)
     keep = []
@@ -72,13 +75,22 @@ def rf_eval(lib, fx, sel, single=False, jac=False, loggf=False):
     st = np.zeros((len(sel), 4))
     rf = np.zeros((len(sel), 4, 6, nd))
     gf = np.zeros((len(sel), 4, max(n, 1)))
-    fn = lib.rf_eval_f32 if single else (lib.rf_eval_jac if jac else lib.rf_eval)
-    r = fn(nd, arr(fx["height"]), arr(fx["T"]), arr(fx["ne"]), arr(fx["nHtot"]),
-                    arr(fx["np"]), arr(fx["vturb"]), arr(fx["vel"]), arr(fx["B"]),
-                    arr(fx["gamma_B"]), arr(fx["chi_B"]), arr(fx["line_pops"]), n, lines,
-                    len(sel), arr(lam), arr(fx["chi_c"][sel]), arr(fx["eta_c"][sel]),
-                    C.c_double(float(fx["mu"])), C.c_double(float(fx["vmicro_char"])),
-                    st.ctypes.data_as(D), rf.ctypes.data_as(D), gf.ctypes.data_as(D))
+    args = [nd, arr(fx["height"]), arr(fx["T"]), arr(fx["ne"]), arr(fx["nHtot"]),
+            arr(fx["np"]), arr(fx["vturb"]), arr(fx["vel"]), arr(fx["B"]),
+            arr(fx["gamma_B"]), arr(fx["chi_B"]), arr(fx["line_pops"]), n, lines,
+            len(sel), arr(lam), arr(fx["chi_c"][sel]), arr(fx["eta_c"][sel]),
+            C.c_double(float(fx["mu"])), C.c_double(float(fx["vmicro_char"])),
+            st.ctypes.data_as(D), rf.ctypes.data_as(D), gf.ctypes.data_as(D)]
+    if setup_dT is None:
+        fn = lib.rf_eval_f32 if single else (lib.rf_eval_jac if jac else lib.rf_eval)
+    else:
+        fn = lib.rf_eval_f32_dT if single else (lib.rf_eval_jac_dT if jac else lib.rf_eval_dT)
+        g = setup_dT.get
+        args += [arr(g("dchi_c")[sel]) if g("dchi_c") is not None else None,
+                 arr(g("deta_c")[sel]) if g("deta_c") is not None else None]
+        args += [arr(g(k)) if g(k) is not None else None
+                 for k in ("dline_pops", "dnp", "dlen_up", "dlen_dn")]
+    r = fn(*args)
     assert r == 0
     return (st, rf, gf) if loggf else (st, rf)
 

@@ -18,6 +18,16 @@ Fixtures (npz, float64):
                   outside every line window, duplicate and unsorted lambda
   lte_b0          B = 0 (polarizable lines with no splitting)
   lte_batch       6 atmospheres of the batched generator (2 x 112 lambda)
+  lte_c0_dT, lte_edge_dT
+                  temperature derivatives of the set-up inputs of lte_c0 /
+                  lte_edge (continuum, stage densities and ln U, proton
+                  density: central differences of harness_dump_lte at
+                  T (1 +- 1e-5), every depth at once, since the set-up is
+                  local in depth; interval lengths from convertScales'
+                  tau_500 rule, rh/rhf1d/multiatmos.c:126-138), and the
+                  reference's own temperature response functions: central
+                  differences of rhf1d() (portable build) with T perturbed at
+                  one depth, the definition of rh/rhf1d/rf_ray.c:205-293
   nlte_c1         six-level Ca II-like atom ACTIVE, 82 depths, 5 rays
   nlte_c4_50/120  the same atom on perturbed 50- and 120-depth atmospheres
                   with velocity fields and other wavelength counts
@@ -156,6 +166,71 @@ def make_lte_batch(ref, wd, n=6, seed=2024):
     print(f"lte_batch: {n} atmospheres, {os.path.getsize(path) / 1e3:.0f} kB")
 
 
+def tau500_len_dT(height, chi_ref, dchi_ref):
+    """d|h_k - h_{k-1}| / dT_{k-1} and / dT_k (entry k >= 1) on a tau_500
+    scale: convertScales sets h_k = h_{k-1} - 2 (tau_k - tau_{k-1}) /
+    (chi_ref_{k-1} + chi_ref_k) (rh/rhf1d/multiatmos.c:126-138), so the
+    interval length scales as 1 / (chi_ref_{k-1} + chi_ref_k)."""
+    n = len(height)
+    up, dn = np.zeros(n), np.zeros(n)
+    dh = np.abs(height[1:] - height[:-1])
+    den = chi_ref[:-1] + chi_ref[1:]
+    up[1:] = -dh * dchi_ref[:-1] / den
+    dn[1:] = -dh * dchi_ref[1:] / den
+    return up, dn
+
+
+FD_STEPS = np.array([3e-3, 1e-3, 3e-4])     # relative temperature steps
+
+
+def lte_dT_case(ref, name, depths, eps=1e-5):
+    fx = dict(np.load(os.path.join(HERE, name + ".npz")))
+    atm, wave, mu = fx["atm"], fx["wave"], float(fx["mu"])
+    wd = rr.scratch_dir()
+    rr.write_inputs(wd, wl.fe_linelist())
+    dumps = []
+    for sgn in (1, -1):
+        a = atm.copy()
+        a[1] = atm[1] * (1 + sgn * eps)
+        dd = os.path.join(wd, f"dump{sgn:+d}")
+        ref.dump_lte(wd, mu, a, wave, dd)
+        dumps.append(rr.read_dump(dd))
+    h = eps * atm[1]
+    dif = lambda f: (f(dumps[0]) - f(dumps[1])) / (2 * h)
+    dchi = dif(lambda d: d["cont"][0])
+    deta = dif(lambda d: d["cont"][1])
+    iref = int(np.argmin(np.abs(fx["lam"] - fx["lambda_ref"])))
+    up, dn = tau500_len_dT(fx["height"], fx["chi_c"][iref], dchi[iref])
+    jobs, keys = [], []
+    for k in depths:
+        for rel in FD_STEPS:
+            for sgn in (1, -1):
+                a = atm.copy()
+                a[1, k] += sgn * rel * atm[1, k]
+                jobs.append((wd, PORTABLE.pyrh_path, mu, a, wave))
+    res = PORTABLE.map(rr._synth_job, jobs)
+    fd = np.zeros((len(depths), len(FD_STEPS), 4, len(res[0][0])))
+    i = 0
+    for a, k in enumerate(depths):
+        for b, rel in enumerate(FD_STEPS):
+            fd[a, b] = (res[i][1] - res[i + 1][1]) / (2 * rel * atm[1, k])
+            i += 2
+    out = dict(dT_chi_c=dchi, dT_eta_c=deta,
+               dT_line_pops=dif(lambda d: d["line_pops"]), dT_np=dif(lambda d: d["np"]),
+               dT_len_up=up, dT_len_dn=dn, fd_depths=np.array(depths, np.int32),
+               fd_steps=FD_STEPS, fd_stokes=fd)
+    path = os.path.join(HERE, name + "_dT.npz")
+    np.savez_compressed(path, **out)
+    shutil.rmtree(wd, ignore_errors=True)
+    print(f"{name}_dT: {len(depths)} depths x {len(FD_STEPS)} steps, "
+          f"{os.path.getsize(path) / 1e3:.0f} kB")
+
+
+def make_lte_dT(ref, wd):
+    lte_dT_case(ref, "lte_c0", [3, 20, 35, 45, 50, 55, 60, 65, 68, 70])
+    lte_dT_case(ref, "lte_edge", [3, 30, 45, 55, 62, 68, 70])
+
+
 NLTE_ATOM = "CaII_synth.atom"
 
 
@@ -206,7 +281,8 @@ def make_nlte(ref, wd):
 
 
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
-          "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "nlte": make_nlte}
+          "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
+          "nlte": make_nlte}
 
 
 def main():

@@ -17,6 +17,12 @@
 
 using namespace pyrh;
 
+// Optional temperature derivatives of the set-up (null members: held fixed);
+// layouts as rf_eval_t's inputs ([nlam][nd], [nline][2][nd], [nd]).
+struct SetupDT {
+  const double *dchi_c, *deta_c, *dline_pops, *dnp, *dlen_up, *dlen_dn;
+};
+
 template <typename R, bool JAC>
 struct Emit {
   int nd;
@@ -34,7 +40,9 @@ struct Emit {
   const R *chi_c, *eta_c;   // [depth] at this wavelength
   const Tape<R>* tp;
   R* gf;                    // [4][PYRH_MAX_LINES] log gf accumulators
-  void operator()(int k, const R* qb, const R* bpl) const {
+  const R *dchi_c, *deta_c; // [depth] at this wavelength, or nullptr
+  const R *len_up, *len_dn; // [depth] d ds_k/dT_{k-1}, d ds_k/dT_k
+  void operator()(int k, const R* qb, const R* bpl, const R* sdn, const R* sup) const {
     R g[4][kNX];
     if (JAC) {
       R q[8], J[8][kNX];
@@ -45,16 +53,27 @@ struct Emit {
           g[s][x] = 0;
           for (int n = 0; n < 8; ++n) g[s][x] += qb[s * 8 + n] * J[n][x];
         }
+      // continuum derivative terms as in local_q_vjp: dq/dchi_c, dq/deta_c
+      const R ichi = R(1) / q[0];
+      for (int s = 0; s < 4; ++s) {
+        const R* a = qb + s * 8;
+        R chib = a[0];
+        for (int n = 1; n < 8; ++n) chib -= a[n] * q[n] * ichi;
+        g[s][0] += chib * (dchi_c ? dchi_c[k] : R(0)) + a[1] * ichi * (deta_c ? deta_c[k] : R(0));
+      }
     } else {
       for (int s = 0; s < 4; ++s)
         for (int x = 0; x < kNX; ++x) g[s][x] = 0;
       local_q_vjp<R, 4>(nline, ld + k, PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
-                        PYRH_MAX_COMPONENTS, tp->q[k], qb, g, gf, tp->z[k]);
+                        PYRH_MAX_COMPONENTS, tp->q[k], qb, g, gf, tp->z[k],
+                        dchi_c ? dchi_c[k] : R(0), deta_c ? deta_c[k] : R(0));
     }
     const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lm)) : R(0);
+    const R ldn = len_dn[k], lup = (k + 1 < nd) ? len_up[k + 1] : R(0);
     for (int s = 0; s < 4; ++s)
       for (int x = 0; x < kNX; ++x)
-        rfl[(s * kNX + x) * nd + k] = double(g[s][x] + (x == 0 ? bpl[s] * dB : R(0)));
+        rfl[(s * kNX + x) * nd + k] =
+            double(g[s][x] + (x == 0 ? bpl[s] * dB + sdn[s] * ldn + sup[s] * lup : R(0)));
   }
 };
 
@@ -67,7 +86,8 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
                      const double* vel, const double* B, const double* gam, const double* chb,
                      const double* line_pops, int nline, const pyrh_line* lines, int nlam,
                      const double* lam, const double* chi_c, const double* eta_c, double mu,
-                     double vmicro_char, double* stokes, double* rf, double* rf_gf) {
+                     double vmicro_char, double* stokes, double* rf, double* rf_gf,
+                     const SetupDT& dT) {
   if (nd < 3 || nd > PYRH_MAX_DEPTH_RF || nline > PYRH_MAX_LINES) return -1;
   static LineDepth<R> ld[PYRH_MAX_LINES][PYRH_MAX_DEPTH_RF];
   static GeoD<R> geo[PYRH_MAX_DEPTH_RF];
@@ -87,13 +107,21 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     for (int k = 0; k < nd; ++k)
       ld[l][k] = line_depth<R>(c, R(T[k]), R(vel[k]), R(vturb[k]), R(B[k]), R(ne[k]), R(nHtot[k]),
                                R(np[k]), R(line_pops[(l * 2 + 0) * nd + k]),
-                               R(line_pops[(l * 2 + 1) * nd + k]), R(mu), true);
+                               R(line_pops[(l * 2 + 1) * nd + k]), R(mu), true,
+                               dT.dline_pops ? R(dT.dline_pops[(l * 2 + 0) * nd + k]) : R(0),
+                               dT.dline_pops ? R(dT.dline_pops[(l * 2 + 1) * nd + k]) : R(0),
+                               dT.dnp ? R(dT.dnp[k]) : R(0));
   }
   for (int k = 0; k < nd; ++k) geo[k] = geometry_d<R>(R(gam[k]), R(chb[k]), R(mu));
   R ds[PYRH_MAX_DEPTH_RF];
   ds[0] = 0;
   for (int k = 1; k < nd; ++k) ds[k] = R(fabs(height[k] - height[k - 1]) / mu);
-  R cc[PYRH_MAX_DEPTH_RF], ec[PYRH_MAX_DEPTH_RF];
+  R lup[PYRH_MAX_DEPTH_RF], ldn[PYRH_MAX_DEPTH_RF];
+  for (int k = 0; k < nd; ++k) {
+    lup[k] = (k >= 1 && dT.dlen_up) ? R(dT.dlen_up[k] / mu) : R(0);
+    ldn[k] = (k >= 1 && dT.dlen_dn) ? R(dT.dlen_dn[k] / mu) : R(0);
+  }
+  R cc[PYRH_MAX_DEPTH_RF], ec[PYRH_MAX_DEPTH_RF], dcc[PYRH_MAX_DEPTH_RF], dec[PYRH_MAX_DEPTH_RF];
   for (int la = 0; la < nlam; ++la) {
     const double lm = lam[la];
     const double dlc = lm * kQ_WING * (vmicro_char / kCLIGHT);
@@ -115,6 +143,8 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     for (int k = 0; k < nd; ++k) {
       cc[k] = R(chi_c[(int64_t)la * nd + k]);
       ec[k] = R(eta_c[(int64_t)la * nd + k]);
+      dcc[k] = dT.dchi_c ? R(dT.dchi_c[(int64_t)la * nd + k]) : R(0);
+      dec[k] = dT.deta_c ? R(dT.deta_c[(int64_t)la * nd + k]) : R(0);
     }
     auto qop = [&](int k, R* q) {
       local_q<R, true>(nline, &ld[0][k], PYRH_MAX_DEPTH_RF, geo[k], dlam, inwin, ncomp, cs, cw, cq,
@@ -128,7 +158,7 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     R gfa[4 * PYRH_MAX_LINES];
     for (int e = 0; e < 4 * PYRH_MAX_LINES; ++e) gfa[e] = R(0);
     Emit<R, JAC> emit{nd, T, lm, rfl, nline, &ld[0][0], geo, dlam, inwin, ncomp, cs, cw, cq, cc, ec,
-                      &tape, gfa};
+                      &tape, gfa, dcc, dec, lup, ldn};
     delo_reverse_stream<R, 4>(tape, ds, nd, B0, B1, seed, emit);
     for (int s = 0; s < 4; ++s)
       for (int l = 0; l < nline; ++l) gfl[s * nline + l] = double(gfa[s * PYRH_MAX_LINES + l]);
@@ -147,6 +177,17 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
   nd, height, T, ne, nHtot, np, vturb, vel, B, gam, chb, line_pops, nline, lines, nlam, lam,  \
       chi_c, eta_c, mu, vmicro_char, stokes, rf, rf_gf
 
-extern "C" int rf_eval(RF_ARGS) { return rf_eval_t<double, false>(RF_PASS); }
-extern "C" int rf_eval_f32(RF_ARGS) { return rf_eval_t<float, false>(RF_PASS); }
-extern "C" int rf_eval_jac(RF_ARGS) { return rf_eval_t<double, true>(RF_PASS); }
+#define DT_ARGS                                                                              \
+  const double *dchi_c, const double *deta_c, const double *dline_pops, const double *dnp,    \
+      const double *dlen_up, const double *dlen_dn
+#define DT_PASS SetupDT{dchi_c, deta_c, dline_pops, dnp, dlen_up, dlen_dn}
+
+extern "C" int rf_eval(RF_ARGS) { return rf_eval_t<double, false>(RF_PASS, SetupDT{}); }
+extern "C" int rf_eval_f32(RF_ARGS) { return rf_eval_t<float, false>(RF_PASS, SetupDT{}); }
+extern "C" int rf_eval_jac(RF_ARGS) { return rf_eval_t<double, true>(RF_PASS, SetupDT{}); }
+// the same with the set-up's temperature derivatives (any of them NULL)
+extern "C" int rf_eval_dT(RF_ARGS, DT_ARGS) { return rf_eval_t<double, false>(RF_PASS, DT_PASS); }
+extern "C" int rf_eval_f32_dT(RF_ARGS, DT_ARGS) {
+  return rf_eval_t<float, false>(RF_PASS, DT_PASS);
+}
+extern "C" int rf_eval_jac_dT(RF_ARGS, DT_ARGS) { return rf_eval_t<double, true>(RF_PASS, DT_PASS); }

@@ -36,6 +36,32 @@ def test_struct_sizes_match_header_layout():
     # 14 doubles + 4 int32 + 32 int32 + 64 doubles
     assert C.sizeof(L.PyrhLine) == 14 * 8 + 4 * 4 + 32 * 4 + 64 * 8
     assert C.sizeof(L.PyrhLteConfig) == 4 * 4 + 2 * 8 + 2 * 4
+    # 3 int32 (+4 padding), 1 int64, 19 array pointers, the set-up derivative pointer
+    assert C.sizeof(L.PyrhLteBatch) == 16 + 8 + 20 * 8
+    assert L.PyrhLteBatch.setup_dT.offset == 16 + 8 + 19 * 8
+    assert C.sizeof(L.PyrhLteSetupDT) == 6 * 8
+
+
+def test_struct_layout_matches_compiled_header(tmp_path):
+    """sizeof/offsetof of the batch structs as a C compiler lays them out
+    from include/pyrh_gb300.h, against the ctypes mirror."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "pyrh_gb300.h"\n'
+                   'int main(void) { printf("%zu %zu %zu %zu\\n", sizeof(pyrh_lte_batch), '
+                   'offsetof(pyrh_lte_batch, setup_dT), sizeof(pyrh_lte_setup_dT), '
+                   'sizeof(pyrh_lte_config)); return 0; }\n')
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    assert got == [C.sizeof(L.PyrhLteBatch), L.PyrhLteBatch.setup_dT.offset,
+                   C.sizeof(L.PyrhLteSetupDT), C.sizeof(L.PyrhLteConfig)]
 
 
 def test_config_validation_without_gpu(golden):
