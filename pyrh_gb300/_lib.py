@@ -23,6 +23,13 @@ PYRH_FULL_STOKES = 3
 PYRH_MAX_LINES = 16
 PYRH_MAX_COMPONENTS = 32
 PYRH_MAX_DEPTH = 512
+PYRH_RF_NPARAM = 6
+PYRH_RF_MAX_DEPTH = 160
+PYRH_NLTE_MAX_LEVELS = 8
+PYRH_NLTE_MAX_ACTIVE = 16
+PYRH_NLTE_MAX_RAYS = 8
+PYRH_NLTE_MAX_DEPTH = 160
+PYRH_NLTE_MAX_NG = 4
 
 _D = C.POINTER(C.c_double)
 _I32 = C.POINTER(C.c_int32)

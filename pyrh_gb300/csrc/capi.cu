@@ -86,6 +86,20 @@ pyrh_status check_batch_shape(const pyrh_lte_batch* b, int nline) {
   return PYRH_OK;
 }
 
+// Dynamic shared memory a block of these kernels may use on the current
+// device: the opt-in maximum per block less 1 KB for static shared memory
+// (200 KB where the device cannot be queried).
+size_t smem_limit() {
+  int dev = 0, v = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+      v <= 2048) {
+    cudaGetLastError();
+    return 200 * 1024;
+  }
+  return (size_t)v - 1024;
+}
+
 pyrh::LteArgs make_args(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nline,
                         const pyrh_lte_config* cfg, void* out, int block) {
   pyrh::LteArgs a;
@@ -127,7 +141,7 @@ pyrh_status launch(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nline,
   const int block = default_block(b->max_nlam, cfg->block_lambda);
   pyrh::LteArgs a = make_args(b, d_lines, nline, cfg, out, block);
   const size_t smem = pyrh::lte_smem_bytes(cfg->precision, nline, a.maxd);
-  if (smem > 200 * 1024)
+  if (smem > smem_limit())
     return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
                 nline, a.maxd);
   // One block per (atmosphere, wavelength tile) by default: a block that
@@ -182,7 +196,7 @@ pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nli
   if (b->setup_dT) ra.dT = *b->setup_dT;
   else memset(&ra.dT, 0, sizeof(ra.dT));
   const size_t smem = pyrh::rf_smem_bytes(cfg->precision, nline, ra.lte.maxd);
-  if (smem > 200 * 1024)
+  if (smem > smem_limit())
     return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
                 nline, ra.lte.maxd);
   const long long work = (long long)ra.lte.natm * ra.lte.tiles;

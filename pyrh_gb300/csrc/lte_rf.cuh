@@ -210,12 +210,41 @@ PYRH_HD void humlicek_d(R a, R v, Cx<R>& W, Cx<R>& dW) {
 
 // ------------------------------------------- per-(line, depth) quantities --
 // Value and derivatives w.r.t. (T, v_los, v_mic, B, gamma, chi) of the
-// line quantities of one depth (kurucz.c:638-680, 745-783).
+// line quantities of one depth (kurucz.c:638-680, 745-783), stored compactly:
+// every one of them depends on T and v_mic (through the Doppler width, the
+// damping and the LTE strength); besides those, only the velocity shift
+// depends on v_los and only the Zeeman splitting on B, and none on the
+// field angles.  So a field keeps its value and two derivatives (DC), and
+// the two single-parameter derivatives are stored once: 20 numbers instead
+// of six full duals (42), which is what the shared-memory tables of the
+// response-function kernel hold per (line, depth).
+template <typename R>
+struct DC {
+  R v, dT, dvt;
+};
+
 template <typename R>
 struct LineDepth {
-  D6<R> inv_vb, vshift, adamp, vB, chil, etal;
-  bool gauss;  // Grad == 0
+  DC<R> inv_vb, vshift, adamp, vB, chil, etal;
+  R dvsh_dvel;   // d vshift / d v_los
+  R dvB_dB;      // d vB / d B
+  bool gauss;    // Grad == 0
 };
+
+// The full dual of a stored field (slot `extra` gets `dx`).
+template <typename R>
+PYRH_HD D6<R> expand(const DC<R>& c, int extra = -1, R dx = R(0)) {
+  D6<R> r = dconst(c.v);
+  r.d[0] = c.dT;
+  r.d[2] = c.dvt;
+  if (extra >= 0) r.d[extra] = dx;
+  return r;
+}
+
+template <typename R>
+PYRH_HD DC<R> compact(const D6<R>& a) {
+  return DC<R>{a.v, a.d[0], a.d[2]};
+}
 
 struct LineConstD {
   double lambda0, Ei, gi, Aji, Bji, Bij, Grad, GStark, GvdWaals, cross, alpha, isotope_frac,
@@ -233,7 +262,6 @@ template <typename R>
 PYRH_HD LineDepth<R> line_depth(const LineConstD& L, R T, R vel, R vturb, R B, R ne, R nHtot,
                                 R np, R nstage, R lnU, R muz, bool moving, R dn_dT = R(0),
                                 R dlnU_dT = R(0), R dnp_dT = R(0)) {
-  LineDepth<R> o;
   const D6<R> dT = dvar(T, 0), dv = dvar(vel, 1), dvt = dvar(vturb, 2), dB = dvar(B, 3);
   D6<R> nst = dconst(nstage), lnUd = dconst(lnU), npd = dconst(np);
   nst.d[0] = dn_dT;
@@ -242,21 +270,22 @@ PYRH_HD LineDepth<R> line_depth(const LineConstD& L, R T, R vel, R vturb, R B, R
   const R vtherm = R(2.0 * kKBOLTZMANN / (kAMU * L.weight));
   const D6<R> vb = dsqrt(vtherm * dT + dvt * dvt);
   const D6<R> one = dconst(R(1));
-  o.inv_vb = R(kCLIGHT / L.lambda0) * (one / vb);
-  o.vshift = moving ? muz * (dv / vb) : dconst(R(0));
+  const D6<R> inv_vb = R(kCLIGHT / L.lambda0) * (one / vb);
+  const D6<R> vshift = moving ? muz * (dv / vb) : dconst(R(0));
   const D6<R> sv = R(1.0 / kSQRTPI) * (one / vb);
-  o.gauss = (L.Grad == 0.0);
-  if (!o.gauss) {
+  const bool gauss = (L.Grad == 0.0);
+  D6<R> adamp;
+  if (!gauss) {
     D6<R> GvdW;
     if (L.vdwaals == 0) GvdW = R(L.cross) * dpow(dT, R(0.3));
     else if (L.vdwaals == 2) GvdW = R(L.cross) * dpow(dT, R((1.0 - L.alpha) / 2.0));
     else GvdW = dconst(R(L.GvdWaals));
     const D6<R> G = dconst(R(L.Grad + L.GStark * ne)) + (dconst(nHtot) - npd) * GvdW;
-    o.adamp = R(L.lambda0 * kNM_TO_M / (4.0 * kPI)) * (G / vb);
+    adamp = R(L.lambda0 * kNM_TO_M / (4.0 * kPI)) * (G / vb);
   } else {
-    o.adamp = dconst(R(-1));
+    adamp = dconst(R(-1));
   }
-  o.vB = R(kLARMOR * L.lambda0) * (dB / vb);
+  const D6<R> vBd = R(kLARMOR * L.lambda0) * (dB / vb);
   const R hc = R(kHPLANCK * kCLIGHT);
   const R hc_la = R(kHPLANCK * kCLIGHT / (L.lambda0 * kNM_TO_M));
   const R B4 = R(kHPLANCK * kCLIGHT / (4.0 * kPI) * L.Bij * L.isotope_frac * L.hyperfine_frac * L.gi);
@@ -264,8 +293,16 @@ PYRH_HD LineDepth<R> line_depth(const LineConstD& L, R T, R vel, R vturb, R B, R
   const D6<R> kT = one / (R(kKBOLTZMANN) * dT);
   const D6<R> ni = nst * dexp(dconst(R(0)) - lnUd - R(L.Ei) * kT);
   const D6<R> nj = ni * dexp(dconst(R(0)) - hc_la * kT);
-  o.chil = (B4 * (ni - nj)) * sv;
-  o.etal = ((B4 * tw) * nj) * sv;
+  LineDepth<R> o;
+  o.inv_vb = compact(inv_vb);
+  o.vshift = compact(vshift);
+  o.adamp = compact(adamp);
+  o.vB = compact(vBd);
+  o.chil = compact((B4 * (ni - nj)) * sv);
+  o.etal = compact(((B4 * tw) * nj) * sv);
+  o.dvsh_dvel = vshift.d[1];
+  o.dvB_dB = vBd.d[3];
+  o.gauss = gauss;
   (void)hc;
   return o;
 }
@@ -318,9 +355,13 @@ PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, int ld_stride, const
   D6<R> cI = dconst(R(0)), cQ = cI, cU = cI, cV = cI, eI = cI, eQ = cI, eU = cI, eV = cI;
   for (int l = 0; l < nline; ++l) {
     if (!((inwin >> l) & 1u)) continue;
-    const LineDepth<R>& L = ld[l * ld_stride];
+    const LineDepth<R>& Ls = ld[l * ld_stride];
+    struct {
+      D6<R> inv_vb, vshift, adamp, vB, chil, etal;
+    } L = {expand(Ls.inv_vb), expand(Ls.vshift, 1, Ls.dvsh_dvel), expand(Ls.adamp),
+           expand(Ls.vB, 3, Ls.dvB_dB), expand(Ls.chil), expand(Ls.etal)};
     const D6<R> v = dlam[l] * L.inv_vb + L.vshift;
-    if (L.gauss) {
+    if (Ls.gauss) {
       const D6<R> phi = (fabs(v.v) <= R(kMAX_GAUSS_DOPPLER)) ? dexp(dconst(R(0)) - v * v) : dconst(R(0));
       cI = cI + L.chil * phi;
       eI = eI + L.etal * phi;
@@ -560,10 +601,16 @@ PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const
         gb[s][3] += fV * dV;
       }
     }
-    for (int s = 0; s < NS; ++s)
-      for (int x = 0; x < kNX; ++x)
-        out[s][x] += ab[s] * L.adamp.d[x] + vb[s] * (dlam[l] * L.inv_vb.d[x] + L.vshift.d[x]) +
-                     vBb[s] * L.vB.d[x] + chilb[s] * L.chil.d[x] + etalb[s] * L.etal.d[x];
+    // the line quantities depend on T and v_mic (slots 0 and 2), the shift
+    // also on v_los (1) and the splitting also on B (3)
+    for (int s = 0; s < NS; ++s) {
+      out[s][0] += ab[s] * L.adamp.dT + vb[s] * (dlam[l] * L.inv_vb.dT + L.vshift.dT) +
+                   vBb[s] * L.vB.dT + chilb[s] * L.chil.dT + etalb[s] * L.etal.dT;
+      out[s][2] += ab[s] * L.adamp.dvt + vb[s] * (dlam[l] * L.inv_vb.dvt + L.vshift.dvt) +
+                   vBb[s] * L.vB.dvt + chilb[s] * L.chil.dvt + etalb[s] * L.etal.dvt;
+      out[s][1] += vb[s] * L.dvsh_dvel;
+      out[s][3] += vBb[s] * L.dvB_dB;
+    }
     if (gf)
       for (int s = 0; s < NS; ++s)
         gf[s * PYRH_MAX_LINES + l] +=

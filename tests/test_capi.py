@@ -42,6 +42,20 @@ def test_struct_sizes_match_header_layout():
     assert C.sizeof(L.PyrhLteSetupDT) == 6 * 8
 
 
+def test_constants_match_header():
+    """Every numeric #define of include/pyrh_gb300.h that the Python layer
+    mirrors has the header's value."""
+    hdr = open(os.path.join(REPO, "include", "pyrh_gb300.h")).read()
+    defines = dict(re.findall(r"#define\s+(PYRH_\w+)\s+(\d+)\b", hdr))
+    enums = dict(re.findall(r"\b(PYRH_\w+)\s*=\s*(\d+)", hdr))
+    mirrored = {k: getattr(L, k) for k in dir(L) if k.startswith("PYRH_")
+                and isinstance(getattr(L, k), int)}
+    assert mirrored
+    for k, v in mirrored.items():
+        assert k in defines or k in enums, k
+        assert int(defines.get(k, enums.get(k))) == v, k
+
+
 def test_struct_layout_matches_compiled_header(tmp_path):
     """sizeof/offsetof of the batch structs as a C compiler lays them out
     from include/pyrh_gb300.h, against the ctypes mirror."""
