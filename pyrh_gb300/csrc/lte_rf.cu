@@ -126,12 +126,34 @@ struct Emit {
   R* rf;             // mode 0: rf_out + 24 * cont_off + la
   R* gf;             // per-thread log gf accumulators [NS][PYRH_MAX_LINES] or nullptr
   const Tape<R>* tp;
+  const FeautAdj<R>* fa;   // lanes with no line in window: the Feautrier adjoint
+                           // of the Stokes I seed (their DELO seeds are zero)
   // k: the depth handed over; qb: dL_s/dq_k; bpl: dL_s/dB_k of the Planck
   // boundary; sdn, sup: dL_s/d ds_k and dL_s/d ds_{k+1} (path lengths)
-  __device__ void operator()(int k, const R* qb, const R* bpl, const R* sdn,
-                             const R* sup) const {
+  __device__ void operator()(int k, const R* qb_in, const R* bpl_in, const R* sdn_in,
+                             const R* sup_in) const {
     constexpr int NS = MODE == 0 ? 4 : 1;
     const RfSmem<R>& sm = *loc->sm;
+    // Feautrier lanes take their own adjoints; selected by value so that
+    // every lane reaches the warp sums below together
+    R qb[NS * 8], bpl[NS], sdn[NS], sup[NS];
+#pragma unroll
+    for (int e = 0; e < NS * 8; ++e) qb[e] = qb_in[e];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      bpl[s] = bpl_in[s];
+      sdn[s] = sdn_in[s];
+      sup[s] = sup_in[s];
+    }
+    if (fa) {
+#pragma unroll
+      for (int e = 0; e < NS * 8; ++e) qb[e] = R(0);
+      qb[0] = fa->chib[k];
+      qb[1] = fa->Sb[k];
+      bpl[0] = (k == nd - 2) ? fa->B0b : (k == nd - 1) ? fa->B1b : R(0);
+      sdn[0] = fa->dsb[k];
+      sup[0] = (k + 1 < nd) ? fa->dsb[k + 1] : R(0);
+    }
     R g[NS][kNX];
 #pragma unroll
     for (int s = 0; s < NS; ++s)
@@ -272,6 +294,14 @@ lte_rf_kernel(RfArgs ra) {
       const double B1 = planck(args.T[doff + nd - 1], lam);
       R st[4];
       delo_forward<R>(tp, sm.ds, nd, B0, B1, st, qop);
+      // no line inside its window: the reference's Feautrier solution
+      const bool feaut = loc.inwin == 0u;
+      FeautTape<R> ftape;
+      FeautAdj<R> fadj;
+      if (feaut) {
+        st[0] = feautrier_fwd<R>(tp, sm.ds, nd, B0, B1, ftape);
+        st[1] = st[2] = st[3] = R(0);
+      }
       R* out = static_cast<R*>(args.out) + 4 * loff;
       if (act)
 #pragma unroll
@@ -292,9 +322,12 @@ lte_rf_kernel(RfArgs ra) {
       em.nl = nl;
       em.la = la;
       em.act = act;
+      em.fa = feaut ? &fadj : nullptr;
       if (MODE == 0) {
         em.rf = static_cast<R*>(ra.rf) + 24 * args.cont_off[p] + la;
-        const R seed[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+        const R one = feaut ? R(0) : R(1);
+        const R seed[4][4] = {{one, 0, 0, 0}, {0, one, 0, 0}, {0, 0, one, 0}, {0, 0, 0, one}};
+        if (feaut) feautrier_vjp<R>(tp, sm.ds, nd, B0, B1, ftape, R(1), fadj);
         delo_reverse_stream<R, 4>(tp, sm.ds, nd, B0, B1, seed, em);
         if (want_gf && act) {
           R* o = static_cast<R*>(ra.rf_gf) + (int64_t)4 * nline * loff + la;
@@ -308,6 +341,11 @@ lte_rf_kernel(RfArgs ra) {
         R seed[1][4];
 #pragma unroll
         for (int s = 0; s < 4; ++s) seed[0][s] = act ? dL[(int64_t)s * nl + la] : R(0);
+        if (feaut) {
+          feautrier_vjp<R>(tp, sm.ds, nd, B0, B1, ftape, seed[0][0], fadj);
+#pragma unroll
+          for (int s = 0; s < 4; ++s) seed[0][s] = R(0);
+        }
         delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
         if (want_gf) gf_block_sum(gfacc, nline, sm.gfs);
       } else {
@@ -326,6 +364,11 @@ lte_rf_kernel(RfArgs ra) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) c2 += __shfl_xor_sync(0xffffffffu, c2, o);
         if ((threadIdx.x & 31u) == 0) atomicAdd(sm.chi2, c2);
+        if (feaut) {
+          feautrier_vjp<R>(tp, sm.ds, nd, B0, B1, ftape, seed[0][0], fadj);
+#pragma unroll
+          for (int s = 0; s < 4; ++s) seed[0][s] = R(0);
+        }
         delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
         if (want_gf) gf_block_sum(gfacc, nline, sm.gfs);
       }

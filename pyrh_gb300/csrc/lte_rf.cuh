@@ -1229,6 +1229,138 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
   emit(N - 1, &qc[0][0], bpl[1], sc, zero_b);
 }
 
+// ------------------------------------------ Feautrier (no line in window) --
+// Where no line is inside its window the reference solves the unpolarized
+// transfer equation with second-order Feautrier (rh/rhf1d/feautrier.c:56-202,
+// ZERO top and THERMALIZED bottom), not DELO-Bezier3; the two differ by
+// ~3e-3 of I there.  feautrier_fwd repeats the synthesis kernel's one-pass
+// bottom-up elimination (solve_feautrier in lte_stokes.cu) on the optical
+// quantities the forward sweep taped (chi = q[0], S = q[1]) and keeps its
+// recurrence (G_k, y_k, dtau_k); feautrier_vjp runs the adjoint of that
+// elimination top-down and returns dL/dchi_k, dL/dS_k, dL/d ds_k (path
+// lengths) and dL/dB of the two bottom Planck values, for dL/dI_0 = Ib.
+template <typename R>
+struct FeautTape {
+  R G[PYRH_MAX_DEPTH_RF], y[PYRH_MAX_DEPTH_RF], dtau[PYRH_MAX_DEPTH_RF];
+};
+
+template <typename R>
+struct FeautAdj {
+  R chib[PYRH_MAX_DEPTH_RF], Sb[PYRH_MAX_DEPTH_RF], dsb[PYRH_MAX_DEPTH_RF];
+  R B0b, B1b;
+};
+
+// Out of line on the device: it runs once per thread at most, and keeping
+// it out of the kernel body keeps that body's instruction footprint small.
+#ifdef __CUDA_ARCH__
+#define PYRH_COLD __host__ __device__ __noinline__
+#else
+#define PYRH_COLD inline
+#endif
+
+template <typename R>
+PYRH_COLD R feautrier_fwd(const Tape<R>& tp, const R* ds, int N, double B0, double B1,
+                          FeautTape<R>& ft) {
+  for (int k = 0; k < N - 1; ++k)
+    ft.dtau[k] = R(0.5) * (tp.q[k][0] + tp.q[k + 1][0]) * ds[k + 1];
+  R dtb = ft.dtau[N - 2];
+  const R hN = R(B1 - (B0 - B1) / (double)dtb);
+  const R abcN = R(1) + R(2) / dtb;
+  const R A1N = R(2) / (dtb * dtb);
+  R G = abcN / A1N;
+  R y = (tp.q[N - 1][1] + R(2) * hN / dtb) / (abcN + A1N);
+  ft.G[N - 1] = G;
+  ft.y[N - 1] = y;
+  for (int k = N - 2; k >= 1; --k) {
+    const R dta = ft.dtau[k - 1];
+    dtb = ft.dtau[k];
+    const R dmid = R(0.5) * (dtb + dta);
+    const R A1 = R(1) / (dmid * dta), C1 = R(1) / (dmid * dtb);
+    const R Gn = (R(1) + C1 * G / (R(1) + G)) / A1;
+    y = (tp.q[k][1] + C1 * y) / (A1 * (R(1) + Gn));
+    G = Gn;
+    ft.G[k] = G;
+    ft.y[k] = y;
+  }
+  const R dt0 = ft.dtau[0];
+  const R abc0 = R(1) + R(2) / dt0, C10 = R(2) / (dt0 * dt0);
+  const R P0 = (tp.q[0][1] + C10 * y) / (abc0 + C10 * G / (R(1) + G));
+  return R(2) * P0;
+}
+
+template <typename R>
+PYRH_COLD void feautrier_vjp(const Tape<R>& tp, const R* ds, int N, double B0, double B1,
+                             const FeautTape<R>& ft, R Ib, FeautAdj<R>& fa) {
+  R dtb_adj[PYRH_MAX_DEPTH_RF];
+  for (int k = 0; k < N; ++k) fa.chib[k] = fa.Sb[k] = fa.dsb[k] = dtb_adj[k] = R(0);
+  // top row: P0 = (S_0 + C10 y_1) / (abc0 + C10 g(G_1)), g(G) = G / (1 + G)
+  R Gb, yb;
+  {
+    const R dt0 = ft.dtau[0], G1 = ft.G[1], y1 = ft.y[1];
+    const R abc0 = R(1) + R(2) / dt0, C10 = R(2) / (dt0 * dt0);
+    const R g1 = G1 / (R(1) + G1);
+    const R den = abc0 + C10 * g1;
+    const R P0 = (tp.q[0][1] + C10 * y1) / den;
+    const R P0b = R(2) * Ib;
+    const R numb = P0b / den, denb = -P0b * P0 / den;
+    fa.Sb[0] += numb;
+    const R C10b = numb * y1 + denb * g1;
+    yb = numb * C10;
+    Gb = denb * C10 / ((R(1) + G1) * (R(1) + G1));
+    dtb_adj[0] += denb * (-R(2) / (dt0 * dt0)) + C10b * (-R(4) / (dt0 * dt0 * dt0));
+  }
+  // interior rows, top-down: step k made (G_k, y_k) from (G_{k+1}, y_{k+1})
+  for (int k = 1; k <= N - 2; ++k) {
+    const R dta = ft.dtau[k - 1], dtb = ft.dtau[k];
+    const R dmid = R(0.5) * (dtb + dta);
+    const R A1 = R(1) / (dmid * dta), C1 = R(1) / (dmid * dtb);
+    const R Gk = ft.G[k], yk = ft.y[k], G = ft.G[k + 1], y = ft.y[k + 1];
+    const R g = G / (R(1) + G);
+    const R D = A1 * (R(1) + Gk);
+    const R Nb = yb / D, Db = -yb * yk / D;
+    fa.Sb[k] += Nb;
+    R C1b = Nb * y;
+    const R ynb = Nb * C1;
+    R A1b = Db * (R(1) + Gk);
+    const R Gkb = Gb + Db * A1;
+    const R Mb = Gkb / A1;
+    A1b -= Gkb * Gk / A1;
+    C1b += Mb * g;
+    const R Gnb = Mb * C1 / ((R(1) + G) * (R(1) + G));
+    const R dmidb = -(A1b * A1 + C1b * C1) / dmid;
+    dtb_adj[k - 1] += -A1b * A1 / dta + R(0.5) * dmidb;
+    dtb_adj[k] += -C1b * C1 / dtb + R(0.5) * dmidb;
+    Gb = Gnb;
+    yb = ynb;
+  }
+  // bottom row: G = abcN / A1N, y = (S + 2 hN / dtb) / (abcN + A1N)
+  {
+    const R dtb = ft.dtau[N - 2];
+    const double hNd = B1 - (B0 - B1) / (double)dtb;
+    const R hN = R(hNd);
+    const R abcN = R(1) + R(2) / dtb, A1N = R(2) / (dtb * dtb);
+    const R den = abcN + A1N;
+    const R y = ft.y[N - 1], G = ft.G[N - 1];
+    const R numb = yb / den, denb = -yb * y / den;
+    fa.Sb[N - 1] += numb;
+    const R hNb = numb * R(2) / dtb;
+    R dtbb = numb * (-R(2) * hN / (dtb * dtb));
+    const R abcNb = denb + Gb / A1N, A1Nb = denb - Gb * G / A1N;
+    dtbb += abcNb * (-R(2) / (dtb * dtb)) + A1Nb * (-R(4) / (dtb * dtb * dtb));
+    fa.B1b = R((double)hNb * (1.0 + 1.0 / (double)dtb));
+    fa.B0b = R(-(double)hNb / (double)dtb);
+    dtbb += R((double)hNb * (B0 - B1) / ((double)dtb * (double)dtb));
+    dtb_adj[N - 2] += dtbb;
+  }
+  // dtau_k = (chi_k + chi_{k+1}) ds_{k+1} / 2
+  for (int k = 0; k < N - 1; ++k) {
+    const R a = R(0.5) * dtb_adj[k];
+    fa.chib[k] += a * ds[k + 1];
+    fa.chib[k + 1] += a * ds[k + 1];
+    fa.dsb[k + 1] += a * (tp.q[k][0] + tp.q[k + 1][0]);
+  }
+}
+
 // dB_nu/dT of planck() (planck.c:38-63)
 PYRH_HD double planck_dT(double T, double lambda) {
   const double hc_kla = (kHPLANCK * kCLIGHT) / (kKBOLTZMANN * kNM_TO_M * lambda);

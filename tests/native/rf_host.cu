@@ -42,7 +42,23 @@ struct Emit {
   R* gf;                    // [4][PYRH_MAX_LINES] log gf accumulators
   const R *dchi_c, *deta_c; // [depth] at this wavelength, or nullptr
   const R *len_up, *len_dn; // [depth] d ds_k/dT_{k-1}, d ds_k/dT_k
-  void operator()(int k, const R* qb, const R* bpl, const R* sdn, const R* sup) const {
+  const FeautAdj<R>* fa;    // no line in window: the Feautrier adjoint of the I seed
+  void operator()(int k, const R* qb_in, const R* bpl_in, const R* sdn_in,
+                  const R* sup_in) const {
+    R qb[32], bpl[4], sdn[4], sup[4];
+    for (int e = 0; e < 32; ++e) qb[e] = fa ? R(0) : qb_in[e];
+    for (int s = 0; s < 4; ++s) {
+      bpl[s] = fa ? R(0) : bpl_in[s];
+      sdn[s] = fa ? R(0) : sdn_in[s];
+      sup[s] = fa ? R(0) : sup_in[s];
+    }
+    if (fa) {
+      qb[0] = fa->chib[k];
+      qb[1] = fa->Sb[k];
+      bpl[0] = (k == nd - 2) ? fa->B0b : (k == nd - 1) ? fa->B1b : R(0);
+      sdn[0] = fa->dsb[k];
+      sup[0] = (k + 1 < nd) ? fa->dsb[k + 1] : R(0);
+    }
     R g[4][kNX];
     if (JAC) {
       R q[8], J[8][kNX];
@@ -139,7 +155,7 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     memset(rfl, 0, sizeof(double) * 4 * kNX * nd);
     double* gfl = rf_gf + (int64_t)la * 4 * nline;
     for (int e = 0; e < 4 * nline; ++e) gfl[e] = 0.0;
-    if (!pol) { for (int s = 0; s < 4; ++s) stokes[la * 4 + s] = 0.0; continue; }
+    (void)pol;   // without a line in window (inwin == 0): Feautrier below
     for (int k = 0; k < nd; ++k) {
       cc[k] = R(chi_c[(int64_t)la * nd + k]);
       ec[k] = R(eta_c[(int64_t)la * nd + k]);
@@ -153,12 +169,21 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     const double B0 = planck(T[nd - 2], lm), B1 = planck(T[nd - 1], lm);
     R out[4];
     delo_forward<R>(tape, ds, nd, B0, B1, out, qop);
+    static FeautTape<R> ft;
+    static FeautAdj<R> fadj;
+    const bool feaut = inwin == 0u;
+    if (feaut) {
+      out[0] = feautrier_fwd<R>(tape, ds, nd, B0, B1, ft);
+      out[1] = out[2] = out[3] = R(0);
+      feautrier_vjp<R>(tape, ds, nd, B0, B1, ft, R(1), fadj);
+    }
     for (int s = 0; s < 4; ++s) stokes[la * 4 + s] = double(out[s]);
-    const R seed[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+    const R one = feaut ? R(0) : R(1);
+    const R seed[4][4] = {{one, 0, 0, 0}, {0, one, 0, 0}, {0, 0, one, 0}, {0, 0, 0, one}};
     R gfa[4 * PYRH_MAX_LINES];
     for (int e = 0; e < 4 * PYRH_MAX_LINES; ++e) gfa[e] = R(0);
     Emit<R, JAC> emit{nd, T, lm, rfl, nline, &ld[0][0], geo, dlam, inwin, ncomp, cs, cw, cq, cc, ec,
-                      &tape, gfa, dcc, dec, lup, ldn};
+                      &tape, gfa, dcc, dec, lup, ldn, feaut ? &fadj : nullptr};
     delo_reverse_stream<R, 4>(tape, ds, nd, B0, B1, seed, emit);
     for (int s = 0; s < 4; ++s)
       for (int l = 0; l < nline; ++l) gfl[s * nline + l] = double(gfa[s * PYRH_MAX_LINES + l]);

@@ -75,7 +75,7 @@ def contract_err(got, seed, rf):
 def test_rf_matches_cpu_adjoint(rf_harness, golden, name, precision):
     fx = golden(name)
     _, _, st, rfs = gpu_rf([fx], precision)
-    win = delo_wavelengths(fx)
+    win = np.arange(len(fx["lam"]))       # DELO-Bezier3 and Feautrier wavelengths
     st_h, rf_h = rf_eval(rf_harness, fx, win)
     ref = rf_h.transpose(1, 2, 3, 0)                  # [4, 6, nd, nsel]
     mine = rfs[0][..., win]
@@ -92,15 +92,16 @@ def test_rf_matches_cpu_adjoint(rf_harness, golden, name, precision):
 @pytest.mark.parametrize("precision,tol", [(FP64, 1e-9), (FP32, 1e-5)])
 def test_rf_stokes_equal_forward_kernel(golden, precision, tol):
     """The RF kernel's forward sweep gives the synthesis kernel's spectra at
-    every DELO-Bezier3 wavelength."""
+    every wavelength: DELO-Bezier3 where a line is in its window, Feautrier
+    elsewhere (lte_edge has four such wavelengths, every case LAMBDA_REF)."""
     b = golden("lte_batch")
-    atms = [batch_member(b, i) for i in range(b["T"].shape[0])]
+    atms = [batch_member(b, i) for i in range(b["T"].shape[0])] + [golden("lte_edge")]
+    atms[-1] = dict(atms[-1], mu=atms[0]["mu"])     # one ray per batch
     dev, cfg, st, _ = gpu_rf(atms, precision)
     dev.run(cfg)
     fwd = lte.split_output(dev.pk, dev.out.cpu().numpy())
     for p, fx in enumerate(atms):
-        win = delo_wavelengths(fx)
-        assert np.abs(st[p][:, win] - fwd[p][:, win]).max() <= tol * fwd[p][0].max()
+        assert np.abs(st[p] - fwd[p]).max() <= tol * fwd[p][0].max()
 
 
 def test_rf_ragged_batch_equals_single(golden):
