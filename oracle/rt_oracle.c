@@ -28,6 +28,7 @@
 #include <string.h>
 
 #include "rt_oracle.h"
+#include "nlte_oracle.h"
 
 /* Physical constants as the reference defines them (rh/constant.h:28-68). */
 #define CLIGHT      2.99792458E+08
@@ -135,11 +136,10 @@ static double rlk_profile(const double *L, const double *zq, const double *zs,
                  (L[RLK_LAMBDA0] * NM_TO_M) / (4.0 * PI * vbroad);
 
   if (!(int) L[RLK_POLARIZABLE]) {
-    /* The reference evaluates Armstrong's Voigt here (kurucz.c:824); only
-       polarizable lines are supported by this oracle. */
-    double H;
-    oracle_humlicek(adamp, v, &H, NULL);
-    return H * sv;
+    /* unpolarizable line: Armstrong's Voigt function, no Zeeman splitting
+       (kurucz.c:824; the restatement of rh/voigt.c:126-243 is in
+       nlte_oracle.c) */
+    return oracle_voigt_armstrong(adamp, v) * sv;
   }
   double sin2g = 1.0 - d->cos_gamma * d->cos_gamma;
   double vB = (LARMOR * L[RLK_LAMBDA0]) * d->B / vbroad;

@@ -10,7 +10,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpyrh_gb300.so")
-UNITS = ["capi.cu", "lte_stokes.cu", "lte_rf.cu", "nlte.cu", "nlte_capi.cu"]
+# the response-function kernels: one unit per precision and mode, so that
+# the largest instantiations compile in parallel
+UNITS = ["capi.cu", "lte_stokes.cu", "lte_rf.cu"] + \
+    [f"lte_rf_fp{p}_{m}.cu" for p in ("32", "64") for m in ("rf", "chi2", "vjp")] + \
+    ["nlte.cu", "nlte_capi.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

@@ -40,10 +40,6 @@ pyrh_status check_lines_host(const pyrh_line* lines, int nline, int stokes_mode)
                   PYRH_MAX_COMPONENTS);
     if (!(L.lambda0 > 0.0) || !(L.weight > 0.0) || !(L.Bji > 0.0))
       return fail(PYRH_ERR_ARG, "line %d: non-positive lambda0, weight or Bji", l);
-    if (L.contributes && !L.polarizable && L.Grad != 0.0)
-      return fail(PYRH_ERR_UNSUPPORTED,
-                  "line %d is not polarizable: the reference evaluates it with "
-                  "Armstrong's Voigt function (kurucz.c:824), not implemented", l);
     for (int c = 0; c < L.ncomp; ++c)
       if (L.comp_q[c] < -1 || L.comp_q[c] > 1)
         return fail(PYRH_ERR_ARG, "line %d component %d: q = %d", l, c, L.comp_q[c]);

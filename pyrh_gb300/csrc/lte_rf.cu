@@ -1,420 +1,44 @@
-// lte_rf.cu -- response functions and chi^2 gradient of the LTE Stokes
-// synthesis on the GPU.
-//
-// One thread owns one (atmosphere, wavelength) pair, as in lte_stokes.cu.
-// Per block (one atmosphere, one tile of wavelengths) the per-(line, depth)
-// quantities and the projected field geometry are computed once, in the
-// working precision, with their derivatives with respect to (T, v_los,
-// v_mic, B, gamma, chi) of the same depth, into shared memory (forward-mode
-// dual numbers, lte_rf.cuh).  Each thread then
-//   1. runs the DELO-Bezier3 recurrence (bezier_1D.c:52-300) to the surface,
-//      evaluating the optical quantities q_k = (chi, S_I..S_V, K'_Q..K'_V) of
-//      its wavelength two depths ahead of their first use, and writes the
-//      recurrence state to a thread-private tape (local memory; depth-major,
-//      so the tape words of a warp's threads are interleaved and coalesce);
-//   2. runs the hand-written adjoint of that recurrence back down
-//      (delo_reverse_stream), which hands over dL/dq_k as soon as depth k is
-//      final;
-//   3. at each handed-over depth, carries dL/dq_k backwards through the
-//      opacity of that depth (local_q_vjp: through the line sums to the
-//      per-line primitives, whose derivatives with respect to the parameters
-//      are the dual parts in shared memory; the Zeeman profile sums and their
-//      derivatives were evaluated once by the forward sweep and taped) and writes
-//      dL/dx_k: for response functions the four
-//      Stokes seeds give RF[s][x][k] (written wavelength-fastest, coalesced);
-//      for the chi^2 gradient the single seed 2 w (S - obs), and for a
-//      vector-Jacobian product the caller's dL/dS, give one value per
-//      (x, k), summed over the block's wavelengths in shared memory and then
-//      added to the atmosphere's gradient in HBM.
-// With the set-up's temperature derivatives (RfArgs::dT), the temperature
-// slot also collects the continuum, population and path-length terms (the
-// reference's finite-difference response functions re-run the set-up for
-// every perturbed temperature, rf_ray.c:257-283).
-// The tape holds 21 values per depth plus the Zeeman profile sums of the
-// first kZLines lines; four depths of adjoints are live at a time.
+// lte_rf.cu -- shared-memory sizing and launch of the response-function
+// kernels (lte_rf_kernel.cuh), whose instantiations live in
+// lte_rf_fp{32,64}_{rf,chi2,vjp}.cu.
 #include <cuda_runtime.h>
-#include <stdint.h>
 
 #include "../../include/pyrh_gb300.h"
-#include "lte_rf.cuh"
 #include "lte_stokes.cuh"
 
 namespace pyrh {
 
-namespace {
-
-template <typename R>
-struct RfSmem {
-  LineDepth<R>* ld;   // [nline][maxd]
-  GeoD<R>* geo;       // [maxd]
-  R* ds;              // [maxd]
-  R* cshift;          // [nline][PYRH_MAX_COMPONENTS]
-  R* cweight;
-  int* cq;
-  int* ncomp;         // [nline]
-  int* contrib;       // [nline]
-  int* polar;         // [nline]
-  double* lam0;       // [nline]
-  R* grad;            // [kNX][maxd] (chi^2 mode)
-  R* len_up;          // [maxd] d ds_k/dT_{k-1} (k >= 1; ds includes 1/mu), or zeros
-  R* len_dn;          // [maxd] d ds_k/dT_k
-  R* chi2;            // [1]
-  R* gfs;             // [nline] log gf gradient of the block (modes 1-2)
-};
-
-__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
-
-template <typename R>
-__host__ __device__ size_t rf_smem_t(int nline, int maxd, RfSmem<R>* s, unsigned char* base) {
-  size_t off = 0;
-  auto take = [&](size_t bytes) {
-    unsigned char* p = base ? base + off : nullptr;
-    off = align16(off + bytes);
-    return p;
-  };
-  unsigned char* p;
-  p = take(sizeof(LineDepth<R>) * nline * maxd); if (s) s->ld = reinterpret_cast<LineDepth<R>*>(p);
-  p = take(sizeof(GeoD<R>) * maxd);              if (s) s->geo = reinterpret_cast<GeoD<R>*>(p);
-  p = take(sizeof(R) * maxd);                    if (s) s->ds = reinterpret_cast<R*>(p);
-  p = take(sizeof(R) * nline * PYRH_MAX_COMPONENTS);   if (s) s->cshift = reinterpret_cast<R*>(p);
-  p = take(sizeof(R) * nline * PYRH_MAX_COMPONENTS);   if (s) s->cweight = reinterpret_cast<R*>(p);
-  p = take(sizeof(int) * nline * PYRH_MAX_COMPONENTS); if (s) s->cq = reinterpret_cast<int*>(p);
-  p = take(sizeof(int) * nline);                 if (s) s->ncomp = reinterpret_cast<int*>(p);
-  p = take(sizeof(int) * nline);                 if (s) s->contrib = reinterpret_cast<int*>(p);
-  p = take(sizeof(int) * nline);                 if (s) s->polar = reinterpret_cast<int*>(p);
-  p = take(sizeof(double) * nline);              if (s) s->lam0 = reinterpret_cast<double*>(p);
-  p = take(sizeof(R) * kNX * maxd);              if (s) s->grad = reinterpret_cast<R*>(p);
-  p = take(sizeof(R) * maxd);                    if (s) s->len_up = reinterpret_cast<R*>(p);
-  p = take(sizeof(R) * maxd);                    if (s) s->len_dn = reinterpret_cast<R*>(p);
-  p = take(sizeof(R) * 4);                       if (s) s->chi2 = reinterpret_cast<R*>(p);
-  p = take(sizeof(R) * (nline > 0 ? nline : 1)); if (s) s->gfs = reinterpret_cast<R*>(p);
-  return off;
-}
-
-// What one thread needs to evaluate q and dq/dx at any depth.
-template <typename R>
-struct Local {
-  const RfSmem<R>* sm;
-  int nline, maxd, nl;
-  unsigned inwin;
-  R dlam[PYRH_MAX_LINES];
-  const R* chi_c;   // continuum of this (atmosphere, wavelength): index k * nl
-  const R* eta_c;
-  const R* dchi_c;  // their temperature derivatives, or nullptr (held fixed)
-  const R* deta_c;
-};
-
-// Sum of every thread's per-line log gf gradient over the warp (shuffles)
-// and the block (one shared atomic per warp and line).
-template <typename R>
-__device__ void gf_block_sum(const R* gfacc, int nline, R* gfs) {
-  for (int l = 0; l < nline; ++l) {
-    R v = gfacc[l];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31u) == 0) atomicAdd(&gfs[l], v);
-  }
-}
-
-template <typename R, int MODE>
-struct Emit {
-  const Local<R>* loc;
-  const double* T;   // temperatures of this atmosphere
-  double lam;
-  int nd, nl, la;
-  bool act;          // this lane holds a wavelength (writes and seeds)
-  R* rf;             // mode 0: rf_out + 24 * cont_off + la
-  R* gf;             // per-thread log gf accumulators [NS][PYRH_MAX_LINES] or nullptr
-  const Tape<R>* tp;
-  const FeautAdj<R>* fa;   // lanes with no line in window: the Feautrier adjoint
-                           // of the Stokes I seed (their DELO seeds are zero)
-  // k: the depth handed over; qb: dL_s/dq_k; bpl: dL_s/dB_k of the Planck
-  // boundary; sdn, sup: dL_s/d ds_k and dL_s/d ds_{k+1} (path lengths)
-  __device__ void operator()(int k, const R* qb_in, const R* bpl_in, const R* sdn_in,
-                             const R* sup_in) const {
-    constexpr int NS = MODE == 0 ? 4 : 1;
-    const RfSmem<R>& sm = *loc->sm;
-    // Feautrier lanes take their own adjoints; selected by value so that
-    // every lane reaches the warp sums below together
-    R qb[NS * 8], bpl[NS], sdn[NS], sup[NS];
-#pragma unroll
-    for (int e = 0; e < NS * 8; ++e) qb[e] = qb_in[e];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) {
-      bpl[s] = bpl_in[s];
-      sdn[s] = sdn_in[s];
-      sup[s] = sup_in[s];
-    }
-    if (fa) {
-#pragma unroll
-      for (int e = 0; e < NS * 8; ++e) qb[e] = R(0);
-      qb[0] = fa->chib[k];
-      qb[1] = fa->Sb[k];
-      bpl[0] = (k == nd - 2) ? fa->B0b : (k == nd - 1) ? fa->B1b : R(0);
-      sdn[0] = fa->dsb[k];
-      sup[0] = (k + 1 < nd) ? fa->dsb[k + 1] : R(0);
-    }
-    R g[NS][kNX];
-#pragma unroll
-    for (int s = 0; s < NS; ++s)
-#pragma unroll
-      for (int x = 0; x < kNX; ++x) g[s][x] = R(0);
-    local_q_vjp<R, NS>(loc->nline, sm.ld + k, loc->maxd, sm.geo[k], loc->dlam, loc->inwin,
-                       sm.ncomp, sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS, tp->q[k], qb,
-                       g, gf, tp->z[k], loc->dchi_c ? loc->dchi_c[(int64_t)k * nl] : R(0),
-                       loc->deta_c ? loc->deta_c[(int64_t)k * nl] : R(0));
-    const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lam)) : R(0);
-    const R ldn = sm.len_dn[k], lup = (k + 1 < nd) ? sm.len_up[k + 1] : R(0);
-#pragma unroll
-    for (int s = 0; s < NS; ++s) {
-#pragma unroll
-      for (int x = 0; x < kNX; ++x) {
-        R v = g[s][x];
-        if (x == 0) v += bpl[s] * dB + sdn[s] * ldn + sup[s] * lup;
-        if (MODE == 0) {
-          if (act) rf[((int64_t)(s * kNX + x) * nd + k) * nl] = v;
-        } else {   // modes 1 and 2: sum over the warp's wavelengths first
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-          if ((threadIdx.x & 31u) == 0) atomicAdd(&sm.grad[x * loc->maxd + k], v);
-        }
-      }
-    }
-  }
-};
-
-// Single-seed modes in FP32 are capped at 128 registers (4 blocks of 128
-// threads per SM): measured 31.5 ms against 35.8 ms uncapped for the
-// gradient of 4096 atmospheres x 224 wavelengths.
-template <typename R, int MODE>
-__global__ void __launch_bounds__(128, (sizeof(R) == 4 && MODE != 0) ? 4 : 1)
-lte_rf_kernel(RfArgs ra) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const LteArgs& args = ra.lte;
-  const int nline = args.nline < PYRH_MAX_LINES ? args.nline : PYRH_MAX_LINES;
-  RfSmem<R> sm;
-  rf_smem_t<R>(nline, args.maxd, &sm, smem_raw);
-  const int BL = blockDim.x;
-
-  for (int i = threadIdx.x; i < nline * PYRH_MAX_COMPONENTS; i += BL) {
-    const int l = i / PYRH_MAX_COMPONENTS, c = i % PYRH_MAX_COMPONENTS;
-    const pyrh_line& L = args.lines[l];
-    sm.cshift[i] = R(L.comp_shift[c]);
-    sm.cweight[i] = R(L.comp_strength[c]);
-    sm.cq[i] = L.comp_q[c];
-  }
-  for (int l = threadIdx.x; l < nline; l += BL) {
-    const pyrh_line& L = args.lines[l];
-    const int nc = L.ncomp < 0 ? 0 : (L.ncomp > PYRH_MAX_COMPONENTS ? PYRH_MAX_COMPONENTS : L.ncomp);
-    sm.ncomp[l] = L.polarizable ? nc : 0;
-    sm.polar[l] = L.polarizable;
-    sm.contrib[l] = L.contributes;
-    sm.lam0[l] = L.lambda0;
-  }
-
-  const double muz = args.mu, imu = 1.0 / args.mu;
-  const int64_t total = (int64_t)args.natm * args.tiles;
-  for (int64_t w = blockIdx.x; w < total; w += gridDim.x) {
-    const int p = (int)(w / args.tiles);
-    const int tile = (int)(w % args.tiles);
-    const int nl = args.nlam[p];
-    const int la0 = tile * BL;
-    if (la0 >= nl) continue;                 // uniform across the block
-    const int nd = args.ndep[p];
-    if (nd < 3 || nd > args.maxd) continue;  // uniform across the block
-    const int64_t doff = args.depth_off[p];
-    __syncthreads();  // shared tables of the previous work item are consumed
-
-    // ---- per-depth and per-(line, depth) values with derivatives ----
-    for (int k = threadIdx.x; k < nd; k += BL) {
-      const int64_t d = doff + k;
-      sm.ds[k] = (k >= 1) ? R(fabs(args.height[d] - args.height[d - 1]) * imu) : R(0);
-      sm.geo[k] = geometry_d<R>(R(args.gamma_B[d]), R(args.chi_B[d]), R(muz));
-      sm.len_up[k] = (k >= 1 && ra.dT.dlen_up) ? R(ra.dT.dlen_up[d] * imu) : R(0);
-      sm.len_dn[k] = (k >= 1 && ra.dT.dlen_dn) ? R(ra.dT.dlen_dn[d] * imu) : R(0);
-      if (MODE != 0)
-        for (int x = 0; x < kNX; ++x) sm.grad[x * args.maxd + k] = R(0);
-    }
-    if (MODE == 1 && threadIdx.x == 0) sm.chi2[0] = R(0);
-    if (MODE != 0)
-      for (int l = threadIdx.x; l < nline; l += BL) sm.gfs[l] = R(0);
-    for (int i = threadIdx.x; i < nline * nd; i += BL) {
-      const int l = i / nd, k = i % nd;
-      const int64_t d = doff + k;
-      const pyrh_line& L = args.lines[l];
-      const LineConstD c = {L.lambda0, L.Ei, L.gi, L.Aji, L.Bji, L.Bij, L.Grad, L.GStark,
-                            L.GvdWaals, L.cross, L.alpha, L.isotope_frac, L.hyperfine_frac,
-                            L.weight, L.vdwaals};
-      const double* dp = ra.dT.dline_pops;
-      sm.ld[l * args.maxd + k] = line_depth<R>(
-          c, R(args.T[d]), R(args.vlos[d]), R(args.vturb[d]), R(args.B[d]), R(args.ne[d]),
-          R(args.nHtot[d]), R(args.np[d]),
-          R(args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d]),
-          R(args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d]), R(muz),
-          args.moving != 0, dp ? R(dp[((int64_t)l * 2 + 0) * args.total_depth + d]) : R(0),
-          dp ? R(dp[((int64_t)l * 2 + 1) * args.total_depth + d]) : R(0),
-          ra.dT.dnp ? R(ra.dT.dnp[d]) : R(0));
-    }
-    __syncthreads();
-
-    // Every lane of a warp that holds at least one wavelength runs the sweep
-    // (lanes past the spectrum repeat its last wavelength with zero seeds and
-    // write nothing), so the per-depth gradient sums can use full-warp
-    // shuffles before one shared atomic per warp.
-    const bool act = la0 + (int)threadIdx.x < nl;
-    const int la = act ? la0 + (int)threadIdx.x : nl - 1;
-    if (la0 + (int)(threadIdx.x & ~31u) < nl) {
-      const int64_t loff = args.lam_off[p];
-      const double lam = args.lambda[loff + la];
-      const double dlc = lam * kQ_WING * (args.vmicro_char / kCLIGHT);
-      Local<R> loc;
-      loc.sm = &sm;
-      loc.nline = nline;
-      loc.maxd = args.maxd;
-      loc.nl = nl;
-      loc.inwin = 0u;
-      for (int l = 0; l < nline; ++l) {
-        loc.dlam[l] = R(lam - sm.lam0[l]);
-        if (fabs(sm.lam0[l] - lam) <= dlc && sm.contrib[l]) loc.inwin |= 1u << l;
-      }
-      loc.chi_c = static_cast<const R*>(args.chi_c) + args.cont_off[p] + la;
-      loc.eta_c = static_cast<const R*>(args.eta_c) + args.cont_off[p] + la;
-      loc.dchi_c = ra.dT.dchi_c ? static_cast<const R*>(ra.dT.dchi_c) + args.cont_off[p] + la
-                                : nullptr;
-      loc.deta_c = ra.dT.deta_c ? static_cast<const R*>(ra.dT.deta_c) + args.cont_off[p] + la
-                                : nullptr;
-
-      Tape<R> tp;
-      auto qop = [&](int k, R* q) {
-        local_q<R, true>(nline, sm.ld + k, args.maxd, sm.geo[k], loc.dlam, loc.inwin, sm.ncomp,
-                         sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS,
-                         loc.chi_c[(int64_t)k * nl], loc.eta_c[(int64_t)k * nl], q, tp.z[k]);
-      };
-      const double B0 = planck(args.T[doff + nd - 2], lam);
-      const double B1 = planck(args.T[doff + nd - 1], lam);
-      R st[4];
-      delo_forward<R>(tp, sm.ds, nd, B0, B1, st, qop);
-      // no line inside its window: the reference's Feautrier solution
-      const bool feaut = loc.inwin == 0u;
-      FeautTape<R> ftape;
-      FeautAdj<R> fadj;
-      if (feaut) {
-        st[0] = feautrier_fwd<R>(tp, sm.ds, nd, B0, B1, ftape);
-        st[1] = st[2] = st[3] = R(0);
-      }
-      R* out = static_cast<R*>(args.out) + 4 * loff;
-      if (act)
-#pragma unroll
-        for (int s = 0; s < 4; ++s) out[(int64_t)s * nl + la] = st[s];
-
-      constexpr int NSG = MODE == 0 ? 4 : 1;
-      const bool want_gf = MODE == 0 ? ra.rf_gf != nullptr : ra.grad_gf != nullptr;
-      R gfacc[NSG * PYRH_MAX_LINES];
-      if (want_gf)
-        for (int e = 0; e < NSG * PYRH_MAX_LINES; ++e) gfacc[e] = R(0);
-      Emit<R, MODE> em;
-      em.loc = &loc;
-      em.tp = &tp;
-      em.gf = want_gf ? gfacc : nullptr;
-      em.T = args.T + doff;
-      em.lam = lam;
-      em.nd = nd;
-      em.nl = nl;
-      em.la = la;
-      em.act = act;
-      em.fa = feaut ? &fadj : nullptr;
-      if (MODE == 0) {
-        em.rf = static_cast<R*>(ra.rf) + 24 * args.cont_off[p] + la;
-        const R one = feaut ? R(0) : R(1);
-        const R seed[4][4] = {{one, 0, 0, 0}, {0, one, 0, 0}, {0, 0, one, 0}, {0, 0, 0, one}};
-        if (feaut) feautrier_vjp<R>(tp, sm.ds, nd, B0, B1, ftape, R(1), fadj);
-        delo_reverse_stream<R, 4>(tp, sm.ds, nd, B0, B1, seed, em);
-        if (want_gf && act) {
-          R* o = static_cast<R*>(ra.rf_gf) + (int64_t)4 * nline * loff + la;
-          for (int l = 0; l < nline; ++l)
-            for (int s = 0; s < 4; ++s)
-              o[(int64_t)(l * 4 + s) * nl] = gfacc[s * PYRH_MAX_LINES + l];
-        }
-      } else if (MODE == 2) {
-        em.rf = nullptr;
-        const R* dL = static_cast<const R*>(ra.weights) + 4 * loff;
-        R seed[1][4];
-#pragma unroll
-        for (int s = 0; s < 4; ++s) seed[0][s] = act ? dL[(int64_t)s * nl + la] : R(0);
-        if (feaut) {
-          feautrier_vjp<R>(tp, sm.ds, nd, B0, B1, ftape, seed[0][0], fadj);
-#pragma unroll
-          for (int s = 0; s < 4; ++s) seed[0][s] = R(0);
-        }
-        delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
-        if (want_gf) gf_block_sum(gfacc, nline, sm.gfs);
-      } else {
-        em.rf = nullptr;
-        const R* obs = static_cast<const R*>(ra.obs) + 4 * loff;
-        const R* wt = static_cast<const R*>(ra.weights) + 4 * loff;
-        R seed[1][4];
-        R c2 = 0;
-#pragma unroll
-        for (int s = 0; s < 4; ++s) {
-          const R wv = act ? wt[(int64_t)s * nl + la] : R(0);
-          const R r = st[s] - obs[(int64_t)s * nl + la];
-          seed[0][s] = R(2) * wv * r;
-          c2 += wv * r * r;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c2 += __shfl_xor_sync(0xffffffffu, c2, o);
-        if ((threadIdx.x & 31u) == 0) atomicAdd(sm.chi2, c2);
-        if (feaut) {
-          feautrier_vjp<R>(tp, sm.ds, nd, B0, B1, ftape, seed[0][0], fadj);
-#pragma unroll
-          for (int s = 0; s < 4; ++s) seed[0][s] = R(0);
-        }
-        delo_reverse_stream<R, 1>(tp, sm.ds, nd, B0, B1, seed, em);
-        if (want_gf) gf_block_sum(gfacc, nline, sm.gfs);
-      }
-    }
-    if (MODE != 0) {
-      __syncthreads();
-      R* grad = static_cast<R*>(ra.grad);
-      for (int i = threadIdx.x; i < kNX * nd; i += BL) {
-        const int x = i / nd, k = i % nd;
-        atomicAdd(&grad[(int64_t)x * args.total_depth + doff + k], sm.grad[x * args.maxd + k]);
-      }
-      if (MODE == 1 && threadIdx.x == 0) atomicAdd(static_cast<R*>(ra.chi2) + p, sm.chi2[0]);
-      if (ra.grad_gf)
-        for (int l = threadIdx.x; l < nline; l += BL)
-          atomicAdd(static_cast<R*>(ra.grad_gf) + (int64_t)p * nline + l, sm.gfs[l]);
-    }
-  }
-}
-
-template <typename R, int MODE>
-cudaError_t launch_mode(const RfArgs& a, int block, int grid, size_t smem, cudaStream_t st) {
-  auto k = lte_rf_kernel<R, MODE>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  k<<<grid, block, smem, st>>>(a);
-  return cudaGetLastError();
-}
-
-}  // namespace
+cudaError_t launch_lte_rf_fp32_m0(const RfArgs& a, int block, int grid, size_t smem,
+                                  cudaStream_t st);
+cudaError_t launch_lte_rf_fp32_m1(const RfArgs& a, int block, int grid, size_t smem,
+                                  cudaStream_t st);
+cudaError_t launch_lte_rf_fp32_m2(const RfArgs& a, int block, int grid, size_t smem,
+                                  cudaStream_t st);
+cudaError_t launch_lte_rf_fp64_m0(const RfArgs& a, int block, int grid, size_t smem,
+                                  cudaStream_t st);
+cudaError_t launch_lte_rf_fp64_m1(const RfArgs& a, int block, int grid, size_t smem,
+                                  cudaStream_t st);
+cudaError_t launch_lte_rf_fp64_m2(const RfArgs& a, int block, int grid, size_t smem,
+                                  cudaStream_t st);
+size_t rf_smem_bytes_fp32(int nline, int maxd);
+size_t rf_smem_bytes_fp64(int nline, int maxd);
 
 size_t rf_smem_bytes(int precision, int nline, int maxd) {
-  return precision == PYRH_FP32 ? rf_smem_t<float>(nline, maxd, nullptr, nullptr)
-                                : rf_smem_t<double>(nline, maxd, nullptr, nullptr);
-}
-
-template <typename R>
-cudaError_t launch_t(const RfArgs& a, int block, int grid, size_t smem, cudaStream_t st) {
-  if (a.mode == 0) return launch_mode<R, 0>(a, block, grid, smem, st);
-  if (a.mode == 1) return launch_mode<R, 1>(a, block, grid, smem, st);
-  return launch_mode<R, 2>(a, block, grid, smem, st);
+  return precision == PYRH_FP32 ? rf_smem_bytes_fp32(nline, maxd)
+                                : rf_smem_bytes_fp64(nline, maxd);
 }
 
 cudaError_t launch_lte_rf(const RfArgs& a, int block, int grid, cudaStream_t st) {
   const size_t smem = rf_smem_bytes(a.lte.precision, a.lte.nline, a.lte.maxd);
-  return a.lte.precision == PYRH_FP32 ? launch_t<float>(a, block, grid, smem, st)
-                                      : launch_t<double>(a, block, grid, smem, st);
+  const bool f32 = a.lte.precision == PYRH_FP32;
+  switch (a.mode) {
+    case 0: return f32 ? launch_lte_rf_fp32_m0(a, block, grid, smem, st)
+                       : launch_lte_rf_fp64_m0(a, block, grid, smem, st);
+    case 1: return f32 ? launch_lte_rf_fp32_m1(a, block, grid, smem, st)
+                       : launch_lte_rf_fp64_m1(a, block, grid, smem, st);
+    default: return f32 ? launch_lte_rf_fp32_m2(a, block, grid, smem, st)
+                        : launch_lte_rf_fp64_m2(a, block, grid, smem, st);
+  }
 }
 
 }  // namespace pyrh

@@ -30,6 +30,7 @@
 
 #include "../../include/pyrh_gb300.h"
 #include "rt_device.cuh"
+#include "voigt_armstrong.cuh"
 
 #ifndef PYRH_MAX_DEPTH_RF
 #define PYRH_MAX_DEPTH_RF PYRH_RF_MAX_DEPTH
@@ -38,6 +39,9 @@
 namespace pyrh {
 
 constexpr int kNX = 6;  // T, v_los, v_mic, B, gamma, chi
+// Zeeman component count that marks a line which is not polarizable: its
+// profile is Armstrong's Voigt function H(a, v), Stokes I only (kurucz.c:824)
+constexpr int kArmstrong = -1;
 
 // ------------------------------------------------------------- duals -----
 template <typename R>
@@ -367,6 +371,15 @@ PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, int ld_stride, const
       eI = eI + L.etal * phi;
       continue;
     }
+    if (ncomp[l] == kArmstrong) {
+      R dHda, dHdv;
+      D6<R> H;
+      H.v = voigt_armstrong_d<R>(L.adamp.v, v.v, dHda, dHdv);
+      for (int i = 0; i < kNX; ++i) H.d[i] = dHda * L.adamp.d[i] + dHdv * v.d[i];
+      cI = cI + L.chil * H;
+      eI = eI + L.etal * H;
+      continue;
+    }
     D6<R> ph[3] = {dconst(R(0)), dconst(R(0)), dconst(R(0))};
     for (int c = 0; c < ncomp[l]; ++c) {
       const R sh = cshift[l * maxcomp + c], w = cweight[l * maxcomp + c];
@@ -409,7 +422,8 @@ PYRH_HD void local_q_jac(int nline, const LineDepth<R>* ld, int ld_stride, const
 // derivatives with respect to the damping a, the reduced frequency x and the
 // Zeeman splitting v_B:  sum w Re W',  sum w Im W',  -sum w sh Im W'
 // (W' = dW/dt, t = a - i x; dH/da = Re W', dH/dx = Im W').  Gaussian lines
-// keep phi and dphi/dx in the first two slots.
+// keep phi and dphi/dx in the first two slots, lines that are not
+// polarizable H, dH/da and dH/dv of Armstrong's function in the first three.
 constexpr int kZLines = 2;
 constexpr int kZ = 12;
 
@@ -417,7 +431,9 @@ constexpr int kZ = 12;
 // value parts, with the single-precision fast Humlicek where R is float.
 // With SUMS, the Humlicek derivative is evaluated as well and the profile
 // sums of the first kZLines in-window lines are stored in z.
-template <typename R, bool SUMS = false>
+// UP = false leaves out the branch for lines that are not polarizable (for
+// blocks without them; see lte_rf_kernel.cuh).
+template <typename R, bool SUMS = false, bool UP = true>
 PYRH_HD void local_q(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
                      const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
                      const R* cweight, const int* cq, int maxcomp, R chi_c, R eta_c, R q[8],
@@ -437,6 +453,24 @@ PYRH_HD void local_q(int nline, const LineDepth<R>* ld, int ld_stride, const Geo
         z[slot][0] = phi;
         z[slot][1] = R(-2) * v * phi;
       }
+      slot += SUMS ? 1 : 0;
+      continue;
+    }
+    if (UP && ncomp[l] == kArmstrong) {
+      R H;
+      if (SUMS) {
+        R dHda, dHdv;
+        H = voigt_armstrong_d<R>(L.adamp.v, v, dHda, dHdv);
+        if (keep) {
+          z[slot][0] = H;
+          z[slot][1] = dHda;
+          z[slot][2] = dHdv;
+        }
+      } else {
+        H = voigt_armstrong_t<R>(L.adamp.v, v);
+      }
+      cI += L.chil.v * H;
+      eI += L.etal.v * H;
       slot += SUMS ? 1 : 0;
       continue;
     }
@@ -505,7 +539,7 @@ PYRH_HD void local_q(int nline, const LineDepth<R>* ld, int ld_stride, const Geo
 // z instead of re-evaluating the Zeeman components.
 // dchic_dT, detac_dT: temperature derivatives of the continuum opacity and
 // emissivity of this (depth, wavelength) from the set-up (zero: held fixed).
-template <typename R, int NS>
+template <typename R, int NS, bool UP = true>
 PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
                          const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
                          const R* cweight, const int* cq, int maxcomp, const R q[8],
@@ -540,6 +574,23 @@ PYRH_HD void local_q_vjp(int nline, const LineDepth<R>* ld, int ld_stride, const
         etalb[s] = eb[s][0] * phi;
         vb[s] = phib * dphi;
         ab[s] = vBb[s] = R(0);
+      }
+    } else if (UP && ncomp[l] == kArmstrong) {
+      R H, dHda, dHdv;
+      if (zl) {
+        H = zl[0];
+        dHda = zl[1];
+        dHdv = zl[2];
+      } else {
+        H = voigt_armstrong_d<R>(L.adamp.v, v, dHda, dHdv);
+      }
+      for (int s = 0; s < NS; ++s) {
+        const R phib = cb[s][0] * L.chil.v + eb[s][0] * L.etal.v;
+        chilb[s] = cb[s][0] * H;
+        etalb[s] = eb[s][0] * H;
+        ab[s] = phib * dHda;
+        vb[s] = phib * dHdv;
+        vBb[s] = R(0);
       }
     } else {
       R phb[NS][3];
@@ -1244,8 +1295,10 @@ struct FeautTape {
   R G[PYRH_MAX_DEPTH_RF], y[PYRH_MAX_DEPTH_RF], dtau[PYRH_MAX_DEPTH_RF];
 };
 
+// Adjoints a scalar (Stokes I only) solver hands to the per-depth
+// contraction: dL/dchi_k, dL/dS_k, dL/d ds_k and the two Planck values.
 template <typename R>
-struct FeautAdj {
+struct ScalarAdj {
   R chib[PYRH_MAX_DEPTH_RF], Sb[PYRH_MAX_DEPTH_RF], dsb[PYRH_MAX_DEPTH_RF];
   R B0b, B1b;
 };
@@ -1290,7 +1343,7 @@ PYRH_COLD R feautrier_fwd(const Tape<R>& tp, const R* ds, int N, double B0, doub
 
 template <typename R>
 PYRH_COLD void feautrier_vjp(const Tape<R>& tp, const R* ds, int N, double B0, double B1,
-                             const FeautTape<R>& ft, R Ib, FeautAdj<R>& fa) {
+                             const FeautTape<R>& ft, R Ib, ScalarAdj<R>& fa) {
   R dtb_adj[PYRH_MAX_DEPTH_RF];
   for (int k = 0; k < N; ++k) fa.chib[k] = fa.Sb[k] = fa.dsb[k] = dtb_adj[k] = R(0);
   // top row: P0 = (S_0 + C10 y_1) / (abc0 + C10 g(G_1)), g(G) = G / (1 + G)
@@ -1359,6 +1412,180 @@ PYRH_COLD void feautrier_vjp(const Tape<R>& tp, const R* ds, int N, double B0, d
     fa.chib[k + 1] += a * ds[k + 1];
     fa.dsb[k + 1] += a * (tp.q[k][0] + tp.q[k + 1][0]);
   }
+}
+
+// ------------------------------- scalar Bezier3 (unpolarized lines only) --
+// Where lines are inside their windows but none of them is polarizable the
+// reference solves with scalar Bezier3 (Piecewise_Bezier3_1D,
+// bezier_1D.c:306-541): clipped control points on S, a one-sided slope at
+// the bottom and in the last interval; it differs from DELO-Bezier3 with
+// K' = 0 by ~2e-3 of I.  Its optical-depth intervals T_k and centred chi
+// derivatives are the ones delo_forward tapes, so the forward pass here
+// reruns only the S recurrence (as solve_scalar in lte_stokes.cu) and keeps
+// I_k; scalar_bezier_vjp runs its adjoint, then dtau_vjp turns the interval
+// adjoints into dL/dchi_k and dL/d ds_k.
+template <typename R>
+struct ScalarTape {
+  R I[PYRH_MAX_DEPTH_RF];
+};
+
+// Adjoint of the intervals T_k = ds_{k+1} (chi_k + chi_{k+1} + c1 + c2) / 4
+// of delo_forward (clipped chi control points from the centred derivatives
+// tp.dchi) for given dL/dT_k (k = 0 .. N-2).
+template <typename R>
+PYRH_COLD void dtau_vjp(const Tape<R>& tp, const R* ds, int N, const R* Tb, R* chib, R* dsb) {
+  R dchib[PYRH_MAX_DEPTH_RF];
+  for (int k = 0; k < N; ++k) dchib[k] = R(0);
+  for (int k = 0; k <= N - 3; ++k) {      // made by step k+1 as its lower interval
+    const R dsd = ds[k + 1], a = R(0.25) * dsd * Tb[k];
+    chib[k + 1] += a;
+    chib[k] += a;
+    dsb[k + 1] += Tb[k] * tp.T[k] / dsd;
+    if (tp.q[k + 1][0] + (dsd / R(3)) * tp.dchi[k + 1] > R(0)) {
+      chib[k + 1] += a;
+      dchib[k + 1] += (dsd / R(3)) * a;
+      dsb[k + 1] += a * tp.dchi[k + 1] / R(3);
+    }
+    if (tp.q[k][0] - (dsd / R(3)) * tp.dchi[k] > R(0)) {
+      chib[k] += a;
+      dchib[k] -= (dsd / R(3)) * a;
+      dsb[k + 1] -= a * tp.dchi[k] / R(3);
+    }
+  }
+  {                                       // the first interval, k = N-2
+    const int k = N - 2;
+    const R dsu = ds[N - 1], a = R(0.25) * dsu * Tb[k];
+    const R dchi_up = tp.dchi_up0;
+    R dchi_upb = R(0);
+    chib[k] += a;
+    chib[k + 1] += a;
+    dsb[N - 1] += Tb[k] * tp.T[k] / dsu;
+    if (tp.q[k][0] - (dsu / R(3)) * tp.dchi[k] > R(0)) {
+      chib[k] += a;
+      dchib[k] -= (dsu / R(3)) * a;
+      dsb[N - 1] -= a * tp.dchi[k] / R(3);
+    }
+    if (tp.q[k + 1][0] + (dsu / R(3)) * dchi_up > R(0)) {
+      chib[k + 1] += a;
+      dchi_upb += (dsu / R(3)) * a;
+      dsb[N - 1] += a * dchi_up / R(3);
+    }
+    chib[k] += dchi_upb / dsu;
+    chib[k + 1] -= dchi_upb / dsu;
+    dsb[N - 1] -= dchi_upb * dchi_up / dsu;
+  }
+  // centred chi derivatives: depth k from ds_{k+1}, ds_k and chi_{k+1..k-1};
+  // depth 0 one-sided
+  for (int k = 1; k <= N - 2; ++k)
+    cent_deriv_vjp<R>(cd_weights<R>(ds[k + 1], ds[k]), tp.q[k + 1][0], tp.q[k][0],
+                      tp.q[k - 1][0], dchib[k], dsb[k + 1], dsb[k], chib[k + 1], chib[k],
+                      chib[k - 1]);
+  chib[0] += dchib[0] / ds[1];
+  chib[1] -= dchib[0] / ds[1];
+  dsb[1] -= dchib[0] * tp.dchi[0] / ds[1];
+}
+
+template <typename R>
+PYRH_COLD R scalar_bezier_fwd(const Tape<R>& tp, const R* ds, int N, double B0, double B1,
+                              ScalarTape<R>& st) {
+  const double dtau0 = 0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * (double)ds[N - 1];
+  R I = R(B1 - (B0 - B1) / dtau0);
+  st.I[N - 1] = I;
+  R dSup = (tp.q[N - 2][1] - tp.q[N - 1][1]) / tp.T[N - 2];
+  for (int k = N - 2; k >= 1; --k) {
+    const R Tk = tp.T[k], Tdw = tp.T[k - 1];
+    const R Su = tp.q[k + 1][1], Sc = tp.q[k][1], Sd = tp.q[k - 1][1];
+    R al, be, ga, th, ep;
+    bezier3_coeffs(Tk, al, be, ga, th, ep);
+    const R dt03 = Tk / R(3);
+    const R dSc = cent_deriv<R>(Tk, Tdw, Su, Sc, Sd);
+    const R c1 = fmax(Sc - dt03 * dSc, R(0)), c2 = fmax(Su + dt03 * dSup, R(0));
+    I = I * ep + al * Sc + be * Su + ga * c1 + th * c2;
+    st.I[k] = I;
+    dSup = dSc;
+  }
+  const double dtau = 0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * (double)ds[1];
+  double w[3];
+  w3(dtau, w);
+  const R dSuw = -(tp.q[0][1] - tp.q[1][1]) / R(dtau);
+  return (R(1) - R(w[0])) * I + R(w[0]) * tp.q[0][1] + R(w[1]) * dSuw;
+}
+
+template <typename R>
+PYRH_COLD void scalar_bezier_vjp(const Tape<R>& tp, const R* ds, int N, double B0, double B1,
+                                 const ScalarTape<R>& st, R Ib, ScalarAdj<R>& fa) {
+  R Tb[PYRH_MAX_DEPTH_RF], dSb[PYRH_MAX_DEPTH_RF];
+  for (int k = 0; k < N; ++k) fa.chib[k] = fa.Sb[k] = fa.dsb[k] = Tb[k] = dSb[k] = R(0);
+  // last interval: I_0 = (1 - w0) I_1 + w0 S_0 + w1 (S_1 - S_0) / dtau
+  R Iub;
+  {
+    const double dtau = 0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * (double)ds[1];
+    double w[3], dw[2];
+    w3_d(dtau, w, dw);
+    const R w0 = R(w[0]), w1 = R(w[1]);
+    const R dSuw = -(tp.q[0][1] - tp.q[1][1]) / R(dtau);
+    Iub = Ib * (R(1) - w0);
+    fa.Sb[0] += Ib * w0;
+    const R dSuwb = Ib * w1;
+    fa.Sb[1] += dSuwb / R(dtau);
+    fa.Sb[0] -= dSuwb / R(dtau);
+    const double dtb = (double)(Ib * (tp.q[0][1] - st.I[1])) * dw[0] +
+                       (double)(Ib * dSuw) * dw[1] - (double)dSuwb * (double)dSuw / dtau;
+    fa.chib[0] += R(0.5 * (double)ds[1] * dtb);
+    fa.chib[1] += R(0.5 * (double)ds[1] * dtb);
+    fa.dsb[1] += R(0.5 * ((double)tp.q[0][0] + (double)tp.q[1][0]) * dtb);
+  }
+  // steps k = 1 .. N-2: I_k = I_{k+1} ep + al S_k + be S_{k+1} + ga c1 + th c2
+  for (int k = 1; k <= N - 2; ++k) {
+    const R Tk = tp.T[k], Tdw = tp.T[k - 1];
+    const R Su = tp.q[k + 1][1], Sc = tp.q[k][1], Sd = tp.q[k - 1][1];
+    R cf[5], dcf[5];
+    bezier3_coeffs_d(Tk, cf, dcf);
+    const R dt03 = Tk / R(3);
+    const R dSc = cent_deriv<R>(Tk, Tdw, Su, Sc, Sd);
+    const bool top = (k == N - 2);
+    const R dSup = top ? (tp.q[N - 2][1] - tp.q[N - 1][1]) / Tk
+                       : cent_deriv<R>(tp.T[k + 1], Tk, tp.q[k + 2][1], Su, Sc);
+    const R c1 = fmax(Sc - dt03 * dSc, R(0)), c2 = fmax(Su + dt03 * dSup, R(0));
+    R Tkb = Iub * (st.I[k + 1] * dcf[4] + Sc * dcf[0] + Su * dcf[1] + c1 * dcf[2] + c2 * dcf[3]);
+    fa.Sb[k] += Iub * cf[0];
+    fa.Sb[k + 1] += Iub * cf[1];
+    const R c1b = Iub * cf[2], c2b = Iub * cf[3];
+    if (Sc - dt03 * dSc > R(0)) {
+      fa.Sb[k] += c1b;
+      Tkb -= c1b * dSc / R(3);
+      dSb[k] -= c1b * dt03;
+    }
+    if (Su + dt03 * dSup > R(0)) {
+      fa.Sb[k + 1] += c2b;
+      Tkb += c2b * dSup / R(3);
+      const R dSupb = c2b * dt03;
+      if (top) {
+        fa.Sb[N - 2] += dSupb / Tk;
+        fa.Sb[N - 1] -= dSupb / Tk;
+        Tkb -= dSupb * dSup / Tk;
+      } else {
+        dSb[k + 1] += dSupb;
+      }
+    }
+    // dS_k has all its terms now (this step's c1, the previous one's c2)
+    cent_deriv_vjp<R>(cd_weights<R>(Tk, Tdw), Su, Sc, Sd, dSb[k], Tkb, Tb[k - 1], fa.Sb[k + 1],
+                      fa.Sb[k], fa.Sb[k - 1]);
+    Tb[k] += Tkb;
+    Iub *= cf[4];
+  }
+  // bottom boundary I_{N-1} = B1 - (B0 - B1) / dtau0
+  {
+    const double dtau0 = 0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * (double)ds[N - 1];
+    const double ib = (double)Iub;
+    fa.B1b = R(ib * (1.0 + 1.0 / dtau0));
+    fa.B0b = R(-ib / dtau0);
+    const double dtb = ib * (B0 - B1) / (dtau0 * dtau0);
+    fa.chib[N - 1] += R(0.5 * (double)ds[N - 1] * dtb);
+    fa.chib[N - 2] += R(0.5 * (double)ds[N - 1] * dtb);
+    fa.dsb[N - 1] += R(0.5 * ((double)tp.q[N - 1][0] + (double)tp.q[N - 2][0]) * dtb);
+  }
+  dtau_vjp<R>(tp, ds, N, Tb, fa.chib, fa.dsb);
 }
 
 // dB_nu/dT of planck() (planck.c:38-63)

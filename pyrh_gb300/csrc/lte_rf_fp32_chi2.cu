@@ -1,0 +1,13 @@
+// lte_rf_fp32_chi2.cu -- the single-precision response-function kernel for the
+// chi^2 gradient (mode 1) (lte_rf_kernel.cuh), in a unit of its own so that the kernel
+// instantiations compile in parallel.
+#include "lte_rf_kernel.cuh"
+
+namespace pyrh {
+
+cudaError_t launch_lte_rf_fp32_m1(const RfArgs& a, int block, int grid, size_t smem,
+                                  cudaStream_t st) {
+  return launch_mode<float, 1>(a, block, grid, smem, st);
+}
+
+}  // namespace pyrh

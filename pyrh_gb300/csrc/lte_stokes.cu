@@ -25,6 +25,7 @@
 
 #include "../../include/pyrh_gb300.h"
 #include "rt_device.cuh"
+#include "voigt_armstrong.cuh"
 #include "lte_stokes.cuh"
 
 namespace pyrh {
@@ -76,7 +77,10 @@ struct Work {
 // Opacity of one wavelength at one depth: chi (total), S[4], K6 = (Q, U, V,
 // Q', U', V') / chi.  Line sums are accumulated in list order and added to
 // the continuum afterwards, as kurucz.c:593-715 and background.c:534-537 do.
-template <typename R, bool MO>
+// UP: the block has lines that are not polarizable (Armstrong's Voigt);
+// blocks without them run an instantiation that does not contain that
+// branch, whose call would otherwise add register spills to the hot loop.
+template <typename R, bool MO, bool UP = false>
 struct Opacity {
   const Smem<R>* sm;
   const R* chi_c;  // continuum base for this (atmosphere, wavelength): index k*nl
@@ -100,6 +104,12 @@ struct Opacity {
       const R chil = lp[LF_CHI * maxd + k], etal = lp[LF_ETA * maxd + k];
       if (a < R(0)) {  // Grad == 0: Doppler core only (kurucz.c:776-779)
         R phi = (fabs(v) <= R(kMAX_GAUSS_DOPPLER)) ? dev_exp(-v * v) : R(0);
+        cI += chil * phi;
+        eI += etal * phi;
+        continue;
+      }
+      if (UP && !sm->meta[3 * l + 1]) {   // not polarizable: Armstrong's Voigt, I only (kurucz.c:824)
+        const R phi = voigt_armstrong_t<R>(a, v);
         cI += chil * phi;
         eI += etal * phi;
         continue;
@@ -278,8 +288,8 @@ __device__ __forceinline__ void delo_last(R w0, R w1, R wd, const R ku[6], const
 
 // DELO-Bezier3 along the ray to the observer; bezier_1D.c:52-300 with
 // to_obs = TRUE (k_start = Ndep-1, k_end = 0, dk = -1).
-template <typename R, bool MO>
-__device__ void solve_stokes(const Opacity<R, MO>& op, const R* ds, int nd, double B0,
+template <typename R, bool MO, bool UP>
+__device__ void solve_stokes(const Opacity<R, MO, UP>& op, const R* ds, int nd, double B0,
                              double B1, R out[4]) {
   constexpr int NK = MO ? 6 : 3;
   // pipeline: u = k+1, c = k, d = k-1, dd = k-2
@@ -359,8 +369,8 @@ __device__ void solve_stokes(const Opacity<R, MO>& op, const R* ds, int nd, doub
 }
 
 // Scalar Bezier3 along the ray to the observer (bezier_1D.c:306-541).
-template <typename R, bool MO>
-__device__ R solve_scalar(const Opacity<R, MO>& op, const R* ds, int nd, double B0, double B1) {
+template <typename R, bool MO, bool UP>
+__device__ R solve_scalar(const Opacity<R, MO, UP>& op, const R* ds, int nd, double B0, double B1) {
   R chi_u, chi_c, chi_d, chi_dd, S4[4], K6[6];
   R S_u, S_c, S_d, S_dd = 0;
   op(nd - 1, chi_u, S4, K6); S_u = S4[0];
@@ -411,8 +421,8 @@ __device__ R solve_scalar(const Opacity<R, MO>& op, const R* ds, int nd, double 
 
 // Feautrier (feautrier.c:56-202, STANDARD order, ZERO top, THERMALIZED
 // bottom), eliminated from the bottom up: P[k] = P[k-1]/(1+G[k]) + y[k].
-template <typename R, bool MO>
-__device__ R solve_feautrier(const Opacity<R, MO>& op, const R* ds, int nd, double B0, double B1) {
+template <typename R, bool MO, bool UP>
+__device__ R solve_feautrier(const Opacity<R, MO, UP>& op, const R* ds, int nd, double B0, double B1) {
   R S4[4], K6[6];
   R chi_b, chi_a;                   // depths k+1 and k
   op(nd - 1, chi_b, S4, K6);
@@ -441,6 +451,60 @@ __device__ R solve_feautrier(const Opacity<R, MO>& op, const R* ds, int nd, doub
   const R abc0 = R(1) + R(2) / dtau_b, C10 = R(2) / (dtau_b * dtau_b);
   const R P0 = (S_a + C10 * y) / (abc0 + C10 * G / (R(1) + G));
   return R(2) * P0;
+}
+
+// Phase 2 of the synthesis kernel: one wavelength per thread, with the
+// solver the reference picks for it (formal.c:94-95, 285-310).
+template <typename R, bool MO, bool UP>
+__device__ __forceinline__ void synth_wavelength(const LteArgs& args, const Smem<R>& sm, int p,
+                                                 int la0, int nl, int nd, int nline,
+                                                 int64_t doff) {
+  const int la = la0 + threadIdx.x;
+  if (la < nl) {
+    const int64_t loff = args.lam_off[p];
+    const double lam = args.lambda[loff + la];
+    const double dlc = lam * kQ_WING * (args.vmicro_char / kCLIGHT);
+    Opacity<R, MO, UP> op;
+    op.sm = &sm;
+    op.nl = nl;
+    op.nline = nline;
+    op.chi_c = static_cast<const R*>(args.chi_c) + args.cont_off[p] + la;
+    op.eta_c = static_cast<const R*>(args.eta_c) + args.cont_off[p] + la;
+    op.inwin = 0u;
+    bool pol = false;
+    for (int l = 0; l < nline; ++l) {
+      const double dl = lam - sm.lam0[l];
+      op.dlam[l] = R(dl);
+      if (fabs(sm.lam0[l] - lam) <= dlc && sm.meta[3 * l + 2]) {
+        op.inwin |= 1u << l;
+        pol |= (sm.meta[3 * l + 1] != 0);
+      }
+    }
+    const double B0 = planck(args.T[doff + nd - 2], lam);
+    const double B1 = planck(args.T[doff + nd - 1], lam);
+    const R* ds = sm.geo + GF_DS * sm.maxd;
+    R st[4] = {0, 0, 0, 0};
+    if (op.inwin == 0u) {
+      st[0] = solve_feautrier<R, MO, UP>(op, ds, nd, B0, B1);
+    } else if (pol && args.stokes_mode == PYRH_FULL_STOKES) {
+      solve_stokes<R, MO, UP>(op, ds, nd, B0, B1, st);
+    } else {
+      st[0] = solve_scalar<R, MO, UP>(op, ds, nd, B0, B1);
+    }
+    R* out = static_cast<R*>(args.out) + 4 * loff;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) out[(int64_t)s * nl + la] = st[s];
+  }
+}
+
+// The same for blocks with lines that are not polarizable, out of line: the
+// kernel's own register allocation then serves the common path alone (one
+// call site, where little is live).
+template <typename R, bool MO>
+__device__ __noinline__ void synth_wavelength_unpol(const LteArgs& args, const Smem<R>& sm, int p,
+                                                    int la0, int nl, int nd, int nline,
+                                                    int64_t doff) {
+  synth_wavelength<R, MO, true>(args, sm, p, la0, nl, nd, nline, doff);
 }
 
 // Resident blocks per SM the FP32 kernel is compiled for (register cap
@@ -553,42 +617,12 @@ lte_stokes_kernel(LteArgs args) {
     __syncthreads();
 
     // ---- phase 2: one wavelength per thread ----
-    const int la = la0 + threadIdx.x;
-    if (la < nl) {
-      const int64_t loff = args.lam_off[p];
-      const double lam = args.lambda[loff + la];
-      const double dlc = lam * kQ_WING * (args.vmicro_char / kCLIGHT);
-      Opacity<R, MO> op;
-      op.sm = &sm;
-      op.nl = nl;
-      op.nline = nline;
-      op.chi_c = static_cast<const R*>(args.chi_c) + args.cont_off[p] + la;
-      op.eta_c = static_cast<const R*>(args.eta_c) + args.cont_off[p] + la;
-      op.inwin = 0u;
-      bool pol = false;
-      for (int l = 0; l < nline; ++l) {
-        const double dl = lam - sm.lam0[l];
-        op.dlam[l] = R(dl);
-        if (fabs(sm.lam0[l] - lam) <= dlc && sm.meta[3 * l + 2]) {
-          op.inwin |= 1u << l;
-          pol |= (sm.meta[3 * l + 1] != 0);
-        }
-      }
-      const double B0 = planck(args.T[doff + nd - 2], lam);
-      const double B1 = planck(args.T[doff + nd - 1], lam);
-      const R* ds = sm.geo + GF_DS * sm.maxd;
-      R st[4] = {0, 0, 0, 0};
-      if (op.inwin == 0u) {
-        st[0] = solve_feautrier<R, MO>(op, ds, nd, B0, B1);
-      } else if (pol && args.stokes_mode == PYRH_FULL_STOKES) {
-        solve_stokes<R, MO>(op, ds, nd, B0, B1, st);
-      } else {
-        st[0] = solve_scalar<R, MO>(op, ds, nd, B0, B1);
-      }
-      R* out = static_cast<R*>(args.out) + 4 * loff;
-#pragma unroll
-      for (int s = 0; s < 4; ++s) out[(int64_t)s * nl + la] = st[s];
-    }
+    bool any_unpol = false;   // the same in every thread of the block
+    for (int l = 0; l < nline; ++l) any_unpol |= sm.meta[3 * l + 2] && !sm.meta[3 * l + 1];
+    if (any_unpol)
+      synth_wavelength_unpol<R, MO>(args, sm, p, la0, nl, nd, nline, doff);
+    else
+      synth_wavelength<R, MO, false>(args, sm, p, la0, nl, nd, nline, doff);
   }
 }
 

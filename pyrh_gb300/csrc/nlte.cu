@@ -27,89 +27,9 @@
 #include "../../include/pyrh_gb300.h"
 #include "nlte.cuh"
 #include "rt_device.cuh"
+#include "voigt_armstrong.cuh"
 
 namespace pyrh {
-
-// ------------------------------------------------------- Armstrong Voigt --
-// Chebyshev coefficients of Dawson(5x) in odd T_{2n+1}(x) on [0,1] and the
-// 20-point Gauss-Hermite rule (positive half), both from their definitions.
-__constant__ double kDawsonCheb[34] = {
-    0.1999999999972224, -0.18400000000299979, 0.15583999999650247, -0.12166400000439881,
-    0.087708159994039123, -0.058514124808690643, 0.036215730162391359, -0.020849765439803627,
-    0.011196011634627011, -0.0056231896167108913, 0.0026487634172264554, -0.0011732670757704463,
-    0.00048995199780883401, -0.00019336308015277829, 7.2287744678832942e-05, -2.565551249788587e-05,
-    8.6620736840759859e-06, -2.7876379719252641e-06, 8.5668736268524721e-07, -2.5184337837693224e-07,
-    7.0936022149218665e-08, -1.917322572749502e-08, 4.9801256466357896e-09, -1.2447733996061773e-09,
-    2.9977766411656295e-10, -6.9644956269250685e-11, 1.5626242538020159e-11, -3.3896879080452118e-12,
-    7.1161574262122503e-13, -1.4472012169242576e-13, 2.8536768232975401e-14, -5.4606927155058021e-15,
-    1.0148769468261627e-15, -1.8333259200975614e-16};
-__constant__ double kGhT[10] = {
-    0.24534070830090124, 0.73747372854539439, 1.2340762153953231, 1.7385377121165861,
-    2.2549740020892757, 2.7888060584281305, 3.3478545673832163, 3.9447640401156252,
-    4.6036824495507442, 5.3874808900112328};
-__constant__ double kGhW[10] = {
-    0.46224366960061009, 0.28667550536283415, 0.10901720602002329, 0.024810520887463643,
-    0.0032437733422378567, 0.00022833863601635365, 7.8025564785320599e-06,
-    1.0860693707692782e-07, 4.3993409922731747e-10, 2.2293936455341447e-13};
-
-__device__ double voigt_armstrong(double a, double v) {
-  if (v < 0.0) v = -v;
-  if ((a < 1.0 && v < 4.0) || (a < 1.8 / (v + 1.0))) {
-    const double a2 = a * a, v2 = v * v;
-    double u1 = ((v2 - a2) > 70.0) ? 0.0 : exp(a2 - v2) * cos(2.0 * v * a);
-    double dn01, dn02;
-    if (v > 5.0) {
-      const double r = 1.0 / v2;
-      dn01 = -r * (0.5 + r * (0.75 + r * (1.875 + r * (6.5625 + r * (29.53125 +
-             r * (1162.4218 + r * 1055.7421))))));
-      dn02 = (1.0 - dn01) / (2.0 * v);
-    } else {
-      double b1 = 0.0, b2 = 0.0, b = 0.0;
-      const double x = v / 5.0, coef = 4.0 * x * x - 2.0;
-      for (int n = 33; n >= 0; --n) {
-        b = coef * b1 - b2 + kDawsonCheb[n];
-        b2 = b1;
-        b1 = b;
-      }
-      dn02 = x * (b - b2);
-      dn01 = 1.0 - 2.0 * v * dn02;
-    }
-    double funct = a * dn01;
-    if (a > 1.0e-8) {
-      double q = 1.0, an = a;
-      for (int n = 2; n <= 50; ++n) {
-        const double dn = (v * dn01 + dn02) * (-2.0 / n);
-        dn02 = dn01;
-        dn01 = dn;
-        if (n % 2) {
-          q = -q;
-          an *= a2;
-          const double g = dn * an;
-          funct += q * g;
-          if (fabs(g / funct) <= 1.0e-8) return u1 - 1.12837917 * funct;
-        }
-      }
-    }
-    return u1 - 1.12837917 * funct;
-  }
-  if (a < 2.5 && v < 4.0) {
-    double g = 0.0;
-    const double a2 = a * a;
-    for (int n = 0; n < 10; ++n) {
-      const double r = kGhT[n] - v, s = kGhT[n] + v;
-      g += (4.0 * kGhT[n] * kGhT[n] - 2.0) *
-           (r * atan(r / a) + s * atan(s / a) - 0.5 * a * (log(a2 + r * r) + log(a2 + s * s))) *
-           kGhW[n];
-    }
-    return g / kPI;
-  }
-  double g = 0.0;
-  const double a2 = a * a;
-  for (int n = 0; n < 10; ++n)
-    g += (1.0 / ((v - kGhT[n]) * (v - kGhT[n]) + a2) + 1.0 / ((v + kGhT[n]) * (v + kGhT[n]) + a2)) *
-         kGhW[n];
-  return (a * g) / kPI;
-}
 
 // ------------------------------------------------------------ helpers ----
 

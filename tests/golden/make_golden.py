@@ -17,6 +17,9 @@ Fixtures (npz, float64):
   lte_edge        mu=0.5, velocity gradient, strong field, lambda points
                   outside every line window, duplicate and unsorted lambda
   lte_b0          B = 0 (polarizable lines with no splitting)
+  lte_nostokes    C0 in STOKES_MODE = NO_STOKES
+  lte_mixed       C0 with two unpolarizable lines (Armstrong's Voigt), one
+                  alone in its window and one among the polarized lines
   lte_batch       6 atmospheres of the batched generator (2 x 112 lambda)
   lte_c0_dT, lte_edge_dT
                   temperature derivatives of the set-up inputs of lte_c0 /
@@ -64,9 +67,10 @@ def base_c0(ref: rr.Reference, workdir: str, ndep: int = 71):
 
 
 def lte_case(ref, name, atm, wave, mu=1.0, magneto_optical="FALSE",
-             extra=None):
+             extra=None, stokes_mode="FULL_STOKES", linelist=None):
     wd = rr.scratch_dir()
-    rr.write_inputs(wd, wl.fe_linelist(), magneto_optical=magneto_optical)
+    rr.write_inputs(wd, linelist or wl.fe_linelist(), magneto_optical=magneto_optical,
+                    stokes_mode=stokes_mode)
     lam_out, stokes, flag = ref.synth(wd, mu, atm, wave)
     _, stokes_portable, _ = PORTABLE.synth(wd, mu, atm, wave)
     dd = os.path.join(wd, "dump")
@@ -133,6 +137,31 @@ def make_lte_edge(ref, wd):
     far = np.array([629.70, 629.85, 630.55, 630.80])    # outside 20 v_char/c
     wave = np.concatenate([core[::-1][:30], far, core[::-1][30:], core[5:8]])
     lte_case(ref, "lte_edge", atm, wave, mu=0.5)
+
+
+UNPOLARIZED = dict(loggf=-1.0, chi_low=3.0, J=(2.0, 2.0), gL=(-0.099, -0.099),
+                   labels=("unknown ab", "unknown ab"), damp=(8.08, -5.42, -7.54),
+                   orbital=(1, 0))
+
+
+def make_lte_modes(ref, wd):
+    """NO_STOKES (pyrh keeps atmos.Stokes = TRUE, pyrh_compute1dray.c:258, so
+    the lines stay polarizable and only the solver is scalar), and a list
+    with two unpolarizable lines: labels without a term designation and
+    Lande factors of -99 (kurucz.c:296, 384-387), which RLKProfile gives
+    Armstrong's Voigt function (kurucz.c:824).  The one at 629.60 nm is the
+    only line in its window (scalar Bezier3 there); the one at 630.20 nm
+    shares its window with the two polarized lines (DELO-Bezier3, Stokes I
+    opacity only)."""
+    logtau, T, ne, nH = base_c0(ref, wd)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH)
+    lte_case(ref, "lte_nostokes", atm, wl.line_wavelengths(101, 0.05),
+             stokes_mode="NO_STOKES")
+    lines = sorted([dict(UNPOLARIZED, lam_vac=629.60), dict(UNPOLARIZED, lam_vac=630.20),
+                    *wl.FE_LINES], key=lambda L: L["lam_vac"])
+    wave = np.concatenate([wl.line_wavelengths(41, 0.05, centres=(629.60,)),
+                           np.linspace(630.10, 630.30, 121)])
+    lte_case(ref, "lte_mixed", atm, wave, linelist=wl.fe_linelist(lines))
 
 
 def make_lte_b0(ref, wd):
@@ -282,6 +311,7 @@ def make_nlte(ref, wd):
 
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
+          "lte_modes": make_lte_modes,
           "nlte": make_nlte}
 
 

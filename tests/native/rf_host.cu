@@ -42,7 +42,7 @@ struct Emit {
   R* gf;                    // [4][PYRH_MAX_LINES] log gf accumulators
   const R *dchi_c, *deta_c; // [depth] at this wavelength, or nullptr
   const R *len_up, *len_dn; // [depth] d ds_k/dT_{k-1}, d ds_k/dT_k
-  const FeautAdj<R>* fa;    // no line in window: the Feautrier adjoint of the I seed
+  const ScalarAdj<R>* fa;    // no line in window: the Feautrier adjoint of the I seed
   void operator()(int k, const R* qb_in, const R* bpl_in, const R* sdn_in,
                   const R* sup_in) const {
     R qb[32], bpl[4], sdn[4], sup[4];
@@ -114,7 +114,7 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     const pyrh_line& L = lines[l];
     LineConstD c = {L.lambda0, L.Ei, L.gi, L.Aji, L.Bji, L.Bij, L.Grad, L.GStark, L.GvdWaals,
                     L.cross, L.alpha, L.isotope_frac, L.hyperfine_frac, L.weight, L.vdwaals};
-    ncomp[l] = L.polarizable ? L.ncomp : 0;
+    ncomp[l] = L.polarizable ? L.ncomp : kArmstrong;
     for (int m = 0; m < PYRH_MAX_COMPONENTS; ++m) {
       cq[l * PYRH_MAX_COMPONENTS + m] = L.comp_q[m];
       cs[l * PYRH_MAX_COMPONENTS + m] = R(L.comp_shift[m]);
@@ -155,7 +155,6 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     memset(rfl, 0, sizeof(double) * 4 * kNX * nd);
     double* gfl = rf_gf + (int64_t)la * 4 * nline;
     for (int e = 0; e < 4 * nline; ++e) gfl[e] = 0.0;
-    (void)pol;   // without a line in window (inwin == 0): Feautrier below
     for (int k = 0; k < nd; ++k) {
       cc[k] = R(chi_c[(int64_t)la * nd + k]);
       ec[k] = R(eta_c[(int64_t)la * nd + k]);
@@ -169,21 +168,27 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     const double B0 = planck(T[nd - 2], lm), B1 = planck(T[nd - 1], lm);
     R out[4];
     delo_forward<R>(tape, ds, nd, B0, B1, out, qop);
+    // the reference's solver: Feautrier without a line in window, scalar
+    // Bezier3 when no line in window is polarizable, DELO-Bezier3 otherwise
     static FeautTape<R> ft;
-    static FeautAdj<R> fadj;
+    static ScalarTape<R> sbt;
+    static ScalarAdj<R> fadj;
     const bool feaut = inwin == 0u;
     if (feaut) {
       out[0] = feautrier_fwd<R>(tape, ds, nd, B0, B1, ft);
-      out[1] = out[2] = out[3] = R(0);
       feautrier_vjp<R>(tape, ds, nd, B0, B1, ft, R(1), fadj);
+    } else if (!pol) {
+      out[0] = scalar_bezier_fwd<R>(tape, ds, nd, B0, B1, sbt);
+      scalar_bezier_vjp<R>(tape, ds, nd, B0, B1, sbt, R(1), fadj);
     }
+    if (!pol) out[1] = out[2] = out[3] = R(0);
     for (int s = 0; s < 4; ++s) stokes[la * 4 + s] = double(out[s]);
-    const R one = feaut ? R(0) : R(1);
+    const R one = pol ? R(1) : R(0);
     const R seed[4][4] = {{one, 0, 0, 0}, {0, one, 0, 0}, {0, 0, one, 0}, {0, 0, 0, one}};
     R gfa[4 * PYRH_MAX_LINES];
     for (int e = 0; e < 4 * PYRH_MAX_LINES; ++e) gfa[e] = R(0);
     Emit<R, JAC> emit{nd, T, lm, rfl, nline, &ld[0][0], geo, dlam, inwin, ncomp, cs, cw, cq, cc, ec,
-                      &tape, gfa, dcc, dec, lup, ldn, feaut ? &fadj : nullptr};
+                      &tape, gfa, dcc, dec, lup, ldn, pol ? nullptr : &fadj};
     delo_reverse_stream<R, 4>(tape, ds, nd, B0, B1, seed, emit);
     for (int s = 0; s < 4; ++s)
       for (int l = 0; l < nline; ++l) gfl[s * nline + l] = double(gfa[s * PYRH_MAX_LINES + l]);

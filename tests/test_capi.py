@@ -99,9 +99,9 @@ def test_line_checks(golden):
                             fx["zeeman_n"][::-1].copy())
     assert lib.pyrh_check_lines(bad, n, L.PYRH_FULL_STOKES) == L.PYRH_ERR_ARG
     lc = fx["line_const"].copy()
-    lc[0, 18] = 0   # not polarizable -> Armstrong Voigt in the reference
+    lc[0, 18] = 0   # not polarizable: Armstrong's Voigt function, Stokes I only
     unp, _ = lte.make_lines(lc, fx["zeeman"], fx["zeeman_n"])
-    assert lib.pyrh_check_lines(unp, n, L.PYRH_FULL_STOKES) == L.PYRH_ERR_UNSUPPORTED
+    assert lib.pyrh_check_lines(unp, n, L.PYRH_FULL_STOKES) == L.PYRH_OK
     assert lib.pyrh_check_lines(lines, L.PYRH_MAX_LINES + 1, 3) == L.PYRH_ERR_ARG
 
 

@@ -42,7 +42,7 @@ def run(atms, precision, mu=1.0, api="host", **cfgkw):
     return [o.astype(np.float64) for o in lte.split_output(pk, out)]
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0", "lte_mixed"])
 def test_fp64_vs_reference(golden, name):
     fx = golden(name)
     m = O.output_mask(fx["lam"], fx["lambda_ref"])
@@ -52,7 +52,7 @@ def test_fp64_vs_reference(golden, name):
     assert np.all(out[1:, fx["tot_flags"][m][:, 1] == 0] == 0.0)
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0", "lte_mixed"])
 def test_fp64_vs_oracle(golden, name):
     fx = golden(name)
     out = run([fx], FP64, mu=float(fx["mu"]))[0]
@@ -60,7 +60,7 @@ def test_fp64_vs_oracle(golden, name):
     assert _err(out, ref).max() < 1e-8
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0", "lte_mixed"])
 def test_fp32_vs_oracle(golden, name):
     fx = golden(name)
     out = run([fx], FP32, mu=float(fx["mu"]))[0]
@@ -91,6 +91,16 @@ def test_no_stokes_mode(golden, precision, tol):
     out = run([fx], precision, stokes_mode=L.PYRH_NO_STOKES)[0]
     ref = O.lte_synth(fx, md_float=False, no_stokes=True)
     assert _err(out[:1], ref[:1]).max() < tol
+    assert np.all(out[1:] == 0.0)
+
+
+@pytest.mark.parametrize("precision,tol", [(FP64, 1e-8), (FP32, 1e-4)])
+def test_no_stokes_mode_vs_reference(golden, precision, tol):
+    """STOKES_MODE = NO_STOKES as the reference runs it (lte_nostokes)."""
+    fx = golden("lte_nostokes")
+    m = O.output_mask(fx["lam"], fx["lambda_ref"])
+    out = run([fx], precision, stokes_mode=L.PYRH_NO_STOKES)[0][:, m]
+    assert _err(out[:1], fx["stokes_ref"][:1]).max() < tol
     assert np.all(out[1:] == 0.0)
 
 

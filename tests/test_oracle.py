@@ -7,7 +7,8 @@ import pytest
 from conftest import batch_member
 from oracle import oracle as O
 
-LTE_CASES = ["lte_c0", "lte_edge", "lte_b0"]
+# lte_mixed: two unpolarizable lines (Armstrong's Voigt, kurucz.c:824)
+LTE_CASES = ["lte_c0", "lte_edge", "lte_b0", "lte_mixed"]
 
 
 def _err(mine, ref):
@@ -59,6 +60,30 @@ def test_oracle_opacity_matches_background_record(golden, name):
                         (np.abs(mine_e - tot_e) / abs(tot_e[0])).max())
             assert flags == (fx["tot_flags"][la][0] | (fx["tot_flags"][la][1] << 1))
     assert worst < 1e-12
+
+
+def test_oracle_no_stokes_vs_reference(golden):
+    """STOKES_MODE = NO_STOKES: pyrh keeps atmos.Stokes = TRUE
+    (pyrh_compute1dray.c:258), so the lines stay polarizable and their
+    Zeeman-summed Stokes I profile goes into the scalar Bezier3 solver
+    (formal.c:94-95); no 4x4 inverse is involved, and the oracle reproduces
+    the reference to rounding."""
+    fx = golden("lte_nostokes")
+    m = O.output_mask(fx["lam"], fx["lambda_ref"])
+    out = O.lte_synth(fx, no_stokes=True)[:, m]
+    assert _err(out, fx["stokes_ref"]).max() < 1e-12
+    assert np.all(fx["stokes_ref"][1:] == 0.0)
+
+
+def test_unpolarizable_lines_use_armstrong(golden):
+    fx = golden("lte_mixed")
+    pol = fx["line_const"][:, 18]
+    assert list(pol) == [0, 1, 0, 1] and list(fx["zeeman_n"][pol == 0]) == [0, 0]
+    # near 629.60 nm only the unpolarizable line is in its window: no Q, U, V
+    m = O.output_mask(fx["lam"], fx["lambda_ref"])
+    near = np.abs(fx["lam_out"] - 629.60) < 0.06
+    assert np.all(fx["stokes_ref"][1:, near] == 0.0)
+    assert fx["stokes_ref"][0, near].min() < 0.9 * fx["stokes_ref"][0, near].max()
 
 
 def test_oracle_batch_fixture(golden):

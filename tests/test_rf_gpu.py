@@ -70,7 +70,7 @@ def contract_err(got, seed, rf):
     return np.abs(got - want).max(axis=1) / np.where(scale > 0, scale, 1.0)
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_mixed"])
 @pytest.mark.parametrize("precision", [FP64, FP32])
 def test_rf_matches_cpu_adjoint(rf_harness, golden, name, precision):
     fx = golden(name)
@@ -92,11 +92,20 @@ def test_rf_matches_cpu_adjoint(rf_harness, golden, name, precision):
 @pytest.mark.parametrize("precision,tol", [(FP64, 1e-9), (FP32, 1e-5)])
 def test_rf_stokes_equal_forward_kernel(golden, precision, tol):
     """The RF kernel's forward sweep gives the synthesis kernel's spectra at
-    every wavelength: DELO-Bezier3 where a line is in its window, Feautrier
-    elsewhere (lte_edge has four such wavelengths, every case LAMBDA_REF)."""
+    every wavelength: DELO-Bezier3 where a polarizable line is in its
+    window, scalar Bezier3 where only unpolarizable lines are (lte_mixed),
+    Feautrier where none is (lte_edge has four such wavelengths, every case
+    LAMBDA_REF)."""
     b = golden("lte_batch")
     atms = [batch_member(b, i) for i in range(b["T"].shape[0])] + [golden("lte_edge")]
     atms[-1] = dict(atms[-1], mu=atms[0]["mu"])     # one ray per batch
+    # lte_mixed has its own line list: a batch of its own, scalar Bezier3
+    # near 629.60 nm
+    mixed = golden("lte_mixed")
+    dm, cm, sm_, _ = gpu_rf([mixed], precision)
+    dm.run(cm)
+    fm = lte.split_output(dm.pk, dm.out.cpu().numpy())[0]
+    assert np.abs(sm_[0] - fm).max() <= tol * fm[0].max()
     dev, cfg, st, _ = gpu_rf(atms, precision)
     dev.run(cfg)
     fwd = lte.split_output(dev.pk, dev.out.cpu().numpy())

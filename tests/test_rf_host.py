@@ -3,9 +3,11 @@ adjoint of DELO-Bezier3 plus dual-number Jacobians of the Zeeman/Voigt
 opacity), evaluated on the CPU through tests/native/rf_host.cu, against
 central finite differences of the oracle's synthesis.
 
-Wavelengths with no line inside its window are solved with Feautrier, as
-the reference does (feautrier.c:56-202), and differentiated through its
-elimination; the others with DELO-Bezier3.
+Each wavelength is solved, and differentiated, with the reference's solver
+(formal.c:94-95, 285-310): DELO-Bezier3 where a polarizable line is inside
+its window, scalar Bezier3 where only unpolarizable lines are (lte_mixed:
+Armstrong's Voigt function, kurucz.c:824), Feautrier where no line is
+(feautrier.c:56-202).
 
 Central differences of the whole synthesis are the reference's definition of
 depth-resolved response functions (rh/rhf1d/rf_ray.c:205-293: perturb one
@@ -67,7 +69,8 @@ def step(fx, key, k, rel):
     return rel * abs(base)
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_batch:0", "lte_batch:1"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_batch:0", "lte_batch:1",
+                                  "lte_mixed"])
 def test_adjoint_matches_finite_differences(rf_harness, golden, name):
     if ":" in name:
         n, i = name.split(":")
@@ -100,7 +103,7 @@ def test_adjoint_matches_finite_differences(rf_harness, golden, name):
     assert not bad, bad
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_mixed"])
 def test_single_precision_adjoint(rf_harness, golden, name):
     fx = golden(name)
     win = delo_wavelengths(fx)
@@ -112,7 +115,7 @@ def test_single_precision_adjoint(rf_harness, golden, name):
         assert np.percentile(e, 99.9) < 2e-4 and e.max() < 1e-3, (PARAMS[x], e.max())
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_batch:0"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_batch:0", "lte_mixed"])
 def test_reverse_mode_opacity_contraction_equals_forward_mode(rf_harness, golden, name):
     """dL/dx through the opacity in reverse mode (local_q_vjp, what the GPU
     kernel runs) equals the contraction of the forward-mode local Jacobian
