@@ -106,6 +106,46 @@ int harness_synth(const char *cwd, double mu, int Ndep, const double *atm,
   return n;
 }
 
+/* harness_synth with log gf values overriding the line list's
+   (loggf_ids: 0-based order of the lines in the list file,
+   kurucz.c:250-260) and, with get_atomic_rfs, the reference's analytical
+   d I / d log gf of those lines (pyrh_solveray.c:144-148), written to
+   rfs[Nloggf][out_cap].  Stokes I only. */
+int harness_synth_loggf(const char *cwd, double mu, int Ndep, const double *atm,
+                        int Nwave, const double *lam, int Nloggf, const int *loggf_ids,
+                        const double *loggf_values, int get_atomic_rfs, int out_cap,
+                        double *out_lam, double *sI, double *rfs)
+{
+  double *a = (double *) malloc(9 * Ndep * sizeof(double));
+  double *w = (double *) malloc(Nwave * sizeof(double));
+  int *ids = (int *) malloc(Nloggf * sizeof(int));
+  double *vals = (double *) malloc(Nloggf * sizeof(double));
+  memcpy(a, atm, 9 * Ndep * sizeof(double));
+  memcpy(w, lam, Nwave * sizeof(double));
+  memcpy(ids, loggf_ids, Nloggf * sizeof(int));
+  memcpy(vals, loggf_values, Nloggf * sizeof(double));
+
+  mySpectrum s = rhf1d((char *) cwd, mu, Ndep,
+                       a + 0 * Ndep, a + 1 * Ndep, a + 2 * Ndep, a + 3 * Ndep,
+                       a + 4 * Ndep, a + 5 * Ndep, a + 6 * Ndep, a + 7 * Ndep,
+                       a + 8 * Ndep, 0, Nwave, w,
+                       0, NULL, NULL, Nloggf, ids, vals, 0, NULL, NULL,
+                       0, NULL, NULL, get_atomic_rfs, 0, 0, NULL);
+  int n = s.nlw;
+  if (n > out_cap) n = -1;
+  else {
+    for (int i = 0; i < n; i++) {
+      out_lam[i] = s.lam[i];
+      sI[i] = s.sI[i];
+      if (get_atomic_rfs)
+        for (int p = 0; p < Nloggf; p++) rfs[(long) p * out_cap + i] = s.rfs[i][p];
+    }
+  }
+  free(s.lam); free(s.sI); free(s.sQ); free(s.sU); free(s.sV);
+  free(a); free(w); free(ids); free(vals);
+  return n;
+}
+
 /* Set-up sequence of rhf1d() up to convertScales(), in the same order as
    pyrh_compute1dray.c:130-311, followed by a dump of the hot-path inputs. */
 int harness_dump_lte(const char *cwd, double mu, int Ndep, const double *atm,

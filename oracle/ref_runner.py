@@ -153,6 +153,26 @@ def _synth_job(args):
     return lam, np.stack([sI, sQ, sU, sV]), flag.value
 
 
+def _loggf_job(args):
+    workdir, pyrh_path, mu, atm, wave, ids, vals, get_rfs = args
+    lib = _lib(pyrh_path)
+    atm = np.ascontiguousarray(atm, dtype=np.float64)
+    wave = np.ascontiguousarray(wave, dtype=np.float64)
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    vals = np.ascontiguousarray(vals, dtype=np.float64)
+    cap = len(wave) + 4096
+    lam, sI = np.zeros(cap), np.zeros(cap)
+    rfs = np.zeros((len(ids), cap))
+    lib.harness_synth_loggf.restype = C.c_int
+    n = lib.harness_synth_loggf(workdir.encode(), C.c_double(mu), atm.shape[1], _p(atm),
+                                len(wave), _p(wave), len(ids),
+                                ids.ctypes.data_as(C.POINTER(C.c_int)), _p(vals), int(get_rfs),
+                                cap, _p(lam), _p(sI), _p(rfs))
+    if n < 0:
+        raise RuntimeError("reference output larger than capacity")
+    return lam[:n].copy(), sI[:n].copy(), rfs[:, :n].copy()
+
+
 def _dump_job(args):
     workdir, pyrh_path, mu, atm, wave, outdir = args
     lib = _lib(pyrh_path)
@@ -217,6 +237,9 @@ class Reference:
 
     def synth(self, workdir, mu, atm, wave):
         return self._run(_synth_job, (workdir, self.pyrh_path, mu, atm, wave))
+
+    def synth_loggf(self, workdir, mu, atm, wave, ids, vals, get_rfs=True):
+        return self._run(_loggf_job, (workdir, self.pyrh_path, mu, atm, wave, ids, vals, get_rfs))
 
     def dump_lte(self, workdir, mu, atm, wave, outdir):
         return self._run(_dump_job, (workdir, self.pyrh_path, mu, atm, wave, outdir))

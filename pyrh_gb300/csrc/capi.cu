@@ -162,9 +162,9 @@ pyrh_status check_rf(const pyrh_lte_batch* b, const pyrh_lte_config* cfg, int nl
   s = check_batch_shape(b, nline);
   if (s != PYRH_OK) return s;
   if (nline > 0 && !lines) return fail(PYRH_ERR_ARG, "lines is NULL");
-  if (cfg->stokes_mode != PYRH_FULL_STOKES || cfg->magneto_optical)
+  if (cfg->magneto_optical)
     return fail(PYRH_ERR_UNSUPPORTED,
-                "response functions need FULL_STOKES without magneto-optical terms");
+                "response functions without magneto-optical terms only");
   if (b->max_ndep > PYRH_RF_MAX_DEPTH)
     return fail(PYRH_ERR_UNSUPPORTED, "max_ndep %d above PYRH_RF_MAX_DEPTH %d", b->max_ndep,
                 PYRH_RF_MAX_DEPTH);

@@ -236,8 +236,10 @@ __device__ __forceinline__ void rf_lane(const RfArgs& ra, const RfSmem<R>& sm, i
     // the reference's solver for this wavelength (formal.c:94-95,
     // 285-310): Feautrier without a line in window, scalar Bezier3 when
     // none of the lines in window is polarizable, DELO-Bezier3 otherwise
+    // (NO_STOKES: scalar throughout, formal.c:94-95)
     bool pol = false;
     for (int l = 0; l < nline; ++l) pol |= ((loc.inwin >> l) & 1u) && sm.polar[l];
+    pol = pol && args.stokes_mode == PYRH_FULL_STOKES;
     const bool feaut = loc.inwin == 0u;
     const bool feaut_or_scalar = !pol;
     FeautTape<R> ftape;

@@ -52,14 +52,16 @@ def rf_harness(tmp_path_factory):
     return C.CDLL(out)
 
 
-def rf_eval(lib, fx, sel, single=False, jac=False, loggf=False, setup_dT=None):
+def rf_eval(lib, fx, sel, single=False, jac=False, loggf=False, setup_dT=None,
+            no_stokes=False):
     """Stokes [nsel, 4] and response functions [nsel, 4, 6, ndep] of one
     atmosphere at the wavelengths fx["lam"][sel] (CPU harness, FP64 or, with
     single=True, FP32; jac=True takes the opacity derivatives in forward
     mode); loggf=True also returns dS/dlog10(gf) [nsel, 4, nline].
     setup_dT: optional dict of the set-up's temperature derivatives
     (dchi_c, deta_c [lambda][depth]; dline_pops [line][2][depth]; dnp,
-    dlen_up, dlen_dn [depth]); missing keys are held fixed."""
+    dlen_up, dlen_dn [depth]); missing keys are held fixed.  no_stokes:
+    STOKES_MODE = NO_STOKES (scalar solvers throughout)."""
     from pyrh_gb300 import lte
     D = C.POINTER(C.c_double)
     keep = []
@@ -90,7 +92,11 @@ def rf_eval(lib, fx, sel, single=False, jac=False, loggf=False, setup_dT=None):
                  arr(g("deta_c")[sel]) if g("deta_c") is not None else None]
         args += [arr(g(k)) if g(k) is not None else None
                  for k in ("dline_pops", "dnp", "dlen_up", "dlen_dn")]
-    r = fn(*args)
+    lib.rf_set_stokes_mode(0 if no_stokes else 3)
+    try:
+        r = fn(*args)
+    finally:
+        lib.rf_set_stokes_mode(3)
     assert r == 0
     return (st, rf, gf) if loggf else (st, rf)
 

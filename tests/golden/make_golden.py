@@ -20,6 +20,9 @@ Fixtures (npz, float64):
   lte_nostokes    C0 in STOKES_MODE = NO_STOKES
   lte_mixed       C0 with two unpolarizable lines (Armstrong's Voigt), one
                   alone in its window and one among the polarized lines
+  lte_loggf       the reference's analytical log gf RFs of Stokes I (NO_STOKES
+                  C0, both lines) and central differences of its synthesis in
+                  log gf
   lte_batch       6 atmospheres of the batched generator (2 x 112 lambda)
   lte_c0_dT, lte_edge_dT
                   temperature derivatives of the set-up inputs of lte_c0 /
@@ -162,6 +165,43 @@ def make_lte_modes(ref, wd):
     wave = np.concatenate([wl.line_wavelengths(41, 0.05, centres=(629.60,)),
                            np.linspace(630.10, 630.30, 121)])
     lte_case(ref, "lte_mixed", atm, wave, linelist=wl.fe_linelist(lines))
+
+
+def make_lte_loggf(ref, wd):
+    """The reference's analytical log gf response functions of Stokes I
+    (compute1d(..., loggf_ids, loggf_values, get_atomic_rfs=True); only its
+    scalar solver propagates them, so STOKES_MODE = NO_STOKES,
+    formal.c:214-235) for both lines of C0, and central differences of the
+    same synthesis in log gf (the line list's values moved by +-h through
+    the same override, kurucz.c:250-260) for comparison."""
+    logtau, T, ne, nH = base_c0(ref, wd)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH)
+    wave = wl.line_wavelengths(101, 0.05)
+    w = rr.scratch_dir()
+    rr.write_inputs(w, wl.fe_linelist(), stokes_mode="NO_STOKES")
+    ids = np.array([0, 1], np.int32)
+    base = np.array([L["loggf"] for L in wl.FE_LINES])
+    lam, sI, rfs = ref.synth_loggf(w, 1.0, atm, wave, ids, base, True)
+    steps = np.array([1e-2, 1e-3, 1e-4])
+    jobs = []
+    for l in range(2):
+        for h in steps:
+            for sgn in (1, -1):
+                v = base.copy()
+                v[l] += sgn * h
+                jobs.append((w, ref.pyrh_path, 1.0, atm, wave, ids, v, False))
+    res = ref.map(rr._loggf_job, jobs)
+    fd = np.zeros((2, len(steps), len(lam)))
+    i = 0
+    for l in range(2):
+        for b, h in enumerate(steps):
+            fd[l, b] = (res[i][1] - res[i + 1][1]) / (2 * h)
+            i += 2
+    path = os.path.join(HERE, "lte_loggf.npz")
+    np.savez_compressed(path, lam_out=lam, sI=sI, rf_analytic=rfs, fd_steps=steps, fd_loggf=fd,
+                        loggf=base, atm=atm, wave=wave)
+    shutil.rmtree(w, ignore_errors=True)
+    print(f"lte_loggf: {len(lam)} lambda, {os.path.getsize(path) / 1e3:.0f} kB")
 
 
 def make_lte_b0(ref, wd):
@@ -311,7 +351,7 @@ def make_nlte(ref, wd):
 
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
-          "lte_modes": make_lte_modes,
+          "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
           "nlte": make_nlte}
 
 

@@ -19,6 +19,10 @@ using namespace pyrh;
 
 // Optional temperature derivatives of the set-up (null members: held fixed);
 // layouts as rf_eval_t's inputs ([nlam][nd], [nline][2][nd], [nd]).
+// STOKES_MODE of the next evaluations (PYRH_FULL_STOKES or PYRH_NO_STOKES)
+static int g_stokes_mode = PYRH_FULL_STOKES;
+extern "C" void rf_set_stokes_mode(int mode) { g_stokes_mode = mode; }
+
 struct SetupDT {
   const double *dchi_c, *deta_c, *dline_pops, *dnp, *dlen_up, *dlen_dn;
 };
@@ -148,7 +152,7 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
       dlam[l] = R(lm - lines[l].lambda0);
       if (fabs(lines[l].lambda0 - lm) <= dlc && lines[l].contributes) {
         inwin |= 1u << l;
-        pol |= lines[l].polarizable != 0;
+        pol |= lines[l].polarizable != 0 && g_stokes_mode == PYRH_FULL_STOKES;
       }
     }
     double* rfl = rf + (int64_t)la * 4 * kNX * nd;

@@ -25,6 +25,7 @@ import numpy as np
 import pytest
 
 from conftest import batch_member, delo_wavelengths, rf_eval
+from oracle import oracle as O
 from pyrh_gb300 import _lib as L
 from pyrh_gb300 import lte, rf as RF
 
@@ -298,3 +299,45 @@ def test_loggf_rf_matches_cpu_adjoint(rf_harness, golden, precision, tol):
     want = np.einsum("sl,nsl->n", seed, gfs)
     scale = np.einsum("sl,nsl->n", np.abs(seed), np.abs(gfs))
     assert np.all(np.abs(gc.cpu().numpy()[0] - want) <= (1e-10 if precision == FP64 else 1e-3) * scale)
+
+
+@pytest.mark.parametrize("precision", [FP64, FP32])
+def test_no_stokes_rf_matches_cpu_adjoint(rf_harness, golden, precision):
+    """STOKES_MODE = NO_STOKES through pyrh_lte_rf: Stokes I and its response
+    functions (scalar solvers at every wavelength) and the log gf RFs,
+    against the CPU adjoint, and the log gf RFs against central differences
+    of the reference's own synthesis in log gf (lte_loggf, 1e-5 in FP64)."""
+    import torch
+    fx, g = golden("lte_nostokes"), golden("lte_loggf")
+    lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
+    cfg = lte.make_config(precision=precision, mu=float(fx["mu"]),
+                          vmicro_char=float(fx["vmicro_char"]), moving=bool(fx["moving"]),
+                          stokes_mode=L.PYRH_NO_STOKES)
+    dev = lte.DeviceBatch(lte.pack([fx], n, precision), lines, n)
+    rf, gf = RF.response_functions(dev, cfg, loggf=True)
+    torch.cuda.synchronize()
+    mine = RF.split_rf(dev.pk, rf.cpu().numpy().astype(np.float64))[0]      # [4, 6, nd, nlam]
+    mine_gf = RF.split_loggf_rf(dev.pk, n, gf.cpu().numpy().astype(np.float64))[0]
+    sel = np.arange(len(fx["lam"]))
+    st_h, rf_h, gf_h = rf_eval(rf_harness, fx, sel, loggf=True, no_stokes=True)
+    ref = rf_h.transpose(1, 2, 3, 0)
+    assert np.all(mine[1:] == 0.0)
+    if precision == FP64:
+        assert rel_err(mine, ref) < 1e-8
+    else:
+        for x in range(6):
+            scale = np.abs(ref[0, x]).max()
+            if scale == 0.0:          # the azimuth does not reach Stokes I
+                assert np.all(mine[0, x] == 0.0)
+                continue
+            e = np.abs(mine[0, x] - ref[0, x]) / scale
+            assert np.percentile(e, 99.9) < 2e-4 and e.max() < 1e-3, (PARAMS[x], e.max())
+    ref_gf = gf_h.transpose(2, 1, 0)                 # [line, stokes, lambda]
+    tol = 1e-8 if precision == FP64 else 1e-4
+    assert np.abs(mine_gf - ref_gf).max() <= tol * np.abs(ref_gf).max()
+    if precision == FP64:
+        out = O.output_mask(fx["lam"], float(fx["lambda_ref"]))
+        for l in range(n):
+            fd = g["fd_loggf"][l]
+            err = np.min(np.abs(fd - mine_gf[l, 0, out]), axis=0).max() / np.abs(fd).max()
+            assert err < 1e-5, (l, err)
