@@ -179,10 +179,10 @@ __device__ __forceinline__ void acc_add(float* hi, float* lo, float v) {
 // Per-block staging of the quantities every thread reads at every depth.
 template <typename R>
 struct NlteShared {
-  R* Gs;      // [nlev^2][nd] Gamma of this block's wavelengths
-  R* Gl;      // [nlev^2][nd] compensation terms of Gs (FP32 mode)
+  R* Gs;      // [nlev (nlev - 1)][nd] off-diagonal Gamma of this block's wavelengths
+  R* Gl;      // the same, compensation terms of Gs (FP32 mode)
   R* Js;      // [nd][32] new J of this block's wavelengths
-  R* Jl;      // [nd][32] compensation terms of Js (FP32 mode)
+  R* Jl;      // unused (J is summed without compensation)
   R* n;       // [nlev][nd] populations
   R* lnst;    // [nlev][nd] log of the LTE populations
   R* iT;      // [nd] 1 / T
@@ -367,6 +367,11 @@ __device__ R feautrier_full(const R* chi, const R* S, const R* ds, int nd, doubl
   return R(2) * P[0];
 }
 
+// Row of Gamma entry (i, j), i != j, in the off-diagonal arrays Gs / Gl.
+__host__ __device__ inline int gamma_slot(int i, int j, int nlev) {
+  return i * (nlev - 1) + j - (j > i ? 1 : 0);
+}
+
 template <typename R>
 __host__ __device__ inline size_t formal_smem_layout(int nlev, int nd, int nrays, int nline,
                                                      NlteShared<R>* sh, unsigned char* base) {
@@ -377,10 +382,13 @@ __host__ __device__ inline size_t formal_smem_layout(int nlev, int nd, int nrays
     return p;
   };
   const bool comp = sizeof(R) == 4;
-  R* Gs = take((size_t)nlev * nlev * nd);
-  R* Gl = take(comp ? (size_t)nlev * nlev * nd : 0);
+  // Gamma: the off-diagonal entries only (transitions are between different
+  // levels), addressed by gamma_slot; J without compensation terms (it sums
+  // at most 2 * PYRH_NLTE_MAX_RAYS terms per entry)
+  R* Gs = take((size_t)nlev * (nlev - 1) * nd);
+  R* Gl = take(comp ? (size_t)nlev * (nlev - 1) * nd : 0);
   R* Js = take((size_t)nd * 32);
-  R* Jl = take(comp ? (size_t)nd * 32 : 0);
+  R* Jl = nullptr;
   R* n = take((size_t)nlev * nd);
   R* lnst = take((size_t)nlev * nd);
   R* iT = take((size_t)nd);
@@ -411,13 +419,12 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
   formal_smem_layout<R>(nlev, b.max_ndep, A.nrays, b.max_nline, &sh, smem_raw);
   const int nthr = blockDim.x;
   const bool comp = sizeof(R) == 4;
-  for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) {
+  for (int e = threadIdx.x; e < nlev * (nlev - 1) * nd; e += nthr) {
     sh.Gs[e] = R(0);
     if (comp) sh.Gl[e] = R(0);
   }
   for (int e = threadIdx.x; e < nd * 32; e += nthr) {
     sh.Js[e] = R(0);
-    if (comp) sh.Jl[e] = R(0);
   }
   for (int e = threadIdx.x; e < nlev * nd; e += nthr) {
     const int i = e / nd, k = e % nd;
@@ -519,7 +526,7 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
       const int nm = coll ? __reduce_max_sync(full, nact) : nact;
       // Gamma, coupling and J at every depth (fillgamma.c:82-332, formal.c:247-256)
       for (int k = 0; k < nd; ++k) {
-        if (mine) acc_add(&sh.Js[k * 32 + lane], &sh.Jl[k * 32 + lane], wdir * I[k]);
+        if (mine) atomicAdd(&sh.Js[k * 32 + lane], wdir * I[k]);
         if (!eval_operator) continue;
         const R psi = mine ? Psi[k] / chis[k] : R(0);
         const R Ieff_k = !mine ? R(0) : angle_dep ? Ieff[k] : I[k] - psi * Ieff[k];
@@ -576,8 +583,9 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
           }
           if (key < 0) continue;
           const int i = key / nlev, j = key % nlev;
-          acc_add(&sh.Gs[(i * nlev + j) * nd + k], &sh.Gl[(i * nlev + j) * nd + k], gij);
-          acc_add(&sh.Gs[(j * nlev + i) * nd + k], &sh.Gl[(j * nlev + i) * nd + k], gji);
+          const int sij = gamma_slot(i, j, nlev) * nd + k, sji = gamma_slot(j, i, nlev) * nd + k;
+          acc_add(&sh.Gs[sij], &sh.Gl[sij], gij);
+          acc_add(&sh.Gs[sji], &sh.Gl[sji], gji);
         }
       }
     }
@@ -587,13 +595,14 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
   for (int e = threadIdx.x; e < nd * 32; e += nthr) {
     const int k = e / 32, l = e % 32;
     if (la0 + l < ns)
-      A.Jnew[coff + (int64_t)k * ns + la0 + l] = (double)sh.Js[e] + (comp ? (double)sh.Jl[e] : 0.0);
+      A.Jnew[coff + (int64_t)k * ns + la0 + l] = (double)sh.Js[e];
   }
   if (eval_operator)
-    for (int e = threadIdx.x; e < nlev * nlev * nd; e += nthr) {
-      const int ij = e / nd, k = e % nd;
+    for (int e = threadIdx.x; e < nlev * (nlev - 1) * nd; e += nthr) {
+      const int s = e / nd, k = e % nd;
+      const int i = s / (nlev - 1), jj = s % (nlev - 1), j = jj + (jj >= i ? 1 : 0);
       const double v = (double)sh.Gs[e] + (comp ? (double)sh.Gl[e] : 0.0);
-      if (v != 0.0) atomicAdd(&A.Gamma[(int64_t)ij * b.total_depth + doff + k], v);
+      if (v != 0.0) atomicAdd(&A.Gamma[(int64_t)(i * nlev + j) * b.total_depth + doff + k], v);
     }
 }
 
