@@ -181,8 +181,8 @@ template <typename R>
 struct NlteShared {
   R* Gs;      // [nlev (nlev - 1)][nd] off-diagonal Gamma of this block's wavelengths
   R* Gl;      // the same, compensation terms of Gs (FP32 mode)
-  R* Js;      // [nd][32] new J of this block's wavelengths
-  R* Jl;      // unused (J is summed without compensation)
+  R* Js;      // [nd][32] new J of this block's wavelengths (no compensation:
+              // at most 2 PYRH_NLTE_MAX_RAYS terms per entry)
   R* n;       // [nlev][nd] populations
   R* lnst;    // [nlev][nd] log of the LTE populations
   R* iT;      // [nd] 1 / T
@@ -388,13 +388,12 @@ __host__ __device__ inline size_t formal_smem_layout(int nlev, int nd, int nrays
   R* Gs = take((size_t)nlev * (nlev - 1) * nd);
   R* Gl = take(comp ? (size_t)nlev * (nlev - 1) * nd : 0);
   R* Js = take((size_t)nd * 32);
-  R* Jl = nullptr;
   R* n = take((size_t)nlev * nd);
   R* lnst = take((size_t)nlev * nd);
   R* iT = take((size_t)nd);
   R* ds = take((size_t)nrays * nd);
   R* wphi = take((size_t)(nline > 0 ? nline : 1) * nd);
-  if (sh) *sh = NlteShared<R>{Gs, Gl, Js, Jl, n, lnst, iT, ds, wphi};
+  if (sh) *sh = NlteShared<R>{Gs, Gl, Js, n, lnst, iT, ds, wphi};
   return off;
 }
 
