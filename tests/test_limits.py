@@ -5,6 +5,8 @@ At the limits (GPU, marked `gpu`):
     1e-8 of I_c and FP32 to 1e-4 (the tolerances of test_lte_gpu.py);
   * PYRH_RF_MAX_DEPTH (160) depths in the response functions, FP64 against
     the CPU adjoint to 1e-8 of each parameter's largest |RF|;
+  * PYRH_NLTE_MAX_DEPTH (160) depths in the NLTE solve, against the NLTE
+    oracle (FP64 1e-6 and the same iteration count, FP32 1e-3);
   * PYRH_MAX_LINES (16) lines, one of them with PYRH_MAX_COMPONENTS (32)
     Zeeman components, all inside their windows at every wavelength, in the
     synthesis (against the oracle) and in the response functions at 71
@@ -173,6 +175,48 @@ def test_response_functions_with_max_lines_and_components(rf_harness, golden, pr
             assert np.percentile(e, 99.9) < 1e-3 and e.max() < 3e-3, (RF.PARAMS[x], e.max())
 
 
+NLTE_LOG = ("T", "ne", "nHtot", "ntotal", "vbroad", "background", "nstar", "n0", "adamp")
+NLTE_LIN = ("vel", "vturb", "height", "C", "wphi", "atm")
+NLTE_REF = ("Gamma1", "J1", "n1", "n_final", "J_final", "I_out", "phi_sample", "phi_sample_la")
+
+
+def deepen_nlte(fx: dict, nd: int) -> dict:
+    """An NLTE fixture on nd depths (interpolated in depth index, log of the
+    positive quantities); the reference's results are dropped."""
+    n0 = len(fx["T"])
+    x0, x = np.arange(n0), np.linspace(0, n0 - 1, nd)
+    out = {k: v for k, v in fx.items() if k not in NLTE_REF}
+    for k in NLTE_LOG + NLTE_LIN:
+        v = np.asarray(fx[k], np.float64)
+        rows = v.reshape(-1, n0)
+        if k in NLTE_LOG:
+            r = np.stack([np.exp(np.interp(x, x0, np.log(row))) for row in rows])
+        else:
+            r = np.stack([np.interp(x, x0, row) for row in rows])
+        out[k] = r.reshape(v.shape[:-1] + (nd,)) if v.ndim > 1 else r[0]
+    m = np.array(fx["meta"]).copy()
+    m[1] = nd
+    out["meta"] = m
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,tol", [(FP64, 1e-6), (FP32, 1e-3)])
+def test_nlte_at_max_depth(golden, precision, tol):
+    """PYRH_NLTE_MAX_DEPTH (160) depths: the C1 atmosphere interpolated onto
+    160 depths, solved to convergence on the GPU and by the NLTE oracle (35
+    iterations); FP64 takes the same number of iterations."""
+    from pyrh_gb300 import nlte
+    fx = deepen_nlte(golden("nlte_c1"), L.PYRH_NLTE_MAX_DEPTH)
+    n_or, _, it_or, _, _ = O.nlte_solve(fx)
+    cfg = nlte.make_config(fx, precision)
+    dev = nlte.DeviceNlte(nlte.pack([fx], cfg.nrays), cfg)
+    assert dev.solve(cfg) == L.PYRH_OK, L.lib().pyrh_last_error()
+    if precision == FP64:
+        assert int(dev.iterations.cpu()[0]) == it_or
+    assert np.abs(dev.populations()[0] / n_or - 1).max() < tol
+
+
 # ----------------------------------------------------------------- CPU ---
 
 def _host_batch(fx, n):
@@ -226,6 +270,15 @@ def test_limits_rejected_before_launch(golden):
     C.memmove(bad, lines, C.sizeof(L.PyrhLine))
     bad[0].ncomp = L.PYRH_MAX_COMPONENTS + 1
     assert lib.pyrh_check_lines(bad, 1, L.PYRH_FULL_STOKES) == L.PYRH_ERR_ARG
+
+
+def test_deepened_nlte_problem_matches_at_original_depths(golden):
+    """deepen_nlte at the fixture's own depth count changes nothing: the
+    oracle still reproduces the reference's converged populations."""
+    fx = golden("nlte_c1")
+    same = deepen_nlte(fx, len(fx["T"]))
+    n, _, it, _, _ = O.nlte_solve(same)
+    assert np.abs(n / fx["n_final"] - 1).max() < 1e-8
 
 
 def test_deepened_atmosphere_is_a_valid_input(golden):
