@@ -87,8 +87,13 @@ __global__ void nlte_profile_kernel(NlteArgs A) {
     if (A.moving) v += (to_obs ? 1.0 : -1.0) * A.muz[mu] * b.vel[doff + k] / vb;
     const double a = L.voigt ? b.adamp[b.adamp_off[p] + (int64_t)L.line_index * nd + k] : 0.0;
     const int64_t idx = L.phi_off + r;
+    // Armstrong's function in the precision the profile is stored in: in
+    // FP32 mode the FP64 evaluation (FP64 pipe saturated, a tenth of the
+    // solve) would be rounded to FP32 anyway
+    const double H = sizeof(R) == 4 ? (double)voigt_armstrong_t<float>(float(a), float(v))
+                                    : voigt_armstrong(a, v);
     if (idx < A.phi_cap)
-      static_cast<R*>(A.phi)[idx] = R(voigt_armstrong(a, v) * L.c_fraction / (kSQRTPI * vb));
+      static_cast<R*>(A.phi)[idx] = R(H * L.c_fraction / (kSQRTPI * vb));
     else
       atomicOr(A.err, 1);
   }
