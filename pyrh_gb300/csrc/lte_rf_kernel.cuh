@@ -337,9 +337,12 @@ __device__ __noinline__ void rf_lane_unpol(const RfArgs& ra, const RfSmem<R>& sm
 
 // Single-seed modes in FP32 are capped at 128 registers (4 blocks of 128
 // threads per SM): measured 31.5 ms against 35.8 ms uncapped for the
-// gradient of 4096 atmospheres x 224 wavelengths.
+// gradient of 4096 atmospheres x 224 wavelengths, and 32.4 ms at 3 blocks.
+// The four-seed full response functions at 168 registers (3 blocks; 120
+// bytes of spills): 59.2 ms against 62.2 ms at 245 registers (2 blocks) and
+// 61.6 ms at 128 registers (4 blocks, 900 bytes of spills).
 template <typename R, int MODE>
-__global__ void __launch_bounds__(128, (sizeof(R) == 4 && MODE != 0) ? 4 : 1)
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? (MODE != 0 ? 4 : 3) : 1)
 lte_rf_kernel(RfArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const LteArgs& args = ra.lte;
