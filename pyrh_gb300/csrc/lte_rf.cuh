@@ -433,8 +433,19 @@ constexpr int kZ = 12;
 // sums of the first kZLines in-window lines are stored in z.
 // UP = false leaves out the branch for lines that are not polarizable (for
 // blocks without them; see lte_rf_kernel.cuh).
+// Out of line on the device: the forward sweep calls it from four sites
+// (three boundary depths and the loop), and one copy of its body instead of
+// four keeps the adjoint kernel's instructions in cache.  Measured on the
+// chi^2 gradient of 4096 atmospheres x 224 wavelengths: 29.4 -> 26.5 ms
+// (full response functions 59.1 -> 55.8 ms); taking the reverse-sweep
+// contraction (local_q_vjp) out of line as well measured slower.
+#ifdef __CUDA_ARCH__
+#define PYRH_OUTLINE __host__ __device__ __noinline__
+#else
+#define PYRH_OUTLINE inline
+#endif
 template <typename R, bool SUMS = false, bool UP = true>
-PYRH_HD void local_q(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
+PYRH_OUTLINE void local_q(int nline, const LineDepth<R>* ld, int ld_stride, const GeoD<R>& geo,
                      const R* dlam, unsigned inwin, const int* ncomp, const R* cshift,
                      const R* cweight, const int* cq, int maxcomp, R chi_c, R eta_c, R q[8],
                      R (*z)[kZ] = nullptr) {
