@@ -1043,6 +1043,39 @@ PYRH_HD void w3_d(double dtau, double w[3], double dw[2]) {
   }
 }
 
+// A hint that moves the cache line of p (generic address: the tape in local
+// memory or a global array) into L1; nothing on the host.
+PYRH_HD void prefetch_l1(const void* p) {
+#ifdef __CUDA_ARCH__
+  asm volatile("prefetch.L1 [%0];" ::"l"(p));
+#else
+  (void)p;
+#endif
+}
+
+// The tape entries that reverse step k+1 reads first (and the profile sums
+// of depth k-1, which the emit after that step contracts): requested during
+// step k so that they arrive while it computes.  Local memory is laid out
+// word by word across the 32 threads of a warp, so one request per word.
+// Chi^2 gradient of 4096 atmospheres x 224 wavelengths: 26.5 -> 25.4 ms;
+// adding L2 requests three steps ahead measured slower (27.6 ms).
+template <typename R>
+PYRH_HD void prefetch_step(const Tape<R>& tp, int k, int N) {
+  const auto pf = [](const void* p) { prefetch_l1(p); };
+  const int k1 = k + 1 < N ? k + 1 : N - 1, k2 = k + 2 < N ? k + 2 : N - 1;
+  pf(&tp.T[k1]);
+  pf(&tp.dchi[k1]);
+  for (int n = 0; n < 8; ++n) pf(&tp.q[k2][n]);
+  for (int n = 0; n < 4; ++n) {
+    pf(&tp.I[k2][n]);
+    pf(&tp.dS0[k2][n]);
+  }
+  for (int n = 0; n < 3; ++n) pf(&tp.dK0[k2][n]);
+  if (k >= 1)
+    for (int j = 0; j < kZLines; ++j)
+      for (int n = 0; n < kZ; ++n) pf(&tp.z[k - 1][j][n]);
+}
+
 // Reverse (adjoint) sweep of delo_forward for NS seeds (seed[s][4] =
 // dL_s/dI_0).  dL/dq_j is handed to emit(j, qb_j, bpl, sdn, sup) as soon as
 // no later step can add to it (step k reaches depths k-2 .. k+1), so only
@@ -1143,6 +1176,7 @@ PYRH_HD void delo_reverse_stream(const Tape<R>& tp, const R* ds, int nd, double 
   }
   // ---- steps k = 1 .. N-2 (reverse order of the forward sweep) ----
   for (int k = 1; k <= N - 2; ++k) {
+    prefetch_step(tp, k, N);
     const R Tk = tp.T[k], Tdw = tp.T[k - 1];
     StepIn<R> st;
     R cf[5], dcf[5];

@@ -169,6 +169,10 @@ struct Emit {
                        sm.ncomp, sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS, tp->q[k], qb,
                        g, gf, tp->z[k], loc->dchi_c ? loc->dchi_c[(int64_t)k * nl] : R(0),
                        loc->deta_c ? loc->deta_c[(int64_t)k * nl] : R(0));
+    if (loc->dchi_c && k + 1 < nd) {   // the set-up derivatives of the next emit
+      prefetch_l1(&loc->dchi_c[(int64_t)(k + 1) * nl]);
+      prefetch_l1(&loc->deta_c[(int64_t)(k + 1) * nl]);
+    }
     const R dB = (k >= nd - 2) ? R(planck_dT(T[k], lam)) : R(0);
     const R ldn = sm.len_dn[k], lup = (k + 1 < nd) ? sm.len_up[k + 1] : R(0);
 #pragma unroll
@@ -225,6 +229,10 @@ __device__ __forceinline__ void rf_lane(const RfArgs& ra, const RfSmem<R>& sm, i
 
     Tape<R> tp;
     auto qop = [&](int k, R* q) {
+      if (k >= 1) {   // the continuum of the depth the next call takes
+        prefetch_l1(&loc.chi_c[(int64_t)(k - 1) * nl]);
+        prefetch_l1(&loc.eta_c[(int64_t)(k - 1) * nl]);
+      }
       local_q<R, true, UP>(nline, sm.ld + k, args.maxd, sm.geo[k], loc.dlam, loc.inwin, sm.ncomp,
                        sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS,
                        loc.chi_c[(int64_t)k * nl], loc.eta_c[(int64_t)k * nl], q, tp.z[k]);
