@@ -195,9 +195,17 @@ pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nli
   if (smem > smem_limit())
     return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
                 nline, ra.lte.maxd);
+  // Sub-blocks (one work item each) per block: in FP32 one block holds the
+  // registers of a whole SM, so that the barrier between the forward and
+  // reverse sweeps aligns every resident warp; fewer where their shared
+  // tables do not fit together.
+  int sub = cfg->precision == PYRH_FP32 ? (mode != 0 ? 4 : 3) : 1;
+  while (sub > 1 && smem * sub > smem_limit()) --sub;
+  ra.sub = sub;
   const long long work = (long long)ra.lte.natm * ra.lte.tiles;
-  long long grid = cfg->persistent_blocks > 0 ? cfg->persistent_blocks : work;
-  if (grid > work) grid = work;
+  const long long blocks = (work + sub - 1) / sub;
+  long long grid = cfg->persistent_blocks > 0 ? cfg->persistent_blocks : blocks;
+  if (grid > blocks) grid = blocks;
   if (grid > 0x7fffffffLL) grid = 0x7fffffffLL;
   cudaError_t e = pyrh::launch_lte_rf(ra, block, (int)grid, st);
   if (e != cudaSuccess) return fail(PYRH_ERR_CUDA, "lte_rf launch: %s", cudaGetErrorString(e));

@@ -193,24 +193,35 @@ struct Emit {
   }
 };
 
-// The work of one lane (atmosphere p, wavelength la0 + threadIdx.x) of the
-// response-function kernel: forward sweep with tape, reverse sweep, and the
-// per-depth contraction.
+// The work of one lane (atmosphere p, wavelength la0 + t; t the thread's
+// place in its sub-block) of the response-function kernel: forward sweep
+// with tape, reverse sweep, and the per-depth contraction.  Every thread of
+// the block calls it (item: its sub-block holds a work item), because the
+// two sweeps are separated by a block-wide barrier.
 template <typename R, int MODE, bool UP>
 __device__ __forceinline__ void rf_lane(const RfArgs& ra, const RfSmem<R>& sm, int nline, int p,
-                                        int la0, int nl, int nd, int64_t doff) {
+                                        int la0, int nl, int nd, int64_t doff, int t, bool item) {
   const LteArgs& args = ra.lte;
   // Every lane of a warp that holds at least one wavelength runs the sweep
   // (lanes past the spectrum repeat its last wavelength with zero seeds and
   // write nothing), so the per-depth gradient sums can use full-warp
   // shuffles before one shared atomic per warp.
-  const bool act = la0 + (int)threadIdx.x < nl;
-  const int la = act ? la0 + (int)threadIdx.x : nl - 1;
-  if (la0 + (int)(threadIdx.x & ~31u) < nl) {
-    const int64_t loff = args.lam_off[p];
-    const double lam = args.lambda[loff + la];
+  const bool act = item && la0 + t < nl;
+  const int la = act ? la0 + t : nl - 1;
+  const bool run = item && la0 + (t & ~31) < nl;   // the same in every lane of a warp
+  int64_t loff = 0;
+  double lam = 0.0, B0 = 0.0, B1 = 0.0;
+  Local<R> loc;
+  Tape<R> tp;
+  R st[4] = {R(0), R(0), R(0), R(0)};
+  bool pol = false, feaut = false;
+  FeautTape<R> ftape;
+  ScalarTape<R> stape;
+  ScalarAdj<R> fadj;
+  if (run) {
+    loff = args.lam_off[p];
+    lam = args.lambda[loff + la];
     const double dlc = lam * kQ_WING * (args.vmicro_char / kCLIGHT);
-    Local<R> loc;
     loc.sm = &sm;
     loc.nline = nline;
     loc.maxd = args.maxd;
@@ -227,7 +238,6 @@ __device__ __forceinline__ void rf_lane(const RfArgs& ra, const RfSmem<R>& sm, i
     loc.deta_c = ra.dT.deta_c ? static_cast<const R*>(ra.dT.deta_c) + args.cont_off[p] + la
                               : nullptr;
 
-    Tape<R> tp;
     auto qop = [&](int k, R* q) {
       if (k >= 1) {   // the continuum of the depth the next call takes
         prefetch_l1(&loc.chi_c[(int64_t)(k - 1) * nl]);
@@ -237,38 +247,39 @@ __device__ __forceinline__ void rf_lane(const RfArgs& ra, const RfSmem<R>& sm, i
                        sm.cshift, sm.cweight, sm.cq, PYRH_MAX_COMPONENTS,
                        loc.chi_c[(int64_t)k * nl], loc.eta_c[(int64_t)k * nl], q, tp.z[k]);
     };
-    const double B0 = planck(args.T[doff + nd - 2], lam);
-    const double B1 = planck(args.T[doff + nd - 1], lam);
-    R st[4];
+    B0 = planck(args.T[doff + nd - 2], lam);
+    B1 = planck(args.T[doff + nd - 1], lam);
     delo_forward<R>(tp, sm.ds, nd, B0, B1, st, qop);
     // the reference's solver for this wavelength (formal.c:94-95,
     // 285-310): Feautrier without a line in window, scalar Bezier3 when
     // none of the lines in window is polarizable, DELO-Bezier3 otherwise
     // (NO_STOKES: scalar throughout, formal.c:94-95)
-    bool pol = false;
     for (int l = 0; l < nline; ++l) pol |= ((loc.inwin >> l) & 1u) && sm.polar[l];
     pol = pol && args.stokes_mode == PYRH_FULL_STOKES;
-    const bool feaut = loc.inwin == 0u;
-    const bool feaut_or_scalar = !pol;
-    FeautTape<R> ftape;
-    ScalarTape<R> stape;
-    ScalarAdj<R> fadj;
+    feaut = loc.inwin == 0u;
     if (feaut) {
       st[0] = feautrier_fwd<R>(tp, sm.ds, nd, B0, B1, ftape);
     } else if (!pol) {
       st[0] = scalar_bezier_fwd<R>(tp, sm.ds, nd, B0, B1, stape);
     }
     if (!pol) st[1] = st[2] = st[3] = R(0);
+    R* out = static_cast<R*>(args.out) + 4 * loff;
+    if (act)
+#pragma unroll
+      for (int s = 0; s < 4; ++s) out[(int64_t)s * nl + la] = st[s];
+  }
+  // Reached by every thread of the block: the forward sweeps of its
+  // sub-blocks end together and their reverse sweeps start together, so
+  // the resident warps run one sweep's instructions at a time.
+  __syncthreads();
+  if (!run) return;
+  {
+    const bool feaut_or_scalar = !pol;
     // adjoint of the unpolarized solvers for the Stokes I seed Ib
     auto unpol_vjp = [&](R Ib) {
       if (feaut) feautrier_vjp<R>(tp, sm.ds, nd, B0, B1, ftape, Ib, fadj);
       else scalar_bezier_vjp<R>(tp, sm.ds, nd, B0, B1, stape, Ib, fadj);
     };
-    R* out = static_cast<R*>(args.out) + 4 * loff;
-    if (act)
-#pragma unroll
-      for (int s = 0; s < 4; ++s) out[(int64_t)s * nl + la] = st[s];
-
     constexpr int NSG = MODE == 0 ? 4 : 1;
     const bool want_gf = MODE == 0 ? ra.rf_gf != nullptr : ra.grad_gf != nullptr;
     R gfacc[NSG * PYRH_MAX_LINES];
@@ -339,34 +350,47 @@ __device__ __forceinline__ void rf_lane(const RfArgs& ra, const RfSmem<R>& sm, i
 
 template <typename R, int MODE>
 __device__ __noinline__ void rf_lane_unpol(const RfArgs& ra, const RfSmem<R>& sm, int nline, int p,
-                                           int la0, int nl, int nd, int64_t doff) {
-  rf_lane<R, MODE, true>(ra, sm, nline, p, la0, nl, nd, doff);
+                                           int la0, int nl, int nd, int64_t doff, int t,
+                                           bool item) {
+  rf_lane<R, MODE, true>(ra, sm, nline, p, la0, nl, nd, doff, t, item);
 }
 
-// Single-seed modes in FP32 are capped at 128 registers (4 blocks of 128
-// threads per SM): measured 31.5 ms against 35.8 ms uncapped for the
-// gradient of 4096 atmospheres x 224 wavelengths, and 32.4 ms at 3 blocks.
-// The four-seed full response functions at 168 registers (3 blocks; 120
-// bytes of spills): 59.2 ms against 62.2 ms at 245 registers (2 blocks) and
-// 61.6 ms at 128 registers (4 blocks, 900 bytes of spills).
+// A block holds ra.sub sub-blocks of blockDim.x / ra.sub threads, each
+// with its own work item (atmosphere, tile of wavelengths) and its own
+// shared tables, so that one block fills the SM and the barrier between the
+// forward and reverse sweeps aligns the sweeps of all resident warps.
+// Single-seed modes in FP32 are capped at 128 registers (512 threads per
+// SM): measured 31.5 ms against 35.8 ms uncapped for the gradient of 4096
+// atmospheres x 224 wavelengths, and 32.4 ms at 384 threads.  The four-seed
+// full response functions at 168 registers (384 threads; 120 bytes of
+// spills): 59.2 ms against 62.2 ms at 245 registers (256 threads) and 61.6 ms
+// at 128 registers (512 threads, 900 bytes of spills).
 template <typename R, int MODE>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? (MODE != 0 ? 4 : 3) : 1)
+constexpr int rf_max_threads() {
+  return sizeof(R) == 4 ? (MODE != 0 ? 512 : 384) : 128;
+}
+
+template <typename R, int MODE>
+__global__ void __launch_bounds__(rf_max_threads<R, MODE>(), 1)
 lte_rf_kernel(RfArgs ra) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const LteArgs& args = ra.lte;
   const int nline = args.nline < PYRH_MAX_LINES ? args.nline : PYRH_MAX_LINES;
+  const int G = ra.sub;
+  const int BL = blockDim.x / G;
+  const int g = threadIdx.x / BL, t = threadIdx.x - g * BL;
   RfSmem<R> sm;
-  rf_smem_t<R>(nline, args.maxd, &sm, smem_raw);
-  const int BL = blockDim.x;
+  const size_t per = rf_smem_t<R>(nline, args.maxd, nullptr, nullptr);
+  rf_smem_t<R>(nline, args.maxd, &sm, smem_raw + per * g);
 
-  for (int i = threadIdx.x; i < nline * PYRH_MAX_COMPONENTS; i += BL) {
+  for (int i = t; i < nline * PYRH_MAX_COMPONENTS; i += BL) {
     const int l = i / PYRH_MAX_COMPONENTS, c = i % PYRH_MAX_COMPONENTS;
     const pyrh_line& L = args.lines[l];
     sm.cshift[i] = R(L.comp_shift[c]);
     sm.cweight[i] = R(L.comp_strength[c]);
     sm.cq[i] = L.comp_q[c];
   }
-  for (int l = threadIdx.x; l < nline; l += BL) {
+  for (int l = t; l < nline; l += BL) {
     const pyrh_line& L = args.lines[l];
     const int nc = L.ncomp < 0 ? 0 : (L.ncomp > PYRH_MAX_COMPONENTS ? PYRH_MAX_COMPONENTS : L.ncomp);
     sm.ncomp[l] = L.polarizable ? nc : kArmstrong;
@@ -377,78 +401,95 @@ lte_rf_kernel(RfArgs ra) {
 
   const double muz = args.mu, imu = 1.0 / args.mu;
   const int64_t total = (int64_t)args.natm * args.tiles;
-  for (int64_t w = blockIdx.x; w < total; w += gridDim.x) {
-    const int p = (int)(w / args.tiles);
-    const int tile = (int)(w % args.tiles);
-    const int nl = args.nlam[p];
-    const int la0 = tile * BL;
-    if (la0 >= nl) continue;                 // uniform across the block
-    const int nd = args.ndep[p];
-    if (nd < 3 || nd > args.maxd) continue;  // uniform across the block
-    const int64_t doff = args.depth_off[p];
+  // every barrier below is reached by every thread: the loop's trip count
+  // is the same across the block, and sub-blocks without a work item skip
+  // only the work between barriers
+  for (int64_t w0 = (int64_t)blockIdx.x * G; w0 < total; w0 += (int64_t)gridDim.x * G) {
+    const int64_t w = w0 + g;
+    int p = 0, nl = 0, la0 = 0, nd = 0;
+    int64_t doff = 0;
+    bool item = w < total;
+    if (item) {
+      p = (int)(w / args.tiles);
+      nl = args.nlam[p];
+      la0 = (int)(w % args.tiles) * BL;
+      nd = args.ndep[p];
+      doff = args.depth_off[p];
+      item = la0 < nl && nd >= 3 && nd <= args.maxd;
+    }
     __syncthreads();  // shared tables of the previous work item are consumed
 
     // ---- per-depth and per-(line, depth) values with derivatives ----
-    for (int k = threadIdx.x; k < nd; k += BL) {
-      const int64_t d = doff + k;
-      sm.ds[k] = (k >= 1) ? R(fabs(args.height[d] - args.height[d - 1]) * imu) : R(0);
-      sm.geo[k] = geometry_d<R>(R(args.gamma_B[d]), R(args.chi_B[d]), R(muz));
-      sm.len_up[k] = (k >= 1 && ra.dT.dlen_up) ? R(ra.dT.dlen_up[d] * imu) : R(0);
-      sm.len_dn[k] = (k >= 1 && ra.dT.dlen_dn) ? R(ra.dT.dlen_dn[d] * imu) : R(0);
+    if (item) {
+      for (int k = t; k < nd; k += BL) {
+        const int64_t d = doff + k;
+        sm.ds[k] = (k >= 1) ? R(fabs(args.height[d] - args.height[d - 1]) * imu) : R(0);
+        sm.geo[k] = geometry_d<R>(R(args.gamma_B[d]), R(args.chi_B[d]), R(muz));
+        sm.len_up[k] = (k >= 1 && ra.dT.dlen_up) ? R(ra.dT.dlen_up[d] * imu) : R(0);
+        sm.len_dn[k] = (k >= 1 && ra.dT.dlen_dn) ? R(ra.dT.dlen_dn[d] * imu) : R(0);
+        if (MODE != 0)
+          for (int x = 0; x < kNX; ++x) sm.grad[x * args.maxd + k] = R(0);
+      }
+      if (MODE == 1 && t == 0) sm.chi2[0] = R(0);
       if (MODE != 0)
-        for (int x = 0; x < kNX; ++x) sm.grad[x * args.maxd + k] = R(0);
-    }
-    if (MODE == 1 && threadIdx.x == 0) sm.chi2[0] = R(0);
-    if (MODE != 0)
-      for (int l = threadIdx.x; l < nline; l += BL) sm.gfs[l] = R(0);
-    for (int i = threadIdx.x; i < nline * nd; i += BL) {
-      const int l = i / nd, k = i % nd;
-      const int64_t d = doff + k;
-      const pyrh_line& L = args.lines[l];
-      const LineConstD c = {L.lambda0, L.Ei, L.gi, L.Aji, L.Bji, L.Bij, L.Grad, L.GStark,
-                            L.GvdWaals, L.cross, L.alpha, L.isotope_frac, L.hyperfine_frac,
-                            L.weight, L.vdwaals};
-      const double* dp = ra.dT.dline_pops;
-      sm.ld[l * args.maxd + k] = line_depth<R>(
-          c, R(args.T[d]), R(args.vlos[d]), R(args.vturb[d]), R(args.B[d]), R(args.ne[d]),
-          R(args.nHtot[d]), R(args.np[d]),
-          R(args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d]),
-          R(args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d]), R(muz),
-          args.moving != 0, dp ? R(dp[((int64_t)l * 2 + 0) * args.total_depth + d]) : R(0),
-          dp ? R(dp[((int64_t)l * 2 + 1) * args.total_depth + d]) : R(0),
-          ra.dT.dnp ? R(ra.dT.dnp[d]) : R(0));
+        for (int l = t; l < nline; l += BL) sm.gfs[l] = R(0);
+      for (int i = t; i < nline * nd; i += BL) {
+        const int l = i / nd, k = i % nd;
+        const int64_t d = doff + k;
+        const pyrh_line& L = args.lines[l];
+        const LineConstD c = {L.lambda0, L.Ei, L.gi, L.Aji, L.Bji, L.Bij, L.Grad, L.GStark,
+                              L.GvdWaals, L.cross, L.alpha, L.isotope_frac, L.hyperfine_frac,
+                              L.weight, L.vdwaals};
+        const double* dp = ra.dT.dline_pops;
+        sm.ld[l * args.maxd + k] = line_depth<R>(
+            c, R(args.T[d]), R(args.vlos[d]), R(args.vturb[d]), R(args.B[d]), R(args.ne[d]),
+            R(args.nHtot[d]), R(args.np[d]),
+            R(args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d]),
+            R(args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d]), R(muz),
+            args.moving != 0, dp ? R(dp[((int64_t)l * 2 + 0) * args.total_depth + d]) : R(0),
+            dp ? R(dp[((int64_t)l * 2 + 1) * args.total_depth + d]) : R(0),
+            ra.dT.dnp ? R(ra.dT.dnp[d]) : R(0));
+      }
     }
     __syncthreads();
 
-    // blocks with lines that are not polarizable take an out-of-line copy of
-    // the lane's work that has their branch; the others a copy without it
-    bool any_unpol = false;   // the same in every thread of the block
+    // lines that are not polarizable take an out-of-line copy of the lane's
+    // work that has their branch, the others a copy without it; the line
+    // list is the same for every atmosphere, so the choice is the same in
+    // every thread of the grid (and both copies hold the sweep barrier)
+    bool any_unpol = false;
     for (int l = 0; l < nline; ++l) any_unpol |= sm.contrib[l] && !sm.polar[l];
     if (any_unpol)
-      rf_lane_unpol<R, MODE>(ra, sm, nline, p, la0, nl, nd, doff);
+      rf_lane_unpol<R, MODE>(ra, sm, nline, p, la0, nl, nd, doff, t, item);
     else
-      rf_lane<R, MODE, false>(ra, sm, nline, p, la0, nl, nd, doff);
+      rf_lane<R, MODE, false>(ra, sm, nline, p, la0, nl, nd, doff, t, item);
     if (MODE != 0) {
       __syncthreads();
-      R* grad = static_cast<R*>(ra.grad);
-      for (int i = threadIdx.x; i < kNX * nd; i += BL) {
-        const int x = i / nd, k = i % nd;
-        atomicAdd(&grad[(int64_t)x * args.total_depth + doff + k], sm.grad[x * args.maxd + k]);
+      if (item) {
+        R* grad = static_cast<R*>(ra.grad);
+        for (int i = t; i < kNX * nd; i += BL) {
+          const int x = i / nd, k = i % nd;
+          atomicAdd(&grad[(int64_t)x * args.total_depth + doff + k], sm.grad[x * args.maxd + k]);
+        }
+        if (MODE == 1 && t == 0) atomicAdd(static_cast<R*>(ra.chi2) + p, sm.chi2[0]);
+        if (ra.grad_gf)
+          for (int l = t; l < nline; l += BL)
+            atomicAdd(static_cast<R*>(ra.grad_gf) + (int64_t)p * nline + l, sm.gfs[l]);
       }
-      if (MODE == 1 && threadIdx.x == 0) atomicAdd(static_cast<R*>(ra.chi2) + p, sm.chi2[0]);
-      if (ra.grad_gf)
-        for (int l = threadIdx.x; l < nline; l += BL)
-          atomicAdd(static_cast<R*>(ra.grad_gf) + (int64_t)p * nline + l, sm.gfs[l]);
     }
   }
 }
 
+// block: threads of one sub-block (the tile width); smem: the shared tables
+// of one sub-block.  The launch has a.sub sub-blocks per block.
 template <typename R, int MODE>
 cudaError_t launch_mode(const RfArgs& a, int block, int grid, size_t smem, cudaStream_t st) {
+  if (a.sub < 1 || block * a.sub > rf_max_threads<R, MODE>()) return cudaErrorInvalidValue;
   auto k = lte_rf_kernel<R, MODE>;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const size_t total = smem * a.sub;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)total);
   if (e != cudaSuccess) return e;
-  k<<<grid, block, smem, st>>>(a);
+  k<<<grid, block * a.sub, total, st>>>(a);
   return cudaGetLastError();
 }
 

@@ -34,6 +34,7 @@ struct RfArgs {
   void *rf_gf;    // mode 0, optional: dS/dlog10(gf) [nline][4][lambda] per atmosphere
   void *grad_gf;  // modes 1-2, optional: dL/dlog10(gf) [natm][nline]
   pyrh_lte_setup_dT dT;   // set-up temperature derivatives (NULL members: held fixed)
+  int sub;                // sub-blocks (work items) per block of the kernel
 };
 
 size_t rf_smem_bytes(int precision, int nline, int maxd);
