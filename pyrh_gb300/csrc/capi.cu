@@ -168,9 +168,9 @@ pyrh_status check_rf(const pyrh_lte_batch* b, const pyrh_lte_config* cfg, int nl
   if (b->max_ndep > PYRH_RF_MAX_DEPTH)
     return fail(PYRH_ERR_UNSUPPORTED, "max_ndep %d above PYRH_RF_MAX_DEPTH %d", b->max_ndep,
                 PYRH_RF_MAX_DEPTH);
-  if (cfg->block_lambda > 128)
-    return fail(PYRH_ERR_ARG, "block_lambda %d above 128 for response functions",
-                cfg->block_lambda);
+  if (cfg->block_lambda > pyrh::rf_max_threads(cfg->precision))
+    return fail(PYRH_ERR_ARG, "block_lambda %d above %d for response functions",
+                cfg->block_lambda, pyrh::rf_max_threads(cfg->precision));
   return PYRH_OK;
 }
 
@@ -199,7 +199,8 @@ pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nli
   // registers of a whole SM, so that the barrier between the forward and
   // reverse sweeps aligns every resident warp; fewer where their shared
   // tables do not fit together.
-  int sub = cfg->precision == PYRH_FP32 ? (mode != 0 ? 4 : 3) : 1;
+  int sub = pyrh::rf_max_threads(cfg->precision, mode) / block;
+  if (sub < 1) return fail(PYRH_ERR_ARG, "block_lambda %d too wide for this mode", block);
   while (sub > 1 && smem * sub > smem_limit()) --sub;
   ra.sub = sub;
   const long long work = (long long)ra.lte.natm * ra.lte.tiles;

@@ -38,6 +38,9 @@ struct RfArgs {
 };
 
 size_t rf_smem_bytes(int precision, int nline, int maxd);
+// Threads per block of the response-function kernel (its launch bound):
+// mode < 0 gives the largest over the modes.
+int rf_max_threads(int precision, int mode = -1);
 cudaError_t launch_lte_rf(const RfArgs &a, int block, int grid, cudaStream_t st);
 
 size_t lte_smem_bytes(int precision, int nline, int maxd);

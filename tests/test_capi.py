@@ -137,3 +137,21 @@ def test_nlte_structs_and_workspace_without_gpu(golden):
     # transitions: continua first, then lines, as the active sets are built
     types = [pk.trans[i].type for i in range(pk.ntrans_total)]
     assert types == [1] * len(fx["continua"]) + [0] * len(fx["lines"])
+
+
+def test_rf_tile_width_checked_without_gpu(golden):
+    """The response-function kernel takes tiles up to its block size (512
+    threads in FP32, 128 in FP64): wider tiles are refused before any
+    device work."""
+    fx = golden("lte_c0")
+    lines, n = lte.make_lines(fx["line_const"], fx["zeeman"], fx["zeeman_n"])
+    pk = lte.pack([fx], n)
+    arrs = {k: np.ascontiguousarray(v) for k, v in pk.arrays.items()}
+    b = lte._batch_struct(pk, lambda k: arrs[k].ctypes.data)
+    cfg = lte.make_config(precision=L.PYRH_FP64, block_lambda=160)
+    lib = L.lib()
+    dummy = C.c_void_p(1)
+    s = lib.pyrh_lte_rf(C.byref(b), C.cast(lines, C.c_void_p), n, C.byref(cfg), dummy, dummy,
+                        None, None)
+    assert s == L.PYRH_ERR_ARG
+    assert b"block_lambda 160 above 128" in lib.pyrh_last_error()
