@@ -1043,16 +1043,6 @@ PYRH_HD void w3_d(double dtau, double w[3], double dw[2]) {
   }
 }
 
-// A hint that moves the cache line of p (generic address: the tape in local
-// memory or a global array) into L1; nothing on the host.
-PYRH_HD void prefetch_l1(const void* p) {
-#ifdef __CUDA_ARCH__
-  asm volatile("prefetch.L1 [%0];" ::"l"(p));
-#else
-  (void)p;
-#endif
-}
-
 // The tape entries that reverse step k+1 reads first (and the profile sums
 // of depth k-1, which the emit after that step contracts): requested during
 // step k so that they arrive while it computes.  Local memory is laid out

@@ -44,6 +44,16 @@ PYRH_HD Cx<R> cmul(Cx<R> a, Cx<R> b) {
 // Division: IEEE in FP64; in FP32 the fast reciprocal-based division
 // (__fdividef, 2 ulp), which the FP32 accuracy budget (1e-4) allows.
 PYRH_HD double fdiv(double a, double b) { return a / b; }
+
+// A hint that moves the cache line of p (generic address: local memory or a
+// global array) into L1; nothing on the host.
+PYRH_HD void prefetch_l1(const void* p) {
+#ifdef __CUDA_ARCH__
+  asm volatile("prefetch.L1 [%0];" ::"l"(p));
+#else
+  (void)p;
+#endif
+}
 PYRH_HD float fdiv(float a, float b) {
 #ifdef __CUDA_ARCH__
   return __fdividef(a, b);
