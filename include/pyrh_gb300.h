@@ -214,9 +214,15 @@ void pyrh_lte_plan_destroy(pyrh_lte_plan plan);
  * bezier_1D.c:416-490).  Parameters, in this order and in the units of
  * pyrh_lte_batch: T [K], v_los [m/s], v_mic [m/s], B [T], gamma_B [rad],
  * chi_B [rad].  The continuum (chi_c, eta_c), stage densities and the
- * height scale are held fixed.  Every wavelength is solved with
- * DELO-Bezier3 (the reference's solver wherever a polarizable line covers
- * the wavelength); FULL_STOKES without magneto-optical terms only. */
+ * height scale are held fixed unless batch->setup_dT gives their
+ * temperature derivatives (then T follows them, as the reference's finite
+ * differences re-run its set-up).  Each wavelength is solved, and
+ * differentiated, with the reference's solver for it: DELO-Bezier3 where a
+ * polarizable line covers it (FULL_STOKES), scalar Bezier3 for NO_STOKES or
+ * where only unpolarizable lines cover it, Feautrier where no line does.
+ * Without magneto-optical terms only.  cfg->block_lambda (0: 128) is the
+ * wavelength tile of one work item, at most 512 (FP32 chi^2 and VJP), 384
+ * (FP32 response functions) or 128 (FP64). */
 #define PYRH_RF_NPARAM    6
 #define PYRH_RF_MAX_DEPTH 160
 
