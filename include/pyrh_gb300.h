@@ -221,8 +221,7 @@ void pyrh_lte_plan_destroy(pyrh_lte_plan plan);
  * polarizable line covers it (FULL_STOKES), scalar Bezier3 for NO_STOKES or
  * where only unpolarizable lines cover it, Feautrier where no line does.
  * Without magneto-optical terms only.  cfg->block_lambda (0: 128) is the
- * wavelength tile of one work item, at most 512 (FP32 chi^2 and VJP), 384
- * (FP32 response functions) or 128 (FP64). */
+ * wavelength tile of one work item: up to 256 in FP32, 128 in FP64. */
 #define PYRH_RF_NPARAM    6
 #define PYRH_RF_MAX_DEPTH 160
 
