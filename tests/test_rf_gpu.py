@@ -126,6 +126,33 @@ def test_rf_ragged_batch_equals_single(golden):
         assert np.abs(both[i] - one[0]).max() <= 1e-12 * np.abs(one[0]).max()
 
 
+def test_fp32_ragged_batch_equals_single(golden):
+    """FP32, where one block holds several work items (sub-blocks) that
+    may belong to different atmospheres or be empty: a ragged batch of five
+    atmospheres gives each atmosphere's response functions (no sums across
+    threads: equal to rounding) and chi^2 gradient (shared-memory sums in a
+    different order: 1e-5 of the largest entry) as it gives alone."""
+    import torch
+    a, c = golden("lte_c0"), dict(golden("lte_edge"))
+    c["mu"] = a["mu"]
+    atms = [a, c, a, c, a]
+    dev, cfg, _, both = gpu_rf(atms, FP32)
+    obs = torch.zeros_like(dev.out)
+    w = torch.ones_like(dev.out)
+    _, g_both = RF.chi2_grad(dev, cfg, obs, w)
+    g_both = g_both.cpu().numpy().astype(np.float64)
+    pk = dev.pk
+    for i, fx in enumerate(atms):
+        d1, _, _, one = gpu_rf([fx], FP32)
+        assert np.abs(both[i] - one[0]).max() <= 1e-6 * np.abs(one[0]).max(), i
+        _, g1 = RF.chi2_grad(d1, cfg, torch.zeros_like(d1.out), torch.ones_like(d1.out))
+        g1 = g1.cpu().numpy().astype(np.float64)
+        d0, nd = int(pk.arrays["depth_off"][i]), int(pk.arrays["ndep"][i])
+        gb = g_both[:, d0:d0 + nd]
+        scale = np.abs(g1).max(axis=1, keepdims=True)
+        assert np.all(np.abs(gb - g1) <= 1e-5 * np.where(scale > 0, scale, 1.0)), i
+
+
 def test_chi2_grad_and_vjp_contract_rf(golden):
     """FP64: chi^2, its gradient and a VJP equal the contraction of the
     response functions (the same linear map, evaluated three ways), to 1e-9
