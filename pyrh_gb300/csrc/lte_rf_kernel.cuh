@@ -4,8 +4,9 @@
 // parallel); lte_rf.cu sizes its shared memory and dispatches.
 //
 // One thread owns one (atmosphere, wavelength) pair, as in lte_stokes.cu.
-// Per block (one atmosphere, one tile of wavelengths) the per-(line, depth)
-// quantities and the projected field geometry are computed once, in the
+// A block holds several sub-blocks, each with its own work item (one
+// atmosphere, one tile of wavelengths) and shared tables.  Per sub-block the
+// per-(line, depth) quantities and the projected field geometry are computed once, in the
 // working precision, with their derivatives with respect to (T, v_los,
 // v_mic, B, gamma, chi) of the same depth, into shared memory (forward-mode
 // dual numbers, lte_rf.cuh).  Each thread then
@@ -26,8 +27,10 @@
 //      Stokes seeds give RF[s][x][k] (written wavelength-fastest, coalesced);
 //      for the chi^2 gradient the single seed 2 w (S - obs), and for a
 //      vector-Jacobian product the caller's dL/dS, give one value per
-//      (x, k), summed over the block's wavelengths in shared memory and then
-//      added to the atmosphere's gradient in HBM.
+//      (x, k), summed over the sub-block's wavelengths in shared memory and
+//      then added to the atmosphere's gradient in HBM.
+// Steps 1 and 2-3 are separated by a block-wide barrier, so that all warps
+// of the SM run the same sweep at a time.
 // With the set-up's temperature derivatives (RfArgs::dT), the temperature
 // slot also collects the continuum, population and path-length terms (the
 // reference's finite-difference response functions re-run the set-up for
