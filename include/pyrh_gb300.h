@@ -170,11 +170,13 @@ pyrh_status pyrh_check_lines(const pyrh_line *host_lines, int32_t nline,
 /* Same computation with HOST inputs and outputs: copies the batch to the
    device, runs pyrh_lte_stokes and copies the Stokes vectors back, all
    inside the call (the shape of a compute1d()-style call,
-   pyrh.pyx:621-642).  When the atmospheres' continuum and spectra follow one
-   another in memory, the continuum (the bulk of the bytes) is uploaded in
-   chunks of about 128 MB of atmospheres, each synthesised on a second
-   internal stream while the next uploads, and its spectra copied back on a
-   third; pyrh_last_launch_count() then reports one launch per chunk.  Host
+   pyrh.pyx:621-642).  When the atmospheres' depths, wavelengths, continuum
+   and spectra follow one another in memory, the batch is uploaded in chunks
+   of atmospheres (about 128 MB of continuum each, after a lead chunk of an
+   eighth of that, so that the first launch waits for little), each
+   synthesised on a second internal stream while the next uploads, and its
+   spectra copied back on a third; pyrh_last_launch_count() then reports one
+   launch per chunk.  Host
    buffers in page-locked memory let the copies run at full speed.  Device
    buffers are cached between calls with the same or smaller sizes.  Not
    re-entrant (one internal workspace). */

@@ -472,17 +472,29 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host
         hb->nlam[p] > hb->max_nlam || hb->depth_off[p] + hb->ndep[p] > hb->total_depth)
       return fail(PYRH_ERR_ARG, "atmosphere %d: inconsistent ndep/nlam/offsets", p);
     if (p > 0 && (hb->cont_off[p] < hb->cont_off[p - 1] + (long long)hb->ndep[p - 1] * hb->nlam[p - 1] ||
-                  hb->lam_off[p] < hb->lam_off[p - 1] + hb->nlam[p - 1]))
+                  hb->lam_off[p] < hb->lam_off[p - 1] + hb->nlam[p - 1] ||
+                  hb->depth_off[p] < hb->depth_off[p - 1] + hb->ndep[p - 1]))
       ordered = false;
   }
   const size_t real = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
-  const size_t D = sizeof(double) * hb->total_depth;
-  // about 128 MB of continuum per chunk, at most 16 chunks
+  // about 128 MB of continuum per chunk, at most 16 chunks, after a lead
+  // chunk of an eighth of that size whose short upload is all that the
+  // first launch waits for
   const long long cont_bytes = 2LL * (long long)real * cont_tot;
-  int nchunk = ordered ? (int)(cont_bytes / (128LL << 20)) : 1;
-  if (nchunk > 16) nchunk = 16;
-  if (nchunk > natm) nchunk = natm;
-  if (nchunk < 1) nchunk = 1;
+  int neq = ordered ? (int)(cont_bytes / (128LL << 20)) : 1;
+  if (neq > 16) neq = 16;
+  if (neq < 1) neq = 1;
+  std::vector<int> pb(1, 0);   // chunk c holds atmospheres [pb[c], pb[c+1])
+  int lead = 0;
+  if (neq > 1) {
+    lead = (int)((long long)natm / (8LL * neq));
+    if (lead > 0) pb.push_back(lead);
+  }
+  for (int c = 1; c <= neq; ++c) {
+    const int e = lead + (int)((long long)(natm - lead) * c / neq);
+    if (e > pb.back()) pb.push_back(e);
+  }
+  const int nchunk = (int)pb.size() - 1;
   std::lock_guard<std::mutex> lock(g_ws.mu);
   CUDA_TRY(g_ws.init(nchunk));
   cudaError_t err = cudaSuccess;
@@ -506,16 +518,29 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host
   UP(nlam, sizeof(int32_t) * natm);
   UP(lam_off, sizeof(int64_t) * natm);
   UP(cont_off, sizeof(int64_t) * natm);
-  UP(lambda, sizeof(double) * nlam_tot);
-  UP(height, D); UP(T, D); UP(ne, D); UP(nHtot, D); UP(np, D);
-  UP(vturb, D); UP(vlos, D); UP(B, D); UP(gamma_B, D); UP(chi_B, D);
-  if (nline > 0) UP(line_pops, D * 2 * nline);
 #undef UP
   pyrh_line* d_lines = nullptr;
   if (nline > 0) {
     d_lines = (pyrh_line*)up(host_lines, sizeof(pyrh_line) * nline);
     if (!d_lines) return fail(PYRH_ERR_CUDA, "upload lines: %s", cudaGetErrorString(err));
   }
+  // Device arrays for the per-depth, per-wavelength and continuum data; each
+  // chunk uploads its own ranges of them.
+  const long long ndt = hb->total_depth;
+  const double* const* hdepth[10] = {&hb->height, &hb->T, &hb->ne, &hb->nHtot, &hb->np,
+                                     &hb->vturb, &hb->vlos, &hb->B, &hb->gamma_B, &hb->chi_B};
+  const double** ddepth[10] = {&db.height, &db.T, &db.ne, &db.nHtot, &db.np,
+                               &db.vturb, &db.vlos, &db.B, &db.gamma_B, &db.chi_B};
+  for (int f = 0; f < 10; ++f) {
+    *ddepth[f] = (const double*)g_ws.get(slot++, sizeof(double) * ndt, &err);
+    if (!*ddepth[f]) return fail(PYRH_ERR_CUDA, "depth buffers: %s", cudaGetErrorString(err));
+  }
+  if (nline > 0) {
+    db.line_pops = (const double*)g_ws.get(slot++, sizeof(double) * ndt * 2 * nline, &err);
+    if (!db.line_pops) return fail(PYRH_ERR_CUDA, "line_pops buffer: %s", cudaGetErrorString(err));
+  }
+  db.lambda = (const double*)g_ws.get(slot++, sizeof(double) * nlam_tot, &err);
+  if (!db.lambda) return fail(PYRH_ERR_CUDA, "lambda buffer: %s", cudaGetErrorString(err));
   unsigned char* d_chi = (unsigned char*)g_ws.get(slot++, real * cont_tot, &err);
   unsigned char* d_eta = d_chi ? (unsigned char*)g_ws.get(slot++, real * cont_tot, &err) : nullptr;
   if (!d_eta) return fail(PYRH_ERR_CUDA, "continuum buffers: %s", cudaGetErrorString(err));
@@ -524,23 +549,35 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host
   const size_t out_bytes = real * 4 * nlam_tot;
   unsigned char* d_out = (unsigned char*)g_ws.get(slot++, out_bytes, &err);
   if (!d_out) return fail(PYRH_ERR_CUDA, "output buffer: %s", cudaGetErrorString(err));
-  // Chunk c: upload its continuum (copy stream), synthesise its atmospheres
-  // once the upload is done (kernel stream c % 2), copy its spectra back
-  // (output stream).  Chunk c+1's upload runs under chunk c's kernel, and
-  // with two kernel streams chunk c+1's blocks fill the SMs that chunk c's
-  // last, partial wave leaves idle.
+  auto h2d = [&](const void* dst, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(const_cast<void*>(dst), src, bytes, cudaMemcpyHostToDevice,
+                           g_ws.stream);
+  };
+  // Chunk c: upload its depths, wavelengths and continuum (copy stream),
+  // synthesise its atmospheres once the upload is done (kernel stream
+  // c % 2), copy its spectra back (output stream).  Chunk c+1's upload runs
+  // under chunk c's kernel, and with two kernel streams chunk c+1's blocks
+  // fill the SMs that chunk c's last, partial wave leaves idle.
   const unsigned char* h_chi = (const unsigned char*)hb->chi_c;
   const unsigned char* h_eta = (const unsigned char*)hb->eta_c;
   for (int c = 0; c < nchunk; ++c) {
-    const int p0 = (int)((long long)natm * c / nchunk);
-    const int p1 = (int)((long long)natm * (c + 1) / nchunk);
-    long long c0 = nchunk == 1 ? 0 : hb->cont_off[p0];
-    long long c1 = nchunk == 1 ? cont_tot
+    const int p0 = pb[c], p1 = pb[c + 1];
+    const bool whole = nchunk == 1;   // also the layout without ordered offsets
+    const long long c0 = whole ? 0 : hb->cont_off[p0];
+    const long long c1 = whole ? cont_tot
                                : hb->cont_off[p1 - 1] + (long long)hb->ndep[p1 - 1] * hb->nlam[p1 - 1];
-    CUDA_TRY(cudaMemcpyAsync(d_chi + real * c0, h_chi + real * c0, real * (c1 - c0),
-                             cudaMemcpyHostToDevice, g_ws.stream));
-    CUDA_TRY(cudaMemcpyAsync(d_eta + real * c0, h_eta + real * c0, real * (c1 - c0),
-                             cudaMemcpyHostToDevice, g_ws.stream));
+    const long long d0 = whole ? 0 : hb->depth_off[p0];
+    const long long d1 = whole ? ndt : hb->depth_off[p1 - 1] + hb->ndep[p1 - 1];
+    const long long l0 = whole ? 0 : hb->lam_off[p0];
+    const long long l1 = whole ? nlam_tot : hb->lam_off[p1 - 1] + hb->nlam[p1 - 1];
+    for (int f = 0; f < 10; ++f)
+      CUDA_TRY(h2d(*ddepth[f] + d0, *hdepth[f] + d0, sizeof(double) * (d1 - d0)));
+    for (long long r = 0; r < 2LL * nline; ++r)
+      CUDA_TRY(h2d(db.line_pops + r * ndt + d0, hb->line_pops + r * ndt + d0,
+                   sizeof(double) * (d1 - d0)));
+    CUDA_TRY(h2d(db.lambda + l0, hb->lambda + l0, sizeof(double) * (l1 - l0)));
+    CUDA_TRY(h2d(d_chi + real * c0, h_chi + real * c0, real * (c1 - c0)));
+    CUDA_TRY(h2d(d_eta + real * c0, h_eta + real * c0, real * (c1 - c0)));
     CUDA_TRY(cudaEventRecord(g_ws.ev_in[c], g_ws.stream));
     cudaStream_t ks = g_ws.kstream[c & 1];
     CUDA_TRY(cudaStreamWaitEvent(ks, g_ws.ev_in[c], 0));
@@ -555,17 +592,10 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host
     if (s != PYRH_OK) return s;
     CUDA_TRY(cudaEventRecord(g_ws.ev_k[c], ks));
     CUDA_TRY(cudaStreamWaitEvent(g_ws.ostream, g_ws.ev_k[c], 0));
-    const long long l0 = nchunk == 1 ? 0 : hb->lam_off[p0];
-    const long long l1 = nchunk == 1 ? nlam_tot : hb->lam_off[p1 - 1] + hb->nlam[p1 - 1];
-    if (nchunk == 1) {
-      CUDA_TRY(cudaMemcpyAsync(host_stokes_out, d_out, out_bytes, cudaMemcpyDeviceToHost,
-                               g_ws.ostream));
-    } else {
-      // Stokes of atmosphere p occupy [4 lam_off[p], 4 lam_off[p] + 4 nlam[p])
-      CUDA_TRY(cudaMemcpyAsync((unsigned char*)host_stokes_out + real * 4 * l0,
-                               d_out + real * 4 * l0, real * 4 * (l1 - l0),
-                               cudaMemcpyDeviceToHost, g_ws.ostream));
-    }
+    // Stokes of atmosphere p occupy [4 lam_off[p], 4 lam_off[p] + 4 nlam[p])
+    CUDA_TRY(cudaMemcpyAsync((unsigned char*)host_stokes_out + real * 4 * l0,
+                             d_out + real * 4 * l0, real * 4 * (l1 - l0),
+                             cudaMemcpyDeviceToHost, g_ws.ostream));
   }
   CUDA_TRY(cudaStreamSynchronize(g_ws.ostream));
   CUDA_TRY(cudaStreamSynchronize(g_ws.kstream[0]));

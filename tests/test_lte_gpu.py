@@ -210,10 +210,11 @@ def test_plan_tunes_and_replays_graph(golden):
 
 
 def test_host_entry_pipelined_chunks_equal_device_path():
-    """pyrh_lte_stokes_host uploads the continuum of a large batch in chunks
-    (about 128 MB each), each synthesised while the next one uploads; the
-    spectra equal the device-resident path's bit for bit (2500 atmospheres:
-    two chunks of 1250)."""
+    """pyrh_lte_stokes_host uploads a large batch in chunks (about 128 MB of
+    continuum each, after a lead chunk of an eighth of that), each
+    synthesised while the next one uploads; the spectra equal the
+    device-resident path's bit for bit (2500 atmospheres: chunks of 156,
+    1172 and 1172)."""
     import torch
     from pyrh_gb300 import workload
     b = workload.synthetic_batch(2500, seed=9, dtype=np.float32)
@@ -221,7 +222,7 @@ def test_host_entry_pipelined_chunks_equal_device_path():
     pk = lte.pack_uniform(b, n, FP32)
     cfg = lte.make_config(precision=FP32, mu=1.0, vmicro_char=b["vmicro_char"])
     out_h = lte.synth_host(pk, lines, n, cfg)
-    assert L.lib().pyrh_last_launch_count() == 2
+    assert L.lib().pyrh_last_launch_count() == 3
     db = lte.DeviceBatch(pk, lines, n)
     db.run(cfg)
     torch.cuda.synchronize()
