@@ -227,3 +227,24 @@ def test_host_entry_pipelined_chunks_equal_device_path():
     db.run(cfg)
     torch.cuda.synchronize()
     assert np.array_equal(out_h, db.out.cpu().numpy())
+
+
+def test_host_entry_unordered_batch_uploads_whole():
+    """Atmospheres listed out of memory order (here reversed) cannot be
+    uploaded chunk by chunk: the host entry uploads the batch in one piece
+    and runs one launch, with the same spectra as the ordered call."""
+    import ctypes as C
+    from pyrh_gb300 import workload
+    b = workload.synthetic_batch(2500, seed=9, dtype=np.float32)
+    lines, n = lte.make_lines(b["line_const"], b["zeeman"], b["zeeman_n"])
+    pk = lte.pack_uniform(b, n, FP32)
+    cfg = lte.make_config(precision=FP32, mu=1.0, vmicro_char=b["vmicro_char"])
+    ordered = lte.synth_host(pk, lines, n, cfg)
+    arrs = {k: np.ascontiguousarray(v) for k, v in pk.arrays.items()}
+    for k in ("ndep", "depth_off", "nlam", "lam_off", "cont_off"):
+        arrs[k] = np.ascontiguousarray(arrs[k][::-1])
+    hb = lte._batch_struct(pk, lambda k: arrs[k].ctypes.data)
+    out = np.zeros_like(ordered)
+    L.check(L.lib().pyrh_lte_stokes_host(C.byref(hb), lines, n, C.byref(cfg), out.ctypes.data))
+    assert L.lib().pyrh_last_launch_count() == 1
+    assert np.array_equal(out, ordered)
