@@ -28,11 +28,6 @@ size_t rf_smem_bytes(int precision, int nline, int maxd) {
                                 : rf_smem_bytes_fp64(nline, maxd);
 }
 
-int rf_max_threads(int precision, int mode) {
-  if (precision != PYRH_FP32) return 128;
-  return mode == 0 ? 384 : 512;
-}
-
 cudaError_t launch_lte_rf(const RfArgs& a, int block, int grid, cudaStream_t st) {
   const size_t smem = rf_smem_bytes(a.lte.precision, a.lte.nline, a.lte.maxd);
   const bool f32 = a.lte.precision == PYRH_FP32;

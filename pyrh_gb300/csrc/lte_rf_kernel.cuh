@@ -368,10 +368,9 @@ __device__ __noinline__ void rf_lane_unpol(const RfArgs& ra, const RfSmem<R>& sm
 // full response functions at 168 registers (384 threads; 120 bytes of
 // spills): 59.2 ms against 62.2 ms at 245 registers (256 threads) and 61.6 ms
 // at 128 registers (512 threads, 900 bytes of spills).
-// (the same numbers as rf_max_threads(precision, mode) in lte_rf.cu)
 template <typename R, int MODE>
 constexpr int rf_max_threads() {
-  return sizeof(R) == 4 ? (MODE != 0 ? 512 : 384) : 128;
+  return ::pyrh::rf_max_threads(sizeof(R) == 4 ? PYRH_FP32 : PYRH_FP64, MODE);
 }
 
 template <typename R, int MODE>

@@ -39,8 +39,12 @@ struct RfArgs {
 
 size_t rf_smem_bytes(int precision, int nline, int maxd);
 // Threads per block of the response-function kernel (its launch bound):
-// mode < 0 gives the largest over the modes.
-int rf_max_threads(int precision, int mode = -1);
+// in FP32 one block takes an SM's registers at 128 per thread (168 for the
+// four-seed full response functions, mode 0); mode < 0 gives the largest
+// over the modes.
+constexpr int rf_max_threads(int precision, int mode = -1) {
+  return precision != PYRH_FP32 ? 128 : (mode == 0 ? 384 : 512);
+}
 cudaError_t launch_lte_rf(const RfArgs &a, int block, int grid, cudaStream_t st);
 
 size_t lte_smem_bytes(int precision, int nline, int maxd);
