@@ -10,9 +10,10 @@
  *     (rh/kurucz.c:511-827, Humlicek 1982 Voigt, rh/humlicek.c:28-118),
  *   - the formal solution of Formal() (rh/rhf1d/formal.c:44-346): DELO-Bezier3
  *     Stokes (rh/rhf1d/bezier_1D.c:52-300) where a polarizable line covers the
- *     wavelength, the scalar Bezier3 solver (bezier_1D.c:306-541) for NO_STOKES,
- *     and the Feautrier solver (rh/rhf1d/feautrier.c:56-202) where no line
- *     covers it,
+ *     wavelength, the scalar Bezier3 solver (bezier_1D.c:306-541) for NO_STOKES
+ *     and where only unpolarizable lines cover it, and the Feautrier solver
+ *     (rh/rhf1d/feautrier.c:56-202) where no line covers it -- or, in a static
+ *     atmosphere (cfg->moving = 0), no polarizable line (formal.c:96-101),
  * for many atmospheres (pixels) at once.  Only the ray towards the observer
  * is solved: the emergent Stokes vector does not depend on the other
  * direction that Formal() also integrates in LTE.
@@ -221,7 +222,8 @@ void pyrh_lte_plan_destroy(pyrh_lte_plan plan);
  * differences re-run its set-up).  Each wavelength is solved, and
  * differentiated, with the reference's solver for it: DELO-Bezier3 where a
  * polarizable line covers it (FULL_STOKES), scalar Bezier3 for NO_STOKES or
- * where only unpolarizable lines cover it, Feautrier where no line does.
+ * where only unpolarizable lines cover it, Feautrier where no line does (in
+ * a static atmosphere also where no polarizable line does).
  * Without magneto-optical terms only.  cfg->block_lambda (0: 128) is the
  * wavelength tile of one work item: up to 256 in FP32, 128 in FP64. */
 #define PYRH_RF_NPARAM    6

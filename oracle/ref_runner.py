@@ -73,7 +73,7 @@ KEYWORD_TEMPLATE = """\
   RLK_SCATTER = FALSE
   HYDROGEN_LTE = TRUE
   VMICRO_CHAR = {vmicro_char}
-  VMACRO_TRESH = 0
+  VMACRO_TRESH = {vmacro_tresh}
   S_INTERPOLATION = S_BEZIER3
   S_INTERPOLATION_STOKES = DELO_BEZIER3
   VACUUM_TO_AIR = FALSE
@@ -95,7 +95,8 @@ def write_inputs(workdir: str, kurucz_lines: str | None, atoms=None,
     opts = dict(nrays=1, nmax_scatter=0, nmax_iter=1, iter_limit="1.0E-2",
                 ng_order=0, ng_delay=10, ng_period=3, vmicro_char=5.0,
                 stokes_mode="FULL_STOKES", magneto_optical="FALSE",
-                kurucz="kurucz.input" if kurucz_lines else "none", extra="")
+                kurucz="kurucz.input" if kurucz_lines else "none", extra="",
+                vmacro_tresh="0")
     opts.update(kw)
     with open(os.path.join(workdir, "keyword.input"), "w") as f:
         f.write(KEYWORD_TEMPLATE.format(**opts))

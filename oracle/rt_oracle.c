@@ -666,7 +666,10 @@ int oracle_lte_synth(const OracleAtmos *A, const OracleLines *LN, int nlam,
       stokes_bezier3(nd, A->height, imu, chi, S, K, B0, B1, md_float, I0);
       for (int s = 0; s < 4; s++) out[(long) s * nlam + la] = I0[s];
     } else {
-      if (flags & 1)
+      /* angle dependent (formal.c:96-101): a polarizable line in window, or
+         any line in a moving atmosphere -- scalar Bezier3; otherwise the
+         angle-independent Feautrier solution (formal.c:284-304) */
+      if ((flags & 1) && ((flags & 2) || LN->moving))
         out[la] = oracle_scalar_bezier3(nd, A->height, imu, chi, Ss, B0, B1, 1, NULL, NULL);
       else
         out[la] = oracle_feautrier(nd, A->height, A->muz, chi, Ss, B0, B1, NULL, NULL);

@@ -253,13 +253,14 @@ __device__ __forceinline__ void rf_lane(const RfArgs& ra, const RfSmem<R>& sm, i
     B0 = planck(args.T[doff + nd - 2], lam);
     B1 = planck(args.T[doff + nd - 1], lam);
     delo_forward<R>(tp, sm.ds, nd, B0, B1, st, qop);
-    // the reference's solver for this wavelength (formal.c:94-95,
-    // 285-310): Feautrier without a line in window, scalar Bezier3 when
-    // none of the lines in window is polarizable, DELO-Bezier3 otherwise
-    // (NO_STOKES: scalar throughout, formal.c:94-95)
+    // the reference's solver for this wavelength (formal.c:94-101,
+    // 284-310): Feautrier where the wavelength is not angle dependent (no
+    // line in window, or only unpolarizable lines in a static atmosphere),
+    // scalar Bezier3 when none of the lines in window is polarizable,
+    // DELO-Bezier3 otherwise (NO_STOKES: scalar where not Feautrier)
     for (int l = 0; l < nline; ++l) pol |= ((loc.inwin >> l) & 1u) && sm.polar[l];
+    feaut = loc.inwin == 0u || (!pol && !args.moving);
     pol = pol && args.stokes_mode == PYRH_FULL_STOKES;
-    feaut = loc.inwin == 0u;
     if (feaut) {
       st[0] = feautrier_fwd<R>(tp, sm.ds, nd, B0, B1, ftape);
     } else if (!pol) {

@@ -484,7 +484,9 @@ __device__ __forceinline__ void synth_wavelength(const LteArgs& args, const Smem
     const double B1 = planck(args.T[doff + nd - 1], lam);
     const R* ds = sm.geo + GF_DS * sm.maxd;
     R st[4] = {0, 0, 0, 0};
-    if (op.inwin == 0u) {
+    // angle dependent (formal.c:96-101): a polarizable line in window, or
+    // any line in a moving atmosphere; otherwise Feautrier (formal.c:284-304)
+    if (op.inwin == 0u || (!pol && !args.moving)) {
       st[0] = solve_feautrier<R, MO, UP>(op, ds, nd, B0, B1);
     } else if (pol && args.stokes_mode == PYRH_FULL_STOKES) {
       solve_stokes<R, MO, UP>(op, ds, nd, B0, B1, st);

@@ -20,6 +20,8 @@ Fixtures (npz, float64):
   lte_nostokes    C0 in STOKES_MODE = NO_STOKES
   lte_mixed       C0 with two unpolarizable lines (Armstrong's Voigt), one
                   alone in its window and one among the polarized lines
+  lte_static      the lines of lte_mixed in a static atmosphere (VMACRO_TRESH
+                  0.1 km/s, no velocity: atmos.moving FALSE), mu = 0.8
   lte_loggf       the reference's analytical log gf RFs of Stokes I (NO_STOKES
                   C0, both lines) and central differences of its synthesis in
                   log gf
@@ -70,10 +72,10 @@ def base_c0(ref: rr.Reference, workdir: str, ndep: int = 71):
 
 
 def lte_case(ref, name, atm, wave, mu=1.0, magneto_optical="FALSE",
-             extra=None, stokes_mode="FULL_STOKES", linelist=None):
+             extra=None, stokes_mode="FULL_STOKES", linelist=None, vmacro_tresh="0"):
     wd = rr.scratch_dir()
     rr.write_inputs(wd, linelist or wl.fe_linelist(), magneto_optical=magneto_optical,
-                    stokes_mode=stokes_mode)
+                    stokes_mode=stokes_mode, vmacro_tresh=vmacro_tresh)
     lam_out, stokes, flag = ref.synth(wd, mu, atm, wave)
     _, stokes_portable, _ = PORTABLE.synth(wd, mu, atm, wave)
     dd = os.path.join(wd, "dump")
@@ -165,6 +167,23 @@ def make_lte_modes(ref, wd):
     wave = np.concatenate([wl.line_wavelengths(41, 0.05, centres=(629.60,)),
                            np.linspace(630.10, 630.30, 121)])
     lte_case(ref, "lte_mixed", atm, wave, linelist=wl.fe_linelist(lines))
+
+
+def make_lte_static(ref, wd):
+    """A static atmosphere: VMACRO_TRESH = 0.1 km/s and no velocity, so
+    atmos.moving stays FALSE (pyrh_compute1dray.c:261-278).  Wavelengths
+    covered only by lines that are not polarizable are then not angle
+    dependent and take the Feautrier solver (formal.c:96-101, 284-304)
+    instead of scalar Bezier3; line shifts are ignored.  The line list of
+    lte_mixed, mu = 0.8."""
+    logtau, T, ne, nH = base_c0(ref, wd)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH, vlos=0.0)
+    lines = sorted([dict(UNPOLARIZED, lam_vac=629.60), dict(UNPOLARIZED, lam_vac=630.20),
+                    *wl.FE_LINES], key=lambda L: L["lam_vac"])
+    wave = np.concatenate([wl.line_wavelengths(41, 0.05, centres=(629.60,)),
+                           np.linspace(630.10, 630.30, 121)])
+    lte_case(ref, "lte_static", atm, wave, mu=0.8, linelist=wl.fe_linelist(lines),
+             vmacro_tresh="0.1")
 
 
 def make_lte_loggf(ref, wd):
@@ -352,6 +371,7 @@ def make_nlte(ref, wd):
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
+          "lte_static": make_lte_static,
           "nlte": make_nlte}
 
 

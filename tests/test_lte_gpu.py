@@ -42,7 +42,7 @@ def run(atms, precision, mu=1.0, api="host", **cfgkw):
     return [o.astype(np.float64) for o in lte.split_output(pk, out)]
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0", "lte_mixed"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0", "lte_mixed", "lte_static"])
 def test_fp64_vs_reference(golden, name):
     fx = golden(name)
     m = O.output_mask(fx["lam"], fx["lambda_ref"])
@@ -52,7 +52,7 @@ def test_fp64_vs_reference(golden, name):
     assert np.all(out[1:, fx["tot_flags"][m][:, 1] == 0] == 0.0)
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0", "lte_mixed"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0", "lte_mixed", "lte_static"])
 def test_fp64_vs_oracle(golden, name):
     fx = golden(name)
     out = run([fx], FP64, mu=float(fx["mu"]))[0]
@@ -60,7 +60,7 @@ def test_fp64_vs_oracle(golden, name):
     assert _err(out, ref).max() < 1e-8
 
 
-@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0", "lte_mixed"])
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_b0", "lte_mixed", "lte_static"])
 def test_fp32_vs_oracle(golden, name):
     fx = golden(name)
     out = run([fx], FP32, mu=float(fx["mu"]))[0]

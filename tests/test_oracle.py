@@ -7,8 +7,10 @@ import pytest
 from conftest import batch_member
 from oracle import oracle as O
 
-# lte_mixed: two unpolarizable lines (Armstrong's Voigt, kurucz.c:824)
-LTE_CASES = ["lte_c0", "lte_edge", "lte_b0", "lte_mixed"]
+# lte_mixed: two unpolarizable lines (Armstrong's Voigt, kurucz.c:824);
+# lte_static: the same lines in a static atmosphere (Feautrier where only
+# unpolarizable lines cover the wavelength, formal.c:96-101)
+LTE_CASES = ["lte_c0", "lte_edge", "lte_b0", "lte_mixed", "lte_static"]
 
 
 def _err(mine, ref):

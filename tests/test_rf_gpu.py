@@ -96,17 +96,18 @@ def test_rf_stokes_equal_forward_kernel(golden, precision, tol):
     every wavelength: DELO-Bezier3 where a polarizable line is in its
     window, scalar Bezier3 where only unpolarizable lines are (lte_mixed),
     Feautrier where none is (lte_edge has four such wavelengths, every case
-    LAMBDA_REF)."""
+    LAMBDA_REF) and, in a static atmosphere, where only unpolarizable lines
+    are (lte_static)."""
     b = golden("lte_batch")
     atms = [batch_member(b, i) for i in range(b["T"].shape[0])] + [golden("lte_edge")]
     atms[-1] = dict(atms[-1], mu=atms[0]["mu"])     # one ray per batch
     # lte_mixed has its own line list: a batch of its own, scalar Bezier3
     # near 629.60 nm
-    mixed = golden("lte_mixed")
-    dm, cm, sm_, _ = gpu_rf([mixed], precision)
-    dm.run(cm)
-    fm = lte.split_output(dm.pk, dm.out.cpu().numpy())[0]
-    assert np.abs(sm_[0] - fm).max() <= tol * fm[0].max()
+    for own in ("lte_mixed", "lte_static"):
+        dm, cm, sm_, _ = gpu_rf([golden(own)], precision)
+        dm.run(cm)
+        fm = lte.split_output(dm.pk, dm.out.cpu().numpy())[0]
+        assert np.abs(sm_[0] - fm).max() <= tol * fm[0].max(), own
     dev, cfg, st, _ = gpu_rf(atms, precision)
     dev.run(cfg)
     fwd = lte.split_output(dev.pk, dev.out.cpu().numpy())
