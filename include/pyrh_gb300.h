@@ -309,7 +309,14 @@ typedef struct {
   const double *nstar;                            /* [nlevel][total_depth] */
   const double *C;                                /* [nlevel^2][total_depth] */
   const double *chi_c, *eta_c, *sca_c;            /* [total_cont] */
-  const int32_t *bgline;                          /* [total_lambda] */
+  const int32_t *bgline;                          /* [total_lambda]: a background
+                                  line covers the wavelength (backgrflags.
+                                  hasline); with cfg->moving the wavelength
+                                  is then angle dependent (formal.c:96-101).
+                                  Background lines enter unpolarized through
+                                  chi_c/eta_c: a polarizable one, which makes
+                                  the reference solve for I, Q, U, V there,
+                                  is outside this entry */
   const pyrh_nlte_transition *trans;              /* [sum ntrans] */
   const double *alpha;                            /* continuum cross-sections */
   const double *adamp;                            /* [sum nline*ndep] */
