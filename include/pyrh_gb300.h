@@ -272,6 +272,9 @@ pyrh_status pyrh_lte_stokes_vjp(const pyrh_lte_batch *batch, const pyrh_line *li
  * emergent intensity of _solveray() (rh/rhf1d/pyrh_solveray.c:82-150).
  * The caller supplies the state that the reference's set-up leaves behind
  * (LTE populations, collision matrix, background, damping, cross-sections).
+ * The formal solution is the scalar one of STOKES_MODE = NO_STOKES: with
+ * FULL_STOKES the reference solves for I, Q, U, V wherever a polarizable
+ * line is in window (formal.c:92-101), which this entry does not.
  */
 #define PYRH_NLTE_MAX_LEVELS  8
 #define PYRH_NLTE_MAX_ACTIVE  16   /* transitions active at one wavelength */
