@@ -22,6 +22,8 @@ Fixtures (npz, float64):
                   alone in its window and one among the polarized lines
   lte_static      the lines of lte_mixed in a static atmosphere (VMACRO_TRESH
                   0.1 km/s, no velocity: atmos.moving FALSE), mu = 0.8
+  lte_static_v    the same with velocities below the threshold (+-0.09 km/s),
+                  which the reference then ignores
   lte_loggf       the reference's analytical log gf RFs of Stokes I (NO_STOKES
                   C0, both lines) and central differences of its synthesis in
                   log gf
@@ -183,6 +185,12 @@ def make_lte_static(ref, wd):
     wave = np.concatenate([wl.line_wavelengths(41, 0.05, centres=(629.60,)),
                            np.linspace(630.10, 630.30, 121)])
     lte_case(ref, "lte_static", atm, wave, mu=0.8, linelist=wl.fe_linelist(lines),
+             vmacro_tresh="0.1")
+    # velocities below the threshold: still static, and the reference
+    # ignores them (no line shifts)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH)
+    atm[3] = np.linspace(-0.09, 0.09, len(logtau))
+    lte_case(ref, "lte_static_v", atm, wave, mu=0.8, linelist=wl.fe_linelist(lines),
              vmacro_tresh="0.1")
 
 
