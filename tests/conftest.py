@@ -93,10 +93,12 @@ def rf_eval(lib, fx, sel, single=False, jac=False, loggf=False, setup_dT=None,
         args += [arr(g(k)) if g(k) is not None else None
                  for k in ("dline_pops", "dnp", "dlen_up", "dlen_dn")]
     lib.rf_set_stokes_mode(0 if no_stokes else 3)
+    lib.rf_set_moving(int(fx["moving"]))
     try:
         r = fn(*args)
     finally:
         lib.rf_set_stokes_mode(3)
+        lib.rf_set_moving(1)
     assert r == 0
     return (st, rf, gf) if loggf else (st, rf)
 

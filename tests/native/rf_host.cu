@@ -22,6 +22,10 @@ using namespace pyrh;
 // STOKES_MODE of the next evaluations (PYRH_FULL_STOKES or PYRH_NO_STOKES)
 static int g_stokes_mode = PYRH_FULL_STOKES;
 extern "C" void rf_set_stokes_mode(int mode) { g_stokes_mode = mode; }
+// atmos.moving: 0 for a static atmosphere (line shifts ignored, and
+// Feautrier where no polarizable line covers the wavelength)
+static int g_moving = 1;
+extern "C" void rf_set_moving(int moving) { g_moving = moving; }
 
 struct SetupDT {
   const double *dchi_c, *deta_c, *dline_pops, *dnp, *dlen_up, *dlen_dn;
@@ -127,7 +131,7 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     for (int k = 0; k < nd; ++k)
       ld[l][k] = line_depth<R>(c, R(T[k]), R(vel[k]), R(vturb[k]), R(B[k]), R(ne[k]), R(nHtot[k]),
                                R(np[k]), R(line_pops[(l * 2 + 0) * nd + k]),
-                               R(line_pops[(l * 2 + 1) * nd + k]), R(mu), true,
+                               R(line_pops[(l * 2 + 1) * nd + k]), R(mu), g_moving != 0,
                                dT.dline_pops ? R(dT.dline_pops[(l * 2 + 0) * nd + k]) : R(0),
                                dT.dline_pops ? R(dT.dline_pops[(l * 2 + 1) * nd + k]) : R(0),
                                dT.dnp ? R(dT.dnp[k]) : R(0));
@@ -146,13 +150,14 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     const double lm = lam[la];
     const double dlc = lm * kQ_WING * (vmicro_char / kCLIGHT);
     unsigned inwin = 0;
-    bool pol = false;
+    bool pol = false, anypol = false;
     R dlam[PYRH_MAX_LINES];
     for (int l = 0; l < nline; ++l) {
       dlam[l] = R(lm - lines[l].lambda0);
       if (fabs(lines[l].lambda0 - lm) <= dlc && lines[l].contributes) {
         inwin |= 1u << l;
         pol |= lines[l].polarizable != 0 && g_stokes_mode == PYRH_FULL_STOKES;
+        anypol |= lines[l].polarizable != 0;
       }
     }
     double* rfl = rf + (int64_t)la * 4 * kNX * nd;
@@ -177,7 +182,7 @@ static int rf_eval_t(int nd, const double* height, const double* T, const double
     static FeautTape<R> ft;
     static ScalarTape<R> sbt;
     static ScalarAdj<R> fadj;
-    const bool feaut = inwin == 0u;
+    const bool feaut = inwin == 0u || (!anypol && !g_moving);
     if (feaut) {
       out[0] = feautrier_fwd<R>(tape, ds, nd, B0, B1, ft);
       feautrier_vjp<R>(tape, ds, nd, B0, B1, ft, R(1), fadj);
