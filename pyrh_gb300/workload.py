@@ -109,16 +109,18 @@ def line_wavelengths(n_per_line: int = 201, half_width: float = 0.05,
 
 
 def kurucz_record(lam_air, loggf, code, E_low_cm, J_low, label_low, E_up_cm,
-                  J_up, label_up, damp, gL_low, gL_up, l_low, l_up) -> str:
+                  J_up, label_up, damp, gL_low, gL_up, l_low, l_up,
+                  iso_log=0.0, hfs_log=0.0) -> str:
     """One line of a Kurucz-format list at the fixed columns that the
     reference reader uses (rh/kurucz.c:187-373): wavelength, log gf, code and
     first energy by whitespace, J at +35, labels at +41 and +69, second energy
     at +53, J at +63, damping at +79, isotope data at +106/+108/+117,
-    hyperfine shifts at +123, Lande factors x1000 at +143, orbital l at +160."""
+    hyperfine shifts at +123, Lande factors x1000 at +143, orbital l at +160.
+    iso_log, hfs_log: log10 of the isotope and hyperfine fractions."""
     rec = (f"{lam_air:11.4f}{loggf:7.3f}{code:6.2f}{E_low_cm:11.3f}{J_low:5.1f} "
            f"{label_low:10s}  {E_up_cm:10.3f}{J_up:5.1f} {label_up:10s}"
            f"{damp[0]:6.2f}{damp[1]:6.2f}{damp[2]:6.2f}"
-           f"{'SYNT':4s} 0 0{0:3d}{0.0:6.3f}{0:3d}{0.0:6.3f}{0:5d}{0:5d}"
+           f"{'SYNT':4s} 0 0{0:3d}{iso_log:6.3f}{0:3d}{hfs_log:6.3f}{0:5d}{0:5d}"
            f"{'':10s}{int(round(gL_low * 1000)):5d}{int(round(gL_up * 1000)):5d}"
            f"{'':7s}{l_low} {l_up}")
     assert rec[35:40].strip() and rec[143:153].strip() and len(rec) <= 171
@@ -144,7 +146,8 @@ def fe_linelist(lines=FE_LINES) -> str:
         out.append(kurucz_record(lam_air, L["loggf"], 26.00, E_low, L["J"][0],
                                  L["labels"][0], E_up, L["J"][1], L["labels"][1],
                                  L["damp"], L["gL"][0], L["gL"][1],
-                                 L["orbital"][0], L["orbital"][1]))
+                                 L["orbital"][0], L["orbital"][1],
+                                 L.get("iso_log", 0.0), L.get("hfs_log", 0.0)))
     return "\n".join(out) + "\n"
 
 

@@ -24,6 +24,8 @@ Fixtures (npz, float64):
                   0.1 km/s, no velocity: atmos.moving FALSE), mu = 0.8
   lte_static_v    the same with velocities below the threshold (+-0.09 km/s),
                   which the reference then ignores
+  lte_broadening  C0 with one line on Unsold's van der Waals broadening and
+                  one with isotope and hyperfine fractions below one
   lte_loggf       the reference's analytical log gf RFs of Stokes I (NO_STOKES
                   C0, both lines) and central differences of its synthesis in
                   log gf
@@ -192,6 +194,20 @@ def make_lte_static(ref, wd):
     atm[3] = np.linspace(-0.09, 0.09, len(logtau))
     lte_case(ref, "lte_static_v", atm, wave, mu=0.8, linelist=wl.fe_linelist(lines),
              vmacro_tresh="0.1")
+
+
+def make_lte_broadening(ref, wd):
+    """Line-list variants of C0: the 630.15 nm line with orbital numbers
+    (s, d) that no Barklem table covers, so the reader falls back to
+    Unsold's van der Waals cross-section (kurucz.c:313-346), and the
+    630.25 nm line with isotope and hyperfine fractions of 10^-0.3 and
+    10^-0.1 (kurucz.c:359-365)."""
+    logtau, T, ne, nH = base_c0(ref, wd)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH)
+    lines = [dict(wl.FE_LINES[0], orbital=(0, 2)),
+             dict(wl.FE_LINES[1], iso_log=-0.3, hfs_log=-0.1)]
+    lte_case(ref, "lte_broadening", atm, wl.line_wavelengths(101, 0.05),
+             linelist=wl.fe_linelist(lines))
 
 
 def make_lte_loggf(ref, wd):
@@ -379,7 +395,7 @@ def make_nlte(ref, wd):
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
-          "lte_static": make_lte_static,
+          "lte_static": make_lte_static, "lte_broadening": make_lte_broadening,
           "nlte": make_nlte}
 
 

@@ -11,7 +11,10 @@ from oracle import oracle as O
 # lte_static: the same lines in a static atmosphere (Feautrier where only
 # unpolarizable lines cover the wavelength, formal.c:96-101); lte_static_v:
 # velocities below VMACRO_TRESH, which the static case ignores
-LTE_CASES = ["lte_c0", "lte_edge", "lte_b0", "lte_mixed", "lte_static", "lte_static_v"]
+# lte_broadening: Unsold van der Waals broadening, isotope and hyperfine
+# fractions below one
+LTE_CASES = ["lte_c0", "lte_edge", "lte_b0", "lte_mixed", "lte_static", "lte_static_v",
+             "lte_broadening"]
 
 
 def _err(mine, ref):
