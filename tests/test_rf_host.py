@@ -70,7 +70,8 @@ def step(fx, key, k, rel):
 
 
 @pytest.mark.parametrize("name", ["lte_c0", "lte_edge", "lte_batch:0", "lte_batch:1",
-                                  "lte_mixed", "lte_static", "lte_static_v"])
+                                  "lte_mixed", "lte_static", "lte_static_v",
+                                  "lte_broadening"])
 def test_adjoint_matches_finite_differences(rf_harness, golden, name):
     if ":" in name:
         n, i = name.split(":")
