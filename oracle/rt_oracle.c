@@ -21,7 +21,11 @@
  *                   the emergent Stokes vector does not depend on the other
  *                   direction, rh/rhf1d/formal.c:167-275)
  *   scalar_bezier3  rh/rhf1d/bezier_1D.c:306-541 (same ray; used when no
- *                   polarizable line covers the wavelength, formal.c:94-95)
+ *                   polarizable line covers the wavelength, formal.c:94-95,
+ *                   and the wavelength is angle dependent, formal.c:96-101)
+ *   feautrier       rh/rhf1d/feautrier.c:56-202 (wavelengths that are not
+ *                   angle dependent: no line in window, or in a static
+ *                   atmosphere no polarizable one, formal.c:284-304)
  */
 #include <math.h>
 #include <stdlib.h>
