@@ -375,17 +375,141 @@ pyrh_status pyrh_nlte_emergent(const pyrh_nlte_batch *batch, const pyrh_nlte_con
    phi_elems is the line-profile size of the batch (as for
    pyrh_nlte_workspace_bytes); batches whose scratch does not fit, or with
    more than 256 atmospheres, are rejected with PYRH_ERR_ARG.  The call
-   allocates nothing.  The first call on a device looks up the array's
-   device address (cudaGetSymbolAddress) with that device current, which
-   also loads this library's device code there if that has not happened
-   yet; make that first call before any stream capture.  Nothing in the
-   array has to start at zero: the call clears its error word and every
-   kernel writes the rest before reading it, so each call may find the
-   previous call's contents there.  All calls share the one array: calls
+   allocates nothing.  Every call looks up the array's device address in
+   the current context (cudaGetSymbolAddress, with the caller's device
+   current) instead of keeping it from an earlier call, so a cudaDeviceReset
+   or another context on the same device between calls is safe; the first
+   call on a device also loads this library's device code there if that has
+   not happened yet, so make that first call before any stream capture.
+   Nothing in the array has to start at zero: the call clears its error
+   word and its flags, and every kernel writes the rest (or zeroes it)
+   before reading it, so each call may find the previous call's contents
+   there.  All calls share the one array: calls
    that overlap on the GPU (other streams, other host threads) race on it. */
 pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch *batch, const pyrh_nlte_config *cfg,
                                    int64_t phi_elems, int32_t *iterations, double *dpops,
                                    void *stream);
+
+/* ====================================================================
+ * Host-side set-up (no device work): the RH model atom, the wavelength
+ * grids of its transitions, the global wavelength grid and the output
+ * index.  These restate the reference's set-up so that a caller can build
+ * pyrh_nlte_batch wavelength tables (lambda, transition nblue / nlambda,
+ * continuum cross-sections) from the *.atom file and keyword values the
+ * reference reads, with bit-identical grids and integer ranges.
+ * ==================================================================== */
+#define PYRH_ATOM_MAX_LEVELS      64
+#define PYRH_ATOM_MAX_LINES       128
+#define PYRH_ATOM_MAX_CONT        64
+#define PYRH_ATOM_MAX_COMPONENTS  8
+#define PYRH_ATOM_MAX_TABLE       4096   /* explicit continuum table rows */
+#define PYRH_ATOM_MAX_COLL        512    /* tabulated collision records */
+#define PYRH_ATOM_MAX_COLLVALS    8192   /* their temperatures and values */
+#define PYRH_ATOM_LABEL           20
+
+typedef enum {
+  PYRH_ATOM_VDW_UNSOLD = 0, PYRH_ATOM_VDW_RIDDER_RENSBERGEN = 1, PYRH_ATOM_VDW_BARKLEM = 2
+} pyrh_atom_vdw;
+
+typedef enum {
+  PYRH_COLL_OMEGA = 0, PYRH_COLL_CE = 1, PYRH_COLL_CI = 2, PYRH_COLL_CP = 3, PYRH_COLL_CH = 4,
+  PYRH_COLL_CH0 = 5, PYRH_COLL_CHP = 6, PYRH_COLL_CR = 7
+} pyrh_coll_type;
+
+typedef struct {
+  double E;              /* J (from E_cm * h c / cm, readatom.c:204) */
+  double E_cm;           /* as read, cm^-1 */
+  double g;
+  int32_t stage, abo_level;
+  char label[PYRH_ATOM_LABEL + 4];
+} pyrh_atom_level;
+
+typedef struct {
+  int32_t i, j;                  /* lower, upper level */
+  int32_t nlambda;               /* as read */
+  int32_t symmetric;             /* no ASYMM keyword */
+  int32_t voigt, prd, vdwaals, ncomponent;
+  double f, lambda0;             /* oscillator strength; vacuum nm */
+  double Aji, Bji, Bij;
+  double qcore, qwing;
+  double cvdw[4], Grad, cStark, g_lande_eff;
+  double c_shift[PYRH_ATOM_MAX_COMPONENTS], c_fraction[PYRH_ATOM_MAX_COMPONENTS];
+} pyrh_atom_line;
+
+typedef struct {
+  int32_t i, j, nlambda, hydrogenic;
+  double alpha0, lambda0, lambda_min;   /* m^2, vacuum nm, nm */
+  int64_t table_off;                    /* explicit: rows in table_lambda/alpha */
+} pyrh_atom_cont;
+
+typedef struct {
+  int32_t type, i, j, ntemp;
+  int32_t temp_off, value_off;          /* into coll_values */
+} pyrh_atom_coll;
+
+typedef struct {
+  char id[4];
+  int32_t nlevel, nline, ncont, nfixed, ntable, ncoll, ncoll_values;
+  pyrh_atom_level level[PYRH_ATOM_MAX_LEVELS];
+  pyrh_atom_line line[PYRH_ATOM_MAX_LINES];
+  pyrh_atom_cont cont[PYRH_ATOM_MAX_CONT];
+  double table_lambda[PYRH_ATOM_MAX_TABLE], table_alpha[PYRH_ATOM_MAX_TABLE];
+  pyrh_atom_coll coll[PYRH_ATOM_MAX_COLL];
+  double coll_values[PYRH_ATOM_MAX_COLLVALS];
+} pyrh_atom;
+
+/* Keyword values the grids depend on. */
+typedef struct {
+  double vmicro_char;    /* m/s (VMICRO_CHAR, km/s in keyword.input) */
+  double B_char;         /* T (B_STRENGTH_CHAR) */
+  int32_t moving;        /* atmos.moving */
+  int32_t stokes;        /* atmos.Stokes (pyrh sets it TRUE in every mode) */
+} pyrh_grid_config;
+
+/* Parses the text of an RH .atom file (replaces readAtom, rh/readatom.c:
+   62-470): levels, bound-bound and bound-free transitions, and the
+   tabulated collision records (TEMP, OMEGA, CE, CI, CP, CH, CH0, CH+, CR).
+   Returns PYRH_ERR_UNSUPPORTED for other collision types or beyond the
+   PYRH_ATOM_MAX_* limits. */
+pyrh_status pyrh_atom_read(const char *text, pyrh_atom *atom);
+
+/* Effective Lande factor of line kr (effectiveLande, rh/zeeman.c:106-125)
+   and whether it is polarizable for an active atom (readatom.c:347-366):
+   1 yes, 0 no, -1 a composite line that would be (an error there). */
+double pyrh_atom_lande_eff(const pyrh_atom *atom, int32_t kr);
+int32_t pyrh_atom_line_polarizable(const pyrh_atom *atom, int32_t kr, int32_t stokes);
+
+/* Wavelength grid of line kr (getLambda, rh/getlambda.c:44-162) and of
+   continuum kr (getLambdaCont, rh/getlambda.c:166-180, or its explicit
+   table).  With lam NULL only the point count is returned; -1 on error. */
+int32_t pyrh_line_grid(const pyrh_atom *atom, int32_t kr, const pyrh_grid_config *cfg,
+                       double *lam, int32_t cap);
+int32_t pyrh_cont_grid(const pyrh_atom *atom, int32_t kr, double *lam, int32_t cap);
+
+/* Global wavelength grid (SortLambda, rh/sortlambda.c:42-420): lambda_ref
+   (if > 0), the caller's wavelengths and the transition grids (ngrid
+   grids, concatenated in grids[], grid_n points each), sorted ascending
+   and with duplicates removed (a value is kept only if strictly larger
+   than the previous one).  wave_inds[i] is the grid index of wave[i] (the
+   reference's spectrum.wave_inds), nblue[g] / nlambda[g] the index range
+   of grid g between its first and last wavelength, every grid point in
+   between included (what the NLTE batch expects in its transitions). */
+pyrh_status pyrh_sort_lambda(const double *wave, int32_t nwave, double lambda_ref,
+                             const double *grids, const int32_t *grid_n, int32_t ngrid,
+                             double *lam, int32_t cap, int32_t *nspect, int32_t *wave_inds,
+                             int32_t *nblue, int32_t *nlambda);
+
+/* Indices of the output wavelengths: every grid point except the one equal
+   to lambda_ref (pyrh_solveray.c:115-156, which assumes it is present;
+   PYRH_ERR_ARG here when it is not). */
+pyrh_status pyrh_output_index(const double *lam, int32_t nspect, double lambda_ref,
+                              int32_t *idx, int32_t *nout);
+
+/* Hydrogenic bound-free cross-section of continuum kr on the wavelengths
+   lam[0..n-1] (sortlambda.c:331-344 with Gaunt_bf, rh/hydrogen.c:269-281). */
+double pyrh_gaunt_bf(double lambda, double n_eff, int32_t charge);
+pyrh_status pyrh_cont_alpha(const pyrh_atom *atom, int32_t kr, const double *lam, int32_t n,
+                            double *alpha);
 
 /* Number of kernel launches the last pyrh_lte_stokes / pyrh_nlte_* call issued. */
 int32_t pyrh_last_launch_count(void);

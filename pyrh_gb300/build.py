@@ -2,6 +2,7 @@
 machinery: the library exposes a plain C ABI, include/pyrh_gb300.h)."""
 from __future__ import annotations
 
+import hashlib
 import os
 import subprocess
 from concurrent.futures import ThreadPoolExecutor
@@ -14,10 +15,21 @@ LIB = os.path.join(HERE, "libpyrh_gb300.so")
 # the largest instantiations compile in parallel
 UNITS = ["capi.cu", "lte_stokes.cu", "lte_rf.cu"] + \
     [f"lte_rf_fp{p}_{m}.cu" for p in ("32", "64") for m in ("rf", "chi2", "vjp")] + \
-    ["nlte.cu", "nlte_capi.cu"]
+    ["nlte.cu", "nlte_capi.cu", "setup_host.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+
+def sources_digest(files) -> str:
+    """Digest of source files given relative to the repository root (ties a
+    recorded measurement to the kernel sources it was taken on)."""
+    repo = os.path.dirname(HERE)
+    h = hashlib.sha256()
+    for f in files:
+        with open(os.path.join(repo, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
 
 
 def _sources_mtime() -> float:
@@ -38,7 +50,7 @@ def build(force: bool = False, verbose: bool = False, out: str | None = None,
     dflags = [f"-D{d}" for d in defines]
 
     def compile_unit(u):
-        obj = os.path.join(bdir, u.replace(".cu", ".o"))
+        obj = os.path.join(bdir, os.path.splitext(u)[0] + ".o")
         cmd = [NVCC, *GENCODE, *FLAGS, *dflags, "-c", os.path.join(CSRC, u), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
