@@ -511,6 +511,30 @@ double pyrh_gaunt_bf(double lambda, double n_eff, int32_t charge);
 pyrh_status pyrh_cont_alpha(const pyrh_atom *atom, int32_t kr, const double *lam, int32_t n,
                             double *alpha);
 
+/* Per-depth NLTE set-up of a batch for one model atom, on the device (one
+   thread per depth point): LTE populations (LTEpops, rh/ltepops.c:33-109),
+   the collision rate matrix (CollisionRate, rh/collision.c:450-700: OMEGA,
+   CE, CI, CP, CH, CH0, CH+ records on their TEMP grids, with the reference's
+   cubic spline, rh/spline.c, or linear interpolation for two points) and the
+   Doppler widths (readatom.c:178-186).  Arrays are device memory indexed by
+   depth point like pyrh_nlte_batch (per level [nlevel][total_depth], per
+   level pair [nlevel^2][total_depth]); the outputs are what that batch takes
+   as nstar, C and vbroad. */
+typedef struct {
+  int64_t total_depth;
+  const double *T, *ne, *ntotal, *vturb;   /* [total_depth] SI; ntotal = abundance * nHtot */
+  const double *nh0, *np;                 /* neutral hydrogen ground level and protons,
+                                             for CP, CH, CH0, CH+ records (else NULL) */
+  double *nstar;                          /* [nlevel][total_depth] */
+  double *C;                              /* [nlevel^2][total_depth] */
+  double *vbroad;                         /* [total_depth] or NULL */
+} pyrh_nlte_setup_batch;
+
+size_t pyrh_nlte_setup_workspace_bytes(const pyrh_atom *atom);
+pyrh_status pyrh_nlte_setup(const pyrh_atom *atom, double weight_amu,
+                            const pyrh_nlte_setup_batch *batch, void *workspace,
+                            size_t workspace_bytes, void *stream);
+
 /* Number of kernel launches the last pyrh_lte_stokes / pyrh_nlte_* call issued. */
 int32_t pyrh_last_launch_count(void);
 

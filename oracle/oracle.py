@@ -255,7 +255,7 @@ def nlte_first_iteration(fx: dict):
     P = nlte_problem(fx, keep)
     phis, wphi = nlte_profiles(fx)
     arr = (_D * max(len(phis), 1))(*[_p(x) for x in phis])
-    n = np.array(fx["n0"], dtype=np.float64)
+    n = np.array(fx["n0"], dtype=np.float64, order="C")
     J0 = keep.f64(nlte_J0(fx))
     J = np.zeros_like(J0)
     G = np.zeros((P.nlevel * P.nlevel, P.ndep))
@@ -270,8 +270,8 @@ def nlte_solve(fx: dict):
     """Converged populations, final J, iteration count and dpops history."""
     keep = _Keep()
     P = nlte_problem(fx, keep)
-    n = np.array(fx["n0"], dtype=np.float64)
-    J = np.array(nlte_J0(fx), dtype=np.float64)
+    n = np.array(fx["n0"], dtype=np.float64, order="C")
+    J = np.array(nlte_J0(fx), dtype=np.float64, order="C")
     dp = np.zeros(P.nmax_iter)
     acc = np.zeros(P.nmax_iter, dtype=np.int32)
     it = _nlte_lib().oracle_nlte_iterate(C.byref(P), _p(n), _p(J), _p(dp),

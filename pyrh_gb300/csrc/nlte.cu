@@ -2,25 +2,29 @@
 // atmospheres.
 //
 // Per iteration (rh/iterate.c:48-143):
-//   gamma_init    Gamma = C, new J = 0                  (fillgamma.c:44-54)
+//   gamma_init    new J = 0, the tiles' rate sums = 0    (fillgamma.c:44-54)
 //   formal        every (atmosphere, wavelength, ray): active-atom opacity
 //                 (opacity.c:64-300), formal solution with the diagonal
 //                 operator for both directions (bezier_1D.c:306-541) or
 //                 Feautrier where no line is active (feautrier.c:56-202),
 //                 cross-coupling (fillgamma.c:251-332) and the Gamma / J
 //                 quadrature (fillgamma.c:82-246, formal.c:247-256)
-//   stateq        per depth: statEquil with Crout LU + one improvement
-//                 (statequil.c:40-102, ludcmp.c:36-177), FP64
+//   jcopy         J = new J
+//   stateq        per depth: Gamma = C + the tiles' rate sums, statEquil
+//                 with Crout LU + one improvement (statequil.c:40-102,
+//                 ludcmp.c:36-177), FP64
 //   ng            per atmosphere: Ng acceleration and MaxChange
 //                 (accelerate.c:68-146, maxchange.c:32-50), FP64;
 //                 converged atmospheres drop out of later launches
 // Line profiles (profile.c:67-371, Armstrong Voigt of voigt.c:126-243) are
 // computed once in FP64 and kept in the workspace in the formal-solution
 // precision.  The per-(wavelength, depth) opacity and rate contributions run
-// in the formal-solution precision; the Gamma quadrature of a block of 32
-// wavelengths x all rays is summed in shared memory in that precision before
-// one FP64 global atomic per entry (in FP32 mode the FP64 units, a small
-// fraction of the FP32 rate on this GPU, stay out of the inner loops).
+// in the formal-solution precision.  A warp owns one tile of 32 wavelengths
+// of one atmosphere and runs every ray through it; its rate and J
+// contributions are summed over the tile's wavelengths with shuffles and
+// added in FP64 to sums that only this warp writes, in program order, and
+// the tiles' sums are added in tile order when the rate matrix is
+// assembled: every sum has a fixed order, so a solve is bit-reproducible.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -128,17 +132,27 @@ __global__ void nlte_wphi_kernel(NlteArgs A) {
   }
 }
 
-// Gamma = C and the new J = 0 for atmospheres still iterating.
+// Rate-matrix partial sums of a wavelength tile: the off-diagonal entries
+// (i, j), i != j, of the tile's 32 wavelengths x all rays, one FP64 value per
+// (tile, entry, depth) at ((tile * nslot + gamma_slot) * total_depth + depth).
+__host__ __device__ inline int gamma_slot(int i, int j, int nlev) {
+  return i * (nlev - 1) + j - (j > i ? 1 : 0);
+}
+
+// The new J = 0 and the tiles' rate partial sums = 0 for atmospheres still
+// iterating (Gamma = C is added back when statEquil assembles the matrix).
 __global__ void nlte_gamma_init_kernel(NlteArgs A) {
   const pyrh_nlte_batch& b = A.b;
   const int p = blockIdx.y;
+  if (blockIdx.x == 0 && p == 0 && threadIdx.x == 0) *A.any = 0;   // nlte_ng_kernel sets it
   if (!A.active[p]) return;
-  const int nd = b.ndep[p], nl2 = b.nlevel * b.nlevel;
+  const int nd = b.ndep[p], nslot = b.nlevel * (b.nlevel - 1);
+  const int ntile = (b.nspect[p] + 31) / 32;
   const int64_t doff = b.depth_off[p];
-  for (int e = threadIdx.x + blockIdx.x * blockDim.x; e < nl2 * nd; e += blockDim.x * gridDim.x) {
-    const int ij = e / nd, k = e % nd;
-    const int64_t g = (int64_t)ij * b.total_depth + doff + k;
-    A.Gamma[g] = b.C[g];
+  for (int e = threadIdx.x + blockIdx.x * blockDim.x; e < ntile * nslot * nd;
+       e += blockDim.x * gridDim.x) {
+    const int ts = e / nd, k = e % nd;
+    A.gslab[(int64_t)ts * b.total_depth + doff + k] = 0.0;
   }
   const int64_t coff = b.cont_off[p], ncont = (int64_t)nd * b.nspect[p];
   for (int64_t e = threadIdx.x + (int64_t)blockIdx.x * blockDim.x; e < ncont;
@@ -165,29 +179,10 @@ struct ActiveSet {
   R hckl;                        // h c / (k_B lambda)
 };
 
-// Shared-memory accumulation.  FP64: atomicAdd.  FP32: compensated -- the
-// atomic returns the value it added to, the rounding error of that one
-// addition follows exactly from it (Knuth's TwoSum), and the errors are summed
-// in a second array that is added back in FP64 when the block flushes.  The
-// quadrature then carries ~FP64 accuracy at FP32 atomic cost.
-__device__ __forceinline__ void acc_add(double* hi, double* lo, double v) {
-  (void)lo;
-  atomicAdd(hi, v);
-}
-__device__ __forceinline__ void acc_add(float* hi, float* lo, float v) {
-  const float old = atomicAdd(hi, v);
-  const float s = old + v;
-  const float bv = s - old;
-  atomicAdd(lo, (old - (s - bv)) + (v - bv));
-}
-
-// Per-block staging of the quantities every thread reads at every depth.
+// Per-block staging of the atmosphere's quantities that every thread reads
+// at every depth (the block's warps are wavelength tiles of one atmosphere).
 template <typename R>
 struct NlteShared {
-  R* Gs;      // [nlev (nlev - 1)][nd] off-diagonal Gamma of this block's wavelengths
-  R* Gl;      // the same, compensation terms of Gs (FP32 mode)
-  R* Js;      // [nd][32] new J of this block's wavelengths (no compensation:
-              // at most 2 PYRH_NLTE_MAX_RAYS terms per entry)
   R* n;       // [nlev][nd] populations
   R* lnst;    // [nlev][nd] log of the LTE populations
   R* iT;      // [nd] 1 / T
@@ -204,11 +199,11 @@ struct NlteOpacity {
   int nd, ns, la, q;
   int64_t coff;
 
-  // Total opacity, source function and the background part of the source
-  // function (eta_c + sca_c J) / chi at depth k, plus the atom's emissivity
-  // (opacity.c:64-300 for the active atom).
-  __device__ __forceinline__ void operator()(int k, R& chi, R& S, R& S_bg, R& eta_atom,
-                                             double Jold) const {
+  // Total opacity, source function, the background part of the source
+  // function (eta_c + sca_c J) / chi, the background opacity chi_c and the
+  // atom's emissivity at depth k (opacity.c:64-300 for the active atom).
+  __device__ __forceinline__ void operator()(int k, R& chi, R& S, R& S_bg, R& chi_bg,
+                                             R& eta_atom, double Jold) const {
     const pyrh_nlte_batch& b = A->b;
     R chi_a = 0, eta_a = 0;
     for (int m = 0; m < as->n; ++m) {
@@ -229,23 +224,16 @@ struct NlteOpacity {
       }
     }
     const int64_t c = coff + (int64_t)k * ns + la;
-    const R ct = chi_a + R(b.chi_c[c]);
+    chi_bg = R(b.chi_c[c]);
+    const R ct = chi_a + chi_bg;
     const R eta_bg = R(b.eta_c[c]) + R(b.sca_c[c]) * R(Jold);
     chi = ct;
     S = (eta_a + eta_bg) / ct;
     S_bg = eta_bg / ct;
     eta_atom = eta_a;
   }
-
-  __device__ __forceinline__ void operator()(int k, R& chi, R& S, R& eta_atom,
-                                             double Jold) const {
-    R S_bg;
-    (*this)(k, chi, S, S_bg, eta_atom, Jold);
-  }
 };
 
-// Scalar Bezier3 with the diagonal operator along one direction; stores
-// I[k] and Psi[k] for every depth (bezier_1D.c:306-541).
 // Mean intensity of one wavelength at depth k ([depth][lambda] storage).
 struct JRow {
   const double* base;
@@ -253,32 +241,33 @@ struct JRow {
   __device__ __forceinline__ double operator[](int k) const { return base[(int64_t)k * stride]; }
 };
 
-template <typename R, typename Op>
-__device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, double B0, double B1,
-                            const JRow& Jold, R* I, R* Psi, R* Ieff, R* chi_out) {
-  // Ieff[k] = I[k] - Psi[k] * S_atom[k], the effective intensity of the
-  // MALI rates (fillgamma.c:121-134), is built term by term in the same
-  // recurrence: the local source enters through S_bg = S - S_atom only, so
-  // no difference of two nearly equal intensities is ever formed.  In
-  // optically thick line cores I and Psi*S_atom agree to many digits, and
-  // forming their difference from single-precision I and Psi would lose
-  // all of them.
+// Scalar Bezier3 with the diagonal operator along one direction
+// (bezier_1D.c:306-541).  Each depth's intensity I, operator Psi, 1 - Psi,
+// effective intensity and opacities are handed to emit(k, ...) as soon as
+// they are known, so the rate and J quadratures run inside the recurrence
+// and nothing is stored per depth.  Returns the intensity at the last depth
+// of the sweep (the emergent one for to_obs).
+template <typename R, typename Op, typename Emit>
+__device__ __forceinline__ R bezier_sweep(const Op& op, const R* ds, int nd, int to_obs,
+                                          double B0, double B1, const JRow& Jold, Emit&& emit) {
+  // Ieff = I - Psi S_atom, the effective intensity of the MALI rates
+  // (fillgamma.c:121-134), is built term by term in the same recurrence: the
+  // local source enters through S_bg = S - S_atom only, so no difference of
+  // two nearly equal intensities is ever formed.  In optically thick line
+  // cores I and Psi S_atom agree to many digits, and forming their
+  // difference from single-precision I and Psi would lose all of them.
   const int dk = to_obs ? -1 : 1, k_start = to_obs ? nd - 1 : 0, k_end = to_obs ? 0 : nd - 1;
   R ea;
   R chi_u, chi_c, chi_d, chi_dd = 0, S_u, S_c, S_d, S_dd = 0, Sb_u, Sb_c, Sb_d, Sb_dd = 0;
-  op(k_start, chi_u, S_u, Sb_u, ea, Jold[k_start]);
-  op(k_start + dk, chi_c, S_c, Sb_c, ea, Jold[k_start + dk]);
-  op(k_start + 2 * dk, chi_d, S_d, Sb_d, ea, Jold[k_start + 2 * dk]);
-  chi_out[k_start] = chi_u;
-  chi_out[k_start + dk] = chi_c;
-  chi_out[k_start + 2 * dk] = chi_d;
+  R cb_u, cb_c, cb_d, cb_dd = 0;
+  op(k_start, chi_u, S_u, Sb_u, cb_u, ea, Jold[k_start]);
+  op(k_start + dk, chi_c, S_c, Sb_c, cb_c, ea, Jold[k_start + dk]);
+  op(k_start + 2 * dk, chi_d, S_d, Sb_d, cb_d, ea, Jold[k_start + 2 * dk]);
   // interval path length between depth a and a+1 is ds[a+1]
   auto dsi = [&](int a, int b2) { return ds[a > b2 ? a : b2]; };
   const R dtau0 = R(0.5) * (chi_u + chi_c) * dsi(k_start, k_start + dk);
   R I_upw = to_obs ? R(B1 - (B0 - B1) / (double)dtau0) : R(0);
-  I[k_start] = I_upw;
-  Psi[k_start] = R(0);
-  Ieff[k_start] = I_upw;
+  emit(k_start, I_upw, R(0), R(1), I_upw, chi_u, cb_u);
   int k = k_start + dk;
   R dsup = dsi(k, k - dk), dsdn = dsi(k + dk, k);
   R dchi_up = (chi_c - chi_u) / dsup;
@@ -291,8 +280,7 @@ __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, doubl
     dsdn = dsi(k + dk, k);
     R dchi_dn;
     if (abs(k - k_end) > 1) {
-      op(k + 2 * dk, chi_dd, S_dd, Sb_dd, ea, Jold[k + 2 * dk]);
-      chi_out[k + 2 * dk] = chi_dd;
+      op(k + 2 * dk, chi_dd, S_dd, Sb_dd, cb_dd, ea, Jold[k + 2 * dk]);
       dchi_dn = cent_deriv<R>(dsdn, dsi(k + 2 * dk, k + dk), chi_c, chi_d, chi_dd);
     } else {
       dchi_dn = (chi_d - chi_c) / dsdn;
@@ -310,13 +298,15 @@ __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, doubl
     // control point minus S_atom: S_bg - dt03 dS_c, or -S_atom where it clips
     const R c1_eff = c1_raw > R(0) ? Sb_c - dt03 * dS_c : Sb_c - S_c;
     const R upw = I_upw * eps + beta * S_u + theta * c2;
-    Ieff[k] = upw + alpha * Sb_c + gamma * c1_eff;
+    const R Ieff = upw + alpha * Sb_c + gamma * c1_eff;
     I_upw = upw + alpha * S_c + gamma * c1;
-    I[k] = I_upw;
-    Psi[k] = alpha + gamma;
+    // 1 - Psi without cancellation: the Bezier3 weights of a constant
+    // source function sum to one (eps + alpha + beta + gamma + theta = 1)
+    emit(k, I_upw, alpha + gamma, eps + beta + theta, Ieff, chi_c, cb_c);
     S_u = S_c; S_c = S_d; S_d = S_dd;
     Sb_u = Sb_c; Sb_c = Sb_d; Sb_d = Sb_dd;
     chi_u = chi_c; chi_c = chi_d; chi_d = chi_dd;
+    cb_u = cb_c; cb_c = cb_d; cb_d = cb_dd;
     dchi_c = dchi_dn;
     dtau_uw = dtau_dw;
     dS_up = dS_c;
@@ -326,16 +316,18 @@ __device__ void bezier_full(const Op& op, const R* ds, int nd, int to_obs, doubl
   double w[3];
   w3(dtau, w);
   const R dS_uw = -(S_c - S_u) / R(dtau);
-  I[k] = (R(1) - R(w[0])) * I_upw + R(w[0]) * S_c + R(w[1]) * dS_uw;
-  Psi[k] = R(w[0] - w[1] / dtau);
-  Ieff[k] = (R(1) - R(w[0])) * I_upw + R(w[0]) * Sb_c + R(w[1]) * ((S_u - Sb_c) / R(dtau));
+  const R I_last = (R(1) - R(w[0])) * I_upw + R(w[0]) * S_c + R(w[1]) * dS_uw;
+  const R Ieff_last =
+      (R(1) - R(w[0])) * I_upw + R(w[0]) * Sb_c + R(w[1]) * ((S_u - Sb_c) / R(dtau));
+  emit(k, I_last, R(w[0] - w[1] / dtau), R((1.0 - w[0]) + w[1] / dtau), Ieff_last, chi_c, cb_c);
+  return I_last;
 }
-
-// Feautrier (feautrier.c:56-202) with P and Psi at every depth; chi and S
-// are stored in I/Psi first and overwritten.
+// Feautrier (feautrier.c:56-202) with P, Psi and 1 - Psi at every depth.
+// P may share storage with S, Psi with F and omPsi with zt: each is written
+// only after the last read of the array it shares.
 template <typename R>
 __device__ R feautrier_full(const R* chi, const R* S, const R* ds, int nd, double muz,
-                            double B0, double B1, R* P, R* Psi, R* F, R* zt) {
+                            double B0, double B1, R* P, R* Psi, R* omPsi, R* F, R* zt) {
   // dtau[k] = 0.5 (chi[k] + chi[k+1]) ds[k+1] for k = 0..nd-2 (ds already / mu)
   auto dtau = [&](int kk) { return R(0.5) * (chi[kk] + chi[kk + 1]) * ds[kk + 1]; };
   const R hN = R(B1 - (B0 - B1) / (double)dtau(nd - 2));
@@ -354,8 +346,14 @@ __device__ R feautrier_full(const R* chi, const R* S, const R* ds, int nd, doubl
   const R abcN = R(1) + R(2) / dN, A1N = R(2) / (dN * dN), StN = S[nd - 1] + R(2) * hN / dN;
   R Pk = (StN + A1N * zt[nd - 2]) / (abcN + A1N * (F[nd - 2] / (R(1) + F[nd - 2])));
   // Psi by the upward G recurrence needs F[k-1]; compute P and Psi together
+  // 1 - Psi = (denominator - 1) Psi, formed from the positive terms of the
+  // denominator without cancellation
   R G = abcN / A1N;
-  Psi[nd - 1] = R(1) / (abcN + A1N * F[nd - 2] / (R(1) + F[nd - 2]));
+  {
+    const R rest = R(2) / dN + A1N * F[nd - 2] / (R(1) + F[nd - 2]);
+    Psi[nd - 1] = R(1) / (R(1) + rest);
+    omPsi[nd - 1] = rest * Psi[nd - 1];
+  }
   P[nd - 1] = Pk;
   for (int k = nd - 2; k >= 0; --k) {
     Pk = Pk / (R(1) + F[k]) + zt[k];
@@ -364,17 +362,18 @@ __device__ R feautrier_full(const R* chi, const R* S, const R* ds, int nd, doubl
   for (int k = nd - 2; k >= 1; --k) {
     const R dm = dtau(k - 1), dp = dtau(k), dmid = R(0.5) * (dp + dm);
     const R A1 = R(1) / (dmid * dm), C1 = R(1) / (dmid * dp);
-    Psi[k] = R(1) / (R(1) + A1 * F[k - 1] / (R(1) + F[k - 1]) + C1 * G / (R(1) + G));
+    const R rest = A1 * F[k - 1] / (R(1) + F[k - 1]) + C1 * G / (R(1) + G);
+    Psi[k] = R(1) / (R(1) + rest);
+    omPsi[k] = rest * Psi[k];
     G = (R(1) + C1 * G / (R(1) + G)) / A1;
   }
-  Psi[0] = R(1) / (abc0 + C10 * G / (R(1) + G));
+  {
+    const R rest = R(2) / d0 + C10 * G / (R(1) + G);
+    Psi[0] = R(1) / (R(1) + rest);
+    omPsi[0] = rest * Psi[0];
+  }
   (void)muz;
   return R(2) * P[0];
-}
-
-// Row of Gamma entry (i, j), i != j, in the off-diagonal arrays Gs / Gl.
-__host__ __device__ inline int gamma_slot(int i, int j, int nlev) {
-  return i * (nlev - 1) + j - (j > i ? 1 : 0);
 }
 
 template <typename R>
@@ -386,32 +385,156 @@ __host__ __device__ inline size_t formal_smem_layout(int nlev, int nd, int nrays
     off += ((sizeof(R) * count + 15) / 16) * 16;
     return p;
   };
-  const bool comp = sizeof(R) == 4;
-  // Gamma: the off-diagonal entries only (transitions are between different
-  // levels), addressed by gamma_slot; J without compensation terms (it sums
-  // at most 2 * PYRH_NLTE_MAX_RAYS terms per entry)
-  R* Gs = take((size_t)nlev * (nlev - 1) * nd);
-  R* Gl = take(comp ? (size_t)nlev * (nlev - 1) * nd : 0);
-  R* Js = take((size_t)nd * 32);
   R* n = take((size_t)nlev * nd);
   R* lnst = take((size_t)nlev * nd);
   R* iT = take((size_t)nd);
   R* ds = take((size_t)nrays * nd);
   R* wphi = take((size_t)(nline > 0 ? nline : 1) * nd);
-  if (sh) *sh = NlteShared<R>{Gs, Gl, Js, n, lnst, iT, ds, wphi};
+  if (sh) *sh = NlteShared<R>{n, lnst, iT, ds, wphi};
   return off;
 }
 
+// Wavelength tiles (warps) per block of the formal kernel.
+constexpr int kFormalWarps = 4;
+
+// Where one warp's rate and J contributions go: the warp is the only writer
+// of its tile's rate partial sums and of its 32 wavelengths' new J, and adds
+// to them in program order, so every sum has a fixed order and the solve is
+// bit-reproducible.
+struct TileSink {
+  double* gslab;      // this tile's partial sums: slot * total_depth + doff + k
+  double* Jn;         // new J of this lane's wavelength, depth stride ns
+  int64_t total_depth, doff;
+  int ns;
+};
+
+// Rate (fillgamma.c:82-332) and J (formal.c:247-256) contributions of one
+// depth of one ray direction, summed over the warp's 32 wavelengths.  All
+// lanes of the warp call it together; lanes with mine == false add nothing.
 template <typename R>
-__global__ void __launch_bounds__(256)
-nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_out) {
+__device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_transition* tr,
+                                          const ActiveSet<R>& as, const NlteShared<R>& sh,
+                                          const TileSink& out, int nd, int nlev, int q, int k,
+                                          bool mine, R wdir, R I_k, R Psi_k, R omp, R Ieff_k,
+                                          R chi_k, R chi_bg) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  if (mine) atomicAdd(out.Jn + (int64_t)k * out.ns, (double)(wdir * I_k));
+  const int nact = mine ? as.n : 0;
+  const int nm = __reduce_max_sync(full, nact);
+  if (nm == 0) return;
+  const R psi = mine ? Psi_k / chi_k : R(0);
+  const R ichi = mine ? R(1) / chi_k : R(0);
+  // per transition: V W (product formed without the h c / 4 pi that cancels
+  // in it), U = TW G V, the stimulated-emission factor G and the
+  // transition's own opacity X
+  R VW[PYRH_NLTE_MAX_ACTIVE], U[PYRH_NLTE_MAX_ACTIVE], G[PYRH_NLTE_MAX_ACTIVE],
+      X[PYRH_NLTE_MAX_ACTIVE];
+  for (int m = 0; m < nact; ++m) {
+    const pyrh_nlte_transition& t = tr[as.t[m]];
+    const R ni = sh.n[t.i * nd + k], nj = sh.n[t.j * nd + k];
+    if (t.type == 0) {
+      const int64_t pi = t.phi_off + ((int64_t)k * 2 * A.nrays + q) * t.nlambda + as.la[m];
+      const R phv = pi < A.phi_cap ? static_cast<const R*>(A.phi)[pi] : R(0);
+      const R vph = as.vb[m] * phv;
+      const R V = R(kHPLANCK * kCLIGHT / (4.0 * kPI)) * vph;
+      G[m] = as.gl[m];
+      VW[m] = vph * (as.wl[m] * sh.wphi[t.line_index * nd + k]);
+      U[m] = (as.tw[m] * G[m]) * V;
+      X[m] = V * (ni - G[m] * nj);
+    } else {
+      G[m] = dev_exp(sh.lnst[t.i * nd + k] - sh.lnst[t.j * nd + k] - as.hckl * sh.iT[k]);
+      VW[m] = as.vb[m] * as.wl[m];
+      U[m] = (as.tw[m] * G[m]) * as.vb[m];
+      X[m] = as.vb[m] * (ni - G[m] * nj);
+    }
+  }
+  for (int m = 0; m < nm; ++m) {
+    int key = -1;
+    R gij = 0, gji = 0;
+    if (m < nact) {
+      const pyrh_nlte_transition& t = tr[as.t[m]];
+      const int i = t.i, j = t.j;
+      key = i * nlev + j;
+      // cross-coupling sums over the active set (addtoCoupling), with the
+      // transition's own terms kept apart: chi_up_o and U_down_o leave out
+      // transition m, X_o is the opacity of everything but m (background
+      // and the other transitions)
+      R chi_up_o = 0, chi_down_j = 0, U_down_o = 0, U_down_i = 0, X_o = chi_bg, chi_self = 0;
+      int cnt = 0;
+      for (int qq = 0; qq < nact; ++qq) {
+        const pyrh_nlte_transition& u = tr[as.t[qq]];
+        const R chicc = VW[qq] * (sh.n[u.i * nd + k] - G[qq] * sh.n[u.j * nd + k]);
+        if (qq == m) chi_self = chicc;
+        else X_o += X[qq];
+        if (u.i == i && qq != m) chi_up_o += chicc;
+        if (u.j == j) {
+          chi_down_j += chicc;
+          if (qq != m) U_down_o += U[qq];
+        }
+        if (u.j == i) { U_down_i += U[qq]; ++cnt; }
+      }
+      const R wlamu = VW[m] * wdir;
+      gji = Ieff_k * wlamu;
+      // fillgamma.c:185-196: (2 h nu^3 / c^2 + Ieff) g V W - chi_up Psi U_down.
+      // The transition's own part of the coupling product,
+      // 2 h nu^3 / c^2 g V W X_m Psi / chi, cancels the spontaneous term to
+      // within the escape fraction 1 - X_m Psi / chi in optically thick
+      // cores; that fraction is formed as X_o / chi + (X_m / chi)(1 - Psi)
+      // from positive terms, and only the products with the other
+      // transitions stay in the coupling term.
+      const R esc = X_o * ichi + (X[m] * ichi) * omp;
+      gij = (Ieff_k + as.tw[m] * esc) * G[m] * wlamu -
+            (chi_self * U_down_o + chi_up_o * (U[m] + U_down_o)) * (psi * wdir);
+      // one term per active transition whose upper level is i
+      if (cnt) gji += R(cnt) * chi_down_j * (psi * U_down_i) * wdir;
+    }
+    // Sum over the lanes that add to the same entry, in an order fixed by
+    // the lane numbers, then one addition by the group's first lane.
+    const unsigned peers = __match_any_sync(full, key);
+    double sij, sji;
+    if (peers == full) {
+      if (key < 0) continue;
+      for (int o = 16; o > 0; o >>= 1) {
+        gij += __shfl_xor_sync(full, gij, o);
+        gji += __shfl_xor_sync(full, gji, o);
+      }
+      sij = (double)gij;
+      sji = (double)gji;
+    } else {
+      const int cnt = key >= 0 ? __popc(peers) : 0;
+      const int maxc = __reduce_max_sync(full, cnt);
+      unsigned rem = key >= 0 ? peers : 0u;
+      sij = 0.0;
+      sji = 0.0;
+      for (int s = 0; s < maxc; ++s) {
+        const int src = rem ? __ffs(rem) - 1 : lane;
+        const R a = __shfl_sync(full, gij, src), c = __shfl_sync(full, gji, src);
+        if (rem) {
+          sij += (double)a;
+          sji += (double)c;
+          rem &= rem - 1;
+        }
+      }
+      if (key < 0 || lane != __ffs(peers) - 1) continue;
+    }
+    if (lane != 0 && peers == full) continue;
+    const int i = key / nlev, j = key % nlev;
+    atomicAdd(out.gslab + (int64_t)gamma_slot(i, j, nlev) * out.total_depth + out.doff + k, sij);
+    atomicAdd(out.gslab + (int64_t)gamma_slot(j, i, nlev) * out.total_depth + out.doff + k, sji);
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(32 * kFormalWarps)
+nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const pyrh_nlte_batch& b = A.b;
   const int p = blockIdx.y;
   if (!emergent_only && !A.active[p]) return;
   const int nd = b.ndep[p], ns = b.nspect[p], nlev = b.nlevel, nt = b.ntrans[p];
-  const int la0 = blockIdx.x * 32;
-  if (la0 >= ns) return;
+  const int tile0 = blockIdx.x * kFormalWarps;
+  if (tile0 * 32 >= ns) return;
   if (nd < 3 || nd > b.max_ndep || nd > PYRH_NLTE_MAX_DEPTH) {   // uniform per block
     if (threadIdx.x == 0) atomicOr(A.err, 2);
     return;
@@ -422,14 +545,6 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
   NlteShared<R> sh;
   formal_smem_layout<R>(nlev, b.max_ndep, A.nrays, b.max_nline, &sh, smem_raw);
   const int nthr = blockDim.x;
-  const bool comp = sizeof(R) == 4;
-  for (int e = threadIdx.x; e < nlev * (nlev - 1) * nd; e += nthr) {
-    sh.Gs[e] = R(0);
-    if (comp) sh.Gl[e] = R(0);
-  }
-  for (int e = threadIdx.x; e < nd * 32; e += nthr) {
-    sh.Js[e] = R(0);
-  }
   for (int e = threadIdx.x; e < nlev * nd; e += nthr) {
     const int i = e / nd, k = e % nd;
     sh.n[e] = R(b.n[(int64_t)i * b.total_depth + doff + k]);
@@ -446,168 +561,98 @@ nlte_formal_kernel(NlteArgs A, int eval_operator, int emergent_only, double* I_o
     sh.wphi[e] = R(A.wphi[b.adamp_off[p] + e]);
   __syncthreads();
 
-  const int lane = threadIdx.x & 31, ray = threadIdx.x >> 5;
-  const int la = la0 + lane;
-  const bool live = (la < ns) && (ray < A.nrays);
-  // A warp is 32 wavelengths of one ray.  Where all its lanes are live they
-  // run the depth and transition loops in step and sum each Gamma
-  // contribution over the warp with a shuffle tree before one shared-memory
-  // addition (lanes almost always share their transitions); elsewhere every
-  // lane adds its own.
+  const int lane = threadIdx.x & 31, tile = tile0 + (threadIdx.x >> 5);
+  if (tile * 32 >= ns) return;   // uniform per warp; no block barrier follows
   const unsigned full = 0xffffffffu;
-  const bool coll = __ballot_sync(full, live) == full;
-  if (live) {
-    const double muz = A.muz[ray];
+  // lanes past the end of the spectrum run the recurrences of the last
+  // wavelength in step with the others and add nothing
+  const int la_raw = tile * 32 + lane;
+  const bool live = la_raw < ns;
+  const int la = live ? la_raw : ns - 1;
+  const double lam = lamp[la];
+  ActiveSet<R> as;
+  as.n = 0;
+  as.bb = false;
+  as.hckl = R((kHPLANCK * kCLIGHT / (kKBOLTZMANN * kNM_TO_M)) / lam);
+  for (int pass = 1; pass >= 0; --pass)       // continua (type 1) first, then lines
+    for (int t = 0; t < nt; ++t) {
+      const pyrh_nlte_transition& T = tr[t];
+      if (T.type != pass) continue;
+      if (la >= T.nblue && la < T.nblue + T.nlambda && as.n < PYRH_NLTE_MAX_ACTIVE) {
+        const int m = as.n++;
+        as.t[m] = t;
+        as.la[m] = la - T.nblue;
+        if (T.type == 0) {
+          as.bb = true;
+          as.vb[m] = R(T.Bij * T.isotope_frac);
+          as.gl[m] = R(T.Bji / T.Bij);
+          as.tw[m] = R(T.Aji / T.Bji);
+          as.wl[m] = R(wlambda_line(lamp + T.nblue, T, as.la[m]));
+        } else {
+          as.vb[m] = R(b.alpha[T.alpha_off + as.la[m]]);
+          as.gl[m] = R(0);
+          as.tw[m] = R(2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M) /
+                       (lam * lam * lam));
+          as.wl[m] = R(4.0 * kPI / kHPLANCK * (wlambda_cont(lamp + T.nblue, T, as.la[m]) / lam));
+        }
+      }
+    }
+  const double B0 = planck(b.T[doff + nd - 2], lam), B1 = planck(b.T[doff + nd - 1], lam);
+  const JRow Jold{b.J + coff + la, ns};
+  // angle-dependent wavelengths (formal.c:96-101) take the Bezier3 solution
+  // in both directions, the others Feautrier once per ray
+  const bool angle_dep = A.moving && (as.bb || b.bgline[b.lam_off[p] + la]);
+  const bool bez = live && angle_dep, feau = live && !angle_dep;
+  const bool any_bez = __any_sync(full, bez), any_feau = __any_sync(full, feau);
+  NlteOpacity<R> op;
+  op.A = &A; op.tr = tr; op.as = &as; op.sh = &sh;
+  op.nd = nd; op.ns = ns; op.la = la; op.coff = coff;
+  TileSink out;
+  out.gslab = A.gslab + (int64_t)tile * nlev * (nlev - 1) * b.total_depth;
+  out.Jn = A.Jnew + coff + la;
+  out.total_depth = b.total_depth;
+  out.doff = doff;
+  out.ns = ns;
+  R emergent = R(0);
+  for (int ray = 0; ray < A.nrays; ++ray) {
     const R* dsl = sh.ds + ray * nd;
-    const double lam = lamp[la];
-    ActiveSet<R> as;
-    as.n = 0;
-    as.bb = false;
-    as.hckl = R((kHPLANCK * kCLIGHT / (kKBOLTZMANN * kNM_TO_M)) / lam);
-    for (int pass = 1; pass >= 0; --pass)       // continua (type 1) first, then lines
-      for (int t = 0; t < nt; ++t) {
-        const pyrh_nlte_transition& T = tr[t];
-        if (T.type != pass) continue;
-        if (la >= T.nblue && la < T.nblue + T.nlambda && as.n < PYRH_NLTE_MAX_ACTIVE) {
-          const int m = as.n++;
-          as.t[m] = t;
-          as.la[m] = la - T.nblue;
-          if (T.type == 0) {
-            as.bb = true;
-            as.vb[m] = R(T.Bij * T.isotope_frac);
-            as.gl[m] = R(T.Bji / T.Bij);
-            as.tw[m] = R(T.Aji / T.Bji);
-            as.wl[m] = R(wlambda_line(lamp + T.nblue, T, as.la[m]));
-          } else {
-            as.vb[m] = R(b.alpha[T.alpha_off + as.la[m]]);
-            as.gl[m] = R(0);
-            as.tw[m] = R(2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M) /
-                         (lam * lam * lam));
-            as.wl[m] = R(4.0 * kPI / kHPLANCK * (wlambda_cont(lamp + T.nblue, T, as.la[m]) / lam));
-          }
-        }
+    if (any_bez) {
+      for (int to_obs = emergent_only ? 1 : 0; to_obs <= 1; ++to_obs) {
+        op.q = 2 * ray + to_obs;
+        const R wdir = R(0.5 * A.wmu[ray]);
+        const int q = op.q;
+        auto emit = [&](int k, R I_k, R Psi_k, R omp, R Ieff_k, R chi_k, R chi_bg) {
+          if (!emergent_only)
+            add_rates<R>(A, tr, as, sh, out, nd, nlev, q, k, bez, wdir, I_k, Psi_k, omp, Ieff_k,
+                         chi_k, chi_bg);
+        };
+        const R Ie = bezier_sweep<R>(op, dsl, nd, to_obs, B0, B1, Jold, emit);
+        if (to_obs && bez) emergent = Ie;
       }
-    const double B0 = planck(b.T[doff + nd - 2], lam), B1 = planck(b.T[doff + nd - 1], lam);
-    const JRow Jold{b.J + coff + la, ns};
-    const bool angle_dep = A.moving && (as.bb || b.bgline[b.lam_off[p] + la]);
-    R I[PYRH_NLTE_MAX_DEPTH], Psi[PYRH_NLTE_MAX_DEPTH], Ieff[PYRH_NLTE_MAX_DEPTH],
-        chis[PYRH_NLTE_MAX_DEPTH];
-    NlteOpacity<R> op;
-    op.A = &A; op.tr = tr; op.as = &as; op.sh = &sh;
-    op.nd = nd; op.ns = ns; op.la = la; op.coff = coff;
-    const int ndir = angle_dep ? 2 : 1;
-    // in a collective warp every lane runs the largest direction count, the
-    // extra pass contributing nothing
-    const int ndir_loop = coll ? __reduce_max_sync(full, ndir) : ndir;
-    for (int dir = 0; dir < ndir_loop; ++dir) {
-      const bool mine = dir < ndir;
-      const int to_obs = angle_dep ? dir : 0;
-      op.q = 2 * ray + to_obs;
-      R wdir = R(0);
-      R emergent = R(0);
-      if (!mine) {
-      } else if (angle_dep) {
-        if (emergent_only && !to_obs) continue;
-        bezier_full<R>(op, dsl, nd, to_obs, B0, B1, Jold, I, Psi, Ieff, chis);
-        wdir = R(0.5 * A.wmu[ray]);
-        emergent = I[0];
-      } else {
-        R S[PYRH_NLTE_MAX_DEPTH];
-        for (int k = 0; k < nd; ++k) {
-          R ea;
-          op(k, chis[k], S[k], ea, Jold[k]);
-          Ieff[k] = ea;   // the atom's emissivity, for I - Psi eta below
-        }
-        R F[PYRH_NLTE_MAX_DEPTH], zt[PYRH_NLTE_MAX_DEPTH];
-        emergent = feautrier_full<R>(chis, S, dsl, nd, muz, B0, B1, I, Psi, F, zt);
-        wdir = R(A.wmu[ray]);
-      }
-      if (emergent_only) {
-        if (mine) I_out[b.lam_off[p] + la] = (double)emergent;
-        continue;
-      }
-      const int nact = mine ? as.n : 0;
-      const int nm = coll ? __reduce_max_sync(full, nact) : nact;
-      // Gamma, coupling and J at every depth (fillgamma.c:82-332, formal.c:247-256)
+    }
+    if (any_feau) {
+      // angle-independent: one Feautrier solution per ray (to_obs index 0)
+      op.q = 2 * ray;
+      // P overwrites S, Psi F and 1 - Psi zt (feautrier_full allows it)
+      R chis[PYRH_NLTE_MAX_DEPTH], S[PYRH_NLTE_MAX_DEPTH], F[PYRH_NLTE_MAX_DEPTH],
+          zt[PYRH_NLTE_MAX_DEPTH], eta[PYRH_NLTE_MAX_DEPTH], cbg[PYRH_NLTE_MAX_DEPTH];
       for (int k = 0; k < nd; ++k) {
-        if (mine) atomicAdd(&sh.Js[k * 32 + lane], wdir * I[k]);
-        if (!eval_operator) continue;
-        const R psi = mine ? Psi[k] / chis[k] : R(0);
-        const R Ieff_k = !mine ? R(0) : angle_dep ? Ieff[k] : I[k] - psi * Ieff[k];
-        // per transition: V W (product formed without the h c / 4 pi that
-        // cancels in it), U = TW G V and the stimulated-emission factor G
-        R VW[PYRH_NLTE_MAX_ACTIVE], U[PYRH_NLTE_MAX_ACTIVE], G[PYRH_NLTE_MAX_ACTIVE];
-        for (int m = 0; m < nact; ++m) {
-          const pyrh_nlte_transition& t = tr[as.t[m]];
-          if (t.type == 0) {
-            const int64_t pi =
-                t.phi_off + ((int64_t)k * 2 * A.nrays + op.q) * t.nlambda + as.la[m];
-            const R phv = pi < A.phi_cap ? static_cast<const R*>(A.phi)[pi] : R(0);
-            const R vph = as.vb[m] * phv;
-            G[m] = as.gl[m];
-            VW[m] = vph * (as.wl[m] * sh.wphi[t.line_index * nd + k]);
-            U[m] = (as.tw[m] * G[m]) * (R(kHPLANCK * kCLIGHT / (4.0 * kPI)) * vph);
-          } else {
-            G[m] = dev_exp(sh.lnst[t.i * nd + k] - sh.lnst[t.j * nd + k] - as.hckl * sh.iT[k]);
-            VW[m] = as.vb[m] * as.wl[m];
-            U[m] = (as.tw[m] * G[m]) * as.vb[m];
-          }
-        }
-        for (int m = 0; m < nm; ++m) {
-          int key = -1;
-          R gij = 0, gji = 0;
-          if (m < nact) {
-            const pyrh_nlte_transition& t = tr[as.t[m]];
-            const int i = t.i, j = t.j;
-            key = i * nlev + j;
-            // cross-coupling sums over the active set (addtoCoupling)
-            R chi_up_i = 0, chi_down_j = 0, U_down_j = 0, U_down_i = 0;
-            int cnt = 0;
-            for (int q = 0; q < nact; ++q) {
-              const pyrh_nlte_transition& u = tr[as.t[q]];
-              const R chicc = VW[q] * (sh.n[u.i * nd + k] - G[q] * sh.n[u.j * nd + k]);
-              if (u.i == i) chi_up_i += chicc;
-              if (u.j == j) { chi_down_j += chicc; U_down_j += U[q]; }
-              if (u.j == i) { U_down_i += U[q]; ++cnt; }
-            }
-            const R wlamu = VW[m] * wdir;
-            gji = Ieff_k * wlamu;
-            gij = (as.tw[m] + Ieff_k) * G[m] * wlamu - chi_up_i * (psi * U_down_j) * wdir;
-            // one term per active transition whose upper level is i
-            if (cnt) gji += R(cnt) * chi_down_j * (psi * U_down_i) * wdir;
-          }
-          // one match per lane and iteration, from this single site
-          const unsigned peers = coll ? __match_any_sync(full, key) : 0u;
-          if (peers == full && key >= 0) {   // the whole warp adds to one entry
-            for (int o = 16; o > 0; o >>= 1) {
-              gij += __shfl_xor_sync(full, gij, o);
-              gji += __shfl_xor_sync(full, gji, o);
-            }
-            if (lane != 0) continue;
-          }
-          if (key < 0) continue;
-          const int i = key / nlev, j = key % nlev;
-          const int sij = gamma_slot(i, j, nlev) * nd + k, sji = gamma_slot(j, i, nlev) * nd + k;
-          acc_add(&sh.Gs[sij], &sh.Gl[sij], gij);
-          acc_add(&sh.Gs[sji], &sh.Gl[sji], gji);
+        R Sb;
+        op(k, chis[k], S[k], Sb, cbg[k], eta[k], Jold[k]);
+      }
+      const R Ie = feautrier_full<R>(chis, S, dsl, nd, A.muz[ray], B0, B1, S, F, zt, F, zt);
+      if (feau) emergent = Ie;
+      if (!emergent_only) {
+        const R wdir = R(A.wmu[ray]);
+        for (int k = 0; k < nd; ++k) {
+          const R Ieff = S[k] - (F[k] / chis[k]) * eta[k];
+          add_rates<R>(A, tr, as, sh, out, nd, nlev, op.q, k, feau, wdir, S[k], F[k], zt[k],
+                       Ieff, chis[k], cbg[k]);
         }
       }
     }
   }
-  __syncthreads();
-  if (emergent_only) return;
-  for (int e = threadIdx.x; e < nd * 32; e += nthr) {
-    const int k = e / 32, l = e % 32;
-    if (la0 + l < ns)
-      A.Jnew[coff + (int64_t)k * ns + la0 + l] = (double)sh.Js[e];
-  }
-  if (eval_operator)
-    for (int e = threadIdx.x; e < nlev * (nlev - 1) * nd; e += nthr) {
-      const int s = e / nd, k = e % nd;
-      const int i = s / (nlev - 1), jj = s % (nlev - 1), j = jj + (jj >= i ? 1 : 0);
-      const double v = (double)sh.Gs[e] + (comp ? (double)sh.Gl[e] : 0.0);
-      if (v != 0.0) atomicAdd(&A.Gamma[(int64_t)(i * nlev + j) * b.total_depth + doff + k], v);
-    }
+  if (emergent_only && live) I_out[b.lam_off[p] + la] = (double)emergent;
 }
 
 // J <- new J for atmospheres still iterating (each wavelength replaces its
@@ -706,9 +751,18 @@ __global__ void nlte_stateq_kernel(NlteArgs A) {
     } else {
       ie = A.isum;
     }
+    // Gamma = C plus the rate sums of the atmosphere's wavelength tiles,
+    // added in tile order
+    const int ntile = (b.nspect[p] + 31) / 32, nslot = nl * (nl - 1);
     for (int i = 0; i < nl; ++i)
-      for (int j = 0; j < nl; ++j)
-        M[i * nl + j] = A.Gamma[(int64_t)(i * nl + j) * b.total_depth + doff + k];
+      for (int j = 0; j < nl; ++j) {
+        double g = b.C[(int64_t)(i * nl + j) * b.total_depth + doff + k];
+        if (i != j) {
+          const double* sl = A.gslab + (int64_t)gamma_slot(i, j, nl) * b.total_depth + doff + k;
+          for (int t = 0; t < ntile; ++t) g += sl[(int64_t)t * nslot * b.total_depth];
+        }
+        M[i * nl + j] = g;
+      }
     for (int i = 0; i < nl; ++i) {
       double d = 0.0;
       M[i * nl + i] = 0.0;
@@ -841,6 +895,7 @@ __global__ void nlte_ng_kernel(NlteArgs A, int init) {
     A.iters[p] += 1;
     A.dpops[p] = dm;
     if (dm < A.iter_limit || A.iters[p] >= A.nmax_iter) A.active[p] = 0;
+    else atomicOr(A.any, 1);
   }
 }
 
@@ -876,15 +931,15 @@ cudaError_t nlte_launch_profiles(const NlteArgs& A, int natm, int64_t max_elems,
 
 template <typename R>
 static cudaError_t launch_formal_t(const NlteArgs& A, int natm, int max_nspect, int maxd,
-                                   int eval_operator, int emergent_only, double* I_out,
-                                   cudaStream_t st) {
+                                   int emergent_only, double* I_out, cudaStream_t st) {
   const size_t smem = nlte_formal_smem(A.b.nlevel, maxd, A.nrays, A.b.max_nline,
                                        sizeof(R) == 4 ? PYRH_FP32 : PYRH_FP64);
   cudaError_t e = cudaFuncSetAttribute(nlte_formal_kernel<R>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  dim3 g((max_nspect + 31) / 32, natm);
-  nlte_formal_kernel<R><<<g, 32 * A.nrays, smem, st>>>(A, eval_operator, emergent_only, I_out);
+  const int ntile = (max_nspect + 31) / 32;
+  dim3 g((ntile + kFormalWarps - 1) / kFormalWarps, natm);
+  nlte_formal_kernel<R><<<g, 32 * kFormalWarps, smem, st>>>(A, emergent_only, I_out);
   return cudaGetLastError();
 }
 
@@ -895,8 +950,8 @@ cudaError_t nlte_launch_iteration(const NlteArgs& A, int natm, int max_nspect, i
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   e = precision == PYRH_FP32
-          ? launch_formal_t<float>(A, natm, max_nspect, maxd, 1, 0, nullptr, st)
-          : launch_formal_t<double>(A, natm, max_nspect, maxd, 1, 0, nullptr, st);
+          ? launch_formal_t<float>(A, natm, max_nspect, maxd, 0, nullptr, st)
+          : launch_formal_t<double>(A, natm, max_nspect, maxd, 0, nullptr, st);
   if (e != cudaSuccess) return e;
   nlte_jcopy_kernel<<<gi, 256, 0, st>>>(A);
   e = cudaGetLastError();
@@ -917,8 +972,8 @@ cudaError_t nlte_launch_ng_init(const NlteArgs& A, int natm, cudaStream_t st) {
 cudaError_t nlte_launch_emergent(const NlteArgs& A, int natm, int max_nspect, int maxd,
                                  int precision, double* I_out, cudaStream_t st) {
   return precision == PYRH_FP32
-             ? launch_formal_t<float>(A, natm, max_nspect, maxd, 0, 1, I_out, st)
-             : launch_formal_t<double>(A, natm, max_nspect, maxd, 0, 1, I_out, st);
+             ? launch_formal_t<float>(A, natm, max_nspect, maxd, 1, I_out, st)
+             : launch_formal_t<double>(A, natm, max_nspect, maxd, 1, I_out, st);
 }
 
 }  // namespace pyrh

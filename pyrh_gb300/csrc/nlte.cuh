@@ -17,8 +17,9 @@ struct NlteArgs {
   // workspace
   void *phi;
   int64_t phi_cap;                // elements of phi
-  double *wphi, *Jnew, *Gamma, *ngprev, *dpops;
+  double *wphi, *Jnew, *gslab, *ngprev, *dpops;   // gslab: per-tile rate sums
   int32_t *count, *active, *iters, *err;
+  int32_t *any;                   // set by nlte_ng_kernel while an atmosphere iterates
 };
 
 size_t nlte_formal_smem(int nlevel, int maxd, int nrays, int max_nline, int precision);

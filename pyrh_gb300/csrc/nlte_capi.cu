@@ -2,7 +2,6 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 
-#include <mutex>
 #include <vector>
 
 #include "../../include/pyrh_gb300.h"
@@ -18,7 +17,7 @@ namespace {
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct Layout {
-  size_t wphi, Jnew, Gamma, ngprev, count, active, iters, err, dpops, phi, fixed;
+  size_t wphi, Jnew, gslab, ngprev, count, active, iters, err, any, dpops, phi, fixed;
 };
 
 Layout layout(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg) {
@@ -27,12 +26,15 @@ Layout layout(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg) {
   const int nlev = b->nlevel, natm = b->natm;
   L.wphi = off; off = align256(off + sizeof(double) * (size_t)(b->max_nline > 0 ? b->max_nline : 1) * b->total_depth);
   L.Jnew = off; off = align256(off + sizeof(double) * (size_t)b->total_cont);
-  L.Gamma = off; off = align256(off + sizeof(double) * (size_t)nlev * nlev * b->total_depth);
+  // rate sums per (wavelength tile of 32, off-diagonal entry, depth)
+  const size_t ntile = (size_t)(b->max_nspect + 31) / 32;
+  L.gslab = off; off = align256(off + sizeof(double) * ntile * nlev * (nlev - 1) * b->total_depth);
   L.ngprev = off; off = align256(off + sizeof(double) * (size_t)(cfg->ng_order + 2) * nlev * b->total_depth);
   L.count = off; off = align256(off + sizeof(int32_t) * natm);
   L.active = off; off = align256(off + sizeof(int32_t) * natm);
   L.iters = off; off = align256(off + sizeof(int32_t) * natm);
   L.err = off; off = align256(off + sizeof(int32_t));
+  L.any = off; off = align256(off + sizeof(int32_t));
   L.dpops = off; off = align256(off + sizeof(double) * natm);
   L.phi = off;
   L.fixed = off;
@@ -93,17 +95,45 @@ pyrh::NlteArgs make_args(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg, 
   char* w = static_cast<char*>(ws);
   A.wphi = reinterpret_cast<double*>(w + L.wphi);
   A.Jnew = reinterpret_cast<double*>(w + L.Jnew);
-  A.Gamma = reinterpret_cast<double*>(w + L.Gamma);
+  A.gslab = reinterpret_cast<double*>(w + L.gslab);
   A.ngprev = reinterpret_cast<double*>(w + L.ngprev);
   A.count = reinterpret_cast<int32_t*>(w + L.count);
   A.active = reinterpret_cast<int32_t*>(w + L.active);
   A.iters = reinterpret_cast<int32_t*>(w + L.iters);
   A.err = reinterpret_cast<int32_t*>(w + L.err);
+  A.any = reinterpret_cast<int32_t*>(w + L.any);
   A.dpops = reinterpret_cast<double*>(w + L.dpops);
   A.phi = w + L.phi;
   const size_t r = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
   A.phi_cap = (int64_t)((ws_bytes - L.phi) / r);
   return A;
+}
+
+// Iterations launched back to back before the host looks at the device's
+// "an atmosphere is still iterating" flag.  Each atmosphere's convergence
+// test runs on the device (nlte_ng_kernel) and converged atmospheres skip
+// the later launches, so at most kChunk - 1 launches of empty iterations
+// follow the last atmosphere's convergence.
+constexpr int kChunk = 4;
+
+cudaError_t iterate(const pyrh::NlteArgs& A, const pyrh_nlte_batch* b,
+                    const pyrh_nlte_config* cfg, cudaStream_t st, int* launches) {
+  cudaError_t e = cudaSuccess;
+  for (int it = 0; e == cudaSuccess && it < cfg->nmax_iter;) {
+    const int n = cfg->nmax_iter - it < kChunk ? cfg->nmax_iter - it : kChunk;
+    for (int c = 0; c < n && e == cudaSuccess; ++c) {
+      e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision,
+                                      st);
+      *launches += 5;
+    }
+    it += n;
+    int32_t any = 0;
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&any, A.any, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (!any) break;
+  }
+  return e;
 }
 
 }  // namespace
@@ -141,19 +171,7 @@ pyrh_status pyrh_nlte_solve(const pyrh_nlte_batch* b, const pyrh_nlte_config* cf
   const int64_t max_elems = (int64_t)b->max_nspect * 2 * cfg->nrays * b->max_ndep;
   if (e == cudaSuccess)
     e = pyrh::nlte_launch_profiles(A, b->natm, max_elems, cfg->precision, st), launches += 2;
-  std::vector<int32_t> active(b->natm, 1);
-  int it = 0;
-  for (; e == cudaSuccess && it < cfg->nmax_iter; ++it) {
-    e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision, st);
-    launches += 5;
-    if (e != cudaSuccess) break;
-    e = cudaMemcpyAsync(active.data(), A.active, sizeof(int32_t) * b->natm,
-                        cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    bool any = false;
-    for (int p = 0; p < b->natm; ++p) any |= active[p] != 0;
-    if (!any) { ++it; break; }
-  }
+  if (e == cudaSuccess) e = iterate(A, b, cfg, st, &launches);
   int32_t err = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&err, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && iterations)
@@ -244,28 +262,19 @@ static __device__ __align__(256) unsigned char g_nlte_static_scratch[PYRH_NLTE_S
 
 namespace {
 
-constexpr int kMaxDevices = 64;
 constexpr int kMaxStaticAtm = 256;
-void* g_static_ptr[kMaxDevices] = {nullptr};
-std::mutex g_static_mu;
 
-// Device address of the static scratch on the current device.  The first
-// call on each device looks the symbol up (with that device current); the
-// host-side name of the array is not a device address and is never passed
-// to a kernel.
+// Device address of the static scratch in the current context, looked up
+// with cudaGetSymbolAddress on every call (with the caller's device
+// current) and never cached: after cudaDeviceReset, or with another context
+// current on the same device, the module and its array may sit at another
+// address.  The host-side name of the array is not a device address and is
+// never passed to a kernel.
 cudaError_t static_scratch(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_nlte_static_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_static_mu);
-  if (!g_static_ptr[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_nlte_static_scratch);
-    if (e != cudaSuccess) return e;
-    g_static_ptr[dev] = p;
-  }
-  *out = g_static_ptr[dev];
+  *out = p;
   return cudaSuccess;
 }
 
@@ -315,17 +324,7 @@ extern "C" pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch* b,
   const int64_t max_elems = (int64_t)b->max_nspect * 2 * cfg->nrays * b->max_ndep;
   if (e == cudaSuccess)
     e = pyrh::nlte_launch_profiles(A, b->natm, max_elems, cfg->precision, st), launches += 2;
-  int32_t active[kMaxStaticAtm];
-  for (int it = 0; e == cudaSuccess && it < cfg->nmax_iter; ++it) {
-    e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision, st);
-    launches += 5;
-    if (e != cudaSuccess) break;
-    e = cudaMemcpyAsync(active, A.active, sizeof(int32_t) * b->natm, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    bool any = false;
-    for (int p = 0; p < b->natm; ++p) any |= active[p] != 0;
-    if (!any) break;
-  }
+  if (e == cudaSuccess) e = iterate(A, b, cfg, st, &launches);
   int32_t err = 0;
   double dp[kMaxStaticAtm];
   if (e == cudaSuccess) e = cudaMemcpyAsync(&err, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
