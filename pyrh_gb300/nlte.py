@@ -232,3 +232,47 @@ class DeviceNlte:
             o, ns = int(self.pk.arrays["lam_off"][p]), int(self.pk.arrays["nspect"][p])
             out.append(I[o:o + ns])
         return out
+
+
+class PyrhNlteSetupBatch(C.Structure):
+    _fields_ = [("total_depth", C.c_int64)] + \
+        [(n, C.c_void_p) for n in ("T", "ne", "ntotal", "vturb", "nh0", "np", "nstar", "C",
+                                   "vbroad")]
+
+
+def device_setup(atom, weight_amu: float, T, ne, ntotal, vturb, nh0=None, np_=None,
+                 device="cuda", stream_ptr: int = 0):
+    """LTE populations [nlevel, nd], collision rates [nlevel^2, nd] and
+    Doppler widths [nd] of one model atom (pyrh_gb300.grid.read_atom) at the
+    depth points given (SI arrays, any number of atmospheres concatenated),
+    computed on the device by pyrh_nlte_setup."""
+    import torch
+    from . import grid as G
+    lib = _lib()
+    lib.pyrh_nlte_setup_workspace_bytes.restype = C.c_size_t
+    lib.pyrh_nlte_setup_workspace_bytes.argtypes = [C.POINTER(G.Atom)]
+    lib.pyrh_nlte_setup.restype = C.c_int
+    lib.pyrh_nlte_setup.argtypes = [C.POINTER(G.Atom), C.c_double,
+                                    C.POINTER(PyrhNlteSetupBatch), C.c_void_p, C.c_size_t,
+                                    C.c_void_p]
+    f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a, np.float64), device=device)
+    ins = {"T": f64(T), "ne": f64(ne), "ntotal": f64(ntotal), "vturb": f64(vturb)}
+    if nh0 is not None:
+        ins["nh0"] = f64(nh0)
+    if np_ is not None:
+        ins["np"] = f64(np_)
+    nd = ins["T"].numel()
+    nl = atom.nlevel
+    out = {"nstar": torch.empty(nl * nd, dtype=torch.float64, device=device),
+           "C": torch.empty(nl * nl * nd, dtype=torch.float64, device=device),
+           "vbroad": torch.empty(nd, dtype=torch.float64, device=device)}
+    b = PyrhNlteSetupBatch()
+    b.total_depth = nd
+    for k, v in list(ins.items()) + list(out.items()):
+        setattr(b, k, v.data_ptr())
+    wsb = lib.pyrh_nlte_setup_workspace_bytes(C.byref(atom))
+    ws = torch.empty(wsb, dtype=torch.uint8, device=device)
+    L.check(lib.pyrh_nlte_setup(C.byref(atom), float(weight_amu), C.byref(b), ws.data_ptr(),
+                                wsb, stream_ptr))
+    return (out["nstar"].view(nl, nd).cpu().numpy(), out["C"].view(nl * nl, nd).cpu().numpy(),
+            out["vbroad"].cpu().numpy())

@@ -298,3 +298,166 @@ def caii_like_atom(seed: int = 11, nlambda_scale: float = 1.0) -> str:
     out.append("")
     out.append(" END")
     return "\n".join(out) + "\n"
+
+
+# ------------------------------------------------------------------------
+# Batched uneven NLTE workload: atmospheres derived from NLTE set-ups that
+# the reference produced (its own background, LTE populations, collision
+# rates, damping and continuum cross-sections for the six-level atom), each
+# re-gridded to its own depth count (uniform in 50..150) and wavelength
+# count (uniform in 700..1100), with the temperature and velocity
+# perturbations of the batched LTE workload.  The temperature moves the
+# set-up consistently to first order: LTE populations by Saha-Boltzmann at
+# fixed n_e and total population, upward collision rates by detailed balance
+# with the downward ones kept, thermal continuum emissivity by the Planck
+# function, Doppler widths by the thermal speed.  The oracle solves the same
+# inputs, so these atmospheres are parity cases in their own right.
+# ------------------------------------------------------------------------
+
+NLTE_DEPTH_LOG = ("T", "ne", "nHtot", "ntotal", "vbroad", "nstar", "n0", "adamp")
+NLTE_DEPTH_LIN = ("vel", "vturb", "height", "C", "wphi", "atm")
+NLTE_RESULTS = ("Gamma1", "J1", "n1", "n_final", "J_final", "I_out", "phi_sample",
+                "phi_sample_la", "J0")
+AMU = 1.6605402e-27
+CA_MASS = 40.08
+
+
+def _lin_weights(x0: np.ndarray, x: np.ndarray):
+    """Indices and weights of linear interpolation from the increasing grid
+    x0 onto x (clamped at the ends), shared by every row interpolated."""
+    j = np.clip(np.searchsorted(x0, x, side="right") - 1, 0, len(x0) - 2)
+    f = np.clip((x - x0[j]) / (x0[j + 1] - x0[j]), 0.0, 1.0)
+    return j, f
+
+
+def _interp_last(v: np.ndarray, jw, log: bool) -> np.ndarray:
+    """Interpolate v along its last axis with _lin_weights (in log for
+    positive quantities)."""
+    j, f = jw
+    a = np.asarray(v, np.float64)
+    if log:
+        a = np.log(np.maximum(a, 1e-300))
+    r = a[..., j] * (1.0 - f) + a[..., j + 1] * f
+    return np.ascontiguousarray(np.exp(r) if log else r)
+
+
+def nlte_regrid_depth(fx: dict, nd: int) -> dict:
+    """An NLTE set-up on nd depths, interpolated in depth index (logarithm of
+    the positive quantities); results of the source run are dropped."""
+    n0 = len(fx["T"])
+    jw = _lin_weights(np.arange(n0, dtype=np.float64), np.linspace(0, n0 - 1, nd))
+    out = {k: v for k, v in fx.items() if k not in NLTE_RESULTS}
+    for k in NLTE_DEPTH_LOG + NLTE_DEPTH_LIN:
+        out[k] = _interp_last(fx[k], jw, k in NLTE_DEPTH_LOG)
+    bg = np.asarray(fx["background"], np.float64)              # [3, nspect, ndep]
+    out["background"] = np.stack([_interp_last(bg[0], jw, True), _interp_last(bg[1], jw, True),
+                                  _interp_last(np.maximum(bg[2], 0.0), jw, False)])
+    m = np.array(fx["meta"]).copy()
+    m[1] = nd
+    out["meta"] = m
+    return out
+
+
+def nlte_regrid_lambda(fx: dict, ns: int) -> dict:
+    """The same set-up on ns spectrum points: the sorted wavelength grid
+    resampled in index, each transition's range mapped onto the new grid,
+    the background interpolated in wavelength and the continuum
+    cross-sections in wavelength along each edge."""
+    lam0 = np.asarray(fx["lambda"], np.float64)
+    n_old = len(lam0)
+    s = (ns - 1) / (n_old - 1)
+    xi = np.linspace(0.0, n_old - 1.0, ns)
+    lam = np.interp(xi, np.arange(n_old), lam0)
+    out = dict(fx)
+    out["lambda"] = lam
+
+    def span(nblue, nl):
+        lo = int(np.ceil(nblue * s - 1e-9))
+        hi = int(np.floor((nblue + nl - 1) * s + 1e-9))
+        return lo, max(hi - lo + 1, 3 if hi >= lo else 0)
+
+    lines = np.array(fx["lines"], np.float64).copy()
+    for r in lines:
+        lo, nl = span(int(r[7]), int(r[8]))
+        r[7], r[8] = lo, min(nl, ns - lo)
+    cont = np.array(fx["continua"], np.float64).copy()
+    alpha_old = np.asarray(fx["alpha"], np.float64)
+    alpha = []
+    off = 0
+    for r in cont:
+        nb, nl, ao = int(r[2]), int(r[3]), int(r[6])
+        lo, nl2 = span(nb, nl)
+        nl2 = min(nl2, ns - lo)
+        a_old = alpha_old[ao:ao + nl]
+        alpha.append(np.exp(np.interp(lam[lo:lo + nl2], lam0[nb:nb + nl], np.log(a_old))))
+        r[2], r[3], r[6] = lo, nl2, off
+        off += nl2
+    out["lines"], out["continua"] = lines, cont
+    out["alpha"] = np.concatenate(alpha) if alpha else np.zeros(1)
+    bg = np.asarray(fx["background"], np.float64)              # [3, nspect, ndep]
+    jw = _lin_weights(lam0, lam)
+    bgT = bg.transpose(0, 2, 1)                                # wavelength last
+    out["background"] = np.stack([_interp_last(bgT[0], jw, True), _interp_last(bgT[1], jw, True),
+                                  _interp_last(bgT[2], jw, False)]).transpose(0, 2, 1).copy()
+    idx = np.clip(np.rint(xi).astype(np.int64), 0, n_old - 1)
+    out["bgflags"] = np.asarray(fx["bgflags"])[idx]
+    m = np.array(fx["meta"]).copy()
+    m[0] = ns
+    out["meta"] = m
+    return out
+
+
+def nlte_perturb(fx: dict, dT: np.ndarray, vlos_kms: float) -> dict:
+    """Temperature offsets dT [ndep] and a line-of-sight velocity offset,
+    with the set-up moved along with T (see the section comment)."""
+    out = dict(fx)
+    T0 = np.asarray(fx["T"], np.float64)
+    T = np.maximum(T0 + dT, 2500.0)
+    out["T"] = T
+    atm = np.array(fx["atm"], np.float64).copy()
+    atm[1] = T
+    atm[3] = atm[3] + vlos_kms
+    out["atm"] = atm
+    out["vel"] = np.asarray(fx["vel"], np.float64) + vlos_kms * 1e3
+    vb2 = np.asarray(fx["vbroad"], np.float64) ** 2 + 2.0 * KBOLTZMANN * (T - T0) / (CA_MASS * AMU)
+    out["vbroad"] = np.sqrt(np.maximum(vb2, 1e4))
+    E = np.asarray(fx["E"], np.float64)[:, None]
+    stage = np.asarray(fx["stage"], np.float64)[:, None]
+    nst = np.asarray(fx["nstar"], np.float64)
+    lf = -E / KBOLTZMANN * (1.0 / T - 1.0 / T0)[None, :] + \
+        1.5 * (stage - stage.min()) * np.log(T / T0)[None, :]
+    w = nst * np.exp(lf - lf.max(axis=0, keepdims=True))
+    nstar = w * (nst.sum(axis=0) / w.sum(axis=0))[None, :]
+    out["nstar"] = nstar
+    out["n0"] = nstar.copy()
+    nl = nstar.shape[0]
+    C = np.array(fx["C"], np.float64).copy()
+    for i in range(nl):
+        for j in range(i + 1, nl):
+            C[j * nl + i] = C[i * nl + j] * nstar[j] / nstar[i]
+    out["C"] = C
+    bg = np.array(fx["background"], np.float64).copy()
+    lam = np.asarray(fx["lambda"], np.float64)
+    ratio = planck_lambda(T[None, :], lam[:, None]) / planck_lambda(T0[None, :], lam[:, None])
+    bg[1] *= ratio
+    out["background"] = bg
+    return out
+
+
+def nlte_batch(bases: list, natm: int, seed: int = 4096, depth_range=(50, 150),
+               lambda_range=(700, 1100)) -> list:
+    """natm NLTE atmospheres for the batched uneven workload: base set-up
+    drawn from `bases`, depth count uniform in depth_range, spectrum points
+    uniform in lambda_range, T nodes N(0, 300 K) at log tau -2, -0.8, 0
+    (natural spline, constant outside) and v_los uniform in [-3, 3] km/s."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(natm):
+        b = bases[int(rng.integers(len(bases)))]
+        nd = int(rng.integers(depth_range[0], depth_range[1] + 1))
+        ns = int(rng.integers(lambda_range[0], lambda_range[1] + 1))
+        fx = nlte_regrid_lambda(nlte_regrid_depth(b, nd), ns)
+        logtau = np.asarray(fx["atm"][0], np.float64)
+        dT = natural_spline(T_NODES, rng.normal(0.0, 300.0, len(T_NODES)), logtau)
+        out.append(nlte_perturb(fx, dT, float(rng.uniform(-3.0, 3.0))))
+    return out

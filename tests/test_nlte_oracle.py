@@ -50,3 +50,39 @@ def test_armstrong_voigt_limits():
         assert abs(O.voigt_armstrong(0.0, v) - np.exp(-v * v)) < 1e-12
     a, v = 0.01, 40.0
     assert abs(O.voigt_armstrong(a, v) / (a / (np.sqrt(np.pi) * v * v)) - 1) < 1e-3
+
+
+# ------------------------------------------- batched uneven NLTE workload --
+
+@pytest.mark.parametrize("name", CASES)
+def test_regrid_at_own_shape_keeps_the_reference_solution(golden, name):
+    """The workload's depth and wavelength re-gridding at the set-up's own
+    shape changes nothing: the oracle still converges to the reference's
+    populations after the reference's iteration count."""
+    from pyrh_gb300 import workload as W
+    fx = golden(name)
+    same = W.nlte_regrid_lambda(W.nlte_regrid_depth(fx, len(fx["T"])), len(fx["lambda"]))
+    n, _, it, _, _ = O.nlte_solve(same)
+    assert np.abs(n / fx["n_final"] - 1).max() < 1e-8
+    assert it == O.nlte_solve(fx)[2]
+
+
+def test_uneven_batch_shapes_and_convergence(golden):
+    """Atmospheres of the batched uneven workload have 50..150 depths and
+    700..1100 wavelengths, consistent transition ranges, and converge in the
+    oracle at the set-ups' convergence limit."""
+    from pyrh_gb300 import workload as W
+    bases = [golden(n) for n in CASES]
+    atms = W.nlte_batch(bases, 12, seed=7)
+    for a in atms:
+        nd, ns = len(a["T"]), len(a["lambda"])
+        assert 50 <= nd <= 150 and 700 <= ns <= 1100
+        assert np.all(np.diff(a["lambda"]) > 0)
+        for r in list(a["lines"]) + list(a["continua"]):
+            nb, nl = (int(r[7]), int(r[8])) if len(r) == 16 else (int(r[2]), int(r[3]))
+            assert nl >= 3 and 0 <= nb and nb + nl <= ns
+        assert a["background"].shape == (3, ns, nd) and a["C"].shape[1] == nd
+        assert np.all(a["nstar"] > 0) and np.all(np.isfinite(a["C"]))
+    for a in atms[:3]:
+        n, _, it, dp, _ = O.nlte_solve(a)
+        assert np.all(np.isfinite(n)) and dp[-1] < float(a["fmeta"][0])
