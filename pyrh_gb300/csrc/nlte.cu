@@ -20,11 +20,13 @@
 // computed once in FP64 and kept in the workspace in the formal-solution
 // precision.  The per-(wavelength, depth) opacity and rate contributions run
 // in the formal-solution precision.  A warp owns one tile of 32 wavelengths
-// of one atmosphere and runs every ray through it; its rate and J
-// contributions are summed over the tile's wavelengths with shuffles and
-// added in FP64 to sums that only this warp writes, in program order, and
-// the tiles' sums are added in tile order when the rate matrix is
-// assembled: every sum has a fixed order, so a solve is bit-reproducible.
+// of one atmosphere and runs the rays of its ray group through it; its rate
+// and J contributions are summed over the tile's wavelengths with shuffles
+// and added to sums that only this warp writes, in program order, and the
+// (tile, group) sums are added in a fixed order when the rate matrix and J
+// are assembled: every sum has a fixed order, so a solve is
+// bit-reproducible.  Background, J and these partial sums are kept in the
+// formal-solution precision.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -132,32 +134,54 @@ __global__ void nlte_wphi_kernel(NlteArgs A) {
   }
 }
 
-// Rate-matrix partial sums of a wavelength tile: the off-diagonal entries
-// (i, j), i != j, of the tile's 32 wavelengths x all rays, one FP64 value per
-// (tile, entry, depth) at ((tile * nslot + gamma_slot) * total_depth + depth).
+// Rate-matrix partial sums of a wavelength tile and ray group: the
+// off-diagonal entries (i, j), i != j, of the tile's 32 wavelengths and the
+// group's rays, one value per (tile, group, entry, depth) at
+// (((tile * ngroup + group) * nslot + gamma_slot) * total_depth + depth).
 __host__ __device__ inline int gamma_slot(int i, int j, int nlev) {
   return i * (nlev - 1) + j - (j > i ? 1 : 0);
 }
 
 // The new J = 0 and the tiles' rate partial sums = 0 for atmospheres still
 // iterating (Gamma = C is added back when statEquil assembles the matrix).
+template <typename R>
 __global__ void nlte_gamma_init_kernel(NlteArgs A) {
   const pyrh_nlte_batch& b = A.b;
   const int p = blockIdx.y;
   if (blockIdx.x == 0 && p == 0 && threadIdx.x == 0) *A.any = 0;   // nlte_ng_kernel sets it
   if (!A.active[p]) return;
   const int nd = b.ndep[p], nslot = b.nlevel * (b.nlevel - 1);
-  const int ntile = (b.nspect[p] + 31) / 32;
+  const int ntg = (b.nspect[p] + 31) / 32 * A.ngroup;   // (tile, ray group) pairs
   const int64_t doff = b.depth_off[p];
-  for (int e = threadIdx.x + blockIdx.x * blockDim.x; e < ntile * nslot * nd;
+  for (int e = threadIdx.x + blockIdx.x * blockDim.x; e < ntg * nslot * nd;
        e += blockDim.x * gridDim.x) {
     const int ts = e / nd, k = e % nd;
-    A.gslab[(int64_t)ts * b.total_depth + doff + k] = 0.0;
+    static_cast<R*>(A.gslab)[(int64_t)ts * b.total_depth + doff + k] = R(0);
   }
   const int64_t coff = b.cont_off[p], ncont = (int64_t)nd * b.nspect[p];
-  for (int64_t e = threadIdx.x + (int64_t)blockIdx.x * blockDim.x; e < ncont;
-       e += (int64_t)blockDim.x * gridDim.x)
-    A.Jnew[coff + e] = 0.0;
+  for (int g = 0; g < A.ngroup; ++g)
+    for (int64_t e = threadIdx.x + (int64_t)blockIdx.x * blockDim.x; e < ncont;
+         e += (int64_t)blockDim.x * gridDim.x)
+      static_cast<R*>(A.Jnew)[g * b.total_cont + coff + e] = R(0);
+}
+
+// Once per solve: the background and the starting J in the formal-solution
+// precision, so that the depth loops convert nothing (in FP32 mode a
+// conversion from or to double runs on the FP64 pipe, a small fraction of
+// the FP32 rate on this GPU).
+template <typename R>
+__global__ void nlte_prepare_kernel(NlteArgs A) {
+  const pyrh_nlte_batch& b = A.b;
+  const int64_t tc = b.total_cont;
+  R* bg = static_cast<R*>(A.bgr);
+  R* Jr = static_cast<R*>(A.Jr);
+  for (int64_t e = threadIdx.x + (int64_t)blockIdx.x * blockDim.x; e < tc;
+       e += (int64_t)blockDim.x * gridDim.x) {
+    bg[e] = R(b.chi_c[e]);
+    bg[tc + e] = R(b.eta_c[e]);
+    bg[2 * tc + e] = R(b.sca_c[e]);
+    Jr[e] = R(b.J[e]);
+  }
 }
 
 // ------------------------------------------------------------ formal -----
@@ -203,7 +227,7 @@ struct NlteOpacity {
   // function (eta_c + sca_c J) / chi, the background opacity chi_c and the
   // atom's emissivity at depth k (opacity.c:64-300 for the active atom).
   __device__ __forceinline__ void operator()(int k, R& chi, R& S, R& S_bg, R& chi_bg,
-                                             R& eta_atom, double Jold) const {
+                                             R& eta_atom, R Jold) const {
     const pyrh_nlte_batch& b = A->b;
     R chi_a = 0, eta_a = 0;
     for (int m = 0; m < as->n; ++m) {
@@ -223,10 +247,11 @@ struct NlteOpacity {
         eta_a += (as->tw[m] * g) * (V * nj);
       }
     }
-    const int64_t c = coff + (int64_t)k * ns + la;
-    chi_bg = R(b.chi_c[c]);
+    const int64_t c = coff + (int64_t)k * ns + la, tc = b.total_cont;
+    const R* bg = static_cast<const R*>(A->bgr);
+    chi_bg = bg[c];
     const R ct = chi_a + chi_bg;
-    const R eta_bg = R(b.eta_c[c]) + R(b.sca_c[c]) * R(Jold);
+    const R eta_bg = bg[tc + c] + bg[2 * tc + c] * Jold;
     chi = ct;
     S = (eta_a + eta_bg) / ct;
     S_bg = eta_bg / ct;
@@ -235,10 +260,11 @@ struct NlteOpacity {
 };
 
 // Mean intensity of one wavelength at depth k ([depth][lambda] storage).
+template <typename R>
 struct JRow {
-  const double* base;
+  const R* base;
   int stride;
-  __device__ __forceinline__ double operator[](int k) const { return base[(int64_t)k * stride]; }
+  __device__ __forceinline__ R operator[](int k) const { return base[(int64_t)k * stride]; }
 };
 
 // Scalar Bezier3 with the diagonal operator along one direction
@@ -249,7 +275,7 @@ struct JRow {
 // of the sweep (the emergent one for to_obs).
 template <typename R, typename Op, typename Emit>
 __device__ __forceinline__ R bezier_sweep(const Op& op, const R* ds, int nd, int to_obs,
-                                          double B0, double B1, const JRow& Jold, Emit&& emit) {
+                                          double B0, double B1, const JRow<R>& Jold, Emit&& emit) {
   // Ieff = I - Psi S_atom, the effective intensity of the MALI rates
   // (fillgamma.c:121-134), is built term by term in the same recurrence: the
   // local source enters through S_bg = S - S_atom only, so no difference of
@@ -401,9 +427,10 @@ constexpr int kFormalWarps = 4;
 // of its tile's rate partial sums and of its 32 wavelengths' new J, and adds
 // to them in program order, so every sum has a fixed order and the solve is
 // bit-reproducible.
+template <typename R>
 struct TileSink {
-  double* gslab;      // this tile's partial sums: slot * total_depth + doff + k
-  double* Jn;         // new J of this lane's wavelength, depth stride ns
+  R* gslab;           // this tile's partial sums: slot * total_depth + doff + k
+  R* Jn;              // new J of this lane's wavelength, depth stride ns
   int64_t total_depth, doff;
   int ns;
 };
@@ -414,12 +441,12 @@ struct TileSink {
 template <typename R>
 __device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_transition* tr,
                                           const ActiveSet<R>& as, const NlteShared<R>& sh,
-                                          const TileSink& out, int nd, int nlev, int q, int k,
+                                          const TileSink<R>& out, int nd, int nlev, int q, int k,
                                           bool mine, R wdir, R I_k, R Psi_k, R omp, R Ieff_k,
                                           R chi_k, R chi_bg) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  if (mine) atomicAdd(out.Jn + (int64_t)k * out.ns, (double)(wdir * I_k));
+  if (mine) atomicAdd(out.Jn + (int64_t)k * out.ns, wdir * I_k);
   const int nact = mine ? as.n : 0;
   const int nm = __reduce_max_sync(full, nact);
   if (nm == 0) return;
@@ -492,27 +519,27 @@ __device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_tra
     // Sum over the lanes that add to the same entry, in an order fixed by
     // the lane numbers, then one addition by the group's first lane.
     const unsigned peers = __match_any_sync(full, key);
-    double sij, sji;
+    R sij, sji;
     if (peers == full) {
       if (key < 0) continue;
       for (int o = 16; o > 0; o >>= 1) {
         gij += __shfl_xor_sync(full, gij, o);
         gji += __shfl_xor_sync(full, gji, o);
       }
-      sij = (double)gij;
-      sji = (double)gji;
+      sij = gij;
+      sji = gji;
     } else {
       const int cnt = key >= 0 ? __popc(peers) : 0;
       const int maxc = __reduce_max_sync(full, cnt);
       unsigned rem = key >= 0 ? peers : 0u;
-      sij = 0.0;
-      sji = 0.0;
+      sij = R(0);
+      sji = R(0);
       for (int s = 0; s < maxc; ++s) {
         const int src = rem ? __ffs(rem) - 1 : lane;
         const R a = __shfl_sync(full, gij, src), c = __shfl_sync(full, gji, src);
         if (rem) {
-          sij += (double)a;
-          sji += (double)c;
+          sij += a;
+          sji += c;
           rem &= rem - 1;
         }
       }
@@ -533,7 +560,11 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
   const int p = blockIdx.y;
   if (!emergent_only && !A.active[p]) return;
   const int nd = b.ndep[p], ns = b.nspect[p], nlev = b.nlevel, nt = b.ntrans[p];
-  const int tile0 = blockIdx.x * kFormalWarps;
+  // block = kFormalWarps tiles of one atmosphere and one ray group: the
+  // group takes rays grp, grp + ngroup, ... (one group unless the batch is
+  // too small to fill the GPU with tiles)
+  const int grp = blockIdx.x % A.ngroup;
+  const int tile0 = (blockIdx.x / A.ngroup) * kFormalWarps;
   if (tile0 * 32 >= ns) return;
   if (nd < 3 || nd > b.max_ndep || nd > PYRH_NLTE_MAX_DEPTH) {   // uniform per block
     if (threadIdx.x == 0) atomicOr(A.err, 2);
@@ -598,7 +629,7 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
       }
     }
   const double B0 = planck(b.T[doff + nd - 2], lam), B1 = planck(b.T[doff + nd - 1], lam);
-  const JRow Jold{b.J + coff + la, ns};
+  const JRow<R> Jold{static_cast<const R*>(A.Jr) + coff + la, ns};
   // angle-dependent wavelengths (formal.c:96-101) take the Bezier3 solution
   // in both directions, the others Feautrier once per ray
   const bool angle_dep = A.moving && (as.bb || b.bgline[b.lam_off[p] + la]);
@@ -607,14 +638,15 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
   NlteOpacity<R> op;
   op.A = &A; op.tr = tr; op.as = &as; op.sh = &sh;
   op.nd = nd; op.ns = ns; op.la = la; op.coff = coff;
-  TileSink out;
-  out.gslab = A.gslab + (int64_t)tile * nlev * (nlev - 1) * b.total_depth;
-  out.Jn = A.Jnew + coff + la;
+  TileSink<R> out;
+  out.gslab = static_cast<R*>(A.gslab) +
+              ((int64_t)tile * A.ngroup + grp) * nlev * (nlev - 1) * b.total_depth;
+  out.Jn = static_cast<R*>(A.Jnew) + grp * b.total_cont + coff + la;
   out.total_depth = b.total_depth;
   out.doff = doff;
   out.ns = ns;
   R emergent = R(0);
-  for (int ray = 0; ray < A.nrays; ++ray) {
+  for (int ray = grp; ray < A.nrays; ray += A.ngroup) {
     const R* dsl = sh.ds + ray * nd;
     if (any_bez) {
       for (int to_obs = emergent_only ? 1 : 0; to_obs <= 1; ++to_obs) {
@@ -656,15 +688,23 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
 }
 
 // J <- new J for atmospheres still iterating (each wavelength replaces its
-// own mean intensity, formal.c:128-139).
+// own mean intensity, formal.c:128-139), the ray groups' sums added in
+// group order; the formal-precision copy of J follows.
+template <typename R>
 __global__ void nlte_jcopy_kernel(NlteArgs A) {
   const pyrh_nlte_batch& b = A.b;
   const int p = blockIdx.y;
   if (!A.active[p]) return;
   const int64_t coff = b.cont_off[p], ncont = (int64_t)b.ndep[p] * b.nspect[p];
+  const R* Jn = static_cast<const R*>(A.Jnew);
+  R* Jr = static_cast<R*>(A.Jr);
   for (int64_t e = threadIdx.x + (int64_t)blockIdx.x * blockDim.x; e < ncont;
-       e += (int64_t)blockDim.x * gridDim.x)
-    b.J[coff + e] = A.Jnew[coff + e];
+       e += (int64_t)blockDim.x * gridDim.x) {
+    double J = (double)Jn[coff + e];
+    for (int g = 1; g < A.ngroup; ++g) J += (double)Jn[g * b.total_cont + coff + e];
+    b.J[coff + e] = J;
+    Jr[coff + e] = R(J);
+  }
 }
 
 // ------------------------------------------------ statistical equilibrium --
@@ -733,6 +773,7 @@ __device__ void lu_solve(int n, double* A, double* bvec) {
   for (int i = 0; i < n; ++i) bvec[i] += res[i];
 }
 
+template <typename R>
 __global__ void nlte_stateq_kernel(NlteArgs A) {
   const pyrh_nlte_batch& b = A.b;
   const int p = blockIdx.y;
@@ -751,15 +792,16 @@ __global__ void nlte_stateq_kernel(NlteArgs A) {
     } else {
       ie = A.isum;
     }
-    // Gamma = C plus the rate sums of the atmosphere's wavelength tiles,
-    // added in tile order
-    const int ntile = (b.nspect[p] + 31) / 32, nslot = nl * (nl - 1);
+    // Gamma = C plus the rate sums of the atmosphere's (tile, ray group)
+    // pairs, added in that order
+    const int ntile = (b.nspect[p] + 31) / 32 * A.ngroup, nslot = nl * (nl - 1);
     for (int i = 0; i < nl; ++i)
       for (int j = 0; j < nl; ++j) {
         double g = b.C[(int64_t)(i * nl + j) * b.total_depth + doff + k];
         if (i != j) {
-          const double* sl = A.gslab + (int64_t)gamma_slot(i, j, nl) * b.total_depth + doff + k;
-          for (int t = 0; t < ntile; ++t) g += sl[(int64_t)t * nslot * b.total_depth];
+          const R* sl = static_cast<const R*>(A.gslab) +
+                        (int64_t)gamma_slot(i, j, nl) * b.total_depth + doff + k;
+          for (int t = 0; t < ntile; ++t) g += (double)sl[(int64_t)t * nslot * b.total_depth];
         }
         M[i * nl + j] = g;
       }
@@ -901,6 +943,14 @@ __global__ void nlte_ng_kernel(NlteArgs A, int init) {
 
 // ----------------------------------------------------------- launching ---
 
+int nlte_ray_groups(int natm, int max_nspect, int nrays) {
+  const long long tiles = (long long)natm * ((max_nspect + 31) / 32);
+  const long long target = 4096;     // warps: about 27 per SM of a 152-SM GPU
+  long long g = (target + tiles - 1) / (tiles > 0 ? tiles : 1);
+  if (g > nrays) g = nrays;
+  return g < 1 ? 1 : (int)g;
+}
+
 size_t nlte_formal_smem(int nlevel, int maxd, int nrays, int max_nline, int precision) {
   return precision == PYRH_FP32
              ? formal_smem_layout<float>(nlevel, maxd, nrays, max_nline, nullptr, nullptr)
@@ -931,36 +981,55 @@ cudaError_t nlte_launch_profiles(const NlteArgs& A, int natm, int64_t max_elems,
 
 template <typename R>
 static cudaError_t launch_formal_t(const NlteArgs& A, int natm, int max_nspect, int maxd,
-                                   int emergent_only, double* I_out, cudaStream_t st) {
+                                   int emergent_only, double* I_out, cudaStream_t st,
+                                   bool set_attr = true) {
   const size_t smem = nlte_formal_smem(A.b.nlevel, maxd, A.nrays, A.b.max_nline,
                                        sizeof(R) == 4 ? PYRH_FP32 : PYRH_FP64);
-  cudaError_t e = cudaFuncSetAttribute(nlte_formal_kernel<R>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaSuccess;
+  if (set_attr)
+    e = cudaFuncSetAttribute(nlte_formal_kernel<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
   if (e != cudaSuccess) return e;
   const int ntile = (max_nspect + 31) / 32;
-  dim3 g((ntile + kFormalWarps - 1) / kFormalWarps, natm);
+  dim3 g((ntile + kFormalWarps - 1) / kFormalWarps * A.ngroup, natm);
   nlte_formal_kernel<R><<<g, 32 * kFormalWarps, smem, st>>>(A, emergent_only, I_out);
   return cudaGetLastError();
 }
 
-cudaError_t nlte_launch_iteration(const NlteArgs& A, int natm, int max_nspect, int maxd,
-                                  int precision, cudaStream_t st) {
+template <typename R>
+static cudaError_t launch_iteration_t(const NlteArgs& A, int natm, int max_nspect, int maxd,
+                                      cudaStream_t st, bool set_attr) {
   dim3 gi(8, natm);
-  nlte_gamma_init_kernel<<<gi, 256, 0, st>>>(A);
+  nlte_gamma_init_kernel<R><<<gi, 256, 0, st>>>(A);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  e = precision == PYRH_FP32
-          ? launch_formal_t<float>(A, natm, max_nspect, maxd, 0, nullptr, st)
-          : launch_formal_t<double>(A, natm, max_nspect, maxd, 0, nullptr, st);
+  e = launch_formal_t<R>(A, natm, max_nspect, maxd, 0, nullptr, st, set_attr);
   if (e != cudaSuccess) return e;
-  nlte_jcopy_kernel<<<gi, 256, 0, st>>>(A);
+  nlte_jcopy_kernel<R><<<gi, 256, 0, st>>>(A);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   dim3 gs((maxd + 127) / 128, natm);
-  nlte_stateq_kernel<<<gs, 128, 0, st>>>(A);
+  nlte_stateq_kernel<R><<<gs, 128, 0, st>>>(A);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   nlte_ng_kernel<<<natm, 256, 0, st>>>(A, 0);
+  return cudaGetLastError();
+}
+
+cudaError_t nlte_launch_iteration(const NlteArgs& A, int natm, int max_nspect, int maxd,
+                                  int precision, cudaStream_t st, bool set_attr) {
+  return precision == PYRH_FP32
+             ? launch_iteration_t<float>(A, natm, max_nspect, maxd, st, set_attr)
+             : launch_iteration_t<double>(A, natm, max_nspect, maxd, st, set_attr);
+}
+
+cudaError_t nlte_launch_prepare(const NlteArgs& A, int precision, cudaStream_t st) {
+  const int64_t tc = A.b.total_cont;
+  int64_t blocks = (tc + 255) / 256;
+  if (blocks > 8192) blocks = 8192;
+  if (blocks < 1) blocks = 1;
+  if (precision == PYRH_FP32) nlte_prepare_kernel<float><<<(unsigned)blocks, 256, 0, st>>>(A);
+  else nlte_prepare_kernel<double><<<(unsigned)blocks, 256, 0, st>>>(A);
   return cudaGetLastError();
 }
 

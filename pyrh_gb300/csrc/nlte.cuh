@@ -13,21 +13,34 @@ struct NlteArgs {
   int nrays;
   double muz[PYRH_NLTE_MAX_RAYS], wmu[PYRH_NLTE_MAX_RAYS];
   int moving, isum, ng_order, ng_delay, ng_period, nmax_iter;
+  int ngroup;                     // ray groups of the formal kernel (nlte_ray_groups)
   double iter_limit;
   // workspace
   void *phi;
   int64_t phi_cap;                // elements of phi
-  double *wphi, *Jnew, *gslab, *ngprev, *dpops;   // gslab: per-tile rate sums
+  double *wphi, *ngprev, *dpops;
+  // in the formal-solution precision: per (tile, ray group) rate sums, the
+  // ray groups' new J, the background [chi_c, eta_c, sca_c] and J
+  void *gslab, *Jnew, *bgr, *Jr;
   int32_t *count, *active, *iters, *err;
   int32_t *any;                   // set by nlte_ng_kernel while an atmosphere iterates
 };
+
+// Ray groups for a batch: enough (tile, group) warps to fill the GPU, at
+// most one group per ray; depends on the batch's shape only.
+int nlte_ray_groups(int natm, int max_nspect, int nrays);
 
 size_t nlte_formal_smem(int nlevel, int maxd, int nrays, int max_nline, int precision);
 cudaError_t nlte_launch_profiles(const NlteArgs &A, int natm, int64_t max_elems, int precision,
                                  cudaStream_t st);
 cudaError_t nlte_launch_ng_init(const NlteArgs &A, int natm, cudaStream_t st);
+// background and starting J in the formal-solution precision (once per solve)
+cudaError_t nlte_launch_prepare(const NlteArgs &A, int precision, cudaStream_t st);
+// One MALI iteration (5 launches).  set_attr = false leaves the formal
+// kernel's shared-memory attribute as an earlier call set it (for stream
+// capture, where the launches are recorded rather than issued).
 cudaError_t nlte_launch_iteration(const NlteArgs &A, int natm, int max_nspect, int maxd,
-                                  int precision, cudaStream_t st);
+                                  int precision, cudaStream_t st, bool set_attr = true);
 cudaError_t nlte_launch_emergent(const NlteArgs &A, int natm, int max_nspect, int maxd,
                                  int precision, double *I_out, cudaStream_t st);
 

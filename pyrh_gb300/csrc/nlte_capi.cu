@@ -17,18 +17,28 @@ namespace {
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct Layout {
-  size_t wphi, Jnew, gslab, ngprev, count, active, iters, err, any, dpops, phi, fixed;
+  size_t wphi, Jnew, gslab, bgr, Jr, ngprev, count, active, iters, err, any, dpops, phi, fixed;
 };
 
-Layout layout(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg) {
+int groups_of(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg) {
+  return pyrh::nlte_ray_groups(b->natm, b->max_nspect, cfg->nrays);
+}
+
+// Workspace layout for `ngroup` ray groups of the formal kernel.
+Layout layout(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg, int ngroup) {
   Layout L;
   size_t off = 0;
   const int nlev = b->nlevel, natm = b->natm;
   L.wphi = off; off = align256(off + sizeof(double) * (size_t)(b->max_nline > 0 ? b->max_nline : 1) * b->total_depth);
-  L.Jnew = off; off = align256(off + sizeof(double) * (size_t)b->total_cont);
-  // rate sums per (wavelength tile of 32, off-diagonal entry, depth)
+  // in the formal-solution precision: the new J of each ray group, the
+  // rate sums per (wavelength tile of 32, ray group, off-diagonal entry,
+  // depth), the background and J
+  const size_t r = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
+  L.Jnew = off; off = align256(off + r * (size_t)ngroup * b->total_cont);
   const size_t ntile = (size_t)(b->max_nspect + 31) / 32;
-  L.gslab = off; off = align256(off + sizeof(double) * ntile * nlev * (nlev - 1) * b->total_depth);
+  L.gslab = off; off = align256(off + r * ntile * ngroup * nlev * (nlev - 1) * b->total_depth);
+  L.bgr = off; off = align256(off + r * 3 * (size_t)b->total_cont);
+  L.Jr = off; off = align256(off + r * (size_t)b->total_cont);
   L.ngprev = off; off = align256(off + sizeof(double) * (size_t)(cfg->ng_order + 2) * nlev * b->total_depth);
   L.count = off; off = align256(off + sizeof(int32_t) * natm);
   L.active = off; off = align256(off + sizeof(int32_t) * natm);
@@ -77,10 +87,11 @@ pyrh_status check(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg) {
 }
 
 pyrh::NlteArgs make_args(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg, void* ws,
-                         size_t ws_bytes, const Layout& L) {
+                         size_t ws_bytes, const Layout& L, int ngroup) {
   pyrh::NlteArgs A;
   A.b = *b;
   A.nrays = cfg->nrays;
+  A.ngroup = ngroup;
   for (int m = 0; m < PYRH_NLTE_MAX_RAYS; ++m) {
     A.muz[m] = m < cfg->nrays ? cfg->muz[m] : 1.0;
     A.wmu[m] = m < cfg->nrays ? cfg->wmu[m] : 0.0;
@@ -94,8 +105,10 @@ pyrh::NlteArgs make_args(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg, 
   A.iter_limit = cfg->iter_limit;
   char* w = static_cast<char*>(ws);
   A.wphi = reinterpret_cast<double*>(w + L.wphi);
-  A.Jnew = reinterpret_cast<double*>(w + L.Jnew);
-  A.gslab = reinterpret_cast<double*>(w + L.gslab);
+  A.Jnew = w + L.Jnew;
+  A.gslab = w + L.gslab;
+  A.bgr = w + L.bgr;
+  A.Jr = w + L.Jr;
   A.ngprev = reinterpret_cast<double*>(w + L.ngprev);
   A.count = reinterpret_cast<int32_t*>(w + L.count);
   A.active = reinterpret_cast<int32_t*>(w + L.active);
@@ -136,6 +149,69 @@ cudaError_t iterate(const pyrh::NlteArgs& A, const pyrh_nlte_batch* b,
   return e;
 }
 
+
+// The same loop with one chunk of kChunk iterations recorded as a CUDA graph
+// and replayed per chunk on the caller's stream (one graph launch instead
+// of 5 kChunk kernel launches).  The recording uses a private stream, since
+// the caller's may be the legacy default stream, which cannot be captured;
+// nothing runs while recording.  The first chunk runs uncaptured, which
+// also sets the formal kernel's shared-memory attribute before the
+// recording; if the capture or the instantiation fails, the remaining
+// chunks run uncaptured.
+cudaError_t iterate_graph(const pyrh::NlteArgs& A, const pyrh_nlte_batch* b,
+                          const pyrh_nlte_config* cfg, cudaStream_t st, int* launches) {
+  cudaError_t e = cudaSuccess;
+  int it = 0;
+  int32_t any = 1;
+  {   // first chunk, uncaptured
+    const int n = cfg->nmax_iter < kChunk ? cfg->nmax_iter : kChunk;
+    for (int c = 0; c < n && e == cudaSuccess; ++c) {
+      e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision,
+                                      st);
+      *launches += 5;
+    }
+    it += n;
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&any, A.any, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess || !any || it >= cfg->nmax_iter) return e;
+  }
+  cudaStream_t cs = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool captured = false;
+  if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+      cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    cudaError_t ce = cudaSuccess;
+    for (int c = 0; c < kChunk && ce == cudaSuccess; ++c)
+      ce = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision,
+                                       cs, false);
+    const cudaError_t ee = cudaStreamEndCapture(cs, &graph);
+    captured = ce == cudaSuccess && ee == cudaSuccess && graph &&
+               cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+  }
+  cudaGetLastError();   // a failed capture leaves no sticky error; clear the last one
+  // iterations beyond nmax_iter do nothing: nlte_ng_kernel retires an
+  // atmosphere once it reaches nmax_iter, so whole chunks are safe
+  for (; e == cudaSuccess && it < cfg->nmax_iter && any; it += kChunk) {
+    if (captured) {
+      e = cudaGraphLaunch(exec, st);
+    } else {
+      for (int c = 0; c < kChunk && e == cudaSuccess; ++c)
+        e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision,
+                                        st);
+    }
+    *launches += 5 * kChunk;
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&any, A.any, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (cs) cudaStreamDestroy(cs);
+  return e;
+}
+
 }  // namespace
 
 extern "C" {
@@ -143,7 +219,7 @@ extern "C" {
 size_t pyrh_nlte_workspace_bytes(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg,
                                  int64_t phi_elems) {
   if (!b || !cfg) return 0;
-  const Layout L = layout(b, cfg);
+  const Layout L = layout(b, cfg, groups_of(b, cfg));
   const size_t r = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
   return L.fixed + r * (size_t)(phi_elems > 0 ? phi_elems : 1);
 }
@@ -153,13 +229,14 @@ pyrh_status pyrh_nlte_solve(const pyrh_nlte_batch* b, const pyrh_nlte_config* cf
   pyrh::set_launches(0);
   pyrh_status s = check(b, cfg);
   if (s != PYRH_OK) return s;
-  const Layout L = layout(b, cfg);
+  const int ngroup = groups_of(b, cfg);
+  const Layout L = layout(b, cfg, ngroup);
   if (!ws || ws_bytes <= L.fixed) {
     pyrh::set_error("workspace of %zu bytes is smaller than %zu", ws_bytes, L.fixed);
     return PYRH_ERR_ARG;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  pyrh::NlteArgs A = make_args(b, cfg, ws, ws_bytes, L);
+  pyrh::NlteArgs A = make_args(b, cfg, ws, ws_bytes, L, ngroup);
   const size_t smem = pyrh::nlte_formal_smem(b->nlevel, b->max_ndep, cfg->nrays, b->max_nline, cfg->precision);
   if (smem > 220 * 1024) {
     pyrh::set_error("shared memory %zu B for %d levels x %d depths", smem, b->nlevel, b->max_ndep);
@@ -168,10 +245,11 @@ pyrh_status pyrh_nlte_solve(const pyrh_nlte_batch* b, const pyrh_nlte_config* cf
   cudaError_t e = cudaMemsetAsync(A.err, 0, sizeof(int32_t), st);
   int launches = 1;
   if (e == cudaSuccess) e = pyrh::nlte_launch_ng_init(A, b->natm, st), ++launches;
+  if (e == cudaSuccess) e = pyrh::nlte_launch_prepare(A, cfg->precision, st), ++launches;
   const int64_t max_elems = (int64_t)b->max_nspect * 2 * cfg->nrays * b->max_ndep;
   if (e == cudaSuccess)
     e = pyrh::nlte_launch_profiles(A, b->natm, max_elems, cfg->precision, st), launches += 2;
-  if (e == cudaSuccess) e = iterate(A, b, cfg, st, &launches);
+  if (e == cudaSuccess) e = iterate_graph(A, b, cfg, st, &launches);
   int32_t err = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&err, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess && iterations)
@@ -215,22 +293,23 @@ pyrh_status pyrh_nlte_emergent(const pyrh_nlte_batch* b, const pyrh_nlte_config*
   one.nrays = 1;
   one.muz[0] = mu_out;
   one.wmu[0] = 1.0;
-  const Layout L = layout(b, &one);
+  const Layout L = layout(b, &one, 1);
   if (!ws || ws_bytes <= L.fixed) {
     pyrh::set_error("workspace of %zu bytes is smaller than %zu", ws_bytes, L.fixed);
     return PYRH_ERR_ARG;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  pyrh::NlteArgs A = make_args(b, &one, ws, ws_bytes, L);
+  pyrh::NlteArgs A = make_args(b, &one, ws, ws_bytes, L, 1);
   cudaError_t e = cudaMemsetAsync(A.err, 0, sizeof(int32_t), st);
   const int64_t max_elems = (int64_t)b->max_nspect * 2 * b->max_ndep;
+  if (e == cudaSuccess) e = pyrh::nlte_launch_prepare(A, one.precision, st);
   if (e == cudaSuccess) e = pyrh::nlte_launch_profiles(A, b->natm, max_elems, one.precision, st);
   if (e == cudaSuccess)
     e = pyrh::nlte_launch_emergent(A, b->natm, b->max_nspect, b->max_ndep, one.precision, I_out, st);
   int32_t err = 0;
   if (e == cudaSuccess) e = cudaMemcpyAsync(&err, A.err, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  pyrh::set_launches(3);
+  pyrh::set_launches(4);
   if (e != cudaSuccess) {
     pyrh::set_error("NLTE emergent: %s", cudaGetErrorString(e));
     return PYRH_ERR_CUDA;
@@ -291,9 +370,16 @@ extern "C" pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch* b,
                     kMaxStaticAtm);
     return PYRH_ERR_ARG;
   }
-  const Layout L = layout(b, cfg);
+  // the workspace solve's ray groups if their partial sums fit, else one
   const size_t r = cfg->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
-  const size_t need = L.fixed + r * (size_t)(phi_elems > 0 ? phi_elems : 1);
+  const size_t phi_bytes = r * (size_t)(phi_elems > 0 ? phi_elems : 1);
+  int ngroup = groups_of(b, cfg);
+  Layout L = layout(b, cfg, ngroup);
+  if (L.fixed + phi_bytes > (size_t)PYRH_NLTE_STATIC_SCRATCH_BYTES && ngroup > 1) {
+    ngroup = 1;
+    L = layout(b, cfg, 1);
+  }
+  const size_t need = L.fixed + phi_bytes;
   if (need > (size_t)PYRH_NLTE_STATIC_SCRATCH_BYTES) {
     pyrh::set_error("pyrh_nlte_solve_static: batch needs %zu bytes of scratch, the static "
                     "scratch holds %zu (PYRH_NLTE_STATIC_SCRATCH_BYTES)",
@@ -312,7 +398,7 @@ extern "C" pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch* b,
     return PYRH_ERR_CUDA;
   }
   cudaStream_t st = (cudaStream_t)stream;
-  pyrh::NlteArgs A = make_args(b, cfg, ws, need, L);
+  pyrh::NlteArgs A = make_args(b, cfg, ws, need, L, ngroup);
   // The array keeps the previous call's contents; the error word is the
   // only part a kernel reads before this call writes it, so it alone is
   // cleared (the kernels write profiles, rate matrices, Ng history and
@@ -321,6 +407,7 @@ extern "C" pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch* b,
   e = cudaMemsetAsync(A.err, 0, sizeof(int32_t), st);
   int launches = 1;
   if (e == cudaSuccess) e = pyrh::nlte_launch_ng_init(A, b->natm, st), ++launches;
+  if (e == cudaSuccess) e = pyrh::nlte_launch_prepare(A, cfg->precision, st), ++launches;
   const int64_t max_elems = (int64_t)b->max_nspect * 2 * cfg->nrays * b->max_ndep;
   if (e == cudaSuccess)
     e = pyrh::nlte_launch_profiles(A, b->natm, max_elems, cfg->precision, st), launches += 2;

@@ -6,7 +6,7 @@ At the limits (GPU, marked `gpu`):
   * PYRH_RF_MAX_DEPTH (160) depths in the response functions, FP64 against
     the CPU adjoint to 1e-8 of each parameter's largest |RF|;
   * PYRH_NLTE_MAX_DEPTH (160) depths in the NLTE solve, against the NLTE
-    oracle (FP64 1e-6 and the same iteration count, FP32 1e-3);
+    oracle (the same iteration count; FP64 1e-6, FP32 1e-4);
   * PYRH_MAX_LINES (16) lines, one of them with PYRH_MAX_COMPONENTS (32)
     Zeeman components, all inside their windows at every wavelength, in the
     synthesis (against the oracle) and in the response functions at 71
@@ -201,19 +201,19 @@ def deepen_nlte(fx: dict, nd: int) -> dict:
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,tol", [(FP64, 1e-6), (FP32, 1e-3)])
+@pytest.mark.parametrize("precision,tol", [(FP64, 1e-6), (FP32, 1e-4)])
 def test_nlte_at_max_depth(golden, precision, tol):
     """PYRH_NLTE_MAX_DEPTH (160) depths: the C1 atmosphere interpolated onto
     160 depths, solved to convergence on the GPU and by the NLTE oracle (35
-    iterations); FP64 takes the same number of iterations."""
+    iterations); both precisions take the same number of iterations.  FP32
+    bound: the convergence criterion itself (measured 4-7e-6)."""
     from pyrh_gb300 import nlte
     fx = deepen_nlte(golden("nlte_c1"), L.PYRH_NLTE_MAX_DEPTH)
     n_or, _, it_or, _, _ = O.nlte_solve(fx)
     cfg = nlte.make_config(fx, precision)
     dev = nlte.DeviceNlte(nlte.pack([fx], cfg.nrays), cfg)
     assert dev.solve(cfg) == L.PYRH_OK, L.lib().pyrh_last_error()
-    if precision == FP64:
-        assert int(dev.iterations.cpu()[0]) == it_or
+    assert int(dev.iterations.cpu()[0]) == it_or
     assert np.abs(dev.populations()[0] / n_or - 1).max() < tol
 
 

@@ -4,15 +4,17 @@ golden populations and emergent intensities.
 
 Tolerances (relative, element-wise):
   FP64: populations and emergent intensity vs reference   1e-6
-  FP32 formal solution (FP64 rates, LU, Ng):               1e-3
-The FP32 bound is measured, not designed: single-precision I and Psi change
-the path of the iteration (a few more or fewer iterations, a different Ng
-extrapolation), so the FP32 run stops at a different point inside the same
-convergence limit of 1e-4; measured errors of the converged populations are
-0.8e-4 to 3.5e-4 on these atmospheres.  The MALI effective intensity
-I - Psi*eta of fillgamma.c:121-134 is formed without cancellation inside the
-Bezier recurrence; formed as a difference it cost up to 2e-3 in optically
-thick line cores.  FP64 is the parity mode.
+  FP32 formal solution (FP64 rates, LU, Ng):               1e-4
+The FP32 bound is the convergence criterion of the runs (ITER_LIMIT 1e-4);
+measured 2-7e-6 with the reference's iteration counts.  Two reformulations
+keep single precision from cancelling in optically thick line cores: the
+MALI effective intensity I - Psi*eta (fillgamma.c:121-134) is built inside
+the Bezier recurrence, and the preconditioned downward rate
+(2 h nu^3/c^2 + Ieff) g V W - chi_up Psi U_down (fillgamma.c:185-196) is
+formed from the escape fraction 1 - X Psi / chi = X_other / chi +
+(X / chi)(1 - Psi) with 1 - Psi from the positive Bezier weights.  Formed
+as differences they cost up to 2e-3 and 9e-4.  Every rate and J sum has a
+fixed order, so solves are bit-reproducible.
 """
 import numpy as np
 import pytest
@@ -64,14 +66,34 @@ def test_converged_fp64(golden, name):
     assert _rel(I[m], fx["I_out"]) < 1e-6
 
 
-def test_converged_fp32(golden):
-    fx = golden("nlte_c1")
+@pytest.mark.parametrize("name", CASES)
+def test_converged_fp32(golden, name):
+    fx = golden(name)
     dev, cfg, st = _solve([fx], L.PYRH_FP32)
     assert st == L.PYRH_OK, L.lib().pyrh_last_error()
-    assert _rel(dev.populations()[0], fx["n_final"]) < 1e-3
+    assert int(dev.iterations.cpu()[0]) == O.nlte_solve(fx)[2]
+    assert _rel(dev.populations()[0], fx["n_final"]) < 1e-4
     assert dev.emergent(cfg, float(fx["fmeta"][2])) == L.PYRH_OK
     m = O.output_mask(fx["lambda"], fx["fmeta"][1])
-    assert _rel(dev.emergent_spectra()[0][m], fx["I_out"]) < 1e-3
+    assert _rel(dev.emergent_spectra()[0][m], fx["I_out"]) < 1e-4
+
+
+@pytest.mark.parametrize("precision", [L.PYRH_FP32, L.PYRH_FP64])
+def test_bit_reproducible(golden, precision):
+    """Three solves of the same ragged batch give identical populations and
+    J, bit for bit (rate and J sums in a fixed order)."""
+    atms = [golden(n) for n in CASES]
+    cfg = nlte.make_config(atms[0], precision)
+    dev = nlte.DeviceNlte(nlte.pack(atms, cfg.nrays), cfg)
+    runs = []
+    for _ in range(3):
+        dev.reset()
+        assert dev.solve(cfg) == L.PYRH_OK, L.lib().pyrh_last_error()
+        runs.append((dev.t["n"].cpu().numpy().copy(), dev.t["J"].cpu().numpy().copy(),
+                     dev.iterations.cpu().numpy().copy()))
+    for n, J, it in runs[1:]:
+        assert np.array_equal(n, runs[0][0]) and np.array_equal(J, runs[0][1])
+        assert np.array_equal(it, runs[0][2])
 
 
 def test_ragged_batch_fp64(golden):

@@ -3,17 +3,16 @@ array, so that the call allocates nothing) against pyrh_nlte_solve with a
 caller-allocated workspace, both through the C ABI, on two static calls in a
 row (the second finds the first's contents in the array).
 
-The two entry points run the same kernels in the same order, but neither is
-bit-reproducible from run to run: the rate matrices and J are sums of
-shared-memory FP64 atomic additions in whatever order the threads arrive,
-and Ng acceleration amplifies those last-digit differences (FP64 runs differ
-by ~1e-8 relative in the populations).  So the comparison uses the solver's
-own parity tolerances: FP64 populations and J within 1e-6 relative of the
-workspace solve and of the reference's converged populations, with identical
-iteration counts; FP32 populations and J within 1e-3 (single-precision I and
-Psi change the iteration's path, so two FP32 runs may stop at different
-iterations inside the same convergence limit).  The file name sorts last so that the static array is first touched
-after every other test's allocations."""
+The two entry points run the same kernels in the same order, and every
+rate and J sum of the solver has a fixed order; where the workspace solve
+splits the rays of a small batch into groups whose partial sums would not
+fit the static array, the static call keeps one group, which adds the same
+terms in another order.  So the comparison uses the solver's parity
+tolerances: FP64 populations and J within 1e-6 relative of the workspace
+solve and of the reference's converged populations, with identical
+iteration counts; FP32 within 1e-4 (the runs' convergence criterion).  The
+file name sorts last so that the static array is first touched after every
+other test's allocations."""
 import ctypes as C
 
 import numpy as np
@@ -25,7 +24,7 @@ from pyrh_gb300 import nlte
 pytestmark = pytest.mark.gpu
 
 STATIC_BYTES = 32 * 1024 * 1024
-TOL = {L.PYRH_FP64: 1e-6, L.PYRH_FP32: 1e-3}
+TOL = {L.PYRH_FP64: 1e-6, L.PYRH_FP32: 1e-4}
 
 
 def _bind():
@@ -62,7 +61,6 @@ def test_static_matches_workspace_solve(golden, names, precision):
     fx = [golden(n) for n in names]
     cfg = nlte.make_config(fx[0], precision)
     dev = nlte.DeviceNlte(nlte.pack(fx, cfg.nrays), cfg)
-    assert dev.ws_bytes <= STATIC_BYTES
     st0 = dev.solve(cfg)
     assert st0 in (L.PYRH_OK, L.PYRH_ERR_NONCONVERGED), L.lib().pyrh_last_error()
     if precision == L.PYRH_FP64:
