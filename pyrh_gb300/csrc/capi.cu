@@ -136,7 +136,7 @@ pyrh_status launch(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nline,
                    const pyrh_lte_config* cfg, void* out, cudaStream_t st) {
   const int block = default_block(b->max_nlam, cfg->block_lambda);
   pyrh::LteArgs a = make_args(b, d_lines, nline, cfg, out, block);
-  const size_t smem = pyrh::lte_smem_bytes(cfg->precision, nline, a.maxd);
+  const size_t smem = pyrh::lte_smem_bytes(cfg->precision, nline, a.maxd, block);
   if (smem > smem_limit())
     return fail(PYRH_ERR_UNSUPPORTED, "shared memory %zu B for %d lines x %d depths", smem,
                 nline, a.maxd);

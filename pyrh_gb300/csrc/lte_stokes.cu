@@ -44,6 +44,7 @@ struct Smem {
   int* cq;       // [nline][PYRH_MAX_COMPONENTS]
   double* lam0;  // [nline]
   int* meta;     // [nline][3]: ncomp, polarizable, contributes
+  R* dlam;       // [nline][block]: lambda - lambda0 of each thread's wavelength
   int maxd;
 };
 
@@ -57,16 +58,21 @@ __device__ __forceinline__ Smem<R> carve(unsigned char* base, int nline, int max
   s.cshift = reinterpret_cast<R*>(base + off); off += sizeof(R) * nline * PYRH_MAX_COMPONENTS;
   s.cweight = reinterpret_cast<R*>(base + off); off += sizeof(R) * nline * PYRH_MAX_COMPONENTS;
   s.cq = reinterpret_cast<int*>(base + off); off += sizeof(int) * nline * PYRH_MAX_COMPONENTS;
-  s.meta = reinterpret_cast<int*>(base + off);
+  s.meta = reinterpret_cast<int*>(base + off); off += sizeof(int) * nline * 3;
+  off = (off + sizeof(R) - 1) / sizeof(R) * sizeof(R);
+  s.dlam = reinterpret_cast<R*>(base + off);
   s.maxd = maxd;
   return s;
 }
 
+// The per-thread line offsets live in shared memory ([line][thread], one
+// bank per thread): as a runtime-indexed register array they took a stack
+// frame and pushed the FP32 kernel into spills.
 template <typename R>
-size_t smem_bytes(int nline, int maxd) {
+size_t smem_bytes(int nline, int maxd, int block) {
   return sizeof(double) * nline + sizeof(R) * GF_N * maxd + sizeof(R) * nline * LF_N * maxd +
          2 * sizeof(R) * nline * PYRH_MAX_COMPONENTS + sizeof(int) * nline * PYRH_MAX_COMPONENTS +
-         sizeof(int) * nline * 3 + 16;
+         sizeof(int) * nline * 3 + sizeof(R) + sizeof(R) * nline * block + 16;
 }
 
 struct Work {
@@ -88,7 +94,8 @@ struct Opacity {
   int nl;
   int nline;
   unsigned inwin;  // bit l: line l inside its window at this wavelength
-  R dlam[PYRH_MAX_LINES];
+  const R* dlam;   // lambda - lambda0 of line l at dlam[l * stride]
+  int stride;
 
   __device__ __forceinline__ void operator()(int k, R& chi, R S[4], R K6[6]) const {
     const int maxd = sm->maxd;
@@ -99,7 +106,7 @@ struct Opacity {
     for (int l = 0; l < nline; ++l) {
       if (!((inwin >> l) & 1u)) continue;
       const R* lp = sm->lp + (size_t)l * LF_N * maxd;
-      const R v = dlam[l] * lp[LF_INVVB * maxd + k] + lp[LF_VSHIFT * maxd + k];
+      const R v = dlam[l * stride] * lp[LF_INVVB * maxd + k] + lp[LF_VSHIFT * maxd + k];
       const R a = lp[LF_ADAMP * maxd + k];
       const R chil = lp[LF_CHI * maxd + k], etal = lp[LF_ETA * maxd + k];
       if (a < R(0)) {  // Grad == 0: Doppler core only (kurucz.c:776-779)
@@ -471,10 +478,12 @@ __device__ __forceinline__ void synth_wavelength(const LteArgs& args, const Smem
     op.chi_c = static_cast<const R*>(args.chi_c) + args.cont_off[p] + la;
     op.eta_c = static_cast<const R*>(args.eta_c) + args.cont_off[p] + la;
     op.inwin = 0u;
+    op.dlam = sm.dlam + threadIdx.x;
+    op.stride = blockDim.x;
     bool pol = false;
     for (int l = 0; l < nline; ++l) {
       const double dl = lam - sm.lam0[l];
-      op.dlam[l] = R(dl);
+      sm.dlam[l * blockDim.x + threadIdx.x] = R(dl);
       if (fabs(sm.lam0[l] - lam) <= dlc && sm.meta[3 * l + 2]) {
         op.inwin |= 1u << l;
         pol |= (sm.meta[3 * l + 1] != 0);
@@ -630,7 +639,7 @@ lte_stokes_kernel(LteArgs args) {
 
 template <typename R>
 static cudaError_t launch_t(const LteArgs& a, int block, int grid, cudaStream_t st) {
-  const size_t sm = smem_bytes<R>(a.nline, a.maxd);
+  const size_t sm = smem_bytes<R>(a.nline, a.maxd, block);
   if (a.magneto_optical) {
     auto k = lte_stokes_kernel<R, true>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -645,8 +654,9 @@ static cudaError_t launch_t(const LteArgs& a, int block, int grid, cudaStream_t 
   return cudaGetLastError();
 }
 
-size_t lte_smem_bytes(int precision, int nline, int maxd) {
-  return precision == PYRH_FP32 ? smem_bytes<float>(nline, maxd) : smem_bytes<double>(nline, maxd);
+size_t lte_smem_bytes(int precision, int nline, int maxd, int block) {
+  return precision == PYRH_FP32 ? smem_bytes<float>(nline, maxd, block)
+                                : smem_bytes<double>(nline, maxd, block);
 }
 
 cudaError_t launch_lte_stokes(const LteArgs& a, int block, int grid, cudaStream_t st) {

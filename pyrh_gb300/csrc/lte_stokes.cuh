@@ -47,7 +47,7 @@ constexpr int rf_max_threads(int precision, int mode = -1) {
 }
 cudaError_t launch_lte_rf(const RfArgs &a, int block, int grid, cudaStream_t st);
 
-size_t lte_smem_bytes(int precision, int nline, int maxd);
+size_t lte_smem_bytes(int precision, int nline, int maxd, int block);
 cudaError_t launch_lte_stokes(const LteArgs &a, int block, int grid, cudaStream_t st);
 
 }  // namespace pyrh
