@@ -29,9 +29,10 @@ METRIC = ("pixel·λ·μ formal solutions/s and RF gradients/s vs plain FP64 "
           "GPU, at 1e-4 rel err")
 UNIT = "pixel*lambda*mu/s"
 WORKLOAD = "batched LTE Stokes synthesis: 16384 atm x 71 depths x 2x112 lambda, mu=1, FP32"
-# DRAM bytes (read + write) per atmosphere of one lte_stokes_kernel launch:
-# ncu, 2048 atmospheres, 285.6 MB + 76.5 MB (profiles/lte_stokes_kernel_batched_16384x224.md).
-TRAFFIC_PER_ATM = (285.631488e6 + 76.459520e6) / 2048
+# ncu figures of the synthesis kernel (DRAM traffic, FP32 flops), recorded
+# with the digest of the kernel sources they were measured on; reported only
+# while those sources are unchanged.
+NCU_TRAFFIC = os.path.join(HERE, "pyrh_gb300", "data", "ncu_traffic.json")
 
 
 def parse():
@@ -45,6 +46,7 @@ def parse():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-rf", action="store_true")
     ap.add_argument("--skip-nlte", action="store_true")
+    ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--rf-natm", type=int, default=4096)
     ap.add_argument("--nlte-natm", type=int, default=1024)
     return ap.parse_args()
@@ -131,6 +133,76 @@ def cpu_baseline_port(batch, nthreads, seconds):
                       f"FP64 oracle (oracle/rt_oracle.c), {t:.1f} s", "seconds": t}
 
 
+def _ncu_record(kernel: str):
+    from pyrh_gb300 import build as B
+    if not os.path.exists(NCU_TRAFFIC):
+        return None, "no ncu capture recorded"
+    with open(NCU_TRAFFIC) as f:
+        rec = json.load(f).get(kernel)
+    if not rec:
+        return None, "no ncu capture recorded for this kernel"
+    if rec["sources_digest"] != B.sources_digest(rec["sources"]):
+        return None, "kernel sources changed since the recorded ncu capture"
+    return rec, None
+
+
+def measured_traffic(kernel: str, natm: int):
+    """DRAM bytes of one launch over natm atmospheres from the recorded ncu
+    capture of `kernel` (scaled by atmospheres), or None when the kernel's
+    sources changed since that capture."""
+    rec, why = _ncu_record(kernel)
+    if rec is None:
+        return None, why
+    per_atm = (rec["dram_bytes_read"] + rec["dram_bytes_write"]) / rec["atmospheres"]
+    return per_atm * natm, (f"ncu dram__bytes_read+write of one launch at {rec['atmospheres']} "
+                            f"atmospheres, scaled by atmospheres ({rec['command']})")
+
+
+def fp32_flops_per_unit(kernel: str):
+    """FP32 flops per (pixel, wavelength) of `kernel` (FADD + FMUL + 2 FFMA
+    thread instructions of the recorded ncu capture), or None."""
+    rec, _ = _ncu_record(kernel)
+    if rec is None:
+        return None
+    return rec["fp32_flops"] / (rec["atmospheres"] * rec["lambda_per_atm"])
+
+
+def lte_accuracy(batch, db, pk, lines, nline, local, sp, nsample=16):
+    """Error of the timed FP32 batch: the FP64 kernel on the same inputs, and
+    the FP64 kernel against the FP64 oracle on a sample of atmospheres."""
+    import torch
+    from oracle import oracle as O
+    from pyrh_gb300 import _lib as L
+    from pyrh_gb300 import lte
+    natm, nl = batch["T"].shape[0], pk.max_nlam
+    pk64 = lte.pack_uniform(batch, nline, L.PYRH_FP64)
+    d64 = lte.DeviceBatch(pk64, lines, nline, device=f"cuda:{local}")
+    cfg64 = lte.make_config(precision=L.PYRH_FP64, mu=1.0, vmicro_char=batch["vmicro_char"])
+    d64.run(cfg64, sp)
+    torch.cuda.synchronize()
+    s64 = d64.out.view(natm, 4, nl)
+    s32 = db.out.view(natm, 4, nl).double()
+    ic = s64[:, 0].amax(dim=1)[:, None, None]
+    err_ic = ((s32 - s64).abs() / ic).amax(dim=(0, 2)).cpu().numpy()
+    rel_I = float(((s32[:, 0] - s64[:, 0]).abs() / s64[:, 0].abs()).max())
+    sub = {k: (v[:nsample] if isinstance(v, np.ndarray) and v.ndim and v.shape[0] == natm
+               else v) for k, v in batch.items()}
+    sub["chi_c"] = np.ascontiguousarray(batch["chi_c"][:nsample].transpose(0, 2, 1), np.float64)
+    sub["eta_c"] = np.ascontiguousarray(batch["eta_c"][:nsample].transpose(0, 2, 1), np.float64)
+    sub["magneto_optical"] = 0
+    sub["moving"] = 1
+    ref = O.lte_synth_batch(sub, os.cpu_count() or 1, md_float=False)
+    g = s64[:nsample].cpu().numpy()
+    err_or = float((np.abs(g - ref) / ref[:, 0].max(axis=1)[:, None, None]).max())
+    del d64
+    return {"fp32_vs_fp64_max_abs_over_Ic": {s: float(e) for s, e in zip("IQUV", err_ic)},
+            "fp32_vs_fp64_max_rel_I": rel_I,
+            "fp64_vs_oracle_max_abs_over_Ic": err_or,
+            "oracle_sample_atmospheres": nsample,
+            "metric": f"|S_fp32 - S_fp64| / I_c per atmosphere (I_c = max I of the atmosphere), "
+                      f"over all {natm} atmospheres and wavelengths; rel_I = |dI| / I per point"}
+
+
 def _events_ms(fn, stream, n):
     import torch
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -183,6 +255,24 @@ def rf_measure(natm, local, stream, steps, warmup):
         RF.chi2_grad(dev, cfg, obs, w, sp)
         fixed_ms = _events_ms(lambda: RF.chi2_grad(dev, cfg, obs, w, sp), stream, steps)
         dev.struct.setup_dT = held
+    # FP32 gradient against the FP64 gradient of the same atmospheres
+    nchk = min(natm, 256)
+    nd = dev.pk.total_depth // natm
+    with torch.cuda.stream(stream):
+        g32 = RF.chi2_grad(dev, cfg, obs, w, sp)[1].view(6, natm, nd)[:, :nchk].double()
+        sub = {k: (v[:nchk] if isinstance(v, np.ndarray) and v.ndim and v.shape[0] == natm
+                   else v) for k, v in batch.items()}
+        d64 = lte.DeviceBatch(lte.pack_uniform(sub, nline, L.PYRH_FP64), lines, nline,
+                              device=f"cuda:{local}")
+        cfg64 = lte.make_config(precision=L.PYRH_FP64, mu=1.0, vmicro_char=batch["vmicro_char"])
+        g64 = RF.chi2_grad(d64, cfg64, obs.view(natm, -1)[:nchk].reshape(-1).double(),
+                           w.view(natm, -1)[:nchk].reshape(-1).double(), sp)[1]
+        g64 = g64.view(6, nchk, nd)
+    torch.cuda.synchronize()
+    diff = (g32 - g64).abs().amax(dim=2)
+    per_atm = (diff / g64.abs().amax(dim=2)).amax(dim=1).cpu().numpy()
+    batch_scale = (diff.amax(dim=1) / g64.abs().amax(dim=(1, 2))).cpu().numpy()
+    del d64
     units = natm * nl
     return {"workload": f"chi^2 gradient and response functions: {natm} atm x 71 depths x "
                         f"{nl} lambda, FP32, targets from perturbed copies + noise 1e-3 I_c; "
@@ -193,45 +283,100 @@ def rf_measure(natm, local, stream, steps, warmup):
             "gradient_cost_vs_forward": grad_ms / fwd_ms,
             "ms_chi2_gradient_setup_fixed": fixed_ms,
             "ms_response_functions": rf_ms,
+            "gradient_fp32_vs_fp64_rel_err": {p: float(e) for p, e in zip(RF.PARAMS, per_atm)},
+            "gradient_fp32_vs_fp64_rel_err_batch_scale": {p: float(e) for p, e in
+                                                          zip(RF.PARAMS, batch_scale)},
+            "gradient_error_metric": f"{nchk} atmospheres, per parameter: max over atmospheres "
+                                     "of max_depth |g32 - g64| / max_depth |g64| (the weakest "
+                                     "fields dominate: their Q, U, V are small differences of "
+                                     "Zeeman components), and max |g32 - g64| / max |g64| over "
+                                     "the whole sample",
             "rf_bytes_written": int(4 * 6 * 71 * units * 4)}
 
 
-def nlte_measure(natm, local):
-    """Batched NLTE MALI (C4 shapes): natm atmospheres cycled from the three
-    reference fixtures (82, 50 and 120 depths; 787, 629 and 989 wavelengths;
-    five rays; Ng order 2 every 5 iterations after 5), each solved
-    independently in one batch.  Converged atmospheres per second and the
-    largest population error against the reference's converged populations
-    at the same convergence limit."""
+def nlte_oracle_solve(atms, nthreads):
+    """Converged populations and iteration counts of the FP64 NLTE oracle
+    (oracle/nlte_oracle.c, one atmosphere per thread), and its wall time."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(nthreads) as ex:
+        res = list(ex.map(O.nlte_solve, atms))
+    return [r[0] for r in res], [int(r[2]) for r in res], time.perf_counter() - t0
+
+
+def nlte_measure(natm, local, nsample=32):
+    """Batched uneven NLTE (the six-level atom, five rays, Ng order 2 every 5
+    iterations after 5): natm atmospheres with 50..150 depths and 700..1100
+    wavelengths, generated from the reference's NLTE set-ups with the
+    batched workload's T and v_los perturbations, solved in one batch.
+    Converged atmospheres per second, FP32 against FP64 on the whole batch,
+    both against the FP64 oracle on a sample, and the oracle's own rate on
+    the host cores (the CPU baseline of this leg)."""
     import torch
     from pyrh_gb300 import _lib as L
-    from pyrh_gb300 import nlte
+    from pyrh_gb300 import nlte, workload
     names = ["nlte_c1", "nlte_c4_50", "nlte_c4_120"]
-    gold = [dict(np.load(os.path.join(HERE, "tests", "golden", n + ".npz"))) for n in names]
-    atms = [gold[i % 3] for i in range(natm)]
-    src = [i % 3 for i in range(natm)]
-    out = {"workload": f"batched NLTE: {natm} atmospheres (50/82/120 depths, 629-989 lambda, "
-                       "5 rays, 6-level atom), formal solution FP32, rates/LU/Ng FP64"}
+    bases = [dict(np.load(os.path.join(HERE, "tests", "golden", n + ".npz"))) for n in names]
+    atms = workload.nlte_batch(bases, natm, seed=4096)
+    nd = [len(a["T"]) for a in atms]
+    ns = [len(a["lambda"]) for a in atms]
+    out = {"workload": f"batched uneven NLTE: {natm} atmospheres, {min(nd)}-{max(nd)} depths, "
+                       f"{min(ns)}-{max(ns)} wavelengths, 5 rays, 6-level atom (5 lines, 5 "
+                       "continua); T nodes +-300 K and v_los +-3 km/s on the reference's NLTE "
+                       "set-ups re-gridded per atmosphere"}
+    pops, its = {}, {}
     for prec, tag in ((L.PYRH_FP32, "fp32"), (L.PYRH_FP64, "fp64")):
-        cfg = nlte.make_config(gold[0], prec)
+        cfg = nlte.make_config(atms[0], prec)
         pk = nlte.pack(atms, cfg.nrays)
         dev = nlte.DeviceNlte(pk, cfg, device=f"cuda:{local}")
         st = dev.solve(cfg)                      # warm-up (first-touch of the workspace)
-        dev.reset()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        st = dev.solve(cfg)
-        torch.cuda.synchronize()
-        t = time.perf_counter() - t0
-        its = dev.iterations.cpu().numpy()
-        pops = dev.populations()
-        err = max(float(np.abs(pops[i] / gold[src[i]]["n_final"] - 1).max()) for i in range(natm))
+        runs, raw = [], []
+        for _ in range(2 if prec == L.PYRH_FP32 else 1):
+            dev.reset()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = dev.solve(cfg)
+            torch.cuda.synchronize()
+            runs.append(time.perf_counter() - t0)
+            raw.append(dev.t["n"].cpu().numpy().copy())
+        t = min(runs)
+        it = dev.iterations.cpu().numpy()
         out[tag] = {"status": int(st), "seconds": t, "converged_atm_per_s": natm / t,
-                    "iterations_min_max": [int(its.min()), int(its.max())],
-                    "max_population_rel_err_vs_reference": err,
+                    "iterations_min_max": [int(it.min()), int(it.max())],
                     "launches": int(L.lib().pyrh_last_launch_count())}
+        if prec == L.PYRH_FP32:
+            out[tag]["bit_identical_rerun"] = bool(np.array_equal(raw[0], raw[1]))
+        pops[tag], its[tag] = dev.populations(), it
         del dev
         torch.cuda.empty_cache()
+    p32, p64 = pops["fp32"], pops["fp64"]
+    errs = np.array([float(np.abs(a / b - 1).max()) for a, b in zip(p32, p64)])
+    same = np.asarray(its["fp32"]) == np.asarray(its["fp64"])
+    out["fp32_vs_fp64_max_population_rel_err"] = float(errs.max())
+    # an FP32 run that meets the convergence limit one iteration earlier or
+    # later than the FP64 run stops at another point of the same path
+    out["fp32_vs_fp64_by_iteration_count"] = {
+        "same_count_atmospheres": int(same.sum()),
+        "same_count_max_rel_err": float(errs[same].max()) if same.any() else None,
+        "different_count_atmospheres": int((~same).sum()),
+        "different_count_max_rel_err": float(errs[~same].max()) if (~same).any() else None}
+    nthreads = os.cpu_count() or 1
+    n_or, it_or, t_or = nlte_oracle_solve(atms[:nsample], nthreads)
+    out["oracle_sample"] = {
+        "atmospheres": nsample,
+        "fp64_max_population_rel_err": max(float(np.abs(p64[i] / n_or[i] - 1).max())
+                                           for i in range(nsample)),
+        "fp32_max_population_rel_err": max(float(np.abs(p32[i] / n_or[i] - 1).max())
+                                           for i in range(nsample)),
+        "fp64_same_iteration_count": bool(all(int(its["fp64"][i]) == it_or[i]
+                                              for i in range(nsample))),
+        "fp32_iteration_count_diff_max": int(max(abs(int(its["fp32"][i]) - it_or[i])
+                                                 for i in range(nsample)))}
+    out["cpu_baseline"] = {"value": nsample / t_or, "unit": "converged atmospheres/s",
+                           "cores": nthreads, "kind": "port",
+                           "sample": f"{nsample} of the {natm} atmospheres, FP64 NLTE oracle "
+                                     f"(oracle/nlte_oracle.c), one per thread, {t_or:.1f} s"}
     return out
 
 
@@ -324,12 +469,31 @@ def main():
     # algorithmic bytes of one launch: every input array once + the output
     alg_bytes = sum(a.nbytes for a in pk.arrays.values()) + db.out.numel() * db.out.element_size()
     achieved = alg_bytes / (ms / 1e3) / 1e9
+    traffic, traffic_src = measured_traffic("lte_stokes_kernel<float,false>", natm)
+    # the FP32 roofline: SMs x 128 FP32 lanes x 2 flops (FMA) x the SM clock
+    # sampled during the timed region
+    fpu = fp32_flops_per_unit("lte_stokes_kernel<float,false>")
+    props = torch.cuda.get_device_properties(local)
+    clock_hz = (clk.get("sm_mhz") or 2070.0) * 1e6
+    fp32_peak = props.multi_processor_count * 128 * 2 * clock_hz / 1e12
+    fp32 = None
+    if fpu is not None:
+        fp32_ach = fpu * units / (ms / 1e3) / 1e12      # one GPU's launch
+        fp32 = {"achieved": fp32_ach, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": fp32_ach / fp32_peak, "flops_per_unit": fpu,
+                "peak_derivation": f"{props.multi_processor_count} SMs x 128 FP32 lanes x 2 "
+                                   f"flops x {clock_hz / 1e6:.0f} MHz (sampled SM clock)",
+                "flops_source": "ncu FADD + FMUL + 2 FFMA thread instructions of one launch "
+                                "(pyrh_gb300/data/ncu_traffic.json)"}
     peaks_path = os.path.join(HERE, "MEASURED_PEAKS.json")
     peak, peak_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):
         with open(peaks_path) as f:
             peak = float(json.load(f)["hbm_gbs"])
         peak_src = "measured"
+
+    accuracy = (lte_accuracy(batch, db, pk, lines, nline, local, sp)
+                if rank == 0 and not args.skip_accuracy else None)
 
     # ---- end to end through the host-buffer C ABI (pinned host memory) ----
     pinned = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory()
@@ -424,15 +588,14 @@ def main():
                 "clocks": clk, "e2e": e2e, "gpu_launches": launches, "plan": tile,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak,
-                             "traffic": TRAFFIC_PER_ATM * natm,
-                             "traffic_source": "ncu dram__bytes_read+write of one launch at "
-                                               "2048 atmospheres, scaled by atmospheres "
-                                               "(profiles/lte_stokes_kernel_batched_16384x224.md)",
+                             "traffic": traffic, "traffic_source": traffic_src,
                              "peak_source": peak_src, "alg_bytes_per_launch": alg_bytes,
                              "kernel": "lte_stokes_kernel<float,false>",
-                             "note": "FP32-pipe bound (ncu: 70 % issue, 45 % FMA pipe); "
-                                     "the HBM fraction is small by construction"},
-                "cpu_baseline": cpu}
+                             "fp32": fp32,
+                             "note": "bound by FP32 issue, not HBM: the fp32 entry is the "
+                                     "roofline that binds; the HBM fraction is small by "
+                                     "construction"},
+                "cpu_baseline": cpu, "accuracy": accuracy}
         line.update(extra)
         print(json.dumps(line), flush=True)
     if dist:

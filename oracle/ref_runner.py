@@ -28,7 +28,20 @@ REF_LIB = os.path.join(HERE, "_ref", "librh_ref.so")
 # rh/bezier_aux.c:235-328 (what the reference compiles to on Arm) instead of
 # the SSE reciprocal-estimate inverse of rh/bezier_aux.c:133-232.
 REF_LIB_PORTABLE = os.path.join(HERE, "_ref", "portable", "librh_ref.so")
-REF_ROOT = os.environ.get("PYRH_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_root() -> str:
+    """The reference checkout: PYRH_REFERENCE_ROOT, else the default of the
+    build recipe oracle/Makefile.ref; empty when neither holds the sources."""
+    env = os.environ.get("PYRH_REFERENCE_ROOT")
+    if env:
+        return env if os.path.isdir(os.path.join(env, "rh")) else ""
+    r = subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), "print-ref"],
+                       capture_output=True, text=True)
+    return r.stdout.strip() if r.returncode == 0 else ""
+
+
+REF_ROOT = reference_root()
 
 _P = C.POINTER(C.c_double)
 
