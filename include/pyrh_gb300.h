@@ -511,6 +511,57 @@ double pyrh_gaunt_bf(double lambda, double n_eff, int32_t charge);
 pyrh_status pyrh_cont_alpha(const pyrh_atom *atom, int32_t kr, const double *lam, int32_t n,
                             double *alpha);
 
+/* Kurucz line list (readKuruczLines, rh/kurucz.c:121-430): one pyrh_line per
+   record of the list text (fixed columns of the RLK format; the air
+   wavelength converted to vacuum, gf to Aji/Bji/Bij, damping constants,
+   isotope and hyperfine fractions), with the van der Waals cross-section
+   from ABO coefficients in the record, Barklem's tables (getBarklemcross,
+   rh/barklem.c:139-197) or Unsold's formula (getUnsoldcross,
+   rh/kurucz.c:985-1020), and the Zeeman pattern of polarizable lines
+   (RLKZeeman, rh/kurucz.c:832-920).  The element data that the reference
+   reads from its abundance and partition-function files come from the
+   caller, indexed by atomic number - 1 (hydrogen and helium at least). */
+#define PYRH_ELEM_MAX_STAGES 4
+
+typedef struct {
+  double weight;                     /* amu */
+  double abund;                      /* number abundance relative to hydrogen */
+  int32_t nstage;                    /* ionisation stages with data */
+  int32_t abundance_set;
+  double ionpot[PYRH_ELEM_MAX_STAGES];   /* J */
+} pyrh_element;
+
+typedef struct {
+  int32_t n1, n2;                    /* rows (lower level neff), columns (upper) */
+  double neff1_0, neff2_0;           /* first effective quantum numbers; step 0.1 */
+  const double *cross, *alpha;       /* [n1][n2] */
+} pyrh_barklem_table;
+
+typedef struct {
+  int32_t stokes;                    /* atmos.Stokes (pyrh: always TRUE) */
+  int32_t ls_lande;                  /* LS_LANDE */
+  const pyrh_element *elements;
+  int32_t nelem;
+  const pyrh_barklem_table *barklem[3];   /* s-p, p-d, d-f tables or NULL */
+  int32_t nloggf;                    /* log gf overrides by record index */
+  const int32_t *loggf_ids;
+  const double *loggf_values;
+} pyrh_kurucz_config;
+
+/* What a record gives beyond pyrh_line (for callers and tests). */
+typedef struct {
+  int32_t pt_index, stage;
+  double gj, Ej, gL_i, gL_j;
+} pyrh_kurucz_extra;
+
+/* Parses a Barklem table file (readBarklemTable, rh/barklem.c:61-135; type
+   0 = s-p, 1 = p-d, 2 = d-f) into caller arrays of n1 x n2 values and
+   fills `table` to point at them. */
+pyrh_status pyrh_barklem_parse(const char *text, int32_t type, double *cross, double *alpha,
+                               pyrh_barklem_table *table);
+pyrh_status pyrh_kurucz_read(const char *text, const pyrh_kurucz_config *cfg, pyrh_line *lines,
+                             pyrh_kurucz_extra *extra, int32_t cap, int32_t *nline);
+
 /* Per-depth NLTE set-up of a batch for one model atom, on the device (one
    thread per depth point): LTE populations (LTEpops, rh/ltepops.c:33-109),
    the collision rate matrix (CollisionRate, rh/collision.c:450-700: OMEGA,

@@ -322,6 +322,42 @@ int harness_dump_lte(const char *cwd, double mu, int Ndep, const double *atm,
     }
   }
   write_f64(outdir, "line_const", lc, 24L * atmos.Nrlk);
+
+  /* What the line-list reader takes besides the list: the element data of
+     each line (weight, stages, abundance, abundance flag, ionisation
+     potentials of the first four stages), hydrogen's and helium's weight
+     and abundance, and the three Barklem tables as readBarklemTable parsed
+     them (rows, columns, first effective quantum numbers, then cross and
+     alpha, row-major). */
+  double *eld = (double *) calloc(8L * (atmos.Nrlk > 0 ? atmos.Nrlk : 1), sizeof(double));
+  for (int n = 0; n < atmos.Nrlk; n++) {
+    Element *el = &atmos.elements[atmos.rlk_lines[n].pt_index - 1];
+    double *E = eld + 8L * n;
+    E[0] = el->weight; E[1] = el->Nstage; E[2] = el->abund; E[3] = el->abundance_set;
+    for (int st = 0; st < 4; st++) E[4 + st] = (st < el->Nstage) ? el->ionpot[st] : 0.0;
+  }
+  write_f64(outdir, "rlk_element", eld, 8L * (atmos.Nrlk > 0 ? atmos.Nrlk : 1));
+  free(eld);
+  double hhe[4] = {atmos.elements[0].weight, atmos.elements[0].abund,
+                   atmos.elements[1].weight, atmos.elements[1].abund};
+  write_f64(outdir, "rlk_hhe", hhe, 4);
+  {
+    enum Barklemtype types[3] = {SP, PD, DF};
+    const char *names[3] = {"barklem_sp", "barklem_pd", "barklem_df"};
+    for (int t = 0; t < 3; t++) {
+      Barklemstruct bs;
+      if (!readBarklemTable(types[t], &bs)) continue;
+      long n12 = (long) bs.N1 * bs.N2;
+      double *tb = (double *) malloc((4 + 2 * n12) * sizeof(double));
+      tb[0] = bs.N1; tb[1] = bs.N2; tb[2] = bs.neff1[0]; tb[3] = bs.neff2[0];
+      for (long e = 0; e < n12; e++) {
+        tb[4 + e] = bs.cross[0][e];
+        tb[4 + n12 + e] = bs.alpha[0][e];
+      }
+      write_f64(outdir, names[t], tb, 4 + 2 * n12);
+      free(tb);
+    }
+  }
   write_f64(outdir, "line_pops", lpop, 2L * atmos.Nrlk * Nspace);
   write_f64(outdir, "zeeman", zm, 3L * atmos.Nrlk * (maxcomp > 0 ? maxcomp : 1));
   write_i32(outdir, "zeeman_n", zn, atmos.Nrlk > 0 ? atmos.Nrlk : 1);

@@ -287,6 +287,15 @@ def read_dump(outdir: str) -> dict:
     mc = max(maxcomp, 1)
     d["zeeman"] = f64("zeeman").reshape(nrlk, 3, mc)
     d["zeeman_n"] = i32("zeeman_n")[:nrlk]
+    # inputs of the line-list reader (element data, Barklem tables), when
+    # the harness wrote them
+    if os.path.exists(os.path.join(outdir, "rlk_element.f64")):
+        d["rlk_element"] = f64("rlk_element").reshape(-1, 8)[:nrlk]
+        d["rlk_hhe"] = f64("rlk_hhe")
+        for t in ("sp", "pd", "df"):
+            path = os.path.join(outdir, f"barklem_{t}.f64")
+            if os.path.exists(path):
+                d[f"barklem_{t}"] = np.fromfile(path)
     return d
 
 

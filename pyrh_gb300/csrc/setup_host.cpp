@@ -526,3 +526,394 @@ pyrh_status pyrh_cont_alpha(const pyrh_atom* a, int32_t kr, const double* lam, i
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// Kurucz line list (readKuruczLines, rh/kurucz.c:121-430), with the van der
+// Waals cross-sections of Barklem's tables (getBarklemcross, getABOcross,
+// rh/barklem.c:139-225, interpolated by cubic convolution as
+// rh/cubeconvol.c:31-151 does) or Unsold's formula (getUnsoldcross,
+// rh/kurucz.c:985-1020), and the Zeeman pattern of polarizable lines
+// (RLKZeeman, rh/kurucz.c:832-920; ZeemanStrength and Lande,
+// rh/zeeman.c:128-200).
+// ------------------------------------------------------------------------
+
+namespace {
+
+constexpr double kAMU_ = 1.6605402E-27;
+constexpr double kKB_ = 1.380658E-23;
+constexpr double kRBOHR_ = 5.29177349E-11;
+constexpr double kABARH_ = 7.42E-41;
+constexpr double kMILLI = 1.0E-03;
+constexpr double kAIR_TO_VACUUM_LIMIT = 199.9352;
+constexpr double kDELTA_NEFF = 0.1;
+constexpr double kLG10 = 2.30258509299404568402;
+
+// 10^x as the reference evaluates it (exp of x ln 10)
+double pow10_ref(double x) { return exp(kLG10 * (x)); }
+
+// air_to_vacuum (rh/vacuumtoair.c), nm
+double air_to_vacuum(double la) {
+  if (la < kAIR_TO_VACUUM_LIMIT) return la;
+  const double sqwave = ((1.0E+07 / la) * (1.0E+07 / la));
+  const double increase = 1.0000834213E+00 + 2.406030E+06 / (1.30E+10 - sqwave) +
+                          1.5997E+04 / (3.89E+09 - sqwave);
+  return la * increase;
+}
+
+// Keys' cubic-convolution kernel
+void cc_kernel(double s, double* k) {
+  k[0] = -s * (1.0 - s * (2.0 - s)) / 2.0;
+  k[1] = 1.0 + s * s * (3.0 * s - 5.0) / 2.0;
+  k[2] = s * (1.0 + s * (4.0 - 3.0 * s)) / 2.0;
+  k[3] = s * s * (s - 1.0) / 2.0;
+}
+
+// Cubic convolution on the table f[Ny][Nx] at fractional indices (x, y),
+// the outermost rows and columns extrapolated linearly at the table's edges
+double cubeconvol(int Nx, int Ny, const double* f, double x, double y) {
+  int i, j;
+  double ux[4], uy[4], ip, jp;
+  if (x <= 0.0) { i = 0; cc_kernel(0.0, ux); }
+  else if (x >= (double)(Nx - 1)) { i = Nx - 2; cc_kernel(1.0, ux); }
+  else { cc_kernel(modf(x, &ip), ux); i = (int)ip; }
+  if (y <= 0.0) { j = 0; cc_kernel(0.0, uy); }
+  else if (y >= (double)(Ny - 1)) { j = Ny - 2; cc_kernel(1.0, uy); }
+  else { cc_kernel(modf(y, &jp), uy); j = (int)jp; }
+  // the 4x4 neighbourhood, rows j-1..j+2 and columns i-1..i+2
+  double c[4][4];
+  const bool lo_x = i == 0, hi_x = i == Nx - 2, lo_y = j == 0, hi_y = j == Ny - 2;
+  for (int m = 0; m < 4; ++m) {
+    const int row = j - 1 + m;
+    if ((lo_y && m == 0) || (hi_y && m == 3)) continue;
+    for (int n = 0; n < 4; ++n) {
+      const int col = i - 1 + n;
+      if ((lo_x && n == 0) || (hi_x && n == 3)) continue;
+      c[m][n] = f[(long)Nx * row + col];
+    }
+    if (lo_x) c[m][0] = 3.0 * (c[m][1] - c[m][2]) + c[m][3];
+    if (hi_x) c[m][3] = 3.0 * (c[m][2] - c[m][1]) + c[m][0];
+  }
+  if (lo_y)
+    for (int n = 0; n < 4; ++n) c[0][n] = 3.0 * (c[1][n] - c[2][n]) + c[3][n];
+  if (hi_y)
+    for (int n = 0; n < 4; ++n) c[3][n] = 3.0 * (c[2][n] - c[1][n]) + c[0][n];
+  double g = 0.0;
+  for (int m = 0; m < 4; ++m)
+    for (int n = 0; n < 4; ++n) g += c[m][n] * ux[n] * uy[m];
+  return g;
+}
+
+// RLKdeterminate (rh/kurucz.c:925-980): spin and orbital momentum from the
+// last word of a level label ("... z5P")
+bool rlk_term(const char* label, double* S, int* L) {
+  std::vector<std::string> w = words(label);
+  if (w.empty()) return false;
+  const std::string& last = w.back();
+  if (last.size() < 2) return false;
+  int multiplicity = 0;
+  char orbit[4] = {0};
+  if (sscanf(last.c_str() + last.size() - 2, "%d%1s", &multiplicity, orbit) != 2 ||
+      !isupper((unsigned char)orbit[0]))
+    return false;
+  *L = orbital(orbit[0]);
+  if (*L < 0) return false;
+  *S = (multiplicity - 1) / 2.0;
+  return true;
+}
+
+// ZeemanStrength (rh/zeeman.c:149-200)
+double zeeman_strength(double Ju, double Mu, double Jl, double Ml) {
+  const int q = (int)(Ml - Mu), dJ = (int)(Ju - Jl);
+  switch (dJ) {
+    case 0:
+      if (q == 0) return 2.0 * (Mu * Mu);
+      if (q == -1) return (Ju + Mu) * (Ju - Mu + 1.0);
+      return (Ju - Mu) * (Ju + Mu + 1.0);
+    case 1:
+      if (q == 0) return 2.0 * ((Ju * Ju) - (Mu * Mu));
+      if (q == -1) return (Ju + Mu) * (Ju + Mu - 1.0);
+      return (Ju - Mu) * (Ju - Mu - 1.0);
+    case -1:
+      if (q == 0) return 2.0 * (((Ju + 1.0) * (Ju + 1.0)) - (Mu * Mu));
+      if (q == -1) return (Ju - Mu + 1.0) * (Ju - Mu + 2.0);
+      return (Ju + Mu + 1.0) * (Ju + Mu + 2.0);
+  }
+  return -1.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+pyrh_status pyrh_barklem_parse(const char* text, int32_t type, double* cross, double* alpha,
+                               pyrh_barklem_table* table) {
+  // readBarklemTable (rh/barklem.c:61-135): three header lines, the cross
+  // table, the rest of that line and one more, the alpha table
+  static const int N1s[3] = {21, 18, 18}, N2s[3] = {18, 18, 18};
+  static const double neff1s[3] = {1.0, 1.3, 2.3}, neff2s[3] = {1.3, 2.3, 3.3};
+  if (!text || !cross || !alpha || !table || type < 0 || type > 2)
+    return fail(PYRH_ERR_ARG, "barklem_parse: arguments");
+  const int N1 = N1s[type], N2 = N2s[type];
+  const char* p = text;
+  auto skip_line = [&]() {
+    while (*p && *p != '\n') ++p;
+    if (*p) ++p;
+  };
+  for (int n = 0; n < 3; ++n) skip_line();
+  auto read_block = [&](double* dst) {
+    for (int e = 0; e < N1 * N2; ++e) {
+      char* end = nullptr;
+      dst[e] = strtod(p, &end);
+      if (end == p) return false;
+      p = end;
+    }
+    return true;
+  };
+  if (!read_block(cross)) return fail(PYRH_ERR_ARG, "barklem_parse: cross table short");
+  skip_line();
+  skip_line();
+  if (!read_block(alpha)) return fail(PYRH_ERR_ARG, "barklem_parse: alpha table short");
+  table->n1 = N1;
+  table->n2 = N2;
+  table->neff1_0 = neff1s[type];
+  table->neff2_0 = neff2s[type];
+  table->cross = cross;
+  table->alpha = alpha;
+  return PYRH_OK;
+}
+
+pyrh_status pyrh_kurucz_read(const char* text, const pyrh_kurucz_config* cfg, pyrh_line* lines,
+                             pyrh_kurucz_extra* extra, int32_t cap, int32_t* nline) {
+  if (!text || !cfg || !lines || !nline || cap < 0 || !cfg->elements || cfg->nelem < 2)
+    return fail(PYRH_ERR_ARG, "kurucz_read: arguments (hydrogen and helium needed)");
+  const double Cfac = 2.0 * kPi * (kQe / kEps0) * (kQe / kMe) / kC;
+  const pyrh_element& H = cfg->elements[0];
+  const pyrh_element& He = cfg->elements[1];
+  int n = 0;
+  const char* p = text;
+  int line_index = 0;
+  while (*p) {
+    const char* e = strchr(p, '\n');
+    const size_t len = e ? (size_t)(e - p) : strlen(p);
+    // fgets of RLK_RECORD_LENGTH + 1 bytes: at most 171 characters a record
+    std::string rec(p, len < 171 ? len : 171);
+    p = e ? e + 1 : p + len;
+    if (rec.empty() || rec[0] == '#') continue;
+    bool blank = true;
+    for (char c : rec)
+      if (!isspace((unsigned char)c)) { blank = false; break; }
+    if (blank) continue;
+    if (n >= cap) return fail(PYRH_ERR_ARG, "kurucz_read: more than %d lines", cap);
+    rec.resize(171, ' ');
+    const char* r = rec.c_str();
+    double lambda_air = 0, gf = 0, Ei = 0, Ej = 0, Ji = 0, Jj = 0;
+    char code[16] = {0};
+    if (sscanf(r, "%lf %lf %15s %lf", &lambda_air, &gf, code, &Ei) != 4 ||
+        sscanf(r + 53, "%lf", &Ej) != 1 || sscanf(r + 35, "%lf", &Ji) != 1 ||
+        sscanf(r + 63, "%lf", &Jj) != 1)
+      return fail(PYRH_ERR_ARG, "kurucz_read: record %d unreadable", line_index);
+    int pt_index = 0, stage = 0;
+    if (sscanf(code, "%d.%d", &pt_index, &stage) != 2 || pt_index < 1 || pt_index > cfg->nelem)
+      return fail(PYRH_ERR_ARG, "kurucz_read: element code %s of record %d", code, line_index);
+    const pyrh_element& el = cfg->elements[pt_index - 1];
+    Ei = fabs(Ei) * (kH * kC) / kCm;
+    Ej = fabs(Ej) * (kH * kC) / kCm;
+    const bool swap = Ej < Ei;
+    char labeli[11] = {0}, labelj[11] = {0};
+    double rEi, rEj;
+    if (swap) {
+      rEi = Ej; rEj = Ei;
+      memcpy(labeli, r + 69, 10);
+      memcpy(labelj, r + 41, 10);
+      std::swap(Ji, Jj);
+    } else {
+      rEi = Ei; rEj = Ej;
+      memcpy(labeli, r + 41, 10);
+      memcpy(labelj, r + 69, 10);
+    }
+    const double gi = 2 * Ji + 1, gj = 2 * Jj + 1;
+    // tabulated (air) wavelength; the upper energy follows from it
+    const double lambda0 = air_to_vacuum(lambda_air) * kNm;
+    rEj = rEi + (kH * kC) / lambda0;
+    double loggf = gf;
+    for (int k = 0; k < cfg->nloggf; ++k)
+      if (cfg->loggf_ids[k] == line_index) loggf = cfg->loggf_values[k];
+    const double Aji = Cfac / ((lambda0) * (lambda0)) * pow10_ref(loggf) / gj;
+    const double Bji = ((lambda0) * (lambda0) * (lambda0)) / (2.0 * kH * kC) * Aji;
+    const double Bij = (gj / gi) * Bji;
+    // orbital numbers of the levels, or ABO coefficients (kurucz.c:263-291)
+    int li = -1, lj = -1;
+    bool abo = false;
+    double a_abo = 0, s_abo = 0;
+    {
+      const int nr = sscanf(r + 160, "%lf %lf", &a_abo, &s_abo);
+      if (nr == 2) {
+        auto small = [](double x) { return x == 0.0 || x == 1.0 || x == 2.0 || x == 3.0; };
+        if (small(a_abo) || small(s_abo)) {
+          li = (int)a_abo;
+          lj = (int)s_abo;
+          if (swap) std::swap(li, lj);
+        } else {
+          abo = true;
+        }
+      }
+    }
+    double Si = 0, Sj = 0;
+    int Li = -1, Lj = -1;
+    const bool determined = rlk_term(labeli, &Si, &Li) && rlk_term(labelj, &Sj, &Lj);
+    bool polarizable = cfg->stokes && determined;
+    double Grad = 0, GStark = 0, GvdW = 0;
+    {
+      char g[19] = {0};
+      memcpy(g, r + 79, 18);
+      if (sscanf(g, "%lf %lf %lf", &Grad, &GStark, &GvdW) != 3)
+        return fail(PYRH_ERR_ARG, "kurucz_read: damping of record %d", line_index);
+    }
+    GStark = (GStark != 0.0) ? pow10_ref(GStark) * (kCm * kCm * kCm) : 0.0;
+    GvdW = (GvdW != 0.0) ? pow10_ref(GvdW) * (kCm * kCm * kCm) : 0.0;
+    // van der Waals cross-section
+    double cross = 0.0, alpha = 0.0;
+    int vdw = PYRH_VDW_KURUCZ;
+    const double reducedmass = kAMU_ / (1.0 / H.weight + 1.0 / el.weight);
+    const double meanvelocity = sqrt(8.0 * kKB_ / (kPi * reducedmass));
+    auto abo_scale = [&](double sigma, double a) {
+      const double crossmean = (kRBOHR_ * kRBOHR_) * pow(meanvelocity / 1.0E4, -a);
+      return sigma * 2.0 * pow(4.0 / kPi, a / 2.0) * exp(lgamma((4.0 - a) / 2.0)) *
+             meanvelocity * crossmean;
+    };
+    bool barklem = false;
+    if (abo) {
+      alpha = a_abo;
+      cross = abo_scale(s_abo, a_abo);
+      vdw = PYRH_VDW_BARKLEM;
+      barklem = true;
+    } else {
+      int t = -1;
+      if ((li == 0 && lj == 1) || (li == 1 && lj == 0)) t = 0;
+      if ((li == 1 && lj == 2) || (li == 2 && lj == 1)) t = 1;
+      if ((li == 2 && lj == 3) || (li == 3 && lj == 2)) t = 2;
+      const pyrh_barklem_table* bt = t >= 0 ? cfg->barklem[t] : nullptr;
+      if (bt && stage == 0 && stage < el.nstage) {
+        const double dEi = el.ionpot[stage] - rEi, dEj = el.ionpot[stage] - rEj;
+        if (dEi > 0.0 && dEj > 0.0) {
+          const double Z = (double)(stage + 1);
+          const double ERyd = kERyd / (1.0 + kMe / (el.weight * kAMU_));
+          double neff1 = Z * sqrt(ERyd / dEi), neff2 = Z * sqrt(ERyd / dEj);
+          if (li > lj) std::swap(neff1, neff2);
+          const double top1 = bt->neff1_0 + (bt->n1 - 1) * kDELTA_NEFF;
+          const double top2 = bt->neff2_0 + (bt->n2 - 1) * kDELTA_NEFF;
+          if (neff1 >= bt->neff1_0 && neff1 <= top1 && neff2 >= bt->neff2_0 && neff2 <= top2) {
+            std::vector<double> g1(bt->n1), g2(bt->n2);
+            for (int k = 0; k < bt->n1; ++k) g1[k] = bt->neff1_0 + k * kDELTA_NEFF;
+            for (int k = 0; k < bt->n2; ++k) g2[k] = bt->neff2_0 + k * kDELTA_NEFF;
+            int i1 = locate(bt->n1, g1.data(), neff1);
+            const double f1 = (double)i1 + (neff1 - g1[i1]) / kDELTA_NEFF;
+            int i2 = locate(bt->n2, g2.data(), neff2);
+            const double f2 = (double)i2 + (neff2 - g2[i2]) / kDELTA_NEFF;
+            const double c = cubeconvol(bt->n2, bt->n1, bt->cross, f2, f1);
+            alpha = cubeconvol(bt->n2, bt->n1, bt->alpha, f2, f1);
+            cross = abo_scale(c, alpha);
+            vdw = PYRH_VDW_BARKLEM;
+            barklem = true;
+          }
+        }
+      }
+    }
+    if (!barklem) {
+      // Unsold (kurucz.c:985-1020)
+      vdw = PYRH_VDW_KURUCZ;
+      if (stage <= el.nstage - 1 && stage < PYRH_ELEM_MAX_STAGES) {
+        const double Z = stage + 1;
+        const double deltaR = ((kERyd / (el.ionpot[stage] - rEj)) * (kERyd / (el.ionpot[stage] - rEj))) -
+                              ((kERyd / (el.ionpot[stage] - rEi)) * (kERyd / (el.ionpot[stage] - rEi)));
+        if (deltaR > 0.0) {
+          const double fourpieps0 = 4.0 * kPi * kEps0;
+          const double vrel35_H = pow(8.0 * kKB_ / (kPi * kAMU_ * el.weight) *
+                                          (1.0 + el.weight / H.weight), 0.3);
+          const double vrel35_He = pow(8.0 * kKB_ / (kPi * kAMU_ * el.weight) *
+                                           (1.0 + el.weight / He.weight), 0.3);
+          const double C625 = pow(2.5 * ((kQe * kQe) / fourpieps0) * (kABARH_ / fourpieps0) * 2 *
+                                      kPi * ((Z * kRBOHR_) * (Z * kRBOHR_)) / kH * deltaR,
+                                  0.4);
+          cross = 8.08 * (vrel35_H + He.abund * vrel35_He) * C625;
+          vdw = PYRH_VDW_UNSOLD;
+        }
+      }
+    }
+    Grad = (Grad != 0.0) ? pow10_ref(Grad) : Aji;
+    double iso_frac = 0.0, hfs_frac = 0.0;
+    int gLi = 0, gLj = 0;
+    if (sscanf(r + 108, "%lf", &iso_frac) != 1 || sscanf(r + 117, "%lf", &hfs_frac) != 1 ||
+        sscanf(r + 143, "%5d%5d", &gLi, &gLj) != 2)
+      return fail(PYRH_ERR_ARG, "kurucz_read: isotope or Lande fields of record %d", line_index);
+    iso_frac = pow10_ref(iso_frac);
+    hfs_frac = pow10_ref(hfs_frac);
+    double gL_i = gLi * kMILLI, gL_j = gLj * kMILLI;
+    if (swap) std::swap(gL_i, gL_j);
+    if (!cfg->ls_lande && cfg->stokes && gL_i != -99 * kMILLI && gL_j != -99 * kMILLI)
+      polarizable = true;
+    pyrh_line& L = lines[n];
+    memset(&L, 0, sizeof(L));
+    L.lambda0 = lambda0 / kNm;
+    L.Ei = rEi;
+    L.gi = gi;
+    L.Aji = Aji;
+    L.Bji = Bji;
+    L.Bij = Bij;
+    L.Grad = Grad;
+    L.GStark = GStark;
+    L.GvdWaals = GvdW;
+    L.cross = cross;
+    L.alpha = alpha;
+    L.vdwaals = vdw;
+    L.isotope_frac = iso_frac;
+    L.hyperfine_frac = hfs_frac;
+    L.weight = el.weight;
+    L.contributes = (stage < el.nstage - 1) && el.abundance_set;
+    L.polarizable = polarizable;
+    L.ncomp = 0;
+    if (polarizable) {
+      // RLKZeeman (kurucz.c:832-920)
+      const double Jl = (gi - 1.0) / 2.0, Ju = (gj - 1.0) / 2.0;
+      double gLl, gLu;
+      if (cfg->ls_lande) {
+        gLl = lande(Si, Li, Jl);
+        gLu = lande(Sj, Lj, Ju);
+      } else {
+        gLl = (gL_i == -99 * kMILLI) ? lande(Si, Li, Jl) : gL_i;
+        gLu = (gL_j == -99 * kMILLI) ? lande(Sj, Lj, Ju) : gL_j;
+      }
+      double norm[3] = {0, 0, 0};
+      int nc = 0;
+      for (double Ml = -Jl; Ml <= Jl; Ml++)
+        for (double Mu = -Ju; Mu <= Ju; Mu++)
+          if (fabs(Mu - Ml) <= 1.0) {
+            if (nc >= PYRH_MAX_COMPONENTS)
+              return fail(PYRH_ERR_UNSUPPORTED, "kurucz_read: record %d has more than %d "
+                          "Zeeman components", line_index, PYRH_MAX_COMPONENTS);
+            L.comp_q[nc] = (int)(Ml - Mu);
+            L.comp_shift[nc] = gLl * Ml - gLu * Mu;
+            L.comp_strength[nc] = zeeman_strength(Ju, Mu, Jl, Ml);
+            norm[L.comp_q[nc] + 1] += L.comp_strength[nc];
+            ++nc;
+          }
+      for (int c = 0; c < nc; ++c) L.comp_strength[c] /= norm[L.comp_q[c] + 1];
+      L.ncomp = nc;
+    }
+    if (extra) {
+      pyrh_kurucz_extra& X = extra[n];
+      X.pt_index = pt_index;
+      X.stage = stage;
+      X.gj = gj;
+      X.Ej = rEj;
+      X.gL_i = gL_i;
+      X.gL_j = gL_j;
+    }
+    ++n;
+    ++line_index;
+  }
+  *nline = n;
+  return PYRH_OK;
+}
+
+}  // extern "C"

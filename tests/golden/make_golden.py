@@ -392,11 +392,50 @@ def make_nlte(ref, wd):
     nlte_case("nlte_c4_120", ndep=120, nlambda_scale=1.25, dT=pert["dT"][1], vlos=-2.0)
 
 
+def make_kurucz(ref, wd):
+    """Inputs and outputs of the reference's Kurucz line-list reader
+    (readKuruczLines, RLKZeeman, the Barklem and Unsold cross-sections) for
+    the line lists of lte_c0 (Barklem s-p broadening), lte_broadening
+    (orbital numbers no table covers: Unsold; isotope and hyperfine
+    fractions) and lte_mixed (two lines that are not polarizable): the list
+    text, each line's element data, hydrogen and helium, the Barklem tables
+    as the reference parsed them, and the line constants and Zeeman patterns
+    it produced."""
+    logtau, T, ne, nH = base_c0(ref, wd)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH)
+    wave = wl.line_wavelengths(21, 0.05)
+    lists = {
+        "c0": wl.fe_linelist(),
+        "broadening": wl.fe_linelist([dict(wl.FE_LINES[0], orbital=(0, 2)),
+                                      dict(wl.FE_LINES[1], iso_log=-0.3, hfs_log=-0.1)]),
+        "mixed": wl.fe_linelist(sorted([dict(UNPOLARIZED, lam_vac=629.60),
+                                        dict(UNPOLARIZED, lam_vac=630.20), *wl.FE_LINES],
+                                       key=lambda L: L["lam_vac"])),
+    }
+    out = {}
+    for name, text in lists.items():
+        w = rr.scratch_dir()
+        rr.write_inputs(w, text)
+        dd = os.path.join(w, "dump")
+        ref.dump_lte(w, 1.0, atm, wave, dd)
+        d = rr.read_dump(dd)
+        out[f"{name}_text"] = np.array(text)
+        for k in ("line_const", "zeeman", "zeeman_n", "rlk_element", "rlk_hhe"):
+            out[f"{name}_{k}"] = d[k]
+        for t in ("sp", "pd", "df"):
+            if f"barklem_{t}" in d:
+                out[f"barklem_{t}"] = d[f"barklem_{t}"]
+        shutil.rmtree(w, ignore_errors=True)
+    path = os.path.join(HERE, "kurucz_lists.npz")
+    np.savez_compressed(path, **out)
+    print(f"kurucz_lists: {os.path.getsize(path) / 1e3:.0f} kB")
+
+
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
           "lte_static": make_lte_static, "lte_broadening": make_lte_broadening,
-          "nlte": make_nlte}
+          "nlte": make_nlte, "kurucz": make_kurucz}
 
 
 def main():

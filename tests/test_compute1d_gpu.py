@@ -84,3 +84,26 @@ def test_compute1d_loggf_override_and_rfs(golden, tmp_path):
         Im = C1.compute1d(cwd, 1.0, 0, fx["atm"], fx["wave"], ids, dn, setup=su)[0]
         ref = fx["fd_loggf"][l, 0]
         assert np.abs((Ip - Im) / (2 * h) - ref).max() < 1e-4 * np.abs(ref).max(), l
+
+
+@pytest.mark.parametrize("lst,name", [("c0", "lte_c0"), ("broadening", "lte_broadening"),
+                                      ("mixed", "lte_mixed")])
+def test_compute1d_from_the_line_list_text(golden, tmp_path, lst, name):
+    """The same synthesis with the line constants and Zeeman patterns read
+    from the Kurucz list text by pyrh_kurucz_read instead of the reference's
+    set-up dump: within 1e-5 of I_c of the reference's spectrum (FP64)."""
+    from pyrh_gb300 import kurucz as K
+    from test_kurucz import elements_of, tables_of
+    with np.load(os.path.join(os.path.dirname(__file__), "golden", "kurucz_lists.npz")) as f:
+        kz = {k: f[k] for k in f.files}
+    fx = golden(name)
+    lc, zm, zn = K.line_tables(*K.read_kurucz(str(kz[lst + "_text"]), elements_of(kz, lst),
+                                              tables_of(kz)))
+    su = setup_of(fx)
+    su.line_const, su.zeeman, su.zeeman_n = lc, zm, zn
+    cwd = keyword_dir(tmp_path, fx, "FULL_STOKES")
+    out = C1.compute1d(cwd, float(fx["mu"]), 0, fx["atm"], fx["wave"], setup=su)
+    ref = fx["stokes_ref_portable"]
+    ic = ref[0].max()
+    for s in range(4):
+        assert np.abs(out[s] - ref[s]).max() < 1e-5 * ic, s
