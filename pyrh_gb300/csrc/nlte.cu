@@ -348,18 +348,27 @@ __device__ __forceinline__ R bezier_sweep(const Op& op, const R* ds, int nd, int
   emit(k, I_last, R(w[0] - w[1] / dtau), R((1.0 - w[0]) + w[1] / dtau), Ieff_last, chi_c, cb_c);
   return I_last;
 }
-// Feautrier (feautrier.c:56-202) with P, Psi and 1 - Psi at every depth.
-// P may share storage with S, Psi with F and omPsi with zt: each is written
-// only after the last read of the array it shares.
+// Feautrier (feautrier.c:56-202) with P, Psi, 1 - Psi and the MALI
+// effective intensity P - Psi S_atom at every depth.  The effective
+// intensity is not formed as that difference (which loses most of its
+// digits in thick line cores, where P and Psi S_atom are both close to S):
+// with the downward elimination P_k = P_{k+1} / (1 + F_k) + zt_k and the
+// upward one P_k = P_{k-1} / (1 + G_k) + Zb_k, row k of the system gives
+//   P_k = Psi_k (S_k + A_k zt_{k-1} + C_k Zb_{k+1}),
+// so P_k - Psi_k S_atom,k = Psi_k (S_bg,k + A_k zt_{k-1} + C_k Zb_{k+1}), a sum
+// of positive terms.  P may share storage with S, Psi with F, 1 - Psi with zt
+// and Ieff with Sbg: each is written only after the last read of the array
+// it shares.
 template <typename R>
-__device__ R feautrier_full(const R* chi, const R* S, const R* ds, int nd, double muz,
-                            double B0, double B1, R* P, R* Psi, R* omPsi, R* F, R* zt) {
+__device__ R feautrier_full(const R* chi, const R* S, const R* Sbg, const R* ds, int nd,
+                            double B0, double B1, R* P, R* Psi, R* omPsi, R* Ieff, R* F, R* zt) {
   // dtau[k] = 0.5 (chi[k] + chi[k+1]) ds[k+1] for k = 0..nd-2 (ds already / mu)
   auto dtau = [&](int kk) { return R(0.5) * (chi[kk] + chi[kk + 1]) * ds[kk + 1]; };
   const R hN = R(B1 - (B0 - B1) / (double)dtau(nd - 2));
-  // rows: A1, C1, abc, St
+  // rows: -A1 P_{k-1} + (1 + A1 + C1) P_k - C1 P_{k+1} = S_k; the surface row
+  // has diagonal abc0 + C10, the bottom row abcN + A1N and source StN
   const R d0 = dtau(0);
-  R abc0 = R(1) + R(2) / d0, C10 = R(2) / (d0 * d0);
+  const R abc0 = R(1) + R(2) / d0, C10 = R(2) / (d0 * d0);
   F[0] = abc0 / C10;
   zt[0] = S[0] / (abc0 + C10);
   for (int k = 1; k < nd - 1; ++k) {
@@ -369,37 +378,48 @@ __device__ R feautrier_full(const R* chi, const R* S, const R* ds, int nd, doubl
     zt[k] = (S[k] + A1 * zt[k - 1]) / (C1 * (R(1) + F[k]));
   }
   const R dN = dtau(nd - 2);
-  const R abcN = R(1) + R(2) / dN, A1N = R(2) / (dN * dN), StN = S[nd - 1] + R(2) * hN / dN;
-  R Pk = (StN + A1N * zt[nd - 2]) / (abcN + A1N * (F[nd - 2] / (R(1) + F[nd - 2])));
-  // Psi by the upward G recurrence needs F[k-1]; compute P and Psi together
+  const R abcN = R(1) + R(2) / dN, A1N = R(2) / (dN * dN), bN = R(2) * hN / dN;
+  const R StN = S[nd - 1] + bN;
+  const R FoN = F[nd - 2] / (R(1) + F[nd - 2]);
+  R Pk = (StN + A1N * zt[nd - 2]) / (abcN + A1N * FoN);
+  // upward elimination, one step behind the downward back-substitution;
   // 1 - Psi = (denominator - 1) Psi, formed from the positive terms of the
   // denominator without cancellation
   R G = abcN / A1N;
+  R Zb = StN / (A1N * (R(1) + G));
   {
-    const R rest = R(2) / dN + A1N * F[nd - 2] / (R(1) + F[nd - 2]);
-    Psi[nd - 1] = R(1) / (R(1) + rest);
-    omPsi[nd - 1] = rest * Psi[nd - 1];
-  }
-  P[nd - 1] = Pk;
-  for (int k = nd - 2; k >= 0; --k) {
-    Pk = Pk / (R(1) + F[k]) + zt[k];
-    P[k] = Pk;
+    const R rest = R(2) / dN + A1N * FoN;
+    const R psi = R(1) / (R(1) + rest);
+    Ieff[nd - 1] = psi * (Sbg[nd - 1] + bN + A1N * zt[nd - 2]);
+    P[nd - 1] = Pk;
+    Psi[nd - 1] = psi;
+    omPsi[nd - 1] = rest * psi;
   }
   for (int k = nd - 2; k >= 1; --k) {
+    Pk = Pk / (R(1) + F[k]) + zt[k];
     const R dm = dtau(k - 1), dp = dtau(k), dmid = R(0.5) * (dp + dm);
     const R A1 = R(1) / (dmid * dm), C1 = R(1) / (dmid * dp);
-    const R rest = A1 * F[k - 1] / (R(1) + F[k - 1]) + C1 * G / (R(1) + G);
-    Psi[k] = R(1) / (R(1) + rest);
-    omPsi[k] = rest * Psi[k];
-    G = (R(1) + C1 * G / (R(1) + G)) / A1;
+    const R CG = C1 * G / (R(1) + G);
+    const R rest = A1 * F[k - 1] / (R(1) + F[k - 1]) + CG;
+    const R psi = R(1) / (R(1) + rest);
+    const R ieff = psi * (Sbg[k] + A1 * zt[k - 1] + C1 * Zb);
+    G = (R(1) + CG) / A1;
+    Zb = (S[k] + C1 * Zb) / (A1 * (R(1) + G));
+    P[k] = Pk;
+    Psi[k] = psi;
+    omPsi[k] = rest * psi;
+    Ieff[k] = ieff;
   }
   {
+    Pk = Pk / (R(1) + F[0]) + zt[0];
     const R rest = R(2) / d0 + C10 * G / (R(1) + G);
-    Psi[0] = R(1) / (R(1) + rest);
-    omPsi[0] = rest * Psi[0];
+    const R psi = R(1) / (R(1) + rest);
+    Ieff[0] = psi * (Sbg[0] + C10 * Zb);
+    P[0] = Pk;
+    Psi[0] = psi;
+    omPsi[0] = rest * psi;
   }
-  (void)muz;
-  return R(2) * P[0];
+  return R(2) * Pk;
 }
 
 template <typename R>
@@ -665,22 +685,20 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
     if (any_feau) {
       // angle-independent: one Feautrier solution per ray (to_obs index 0)
       op.q = 2 * ray;
-      // P overwrites S, Psi F and 1 - Psi zt (feautrier_full allows it)
+      // P overwrites S, Psi F, 1 - Psi zt and Ieff Sb (feautrier_full allows it)
       R chis[PYRH_NLTE_MAX_DEPTH], S[PYRH_NLTE_MAX_DEPTH], F[PYRH_NLTE_MAX_DEPTH],
-          zt[PYRH_NLTE_MAX_DEPTH], eta[PYRH_NLTE_MAX_DEPTH], cbg[PYRH_NLTE_MAX_DEPTH];
+          zt[PYRH_NLTE_MAX_DEPTH], Sb[PYRH_NLTE_MAX_DEPTH], cbg[PYRH_NLTE_MAX_DEPTH];
       for (int k = 0; k < nd; ++k) {
-        R Sb;
-        op(k, chis[k], S[k], Sb, cbg[k], eta[k], Jold[k]);
+        R eta_a;
+        op(k, chis[k], S[k], Sb[k], cbg[k], eta_a, Jold[k]);
       }
-      const R Ie = feautrier_full<R>(chis, S, dsl, nd, A.muz[ray], B0, B1, S, F, zt, F, zt);
+      const R Ie = feautrier_full<R>(chis, S, Sb, dsl, nd, B0, B1, S, F, zt, Sb, F, zt);
       if (feau) emergent = Ie;
       if (!emergent_only) {
         const R wdir = R(A.wmu[ray]);
-        for (int k = 0; k < nd; ++k) {
-          const R Ieff = S[k] - (F[k] / chis[k]) * eta[k];
+        for (int k = 0; k < nd; ++k)
           add_rates<R>(A, tr, as, sh, out, nd, nlev, op.q, k, feau, wdir, S[k], F[k], zt[k],
-                       Ieff, chis[k], cbg[k]);
-        }
+                       Sb[k], chis[k], cbg[k]);
       }
     }
   }

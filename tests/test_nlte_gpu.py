@@ -9,7 +9,9 @@ The FP32 bound is the convergence criterion of the runs (ITER_LIMIT 1e-4);
 measured 2-7e-6 with the reference's iteration counts.  Two reformulations
 keep single precision from cancelling in optically thick line cores: the
 MALI effective intensity I - Psi*eta (fillgamma.c:121-134) is built inside
-the Bezier recurrence, and the preconditioned downward rate
+the Bezier recurrence (and, for Feautrier wavelengths, as Psi times a sum of
+positive terms of the two one-sided eliminations), and the preconditioned
+downward rate
 (2 h nu^3/c^2 + Ieff) g V W - chi_up Psi U_down (fillgamma.c:185-196) is
 formed from the escape fraction 1 - X Psi / chi = X_other / chi +
 (X / chi)(1 - Psi) with 1 - Psi from the positive Bezier weights.  Formed
