@@ -274,7 +274,13 @@ pyrh_status pyrh_lte_stokes_vjp(const pyrh_lte_batch *batch, const pyrh_line *li
  * (LTE populations, collision matrix, background, damping, cross-sections).
  * The formal solution is the scalar one of STOKES_MODE = NO_STOKES: with
  * FULL_STOKES the reference solves for I, Q, U, V wherever a polarizable
- * line is in window (formal.c:92-101), which this entry does not.
+ * line is in window (formal.c:92-101), which this entry does not.  A
+ * wavelength takes scalar Bezier3 in both directions of every ray where it
+ * is angle dependent -- a polarized line in its active set or a polarized
+ * background (even in a static atmosphere: the reference always sets
+ * atmos.Stokes, pyrh_compute1dray.c:85, and only FIELD_FREE makes a set
+ * unpolarized, opacity.c:574-589), or, in a moving atmosphere, any line --
+ * and Feautrier once per ray otherwise (formal.c:92-101, 284-310).
  */
 #define PYRH_NLTE_MAX_LEVELS  8
 #define PYRH_NLTE_MAX_ACTIVE  16   /* transitions active at one wavelength */
@@ -291,6 +297,10 @@ typedef struct {
   int32_t symmetric;     /* line->symmetric (getlambda.c:194) */
   int32_t voigt;         /* line->Voigt (damping used) */
   int32_t line_index;    /* row of adamp for lines */
+  int32_t polarized;     /* lines: line->polarizable with STOKES_MODE other than
+                            FIELD_FREE: its wavelengths are angle dependent
+                            (containsPolarized, opacity.c:574-589) */
+  int32_t reserved;      /* 0 */
   int64_t phi_off;       /* line profile block offset in the workspace */
   int64_t alpha_off;     /* continua: first cross-section in alpha[] */
   double lambda0, Aji, Bji, Bij, isotope_frac, c_shift, c_fraction;
@@ -312,14 +322,14 @@ typedef struct {
   const double *nstar;                            /* [nlevel][total_depth] */
   const double *C;                                /* [nlevel^2][total_depth] */
   const double *chi_c, *eta_c, *sca_c;            /* [total_cont] */
-  const int32_t *bgline;                          /* [total_lambda]: a background
-                                  line covers the wavelength (backgrflags.
-                                  hasline); with cfg->moving the wavelength
-                                  is then angle dependent (formal.c:96-101).
-                                  Background lines enter unpolarized through
-                                  chi_c/eta_c: a polarizable one, which makes
-                                  the reference solve for I, Q, U, V there,
-                                  is outside this entry */
+  const int32_t *bgline;                          /* [total_lambda]: backgrflags,
+                                  bit 0 hasline (a background line covers
+                                  the wavelength: angle dependent with
+                                  cfg->moving), bit 1 ispolarized (angle
+                                  dependent; formal.c:92-101).  Background
+                                  lines enter through chi_c/eta_c, Stokes I
+                                  only (the I, Q, U, V solve of FULL_STOKES
+                                  is outside this entry) */
   const pyrh_nlte_transition *trans;              /* [sum ntrans] */
   const double *alpha;                            /* continuum cross-sections */
   const double *adamp;                            /* [sum nline*ndep] */

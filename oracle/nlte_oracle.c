@@ -277,13 +277,14 @@ static int solve_linear_eq(int n, double *A, double *b)
 typedef struct {
   int nact, type[NLTE_MAX_ACTIVE], kr[NLTE_MAX_ACTIVE], la[NLTE_MAX_ACTIVE];
   int i[NLTE_MAX_ACTIVE], j[NLTE_MAX_ACTIVE];
-  int boundbound;
+  int boundbound, polarized;
 } ActiveSet;
 
 static void active_set(const NlteProblem *P, int ns, ActiveSet *as)
 {
   as->nact = 0;
   as->boundbound = 0;
+  as->polarized = 0;
   for (int kr = 0; kr < P->ncont; kr++) {        /* continua first (sortlambda.c:290-335) */
     const double *Cr = P->cont + (long) kr * NC_NREC;
     int nb = (int) Cr[NC_NBLUE], nl = (int) Cr[NC_NLAMBDA];
@@ -301,6 +302,7 @@ static void active_set(const NlteProblem *P, int ns, ActiveSet *as)
       as->type[n] = 0; as->kr[n] = kr; as->la[n] = ns - nb;
       as->i[n] = (int) L[NL_I]; as->j[n] = (int) L[NL_J];
       as->boundbound = 1;
+      if ((int) L[NL_POLARIZED]) as->polarized = 1;
     }
   }
 }
@@ -445,7 +447,10 @@ static void formal_lambda(const NlteProblem *P, int ns, int nrays, const double 
   double *J = J_new + (long) ns * nd;
   for (int k = 0; k < nd; k++) W->Jdag[k] = Jold[(long) ns * nd + k];
   if (update_J) for (int k = 0; k < nd; k++) J[k] = 0.0;
-  int angle_dep = P->moving && (as.boundbound || P->bgline[ns]);
+  /* formal.c:92-101: a polarized active set or background, or a moving
+     atmosphere with a line at this wavelength */
+  int angle_dep = as.polarized || (P->bgline[ns] & 2) ||
+                  (P->moving && (as.boundbound || (P->bgline[ns] & 1)));
   double *chi = (double *) malloc(nd * sizeof(double));
   if (angle_dep) {
     for (int mu = 0; mu < nrays; mu++) {

@@ -12,7 +12,7 @@ extern "C" {
 /* line record (double[NL_NREC]) */
 enum { NL_I = 0, NL_J, NL_LAMBDA0, NL_AJI, NL_BJI, NL_BIJ, NL_ISOFRAC, NL_NBLUE,
        NL_NLAMBDA, NL_SYMMETRIC, NL_NCOMP, NL_CSHIFT, NL_CFRAC, NL_VOIGT, NL_PRD,
-       NL_NREC = 16 };
+       NL_POLARIZED, NL_NREC = 16 };
 /* continuum record (double[NC_NREC]) */
 enum { NC_I = 0, NC_J, NC_NBLUE, NC_NLAMBDA, NC_LAMBDA0, NC_HYDRO, NC_AOFF, NC_NREC = 8 };
 
@@ -22,7 +22,8 @@ typedef struct {
   const double *muz, *wmu;              /* [nrays] */
   const double *height, *T, *vel, *vbroad;   /* [ndep] SI */
   const double *chi_c, *eta_c, *sca_c;  /* [nspect][ndep] */
-  const int *bgline;                    /* [nspect] background line flag */
+  const int *bgline;                    /* [nspect] backgrflags: bit 0 hasline,
+                                           bit 1 ispolarized */
   const double *nstar, *ntotal, *C;     /* [nlevel][ndep], [ndep], [nlevel^2][ndep] */
   const double *lines, *adamp;          /* [nline][NL_NREC], [nline][ndep] */
   const double *cont, *alpha;           /* [ncont][NC_NREC], concatenated */

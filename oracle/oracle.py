@@ -207,7 +207,7 @@ def nlte_problem(fx: dict, keep: _Keep) -> NlteProblem:
     P.chi_c = _p(keep.f64(bg[0]))
     P.eta_c = _p(keep.f64(bg[1]))
     P.sca_c = _p(keep.f64(bg[2]))
-    fl = np.ascontiguousarray(fx["bgflags"] & 1, dtype=np.int32)
+    fl = np.ascontiguousarray(fx["bgflags"] & 3, dtype=np.int32)
     keep.arrays.append(fl)
     P.bgline = fl.ctypes.data_as(_I)
     return P

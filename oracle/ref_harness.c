@@ -513,7 +513,9 @@ int harness_nlte(const char *cwd, double mu, int Ndep, const double *atm, int Nw
     dump_matrix(outdir, "C", atom->C, Nl * Nl, Nspace);
     write_f64(outdir, "vbroad", atom->vbroad, Nspace);
     /* lines: [i, j, lambda0, Aji, Bji, Bij, isotope_frac, Nblue, Nlambda,
-               symmetric, Ncomponent, c_shift0, c_fraction0, Voigt, PRD, 0] */
+               symmetric, Ncomponent, c_shift0, c_fraction0, Voigt, PRD,
+               polarized]; polarized: the line makes the active set
+               polarized (containsPolarized, rh/opacity.c:574-589) */
     double *lr = (double *) calloc(16L * atom->Nline, sizeof(double));
     double *ad = (double *) calloc((long) atom->Nline * Nspace, sizeof(double));
     double *wp = (double *) calloc((long) atom->Nline * Nspace, sizeof(double));
@@ -528,13 +530,18 @@ int harness_nlte(const char *cwd, double mu, int Ndep, const double *atm, int Nw
       r[11] = l->Ncomponent > 0 ? l->c_shift[0] : 0.0;
       r[12] = l->Ncomponent > 0 ? l->c_fraction[0] : 1.0;
       r[13] = l->Voigt; r[14] = l->PRD;
+      r[15] = atmos.Stokes && input.StokesMode != FIELD_FREE && l->polarizable;
       if (l->Voigt) Damping(l, ad + (long) kr * Nspace);
       memcpy(wp + (long) kr * Nspace, l->wphi, Nspace * sizeof(double));
       int sel[5] = {0, l->Nlambda / 4, l->Nlambda / 2, (3 * l->Nlambda) / 4, l->Nlambda - 1};
+      /* the profile is stored per (lambda, ray, direction) only where it
+         depends on the angle (rh/profile.c:154-170); otherwise one row per
+         lambda serves every ray and direction */
+      int angle_dep = atmos.moving || (l->polarizable && input.StokesMode > FIELD_FREE);
       for (int s = 0; s < 5; s++) {
         phla[kr * 5 + s] = sel[s];
         for (int q = 0; q < 2 * atmos.Nrays; q++) {
-          int lamu = 2 * atmos.Nrays * sel[s] + q;
+          int lamu = angle_dep ? 2 * atmos.Nrays * sel[s] + q : sel[s];
           memcpy(ph + (((long) kr * 5 + s) * 2 * atmos.Nrays + q) * Nspace, l->phi[lamu],
                  Nspace * sizeof(double));
         }

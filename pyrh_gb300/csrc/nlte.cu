@@ -195,7 +195,8 @@ struct ActiveSet {
   int n;
   int t[PYRH_NLTE_MAX_ACTIVE];   // transition index
   int la[PYRH_NLTE_MAX_ACTIVE];  // wavelength index within the transition
-  bool bb;
+  bool bb;                       // a line is active (containsBoundBound)
+  bool pol;                      // a polarized line is active (containsPolarized)
   R vb[PYRH_NLTE_MAX_ACTIVE];    // lines: B_ij isotope_frac; continua: alpha(lambda)
   R gl[PYRH_NLTE_MAX_ACTIVE];    // lines: B_ji / B_ij
   R tw[PYRH_NLTE_MAX_ACTIVE];    // lines: A_ji / B_ji; continua: 2 h c / lambda^3
@@ -624,6 +625,7 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
   ActiveSet<R> as;
   as.n = 0;
   as.bb = false;
+  as.pol = false;
   as.hckl = R((kHPLANCK * kCLIGHT / (kKBOLTZMANN * kNM_TO_M)) / lam);
   for (int pass = 1; pass >= 0; --pass)       // continua (type 1) first, then lines
     for (int t = 0; t < nt; ++t) {
@@ -635,6 +637,7 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
         as.la[m] = la - T.nblue;
         if (T.type == 0) {
           as.bb = true;
+          if (T.polarized) as.pol = true;
           as.vb[m] = R(T.Bij * T.isotope_frac);
           as.gl[m] = R(T.Bji / T.Bij);
           as.tw[m] = R(T.Aji / T.Bji);
@@ -650,9 +653,11 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
     }
   const double B0 = planck(b.T[doff + nd - 2], lam), B1 = planck(b.T[doff + nd - 1], lam);
   const JRow<R> Jold{static_cast<const R*>(A.Jr) + coff + la, ns};
-  // angle-dependent wavelengths (formal.c:96-101) take the Bezier3 solution
+  // angle-dependent wavelengths (formal.c:92-101: a polarized active set or
+  // background, or a line in a moving atmosphere) take the Bezier3 solution
   // in both directions, the others Feautrier once per ray
-  const bool angle_dep = A.moving && (as.bb || b.bgline[b.lam_off[p] + la]);
+  const int bgf = b.bgline[b.lam_off[p] + la];
+  const bool angle_dep = as.pol || (bgf & 2) || (A.moving && (as.bb || (bgf & 1)));
   const bool bez = live && angle_dep, feau = live && !angle_dep;
   const bool any_bez = __any_sync(full, bez), any_feau = __any_sync(full, feau);
   NlteOpacity<R> op;

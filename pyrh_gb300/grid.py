@@ -88,6 +88,8 @@ def _lib():
     lib.pyrh_cont_alpha.argtypes = [C.POINTER(Atom), C.c_int32, _D, C.c_int32, _D]
     lib.pyrh_atom_lande_eff.restype = C.c_double
     lib.pyrh_atom_lande_eff.argtypes = [C.POINTER(Atom), C.c_int32]
+    lib.pyrh_atom_line_polarizable.restype = C.c_int32
+    lib.pyrh_atom_line_polarizable.argtypes = [C.POINTER(Atom), C.c_int32, C.c_int32]
     return lib
 
 
@@ -104,6 +106,19 @@ def read_atom(text: str) -> Atom:
     atom = Atom()
     L.check(_lib().pyrh_atom_read(text.encode(), C.byref(atom)))
     return atom
+
+
+def line_polarized(atom: Atom, kr: int, field_free: bool = False) -> bool:
+    """Whether line kr of an active atom makes the wavelengths it covers
+    angle dependent in the NLTE formal solution (the `polarized` field of
+    pyrh_nlte_transition): polarizable (readatom.c:347-366, with
+    atmos.Stokes, which pyrh always sets, pyrh_compute1dray.c:85) under a
+    STOKES_MODE other than FIELD_FREE (containsPolarized,
+    opacity.c:574-589)."""
+    pol = _lib().pyrh_atom_line_polarizable(C.byref(atom), int(kr), 1)
+    if pol < 0:
+        raise ValueError(f"line {kr}: composite line with polarization")
+    return bool(pol) and not field_free
 
 
 @dataclass

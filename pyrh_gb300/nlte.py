@@ -8,6 +8,12 @@ leaves before its Iterate() (rh/rhf1d/pyrh_compute1dray.c:280-323):
   nstar, n0 [nlevel, ndep]; C [nlevel^2, ndep]; lines [nline, 16] and
   continua [ncont, 8] transition records; adamp [nline, ndep]; alpha;
   optional J0 [nspect, ndep] (zero when absent).
+A line record is [i, j, lambda0, Aji, Bji, Bij, isotope_frac, Nblue,
+Nlambda, symmetric, Ncomponent, c_shift, c_fraction, Voigt, PRD,
+polarized], polarized = line->polarizable with STOKES_MODE other than
+FIELD_FREE (the wavelengths it covers are angle dependent, opacity.c:574-589;
+pyrh_atom_line_polarizable gives it from the model atom); bgflags holds
+backgrflags' hasline (bit 0) and ispolarized (bit 1).
 """
 from __future__ import annotations
 
@@ -23,7 +29,7 @@ MAX_RAYS = 8
 
 class PyrhNlteTransition(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("type", "i", "j", "nblue", "nlambda", "symmetric",
-                                         "voigt", "line_index")] + \
+                                         "voigt", "line_index", "polarized", "reserved")] + \
         [("phi_off", C.c_int64), ("alpha_off", C.c_int64)] + \
         [(n, C.c_double) for n in ("lambda0", "Aji", "Bji", "Bij", "isotope_frac", "c_shift",
                                    "c_fraction")]
@@ -132,6 +138,7 @@ def pack(atms: list[dict], nrays: int) -> PackedNlte:
             if int(l[14]):
                 raise ValueError("PRD lines are not supported")
             t.line_index = li
+            t.polarized = int(l[15])
             t.phi_off = phi_off
             phi_off += int(l[8]) * 2 * nrays * nd
             trans.append(t)
@@ -153,7 +160,7 @@ def pack(atms: list[dict], nrays: int) -> PackedNlte:
         chi_c=np.concatenate([b[0].ravel() for b in bgT]),
         eta_c=np.concatenate([b[1].ravel() for b in bgT]),
         sca_c=np.concatenate([b[2].ravel() for b in bgT]),
-        bgline=np.concatenate([np.asarray(a["bgflags"], np.int32) & 1 for a in atms]),
+        bgline=np.concatenate([np.asarray(a["bgflags"], np.int32) & 3 for a in atms]),
         alpha=np.concatenate(alpha_all) if alpha_all else np.zeros(1),
         adamp=np.concatenate(adamp_all) if adamp_all else np.zeros(1),
         n=np.ascontiguousarray(lev("n0")),

@@ -43,6 +43,8 @@ Fixtures (npz, float64):
   nlte_c1         six-level Ca II-like atom ACTIVE, 82 depths, 5 rays
   nlte_c4_50/120  the same atom on perturbed 50- and 120-depth atmospheres
                   with velocity fields and other wavelength counts
+  nlte_static     nlte_c1 in a static atmosphere (VMACRO_TRESH 0.1 km/s, no
+                  velocity): every wavelength takes the Feautrier solver
 
 stokes_ref comes from the reference as setup.py builds it on x86 (-DSIMDON,
 SSE reciprocal-estimate 4x4 inverse); stokes_ref_portable from the same
@@ -347,7 +349,7 @@ NLTE_ATOM = "CaII_synth.atom"
 
 
 def nlte_case(name, ndep=82, nlambda_scale=1.0, atom_seed=11, dT=None, vlos=0.0,
-              mu_out=1.0, nrays=5):
+              mu_out=1.0, nrays=5, vmacro_tresh="0"):
     """NLTE MALI with the six-level Ca II-like atom ACTIVE: the reference's
     set-up state, one hand-made iteration (Gamma, J, statEquil), and the
     converged populations and emergent intensity (N_MAX_SCATTER = 0, Ng
@@ -357,7 +359,8 @@ def nlte_case(name, ndep=82, nlambda_scale=1.0, atom_seed=11, dT=None, vlos=0.0,
     wd = rr.scratch_dir()
     rr.write_inputs(wd, None, atoms=list(rr.PASSIVE_ATOMS) + [NLTE_ATOM], active=NLTE_ATOM,
                     nrays=nrays, nmax_iter=200, iter_limit="1.0E-4", ng_order=2, ng_delay=5,
-                    ng_period=5, stokes_mode="NO_STOKES", nmax_scatter=0)
+                    ng_period=5, stokes_mode="NO_STOKES", nmax_scatter=0,
+                    vmacro_tresh=vmacro_tresh)
     lt = wl.logtau_grid(ndep)
     T = wl.base_temperature(lt) + (0.0 if dT is None else dT)
     ne, nH = ref.hse(wd, lt, T)
@@ -390,6 +393,14 @@ def make_nlte(ref, wd):
     lt120 = wl.logtau_grid(120)
     pert = wl.perturbations(2, 98, lt120)
     nlte_case("nlte_c4_120", ndep=120, nlambda_scale=1.25, dT=pert["dT"][1], vlos=-2.0)
+
+
+def make_nlte_static(ref, wd):
+    """nlte_c1 with VMACRO_TRESH = 0.1 km/s and no velocity: atmos.moving
+    stays FALSE, so no wavelength is angle dependent and every one takes
+    the Feautrier solver (formal.c:96-101, 284-304), and the line profiles
+    are stored once per wavelength (profile.c:154-170)."""
+    nlte_case("nlte_static", ndep=82, vmacro_tresh="0.1")
 
 
 def make_kurucz(ref, wd):
@@ -435,7 +446,7 @@ MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
           "lte_static": make_lte_static, "lte_broadening": make_lte_broadening,
-          "nlte": make_nlte, "kurucz": make_kurucz}
+          "nlte": make_nlte, "nlte_static": make_nlte_static, "kurucz": make_kurucz}
 
 
 def main():

@@ -122,7 +122,7 @@ def test_pack_layout(golden):
 def test_nlte_structs_and_workspace_without_gpu(golden):
     import ctypes as C
     from pyrh_gb300 import nlte
-    assert C.sizeof(nlte.PyrhNlteTransition) == 8 * 4 + 2 * 8 + 7 * 8
+    assert C.sizeof(nlte.PyrhNlteTransition) == 10 * 4 + 2 * 8 + 7 * 8
     fx = golden("nlte_c1")
     cfg = nlte.make_config(fx)
     pk = nlte.pack([fx], cfg.nrays)

@@ -11,7 +11,7 @@ import pytest
 from pyrh_gb300 import _lib as L
 from pyrh_gb300 import grid as G
 
-NLTE = ["nlte_c1", "nlte_c4_50", "nlte_c4_120"]
+NLTE = ["nlte_c1", "nlte_c4_50", "nlte_c4_120", "nlte_static"]
 LTE = ["lte_c0", "lte_edge", "lte_b0", "lte_mixed", "lte_static", "lte_static_v",
        "lte_nostokes", "lte_broadening"]
 
@@ -35,6 +35,10 @@ def test_nlte_grid_matches_reference(golden, name):
         ln, ref = atom.line[kr], fx["lines"][kr]
         assert (ln.i, ln.j) == (int(ref[0]), int(ref[1]))
         assert ln.lambda0 == ref[2] and ln.Aji == ref[3] and ln.Bji == ref[4] and ln.Bij == ref[5]
+        # whether the line polarizes the active set (NO_STOKES: only
+        # FIELD_FREE would not)
+        assert G.line_polarized(atom, kr) == bool(ref[15])
+        assert not G.line_polarized(atom, kr, field_free=True)
 
 
 @pytest.mark.parametrize("name", LTE)

@@ -40,7 +40,7 @@ def test_setup_matches_reference(golden, name):
     assert np.abs(vb / fx["vbroad"] - 1).max() < 1e-14
 
 
-@pytest.mark.parametrize("name", ["nlte_c1", "nlte_c4_120"])
+@pytest.mark.parametrize("name", ["nlte_c1", "nlte_c4_120", "nlte_static"])
 def test_solve_from_atom_file(golden, name):
     fx = golden(name)
     atom, (nstar, Cm, vb) = _setup(fx)
@@ -51,6 +51,7 @@ def test_solve_from_atom_file(golden, name):
     mine["lambda"] = g.lam
     lines = np.array(fx["lines"], np.float64).copy()
     lines[:, 7:9] = g.line_range
+    lines[:, 15] = [G.line_polarized(atom, kr) for kr in range(atom.nline)]
     cont = np.array(fx["continua"], np.float64).copy()
     cont[:, 2:4] = g.cont_range
     off = np.concatenate([[0], np.cumsum(cont[:, 3])[:-1]])
