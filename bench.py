@@ -361,6 +361,25 @@ def nlte_measure(natm, local, nsample=32):
         "same_count_max_rel_err": float(errs[same].max()) if same.any() else None,
         "different_count_atmospheres": int((~same).sum()),
         "different_count_max_rel_err": float(errs[~same].max()) if (~same).any() else None}
+    # Both runs stop once no population changes by more than the limit in an
+    # iteration, so each lies within about that change (times the Ng
+    # amplification of a slowly converging atmosphere) of the fixed point.
+    # Where FP32 and FP64 differ most, measure how far each is from the
+    # fixed point itself: an FP64 solve run to a 1e-9 limit.
+    worst = np.argsort(-errs)[:min(64, natm)]
+    cfg = nlte.make_config(atms[0], L.PYRH_FP64, nmax_iter=400)
+    cfg.iter_limit = 1e-9
+    dev = nlte.DeviceNlte(nlte.pack([atms[i] for i in worst], cfg.nrays), cfg,
+                          device=f"cuda:{local}")
+    st = dev.solve(cfg)
+    pfix = dev.populations()
+    del dev
+    torch.cuda.empty_cache()
+    out["fixed_point_sample"] = {
+        "atmospheres": len(worst), "selection": "largest FP32-vs-FP64 difference",
+        "status": int(st),
+        "fp32_max_rel_err": max(float(np.abs(p32[i] / f - 1).max()) for i, f in zip(worst, pfix)),
+        "fp64_max_rel_err": max(float(np.abs(p64[i] / f - 1).max()) for i, f in zip(worst, pfix))}
     nthreads = os.cpu_count() or 1
     n_or, it_or, t_or = nlte_oracle_solve(atms[:nsample], nthreads)
     out["oracle_sample"] = {
