@@ -335,6 +335,14 @@ typedef struct {
   const double *adamp;                            /* [sum nline*ndep] */
   double *n;        /* [nlevel][total_depth]: start populations, then result */
   double *J;        /* [total_cont]: start mean intensity, then the last one */
+  /* Optional (NULL: not kept): the radiative rates of every transition
+     after its atmosphere's last formal solution, as addtoRates leaves them
+     (rh/fillgamma.c:375-461; zeroed before each formal solution,
+     rh/iterate.c:178): R_ij in slot 2t and R_ji in slot 2t + 1 of
+     transition t (the atmosphere's table order), [2 max_ntrans][total_depth],
+     s^-1.  max_ntrans >= every ntrans[p]; read only with rates. */
+  int32_t max_ntrans;
+  double *rates;
 } pyrh_nlte_batch;
 
 typedef struct {

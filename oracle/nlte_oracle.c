@@ -428,13 +428,33 @@ static void add_gamma(const NlteProblem *P, const ActiveSet *as, int ns, double 
   }
 }
 
+/* addtoRates (fillgamma.c:375-461): R_ij += I V W wmu, R_ji += g (2 h nu^3 /
+   c^2 + I) V W wmu, into rates [nline][2][ndep] followed by [ncont][2][ndep]. */
+static void add_rates(const NlteProblem *P, const ActiveSet *as, int ns, double wmu,
+                      const Work *W, double *rates)
+{
+  int nd = P->ndep;
+  for (int m = 0; m < as->nact; m++) {
+    double t = twohnu3_of(P, as, m, ns);
+    long row = as->type[m] == 0 ? as->kr[m] : P->nline + as->kr[m];
+    double *Rij = rates + 2 * row * nd, *Rji = Rij + nd;
+    const double *Vij = W->Vij + (long) m * nd, *gij = W->gij + (long) m * nd;
+    const double *wla = W->wla + (long) m * nd;
+    for (int k = 0; k < nd; k++) {
+      double wlamu = Vij[k] * wla[k] * wmu;
+      Rij[k] += W->I[k] * wlamu;
+      Rji[k] += gij[k] * (t + W->I[k]) * wlamu;
+    }
+  }
+}
+
 /* Formal() for one wavelength (formal.c:44-346).  J_new[ns] is replaced by
    the new mean intensity when update_J; Gamma accumulates when gamma != NULL;
    Iem[mu] receives the emergent intensity. */
 static void formal_lambda(const NlteProblem *P, int ns, int nrays, const double *muz,
                           const double *wmu, double **phi, const double *wphi,
                           const double *n, const double *Jold, double *J_new, int update_J,
-                          double *Gamma, Work *W, double *Iem)
+                          double *Gamma, Work *W, double *Iem, double *rates)
 {
   int nd = P->ndep;
   ActiveSet as;
@@ -469,6 +489,7 @@ static void formal_lambda(const NlteProblem *P, int ns, int nrays, const double 
           add_gamma(P, &as, ns, w, W, Gamma);
         }
         if (update_J) for (int k = 0; k < nd; k++) J[k] += w * W->I[k];
+        if (update_J && rates) add_rates(P, &as, ns, w, W, rates);
       }
       Iem[mu] = W->I[0];
     }
@@ -486,6 +507,7 @@ static void formal_lambda(const NlteProblem *P, int ns, int nrays, const double 
         add_gamma(P, &as, ns, wmu[mu], W, Gamma);
       }
       if (update_J) for (int k = 0; k < nd; k++) J[k] += W->I[k] * wmu[mu];
+      if (update_J && rates) add_rates(P, &as, ns, wmu[mu], W, rates);
     }
   }
   free(chi);
@@ -531,20 +553,29 @@ static void free_phi(const NlteProblem *P, double **phi)
   free(phi);
 }
 
-/* One pass over the spectrum: Gamma = C + radiative, J replaced.  Gamma
-   may be NULL (no operator). */
-void oracle_nlte_spectrum(const NlteProblem *P, const double *n, const double *Jold,
-                          double *J_new, double *Gamma, double **phi, const double *wphi)
+/* One pass over the spectrum: Gamma = C + radiative, J replaced, and, when
+   rates is not NULL, the radiative rates of this pass (solveSpectrum,
+   iterate.c:146-260, zeroes them first).  Gamma may be NULL (no operator). */
+void oracle_nlte_spectrum_rates(const NlteProblem *P, const double *n, const double *Jold,
+                                double *J_new, double *Gamma, double **phi,
+                                const double *wphi, double *rates)
 {
   int nd = P->ndep, nl = P->nlevel;
   Work W;
   work_alloc(&W, nd, nl);
   double Iem[64];
   if (Gamma) memcpy(Gamma, P->C, sizeof(double) * nl * nl * nd);
+  if (rates) memset(rates, 0, sizeof(double) * 2 * (P->nline + P->ncont) * nd);
   for (int ns = 0; ns < P->nspect; ns++)
     formal_lambda(P, ns, P->nrays, P->muz, P->wmu, phi, wphi, n, Jold, J_new, 1, Gamma,
-                  &W, Iem);
+                  &W, Iem, rates);
   work_free(&W);
+}
+
+void oracle_nlte_spectrum(const NlteProblem *P, const double *n, const double *Jold,
+                          double *J_new, double *Gamma, double **phi, const double *wphi)
+{
+  oracle_nlte_spectrum_rates(P, n, Jold, J_new, Gamma, phi, wphi, NULL);
 }
 
 /* statEquil (statequil.c:40-102) on n [nlevel][ndep] in place. */
@@ -646,9 +677,10 @@ static double ng_maxchange(const Ng *g)
 
 /* Iterate (iterate.c:48-143): n (in/out) [nlevel][ndep], J (in/out)
    [nspect][ndep].  Returns the number of iterations; dpops[it] receives
-   the convergence metric of each. */
-int oracle_nlte_iterate(const NlteProblem *P, double *n, double *J, double *dpops,
-                        int *accelerated)
+   the convergence metric of each; rates (may be NULL) those of the last
+   formal pass. */
+int oracle_nlte_iterate_rates(const NlteProblem *P, double *n, double *J, double *dpops,
+                              int *accelerated, double *rates)
 {
   int nd = P->ndep, nl = P->nlevel;
   double **phi = alloc_phi(P, P->nrays);
@@ -661,7 +693,7 @@ int oracle_nlte_iterate(const NlteProblem *P, double *n, double *J, double *dpop
   int niter = 1, done = 0;
   while (niter <= P->nmax_iter) {
     memcpy(Jn, J, sizeof(double) * P->nspect * nd);
-    oracle_nlte_spectrum(P, n, J, Jn, Gamma, phi, wphi);
+    oracle_nlte_spectrum_rates(P, n, J, Jn, Gamma, phi, wphi, rates);
     memcpy(J, Jn, sizeof(double) * P->nspect * nd);
     oracle_stat_equil(P, Gamma, n);
     int acc = ng_accelerate(&g, n);
@@ -675,6 +707,12 @@ int oracle_nlte_iterate(const NlteProblem *P, double *n, double *J, double *dpop
   free(g.prev); free(Gamma); free(Jn); free(wphi);
   free_phi(P, phi);
   return done;
+}
+
+int oracle_nlte_iterate(const NlteProblem *P, double *n, double *J, double *dpops,
+                        int *accelerated)
+{
+  return oracle_nlte_iterate_rates(P, n, J, dpops, accelerated, NULL);
 }
 
 /* Emergent intensity at mu_out with the populations n and the fixed mean
@@ -693,7 +731,7 @@ void oracle_nlte_emergent(const NlteProblem *P, double mu_out, const double *n,
   double *Jdummy = malloc(sizeof(double) * P->nspect * nd);
   for (int ns = 0; ns < P->nspect; ns++) {
     double Iem[1];
-    formal_lambda(P, ns, 1, muz, wmu, phi, wphi, n, J, Jdummy, 0, NULL, &W, Iem);
+    formal_lambda(P, ns, 1, muz, wmu, phi, wphi, n, J, Jdummy, 0, NULL, &W, Iem, NULL);
     Iout[ns] = Iem[0];
   }
   free(Jdummy);

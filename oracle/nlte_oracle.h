@@ -39,6 +39,13 @@ void oracle_nlte_spectrum(const NlteProblem *P, const double *n, const double *J
 int oracle_stat_equil(const NlteProblem *P, const double *Gamma, double *n);
 int oracle_nlte_iterate(const NlteProblem *P, double *n, double *J, double *dpops,
                         int *accelerated);
+/* the same with the radiative rates (addtoRates, fillgamma.c:375-461) of
+   the pass, [nline][2][ndep] followed by [ncont][2][ndep] */
+void oracle_nlte_spectrum_rates(const NlteProblem *P, const double *n, const double *Jold,
+                                double *J_new, double *Gamma, double **phi,
+                                const double *wphi, double *rates);
+int oracle_nlte_iterate_rates(const NlteProblem *P, double *n, double *J, double *dpops,
+                              int *accelerated, double *rates);
 void oracle_nlte_emergent(const NlteProblem *P, double mu_out, const double *n,
                           const double *J, double *Iout);
 

@@ -226,8 +226,15 @@ def _nlte_lib():
     L.oracle_voigt_armstrong.restype = C.c_double
     L.oracle_voigt_armstrong.argtypes = [C.c_double, C.c_double]
     L.oracle_nlte_iterate.restype = C.c_int
+    L.oracle_nlte_iterate_rates.restype = C.c_int
     L.oracle_stat_equil.restype = C.c_int
     return L
+
+
+def _split_rates(fx: dict, R: np.ndarray) -> dict:
+    nline, ncont, nd = len(fx["lines"]), len(fx["continua"]), len(fx["T"])
+    R = R.reshape(nline + ncont, 2, nd)
+    return {"lines": R[:nline], "continua": R[nline:]}
 
 
 def voigt_armstrong(a, v):
@@ -248,9 +255,11 @@ def nlte_profiles(fx: dict, nrays=None, muz=None, wmu=None):
     return phis, wphi
 
 
-def nlte_first_iteration(fx: dict):
+def nlte_first_iteration(fx: dict, rates: bool = False):
     """Gamma and J after one formal pass with the starting populations and
-    J, and the populations after one statEquil (no acceleration)."""
+    J, and the populations after one statEquil (no acceleration); with
+    rates, also that pass's radiative rates {"lines": [nline, 2, ndep],
+    "continua": [ncont, 2, ndep]} (R_ij, R_ji)."""
     keep = _Keep()
     P = nlte_problem(fx, keep)
     phis, wphi = nlte_profiles(fx)
@@ -260,22 +269,29 @@ def nlte_first_iteration(fx: dict):
     J = np.zeros_like(J0)
     G = np.zeros((P.nlevel * P.nlevel, P.ndep))
     L = _nlte_lib()
-    L.oracle_nlte_spectrum(C.byref(P), _p(n), _p(J0), _p(J), _p(G), arr, _p(wphi))
+    R = np.zeros(2 * (P.nline + P.ncont) * P.ndep)
+    L.oracle_nlte_spectrum_rates(C.byref(P), _p(n), _p(J0), _p(J), _p(G), arr, _p(wphi),
+                                 _p(R))
     n1 = n.copy()
     L.oracle_stat_equil(C.byref(P), _p(G), _p(n1))
-    return G, J, n1
+    return (G, J, n1, _split_rates(fx, R)) if rates else (G, J, n1)
 
 
-def nlte_solve(fx: dict):
-    """Converged populations, final J, iteration count and dpops history."""
+def nlte_solve(fx: dict, rates: bool = False):
+    """Converged populations, final J, iteration count and dpops history;
+    with rates, also the radiative rates of the last formal pass (as
+    nlte_first_iteration gives them)."""
     keep = _Keep()
     P = nlte_problem(fx, keep)
     n = np.array(fx["n0"], dtype=np.float64, order="C")
     J = np.array(nlte_J0(fx), dtype=np.float64, order="C")
     dp = np.zeros(P.nmax_iter)
     acc = np.zeros(P.nmax_iter, dtype=np.int32)
-    it = _nlte_lib().oracle_nlte_iterate(C.byref(P), _p(n), _p(J), _p(dp),
-                                         acc.ctypes.data_as(_I))
+    R = np.zeros(2 * (P.nline + P.ncont) * P.ndep)
+    it = _nlte_lib().oracle_nlte_iterate_rates(C.byref(P), _p(n), _p(J), _p(dp),
+                                               acc.ctypes.data_as(_I), _p(R))
+    if rates:
+        return n, J, it, dp[:it], acc[:it], _split_rates(fx, R)
     return n, J, it, dp[:it], acc[:it]
 
 

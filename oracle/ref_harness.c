@@ -463,6 +463,28 @@ static void dump_matrix(const char *dir, const char *name, double **m, int n1, i
 /* mode 0: dump the set-up, run one iteration by hand (Gamma, J, statEquil)
    and dump it.  mode 1: run Iterate() and _solveray() and dump the
    converged populations and the emergent intensity. */
+/* Radiative rates of the active atom as addtoRates left them
+   (rh/fillgamma.c:375-461): <prefix>_line [Nline][2][Nspace] and
+   <prefix>_cont [Ncont][2][Nspace], R_ij then R_ji. */
+static void dump_rates(const char *outdir, const char *prefix, Atom *atom, int Nspace)
+{
+  char name[64];
+  double *r = (double *) malloc(2L * (atom->Nline + atom->Ncont + 1) * Nspace * sizeof(double));
+  for (int kr = 0; kr < atom->Nline; kr++) {
+    memcpy(r + (2L * kr) * Nspace, atom->line[kr].Rij, Nspace * sizeof(double));
+    memcpy(r + (2L * kr + 1) * Nspace, atom->line[kr].Rji, Nspace * sizeof(double));
+  }
+  snprintf(name, sizeof(name), "%s_line", prefix);
+  write_f64(outdir, name, r, 2L * atom->Nline * Nspace);
+  for (int kr = 0; kr < atom->Ncont; kr++) {
+    memcpy(r + (2L * kr) * Nspace, atom->continuum[kr].Rij, Nspace * sizeof(double));
+    memcpy(r + (2L * kr + 1) * Nspace, atom->continuum[kr].Rji, Nspace * sizeof(double));
+  }
+  snprintf(name, sizeof(name), "%s_cont", prefix);
+  write_f64(outdir, name, r, 2L * atom->Ncont * Nspace);
+  free(r);
+}
+
 int harness_nlte(const char *cwd, double mu, int Ndep, const double *atm, int Nwave,
                  const double *lam, const char *outdir, int mode)
 {
@@ -576,11 +598,13 @@ int harness_nlte(const char *cwd, double mu, int Ndep, const double *atm, int Nw
     solveSpectrum(TRUE, FALSE);
     dump_matrix(outdir, "Gamma1", atom->Gamma, Nl * Nl, Nspace);
     dump_matrix(outdir, "J1", spectrum.J, Nspect, Nspace);
+    dump_rates(outdir, "R1", atom, Nspace);
     statEquil(atom, input.isum);
     dump_matrix(outdir, "n1", atom->n, Nl, Nspace);
   } else {
     Iterate(input.NmaxIter, input.iterLimit);
     dump_matrix(outdir, "n_final", atom->n, Nl, Nspace);
+    dump_rates(outdir, "R_final", atom, Nspace);
     dump_matrix(outdir, "J_final", spectrum.J, Nspect, Nspace);
     mySpectrum spec;
     spec.nlw = spectrum.Nspect;

@@ -364,12 +364,18 @@ def read_nlte_dump(outdir: str) -> dict:
         d["Gamma1"] = f64("Gamma1").reshape(nl * nl, nd)
         d["J1"] = f64("J1").reshape(ns, nd)
         d["n1"] = f64("n1").reshape(nl, nd)
+        if ex("R1_line", ".f64"):
+            d["R1_line"] = f64("R1_line").reshape(nline, 2, nd)
+            d["R1_cont"] = f64("R1_cont").reshape(ncont, 2, nd)
     if ex("n_final", ".f64"):
         nl = len(f64("g")) if ex("g", ".f64") else None
         d["n_final"] = f64("n_final")
         d["J_final"] = f64("J_final")
         d["lam_out"] = f64("lam_out")
         d["I_out"] = f64("I_out")
+        if ex("R_final_line", ".f64"):
+            d["R_final_line"] = f64("R_final_line")
+            d["R_final_cont"] = f64("R_final_cont")
     return d
 
 

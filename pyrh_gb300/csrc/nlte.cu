@@ -158,6 +158,17 @@ __global__ void nlte_gamma_init_kernel(NlteArgs A) {
     const int ts = e / nd, k = e % nd;
     static_cast<R*>(A.gslab)[(int64_t)ts * b.total_depth + doff + k] = R(0);
   }
+  if (A.rslab) {
+    if (b.ntrans[p] > A.max_ntrans) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(A.err, 4);
+    }
+    const int nr = 2 * A.max_ntrans;
+    for (int e = threadIdx.x + blockIdx.x * blockDim.x; e < ntg * nr * nd;
+         e += blockDim.x * gridDim.x) {
+      const int ts = e / nd, k = e % nd;
+      static_cast<R*>(A.rslab)[(int64_t)ts * b.total_depth + doff + k] = R(0);
+    }
+  }
   const int64_t coff = b.cont_off[p], ncont = (int64_t)nd * b.nspect[p];
   for (int g = 0; g < A.ngroup; ++g)
     for (int64_t e = threadIdx.x + (int64_t)blockIdx.x * blockDim.x; e < ncont;
@@ -451,10 +462,46 @@ constexpr int kFormalWarps = 4;
 template <typename R>
 struct TileSink {
   R* gslab;           // this tile's partial sums: slot * total_depth + doff + k
+  R* rslab;           // its radiative-rate sums (2 t + {0: R_ij, 1: R_ji}), or nullptr
   R* Jn;              // new J of this lane's wavelength, depth stride ns
   int64_t total_depth, doff;
   int ns;
 };
+
+// Sums a and c over the lanes of the warp that hold the same key, in an
+// order fixed by the lane numbers (a shuffle tree when the whole warp shares
+// the key); returns true on the one lane of each group with key >= 0, which
+// then holds the group's sums.  All lanes of the warp call it together.
+template <typename R>
+__device__ __forceinline__ bool keyed_warp_sum(int key, R& a, R& c) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(full, key);
+  if (peers == full) {
+    if (key < 0) return false;
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(full, a, o);
+      c += __shfl_xor_sync(full, c, o);
+    }
+    return lane == 0;
+  }
+  const int cnt = key >= 0 ? __popc(peers) : 0;
+  const int maxc = __reduce_max_sync(full, cnt);
+  unsigned rem = key >= 0 ? peers : 0u;
+  R sa = R(0), sc = R(0);
+  for (int s = 0; s < maxc; ++s) {
+    const int src = rem ? __ffs(rem) - 1 : lane;
+    const R x = __shfl_sync(full, a, src), y = __shfl_sync(full, c, src);
+    if (rem) {
+      sa += x;
+      sc += y;
+      rem &= rem - 1;
+    }
+  }
+  a = sa;
+  c = sc;
+  return key >= 0 && lane == __ffs(peers) - 1;
+}
 
 // Rate (fillgamma.c:82-332) and J (formal.c:247-256) contributions of one
 // depth of one ray direction, summed over the warp's 32 wavelengths.  All
@@ -537,39 +584,28 @@ __device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_tra
       // one term per active transition whose upper level is i
       if (cnt) gji += R(cnt) * chi_down_j * (psi * U_down_i) * wdir;
     }
-    // Sum over the lanes that add to the same entry, in an order fixed by
-    // the lane numbers, then one addition by the group's first lane.
-    const unsigned peers = __match_any_sync(full, key);
-    R sij, sji;
-    if (peers == full) {
-      if (key < 0) continue;
-      for (int o = 16; o > 0; o >>= 1) {
-        gij += __shfl_xor_sync(full, gij, o);
-        gji += __shfl_xor_sync(full, gji, o);
-      }
-      sij = gij;
-      sji = gji;
-    } else {
-      const int cnt = key >= 0 ? __popc(peers) : 0;
-      const int maxc = __reduce_max_sync(full, cnt);
-      unsigned rem = key >= 0 ? peers : 0u;
-      sij = R(0);
-      sji = R(0);
-      for (int s = 0; s < maxc; ++s) {
-        const int src = rem ? __ffs(rem) - 1 : lane;
-        const R a = __shfl_sync(full, gij, src), c = __shfl_sync(full, gji, src);
-        if (rem) {
-          sij += a;
-          sji += c;
-          rem &= rem - 1;
-        }
-      }
-      if (key < 0 || lane != __ffs(peers) - 1) continue;
+    if (keyed_warp_sum<R>(key, gij, gji)) {
+      const int i = key / nlev, j = key % nlev;
+      atomicAdd(out.gslab + (int64_t)gamma_slot(i, j, nlev) * out.total_depth + out.doff + k, gij);
+      atomicAdd(out.gslab + (int64_t)gamma_slot(j, i, nlev) * out.total_depth + out.doff + k, gji);
     }
-    if (lane != 0 && peers == full) continue;
-    const int i = key / nlev, j = key % nlev;
-    atomicAdd(out.gslab + (int64_t)gamma_slot(i, j, nlev) * out.total_depth + out.doff + k, sij);
-    atomicAdd(out.gslab + (int64_t)gamma_slot(j, i, nlev) * out.total_depth + out.doff + k, sji);
+    if (out.rslab) {
+      // addtoRates (fillgamma.c:446-452): R_ij += I V W, R_ji += g (2 h nu^3 /
+      // c^2 + I) V W, with the intensity itself (not Ieff)
+      int rkey = -1;
+      R rij = 0, rji = 0;
+      if (m < nact && as.t[m] < A.max_ntrans) {
+        rkey = as.t[m];
+        const R wlamu = VW[m] * wdir;
+        rij = I_k * wlamu;
+        rji = G[m] * (as.tw[m] + I_k) * wlamu;
+      }
+      if (keyed_warp_sum<R>(rkey, rij, rji)) {
+        R* r = out.rslab + (int64_t)(2 * rkey) * out.total_depth + out.doff + k;
+        atomicAdd(r, rij);
+        atomicAdd(r + out.total_depth, rji);
+      }
+    }
   }
 }
 
@@ -666,6 +702,9 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
   TileSink<R> out;
   out.gslab = static_cast<R*>(A.gslab) +
               ((int64_t)tile * A.ngroup + grp) * nlev * (nlev - 1) * b.total_depth;
+  out.rslab = A.rslab ? static_cast<R*>(A.rslab) +
+                            ((int64_t)tile * A.ngroup + grp) * 2 * A.max_ntrans * b.total_depth
+                      : nullptr;
   out.Jn = static_cast<R*>(A.Jnew) + grp * b.total_cont + coff + la;
   out.total_depth = b.total_depth;
   out.doff = doff;
@@ -708,6 +747,30 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
     }
   }
   if (emergent_only && live) I_out[b.lam_off[p] + la] = (double)emergent;
+}
+
+// R_ij and R_ji of the atmospheres that took part in this formal solution
+// (the others keep those of their last one): the (tile, ray group) sums
+// added in a fixed order.
+template <typename R>
+__global__ void nlte_rates_kernel(NlteArgs A) {
+  const pyrh_nlte_batch& b = A.b;
+  const int p = blockIdx.y;
+  if (!A.active[p]) return;
+  const int nd = b.ndep[p];
+  const int nt = b.ntrans[p] < A.max_ntrans ? b.ntrans[p] : A.max_ntrans;
+  const int ntg = (b.nspect[p] + 31) / 32 * A.ngroup;
+  const int64_t doff = b.depth_off[p], td = b.total_depth;
+  const int64_t tstride = (int64_t)2 * A.max_ntrans * td;
+  const R* rs = static_cast<const R*>(A.rslab);
+  for (int e = threadIdx.x + blockIdx.x * blockDim.x; e < 2 * nt * nd;
+       e += blockDim.x * gridDim.x) {
+    const int slot = e / nd, k = e % nd;
+    const R* s = rs + (int64_t)slot * td + doff + k;
+    double r = 0.0;
+    for (int t = 0; t < ntg; ++t) r += (double)s[t * tstride];
+    b.rates[(int64_t)slot * td + doff + k] = r;
+  }
 }
 
 // J <- new J for atmospheres still iterating (each wavelength replaces its
@@ -1028,6 +1091,11 @@ static cudaError_t launch_iteration_t(const NlteArgs& A, int natm, int max_nspec
   if (e != cudaSuccess) return e;
   e = launch_formal_t<R>(A, natm, max_nspect, maxd, 0, nullptr, st, set_attr);
   if (e != cudaSuccess) return e;
+  if (A.rslab) {
+    nlte_rates_kernel<R><<<gi, 256, 0, st>>>(A);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   nlte_jcopy_kernel<R><<<gi, 256, 0, st>>>(A);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
@@ -1038,6 +1106,8 @@ static cudaError_t launch_iteration_t(const NlteArgs& A, int natm, int max_nspec
   nlte_ng_kernel<<<natm, 256, 0, st>>>(A, 0);
   return cudaGetLastError();
 }
+
+int nlte_iteration_launches(const NlteArgs& A) { return A.rslab ? 6 : 5; }
 
 cudaError_t nlte_launch_iteration(const NlteArgs& A, int natm, int max_nspect, int maxd,
                                   int precision, cudaStream_t st, bool set_attr) {

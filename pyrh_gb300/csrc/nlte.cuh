@@ -22,6 +22,10 @@ struct NlteArgs {
   // in the formal-solution precision: per (tile, ray group) rate sums, the
   // ray groups' new J, the background [chi_c, eta_c, sca_c] and J
   void *gslab, *Jnew, *bgr, *Jr;
+  // per (tile, ray group) sums of the radiative rates R_ij, R_ji
+  // ([2 max_ntrans][total_depth] each), or nullptr when b.rates is NULL
+  void *rslab;
+  int max_ntrans;
   int32_t *count, *active, *iters, *err;
   int32_t *any;                   // set by nlte_ng_kernel while an atmosphere iterates
 };
@@ -36,7 +40,10 @@ cudaError_t nlte_launch_profiles(const NlteArgs &A, int natm, int64_t max_elems,
 cudaError_t nlte_launch_ng_init(const NlteArgs &A, int natm, cudaStream_t st);
 // background and starting J in the formal-solution precision (once per solve)
 cudaError_t nlte_launch_prepare(const NlteArgs &A, int precision, cudaStream_t st);
-// One MALI iteration (5 launches).  set_attr = false leaves the formal
+// Kernel launches of one MALI iteration: 5, and one more that keeps the
+// radiative rates when the batch asks for them.
+int nlte_iteration_launches(const NlteArgs &A);
+// One MALI iteration.  set_attr = false leaves the formal
 // kernel's shared-memory attribute as an earlier call set it (for stream
 // capture, where the launches are recorded rather than issued).
 cudaError_t nlte_launch_iteration(const NlteArgs &A, int natm, int max_nspect, int maxd,

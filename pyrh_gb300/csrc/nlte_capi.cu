@@ -17,7 +17,8 @@ namespace {
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct Layout {
-  size_t wphi, Jnew, gslab, bgr, Jr, ngprev, count, active, iters, err, any, dpops, phi, fixed;
+  size_t wphi, Jnew, gslab, rslab, bgr, Jr, ngprev, count, active, iters, err, any, dpops, phi,
+      fixed;
 };
 
 int groups_of(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg) {
@@ -37,6 +38,9 @@ Layout layout(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg, int ngroup)
   L.Jnew = off; off = align256(off + r * (size_t)ngroup * b->total_cont);
   const size_t ntile = (size_t)(b->max_nspect + 31) / 32;
   L.gslab = off; off = align256(off + r * ntile * ngroup * nlev * (nlev - 1) * b->total_depth);
+  // the radiative rates' sums, only when the batch keeps the rates
+  const size_t nr = b->rates && b->max_ntrans > 0 ? 2 * (size_t)b->max_ntrans : 0;
+  L.rslab = off; off = align256(off + r * ntile * ngroup * nr * b->total_depth);
   L.bgr = off; off = align256(off + r * 3 * (size_t)b->total_cont);
   L.Jr = off; off = align256(off + r * (size_t)b->total_cont);
   L.ngprev = off; off = align256(off + sizeof(double) * (size_t)(cfg->ng_order + 2) * nlev * b->total_depth);
@@ -83,6 +87,10 @@ pyrh_status check(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg) {
                         b->bgline, b->trans, b->n, b->J};
   for (const void* p : ptrs)
     if (!p) { pyrh::set_error("a batch array pointer is NULL"); return PYRH_ERR_ARG; }
+  if (b->rates && b->max_ntrans < 1) {
+    pyrh::set_error("rates requested with max_ntrans %d", b->max_ntrans);
+    return PYRH_ERR_ARG;
+  }
   return PYRH_OK;
 }
 
@@ -107,6 +115,8 @@ pyrh::NlteArgs make_args(const pyrh_nlte_batch* b, const pyrh_nlte_config* cfg, 
   A.wphi = reinterpret_cast<double*>(w + L.wphi);
   A.Jnew = w + L.Jnew;
   A.gslab = w + L.gslab;
+  A.rslab = b->rates ? w + L.rslab : nullptr;
+  A.max_ntrans = b->rates ? b->max_ntrans : 0;
   A.bgr = w + L.bgr;
   A.Jr = w + L.Jr;
   A.ngprev = reinterpret_cast<double*>(w + L.ngprev);
@@ -137,7 +147,7 @@ cudaError_t iterate(const pyrh::NlteArgs& A, const pyrh_nlte_batch* b,
     for (int c = 0; c < n && e == cudaSuccess; ++c) {
       e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision,
                                       st);
-      *launches += 5;
+      *launches += pyrh::nlte_iteration_launches(A);
     }
     it += n;
     int32_t any = 0;
@@ -152,7 +162,7 @@ cudaError_t iterate(const pyrh::NlteArgs& A, const pyrh_nlte_batch* b,
 
 // The same loop with one chunk of kChunk iterations recorded as a CUDA graph
 // and replayed per chunk on the caller's stream (one graph launch instead
-// of 5 kChunk kernel launches).  The recording uses a private stream, since
+// of kChunk iterations of kernel launches).  The recording uses a private stream, since
 // the caller's may be the legacy default stream, which cannot be captured;
 // nothing runs while recording.  The first chunk runs uncaptured, which
 // also sets the formal kernel's shared-memory attribute before the
@@ -168,7 +178,7 @@ cudaError_t iterate_graph(const pyrh::NlteArgs& A, const pyrh_nlte_batch* b,
     for (int c = 0; c < n && e == cudaSuccess; ++c) {
       e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision,
                                       st);
-      *launches += 5;
+      *launches += pyrh::nlte_iteration_launches(A);
     }
     it += n;
     if (e == cudaSuccess)
@@ -201,7 +211,7 @@ cudaError_t iterate_graph(const pyrh::NlteArgs& A, const pyrh_nlte_batch* b,
         e = pyrh::nlte_launch_iteration(A, b->natm, b->max_nspect, b->max_ndep, cfg->precision,
                                         st);
     }
-    *launches += 5 * kChunk;
+    *launches += pyrh::nlte_iteration_launches(A) * kChunk;
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(&any, A.any, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -266,8 +276,9 @@ pyrh_status pyrh_nlte_solve(const pyrh_nlte_batch* b, const pyrh_nlte_config* cf
     return PYRH_ERR_CUDA;
   }
   if (err) {
-    pyrh::set_error(err & 2 ? "an atmosphere's ndep exceeds max_ndep or the depth limit"
-                            : "line profiles do not fit the workspace (phi_off beyond capacity)");
+    pyrh::set_error(err & 4   ? "an atmosphere's ntrans exceeds max_ntrans (rates)"
+                    : err & 2 ? "an atmosphere's ndep exceeds max_ndep or the depth limit"
+                              : "line profiles do not fit the workspace (phi_off beyond capacity)");
     return PYRH_ERR_ARG;
   }
   for (int p = 0; p < b->natm; ++p)
@@ -428,8 +439,9 @@ extern "C" pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch* b,
     return PYRH_ERR_CUDA;
   }
   if (err) {
-    pyrh::set_error(err & 2 ? "an atmosphere's ndep exceeds max_ndep or the depth limit"
-                            : "line profiles do not fit the static scratch (phi_off beyond phi_elems)");
+    pyrh::set_error(err & 4   ? "an atmosphere's ntrans exceeds max_ntrans (rates)"
+                    : err & 2 ? "an atmosphere's ndep exceeds max_ndep or the depth limit"
+                              : "line profiles do not fit the static scratch (phi_off beyond phi_elems)");
     return PYRH_ERR_ARG;
   }
   for (int p = 0; p < b->natm; ++p)

@@ -43,7 +43,8 @@ class PyrhNlteBatch(C.Structure):
                                    "cont_off", "trans_off", "adamp_off", "lambda_", "height",
                                    "T", "vel", "vbroad", "ntotal", "nstar", "C", "chi_c",
                                    "eta_c", "sca_c", "bgline", "trans", "alpha", "adamp", "n",
-                                   "J")]
+                                   "J")] + \
+        [("max_ntrans", C.c_int32), ("rates", C.c_void_p)]
 
 
 class PyrhNlteConfig(C.Structure):
@@ -176,7 +177,9 @@ def pack(atms: list[dict], nrays: int) -> PackedNlte:
 class DeviceNlte:
     """A packed NLTE batch in GPU memory with its workspace."""
 
-    def __init__(self, pk: PackedNlte, cfg: PyrhNlteConfig, device="cuda"):
+    def __init__(self, pk: PackedNlte, cfg: PyrhNlteConfig, device="cuda", rates=False):
+        """rates: keep every transition's radiative rates R_ij, R_ji after
+        its atmosphere's last formal solution (radiative_rates())."""
         import torch
         self.pk = pk
         self.t = {k: torch.from_numpy(np.ascontiguousarray(v)).to(device)
@@ -192,6 +195,13 @@ class DeviceNlte:
         for k, v in self.t.items():
             setattr(b, k, v.data_ptr())
         b.trans = self.trans_t.data_ptr()
+        self.max_ntrans = int(pk.arrays["ntrans"].max())
+        self.rates = None
+        if rates:
+            self.rates = torch.zeros(2 * self.max_ntrans * pk.shape["total_depth"],
+                                     dtype=torch.float64, device=device)
+            b.max_ntrans = self.max_ntrans
+            b.rates = self.rates.data_ptr()
         self.batch = b
         self.ws_bytes = _lib().pyrh_nlte_workspace_bytes(C.byref(b), C.byref(cfg), pk.phi_elems)
         self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=device)
@@ -230,6 +240,23 @@ class DeviceNlte:
             o = int(self.pk.arrays["cont_off"][p])
             nd, ns = int(self.pk.arrays["ndep"][p]), int(self.pk.arrays["nspect"][p])
             out.append(J[o:o + nd * ns].reshape(nd, ns).T)
+        return out
+
+    def radiative_rates(self) -> list[dict]:
+        """Per atmosphere {"continua": [ncont, 2, ndep], "lines": [nline, 2,
+        ndep]}: R_ij and R_ji [s^-1] of each transition after the
+        atmosphere's last formal solution (needs rates=True)."""
+        if self.rates is None:
+            raise ValueError("DeviceNlte was made without rates=True")
+        R = self.rates.cpu().numpy().reshape(2 * self.max_ntrans, -1)
+        a = self.pk.arrays
+        out = []
+        for p in range(self.pk.natm):
+            o, nd = int(a["depth_off"][p]), int(a["ndep"][p])
+            t0, nt = int(a["trans_off"][p]), int(a["ntrans"][p])
+            r = R[:2 * nt, o:o + nd].reshape(nt, 2, nd)
+            ncont = sum(1 for i in range(t0, t0 + nt) if self.pk.trans[i].type == 1)
+            out.append({"continua": r[:ncont], "lines": r[ncont:]})
         return out
 
     def emergent_spectra(self) -> list[np.ndarray]:

@@ -375,7 +375,9 @@ def nlte_case(name, ndep=82, nlambda_scale=1.0, atom_seed=11, dT=None, vlos=0.0,
     assert not np.any(d["J0"]), "N_MAX_SCATTER = 0 leaves J = 0 before the first iteration"
     out.update(atm=atm, wave=wave, atom_text=np.array(wl.caii_like_atom(atom_seed, nlambda_scale)),
                n_final=d1["n_final"].reshape(nl, -1), J_final=d1["J_final"].reshape(d["J1"].shape),
-               lam_out=d1["lam_out"], I_out=d1["I_out"])
+               lam_out=d1["lam_out"], I_out=d1["I_out"],
+               R_final_line=d1["R_final_line"].reshape(len(d["lines"]), 2, ndep),
+               R_final_cont=d1["R_final_cont"].reshape(len(d["continua"]), 2, ndep))
     path = os.path.join(HERE, name + ".npz")
     np.savez_compressed(path, **out)
     shutil.rmtree(wd, ignore_errors=True)

@@ -83,6 +83,27 @@ def test_converged_fp32(golden, name):
     assert _rel(dev.emergent_spectra()[0][m], fx["I_out"]) < 1e-4
 
 
+@pytest.mark.parametrize("name", PINNED)
+@pytest.mark.parametrize("precision", [L.PYRH_FP32, L.PYRH_FP64])
+def test_radiative_rates(golden, name, precision):
+    """R_ij and R_ji of every transition (addtoRates, fillgamma.c:375-461)
+    after the first formal pass and after the last one of the converged
+    solve, against the reference's; keeping them changes nothing else."""
+    fx = golden(name)
+    tol1, tol = (1e-9, 1e-6) if precision == L.PYRH_FP64 else (1e-5, 1e-4)
+    for nmax, keys, bound in ((1, ("R1_line", "R1_cont"), tol1),
+                              (None, ("R_final_line", "R_final_cont"), tol)):
+        cfg = nlte.make_config(fx, precision, nmax_iter=nmax)
+        dev = nlte.DeviceNlte(nlte.pack([fx], cfg.nrays), cfg, rates=True)
+        st = dev.solve(cfg)
+        assert st == L.PYRH_OK or (nmax == 1 and st == L.PYRH_ERR_NONCONVERGED)
+        R = dev.radiative_rates()[0]
+        assert _rel(R["lines"], fx[keys[0]]) < bound
+        assert _rel(R["continua"], fx[keys[1]]) < bound
+        ref = fx["n1"] if nmax == 1 else fx["n_final"]
+        assert _rel(dev.populations()[0], ref) < (1e-7 if precision == L.PYRH_FP64 else 1e-4)
+
+
 @pytest.mark.parametrize("precision", [L.PYRH_FP32, L.PYRH_FP64])
 def test_bit_reproducible(golden, precision):
     """Three solves of the same ragged batch give identical populations and

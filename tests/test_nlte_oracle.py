@@ -47,6 +47,19 @@ def test_converged_populations_and_emergent(golden, name):
     assert np.abs(Iem[m] / fx["I_out"] - 1).max() < 1e-6
 
 
+@pytest.mark.parametrize("name", PINNED)
+def test_radiative_rates(golden, name):
+    """R_ij and R_ji of every transition (addtoRates) after the first
+    formal pass and after the last one of the converged run."""
+    fx = golden(name)
+    R1 = O.nlte_first_iteration(fx, rates=True)[3]
+    for kind, key in (("lines", "R1_line"), ("continua", "R1_cont")):
+        assert np.abs(R1[kind] / fx[key] - 1).max() < 1e-12, kind
+    R = O.nlte_solve(fx, rates=True)[5]
+    for kind, key in (("lines", "R_final_line"), ("continua", "R_final_cont")):
+        assert np.abs(R[kind] / fx[key] - 1).max() < 1e-7, kind
+
+
 def test_armstrong_voigt_limits():
     # H(0, v) = exp(-v^2); Lorentz wings H ~ a / (sqrt(pi) v^2)
     for v in (0.0, 0.5, 1.7, 3.9):
