@@ -604,6 +604,100 @@ pyrh_status pyrh_nlte_setup(const pyrh_atom *atom, double weight_amu,
                             const pyrh_nlte_setup_batch *batch, void *workspace,
                             size_t workspace_bytes, void *stream);
 
+/* ---------------------------------------------------- background continuum --
+ * The angle-independent background opacity, emissivity and scattering
+ * opacity of Background() (rh/background.c:329-460; replaces the per-call
+ * host pass of the reference's set-up, rhf1d() -> Background()): Thomson
+ * (rh/thomson.c:35), H- bound-free and free-free (rh/hydrogen.c:310-615),
+ * OH and CH bound-free (rh/ohchbf.c:53-691), hydrogen bound-free and
+ * free-free (rh/hydrogen.c:151-305), Rayleigh scattering by H and He
+ * (rh/rayleigh.c:33-100), H + H+ free-free, H2 Rayleigh and H2- free-free
+ * (rh/hydrogen.c:621-995), bound-free of the passive metals
+ * (rh/metal.c:71-171), with the optional fudge factors of compute1d
+ * (background.c:365-455).  Line opacities (Kurucz lists, passive
+ * bound-bound) are not part of it.  FP64.
+ *
+ * The model holds the atomic data every atmosphere shares; the batch holds
+ * each atmosphere's temperatures, densities and wavelengths.  Outputs are in
+ * the continuum layout of pyrh_lte_batch / pyrh_nlte_batch
+ * (cont_off[p] + k * nspect[p] + la). */
+#define PYRH_BG_MAX_OVERLAP 256   /* metal continua covering one wavelength */
+#define PYRH_BG_MAX_DEPTH 512     /* depth points of one atmosphere */
+
+/* A bound-free continuum: hydrogenic, alpha0 (lambda / lambda0)^3 g(lambda)
+   / gbf0 with Seaton's Gaunt factor g(lambda, n_eff, charge) (hydrogen.c:269,
+   metal.c:128-137; for hydrogen alpha0 = sigma0 n_eff, gbf0 = 1, charge =
+   stage + 1, hydrogen.c:183-200), or the natural cubic spline of a table
+   (spline.c); it adds where lambda_min <= lambda <= lambda0. */
+typedef struct {
+  int32_t hydrogenic;       /* 1 hydrogenic, 0 table */
+  int32_t ntab;             /* table points (ascending lambda) at tab_off */
+  int32_t n_i, n_j;         /* rows of pops: populations of the lower / upper level */
+  int32_t nstar_i, nstar_j; /* rows of pops: their LTE populations */
+  int64_t tab_off;          /* first point in tab_lambda / tab_alpha / tab_m2 */
+  double lambda0, lambda_min;   /* nm */
+  double alpha0, n_eff, charge, gbf0;
+} pyrh_bg_continuum;
+
+/* A bound-bound transition from the ground level of a Rayleigh scatterer
+   (rayleigh.c:60-90): it adds f (lambda0^2 / (lambda^2 - lambda0^2))^2 where
+   lambda > lambda_red = lambda0 (1 + qwing vmicro_char / c), with
+   f = Aji (g_j / g_0) (lambda0 [m])^2 / C. */
+typedef struct {
+  double lambda0, lambda_red, f;
+  int32_t scatterer;        /* 0 hydrogen, 1 helium */
+  int32_t reserved;
+} pyrh_bg_rayleigh_line;
+
+typedef struct {
+  int32_t ncont_h;          /* hydrogen's continua, first in cont (not used
+                               when h_active: an active hydrogen adds its own) */
+  int32_t ncont_metal;      /* then the passive metals' in the reference's atom order */
+  const pyrh_bg_continuum *cont;                 /* device */
+  const double *tab_lambda, *tab_alpha;          /* device, the tables of cont */
+  double *tab_m2;           /* device, [ntab_total + 34]: spline second derivatives,
+                               filled by pyrh_background_prepare */
+  int64_t ntab_total;
+  int32_t nray;
+  const pyrh_bg_rayleigh_line *ray;              /* device */
+  double ray_limit[2];      /* per scatterer: the shortest lambda_red of its ground lines */
+  int32_t ray_pop[2];       /* per scatterer: row of pops holding its ground level (-1: none) */
+  int32_t pop_nh0, pop_np;  /* rows of pops: hydrogen ground level, protons */
+  int32_t npop;             /* rows of pops every index above stays below */
+  int32_t h_active;
+  int32_t has_h2, has_oh, has_ch;   /* molecules present (atmos.H2, OH, CH) */
+  int32_t add_scatter;      /* chi_c includes the scattering opacity (NLTE set-up) */
+  int32_t nfudge;           /* optional fudge: 0 or the table length */
+  const double *fudge_lambda;   /* device [nfudge] nm, ascending */
+  const double *fudge;          /* device [3][nfudge]: H-minus, scattering, metals */
+} pyrh_bg_model;
+
+typedef struct {
+  int32_t natm, max_nspect, max_ndep;   /* max_ndep <= PYRH_BG_MAX_DEPTH */
+  int32_t precision;        /* pyrh_precision of the outputs and of the depth loop
+                               (the wavelength terms are FP64 either way) */
+  int64_t total_depth;
+  const int32_t *ndep, *nspect;                    /* [natm] */
+  const int64_t *depth_off, *lam_off, *cont_off;   /* [natm] */
+  const double *lambda;                            /* [total_lambda] nm */
+  const double *T, *ne, *nHmin, *nH2, *nOH, *nCH;  /* [total_depth] K, m^-3 (nH2 / nOH
+                                                      / nCH only where present) */
+  const void *pops;         /* [npop][total_depth] the level populations the model's rows
+                               name, double or float following precision */
+  void *chi_c, *eta_c, *sca_c;                     /* [total_cont] out, double or float */
+} pyrh_bg_batch;
+
+/* Once per model (and again if it changes): checks every row and table
+   index against npop and ntab_total, and puts the spline second derivatives
+   of every tabulated continuum and of the H- bound-free table into
+   model->tab_m2.  PYRH_ERR_UNSUPPORTED when more than PYRH_BG_MAX_OVERLAP
+   metal continua cover one wavelength.  pyrh_background takes only a
+   model that passed it. */
+pyrh_status pyrh_background_prepare(const pyrh_bg_model *model, void *stream);
+/* The background of every atmosphere and wavelength of the batch. */
+pyrh_status pyrh_background(const pyrh_bg_model *model, const pyrh_bg_batch *batch,
+                            void *stream);
+
 /* Number of kernel launches the last pyrh_lte_stokes / pyrh_nlte_* call issued. */
 int32_t pyrh_last_launch_count(void);
 

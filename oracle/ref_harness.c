@@ -146,16 +146,19 @@ int harness_synth_loggf(const char *cwd, double mu, int Ndep, const double *atm,
   return n;
 }
 
-/* Set-up sequence of rhf1d() up to convertScales(), in the same order as
-   pyrh_compute1dray.c:130-311, followed by a dump of the hot-path inputs. */
-int harness_dump_lte(const char *cwd, double mu, int Ndep, const double *atm,
-                     int Nwave, const double *lam, const char *outdir)
+/* Set-up sequence of rhf1d() up to SortLambda() and getBoundary(), in the
+   same order as pyrh_compute1dray.c:130-311, on private copies of the
+   atmosphere rows and wavelengths (returned in *pa / *pw). */
+static void lte_setup(const char *cwd, double mu, int Ndep, const double *atm, int Nwave,
+                      const double *lam, double **pa, double **pw)
 {
   char tmp[512];
   double *a = (double *) malloc(9 * Ndep * sizeof(double));
   double *w = (double *) malloc(Nwave * sizeof(double));
   memcpy(a, atm, 9 * Ndep * sizeof(double));
   memcpy(w, lam, Nwave * sizeof(double));
+  *pa = a;
+  *pw = w;
 
   snprintf(commandline.keyword_input, sizeof(commandline.keyword_input),
            "%s/keyword.input", cwd);
@@ -214,6 +217,15 @@ int harness_dump_lte(const char *cwd, double mu, int Ndep, const double *atm,
   Bproject();
   SortLambda(w, Nwave);
   getBoundary(&geometry);
+}
+
+/* Set-up sequence of rhf1d() up to convertScales(), in the same order as
+   pyrh_compute1dray.c:130-311, followed by a dump of the hot-path inputs. */
+int harness_dump_lte(const char *cwd, double mu, int Ndep, const double *atm,
+                     int Nwave, const double *lam, const char *outdir)
+{
+  double *a, *w;
+  lte_setup(cwd, mu, Ndep, atm, Nwave, lam, &a, &w);
 
   int Nspect = spectrum.Nspect, Nspace = atmos.Nspace;
 
@@ -384,6 +396,148 @@ void initScatter(void);
 void getProfiles(void);
 void Iterate(int NmaxIter, double iterLimit);
 void _solveray(double muz, mySpectrum *spec);
+
+/* The background continuum of the LTE set-up (Background(), rh/background.c:
+   139-631, without line lists: KURUCZ_DATA none, ALLOW_PASSIVE_BB FALSE),
+   each of its processes evaluated alone at every wavelength, and what they
+   read: the densities after the set-up and the atomic data.  Files:
+     lambda [Nspect]; T, ne, nHmin, nH2, nOH, nCH [Nspace] (zeros where a
+     molecule is absent, mol_present[3] says which is present);
+     cont [3][Nspect][Nspace] chi_c, eta_c, sca_c as Background() stores them;
+     comp [13][2][Nspect][Nspace]: per process (0 Thomson, 1 Hminus_bf,
+       2 Hminus_ff, 3 OH_bf, 4 CH_bf, 5 Hydrogen_bf, 6 Hydrogen_ff,
+       7 Rayleigh H, 8 Rayleigh He, 9 H2plus_ff, 10 Rayleigh_H2,
+       11 H2minus_ff, 12 Metal_bf) its opacity and its emissivity (or its
+       scattering opacity), zero where the routine reports no contribution;
+     atoms_meta [Natom][4] Nlevel, Ncont, Nline, active; atoms_lev [sum
+     Nlevel][3] E, g, stage; atoms_n, atoms_nstar [sum Nlevel][Nspace];
+     atoms_cont [sum Ncont][8] i, j, lambda0, lambda[0], hydrogenic, alpha0,
+     Nlambda, table offset; atoms_tab [sum Nlambda][2] lambda, alpha;
+     atoms_line [sum Nline][5] i, j, lambda0, qwing, Aji; misc [4]
+     vmicro_char, index of the He model (-1: none), index of H, Natom. */
+int harness_dump_background(const char *cwd, double mu, int Ndep, const double *atm,
+                            int Nwave, const double *lam, const char *outdir)
+{
+  double *a, *w;
+  lte_setup(cwd, mu, Ndep, atm, Nwave, lam, &a, &w);
+  int Nspect = spectrum.Nspect, Nspace = atmos.Nspace;
+  strcpy(input.KuruczData, "none");
+  atmos.Nrlk = 0;
+  Background(FALSE, FALSE);
+
+  double *cont = (double *) malloc(3L * Nspect * Nspace * sizeof(double));
+  for (int la = 0; la < Nspect; la++) {
+    memcpy(cont + (0L * Nspect + la) * Nspace, spectrum.chi_c_lam[la], Nspace * sizeof(double));
+    memcpy(cont + (1L * Nspect + la) * Nspace, spectrum.eta_c_lam[la], Nspace * sizeof(double));
+    memcpy(cont + (2L * Nspect + la) * Nspace, spectrum.sca_c_lam[la], Nspace * sizeof(double));
+  }
+  write_f64(outdir, "lambda", spectrum.lambda, Nspect);
+  write_f64(outdir, "cont", cont, 3L * Nspect * Nspace);
+  free(cont);
+
+  /* each process alone (the routines keep their temperature indices from
+     the Background() pass, which used the same temperatures) */
+  const int NC = 13;
+  double *comp = (double *) calloc((size_t) NC * 2 * Nspect * Nspace, sizeof(double));
+  double *c1 = (double *) malloc(4L * Nspace * sizeof(double));
+  double *c2 = (double *) malloc(4L * Nspace * sizeof(double));
+  Atom *He = atmos.elements[1].model;
+  for (int la = 0; la < Nspect; la++) {
+    double lw = spectrum.lambda[la];
+    for (int c = 0; c < NC; c++) {
+      bool_t ok = FALSE, two = TRUE;
+      for (int k = 0; k < Nspace; k++) c1[k] = c2[k] = 0.0;
+      switch (c) {
+        case 0: Thomson(c2); ok = TRUE; break;
+        case 1: ok = Hminus_bf(lw, c1, c2); break;
+        case 2: ok = Hminus_ff(lw, c1); two = FALSE; break;
+        case 3: ok = OH_bf_opac(lw, c1, c2); break;
+        case 4: ok = CH_bf_opac(lw, c1, c2); break;
+        case 5: ok = Hydrogen_bf(lw, c1, c2); break;
+        case 6: Hydrogen_ff(lw, c1); ok = TRUE; two = FALSE; break;
+        case 7: ok = Rayleigh(lw, atmos.H, c2); break;
+        case 8: ok = He ? Rayleigh(lw, He, c2) : FALSE; break;
+        case 9: ok = H2plus_ff(lw, c1); two = FALSE; break;
+        case 10: ok = Rayleigh_H2(lw, c2); break;
+        case 11: ok = H2minus_ff(lw, c1); two = FALSE; break;
+        case 12: ok = Metal_bf(lw, atmos.Natom - 1, atmos.atoms + 1, c1, c2); break;
+      }
+      if (!ok) continue;
+      double *dst = comp + (((size_t) c * 2) * Nspect + la) * Nspace;
+      memcpy(dst, c1, Nspace * sizeof(double));
+      if (two) memcpy(dst + (size_t) Nspect * Nspace, c2, Nspace * sizeof(double));
+    }
+  }
+  write_f64(outdir, "comp", comp, (long) NC * 2 * Nspect * Nspace);
+  free(comp); free(c1); free(c2);
+
+  /* densities */
+  double *z = (double *) calloc(Nspace, sizeof(double));
+  int mp[3] = {atmos.H2 != NULL, atmos.OH != NULL, atmos.CH != NULL};
+  write_f64(outdir, "T", atmos.T, Nspace);
+  write_f64(outdir, "ne", atmos.ne, Nspace);
+  write_f64(outdir, "nHmin", atmos.nHmin, Nspace);
+  write_f64(outdir, "nH2", atmos.H2 ? atmos.H2->n : z, Nspace);
+  write_f64(outdir, "nOH", atmos.OH ? atmos.OH->n : z, Nspace);
+  write_f64(outdir, "nCH", atmos.CH ? atmos.CH->n : z, Nspace);
+  write_i32(outdir, "mol_present", mp, 3);
+  free(z);
+
+  /* atomic data */
+  int Natom = atmos.Natom, nlev = 0, ncont = 0, nline = 0, ntab = 0;
+  for (int m = 0; m < Natom; m++) {
+    Atom *at = &atmos.atoms[m];
+    nlev += at->Nlevel; ncont += at->Ncont; nline += at->Nline;
+    for (int kr = 0; kr < at->Ncont; kr++) ntab += at->continuum[kr].Nlambda;
+  }
+  int *meta = (int *) malloc(4L * Natom * sizeof(int));
+  double *lev = (double *) malloc(3L * nlev * sizeof(double));
+  double *pn = (double *) malloc((long) nlev * Nspace * sizeof(double));
+  double *pst = (double *) malloc((long) nlev * Nspace * sizeof(double));
+  double *cr = (double *) malloc(8L * (ncont > 0 ? ncont : 1) * sizeof(double));
+  double *tb = (double *) malloc(2L * (ntab > 0 ? ntab : 1) * sizeof(double));
+  double *lr = (double *) malloc(5L * (nline > 0 ? nline : 1) * sizeof(double));
+  int il = 0, ic = 0, it = 0, ik = 0, he_index = -1, h_index = -1;
+  for (int m = 0; m < Natom; m++) {
+    Atom *at = &atmos.atoms[m];
+    if (at == He) he_index = m;
+    if (at == atmos.H) h_index = m;
+    meta[4 * m] = at->Nlevel; meta[4 * m + 1] = at->Ncont;
+    meta[4 * m + 2] = at->Nline; meta[4 * m + 3] = at->active;
+    for (int i = 0; i < at->Nlevel; i++, il++) {
+      lev[3 * il] = at->E[i]; lev[3 * il + 1] = at->g[i]; lev[3 * il + 2] = at->stage[i];
+      memcpy(pn + (long) il * Nspace, at->n[i], Nspace * sizeof(double));
+      memcpy(pst + (long) il * Nspace, at->nstar[i], Nspace * sizeof(double));
+    }
+    for (int kr = 0; kr < at->Ncont; kr++, ic++) {
+      AtomicContinuum *c = &at->continuum[kr];
+      double *r = cr + 8L * ic;
+      r[0] = c->i; r[1] = c->j; r[2] = c->lambda0; r[3] = c->lambda[0];
+      r[4] = c->hydrogenic; r[5] = c->alpha0; r[6] = c->Nlambda; r[7] = it;
+      for (int t = 0; t < c->Nlambda; t++, it++) {
+        tb[2L * it] = c->lambda[t];
+        tb[2L * it + 1] = c->alpha[t];
+      }
+    }
+    for (int kr = 0; kr < at->Nline; kr++, ik++) {
+      AtomicLine *l = &at->line[kr];
+      double *r = lr + 5L * ik;
+      r[0] = l->i; r[1] = l->j; r[2] = l->lambda0; r[3] = l->qwing; r[4] = l->Aji;
+    }
+  }
+  write_i32(outdir, "atoms_meta", meta, 4L * Natom);
+  write_f64(outdir, "atoms_lev", lev, 3L * nlev);
+  write_f64(outdir, "atoms_n", pn, (long) nlev * Nspace);
+  write_f64(outdir, "atoms_nstar", pst, (long) nlev * Nspace);
+  write_f64(outdir, "atoms_cont", cr, 8L * ncont);
+  write_f64(outdir, "atoms_tab", tb, 2L * ntab);
+  write_f64(outdir, "atoms_line", lr, 5L * nline);
+  double misc[4] = {atmos.vmicro_char, he_index, h_index, Natom};
+  write_f64(outdir, "misc", misc, 4);
+  free(meta); free(lev); free(pn); free(pst); free(cr); free(tb); free(lr);
+  free(a); free(w);
+  return Nspect;
+}
 
 /* Set-up of rhf1d() with an ACTIVE atom, up to initScatter()
    (pyrh_compute1dray.c:130-323). */

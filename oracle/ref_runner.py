@@ -198,6 +198,38 @@ def _dump_job(args):
                                 _p(atm), len(wave), _p(wave), outdir.encode())
 
 
+def _background_job(args):
+    workdir, pyrh_path, mu, atm, wave, outdir = args
+    lib = _lib(pyrh_path)
+    atm = np.ascontiguousarray(atm, dtype=np.float64)
+    wave = np.ascontiguousarray(wave, dtype=np.float64)
+    os.makedirs(outdir, exist_ok=True)
+    lib.harness_dump_background.restype = C.c_int
+    return lib.harness_dump_background(workdir.encode(), C.c_double(mu), atm.shape[1],
+                                       _p(atm), len(wave), _p(wave), outdir.encode())
+
+
+def read_background_dump(outdir: str) -> dict:
+    """The files of harness_dump_background as arrays."""
+    f64 = lambda n: np.fromfile(os.path.join(outdir, n + ".f64"))
+    i32 = lambda n: np.fromfile(os.path.join(outdir, n + ".i32"), dtype=np.int32)
+    d = {"lambda": f64("lambda")}
+    ns, nd = len(d["lambda"]), len(f64("T"))
+    for k in ("T", "ne", "nHmin", "nH2", "nOH", "nCH", "misc"):
+        d[k] = f64(k)
+    d["mol_present"] = i32("mol_present")
+    d["cont"] = f64("cont").reshape(3, ns, nd)
+    d["comp"] = f64("comp").reshape(13, 2, ns, nd)
+    d["atoms_meta"] = i32("atoms_meta").reshape(-1, 4)
+    d["atoms_lev"] = f64("atoms_lev").reshape(-1, 3)
+    d["atoms_n"] = f64("atoms_n").reshape(-1, nd)
+    d["atoms_nstar"] = f64("atoms_nstar").reshape(-1, nd)
+    d["atoms_cont"] = f64("atoms_cont").reshape(-1, 8)
+    d["atoms_tab"] = f64("atoms_tab").reshape(-1, 2)
+    d["atoms_line"] = f64("atoms_line").reshape(-1, 5)
+    return d
+
+
 def _vac2air_job(args):
     pyrh_path, lam_vac = args
     lib = _lib(pyrh_path)
@@ -257,6 +289,9 @@ class Reference:
 
     def dump_lte(self, workdir, mu, atm, wave, outdir):
         return self._run(_dump_job, (workdir, self.pyrh_path, mu, atm, wave, outdir))
+
+    def dump_background(self, workdir, mu, atm, wave, outdir):
+        return self._run(_background_job, (workdir, self.pyrh_path, mu, atm, wave, outdir))
 
     def nlte(self, workdir, mu, atm, wave, outdir, mode):
         return self._run(_nlte_job, (workdir, self.pyrh_path, mu, atm, wave, outdir, mode))

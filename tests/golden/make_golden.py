@@ -45,6 +45,11 @@ Fixtures (npz, float64):
                   with velocity fields and other wavelength counts
   nlte_static     nlte_c1 in a static atmosphere (VMACRO_TRESH 0.1 km/s, no
                   velocity): every wavelength takes the Feautrier solver
+  background      the background continuum of the LTE set-up (Background()
+                  without line lists) at 240 wavelengths from 120 to 20000
+                  nm for the C0 atmosphere and a cooler one, with the
+                  densities and atomic data it reads, and for C0 each
+                  process alone
 
 stokes_ref comes from the reference as setup.py builds it on x86 (-DSIMDON,
 SSE reciprocal-estimate 4x4 inverse); stokes_ref_portable from the same
@@ -405,6 +410,45 @@ def make_nlte_static(ref, wd):
     nlte_case("nlte_static", ndep=82, vmacro_tresh="0.1")
 
 
+def make_background(ref, wd):
+    """Background() (background.c:139-631, no Kurucz list, no passive
+    lines) on the C0 atmosphere and on a cooler one (T - 1500 K above log
+    tau 0, at least 2600 K, so that the molecules and the low-temperature
+    ends of the tables matter), both with their own hse() densities."""
+    wave = np.geomspace(120.0, 20000.0, 240)
+    out = {}
+    for a, shift in enumerate((0.0, 1500.0)):
+        logtau = wl.logtau_grid(71)
+        T = wl.base_temperature(logtau)
+        T = np.where(logtau < 0.0, np.maximum(T - shift, 2600.0), T)
+        w = rr.scratch_dir()
+        rr.write_inputs(w, None)
+        ne, nH = ref.hse(w, logtau, T)
+        atm = wl.atmosphere_rows(logtau, T, ne / 1e6, nH / 1e6)
+        d = rr.read_background_dump(_dump_background(ref, w, atm, wave))
+        if a == 0:
+            for k in ("lambda", "mol_present", "misc", "atoms_meta", "atoms_lev", "atoms_cont",
+                      "atoms_tab", "atoms_line", "comp"):
+                out[k] = d[k]
+        else:
+            assert np.array_equal(d["lambda"], out["lambda"])
+            assert np.array_equal(d["atoms_cont"], out["atoms_cont"])
+        for k in ("T", "ne", "nHmin", "nH2", "nOH", "nCH", "atoms_n", "atoms_nstar", "cont"):
+            out.setdefault(k, []).append(d[k])
+        shutil.rmtree(w, ignore_errors=True)
+    for k in ("T", "ne", "nHmin", "nH2", "nOH", "nCH", "atoms_n", "atoms_nstar", "cont"):
+        out[k] = np.stack(out[k])
+    path = os.path.join(HERE, "background.npz")
+    np.savez_compressed(path, **out)
+    print(f"background: {len(out['lambda'])} lambda, {os.path.getsize(path) / 1e3:.0f} kB")
+
+
+def _dump_background(ref, workdir, atm, wave):
+    outdir = os.path.join(workdir, "bg")
+    ref.dump_background(workdir, 1.0, atm, wave, outdir)
+    return outdir
+
+
 def make_kurucz(ref, wd):
     """Inputs and outputs of the reference's Kurucz line-list reader
     (readKuruczLines, RLKZeeman, the Barklem and Unsold cross-sections) for
@@ -448,7 +492,8 @@ MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
           "lte_static": make_lte_static, "lte_broadening": make_lte_broadening,
-          "nlte": make_nlte, "nlte_static": make_nlte_static, "kurucz": make_kurucz}
+          "nlte": make_nlte, "nlte_static": make_nlte_static, "kurucz": make_kurucz,
+          "background": make_background}
 
 
 def main():
