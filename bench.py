@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-rf", action="store_true")
     ap.add_argument("--skip-nlte", action="store_true")
+    ap.add_argument("--skip-background", action="store_true")
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--rf-natm", type=int, default=4096)
     ap.add_argument("--nlte-natm", type=int, default=1024)
@@ -303,6 +304,55 @@ def nlte_oracle_solve(atms, nthreads):
     with ThreadPoolExecutor(nthreads) as ex:
         res = list(ex.map(O.nlte_solve, atms))
     return [r[0] for r in res], [int(r[2]) for r in res], time.perf_counter() - t0
+
+
+def background_measure(natm, local, stream, steps, warmup):
+    """GPU background continuum (Background(), rh/background.c:329-460) at
+    the batched synthesis' shape: natm atmospheres x 224 wavelengths x 71
+    depths (the C0 atmosphere of the background fixture, whose densities and
+    atomic data the reference's set-up produced), FP32 and FP64, CUDA
+    events; the FP64 result against the reference's own Background() on the
+    fixture's two atmospheres (120-20000 nm) and FP32 against FP64."""
+    import torch
+    from pyrh_gb300 import _lib as L
+    from pyrh_gb300 import background as BGR
+    fx = dict(np.load(os.path.join(HERE, "tests", "golden", "background.npz")))
+    dev = BGR.DeviceBackground(BGR.model_from_setup(fx), device=f"cuda:{local}")
+    lam = np.linspace(630.0, 630.35, 224)
+    atm = BGR.setup_atmosphere(fx, 0)
+    out = {"workload": f"{natm} atmospheres x 224 wavelengths (630.0-630.35 nm) x 71 depths; "
+                       "11 passive atoms (157 continua), H2, OH, CH"}
+    units = natm * 224 * 71
+    for prec, tag in ((L.PYRH_FP32, "fp32"), (L.PYRH_FP64, "fp64")):
+        b, keep = dev.replicated_batch(atm, lam, natm, prec)
+        for _ in range(warmup):
+            dev.run(b, stream.cuda_stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            dev.run(b, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out[tag] = {"ms": ms, "value": units / (ms / 1e3), "unit": "lambda*depth points/s",
+                    "bytes_written": 3 * units * (4 if prec == L.PYRH_FP32 else 8)}
+        del keep
+        torch.cuda.empty_cache()
+    atms = [BGR.setup_atmosphere(fx, a) for a in range(2)]
+    r64 = dev.compute(atms)
+    r32 = dev.compute(atms, precision=L.PYRH_FP32)
+    err_ref, err_32 = 0.0, 0.0
+    for q in range(3):
+        for a in range(2):
+            err_ref = max(err_ref, float(np.abs(r64[q][a] / fx["cont"][a][q] - 1).max()))
+            m = np.abs(r64[q][a]) > 1e-30
+            err_32 = max(err_32, float(np.abs(r32[q][a][m] / r64[q][a][m] - 1).max()))
+    out["fp64_vs_reference_max_rel_err"] = err_ref
+    out["fp32_vs_fp64_max_rel_err"] = err_32
+    out["error_metric"] = ("chi_c, eta_c, sca_c element-wise relative, 2 atmospheres x 241 "
+                           "wavelengths x 71 depths (FP32: where |FP64| > 1e-30)")
+    return out
 
 
 def nlte_measure(natm, local, nsample=32):
@@ -591,6 +641,10 @@ def main():
         torch.cuda.empty_cache()
     if rank == 0 and not args.skip_nlte:
         extra["nlte"] = nlte_measure(args.nlte_natm, local)
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.skip_background:
+        extra["background"] = background_measure(args.natm, local, stream,
+                                                 max(2, min(args.steps, 5)), args.warmup)
         torch.cuda.empty_cache()
 
     cpu = None

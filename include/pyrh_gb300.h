@@ -621,7 +621,6 @@ pyrh_status pyrh_nlte_setup(const pyrh_atom *atom, double weight_amu,
  * each atmosphere's temperatures, densities and wavelengths.  Outputs are in
  * the continuum layout of pyrh_lte_batch / pyrh_nlte_batch
  * (cont_off[p] + k * nspect[p] + la). */
-#define PYRH_BG_MAX_OVERLAP 256   /* metal continua covering one wavelength */
 #define PYRH_BG_MAX_DEPTH 512     /* depth points of one atmosphere */
 
 /* A bound-free continuum: hydrogenic, alpha0 (lambda / lambda0)^3 g(lambda)
@@ -657,6 +656,9 @@ typedef struct {
   const double *tab_lambda, *tab_alpha;          /* device, the tables of cont */
   double *tab_m2;           /* device, [ntab_total + 34]: spline second derivatives,
                                filled by pyrh_background_prepare */
+  float *tab_f32;           /* device, [3][ntab_total]: tab_lambda, tab_alpha and tab_m2
+                               in FP32, filled by pyrh_background_prepare for FP32
+                               batches (NULL: FP64 batches only) */
   int64_t ntab_total;
   int32_t nray;
   const pyrh_bg_rayleigh_line *ray;              /* device */
@@ -664,6 +666,9 @@ typedef struct {
   int32_t ray_pop[2];       /* per scatterer: row of pops holding its ground level (-1: none) */
   int32_t pop_nh0, pop_np;  /* rows of pops: hydrogen ground level, protons */
   int32_t npop;             /* rows of pops every index above stays below */
+  int32_t nonlte;           /* 1 if a metal continuum's n rows are not its n* rows
+                               (populations other than the LTE ones); checked by
+                               pyrh_background_prepare */
   int32_t h_active;
   int32_t has_h2, has_oh, has_ch;   /* molecules present (atmos.H2, OH, CH) */
   int32_t add_scatter;      /* chi_c includes the scattering opacity (NLTE set-up) */
@@ -688,11 +693,12 @@ typedef struct {
 } pyrh_bg_batch;
 
 /* Once per model (and again if it changes): checks every row and table
-   index against npop and ntab_total, and puts the spline second derivatives
-   of every tabulated continuum and of the H- bound-free table into
-   model->tab_m2.  PYRH_ERR_UNSUPPORTED when more than PYRH_BG_MAX_OVERLAP
-   metal continua cover one wavelength.  pyrh_background takes only a
-   model that passed it. */
+   index against npop and ntab_total and the nonlte flag against the rows,
+   and puts the spline second derivatives of every tabulated continuum and
+   of the H- bound-free table into model->tab_m2 (and the FP32 copies into
+   tab_f32).  pyrh_background takes only a model that passed it;
+   PYRH_ERR_UNSUPPORTED there when max_ndep needs more shared memory than a
+   block has (more than about 1300 depths in FP64). */
 pyrh_status pyrh_background_prepare(const pyrh_bg_model *model, void *stream);
 /* The background of every atmosphere and wavelength of the batch. */
 pyrh_status pyrh_background(const pyrh_bg_model *model, const pyrh_bg_batch *batch,

@@ -53,9 +53,11 @@ class BgRayleighLine(C.Structure):
 class BgModel(C.Structure):
     _fields_ = [("ncont_h", C.c_int32), ("ncont_metal", C.c_int32), ("cont", C.c_void_p),
                 ("tab_lambda", C.c_void_p), ("tab_alpha", C.c_void_p), ("tab_m2", C.c_void_p),
+                ("tab_f32", C.c_void_p),
                 ("ntab_total", C.c_int64), ("nray", C.c_int32), ("ray", C.c_void_p),
                 ("ray_limit", C.c_double * 2), ("ray_pop", C.c_int32 * 2),
                 ("pop_nh0", C.c_int32), ("pop_np", C.c_int32), ("npop", C.c_int32),
+                ("nonlte", C.c_int32),
                 ("h_active", C.c_int32), ("has_h2", C.c_int32), ("has_oh", C.c_int32),
                 ("has_ch", C.c_int32), ("add_scatter", C.c_int32), ("nfudge", C.c_int32),
                 ("fudge_lambda", C.c_void_p), ("fudge", C.c_void_p)]
@@ -218,16 +220,22 @@ class DeviceBackground:
         self.ta = torch.from_numpy(np.append(model.tab_alpha, 0.0)).to(device)
         self.m2 = torch.zeros(len(model.tab_lambda) + HMIN_BF_POINTS, dtype=torch.float64,
                               device=device)
+        self.f32 = torch.zeros(3 * max(len(model.tab_lambda), 1), dtype=torch.float32,
+                               device=device)
         m = BgModel()
         m.ncont_h, m.ncont_metal = model.ncont_h, model.ncont_metal
         m.cont = self.cont_t.data_ptr()
         m.tab_lambda, m.tab_alpha, m.tab_m2 = self.tl.data_ptr(), self.ta.data_ptr(), self.m2.data_ptr()
+        m.tab_f32 = self.f32.data_ptr()
         m.ntab_total = len(model.tab_lambda)
         m.nray = model.nray
         m.ray = self.ray_t.data_ptr()
         m.ray_limit[0], m.ray_limit[1] = model.ray_limit
         m.ray_pop[0], m.ray_pop[1] = model.ray_pop
         m.pop_nh0, m.pop_np, m.npop = model.pop_nh0, model.pop_np, model.npop
+        m.nonlte = int(any(model.cont[c].n_i != model.cont[c].nstar_i or
+                           model.cont[c].n_j != model.cont[c].nstar_j
+                           for c in range(model.ncont_h, model.ncont_h + model.ncont_metal)))
         m.h_active = int(model.h_active)
         m.has_h2, m.has_oh, m.has_ch = (int(x) for x in model.molecules)
         m.add_scatter = int(add_scatter)
@@ -239,6 +247,38 @@ class DeviceBackground:
             m.fudge_lambda, m.fudge = self.fl.data_ptr(), self.fv.data_ptr()
         self.m = m
         L.check(_lib().pyrh_background_prepare(C.byref(m), stream_ptr))
+
+    def replicated_batch(self, atm: dict, lam, natm: int, precision=L.PYRH_FP32):
+        """A device batch of natm copies of one atmosphere on the wavelengths
+        lam (for timing): (BgBatch, the tensors behind it)."""
+        import torch
+        dev = self.device
+        nd, ns = len(atm["T"]), len(lam)
+        rep = lambda x: torch.from_numpy(np.ascontiguousarray(
+            np.tile(np.asarray(x, np.float64), natm))).to(dev)
+        rows = atm["nstar"] if self.model.lte else np.concatenate([atm["n"], atm["nstar"]], axis=0)
+        dt = np.float32 if precision == L.PYRH_FP32 else np.float64
+        t = {"ndep": torch.full((natm,), nd, dtype=torch.int32, device=dev),
+             "nspect": torch.full((natm,), ns, dtype=torch.int32, device=dev),
+             "depth_off": torch.arange(natm, dtype=torch.int64, device=dev) * nd,
+             "lam_off": torch.arange(natm, dtype=torch.int64, device=dev) * ns,
+             "cont_off": torch.arange(natm, dtype=torch.int64, device=dev) * (nd * ns),
+             "lambda_": rep(lam), "T": rep(atm["T"]), "ne": rep(atm["ne"]),
+             "nHmin": rep(atm["nHmin"]), "nH2": rep(atm["nH2"]), "nOH": rep(atm["nOH"]),
+             "nCH": rep(atm["nCH"]),
+             "pops": torch.from_numpy(np.ascontiguousarray(np.tile(rows, (1, natm)), dt)).to(dev)}
+        for k in ("chi_c", "eta_c", "sca_c"):
+            t[k] = torch.empty(natm * nd * ns, dtype=torch.float32 if dt == np.float32
+                               else torch.float64, device=dev)
+        b = BgBatch()
+        b.natm, b.max_nspect, b.max_ndep, b.total_depth = natm, ns, nd, natm * nd
+        b.precision = int(precision)
+        for k, v in t.items():
+            setattr(b, k, v.data_ptr())
+        return b, t
+
+    def run(self, batch: BgBatch, stream_ptr: int = 0) -> None:
+        L.check(_lib().pyrh_background(C.byref(self.m), C.byref(batch), stream_ptr))
 
     def compute(self, atms: list[dict], precision=L.PYRH_FP64, stream_ptr: int = 0):
         """(chi_c, eta_c, sca_c), each a list of [nspect, ndep] arrays, in

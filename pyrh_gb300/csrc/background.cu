@@ -150,6 +150,44 @@ __device__ __forceinline__ double gaunt_bf(double lam, double n_eff, double char
          0.0496 * (x3 * x3) * (1.0 - (1.0 - nsqx) * 0.66666667 * nsqx);
 }
 
+// The same in the working precision (the metal continua's cross-sections,
+// evaluated per atmosphere).
+template <typename R>
+__device__ __forceinline__ R gaunt_bf_r(R lam, R n_eff, R charge) {
+  if constexpr (sizeof(R) == 8) {
+    return gaunt_bf(lam, n_eff, charge);
+  } else {
+    const float x = (float(kHPLANCK * kCLIGHT / kNM_TO_M / kE_RYDBERG) / lam) / (charge * charge);
+    const float x3 = powf(x, 0.33333333f);
+    const float nsqx = 1.0f / ((n_eff * n_eff) * x);
+    return 1.0f + 0.1728f * x3 * (1.0f - 2.0f * nsqx) -
+           0.0496f * (x3 * x3) * (1.0f - (1.0f - nsqx) * 0.66666667f * nsqx);
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ int bracket_r(const R* t, int n, R x) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (hi + lo) >> 1;
+    if (x >= t[mid]) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <typename R>
+__device__ __forceinline__ R spline_eval_r(const R* x, const R* y, const R* M, int n, R v) {
+  if (v <= x[0]) return y[0];
+  if (v >= x[n - 1]) return y[n - 1];
+  const int j = bracket_r<R>(x, n, v);
+  const R hj = x[j + 1] - x[j];
+  const R fx = (v - x[j]) / hj;
+  const R fx1 = R(1) - fx;
+  return fx1 * y[j] + fx * y[j + 1] +
+         (fx1 * (fx1 * fx1 - R(1)) * M[j] + fx * (fx * fx - R(1)) * M[j + 1]) * (hj * hj) / R(6);
+}
+
 // Natural cubic spline through (x, y) with second derivatives M (spline.c).
 __device__ __forceinline__ double spline_eval(const double* x, const double* y, const double* M,
                                               int n, double v) {
@@ -161,6 +199,30 @@ __device__ __forceinline__ double spline_eval(const double* x, const double* y, 
   const double fx1 = 1 - fx;
   return fx1 * y[j] + fx * y[j + 1] +
          (fx1 * (fx1 * fx1 - 1) * M[j] + fx * (fx * fx - 1) * M[j + 1]) * (hj * hj) / 6.0;
+}
+
+// Cross-section of a metal continuum at lambda (metal.c:126-140).
+template <typename R>
+__device__ __forceinline__ R metal_alpha(const pyrh_bg_model& m, const pyrh_bg_continuum& C,
+                                         double lam) {
+  if constexpr (sizeof(R) == 8) {
+    if (C.hydrogenic) {
+      const double r = lam / C.lambda0;
+      return C.alpha0 * (r * r * r) * gaunt_bf(lam, C.n_eff, C.charge) / C.gbf0;
+    }
+    return spline_eval(m.tab_lambda + C.tab_off, m.tab_alpha + C.tab_off, m.tab_m2 + C.tab_off,
+                       C.ntab, lam);
+  } else {
+    const float l = (float)lam;
+    if (C.hydrogenic) {
+      const float r = l / (float)C.lambda0;
+      return (float)C.alpha0 * (r * r * r) * gaunt_bf_r<float>(l, (float)C.n_eff, (float)C.charge) /
+             (float)C.gbf0;
+    }
+    const int64_t N = m.ntab_total;
+    return spline_eval_r<float>(m.tab_f32 + C.tab_off, m.tab_f32 + N + C.tab_off,
+                                m.tab_f32 + 2 * N + C.tab_off, C.ntab, l);
+  }
 }
 
 // linear.c:22-51 for one value of an ascending table.
@@ -203,6 +265,13 @@ __global__ void bg_spline_kernel(pyrh_bg_model m) {
     if (C.hydrogenic || C.ntab < 2 || C.ntab > 64) return;
     spline_coef(m.tab_lambda + C.tab_off, m.tab_alpha + C.tab_off, C.ntab,
                 m.tab_m2 + C.tab_off, u);
+    if (m.tab_f32)
+      for (int i = 0; i < C.ntab; ++i) {
+        const int64_t o = C.tab_off + i;
+        m.tab_f32[o] = (float)m.tab_lambda[o];
+        m.tab_f32[m.ntab_total + o] = (float)m.tab_alpha[o];
+        m.tab_f32[2 * m.ntab_total + o] = (float)m.tab_m2[o];
+      }
   } else if (c == ncont) {
     spline_coef(kHmBfLam, kHmBfAlpha, kHmBfN, m.tab_m2 + m.ntab_total, u);
   }
@@ -261,7 +330,7 @@ struct LambdaTerms {
   bool hmbf, hm_long, oh, ch, ray[2], h2p, rh2, h2m;
   R hck, tw, a_hm, john[6], li_hm, ei_oh, ei_ch, nu3, x3ff, yT, sig_ray[2], li_h2p, sig_rh2,
       li_h2m, hf, sf, mf;
-  int nh, nmet;
+  int nh;
   // Each covered continuum is one entry (cross-section, row): row >= 0 names
   // the lower level's population row of a continuum whose populations are
   // the LTE ones (n = n*: its emissivity 2 h nu^3 / c^2 (n*_i / n*_j) e^-x
@@ -269,9 +338,6 @@ struct LambdaTerms {
   // -1 - row of any other.
   int hc_row[kMaxHCont];
   R hc_sig[kMaxHCont];
-  int mc_row[PYRH_BG_MAX_OVERLAP];
-  R mc_alpha[PYRH_BG_MAX_OVERLAP];
-
   __device__ void init(const pyrh_bg_model& m, double lam, double sigma_T) {
     const double hc_kla = (kHPLANCK * kCLIGHT) / (kKBOLTZMANN * kNM_TO_M * lam);
     const double lm = kNM_TO_M * lam;
@@ -358,24 +424,6 @@ struct LambdaTerms {
       const int j = bracket(kH2mLam, kH2mNL, lam);
       li_h2m = R(j + (lam - kH2mLam[j]) / (kH2mLam[j + 1] - kH2mLam[j]));
     }
-    // metals: cross-sections of the continua covering lambda
-    nmet = 0;
-    for (int c = m.ncont_h; c < m.ncont_h + m.ncont_metal; ++c) {
-      const pyrh_bg_continuum& C = m.cont[c];
-      if (!(lam <= C.lambda0 && lam >= C.lambda_min)) continue;
-      if (nmet == PYRH_BG_MAX_OVERLAP) break;
-      double a;
-      if (C.hydrogenic) {
-        const double r = lam / C.lambda0;
-        a = C.alpha0 * (r * r * r) * gaunt_bf(lam, C.n_eff, C.charge) / C.gbf0;
-      } else {
-        a = spline_eval(m.tab_lambda + C.tab_off, m.tab_alpha + C.tab_off, m.tab_m2 + C.tab_off,
-                        C.ntab, lam);
-      }
-      mc_row[nmet] = (C.n_i == C.nstar_i && C.n_j == C.nstar_j) ? C.n_i : -1 - c;
-      mc_alpha[nmet] = R(a);
-      ++nmet;
-    }
     hf = sf = mf = R(1);
     if (m.nfudge > 1) {
       hf = R(linear(m.fudge_lambda, m.fudge, m.nfudge, lam));
@@ -385,13 +433,24 @@ struct LambdaTerms {
   }
 };
 
-// Atmospheres per block: the wavelength terms are evaluated once for the
-// group when its atmospheres share the wavelength (the usual batch).
+// Atmospheres per block, at most: the wavelength terms are evaluated once
+// for the group when its atmospheres share the wavelength (the usual
+// batch); small batches take smaller groups so that every SM has blocks.
 constexpr int kGroup = 8;
+
+// Shared memory of a block: the depth fields, then the metal continua's
+// per-depth sums [nacc][max_ndep][blockDim] (nacc 1, or 3 with non-LTE
+// continua): each thread adds its wavelength's continua into its own
+// column, one continuum at a time, so the cross-sections are evaluated once
+// per atmosphere and wavelength and never stored.
+template <typename R>
+__host__ __device__ inline size_t bg_smem_bytes(int max_ndep, int block, int nonlte) {
+  return sizeof(R) * (size_t)max_ndep * (kDepthFields + (size_t)(nonlte ? 3 : 1) * block);
+}
 
 template <typename R>
 __global__ void __launch_bounds__(kBlock)
-bg_kernel(pyrh_bg_model m, pyrh_bg_batch b) {
+bg_kernel(pyrh_bg_model m, pyrh_bg_batch b, int group) {
   extern __shared__ __align__(16) unsigned char bg_smem[];
   R* ds = reinterpret_cast<R*>(bg_smem);
   const int MD = b.max_ndep;
@@ -404,18 +463,22 @@ bg_kernel(pyrh_bg_model m, pyrh_bg_batch b) {
   const double sigma_ff = 4.0 / 3.0 * sqrt(2.0 * kPI / (3.0 * kKBOLTZMANN)) * (C0 * C0 * C0) /
                           (kHPLANCK * kCLIGHT);
   const R sT = R(sigma_T);
-  const int la = blockIdx.x * kBlock + threadIdx.x;
+  const int bd = blockDim.x, tid = threadIdx.x;
+  const int la = blockIdx.x * bd + tid;
+  R* acc_s = ds + kDepthFields * MD;       // sum of alpha n_i of the LTE continua
+  R* acc_c = acc_s + (size_t)MD * bd;      // non-LTE: sum of alpha n_i
+  R* acc_e = acc_c + (size_t)MD * bd;      // non-LTE: sum of alpha (n*_i / n*_j) n_j
   LambdaTerms<R> t;
   double lam_have = -1.0;
   R* chi_o = static_cast<R*>(b.chi_c);
   R* eta_o = static_cast<R*>(b.eta_c);
   R* sca_o = static_cast<R*>(b.sca_c);
   auto D = [&](int f, int k) { return ds[f * MD + k]; };
-  for (int pi = 0; pi < kGroup; ++pi) {
-    const int p = blockIdx.y * kGroup + pi;
+  for (int pi = 0; pi < group; ++pi) {
+    const int p = blockIdx.y * group + pi;
     if (p >= b.natm) break;                              // uniform in the block
     const int nd = b.ndep[p], ns = b.nspect[p];
-    if ((int)blockIdx.x * kBlock >= ns || nd > MD) continue;   // uniform in the block
+    if ((int)blockIdx.x * bd >= ns || nd > MD) continue;   // uniform in the block
     const int64_t doff = b.depth_off[p], coff = b.cont_off[p];
     __syncthreads();                                     // the previous atmosphere's reads
     for (int k = threadIdx.x; k < nd; k += blockDim.x) {
@@ -449,6 +512,30 @@ bg_kernel(pyrh_bg_model m, pyrh_bg_batch b) {
     if (!(lam == lam_have)) {
       t.init(m, lam, sigma_T);
       lam_have = lam;
+    }
+    // metals (metal.c:103-153): per-depth sums of the continua covering lambda
+    for (int k = 0; k < nd; ++k) acc_s[k * bd + tid] = R(0);
+    if (m.nonlte)
+      for (int k = 0; k < nd; ++k) acc_c[k * bd + tid] = acc_e[k * bd + tid] = R(0);
+    bool any_metal = false;
+    for (int c = m.ncont_h; c < m.ncont_h + m.ncont_metal; ++c) {
+      const pyrh_bg_continuum& C = m.cont[c];
+      if (!(lam <= C.lambda0 && lam >= C.lambda_min)) continue;
+      any_metal = true;
+      const R a = metal_alpha<R>(m, C, lam);
+      if (C.n_i == C.nstar_i && C.n_j == C.nstar_j) {
+        const R* pi = P + (int64_t)C.n_i * td + doff;
+        for (int k = 0; k < nd; ++k) acc_s[k * bd + tid] += a * pi[k];
+      } else {
+        const R* pi = P + (int64_t)C.n_i * td + doff;
+        const R* pj = P + (int64_t)C.n_j * td + doff;
+        const R* si = P + (int64_t)C.nstar_i * td + doff;
+        const R* sj = P + (int64_t)C.nstar_j * td + doff;
+        for (int k = 0; k < nd; ++k) {
+          acc_c[k * bd + tid] += a * pi[k];
+          acc_e[k * bd + tid] += a * (si[k] / sj[k] * pj[k]);
+        }
+      }
     }
 
     // --- down the atmosphere
@@ -541,11 +628,12 @@ bg_kernel(pyrh_bg_model m, pyrh_bg_batch b) {
         chi += cff;
         eta += cff * B;
       }
-      if (t.nmet > 0) {
-        R cm, em;
-        continuum_sums<R>(m, P, td, d, t.mc_row, t.mc_alpha, t.nmet, omex, t.tw * ex, cm, em);
-        chi += cm * t.mf;
-        eta += em * t.mf;
+      if (any_metal) {
+        const R sl = acc_s[k * bd + tid];
+        const R cm = m.nonlte ? sl + acc_c[k * bd + tid] : sl;
+        const R em = m.nonlte ? sl + acc_e[k * bd + tid] : sl;
+        chi += cm * omex * t.mf;
+        eta += t.tw * ex * em * t.mf;
       }
       sca *= t.sf;
       if (m.add_scatter) chi += sca;
@@ -571,8 +659,8 @@ pyrh_status pyrh_background_prepare(const pyrh_bg_model* model, void* stream) {
     return PYRH_ERR_ARG;
   }
   const int ncont = model->ncont_h + model->ncont_metal;
-  // the widest overlap of metal continua, from a host copy of the edges
-  if (model->ncont_metal > 0) {
+  // rows, tables and the nonlte flag, from a host copy of the continua
+  if (ncont > 0) {
     pyrh_bg_continuum* hc = new pyrh_bg_continuum[ncont];
     cudaError_t e = cudaMemcpy(hc, model->cont, sizeof(pyrh_bg_continuum) * ncont,
                                cudaMemcpyDeviceToHost);
@@ -581,8 +669,7 @@ pyrh_status pyrh_background_prepare(const pyrh_bg_model* model, void* stream) {
       pyrh::set_error("background model: %s", cudaGetErrorString(e));
       return PYRH_ERR_CUDA;
     }
-    int worst = 0;
-    bool bad_tab = false, bad_row = false;
+    bool bad_tab = false, bad_row = false, nonlte = false;
     auto row_ok = [&](int32_t r) { return r >= 0 && r < model->npop; };
     for (int c = 0; c < ncont; ++c) {
       const pyrh_bg_continuum& C = hc[c];
@@ -592,22 +679,18 @@ pyrh_status pyrh_background_prepare(const pyrh_bg_model* model, void* stream) {
                             C.tab_off + C.ntab > model->ntab_total))
         bad_tab = true;
       if (c < model->ncont_h) continue;
-      int n = 0;
-      for (int q = model->ncont_h; q < ncont; ++q)
-        if (C.lambda0 <= hc[q].lambda0 && C.lambda0 >= hc[q].lambda_min) ++n;
-      worst = n > worst ? n : worst;
+      if (C.n_i != C.nstar_i || C.n_j != C.nstar_j) nonlte = true;
     }
     delete[] hc;
+    if (nonlte && !model->nonlte) {
+      pyrh::set_error("background model: non-LTE metal continua with nonlte = 0");
+      return PYRH_ERR_ARG;
+    }
     if (bad_row || bad_tab) {
       pyrh::set_error(bad_row ? "background model: a population row outside [0, npop)"
                               : "background model: a table with fewer than 2 or more than 64 "
                                 "points, or outside ntab_total");
       return PYRH_ERR_ARG;
-    }
-    if (worst > PYRH_BG_MAX_OVERLAP) {
-      pyrh::set_error("background model: %d metal continua overlap (limit %d)", worst,
-                      PYRH_BG_MAX_OVERLAP);
-      return PYRH_ERR_UNSUPPORTED;
     }
   }
   const int n = ncont + 1;
@@ -631,9 +714,8 @@ pyrh_status pyrh_background(const pyrh_bg_model* model, const pyrh_bg_batch* b, 
     pyrh::set_error("background batch: NULL array or empty batch");
     return PYRH_ERR_ARG;
   }
-  if (b->natm > 65535 * pyrh::kGroup) {
-    pyrh::set_error("background batch: %d atmospheres (limit %d per call)", b->natm,
-                    65535 * pyrh::kGroup);
+  if (b->natm > 65535) {
+    pyrh::set_error("background batch: %d atmospheres (limit 65535 per call)", b->natm);
     return PYRH_ERR_ARG;
   }
   if (b->max_ndep < 1 || b->max_ndep > PYRH_BG_MAX_DEPTH) {
@@ -648,21 +730,41 @@ pyrh_status pyrh_background(const pyrh_bg_model* model, const pyrh_bg_batch* b, 
     pyrh::set_error("background model: a population row outside [0, npop) or a NULL table");
     return PYRH_ERR_ARG;
   }
-  dim3 g((b->max_nspect + pyrh::kBlock - 1) / pyrh::kBlock,
-         (b->natm + pyrh::kGroup - 1) / pyrh::kGroup);
-  const size_t r = b->precision == PYRH_FP32 ? sizeof(float) : sizeof(double);
-  const size_t smem = r * pyrh::kDepthFields * (size_t)b->max_ndep;
+  // the widest block (of 32 to 128 threads) whose sums fit the shared memory
+  const bool f32 = b->precision == PYRH_FP32;
+  if (f32 && !model->tab_f32) {
+    pyrh::set_error("background: an FP32 batch needs model->tab_f32");
+    return PYRH_ERR_ARG;
+  }
+  auto smem_of = [&](int bs) {
+    return f32 ? pyrh::bg_smem_bytes<float>(b->max_ndep, bs, model->nonlte)
+               : pyrh::bg_smem_bytes<double>(b->max_ndep, bs, model->nonlte);
+  };
+  int bs = pyrh::kBlock;
+  while (bs > 32 && smem_of(bs) > 160 * 1024) bs -= 32;
+  const size_t smem = smem_of(bs);
+  if (smem > 220 * 1024) {
+    pyrh::set_error("background: %d depths need %zu B of shared memory", b->max_ndep, smem);
+    return PYRH_ERR_UNSUPPORTED;
+  }
+  const int ntile = (b->max_nspect + bs - 1) / bs;
+  int dev = 0, nsm = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  int group = (int)(((int64_t)b->natm * ntile) / (4 * (int64_t)nsm));
+  group = group < 1 ? 1 : (group > pyrh::kGroup ? pyrh::kGroup : group);
+  dim3 g(ntile, (b->natm + group - 1) / group);
   cudaError_t ea;
-  if (b->precision == PYRH_FP32) {
+  if (f32) {
     ea = cudaFuncSetAttribute(pyrh::bg_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)smem);
     if (ea == cudaSuccess)
-      pyrh::bg_kernel<float><<<g, pyrh::kBlock, smem, (cudaStream_t)stream>>>(*model, *b);
+      pyrh::bg_kernel<float><<<g, bs, smem, (cudaStream_t)stream>>>(*model, *b, group);
   } else {
     ea = cudaFuncSetAttribute(pyrh::bg_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)smem);
     if (ea == cudaSuccess)
-      pyrh::bg_kernel<double><<<g, pyrh::kBlock, smem, (cudaStream_t)stream>>>(*model, *b);
+      pyrh::bg_kernel<double><<<g, bs, smem, (cudaStream_t)stream>>>(*model, *b, group);
   }
   if (ea != cudaSuccess) {
     pyrh::set_error("background: %s", cudaGetErrorString(ea));

@@ -4,6 +4,7 @@
     python -m pyrh_gb300.profile_case grad --natm 2048 --reps 2
     python -m pyrh_gb300.profile_case rf   --natm 512  --reps 2
     python -m pyrh_gb300.profile_case nlte --natm 64   --reps 1
+    python -m pyrh_gb300.profile_case background --natm 1024 --reps 3
 
 lte:  pyrh_lte_stokes (FP32) over natm perturbed atmospheres, 71 depths,
       2 x 112 wavelengths (the batched synthesis workload at a smaller size).
@@ -11,6 +12,8 @@ grad: pyrh_lte_chi2_grad (FP32) on the same shape.
 rf:   pyrh_lte_rf (FP32): full depth-resolved response functions.
 nlte: pyrh_nlte_solve (FP32 formal solution) over natm atmospheres cycled
       from the three NLTE fixtures of tests/golden.
+background: pyrh_background (FP32) for natm copies of the C0 atmosphere of
+      the background fixture on 224 wavelengths at 630.0-630.35 nm.
 Prints one line per case with the time of the last repetition (CUDA events).
 """
 from __future__ import annotations
@@ -36,7 +39,7 @@ def _time(fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["lte", "grad", "rf", "nlte"])
+    ap.add_argument("case", choices=["lte", "grad", "rf", "nlte", "background"])
     ap.add_argument("--natm", type=int, default=2048)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--fp64", action="store_true")
@@ -45,7 +48,17 @@ def main(argv=None):
     from . import _lib as L
     from . import lte, nlte, rf as RF, workload
     prec = L.PYRH_FP64 if a.fp64 else L.PYRH_FP32
-    if a.case == "nlte":
+    if a.case == "background":
+        from . import background as BGR
+        here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+        fx = dict(np.load(os.path.join(here, "tests", "golden", "background.npz")))
+        dev = BGR.DeviceBackground(BGR.model_from_setup(fx))
+        batch, keep = dev.replicated_batch(BGR.setup_atmosphere(fx, 0),
+                                           np.linspace(630.0, 630.35, 224), a.natm, prec)
+
+        def run():
+            dev.run(batch)
+    elif a.case == "nlte":
         here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
         names = ["nlte_c1", "nlte_c4_50", "nlte_c4_120"]
         gold = [dict(np.load(os.path.join(here, "tests", "golden", n + ".npz"))) for n in names]
