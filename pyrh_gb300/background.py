@@ -195,6 +195,14 @@ def model_from_setup(s: dict, lte: bool = True) -> Model:
                  npop=nlev if lte else 2 * nlev, lte=lte, h_active=h_active, molecules=mol)
 
 
+def continuum_on(dev: "DeviceBackground", atm: dict, lam, precision=L.PYRH_FP64):
+    """chi_c and eta_c [nlam, ndep] of one atmosphere on the wavelengths lam
+    (the layout compute1d's LteSetup and pyrh_gb300.lte take)."""
+    chi, eta, _ = dev.compute([dict(atm, **{"lambda": np.asarray(lam, np.float64)})],
+                              precision=precision)
+    return chi[0], eta[0]
+
+
 def setup_atmosphere(s: dict, a: int) -> dict:
     """Atmosphere a of the `background` fixture in the form compute() takes."""
     return {"lambda": s["lambda"], "T": s["T"][a], "ne": s["ne"][a], "nHmin": s["nHmin"][a],

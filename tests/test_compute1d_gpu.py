@@ -107,3 +107,31 @@ def test_compute1d_from_the_line_list_text(golden, tmp_path, lst, name):
     ic = ref[0].max()
     for s in range(4):
         assert np.abs(out[s] - ref[s]).max() < 1e-5 * ic, s
+
+
+@pytest.mark.parametrize("precision,tol", [(L.PYRH_FP64, 1e-5), (L.PYRH_FP32, 1e-4)])
+def test_compute1d_with_the_gpu_background(golden, tmp_path, precision, tol):
+    """The per-wavelength set-up of the C0 synthesis on the device: the
+    background continuum from the set-up's densities (pyrh_background, the
+    `background` fixture's C0 atmosphere is lte_c0's) on the wavelength grid
+    the library builds, then the synthesis -- against the reference's
+    compute1d.  The continuum itself within 1e-12 of the reference's (FP64)."""
+    from dataclasses import replace
+
+    from pyrh_gb300 import background as B
+    fx, bg = golden("lte_c0"), golden("background")
+    assert np.array_equal(fx["T"], bg["T"][0]) and np.array_equal(fx["ne"], bg["ne"][0])
+    dev = B.DeviceBackground(B.model_from_setup(bg))
+    chi, eta = B.continuum_on(dev, B.setup_atmosphere(bg, 0), fx["lam"], precision)
+    if precision == L.PYRH_FP64:
+        assert np.abs(chi / fx["chi_c"] - 1).max() < 1e-12
+        assert np.abs(eta / fx["eta_c"] - 1).max() < 1e-12
+    setup = replace(setup_of(fx), chi_c=np.asarray(chi, np.float64),
+                    eta_c=np.asarray(eta, np.float64))
+    cwd = keyword_dir(tmp_path, fx, "FULL_STOKES")
+    sI, sQ, sU, sV, lam = C1.compute1d(cwd, float(fx["mu"]), 0, np.ascontiguousarray(fx["atm"]),
+                                        fx["wave"], setup=setup, precision=precision)
+    ref = fx["stokes_ref_portable"]
+    ic = ref[0].max()
+    for s, got in enumerate((sI, sQ, sU, sV)):
+        assert np.abs(got - ref[s]).max() < tol * ic, (s, np.abs(got - ref[s]).max() / ic)
