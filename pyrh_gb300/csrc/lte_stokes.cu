@@ -45,7 +45,23 @@ struct Smem {
   double* lam0;  // [nline]
   int* meta;     // [nline][3]: ncomp, polarizable, contributes
   R* dlam;       // [nline][block]: lambda - lambda0 of each thread's wavelength
+  float* lc;     // [nline][LC_N]: per-line constants of the FP32 set-up
   int maxd;
+};
+
+// Per-line constants of the single-precision set-up (phase 1 of the FP32
+// kernel), formed in FP64 once per block.
+enum LineConst {
+  LC_VTH = 0,  // 2 k / (amu weight): v_D^2 = LC_VTH T + v_turb^2
+  LC_CL0,      // c / lambda0
+  LC_DAMP,     // lambda0 [m] / (4 pi)
+  LC_LARM,     // Larmor constant x lambda0
+  LC_XI,       // E_i / k
+  LC_XIJ,      // h c / (lambda0 k)
+  LC_BIJ,      // h c / (4 pi) B_ij x isotope and hyperfine fractions x g_i
+  LC_BIJE,     // the same x A_ji / B_ji
+  LC_GRAD, LC_GSTARK, LC_CROSS, LC_VDWX,  // damping: G_vdW = LC_CROSS T^LC_VDWX
+  LC_N
 };
 
 template <typename R>
@@ -60,19 +76,24 @@ __device__ __forceinline__ Smem<R> carve(unsigned char* base, int nline, int max
   s.cq = reinterpret_cast<int*>(base + off); off += sizeof(int) * nline * PYRH_MAX_COMPONENTS;
   s.meta = reinterpret_cast<int*>(base + off); off += sizeof(int) * nline * 3;
   off = (off + sizeof(R) - 1) / sizeof(R) * sizeof(R);
-  s.dlam = reinterpret_cast<R*>(base + off);
+  s.dlam = reinterpret_cast<R*>(base + off); off += sizeof(R) * nline * blockDim.x;
+  s.lc = reinterpret_cast<float*>(base + off);
   s.maxd = maxd;
   return s;
 }
 
 // The per-thread line offsets live in shared memory ([line][thread], one
 // bank per thread): as a runtime-indexed register array they took a stack
-// frame and pushed the FP32 kernel into spills.
+// frame and pushed the FP32 kernel into spills.  (The DELO window's opacity
+// at four depths, 28 values in registers, also spills at the 64-register cap;
+// a per-thread ring of it in shared memory removed those spills but measured
+// slower: the spilled values are L1 hits, the ring's loads cost issue slots.)
 template <typename R>
 size_t smem_bytes(int nline, int maxd, int block) {
   return sizeof(double) * nline + sizeof(R) * GF_N * maxd + sizeof(R) * nline * LF_N * maxd +
          2 * sizeof(R) * nline * PYRH_MAX_COMPONENTS + sizeof(int) * nline * PYRH_MAX_COMPONENTS +
-         sizeof(int) * nline * 3 + sizeof(R) + sizeof(R) * nline * block + 16;
+         sizeof(int) * nline * 3 + sizeof(R) + sizeof(R) * nline * block +
+         sizeof(float) * nline * LC_N + 16;
 }
 
 struct Work {
@@ -489,8 +510,10 @@ __device__ __forceinline__ void synth_wavelength(const LteArgs& args, const Smem
         pol |= (sm.meta[3 * l + 1] != 0);
       }
     }
-    const double B0 = planck(args.T[doff + nd - 2], lam);
-    const double B1 = planck(args.T[doff + nd - 1], lam);
+    const double B0 = sizeof(R) == 4 ? (double)planck_f((float)args.T[doff + nd - 2], lam)
+                                     : planck(args.T[doff + nd - 2], lam);
+    const double B1 = sizeof(R) == 4 ? (double)planck_f((float)args.T[doff + nd - 1], lam)
+                                     : planck(args.T[doff + nd - 1], lam);
     const R* ds = sm.geo + GF_DS * sm.maxd;
     R st[4] = {0, 0, 0, 0};
     // angle dependent (formal.c:96-101): a polarizable line in window, or
@@ -516,6 +539,162 @@ __device__ __noinline__ void synth_wavelength_unpol(const LteArgs& args, const S
                                                     int la0, int nl, int nd, int nline,
                                                     int64_t doff) {
   synth_wavelength<R, MO, true>(args, sm, p, la0, nl, nd, nline, doff);
+}
+
+// Phase 1 of the synthesis kernel in FP64: per depth, the path length and
+// the projected field geometry (Bproject, project.c:38-79); per line and
+// depth, the Doppler width, shift, damping, Zeeman splitting and LTE line
+// opacity and emissivity (kurucz.c:638-680, 729-790).
+template <typename R>
+__device__ __forceinline__ void setup_f64(const LteArgs& args, const Smem<R>& sm, int64_t doff,
+                                          int nd, int nline, double muz, double imu) {
+  for (int k = threadIdx.x; k < nd; k += blockDim.x) {
+    const int64_t d = doff + k;
+    const double z_k = args.height[d];
+    sm.geo[GF_DS * sm.maxd + k] = (k >= 1) ? R(fabs(z_k - args.height[d - 1]) * imu) : R(0);
+    // Bproject (project.c:38-79)
+    const double gam = args.gamma_B[d], chb = args.chi_B[d];
+    double cg, c2c, s2c;
+    if (muz == 1.0) {
+      cg = cos(gam); c2c = cos(2.0 * chb); s2c = sin(2.0 * chb);
+    } else {
+      const double mux = sqrt(1.0 - muz * muz), csc = 1.0 / sqrt(1.0 - muz * muz);
+      const double sg = sin(gam);
+      const double bx = sg * cos(chb), by = sg * sin(chb), bz = cos(gam);
+      const double b3 = mux * bx + muz * bz;
+      const double b1 = csc * (bz - muz * b3);
+      const double b2 = csc * (-mux * by);
+      cg = b3;
+      c2c = (b1 * b1 - b2 * b2) / (1.0 - b3 * b3);
+      s2c = 2.0 * b1 * b2 / (1.0 - b3 * b3);
+    }
+    const double s2g = 1.0 - cg * cg;
+    sm.geo[GF_GQ * sm.maxd + k] = R(s2g * c2c);
+    sm.geo[GF_GU * sm.maxd + k] = R(s2g * s2c);
+    sm.geo[GF_GV * sm.maxd + k] = R(cg);
+    sm.geo[GF_SIN2G * sm.maxd + k] = R(s2g);
+  }
+  for (int i = threadIdx.x; i < nline * nd; i += blockDim.x) {
+    const int l = i / nd, k = i % nd;
+    const int64_t d = doff + k;
+    const pyrh_line& L = args.lines[l];
+    const double T = args.T[d], vt = args.vturb[d];
+    const double vtherm = 2.0 * kKBOLTZMANN / (kAMU * L.weight);
+    const double vb = sqrt(vtherm * T + vt * vt);
+    const double sv = 1.0 / (kSQRTPI * vb);
+    R* lp = sm.lp + (size_t)l * LF_N * sm.maxd;
+    lp[LF_INVVB * sm.maxd + k] = R(kCLIGHT / (L.lambda0 * vb));
+    lp[LF_VSHIFT * sm.maxd + k] = args.moving ? R(muz * args.vlos[d] / vb) : R(0);
+    double adamp = -1.0;
+    if (L.Grad != 0.0) {
+      double GvdW;
+      if (L.vdwaals == PYRH_VDW_UNSOLD) GvdW = L.cross * pow(T, 0.3);
+      else if (L.vdwaals == PYRH_VDW_BARKLEM) GvdW = L.cross * pow(T, (1.0 - L.alpha) / 2.0);
+      else GvdW = L.GvdWaals;
+      adamp = (L.Grad + L.GStark * args.ne[d] + GvdW * (args.nHtot[d] - args.np[d])) *
+              (L.lambda0 * kNM_TO_M) / (4.0 * kPI * vb);
+    }
+    lp[LF_ADAMP * sm.maxd + k] = R(adamp);
+    lp[LF_VB * sm.maxd + k] = R((kLARMOR * L.lambda0) * args.B[d] / vb);
+    // LTE line strength (kurucz.c:638-680)
+    const double hc = kHPLANCK * kCLIGHT;
+    const double hc_la = hc / (L.lambda0 * kNM_TO_M);
+    const double Bijhc_4PI = hc / (4.0 * kPI) * L.Bij * L.isotope_frac * L.hyperfine_frac * L.gi;
+    const double twohnu3_c2 = L.Aji / L.Bji;
+    const double kT = 1.0 / (kKBOLTZMANN * T);
+    const double nst = args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d];
+    const double lnU = args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d];
+    const double ni_gi = nst * exp(-L.Ei * kT - lnU);
+    const double nj_gj = ni_gi * exp(-hc_la * kT);
+    lp[LF_CHI * sm.maxd + k] = R(Bijhc_4PI * (ni_gi - nj_gj) * sv);
+    lp[LF_ETA * sm.maxd + k] = R(Bijhc_4PI * twohnu3_c2 * nj_gj * sv);
+  }
+}
+
+// Per-line constants of the FP32 set-up (formed in FP64, stored as float).
+__device__ __forceinline__ void line_constants(const pyrh_line& L, float* c) {
+  const double hc = kHPLANCK * kCLIGHT;
+  c[LC_VTH] = float(2.0 * kKBOLTZMANN / (kAMU * L.weight));
+  c[LC_CL0] = float(kCLIGHT / L.lambda0);
+  c[LC_DAMP] = float((L.lambda0 * kNM_TO_M) / (4.0 * kPI));
+  c[LC_LARM] = float(kLARMOR * L.lambda0);
+  c[LC_XI] = float(L.Ei / kKBOLTZMANN);
+  c[LC_XIJ] = float(hc / (L.lambda0 * kNM_TO_M * kKBOLTZMANN));
+  const double bij = hc / (4.0 * kPI) * L.Bij * L.isotope_frac * L.hyperfine_frac * L.gi;
+  c[LC_BIJ] = float(bij);
+  c[LC_BIJE] = float(bij * (L.Aji / L.Bji));
+  c[LC_GRAD] = float(L.Grad);
+  c[LC_GSTARK] = float(L.GStark);
+  if (L.vdwaals == PYRH_VDW_UNSOLD) {
+    c[LC_CROSS] = float(L.cross); c[LC_VDWX] = 0.3f;
+  } else if (L.vdwaals == PYRH_VDW_BARKLEM) {
+    c[LC_CROSS] = float(L.cross); c[LC_VDWX] = float((1.0 - L.alpha) / 2.0);
+  } else {
+    c[LC_CROSS] = float(L.GvdWaals); c[LC_VDWX] = 0.0f;
+  }
+}
+
+// Phase 1 in FP32 (the FP32 kernel): the same quantities from the per-line
+// constants, without FP64 arithmetic except the path lengths (a difference
+// of heights) and the geometry of oblique rays.
+template <typename R>
+__device__ __forceinline__ void setup_f32(const LteArgs& args, const Smem<R>& sm, int64_t doff,
+                                          int nd, int nline, double muz, double imu) {
+  const int maxd = sm.maxd;
+  for (int k = threadIdx.x; k < nd; k += blockDim.x) {
+    const int64_t d = doff + k;
+    sm.geo[GF_DS * maxd + k] = (k >= 1) ? R(fabs(args.height[d] - args.height[d - 1]) * imu) : R(0);
+    float cg, c2c, s2c;
+    if (muz == 1.0) {
+      cg = cosf((float)args.gamma_B[d]);
+      sincosf(2.0f * (float)args.chi_B[d], &s2c, &c2c);
+    } else {  // Bproject for an oblique ray, in FP64 (the denominators vanish along the ray)
+      const double gam = args.gamma_B[d], chb = args.chi_B[d];
+      const double mux = sqrt(1.0 - muz * muz), csc = 1.0 / sqrt(1.0 - muz * muz);
+      const double sg = sin(gam);
+      const double bx = sg * cos(chb), by = sg * sin(chb), bz = cos(gam);
+      const double b3 = mux * bx + muz * bz;
+      const double b1 = csc * (bz - muz * b3);
+      const double b2 = csc * (-mux * by);
+      cg = float(b3);
+      c2c = float((b1 * b1 - b2 * b2) / (1.0 - b3 * b3));
+      s2c = float(2.0 * b1 * b2 / (1.0 - b3 * b3));
+    }
+    const float s2g = 1.0f - cg * cg;
+    sm.geo[GF_GQ * maxd + k] = R(s2g * c2c);
+    sm.geo[GF_GU * maxd + k] = R(s2g * s2c);
+    sm.geo[GF_GV * maxd + k] = R(cg);
+    sm.geo[GF_SIN2G * maxd + k] = R(s2g);
+  }
+  const float rsqrtpi = float(1.0 / kSQRTPI);
+  for (int i = threadIdx.x; i < nline * nd; i += blockDim.x) {
+    const int l = i / nd, k = i % nd;
+    const int64_t d = doff + k;
+    const float* c = sm.lc + l * LC_N;
+    const float T = (float)args.T[d], vt = (float)args.vturb[d];
+    const float vb = sqrtf(fmaf(c[LC_VTH], T, vt * vt));
+    const float rvb = 1.0f / vb;
+    R* lp = sm.lp + (size_t)l * LF_N * maxd;
+    lp[LF_INVVB * maxd + k] = R(c[LC_CL0] * rvb);
+    lp[LF_VSHIFT * maxd + k] = args.moving ? R((float)(muz * args.vlos[d]) * rvb) : R(0);
+    float adamp = -1.0f;
+    if (c[LC_GRAD] != 0.0f) {
+      const float GvdW = c[LC_CROSS] * powf(T, c[LC_VDWX]);
+      adamp = (c[LC_GRAD] + c[LC_GSTARK] * (float)args.ne[d] +
+               GvdW * (float)(args.nHtot[d] - args.np[d])) * c[LC_DAMP] * rvb;
+    }
+    lp[LF_ADAMP * maxd + k] = R(adamp);
+    lp[LF_VB * maxd + k] = R(c[LC_LARM] * (float)args.B[d] * rvb);
+    // LTE line strength (kurucz.c:638-680)
+    const float rT = 1.0f / T;
+    const float nst = (float)args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d];
+    const float lnU = (float)args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d];
+    const float ni_gi = nst * expf(-c[LC_XI] * rT - lnU);
+    const float nj_gj = ni_gi * expf(-c[LC_XIJ] * rT);
+    const float sv = rvb * rsqrtpi;
+    lp[LF_CHI * maxd + k] = R(c[LC_BIJ] * (ni_gi - nj_gj) * sv);
+    lp[LF_ETA * maxd + k] = R(c[LC_BIJE] * nj_gj * sv);
+  }
 }
 
 // Resident blocks per SM the FP32 kernel is compiled for (register cap
@@ -548,6 +727,7 @@ lte_stokes_kernel(LteArgs args) {
                              : 0;
     sm.meta[3 * l + 1] = args.lines[l].polarizable;
     sm.meta[3 * l + 2] = args.lines[l].contributes;
+    if (sizeof(R) == 4) line_constants(args.lines[l], sm.lc + l * LC_N);
   }
 
   const double muz = args.mu, imu = 1.0 / args.mu;
@@ -564,67 +744,10 @@ lte_stokes_kernel(LteArgs args) {
     __syncthreads();  // shared tables of the previous work item are consumed
 
     // ---- phase 1: depth- and line-dependent, wavelength-independent ----
-    for (int k = threadIdx.x; k < nd; k += BL) {
-      const int64_t d = doff + k;
-      const double z_k = args.height[d];
-      sm.geo[GF_DS * sm.maxd + k] = (k >= 1) ? R(fabs(z_k - args.height[d - 1]) * imu) : R(0);
-      // Bproject (project.c:38-79)
-      const double gam = args.gamma_B[d], chb = args.chi_B[d];
-      double cg, c2c, s2c;
-      if (muz == 1.0) {
-        cg = cos(gam); c2c = cos(2.0 * chb); s2c = sin(2.0 * chb);
-      } else {
-        const double mux = sqrt(1.0 - muz * muz), csc = 1.0 / sqrt(1.0 - muz * muz);
-        const double sg = sin(gam);
-        const double bx = sg * cos(chb), by = sg * sin(chb), bz = cos(gam);
-        const double b3 = mux * bx + muz * bz;
-        const double b1 = csc * (bz - muz * b3);
-        const double b2 = csc * (-mux * by);
-        cg = b3;
-        c2c = (b1 * b1 - b2 * b2) / (1.0 - b3 * b3);
-        s2c = 2.0 * b1 * b2 / (1.0 - b3 * b3);
-      }
-      const double s2g = 1.0 - cg * cg;
-      sm.geo[GF_GQ * sm.maxd + k] = R(s2g * c2c);
-      sm.geo[GF_GU * sm.maxd + k] = R(s2g * s2c);
-      sm.geo[GF_GV * sm.maxd + k] = R(cg);
-      sm.geo[GF_SIN2G * sm.maxd + k] = R(s2g);
-    }
-    for (int i = threadIdx.x; i < nline * nd; i += BL) {
-      const int l = i / nd, k = i % nd;
-      const int64_t d = doff + k;
-      const pyrh_line& L = args.lines[l];
-      const double T = args.T[d], vt = args.vturb[d];
-      const double vtherm = 2.0 * kKBOLTZMANN / (kAMU * L.weight);
-      const double vb = sqrt(vtherm * T + vt * vt);
-      const double sv = 1.0 / (kSQRTPI * vb);
-      R* lp = sm.lp + (size_t)l * LF_N * sm.maxd;
-      lp[LF_INVVB * sm.maxd + k] = R(kCLIGHT / (L.lambda0 * vb));
-      lp[LF_VSHIFT * sm.maxd + k] = args.moving ? R(muz * args.vlos[d] / vb) : R(0);
-      double adamp = -1.0;
-      if (L.Grad != 0.0) {
-        double GvdW;
-        if (L.vdwaals == PYRH_VDW_UNSOLD) GvdW = L.cross * pow(T, 0.3);
-        else if (L.vdwaals == PYRH_VDW_BARKLEM) GvdW = L.cross * pow(T, (1.0 - L.alpha) / 2.0);
-        else GvdW = L.GvdWaals;
-        adamp = (L.Grad + L.GStark * args.ne[d] + GvdW * (args.nHtot[d] - args.np[d])) *
-                (L.lambda0 * kNM_TO_M) / (4.0 * kPI * vb);
-      }
-      lp[LF_ADAMP * sm.maxd + k] = R(adamp);
-      lp[LF_VB * sm.maxd + k] = R((kLARMOR * L.lambda0) * args.B[d] / vb);
-      // LTE line strength (kurucz.c:638-680)
-      const double hc = kHPLANCK * kCLIGHT;
-      const double hc_la = hc / (L.lambda0 * kNM_TO_M);
-      const double Bijhc_4PI = hc / (4.0 * kPI) * L.Bij * L.isotope_frac * L.hyperfine_frac * L.gi;
-      const double twohnu3_c2 = L.Aji / L.Bji;
-      const double kT = 1.0 / (kKBOLTZMANN * T);
-      const double nst = args.line_pops[((int64_t)l * 2 + 0) * args.total_depth + d];
-      const double lnU = args.line_pops[((int64_t)l * 2 + 1) * args.total_depth + d];
-      const double ni_gi = nst * exp(-L.Ei * kT - lnU);
-      const double nj_gj = ni_gi * exp(-hc_la * kT);
-      lp[LF_CHI * sm.maxd + k] = R(Bijhc_4PI * (ni_gi - nj_gj) * sv);
-      lp[LF_ETA * sm.maxd + k] = R(Bijhc_4PI * twohnu3_c2 * nj_gj * sv);
-    }
+    if (sizeof(R) == 4)
+      setup_f32(args, sm, doff, nd, nline, muz, imu);
+    else
+      setup_f64(args, sm, doff, nd, nline, muz, imu);
     __syncthreads();
 
     // ---- phase 2: one wavelength per thread ----

@@ -259,6 +259,17 @@ PYRH_HD double planck(double T, double lambda) {
   return (x <= 150.0) ? twohnu3_c2 / (exp(x) - 1.0) : 0.0;
 }
 
+// The same in single precision (the FP32 synthesis kernel's boundary
+// condition); exp(x) overflows float above x = 88, where B is far below the
+// smallest emissivity of a float continuum, so the cut is at 80.
+PYRH_HD float planck_f(float T, double lambda) {
+  const float hc_kla = float((kHPLANCK * kCLIGHT) / (kKBOLTZMANN * kNM_TO_M)) / float(lambda);
+  const float l = float(lambda);
+  const float twohnu3_c2 = float(2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M)) / (l * l * l);
+  const float x = hc_kla / T;
+  return (x <= 80.0f) ? twohnu3_c2 / (expf(x) - 1.0f) : 0.0f;
+}
+
 // Solve M x = b for a 4x4 system by LU without pivoting (the DELO-Bezier
 // matrices are unit-diagonal-dominated; the reference inverts them by
 // cofactors, rh/bezier_aux.c:133-329).  All indices are compile-time.
