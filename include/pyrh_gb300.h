@@ -704,6 +704,76 @@ pyrh_status pyrh_background_prepare(const pyrh_bg_model *model, void *stream);
 pyrh_status pyrh_background(const pyrh_bg_model *model, const pyrh_bg_batch *batch,
                             void *stream);
 
+/* -------------------------------------- element tables and LTE populations --
+ * The element data of the reference's abundance and partition-function files
+ * (readAbundance, rh/abundance.c:72-220), and on the device, one thread per
+ * depth point: the LTE ionisation-stage populations (LTEpops_elem,
+ * rh/ltepops.c:116-166), the stage density and log partition function each
+ * Kurucz line reads (rlk_opacity, rh/kurucz.c:662-677: the line_pops input
+ * of pyrh_lte_batch) and the electron density (Solve_ne with getfjk,
+ * rh/solvene.c:55-198, as pyrh's get_ne_from_nH runs it,
+ * rh/rhf1d/pyrh_hse.c:555-650: hydrogen in LTE, every element's stage
+ * fractions from its partition functions).  Elements are indexed by atomic
+ * number - 1 (the reference's table of 99 elements, rh/atomweights.h). */
+#define PYRH_NELEM 99
+#define PYRH_PF_MAX_STAGES 8     /* stages of one element in the tables */
+
+typedef struct {
+  int32_t nelem;                /* PYRH_NELEM */
+  int32_t npf;                  /* temperatures of the partition-function grid */
+  const double *Tpf;            /* [npf] K, ascending */
+  const double *abund;          /* [nelem] number abundance relative to hydrogen */
+  const int32_t *nstage;        /* [nelem] stages (<= PYRH_PF_MAX_STAGES) */
+  const int32_t *stage_off;     /* [nelem] first row of the element in lnpf and ionpot */
+  const double *lnpf;           /* [sum nstage][npf] ln U of each stage */
+  const double *ionpot;         /* [sum nstage] ionisation potential of each stage, J */
+} pyrh_elem_tables;
+
+/* Abundances from the text of an abundance file (readAbundance,
+   abundance.c:97-176): "ID value" records, '#' comments; the value of the
+   n-th record (1-based, comments not counted) is replaced by ab_val[i] where
+   ab_id[i] == n (compute1d's atomic_number / atomic_abundance); a hydrogen
+   value of 12.0 means the values are log10 + 12; metallicity (dex) scales
+   every element but hydrogen.  abund and abundance_set are [PYRH_NELEM]. */
+pyrh_status pyrh_abundance_parse(const char *text, int32_t nabun, const int32_t *ab_id,
+                                 const double *ab_val, double metallicity, double *abund,
+                                 int32_t *abundance_set);
+/* The partition-function file (XDR: Npf, Tpf[Npf], then per element its
+   atomic number, Nstage, U[Nstage][Npf] and ionisation potentials in cm^-1;
+   abundance.c:151-220).  With lnpf == NULL only *npf and *nrows (sum of
+   nstage) are set.  Otherwise Tpf [npf], nstage and stage_off [PYRH_NELEM],
+   lnpf [nrows][npf] and ionpot [nrows] are filled; for elements with
+   abundance_set the partition functions become ln U and the potentials J, as
+   the reference converts them (the others keep the file's values). */
+pyrh_status pyrh_pf_parse(const unsigned char *bytes, size_t nbytes,
+                          const int32_t *abundance_set, int32_t *npf, int32_t *nrows,
+                          double *Tpf, int32_t *nstage, int32_t *stage_off, double *lnpf,
+                          double *ionpot);
+
+/* The device arrays below are [npoint] (one value per depth point of a
+   batch); tables holds device pointers. */
+/* Stage populations of the selected elements (LTEpops_elem at the given
+   electron density): pops [sum over sel of nstage][npoint], the elements in
+   the order of sel (a host array of element indices). */
+pyrh_status pyrh_lte_stage_pops(const pyrh_elem_tables *tables, int64_t npoint,
+                                const double *T, const double *ne, const double *nHtot,
+                                int32_t nsel, const int32_t *sel, double *pops, void *stream);
+/* line_pops [nline][2][npoint] of pyrh_lte_batch for lines of the given
+   elements and stages (host arrays): the stage density n[stage] and
+   ln U_stage(T) of each line's element at every depth point. */
+pyrh_status pyrh_line_pops(const pyrh_elem_tables *tables, int64_t npoint, const double *T,
+                           const double *ne, const double *nHtot, int32_t nline,
+                           const int32_t *elem, const int32_t *stage, double *line_pops,
+                           void *stream);
+/* Electron density by Solve_ne's Newton iteration (at most 10 steps, to a
+   relative change of 1e-2), from hydrogen's ionisation alone when
+   fromscratch, else from the values in ne; ne is overwritten.  niter
+   (device [npoint], or NULL) receives the steps taken, -1 where the
+   iteration did not reach its limit (the reference warns and goes on). */
+pyrh_status pyrh_solve_ne(const pyrh_elem_tables *tables, int64_t npoint, const double *T,
+                          const double *nHtot, double *ne, int32_t fromscratch, int32_t *niter,
+                          void *stream);
+
 /* Number of kernel launches the last pyrh_lte_stokes / pyrh_nlte_* call issued. */
 int32_t pyrh_last_launch_count(void);
 

@@ -12,6 +12,9 @@
  *                    consumes (continuum, line constants, LTE stage densities,
  *                    height scale, Zeeman patterns, total background records)
  *                    as raw little-endian float64/int32 files into a directory.
+ *  harness_dump_ltepops writes the element tables (partition functions,
+ *                    ionisation potentials, abundances), LTEpops_elem() of
+ *                    every element and Solve_ne() after the same set-up.
  *  harness_dump_nlte performs the whole rhf1d() sequence with one ACTIVE atom
  *                    and writes the converged populations, the collision
  *                    matrix, the wavelength grid and the emergent intensity.
@@ -149,8 +152,23 @@ int harness_synth_loggf(const char *cwd, double mu, int Ndep, const double *atm,
 /* Set-up sequence of rhf1d() up to SortLambda() and getBoundary(), in the
    same order as pyrh_compute1dray.c:130-311, on private copies of the
    atmosphere rows and wavelengths (returned in *pa / *pw). */
+static void lte_setup_ab(const char *cwd, double mu, int Ndep, const double *atm, int Nwave,
+                         const double *lam, double **pa, double **pw, int Nabun, int *ab_id,
+                         double *ab_val, int force_h_lte);
+
 static void lte_setup(const char *cwd, double mu, int Ndep, const double *atm, int Nwave,
                       const double *lam, double **pa, double **pw)
+{
+  lte_setup_ab(cwd, mu, Ndep, atm, Nwave, lam, pa, pw, 0, NULL, NULL, 0);
+}
+
+/* lte_setup with abundance overrides (as rhf1d() passes compute1d's
+   atomic_number / atomic_abundance to MULTIatmos) and, with force_h_lte,
+   hydrogen in LTE as get_ne_from_nH() sets it before reading the atoms
+   (rh/rhf1d/pyrh_hse.c:594). */
+static void lte_setup_ab(const char *cwd, double mu, int Ndep, const double *atm, int Nwave,
+                         const double *lam, double **pa, double **pw, int Nabun, int *ab_id,
+                         double *ab_val, int force_h_lte)
 {
   char tmp[512];
   double *a = (double *) malloc(9 * Ndep * sizeof(double));
@@ -182,7 +200,8 @@ static void lte_setup(const char *cwd, double mu, int Ndep, const double *atm, i
   atmos.Nrlk = 0;
   geometry.Ndep = Ndep;
 
-  MULTIatmos(&atmos, &geometry, 0, NULL, NULL);
+  if (force_h_lte) atmos.H_LTE = TRUE;
+  MULTIatmos(&atmos, &geometry, Nabun, ab_id, ab_val);
   atmos.active_layer = -1;
   geometry.scale = TAU500;
   for (int k = 0; k < Ndep; k++) geometry.tau_ref[k] = POW10(a[k]);
@@ -383,6 +402,70 @@ int harness_dump_lte(const char *cwd, double mu, int Ndep, const double *atm,
   free(cont); free(cflags); free(tot_chi); free(tot_eta); free(tot_chip);
   free(tflags); free(lc); free(lpop); free(zm); free(zn);
   return Nspect;
+}
+
+/* Element tables, LTE stage populations and the electron density
+   (readAbundance rh/abundance.c:72-220, LTEpops_elem rh/ltepops.c:116-166,
+   Solve_ne and getfjk rh/solvene.c:55-198), after the set-up of rhf1d() with
+   the abundance overrides and hydrogen in LTE, as get_ne_from_nH() runs it
+   (rh/rhf1d/pyrh_hse.c:555-650).  Files:
+     Tpf [Npf]; el_meta [Nelem][4] Nstage, abundance_set, abund, weight;
+     el_pf [sum Nstage][Npf] (natural log for elements with an abundance);
+     el_ionpot [sum Nstage] (J for elements with an abundance);
+     T, ne, nHtot [Nspace] (SI);
+     el_n [sum Nstage][Nspace] LTEpops_elem() of each element with an
+       abundance at the atmosphere's own electron density (zeros otherwise);
+     ne_solved [Nspace] Solve_ne(fromscratch = TRUE);
+     ne_warm [Nspace] Solve_ne(fromscratch = FALSE), from the atmosphere's ne. */
+void Solve_ne(double *ne, bool_t fromscratch);
+void LTEpops_elem(Element *element);
+
+int harness_dump_ltepops(const char *cwd, int Ndep, const double *atm, int Nabun,
+                         int *ab_id, double *ab_val, const char *outdir)
+{
+  double *a, *w, lam500 = 500.0;
+  lte_setup_ab(cwd, 1.0, Ndep, atm, 1, &lam500, &a, &w, Nabun, ab_id, ab_val, 1);
+  int Nspace = atmos.Nspace, Nelem = atmos.Nelem, Npf = atmos.Npf, nst = 0;
+  for (int n = 0; n < Nelem; n++) nst += atmos.elements[n].Nstage;
+  double *meta = (double *) calloc(4L * Nelem, sizeof(double));
+  double *pf = (double *) calloc((long) nst * Npf, sizeof(double));
+  double *ion = (double *) calloc(nst, sizeof(double));
+  double *pops = (double *) calloc((long) nst * Nspace, sizeof(double));
+  long row = 0;
+  for (int n = 0; n < Nelem; n++) {
+    Element *el = &atmos.elements[n];
+    meta[4 * n + 0] = el->Nstage;
+    meta[4 * n + 1] = el->abundance_set;
+    meta[4 * n + 2] = el->abund;
+    meta[4 * n + 3] = el->weight;
+    if (el->abundance_set) {
+      if (el->n == NULL) el->n = matrix_double(el->Nstage, Nspace);
+      LTEpops_elem(el);
+    }
+    for (int i = 0; i < el->Nstage; i++, row++) {
+      memcpy(pf + row * Npf, el->pf[i], Npf * sizeof(double));
+      ion[row] = el->ionpot[i];
+      if (el->abundance_set) memcpy(pops + row * Nspace, el->n[i], Nspace * sizeof(double));
+    }
+  }
+  double *ne1 = (double *) malloc(Nspace * sizeof(double));
+  double *ne2 = (double *) malloc(Nspace * sizeof(double));
+  memcpy(ne1, atmos.ne, Nspace * sizeof(double));
+  memcpy(ne2, atmos.ne, Nspace * sizeof(double));
+  Solve_ne(ne1, TRUE);
+  Solve_ne(ne2, FALSE);
+  write_f64(outdir, "Tpf", atmos.Tpf, Npf);
+  write_f64(outdir, "el_meta", meta, 4L * Nelem);
+  write_f64(outdir, "el_pf", pf, (long) nst * Npf);
+  write_f64(outdir, "el_ionpot", ion, nst);
+  write_f64(outdir, "T", atmos.T, Nspace);
+  write_f64(outdir, "ne", atmos.ne, Nspace);
+  write_f64(outdir, "nHtot", atmos.nHtot, Nspace);
+  write_f64(outdir, "el_n", pops, (long) nst * Nspace);
+  write_f64(outdir, "ne_solved", ne1, Nspace);
+  write_f64(outdir, "ne_warm", ne2, Nspace);
+  free(meta); free(pf); free(ion); free(pops); free(ne1); free(ne2);
+  return Nspace;
 }
 
 /* ------------------------------------------------------------------ NLTE */

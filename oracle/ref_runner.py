@@ -209,6 +209,29 @@ def _background_job(args):
                                        _p(atm), len(wave), _p(wave), outdir.encode())
 
 
+def _ltepops_job(args):
+    workdir, pyrh_path, atm, ab_id, ab_val, outdir = args
+    lib = _lib(pyrh_path)
+    atm = np.ascontiguousarray(atm, dtype=np.float64)
+    ab_id = np.ascontiguousarray(ab_id, dtype=np.int32)
+    ab_val = np.ascontiguousarray(ab_val, dtype=np.float64)
+    os.makedirs(outdir, exist_ok=True)
+    lib.harness_dump_ltepops.restype = C.c_int
+    return lib.harness_dump_ltepops(workdir.encode(), atm.shape[1], _p(atm), len(ab_id),
+                                    ab_id.ctypes.data_as(C.POINTER(C.c_int)), _p(ab_val),
+                                    outdir.encode())
+
+
+def read_ltepops_dump(outdir: str) -> dict:
+    """The files of harness_dump_ltepops as arrays."""
+    f64 = lambda n: np.fromfile(os.path.join(outdir, n + ".f64"))
+    d = {k: f64(k) for k in ("Tpf", "el_ionpot", "T", "ne", "nHtot", "ne_solved", "ne_warm")}
+    d["el_meta"] = f64("el_meta").reshape(-1, 4)
+    d["el_pf"] = f64("el_pf").reshape(-1, len(d["Tpf"]))
+    d["el_n"] = f64("el_n").reshape(-1, len(d["T"]))
+    return d
+
+
 def read_background_dump(outdir: str) -> dict:
     """The files of harness_dump_background as arrays."""
     f64 = lambda n: np.fromfile(os.path.join(outdir, n + ".f64"))
@@ -292,6 +315,9 @@ class Reference:
 
     def dump_background(self, workdir, mu, atm, wave, outdir):
         return self._run(_background_job, (workdir, self.pyrh_path, mu, atm, wave, outdir))
+
+    def dump_ltepops(self, workdir, atm, ab_id, ab_val, outdir):
+        return self._run(_ltepops_job, (workdir, self.pyrh_path, atm, ab_id, ab_val, outdir))
 
     def nlte(self, workdir, mu, atm, wave, outdir, mode):
         return self._run(_nlte_job, (workdir, self.pyrh_path, mu, atm, wave, outdir, mode))

@@ -1,0 +1,176 @@
+// elements_host.cpp -- host readers of the element data: the abundance file
+// and the Kurucz partition-function file.
+//
+// Reference routine restated here (file:line in the reference tree):
+//   readAbundance   rh/abundance.c:72-220  (record matching, the pyrh
+//                                           overrides by record number, the
+//                                           DEX and metallicity conversions,
+//                                           the XDR partition-function file
+//                                           and its conversion to ln U and J)
+//   getLine         rh/getline.c:30-55     (comment and blank lines)
+// The file formats are the reference's, so they are parsed field for field;
+// every conversion keeps the reference's expression (POW10(x) is
+// exp(LG10 x), rh/rh.h:50) so the tables come out bit-identical.
+#include <ctype.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+
+#include "../../include/pyrh_gb300.h"
+
+namespace pyrh {
+void set_error(const char* fmt, ...);
+}
+
+namespace {
+
+constexpr double kLG10 = 2.30258509299404568402;   // ln 10
+constexpr double kH = 6.6260755E-34;
+constexpr double kC = 2.99792458E+08;
+constexpr double kCM_TO_M = 1.0E-02;
+
+// Symbols of the 99 elements in atomic-number order, two characters wide
+// (the IDs the abundance records are matched against).
+const char* const kElementID[PYRH_NELEM] = {
+    "H ", "HE", "LI", "BE", "B ", "C ", "N ", "O ", "F ", "NE", "NA", "MG", "AL", "SI", "P ",
+    "S ", "CL", "AR", "K ", "CA", "SC", "TI", "V ", "CR", "MN", "FE", "CO", "NI", "CU", "ZN",
+    "GA", "GE", "AS", "SE", "BR", "KR", "RB", "SR", "Y ", "ZR", "NB", "MO", "TC", "RU", "RH",
+    "PD", "AG", "CD", "IN", "SN", "SB", "TE", "I ", "XE", "CS", "BA", "LA", "CE", "PR", "ND",
+    "PM", "SM", "EU", "GD", "TB", "DY", "HO", "ER", "TM", "YB", "LU", "HF", "TA", "W ", "RE",
+    "OS", "IR", "PT", "AU", "HG", "TL", "PB", "BI", "PO", "AT", "RN", "FR", "RA", "AC", "TH",
+    "PA", "U ", "NP", "PU", "AM", "CM", "BK", "CF", "ES"};
+
+pyrh_status fail(pyrh_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  pyrh::set_error("%s", buf);
+  return s;
+}
+
+// Big-endian XDR words.
+struct Xdr {
+  const unsigned char* p;
+  size_t n, off = 0;
+  bool ok = true;
+  bool i32(int32_t* v) {
+    if (off + 4 > n) return ok = false;
+    const uint32_t u = (uint32_t)p[off] << 24 | (uint32_t)p[off + 1] << 16 |
+                       (uint32_t)p[off + 2] << 8 | (uint32_t)p[off + 3];
+    memcpy(v, &u, 4);
+    off += 4;
+    return true;
+  }
+  bool f64(double* v) {
+    if (off + 8 > n) return ok = false;
+    uint64_t u = 0;
+    for (int i = 0; i < 8; ++i) u = (u << 8) | p[off + i];
+    memcpy(v, &u, 8);
+    off += 8;
+    return true;
+  }
+};
+
+}  // namespace
+
+extern "C" pyrh_status pyrh_abundance_parse(const char* text, int32_t nabun,
+                                            const int32_t* ab_id, const double* ab_val,
+                                            double metallicity, double* abund,
+                                            int32_t* abundance_set) {
+  if (!text || !abund || !abundance_set) return fail(PYRH_ERR_ARG, "abundance: NULL argument");
+  if (nabun < 0 || (nabun > 0 && (!ab_id || !ab_val)))
+    return fail(PYRH_ERR_ARG, "abundance: override arrays missing");
+  for (int n = 0; n < PYRH_NELEM; ++n) {
+    abund[n] = 0.0;
+    abundance_set[n] = 0;
+  }
+  bool dex = false;
+  int record = 1;
+  const char* s = text;
+  while (*s) {
+    const char* e = strchr(s, '\n');
+    std::string line = e ? std::string(s, e - s) : std::string(s);
+    s = e ? e + 1 : s + line.size();
+    // getLine: skip lines whose first character is the comment mark and
+    // lines without a token
+    char tok[2];
+    if (line.empty() || line[0] == '#' || sscanf(line.c_str(), "%1s", tok) < 1) continue;
+    char id[64];
+    double value;
+    if (sscanf(line.c_str(), "%63s %lf", id, &value) != 2)
+      return fail(PYRH_ERR_ARG, "abundance: unreadable record '%s'", line.c_str());
+    for (char* c = id; *c; ++c) *c = (char)toupper((unsigned char)*c);
+    if (strlen(id) == 1) strcat(id, " ");
+    for (int i = 0; i < nabun; ++i)
+      if (ab_id[i] == record) {
+        value = ab_val[i];
+        break;
+      }
+    ++record;
+    for (int n = 0; n < PYRH_NELEM; ++n)
+      if (strstr(kElementID[n], id)) {
+        abund[n] = value;
+        if (strstr(id, "H ") && value == 12.0) dex = true;
+        abundance_set[n] = 1;
+        break;
+      }
+  }
+  const double metal = exp(kLG10 * metallicity);
+  for (int n = 0; n < PYRH_NELEM; ++n) {
+    if (!abundance_set[n]) continue;
+    if (dex) abund[n] = exp(kLG10 * (abund[n] - 12.0));
+    if (metal != 1.0 && n != 0) abund[n] *= metal;
+  }
+  return PYRH_OK;
+}
+
+extern "C" pyrh_status pyrh_pf_parse(const unsigned char* bytes, size_t nbytes,
+                                     const int32_t* abundance_set, int32_t* npf,
+                                     int32_t* nrows, double* Tpf, int32_t* nstage,
+                                     int32_t* stage_off, double* lnpf, double* ionpot) {
+  if (!bytes || !npf || !nrows) return fail(PYRH_ERR_ARG, "pf: NULL argument");
+  Xdr x{bytes, nbytes};
+  int32_t np = 0;
+  if (!x.i32(&np) || np < 2 || np > 100000) return fail(PYRH_ERR_ARG, "pf: bad Npf");
+  const bool fill = lnpf != nullptr;
+  if (fill && (!abundance_set || !Tpf || !nstage || !stage_off || !ionpot))
+    return fail(PYRH_ERR_ARG, "pf: NULL output array");
+  for (int k = 0; k < np; ++k) {
+    double t;
+    if (!x.f64(&t)) return fail(PYRH_ERR_ARG, "pf: file ends in the temperature grid");
+    if (fill) Tpf[k] = t;
+  }
+  int32_t rows = 0;
+  for (int n = 0; n < PYRH_NELEM; ++n) {
+    int32_t pti, ns;
+    if (!x.i32(&pti) || !x.i32(&ns))
+      return fail(PYRH_ERR_ARG, "pf: file ends before element %d", n + 1);
+    if (ns < 1 || ns > PYRH_PF_MAX_STAGES)
+      return fail(PYRH_ERR_UNSUPPORTED, "pf: element %d has %d stages (limit %d)", n + 1, ns,
+                  PYRH_PF_MAX_STAGES);
+    if (fill) {
+      nstage[n] = ns;
+      stage_off[n] = rows;
+    }
+    for (int i = 0; i < ns * np; ++i) {
+      double u;
+      if (!x.f64(&u)) return fail(PYRH_ERR_ARG, "pf: file ends in element %d", n + 1);
+      if (fill) lnpf[(int64_t)rows * np + i] = abundance_set[n] ? log(u) : u;
+    }
+    for (int i = 0; i < ns; ++i) {
+      double v;
+      if (!x.f64(&v)) return fail(PYRH_ERR_ARG, "pf: file ends in element %d", n + 1);
+      if (fill) ionpot[rows + i] = abundance_set[n] ? v * ((kH * kC) / kCM_TO_M) : v;
+    }
+    rows += ns;
+  }
+  *npf = np;
+  *nrows = rows;
+  return PYRH_OK;
+}

@@ -50,6 +50,10 @@ Fixtures (npz, float64):
                   nm for the C0 atmosphere and a cooler one, with the
                   densities and atomic data it reads, and for C0 each
                   process alone
+  ltepops         the element tables (Kurucz partition functions, ionisation
+                  potentials, abundances) as the reference parsed them,
+                  LTEpops_elem() of every element and Solve_ne() for three
+                  atmospheres, one with abundance overrides
 
 stokes_ref comes from the reference as setup.py builds it on x86 (-DSIMDON,
 SSE reciprocal-estimate 4x4 inverse); stokes_ref_portable from the same
@@ -488,12 +492,55 @@ def make_kurucz(ref, wd):
     print(f"kurucz_lists: {os.path.getsize(path) / 1e3:.0f} kB")
 
 
+def make_ltepops(ref, wd):
+    """Element tables as readAbundance() parsed them (partition functions and
+    ionisation potentials of the Kurucz pf file, abundances of the abundance
+    file), LTEpops_elem() of every element at the atmosphere's own electron
+    density, and Solve_ne() from scratch (hydrogen in LTE) and from the
+    given electron density, for the C0 atmosphere, a cooler one (T - 1500 K
+    above log tau 0, at least 2600 K) and C0 with overridden abundances
+    (entries 1 and 26 of the abundance file, as compute1d's atomic_number /
+    atomic_abundance give them)."""
+    cases = []
+    for shift, ab_id, ab_val in ((0.0, [], []), (1500.0, [], []),
+                                 (0.0, [1, 26], [12.0, 7.10])):
+        logtau = wl.logtau_grid(71)
+        T = wl.base_temperature(logtau)
+        T = np.where(logtau < 0.0, np.maximum(T - shift, 2600.0), T)
+        w = rr.scratch_dir()
+        rr.write_inputs(w, None)
+        ne, nH = ref.hse(w, logtau, T)
+        atm = wl.atmosphere_rows(logtau, T, ne / 1e6, nH / 1e6)
+        outdir = os.path.join(w, "lp")
+        ref.dump_ltepops(w, atm, ab_id, ab_val, outdir)
+        d = rr.read_ltepops_dump(outdir)
+        d["ab_id"] = np.array(ab_id, np.int32)
+        d["ab_val"] = np.array(ab_val, np.float64)
+        cases.append(d)
+        shutil.rmtree(w, ignore_errors=True)
+    out = {"Tpf": cases[0]["Tpf"], "el_pf": cases[0]["el_pf"],
+           "el_ionpot": cases[0]["el_ionpot"],
+           "abundance_text": np.array(open(os.path.join(rr.REF_ROOT, "rh", "Atoms",
+                                                        "abundance.input")).read())}
+    for c in cases[1:]:
+        assert np.array_equal(c["Tpf"], out["Tpf"])
+    for k in ("el_meta", "T", "ne", "nHtot", "el_n", "ne_solved", "ne_warm"):
+        out[k] = np.stack([c[k] for c in cases])
+    out["ab_id"] = np.array([np.pad(c["ab_id"], (0, 2 - len(c["ab_id"])), constant_values=-1)
+                             for c in cases])
+    out["ab_val"] = np.array([np.pad(c["ab_val"], (0, 2 - len(c["ab_val"]))) for c in cases])
+    path = os.path.join(HERE, "ltepops.npz")
+    np.savez_compressed(path, **out)
+    print(f"ltepops: {len(out['Tpf'])} pf temperatures, {out['el_meta'].shape[1]} elements, "
+          f"{os.path.getsize(path) / 1e3:.0f} kB")
+
+
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
           "lte_static": make_lte_static, "lte_broadening": make_lte_broadening,
           "nlte": make_nlte, "nlte_static": make_nlte_static, "kurucz": make_kurucz,
-          "background": make_background}
+          "background": make_background, "ltepops": make_ltepops}
 
 
 def main():
