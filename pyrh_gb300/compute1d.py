@@ -97,16 +97,20 @@ class LteSetup:
     heights [ndep] (m), proton density np [ndep] (m^-3), stage densities
     and ln U of each line's element line_pops [nline, 2, ndep], and the
     line list (line_const, zeeman, zeeman_n: the layout of
-    pyrh_gb300.lte.make_lines)."""
+    pyrh_gb300.lte.make_lines).  With line_pops None, compute1d forms them
+    on the device from the atmosphere (pyrh_line_pops) and the element
+    tables: `elements` (a pyrh_gb300.ltepops.ElementTables), else the
+    abundance and partition-function files the run in cwd names."""
     lam: np.ndarray
     chi_c: np.ndarray
     eta_c: np.ndarray
     height: np.ndarray
     np: np.ndarray
-    line_pops: np.ndarray
+    line_pops: np.ndarray | None
     line_const: np.ndarray
     zeeman: np.ndarray
     zeeman_n: np.ndarray
+    elements: object = None
 
 
 def _line_constants(setup: LteSetup, loggf_ids, loggf_values) -> np.ndarray:
@@ -172,8 +176,15 @@ def compute1d(cwd, mu, atm_scale, atmosphere, wave, loggf_ids=None, loggf_values
         raise ValueError("the set-up's wavelength grid is not the one these wavelengths make")
     lc = _line_constants(setup, loggf_ids, loggf_values)
     lines, nline = lte.make_lines(lc, setup.zeeman, setup.zeeman_n)
+    line_pops = setup.line_pops
+    if line_pops is None:
+        from . import ltepops as LP
+        tab = setup.elements if setup.elements is not None else LP.tables_from_files(cwd)
+        line_pops = LP.line_pops(LP.DeviceTables(tab, device), T, ne, nH,
+                                 lc[:, 1].astype(np.int32) - 1,
+                                 lc[:, 2].astype(np.int32)).cpu().numpy()
     atm = dict(height=setup.height, T=T, ne=ne, nHtot=nH, np=setup.np, vturb=vturb, vel=vel,
-               B=B, gamma_B=gam, chi_B=chi, line_pops=setup.line_pops, lam=g.lam,
+               B=B, gamma_B=gam, chi_B=chi, line_pops=line_pops, lam=g.lam,
                chi_c=setup.chi_c, eta_c=setup.eta_c)
     pk = lte.pack([atm], nline, precision)
     dev = lte.DeviceBatch(pk, lines, nline, device=device)

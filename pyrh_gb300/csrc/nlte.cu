@@ -234,12 +234,21 @@ struct NlteOpacity {
   const NlteShared<R>* sh;
   int nd, ns, la, q;
   int64_t coff;
+  bool act;   // the lane's wavelength takes part in this solution (else no loads)
 
   // Total opacity, source function, the background part of the source
   // function (eta_c + sca_c J) / chi, the background opacity chi_c and the
   // atom's emissivity at depth k (opacity.c:64-300 for the active atom).
+  // Lanes that do not take part in the current solution (the other solver's
+  // wavelengths of a mixed warp, which run along so that the warp's rate sums
+  // stay converged and add nothing) get unit opacity without reading memory.
   __device__ __forceinline__ void operator()(int k, R& chi, R& S, R& S_bg, R& chi_bg,
                                              R& eta_atom, R Jold) const {
+    if (!act) {
+      chi = chi_bg = R(1);
+      S = S_bg = eta_atom = R(0);
+      return;
+    }
     const pyrh_nlte_batch& b = A->b;
     R chi_a = 0, eta_a = 0;
     for (int m = 0; m < as->n; ++m) {
@@ -713,6 +722,7 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
   for (int ray = grp; ray < A.nrays; ray += A.ngroup) {
     const R* dsl = sh.ds + ray * nd;
     if (any_bez) {
+      op.act = bez;
       for (int to_obs = emergent_only ? 1 : 0; to_obs <= 1; ++to_obs) {
         op.q = 2 * ray + to_obs;
         const R wdir = R(0.5 * A.wmu[ray]);
@@ -729,6 +739,7 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
     if (any_feau) {
       // angle-independent: one Feautrier solution per ray (to_obs index 0)
       op.q = 2 * ray;
+      op.act = feau;
       // P overwrites S, Psi F, 1 - Psi zt and Ieff Sb (feautrier_full allows it)
       R chis[PYRH_NLTE_MAX_DEPTH], S[PYRH_NLTE_MAX_DEPTH], F[PYRH_NLTE_MAX_DEPTH],
           zt[PYRH_NLTE_MAX_DEPTH], Sb[PYRH_NLTE_MAX_DEPTH], cbg[PYRH_NLTE_MAX_DEPTH];

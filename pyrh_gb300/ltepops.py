@@ -181,6 +181,8 @@ def stage_pops(dev: DeviceTables, T, ne, nHtot, elements):
     import torch
     T, ne, nHtot = (_dev(x, dev.device) for x in (T, ne, nHtot))
     sel = np.ascontiguousarray(elements, np.int32)
+    if np.any((sel < 0) | (sel >= NELEM)):
+        raise ValueError("element index outside 0..98")
     rows = int(sum(dev.host.nstage[e] for e in sel))
     out = torch.zeros((rows, T.numel()), dtype=torch.float64, device=dev.device)
     L.check(_lib().pyrh_lte_stage_pops(C.byref(dev.struct), T.numel(), T.data_ptr(),

@@ -135,3 +135,30 @@ def test_compute1d_with_the_gpu_background(golden, tmp_path, precision, tol):
     ic = ref[0].max()
     for s, got in enumerate((sI, sQ, sU, sV)):
         assert np.abs(got - ref[s]).max() < tol * ic, (s, np.abs(got - ref[s]).max() / ic)
+
+
+@pytest.mark.parametrize("name", ["lte_c0", "lte_edge"])
+def test_compute1d_forms_line_pops_from_the_atmosphere(golden, tmp_path, name):
+    """With no line_pops in the set-up, compute1d forms the stage densities
+    and partition functions of the lines on the device (pyrh_line_pops) from
+    the element tables the reference read (fixture ltepops): the spectra
+    equal those from the reference's own line_pops and match the
+    reference's compute1d."""
+    from pyrh_gb300 import ltepops as LP
+    fx = golden(name)
+    lp = golden("ltepops")
+    meta = lp["el_meta"][0]
+    ns = meta[:, 0].astype(np.int32)
+    tab = LP.ElementTables(lp["Tpf"], meta[:, 2].copy(), meta[:, 1].astype(np.int32), ns,
+                           np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32),
+                           lp["el_pf"], lp["el_ionpot"])
+    cwd = keyword_dir(tmp_path, fx, "FULL_STOKES")
+    atm = np.ascontiguousarray(fx["atm"])
+    su = setup_of(fx)
+    base = C1.compute1d(cwd, float(fx["mu"]), 0, atm, fx["wave"], setup=su)
+    su.line_pops, su.elements = None, tab
+    got = C1.compute1d(cwd, float(fx["mu"]), 0, atm, fx["wave"], setup=su)
+    ic = base[0].max()
+    for s in range(4):
+        assert np.abs(got[s] - base[s]).max() < 1e-10 * ic
+        assert np.abs(got[s] - fx["stokes_ref_portable"][s]).max() < 1e-5 * ic

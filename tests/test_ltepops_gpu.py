@@ -67,7 +67,7 @@ def test_batched_points_and_limits(golden):
     np.testing.assert_allclose(ne, ref, rtol=1e-12, atol=0)
     with pytest.raises(RuntimeError):
         LP.line_pops(dev, T, T, nH, [25], [7])       # Fe has fewer stages
-    with pytest.raises(RuntimeError):
+    with pytest.raises(ValueError):
         LP.stage_pops(dev, T, T, nH, [99])
     assert LP.line_pops(dev, T[:0], T[:0], nH[:0], [25], [0]).numel() == 0
 
