@@ -213,6 +213,12 @@ struct ActiveSet {
   R tw[PYRH_NLTE_MAX_ACTIVE];    // lines: A_ji / B_ji; continua: 2 h c / lambda^3
   R wl[PYRH_NLTE_MAX_ACTIVE];    // lines: wlambda (Hz); continua: 4 pi wlambda / (h lambda)
   R hckl;                        // h c / (k_B lambda)
+  // per active transition m with levels (i, j): its key i nlev + j and the
+  // active transitions (bit qq) whose lower level is i (but not m itself),
+  // whose upper level is j, and whose upper level is i -- what the
+  // cross-coupling sums of addtoCoupling select at every depth
+  int key[PYRH_NLTE_MAX_ACTIVE];
+  unsigned up_i[PYRH_NLTE_MAX_ACTIVE], up_j[PYRH_NLTE_MAX_ACTIVE], dn_i[PYRH_NLTE_MAX_ACTIVE];
 };
 
 // Per-block staging of the atmosphere's quantities that every thread reads
@@ -533,7 +539,7 @@ __device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_tra
   // in it), U = TW G V, the stimulated-emission factor G and the
   // transition's own opacity X
   R VW[PYRH_NLTE_MAX_ACTIVE], U[PYRH_NLTE_MAX_ACTIVE], G[PYRH_NLTE_MAX_ACTIVE],
-      X[PYRH_NLTE_MAX_ACTIVE];
+      X[PYRH_NLTE_MAX_ACTIVE], CC[PYRH_NLTE_MAX_ACTIVE];
   for (int m = 0; m < nact; ++m) {
     const pyrh_nlte_transition& t = tr[as.t[m]];
     const R ni = sh.n[t.i * nd + k], nj = sh.n[t.j * nd + k];
@@ -552,32 +558,30 @@ __device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_tra
       U[m] = (as.tw[m] * G[m]) * as.vb[m];
       X[m] = as.vb[m] * (ni - G[m] * nj);
     }
+    CC[m] = VW[m] * (ni - G[m] * nj);   // the transition's opacity with the weight W
   }
   for (int m = 0; m < nm; ++m) {
     int key = -1;
     R gij = 0, gji = 0;
     if (m < nact) {
-      const pyrh_nlte_transition& t = tr[as.t[m]];
-      const int i = t.i, j = t.j;
-      key = i * nlev + j;
+      key = as.key[m];
       // cross-coupling sums over the active set (addtoCoupling), with the
       // transition's own terms kept apart: chi_up_o and U_down_o leave out
       // transition m, X_o is the opacity of everything but m (background
-      // and the other transitions)
-      R chi_up_o = 0, chi_down_j = 0, U_down_o = 0, U_down_i = 0, X_o = chi_bg, chi_self = 0;
-      int cnt = 0;
-      for (int qq = 0; qq < nact; ++qq) {
-        const pyrh_nlte_transition& u = tr[as.t[qq]];
-        const R chicc = VW[qq] * (sh.n[u.i * nd + k] - G[qq] * sh.n[u.j * nd + k]);
-        if (qq == m) chi_self = chicc;
-        else X_o += X[qq];
-        if (u.i == i && qq != m) chi_up_o += chicc;
-        if (u.j == j) {
-          chi_down_j += chicc;
-          if (qq != m) U_down_o += U[qq];
-        }
-        if (u.j == i) { U_down_i += U[qq]; ++cnt; }
+      // and the other transitions); each sum runs over the transitions in
+      // active-set order
+      R chi_up_o = 0, chi_down_j = 0, U_down_o = 0, U_down_i = 0, X_o = chi_bg;
+      const R chi_self = CC[m];
+      for (int qq = 0; qq < nact; ++qq)
+        if (qq != m) X_o += X[qq];
+      for (unsigned r = as.up_i[m]; r; r &= r - 1) chi_up_o += CC[__ffs(r) - 1];
+      for (unsigned r = as.up_j[m]; r; r &= r - 1) {
+        const int qq = __ffs(r) - 1;
+        chi_down_j += CC[qq];
+        if (qq != m) U_down_o += U[qq];
       }
+      for (unsigned r = as.dn_i[m]; r; r &= r - 1) U_down_i += U[__ffs(r) - 1];
+      const int cnt = __popc(as.dn_i[m]);
       const R wlamu = VW[m] * wdir;
       gji = Ieff_k * wlamu;
       // fillgamma.c:185-196: (2 h nu^3 / c^2 + Ieff) g V W - chi_up Psi U_down.
@@ -696,6 +700,20 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
         }
       }
     }
+  for (int m = 0; m < as.n; ++m) {
+    const pyrh_nlte_transition& T = tr[as.t[m]];
+    as.key[m] = T.i * nlev + T.j;
+    unsigned ui = 0, uj = 0, di = 0;
+    for (int qq = 0; qq < as.n; ++qq) {
+      const pyrh_nlte_transition& U = tr[as.t[qq]];
+      if (U.i == T.i && qq != m) ui |= 1u << qq;
+      if (U.j == T.j) uj |= 1u << qq;
+      if (U.j == T.i) di |= 1u << qq;
+    }
+    as.up_i[m] = ui;
+    as.up_j[m] = uj;
+    as.dn_i[m] = di;
+  }
   const double B0 = planck(b.T[doff + nd - 2], lam), B1 = planck(b.T[doff + nd - 1], lam);
   const JRow<R> Jold{static_cast<const R*>(A.Jr) + coff + la, ns};
   // angle-dependent wavelengths (formal.c:92-101: a polarized active set or
