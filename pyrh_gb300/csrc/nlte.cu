@@ -528,7 +528,6 @@ __device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_tra
                                           bool mine, R wdir, R I_k, R Psi_k, R omp, R Ieff_k,
                                           R chi_k, R chi_bg) {
   const unsigned full = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
   if (mine) atomicAdd(out.Jn + (int64_t)k * out.ns, wdir * I_k);
   const int nact = mine ? as.n : 0;
   const int nm = __reduce_max_sync(full, nact);

@@ -29,7 +29,6 @@ void set_launches(int n);
 
 namespace {
 
-constexpr double kC = 2.99792458E+08;
 constexpr double kH = 6.6260755E-34;
 constexpr double kK = 1.380658E-23;
 constexpr double kAMU = 1.6605402E-27;
