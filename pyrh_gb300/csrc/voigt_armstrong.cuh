@@ -34,6 +34,22 @@ namespace pyrh {
     0.46224366960061009, 0.28667550536283415, 0.10901720602002329, 0.024810520887463643, \
     0.0032437733422378567, 0.00022833863601635365, 7.8025564785320599e-06, \
     1.0860693707692782e-07, 4.3993409922731747e-10, 2.2293936455341447e-13}
+// -2 / n of the series in a (n = 2..50), formed by the compiler: the same
+// correctly rounded quotients a division in the loop gives.
+#define PYRH_ARM_N2(n) (-2.0 / (n))
+#define PYRH_ARMSTRONG_NEG2N { 0.0, 0.0, \
+    PYRH_ARM_N2(2), PYRH_ARM_N2(3), PYRH_ARM_N2(4), PYRH_ARM_N2(5), PYRH_ARM_N2(6), \
+    PYRH_ARM_N2(7), PYRH_ARM_N2(8), PYRH_ARM_N2(9), PYRH_ARM_N2(10), PYRH_ARM_N2(11), \
+    PYRH_ARM_N2(12), PYRH_ARM_N2(13), PYRH_ARM_N2(14), PYRH_ARM_N2(15), PYRH_ARM_N2(16), \
+    PYRH_ARM_N2(17), PYRH_ARM_N2(18), PYRH_ARM_N2(19), PYRH_ARM_N2(20), PYRH_ARM_N2(21), \
+    PYRH_ARM_N2(22), PYRH_ARM_N2(23), PYRH_ARM_N2(24), PYRH_ARM_N2(25), PYRH_ARM_N2(26), \
+    PYRH_ARM_N2(27), PYRH_ARM_N2(28), PYRH_ARM_N2(29), PYRH_ARM_N2(30), PYRH_ARM_N2(31), \
+    PYRH_ARM_N2(32), PYRH_ARM_N2(33), PYRH_ARM_N2(34), PYRH_ARM_N2(35), PYRH_ARM_N2(36), \
+    PYRH_ARM_N2(37), PYRH_ARM_N2(38), PYRH_ARM_N2(39), PYRH_ARM_N2(40), PYRH_ARM_N2(41), \
+    PYRH_ARM_N2(42), PYRH_ARM_N2(43), PYRH_ARM_N2(44), PYRH_ARM_N2(45), PYRH_ARM_N2(46), \
+    PYRH_ARM_N2(47), PYRH_ARM_N2(48), PYRH_ARM_N2(49), PYRH_ARM_N2(50)}
+static __constant__ double kArmNeg2N[51] = PYRH_ARMSTRONG_NEG2N;
+static const double kArmNeg2NHost[51] = PYRH_ARMSTRONG_NEG2N;
 static __constant__ double kDawsonCheb[34] = PYRH_ARMSTRONG_DAWSON;
 static __constant__ double kGhT[10] = PYRH_ARMSTRONG_GH_T;
 static __constant__ double kGhW[10] = PYRH_ARMSTRONG_GH_W;
@@ -56,6 +72,37 @@ PYRH_HD double arm_ght(int n) {
   return kGhTHost[n];
 #endif
 }
+PYRH_HD double arm_neg2n(int n) {
+#ifdef __CUDA_ARCH__
+  return kArmNeg2N[n];
+#else
+  return kArmNeg2NHost[n];
+#endif
+}
+
+// The series' stopping test |g / funct| <= 1e-8 (voigt.c).  In FP64 it is
+// decided by a product where the quotient is clearly on one side and by
+// the division itself only within 1e-12 of the limit, so every decision is
+// the division's (FP64 divisions dominated the profile kernel's time); in
+// other precisions and for dual numbers the division is kept as written.
+template <typename R>
+PYRH_HD bool arm_series_done(const R& g, const R& funct) {
+  return fabs(g / funct) <= R(1.0e-8);
+}
+template <>
+PYRH_HD bool arm_series_done<double>(const double& g, const double& funct) {
+  const double ag = fabs(g), lim = 1.0e-8 * fabs(funct);
+  if (ag < lim * (1.0 - 1.0e-12)) return true;
+  if (ag > lim * (1.0 + 1.0e-12)) return false;
+  return fabs(g / funct) <= 1.0e-8;
+}
+
+// -2 / n: from the table in FP64 (the same value), divided otherwise.
+template <typename R>
+PYRH_HD R arm_m2n(int n) { return R(-2) / R(n); }
+template <>
+PYRH_HD double arm_m2n<double>(int n) { return arm_neg2n(n); }
+
 PYRH_HD double arm_ghw(int n) {
 #ifdef __CUDA_ARCH__
   return kGhW[n];
@@ -177,7 +224,7 @@ PYRH_VOIGT_FN R voigt_armstrong_t(R a, R v) {
     if (a > R(1.0e-8)) {
       R q = R(1), an = a;
       for (int n = 2; n <= 50; ++n) {
-        const R dn = (v * dn01 + dn02) * (R(-2) / R(n));
+        const R dn = (v * dn01 + dn02) * arm_m2n<R>(n);
         dn02 = dn01;
         dn01 = dn;
         if (n % 2) {
@@ -185,7 +232,7 @@ PYRH_VOIGT_FN R voigt_armstrong_t(R a, R v) {
           an *= a2;
           const R g = dn * an;
           funct += q * g;
-          if (fabs(g / funct) <= R(1.0e-8)) return u1 - R(1.12837917) * funct;
+          if (arm_series_done<R>(g, funct)) return u1 - R(1.12837917) * funct;
         }
       }
     }
