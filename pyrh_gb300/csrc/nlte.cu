@@ -197,28 +197,39 @@ __global__ void nlte_prepare_kernel(NlteArgs A) {
 
 // ------------------------------------------------------------ formal -----
 
-// The transitions active at one wavelength and their wavelength-only
-// constants, in the formal-solution precision R.  Line quantities are kept
-// without the factor h c / (4 pi) where products would leave the single-
-// precision range (V W reaches 1e15 and W alone 1e33).
+// Transitions active across a warp's tile of 32 wavelengths: the union of
+// the lanes' active sets, each transition once, continua in transition order
+// and then lines (the order of every lane's own active set), in shared
+// memory.  Line quantities are kept without the factor h c / (4 pi) where
+// products would leave the single-precision range (V W reaches 1e15 and W
+// alone 1e33).
+constexpr int kMaxUnion = 32;
+
+template <typename R>
+struct UnionEntry {
+  int64_t phi_off;
+  int t, type, i, j, key;        // transition index, type, levels, key i nlev + j
+  int nblue, nlambda, line_index;
+  // the entries (bits) whose lower level is i (not this one), whose upper
+  // level is j, and whose upper level is i: what the cross-coupling sums of
+  // addtoCoupling select
+  unsigned up_i, up_j, dn_i;
+  R vb, gl, tw;                  // lines: B_ij isotope_frac, B_ji / B_ij, A_ji / B_ji
+};
+
+// One lane's active set: its entries of the warp's union and its
+// wavelength-only constants, in the formal-solution precision R.
 template <typename R>
 struct ActiveSet {
-  int n;
-  int t[PYRH_NLTE_MAX_ACTIVE];   // transition index
-  int la[PYRH_NLTE_MAX_ACTIVE];  // wavelength index within the transition
+  const UnionEntry<R>* ue;       // the warp's union (shared memory)
+  unsigned lm;                   // this lane's entries (bit u: entry u)
+  int la;                        // wavelength index in the atmosphere's grid
   bool bb;                       // a line is active (containsBoundBound)
   bool pol;                      // a polarized line is active (containsPolarized)
-  R vb[PYRH_NLTE_MAX_ACTIVE];    // lines: B_ij isotope_frac; continua: alpha(lambda)
-  R gl[PYRH_NLTE_MAX_ACTIVE];    // lines: B_ji / B_ij
-  R tw[PYRH_NLTE_MAX_ACTIVE];    // lines: A_ji / B_ji; continua: 2 h c / lambda^3
-  R wl[PYRH_NLTE_MAX_ACTIVE];    // lines: wlambda (Hz); continua: 4 pi wlambda / (h lambda)
   R hckl;                        // h c / (k_B lambda)
-  // per active transition m with levels (i, j): its key i nlev + j and the
-  // active transitions (bit qq) whose lower level is i (but not m itself),
-  // whose upper level is j, and whose upper level is i -- what the
-  // cross-coupling sums of addtoCoupling select at every depth
-  int key[PYRH_NLTE_MAX_ACTIVE];
-  unsigned up_i[PYRH_NLTE_MAX_ACTIVE], up_j[PYRH_NLTE_MAX_ACTIVE], dn_i[PYRH_NLTE_MAX_ACTIVE];
+  R twc;                         // continua: 2 h c / lambda^3
+  R vbc[kMaxUnion];              // continua: alpha(lambda) of entry u
+  R wl[kMaxUnion];               // lines: wlambda (Hz); continua: 4 pi wlambda / (h lambda)
 };
 
 // Per-block staging of the atmosphere's quantities that every thread reads
@@ -257,21 +268,22 @@ struct NlteOpacity {
     }
     const pyrh_nlte_batch& b = A->b;
     R chi_a = 0, eta_a = 0;
-    for (int m = 0; m < as->n; ++m) {
-      const pyrh_nlte_transition& t = tr[as->t[m]];
-      const R ni = sh->n[t.i * nd + k], nj = sh->n[t.j * nd + k];
-      if (t.type == 0) {
-        const int64_t pi = t.phi_off + ((int64_t)k * 2 * A->nrays + q) * t.nlambda + as->la[m];
+    for (unsigned r = as->lm; r; r &= r - 1) {
+      const int u = __ffs(r) - 1;
+      const UnionEntry<R>& e = as->ue[u];
+      const R ni = sh->n[e.i * nd + k], nj = sh->n[e.j * nd + k];
+      if (e.type == 0) {
+        const int64_t pi = e.phi_off + ((int64_t)k * 2 * A->nrays + q) * e.nlambda + (as->la - e.nblue);
         const R phv = pi < A->phi_cap ? static_cast<const R*>(A->phi)[pi] : R(0);
-        const R V = R(kHPLANCK * kCLIGHT / (4.0 * kPI)) * (as->vb[m] * phv);
-        chi_a += V * (ni - as->gl[m] * nj);
-        eta_a += (as->tw[m] * as->gl[m]) * (V * nj);
+        const R V = R(kHPLANCK * kCLIGHT / (4.0 * kPI)) * (e.vb * phv);
+        chi_a += V * (ni - e.gl * nj);
+        eta_a += (e.tw * e.gl) * (V * nj);
       } else {
-        const R g = dev_exp(sh->lnst[t.i * nd + k] - sh->lnst[t.j * nd + k] -
+        const R g = dev_exp(sh->lnst[e.i * nd + k] - sh->lnst[e.j * nd + k] -
                             as->hckl * sh->iT[k]);
-        const R V = as->vb[m];
+        const R V = as->vbc[u];
         chi_a += V * (ni - g * nj);
-        eta_a += (as->tw[m] * g) * (V * nj);
+        eta_a += (as->twc * g) * (V * nj);
       }
     }
     const int64_t c = coff + (int64_t)k * ns + la, tc = b.total_cont;
@@ -522,66 +534,68 @@ __device__ __forceinline__ bool keyed_warp_sum(int key, R& a, R& c) {
 // depth of one ray direction, summed over the warp's 32 wavelengths.  All
 // lanes of the warp call it together; lanes with mine == false add nothing.
 template <typename R>
-__device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_transition* tr,
-                                          const ActiveSet<R>& as, const NlteShared<R>& sh,
-                                          const TileSink<R>& out, int nd, int nlev, int q, int k,
-                                          bool mine, R wdir, R I_k, R Psi_k, R omp, R Ieff_k,
-                                          R chi_k, R chi_bg) {
+__device__ __forceinline__ void add_rates(const NlteArgs& A, const ActiveSet<R>& as, int nunion,
+                                          const NlteShared<R>& sh, const TileSink<R>& out,
+                                          int nd, int nlev, int q, int k, bool mine, R wdir,
+                                          R I_k, R Psi_k, R omp, R Ieff_k, R chi_k, R chi_bg) {
   const unsigned full = 0xffffffffu;
   if (mine) atomicAdd(out.Jn + (int64_t)k * out.ns, wdir * I_k);
-  const int nact = mine ? as.n : 0;
-  const int nm = __reduce_max_sync(full, nact);
-  if (nm == 0) return;
+  if (!__any_sync(full, mine)) return;
+  const unsigned lm = mine ? as.lm : 0u;
   const R psi = mine ? Psi_k / chi_k : R(0);
   const R ichi = mine ? R(1) / chi_k : R(0);
-  // per transition: V W (product formed without the h c / 4 pi that cancels
-  // in it), U = TW G V, the stimulated-emission factor G and the
-  // transition's own opacity X
-  R VW[PYRH_NLTE_MAX_ACTIVE], U[PYRH_NLTE_MAX_ACTIVE], G[PYRH_NLTE_MAX_ACTIVE],
-      X[PYRH_NLTE_MAX_ACTIVE], CC[PYRH_NLTE_MAX_ACTIVE];
-  for (int m = 0; m < nact; ++m) {
-    const pyrh_nlte_transition& t = tr[as.t[m]];
-    const R ni = sh.n[t.i * nd + k], nj = sh.n[t.j * nd + k];
-    if (t.type == 0) {
-      const int64_t pi = t.phi_off + ((int64_t)k * 2 * A.nrays + q) * t.nlambda + as.la[m];
+  // per entry: V W (product formed without the h c / 4 pi that cancels in
+  // it), U = TW G V, the stimulated-emission factor G, the transition's own
+  // opacity X and its opacity with the weight W, CC
+  R VW[kMaxUnion], U[kMaxUnion], G[kMaxUnion], X[kMaxUnion], CC[kMaxUnion];
+  for (unsigned r = lm; r; r &= r - 1) {
+    const int u = __ffs(r) - 1;
+    const UnionEntry<R>& e = as.ue[u];
+    const R ni = sh.n[e.i * nd + k], nj = sh.n[e.j * nd + k];
+    if (e.type == 0) {
+      const int64_t pi = e.phi_off + ((int64_t)k * 2 * A.nrays + q) * e.nlambda + (as.la - e.nblue);
       const R phv = pi < A.phi_cap ? static_cast<const R*>(A.phi)[pi] : R(0);
-      const R vph = as.vb[m] * phv;
+      const R vph = e.vb * phv;
       const R V = R(kHPLANCK * kCLIGHT / (4.0 * kPI)) * vph;
-      G[m] = as.gl[m];
-      VW[m] = vph * (as.wl[m] * sh.wphi[t.line_index * nd + k]);
-      U[m] = (as.tw[m] * G[m]) * V;
-      X[m] = V * (ni - G[m] * nj);
+      G[u] = e.gl;
+      VW[u] = vph * (as.wl[u] * sh.wphi[e.line_index * nd + k]);
+      U[u] = (e.tw * G[u]) * V;
+      X[u] = V * (ni - G[u] * nj);
     } else {
-      G[m] = dev_exp(sh.lnst[t.i * nd + k] - sh.lnst[t.j * nd + k] - as.hckl * sh.iT[k]);
-      VW[m] = as.vb[m] * as.wl[m];
-      U[m] = (as.tw[m] * G[m]) * as.vb[m];
-      X[m] = as.vb[m] * (ni - G[m] * nj);
+      G[u] = dev_exp(sh.lnst[e.i * nd + k] - sh.lnst[e.j * nd + k] - as.hckl * sh.iT[k]);
+      VW[u] = as.vbc[u] * as.wl[u];
+      U[u] = (as.twc * G[u]) * as.vbc[u];
+      X[u] = as.vbc[u] * (ni - G[u] * nj);
     }
-    CC[m] = VW[m] * (ni - G[m] * nj);   // the transition's opacity with the weight W
+    CC[u] = VW[u] * (ni - G[u] * nj);
   }
-  for (int m = 0; m < nm; ++m) {
+  const int nu = nunion;
+  for (int u = 0; u < nu; ++u) {
+    const bool has = (lm >> u) & 1u;
+    const UnionEntry<R>& e = as.ue[u];
     int key = -1;
     R gij = 0, gji = 0;
-    if (m < nact) {
-      key = as.key[m];
-      // cross-coupling sums over the active set (addtoCoupling), with the
-      // transition's own terms kept apart: chi_up_o and U_down_o leave out
-      // transition m, X_o is the opacity of everything but m (background
-      // and the other transitions); each sum runs over the transitions in
-      // active-set order
+    if (has) {
+      key = e.key;
+      const R tw = e.type == 0 ? e.tw : as.twc;
+      // cross-coupling sums over the lane's active set (addtoCoupling), with
+      // the transition's own terms kept apart: chi_up_o and U_down_o leave
+      // out this transition, X_o is the opacity of everything but it
+      // (background and the other transitions); each sum runs over the
+      // transitions in active-set order
       R chi_up_o = 0, chi_down_j = 0, U_down_o = 0, U_down_i = 0, X_o = chi_bg;
-      const R chi_self = CC[m];
-      for (int qq = 0; qq < nact; ++qq)
-        if (qq != m) X_o += X[qq];
-      for (unsigned r = as.up_i[m]; r; r &= r - 1) chi_up_o += CC[__ffs(r) - 1];
-      for (unsigned r = as.up_j[m]; r; r &= r - 1) {
+      const R chi_self = CC[u];
+      for (unsigned r = lm & ~(1u << u); r; r &= r - 1) X_o += X[__ffs(r) - 1];
+      for (unsigned r = e.up_i & lm; r; r &= r - 1) chi_up_o += CC[__ffs(r) - 1];
+      for (unsigned r = e.up_j & lm; r; r &= r - 1) {
         const int qq = __ffs(r) - 1;
         chi_down_j += CC[qq];
-        if (qq != m) U_down_o += U[qq];
+        if (qq != u) U_down_o += U[qq];
       }
-      for (unsigned r = as.dn_i[m]; r; r &= r - 1) U_down_i += U[__ffs(r) - 1];
-      const int cnt = __popc(as.dn_i[m]);
-      const R wlamu = VW[m] * wdir;
+      const unsigned di = e.dn_i & lm;
+      for (unsigned r = di; r; r &= r - 1) U_down_i += U[__ffs(r) - 1];
+      const int cnt = __popc(di);
+      const R wlamu = VW[u] * wdir;
       gji = Ieff_k * wlamu;
       // fillgamma.c:185-196: (2 h nu^3 / c^2 + Ieff) g V W - chi_up Psi U_down.
       // The transition's own part of the coupling product,
@@ -590,9 +604,9 @@ __device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_tra
       // cores; that fraction is formed as X_o / chi + (X_m / chi)(1 - Psi)
       // from positive terms, and only the products with the other
       // transitions stay in the coupling term.
-      const R esc = X_o * ichi + (X[m] * ichi) * omp;
-      gij = (Ieff_k + as.tw[m] * esc) * G[m] * wlamu -
-            (chi_self * U_down_o + chi_up_o * (U[m] + U_down_o)) * (psi * wdir);
+      const R esc = X_o * ichi + (X[u] * ichi) * omp;
+      gij = (Ieff_k + tw * esc) * G[u] * wlamu -
+            (chi_self * U_down_o + chi_up_o * (U[u] + U_down_o)) * (psi * wdir);
       // one term per active transition whose upper level is i
       if (cnt) gji += R(cnt) * chi_down_j * (psi * U_down_i) * wdir;
     }
@@ -606,11 +620,11 @@ __device__ __forceinline__ void add_rates(const NlteArgs& A, const pyrh_nlte_tra
       // c^2 + I) V W, with the intensity itself (not Ieff)
       int rkey = -1;
       R rij = 0, rji = 0;
-      if (m < nact && as.t[m] < A.max_ntrans) {
-        rkey = as.t[m];
-        const R wlamu = VW[m] * wdir;
+      if (has && e.t < A.max_ntrans) {
+        rkey = e.t;
+        const R wlamu = VW[u] * wdir;
         rij = I_k * wlamu;
-        rji = G[m] * (as.tw[m] + I_k) * wlamu;
+        rji = G[u] * ((e.type == 0 ? e.tw : as.twc) + I_k) * wlamu;
       }
       if (keyed_warp_sum<R>(rkey, rij, rji)) {
         R* r = out.rslab + (int64_t)(2 * rkey) * out.total_depth + out.doff + k;
@@ -643,7 +657,9 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
   const pyrh_nlte_transition* tr = b.trans + b.trans_off[p];
   const double* lamp = b.lambda + b.lam_off[p];
   NlteShared<R> sh;
-  formal_smem_layout<R>(nlev, b.max_ndep, A.nrays, b.max_nline, &sh, smem_raw);
+  // the union tables of the block's warps follow the staged arrays
+  const size_t union_off = formal_smem_layout<R>(nlev, b.max_ndep, A.nrays, b.max_nline, &sh,
+                                                 smem_raw);
   const int nthr = blockDim.x;
   for (int e = threadIdx.x; e < nlev * nd; e += nthr) {
     const int i = e / nd, k = e % nd;
@@ -670,49 +686,76 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
   const bool live = la_raw < ns;
   const int la = live ? la_raw : ns - 1;
   const double lam = lamp[la];
+  // the warp's union of active sets: every transition that covers some
+  // lane's wavelength (each lane taking at most PYRH_NLTE_MAX_ACTIVE, the
+  // first in continua-then-lines order, as the active set of one wavelength
+  // holds them), built in that order by one ballot per transition
+  UnionEntry<R>* ue = reinterpret_cast<UnionEntry<R>*>(smem_raw + union_off) +
+                      (threadIdx.x >> 5) * kMaxUnion;
   ActiveSet<R> as;
-  as.n = 0;
+  as.ue = ue;
+  as.lm = 0u;
+  as.la = la;
   as.bb = false;
   as.pol = false;
   as.hckl = R((kHPLANCK * kCLIGHT / (kKBOLTZMANN * kNM_TO_M)) / lam);
+  as.twc = R(2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M) / (lam * lam * lam));
+  int nunion = 0, nown = 0;
   for (int pass = 1; pass >= 0; --pass)       // continua (type 1) first, then lines
     for (int t = 0; t < nt; ++t) {
       const pyrh_nlte_transition& T = tr[t];
       if (T.type != pass) continue;
-      if (la >= T.nblue && la < T.nblue + T.nlambda && as.n < PYRH_NLTE_MAX_ACTIVE) {
-        const int m = as.n++;
-        as.t[m] = t;
-        as.la[m] = la - T.nblue;
+      const bool mine_t = la >= T.nblue && la < T.nblue + T.nlambda && nown < PYRH_NLTE_MAX_ACTIVE;
+      const unsigned who = __ballot_sync(full, mine_t);
+      if (!who) continue;
+      if (nunion == kMaxUnion) {            // uniform: more transitions than a table holds
+        if (lane == 0) atomicOr(A.err, 8);
+        continue;
+      }
+      const int u = nunion++;
+      if (lane == (u & 31)) {
+        UnionEntry<R>& e = ue[u];
+        e.t = t;
+        e.type = T.type;
+        e.i = T.i;
+        e.j = T.j;
+        e.key = T.i * nlev + T.j;
+        e.nblue = T.nblue;
+        e.nlambda = T.nlambda;
+        e.line_index = T.line_index;
+        e.phi_off = T.phi_off;
+        e.vb = T.type == 0 ? R(T.Bij * T.isotope_frac) : R(0);
+        e.gl = T.type == 0 ? R(T.Bji / T.Bij) : R(0);
+        e.tw = T.type == 0 ? R(T.Aji / T.Bji) : R(0);
+      }
+      if (mine_t) {
+        ++nown;
+        as.lm |= 1u << u;
+        const int lt = la - T.nblue;
         if (T.type == 0) {
           as.bb = true;
           if (T.polarized) as.pol = true;
-          as.vb[m] = R(T.Bij * T.isotope_frac);
-          as.gl[m] = R(T.Bji / T.Bij);
-          as.tw[m] = R(T.Aji / T.Bji);
-          as.wl[m] = R(wlambda_line(lamp + T.nblue, T, as.la[m]));
+          as.vbc[u] = R(0);
+          as.wl[u] = R(wlambda_line(lamp + T.nblue, T, lt));
         } else {
-          as.vb[m] = R(b.alpha[T.alpha_off + as.la[m]]);
-          as.gl[m] = R(0);
-          as.tw[m] = R(2.0 * kHPLANCK * kCLIGHT / (kNM_TO_M * kNM_TO_M * kNM_TO_M) /
-                       (lam * lam * lam));
-          as.wl[m] = R(4.0 * kPI / kHPLANCK * (wlambda_cont(lamp + T.nblue, T, as.la[m]) / lam));
+          as.vbc[u] = R(b.alpha[T.alpha_off + lt]);
+          as.wl[u] = R(4.0 * kPI / kHPLANCK * (wlambda_cont(lamp + T.nblue, T, lt) / lam));
         }
       }
     }
-  for (int m = 0; m < as.n; ++m) {
-    const pyrh_nlte_transition& T = tr[as.t[m]];
-    as.key[m] = T.i * nlev + T.j;
+  __syncwarp();
+  for (int u = lane; u < nunion; u += 32) {   // coupling partners of each entry
     unsigned ui = 0, uj = 0, di = 0;
-    for (int qq = 0; qq < as.n; ++qq) {
-      const pyrh_nlte_transition& U = tr[as.t[qq]];
-      if (U.i == T.i && qq != m) ui |= 1u << qq;
-      if (U.j == T.j) uj |= 1u << qq;
-      if (U.j == T.i) di |= 1u << qq;
+    for (int qq = 0; qq < nunion; ++qq) {
+      if (ue[qq].i == ue[u].i && qq != u) ui |= 1u << qq;
+      if (ue[qq].j == ue[u].j) uj |= 1u << qq;
+      if (ue[qq].j == ue[u].i) di |= 1u << qq;
     }
-    as.up_i[m] = ui;
-    as.up_j[m] = uj;
-    as.dn_i[m] = di;
+    ue[u].up_i = ui;
+    ue[u].up_j = uj;
+    ue[u].dn_i = di;
   }
+  __syncwarp();
   const double B0 = planck(b.T[doff + nd - 2], lam), B1 = planck(b.T[doff + nd - 1], lam);
   const JRow<R> Jold{static_cast<const R*>(A.Jr) + coff + la, ns};
   // angle-dependent wavelengths (formal.c:92-101: a polarized active set or
@@ -746,7 +789,7 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
         const int q = op.q;
         auto emit = [&](int k, R I_k, R Psi_k, R omp, R Ieff_k, R chi_k, R chi_bg) {
           if (!emergent_only)
-            add_rates<R>(A, tr, as, sh, out, nd, nlev, q, k, bez, wdir, I_k, Psi_k, omp, Ieff_k,
+            add_rates<R>(A, as, nunion, sh, out, nd, nlev, q, k, bez, wdir, I_k, Psi_k, omp, Ieff_k,
                          chi_k, chi_bg);
         };
         const R Ie = bezier_sweep<R>(op, dsl, nd, to_obs, B0, B1, Jold, emit);
@@ -769,7 +812,7 @@ nlte_formal_kernel(NlteArgs A, int emergent_only, double* I_out) {
       if (!emergent_only) {
         const R wdir = R(A.wmu[ray]);
         for (int k = 0; k < nd; ++k)
-          add_rates<R>(A, tr, as, sh, out, nd, nlev, op.q, k, feau, wdir, S[k], F[k], zt[k],
+          add_rates<R>(A, as, nunion, sh, out, nd, nlev, op.q, k, feau, wdir, S[k], F[k], zt[k],
                        Sb[k], chis[k], cbg[k]);
       }
     }
@@ -1067,8 +1110,10 @@ int nlte_ray_groups(int natm, int max_nspect, int nrays) {
 
 size_t nlte_formal_smem(int nlevel, int maxd, int nrays, int max_nline, int precision) {
   return precision == PYRH_FP32
-             ? formal_smem_layout<float>(nlevel, maxd, nrays, max_nline, nullptr, nullptr)
-             : formal_smem_layout<double>(nlevel, maxd, nrays, max_nline, nullptr, nullptr);
+             ? formal_smem_layout<float>(nlevel, maxd, nrays, max_nline, nullptr, nullptr) +
+                   kFormalWarps * kMaxUnion * sizeof(UnionEntry<float>)
+             : formal_smem_layout<double>(nlevel, maxd, nrays, max_nline, nullptr, nullptr) +
+                   kFormalWarps * kMaxUnion * sizeof(UnionEntry<double>);
 }
 
 template <typename R>

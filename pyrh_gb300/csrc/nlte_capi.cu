@@ -276,7 +276,8 @@ pyrh_status pyrh_nlte_solve(const pyrh_nlte_batch* b, const pyrh_nlte_config* cf
     return PYRH_ERR_CUDA;
   }
   if (err) {
-    pyrh::set_error(err & 4   ? "an atmosphere's ntrans exceeds max_ntrans (rates)"
+    pyrh::set_error(err & 8   ? "more than 32 transitions active across one tile of 32 wavelengths"
+                    : err & 4 ? "an atmosphere's ntrans exceeds max_ntrans (rates)"
                     : err & 2 ? "an atmosphere's ndep exceeds max_ndep or the depth limit"
                               : "line profiles do not fit the workspace (phi_off beyond capacity)");
     return PYRH_ERR_ARG;
@@ -326,7 +327,8 @@ pyrh_status pyrh_nlte_emergent(const pyrh_nlte_batch* b, const pyrh_nlte_config*
     return PYRH_ERR_CUDA;
   }
   if (err) {
-    pyrh::set_error("line profiles do not fit the workspace");
+    pyrh::set_error(err & 8 ? "more than 32 transitions active across one tile of 32 wavelengths"
+                            : "line profiles do not fit the workspace");
     return PYRH_ERR_ARG;
   }
   return PYRH_OK;
@@ -439,7 +441,8 @@ extern "C" pyrh_status pyrh_nlte_solve_static(const pyrh_nlte_batch* b,
     return PYRH_ERR_CUDA;
   }
   if (err) {
-    pyrh::set_error(err & 4   ? "an atmosphere's ntrans exceeds max_ntrans (rates)"
+    pyrh::set_error(err & 8   ? "more than 32 transitions active across one tile of 32 wavelengths"
+                    : err & 4 ? "an atmosphere's ntrans exceeds max_ntrans (rates)"
                     : err & 2 ? "an atmosphere's ndep exceeds max_ndep or the depth limit"
                               : "line profiles do not fit the static scratch (phi_off beyond phi_elems)");
     return PYRH_ERR_ARG;
