@@ -93,11 +93,12 @@ __global__ void nlte_profile_kernel(NlteArgs A) {
     if (A.moving) v += (to_obs ? 1.0 : -1.0) * A.muz[mu] * b.vel[doff + k] / vb;
     const double a = L.voigt ? b.adamp[b.adamp_off[p] + (int64_t)L.line_index * nd + k] : 0.0;
     const int64_t idx = L.phi_off + r;
-    // Armstrong's function in FP64 in both modes.  Evaluated in FP32 (its
-    // own error below 1.5e-5) the FP32 solve ran 12 % faster, but the
+    // Armstrong's function in FP64; for FP32 profiles with the Gaussian
+    // factor in FP32 and the Dawson sum cut at 1e-10 (H within 2e-7 of
+    // itself).  Evaluated wholly in FP32 (its own error up to 1.5e-5) the
     // converged populations moved from 2.5e-4 to 5.9e-4 of the reference's
     // over the 1024-atmosphere batch and past 1e-3 at 160 depths.
-    const double H = voigt_armstrong(a, v);
+    const double H = sizeof(R) == 4 ? voigt_armstrong_t<double, true>(a, v) : voigt_armstrong(a, v);
     if (idx < A.phi_cap)
       static_cast<R*>(A.phi)[idx] = R(H * L.c_fraction / (kSQRTPI * vb));
     else
