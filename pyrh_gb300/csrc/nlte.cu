@@ -62,6 +62,10 @@ __device__ __forceinline__ double wlambda_cont(const double* lam, const pyrh_nlt
 // ---------------------------------------------------------- profiles -----
 // phi block of a line: [k][2*nrays][nlambda], lambda fastest.
 
+// One thread per (line, depth, wavelength) evaluates the profile of every
+// ray and direction: the Doppler offset, the damping and the normalisation
+// are formed once, the ray's velocity shift once per ray, and a static
+// atmosphere (no shift) takes one evaluation for all of them.
 template <typename R>
 __global__ void nlte_profile_kernel(NlteArgs A) {
   const int p = blockIdx.y;
@@ -72,37 +76,55 @@ __global__ void nlte_profile_kernel(NlteArgs A) {
   const double* lam = b.lambda + b.lam_off[p];
   int64_t total = 0;
   for (int t = 0; t < nt; ++t)
-    if (tr[t].type == 0) total += (int64_t)tr[t].nlambda * nq * nd;
+    if (tr[t].type == 0) total += (int64_t)tr[t].nlambda * nd;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
     int64_t r = e;
     int t = 0;
     for (; t < nt; ++t) {
       if (tr[t].type != 0) continue;
-      const int64_t sz = (int64_t)tr[t].nlambda * nq * nd;
+      const int64_t sz = (int64_t)tr[t].nlambda * nd;
       if (r < sz) break;
       r -= sz;
     }
     const pyrh_nlte_transition& L = tr[t];
     const int la = (int)(r % L.nlambda);
-    const int q = (int)((r / L.nlambda) % nq);
-    const int k = (int)(r / ((int64_t)L.nlambda * nq));
-    const int mu = q / 2, to_obs = q % 2;
+    const int k = (int)(r / L.nlambda);
     const double vb = b.vbroad[doff + k];
-    double v = (lam[L.nblue + la] - L.lambda0 - L.c_shift) * kCLIGHT / (vb * L.lambda0);
-    if (A.moving) v += (to_obs ? 1.0 : -1.0) * A.muz[mu] * b.vel[doff + k] / vb;
+    const double v0 = (lam[L.nblue + la] - L.lambda0 - L.c_shift) * kCLIGHT / (vb * L.lambda0);
     const double a = L.voigt ? b.adamp[b.adamp_off[p] + (int64_t)L.line_index * nd + k] : 0.0;
-    const int64_t idx = L.phi_off + r;
-    // Armstrong's function in FP64; for FP32 profiles with the Gaussian
-    // factor in FP32 and the Dawson sum cut at 1e-10 (H within 2e-7 of
-    // itself).  Evaluated wholly in FP32 (its own error up to 1.5e-5) the
-    // converged populations moved from 2.5e-4 to 5.9e-4 of the reference's
-    // over the 1024-atmosphere batch and past 1e-3 at 160 depths.
-    const double H = sizeof(R) == 4 ? voigt_armstrong_t<double, true>(a, v) : voigt_armstrong(a, v);
-    if (idx < A.phi_cap)
-      static_cast<R*>(A.phi)[idx] = R(H * L.c_fraction / (kSQRTPI * vb));
-    else
+    const double den = kSQRTPI * vb;
+    // the first element of the line's block for this depth and wavelength;
+    // direction q is nlambda further on per q
+    const int64_t base = L.phi_off + (int64_t)k * nq * L.nlambda + la;
+    if (base + (int64_t)(nq - 1) * L.nlambda >= A.phi_cap) {
       atomicOr(A.err, 1);
+      continue;
+    }
+    R* out = static_cast<R*>(A.phi) + base;
+    double H_static = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      const int mu = q / 2, to_obs = q % 2;
+      double v = v0;
+      double H;
+      if (A.moving) {
+        const double d = A.muz[mu] * b.vel[doff + k] / vb;
+        v += to_obs ? d : -d;
+      }
+      if (A.moving || q == 0) {
+        // Armstrong's function in FP64; for FP32 profiles with the Gaussian
+        // factor in FP32 and the Dawson sum cut at 1e-10 (H within 2e-7 of
+        // itself).  Evaluated wholly in FP32 (its own error up to 1.5e-5)
+        // the converged populations moved from 2.5e-4 to 5.9e-4 of the
+        // reference's over the 1024-atmosphere batch and past 1e-3 at 160
+        // depths.
+        H = sizeof(R) == 4 ? voigt_armstrong_t<double, true>(a, v) : voigt_armstrong(a, v);
+        H_static = H;
+      } else {
+        H = H_static;
+      }
+      out[(int64_t)q * L.nlambda] = R(H * L.c_fraction / den);
+    }
   }
 }
 
