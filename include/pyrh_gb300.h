@@ -774,6 +774,63 @@ pyrh_status pyrh_solve_ne(const pyrh_elem_tables *tables, int64_t npoint, const 
                           const double *nHtot, double *ne, int32_t fromscratch, int32_t *niter,
                           void *stream);
 
+/* ------------------------------------------------------ chemical equilibrium --
+ * Molecule files (readMolecule, rh/readmolecule.c:66-240: ID, charge,
+ * constituents, dissociation energy, fit type, formation temperatures,
+ * partition-function and equilibrium-constant fits) and, on the device with
+ * one thread per depth point, the molecular equilibrium of
+ * ChemicalEquilibrium (rh/chemequil.c:107-390): Newton iteration on the
+ * nuclei's conservation and the molecules' Saha equations with H- in the
+ * hydrogen balance, equilibrium constants by equilconstant
+ * (rh/chemequil.c:456-535), Crout LU with one improvement (ludcmp.c),
+ * stopping at a relative change of 1e-3 or after 10 steps
+ * (rh/background.h:18-19). */
+#define PYRH_MOL_MAX_ELEMENTS 4
+#define PYRH_MOL_MAX_COEF 12
+#define PYRH_CHEM_MAX_NUCLEI 8
+#define PYRH_CHEM_MAX_MOLECULES 24
+
+typedef enum {
+  PYRH_FIT_KURUCZ_70 = 0, PYRH_FIT_KURUCZ_85 = 1, PYRH_FIT_SAUVAL_TATUM_84 = 2,
+  PYRH_FIT_IRWIN_81 = 3, PYRH_FIT_TSUJI_73 = 4
+} pyrh_mol_fit;
+
+typedef struct {
+  char id[16];
+  int32_t charge;                               /* 0 or 1 */
+  int32_t nelement;                             /* constituent elements */
+  int32_t pt_index[PYRH_MOL_MAX_ELEMENTS];      /* element index (atomic number - 1) */
+  int32_t pt_count[PYRH_MOL_MAX_ELEMENTS];      /* atoms of each */
+  int32_t nnuclei;                              /* atoms in the molecule */
+  int32_t fit;                                  /* pyrh_mol_fit */
+  double ediss;                                 /* dissociation energy, J */
+  double tmin, tmax;                            /* formation range, K */
+  int32_t npf, neqc;
+  double pf_coef[PYRH_MOL_MAX_COEF];            /* in the reference's storage order */
+  double eqc_coef[PYRH_MOL_MAX_COEF];
+} pyrh_molecule;
+
+/* Parses the text of one molecule file; constituents must be elements with
+   abundance_set ([PYRH_NELEM]). */
+pyrh_status pyrh_molecule_read(const char *text, const int32_t *abundance_set,
+                               pyrh_molecule *molecule);
+
+/* Chemical equilibrium at npoint depth points for the molecules mol[nmol]
+   (host array; the first must be H2, as the reference requires).  The
+   nuclei are the elements bound in some molecule, in element order
+   (hydrogen first); fn0_model (host array [PYRH_NELEM] of device pointers,
+   or NULL) gives, for an element with an atom model, the neutral fraction of
+   its LTE populations at every point; elements without one take theirs
+   from the tables' partition functions (getfjk).  Outputs (device):
+   nmol [nmol][npoint] molecule densities, nHmin [npoint], nnuc
+   [nnuclei][npoint] the nuclei's atomic densities afterwards (a model atom's
+   populations scale by nnuc / its total), niter [npoint] steps taken (-1:
+   not converged; may be NULL). */
+pyrh_status pyrh_chem_equil(const pyrh_elem_tables *tables, const pyrh_molecule *mol,
+                            int32_t nmol, int64_t npoint, const double *T, const double *ne,
+                            const double *nHtot, const double *const *fn0_model, double *nmol_out,
+                            double *nHmin, double *nnuc, int32_t *niter, void *stream);
+
 /* Number of kernel launches the last pyrh_lte_stokes / pyrh_nlte_* call issued. */
 int32_t pyrh_last_launch_count(void);
 

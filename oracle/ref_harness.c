@@ -15,6 +15,7 @@
  *  harness_dump_ltepops writes the element tables (partition functions,
  *                    ionisation potentials, abundances), LTEpops_elem() of
  *                    every element and Solve_ne() after the same set-up.
+ *  harness_dump_chem writes ChemicalEquilibrium()'s inputs and results.
  *  harness_dump_nlte performs the whole rhf1d() sequence with one ACTIVE atom
  *                    and writes the converged populations, the collision
  *                    matrix, the wavelength grid and the emergent intensity.
@@ -466,6 +467,78 @@ int harness_dump_ltepops(const char *cwd, int Ndep, const double *atm, int Nabun
   write_f64(outdir, "ne_warm", ne2, Nspace);
   free(meta); free(pf); free(ion); free(pops); free(ne1); free(ne2);
   return Nspace;
+}
+
+#define PYRH_HARNESS_MAX_NUC 32
+/* Chemical equilibrium (ChemicalEquilibrium, rh/chemequil.c:107-390) after
+   the set-up of rhf1d() and the LTE populations of the atoms
+   (SetLTEQuantities, rh/ltepops.c:224-249).  Files:
+     T, ne, nHtot [Nspace] (SI);
+     nuclei [Nnuclei] element index of each nucleus (elements bound in a
+       molecule, in element order); nuc_model [Nnuclei] 1 if an atom model
+       gives its neutral fraction;
+     fn0 [Nnuclei][Nspace] the neutral fraction the equilibrium starts from
+       (from the model's LTE populations, else from the element's partition
+       functions, getfjk), as rh/chemequil.c:227-246 forms it;
+     nmol [Nmolecule][Nspace], nHmin [Nspace] the results;
+     ntot_model [Nnuclei][Nspace] the model atoms' total density afterwards
+       (the nucleus' atomic density; zeros for nuclei without a model). */
+void SetLTEQuantities(void);
+void ChemicalEquilibrium(int NmaxIter, double iterLimit);
+void getfjk(Element *element, double ne, int k, double *fjk, double *dfjk);
+
+int harness_dump_chem(const char *cwd, int Ndep, const double *atm, const char *outdir)
+{
+  double *a, *w, lam500 = 500.0;
+  lte_setup(cwd, 1.0, Ndep, atm, 1, &lam500, &a, &w);
+  SetLTEQuantities();
+  int Nspace = atmos.Nspace, nn = 0;
+  int nuc[PYRH_HARNESS_MAX_NUC], model[PYRH_HARNESS_MAX_NUC];
+  for (int i = 0; i < atmos.Nelem && nn < PYRH_HARNESS_MAX_NUC; i++)
+    if (atmos.elements[i].Nmolecule > 0) {
+      nuc[nn] = i;
+      model[nn] = atmos.elements[i].model != NULL;
+      nn++;
+    }
+  double *fn0 = (double *) calloc((long) nn * Nspace, sizeof(double));
+  double fjk[16], dfjk[16];
+  for (int i = 0; i < nn; i++) {
+    Element *el = &atmos.elements[nuc[i]];
+    Atom *atom = el->model;
+    for (int k = 0; k < Nspace; k++) {
+      if (atom == NULL) {
+        getfjk(el, atmos.ne[k], k, fjk, dfjk);
+        fn0[(long) i * Nspace + k] = fjk[0];
+      } else {
+        double s = 0.0;
+        for (int j = 0; j < atom->Nlevel; j++) {
+          if (atom->stage[j] > 0) break;
+          if (atom->active && atom->initial_solution != OLD_POPULATIONS) s += atom->nstar[j][k];
+          else s += atom->n[j][k];
+        }
+        fn0[(long) i * Nspace + k] = s / atom->ntotal[k];
+      }
+    }
+  }
+  ChemicalEquilibrium(N_MAX_CHEM_ITER, CHEM_ITER_LIMIT);
+  double *nmol = (double *) malloc((long) atmos.Nmolecule * Nspace * sizeof(double));
+  for (int m = 0; m < atmos.Nmolecule; m++)
+    memcpy(nmol + (long) m * Nspace, atmos.molecules[m].n, Nspace * sizeof(double));
+  double *ntot = (double *) calloc((long) nn * Nspace, sizeof(double));
+  for (int i = 0; i < nn; i++)
+    if (atmos.elements[nuc[i]].model)
+      memcpy(ntot + (long) i * Nspace, atmos.elements[nuc[i]].model->ntotal, Nspace * sizeof(double));
+  write_f64(outdir, "T", atmos.T, Nspace);
+  write_f64(outdir, "ne", atmos.ne, Nspace);
+  write_f64(outdir, "nHtot", atmos.nHtot, Nspace);
+  write_i32(outdir, "nuclei", nuc, nn);
+  write_i32(outdir, "nuc_model", model, nn);
+  write_f64(outdir, "fn0", fn0, (long) nn * Nspace);
+  write_f64(outdir, "nmol", nmol, (long) atmos.Nmolecule * Nspace);
+  write_f64(outdir, "nHmin", atmos.nHmin, Nspace);
+  write_f64(outdir, "ntot_model", ntot, (long) nn * Nspace);
+  free(fn0); free(nmol); free(ntot);
+  return atmos.Nmolecule;
 }
 
 /* ------------------------------------------------------------------ NLTE */

@@ -232,6 +232,27 @@ def read_ltepops_dump(outdir: str) -> dict:
     return d
 
 
+def _chem_job(args):
+    workdir, pyrh_path, atm, outdir = args
+    lib = _lib(pyrh_path)
+    atm = np.ascontiguousarray(atm, dtype=np.float64)
+    os.makedirs(outdir, exist_ok=True)
+    lib.harness_dump_chem.restype = C.c_int
+    return lib.harness_dump_chem(workdir.encode(), atm.shape[1], _p(atm), outdir.encode())
+
+
+def read_chem_dump(outdir: str) -> dict:
+    """The files of harness_dump_chem as arrays."""
+    f64 = lambda n: np.fromfile(os.path.join(outdir, n + ".f64"))
+    i32 = lambda n: np.fromfile(os.path.join(outdir, n + ".i32"), dtype=np.int32)
+    d = {k: f64(k) for k in ("T", "ne", "nHtot", "nHmin")}
+    nd = len(d["T"])
+    d["nuclei"], d["nuc_model"] = i32("nuclei"), i32("nuc_model")
+    for k in ("fn0", "nmol", "ntot_model"):
+        d[k] = f64(k).reshape(-1, nd)
+    return d
+
+
 def read_background_dump(outdir: str) -> dict:
     """The files of harness_dump_background as arrays."""
     f64 = lambda n: np.fromfile(os.path.join(outdir, n + ".f64"))
@@ -318,6 +339,9 @@ class Reference:
 
     def dump_ltepops(self, workdir, atm, ab_id, ab_val, outdir):
         return self._run(_ltepops_job, (workdir, self.pyrh_path, atm, ab_id, ab_val, outdir))
+
+    def dump_chem(self, workdir, atm, outdir):
+        return self._run(_chem_job, (workdir, self.pyrh_path, atm, outdir))
 
     def nlte(self, workdir, mu, atm, wave, outdir, mode):
         return self._run(_nlte_job, (workdir, self.pyrh_path, mu, atm, wave, outdir, mode))

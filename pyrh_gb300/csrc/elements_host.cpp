@@ -1,13 +1,15 @@
-// elements_host.cpp -- host readers of the element data: the abundance file
-// and the Kurucz partition-function file.
+// elements_host.cpp -- host readers of the element and molecule data: the
+// abundance file, the Kurucz partition-function file and molecule files.
 //
-// Reference routine restated here (file:line in the reference tree):
+// Reference routines restated here (file:line in the reference tree):
 //   readAbundance   rh/abundance.c:72-220  (record matching, the pyrh
 //                                           overrides by record number, the
 //                                           DEX and metallicity conversions,
 //                                           the XDR partition-function file
 //                                           and its conversion to ln U and J)
 //   getLine         rh/getline.c:30-55     (comment and blank lines)
+//   readMolecule    rh/readmolecule.c:66-240 (the molecule file up to its
+//                                           equilibrium-constant fit)
 // The file formats are the reference's, so they are parsed field for field;
 // every conversion keeps the reference's expression (POW10(x) is
 // exp(LG10 x), rh/rh.h:50) so the tables come out bit-identical.
@@ -172,5 +174,109 @@ extern "C" pyrh_status pyrh_pf_parse(const unsigned char* bytes, size_t nbytes,
   }
   *npf = np;
   *nrows = rows;
+  return PYRH_OK;
+}
+
+// ---------------------------------------------------------------- molecules --
+// readMolecule (rh/readmolecule.c:66-240): the records up to the
+// equilibrium-constant fit, each on the next line that is neither blank nor
+// a comment (getLine).
+namespace {
+
+struct Lines {
+  const char* s;
+  bool next(std::string& out) {
+    while (*s) {
+      const char* e = strchr(s, '\n');
+      std::string line = e ? std::string(s, e - s) : std::string(s);
+      s = e ? e + 1 : s + line.size();
+      char tok[2];
+      if (line.empty() || line[0] == '#' || sscanf(line.c_str(), "%1s", tok) < 1) continue;
+      out = line;
+      return true;
+    }
+    return false;
+  }
+};
+
+// "N c_1 ... c_N" stored backwards, as the reference reads them
+bool read_fit(const std::string& line, int32_t* n, double* coef) {
+  std::string buf = line;
+  char* save = nullptr;
+  char* tok = strtok_r(&buf[0], " ", &save);
+  if (!tok || sscanf(tok, "%d", n) != 1 || *n < 0 || *n > PYRH_MOL_MAX_COEF) return false;
+  for (int i = *n - 1; i >= 0; --i) {
+    tok = strtok_r(nullptr, " ", &save);
+    if (!tok || sscanf(tok, "%lf", coef + i) != 1) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" pyrh_status pyrh_molecule_read(const char* text, const int32_t* abundance_set,
+                                          pyrh_molecule* m) {
+  if (!text || !abundance_set || !m) return fail(PYRH_ERR_ARG, "molecule: NULL argument");
+  memset(m, 0, sizeof(*m));
+  Lines in{text};
+  std::string line;
+  if (!in.next(line) || sscanf(line.c_str(), "%15s", m->id) != 1)
+    return fail(PYRH_ERR_ARG, "molecule: no ID");
+  if (!in.next(line) || sscanf(line.c_str(), "%d", &m->charge) != 1)
+    return fail(PYRH_ERR_ARG, "molecule %s: no charge", m->id);
+  if (m->charge < 0 || m->charge > 1)
+    return fail(PYRH_ERR_ARG, "molecule %s: only neutral or singly charged molecules", m->id);
+  if (!in.next(line)) return fail(PYRH_ERR_ARG, "molecule %s: no constituents", m->id);
+  {
+    std::string buf = line;
+    char* save = nullptr;
+    for (char* tok = strtok_r(&buf[0], " ,", &save); tok; tok = strtok_r(nullptr, " ,", &save)) {
+      if (m->nelement == PYRH_MOL_MAX_ELEMENTS)
+        return fail(PYRH_ERR_UNSUPPORTED, "molecule %s: more than %d elements", m->id,
+                    PYRH_MOL_MAX_ELEMENTS);
+      int count = 1;
+      char el[32];
+      if (sscanf(tok, "%d%31s", &count, el) == 0) {
+        count = 1;
+        if (sscanf(tok, "%31s", el) != 1) continue;
+      }
+      for (char* c = el; *c; ++c) *c = (char)toupper((unsigned char)*c);
+      if (strlen(el) == 1) strcat(el, " ");
+      int found = -1;
+      for (int n = 0; n < PYRH_NELEM; ++n)
+        if (strstr(el, kElementID[n])) {
+          if (abundance_set[n]) found = n;
+          break;
+        }
+      if (found < 0)
+        return fail(PYRH_ERR_ARG, "molecule %s: element %s unknown or without abundance", m->id,
+                    el);
+      m->pt_index[m->nelement] = found;
+      m->pt_count[m->nelement] = count;
+      m->nnuclei += count;
+      ++m->nelement;
+    }
+    if (m->nelement == 0) return fail(PYRH_ERR_ARG, "molecule %s: no constituents", m->id);
+  }
+  if (!in.next(line) || sscanf(line.c_str(), "%lf", &m->ediss) != 1)
+    return fail(PYRH_ERR_ARG, "molecule %s: no dissociation energy", m->id);
+  m->ediss *= 1.60217733E-19;   // EV
+  char fit[64] = "";
+  if (!in.next(line) || sscanf(line.c_str(), "%63s", fit) != 1)
+    return fail(PYRH_ERR_ARG, "molecule %s: no fit type", m->id);
+  if (strstr(fit, "KURUCZ_70")) m->fit = PYRH_FIT_KURUCZ_70;
+  else if (strstr(fit, "KURUCZ_85")) m->fit = PYRH_FIT_KURUCZ_85;
+  else if (strstr(fit, "SAUVAL_TATUM_84")) m->fit = PYRH_FIT_SAUVAL_TATUM_84;
+  else if (strstr(fit, "IRWIN_81")) m->fit = PYRH_FIT_IRWIN_81;
+  else if (strstr(fit, "TSUJI_73")) m->fit = PYRH_FIT_TSUJI_73;
+  else return fail(PYRH_ERR_ARG, "molecule %s: unknown fit %s", m->id, fit);
+  if (m->charge > 0 && m->fit != PYRH_FIT_KURUCZ_70 && m->fit != PYRH_FIT_KURUCZ_85)
+    return fail(PYRH_ERR_ARG, "molecule %s: a charged molecule needs a KURUCZ fit", m->id);
+  if (!in.next(line) || sscanf(line.c_str(), "%lf %lf", &m->tmin, &m->tmax) != 2)
+    return fail(PYRH_ERR_ARG, "molecule %s: no formation temperatures", m->id);
+  if (!in.next(line) || !read_fit(line, &m->npf, m->pf_coef))
+    return fail(PYRH_ERR_ARG, "molecule %s: partition-function fit", m->id);
+  if (!in.next(line) || !read_fit(line, &m->neqc, m->eqc_coef))
+    return fail(PYRH_ERR_ARG, "molecule %s: equilibrium-constant fit", m->id);
   return PYRH_OK;
 }

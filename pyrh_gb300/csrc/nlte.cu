@@ -32,6 +32,7 @@
 
 #include "../../include/pyrh_gb300.h"
 #include "nlte.cuh"
+#include "lu_device.cuh"
 #include "rt_device.cuh"
 #include "voigt_armstrong.cuh"
 
@@ -889,70 +890,6 @@ __global__ void nlte_jcopy_kernel(NlteArgs A) {
 
 // ------------------------------------------------ statistical equilibrium --
 
-__device__ void lu_solve(int n, double* A, double* bvec) {
-  double Ac[PYRH_NLTE_MAX_LEVELS * PYRH_NLTE_MAX_LEVELS], bc[PYRH_NLTE_MAX_LEVELS];
-  double vv[PYRH_NLTE_MAX_LEVELS], res[PYRH_NLTE_MAX_LEVELS];
-  int index[PYRH_NLTE_MAX_LEVELS];
-  for (int i = 0; i < n * n; ++i) Ac[i] = A[i];
-  for (int i = 0; i < n; ++i) bc[i] = bvec[i];
-  for (int i = 0; i < n; ++i) {
-    double big = 0.0;
-    for (int j = 0; j < n; ++j) big = fmax(big, fabs(A[i * n + j]));
-    vv[i] = (big == 0.0) ? 0.0 : 1.0 / big;
-  }
-  for (int j = 0; j < n; ++j) {
-    int imax = 0;
-    for (int i = 0; i < j; ++i) {
-      double sum = A[i * n + j];
-      for (int k = 0; k < i; ++k) sum -= A[i * n + k] * A[k * n + j];
-      A[i * n + j] = sum;
-    }
-    double big = 0.0;
-    for (int i = j; i < n; ++i) {
-      double sum = A[i * n + j];
-      for (int k = 0; k < j; ++k) sum -= A[i * n + k] * A[k * n + j];
-      A[i * n + j] = sum;
-      const double dum = vv[i] * fabs(sum);
-      if (dum >= big) { big = dum; imax = i; }
-    }
-    if (j != imax) {
-      for (int k = 0; k < n; ++k) {
-        const double t = A[imax * n + k];
-        A[imax * n + k] = A[j * n + k];
-        A[j * n + k] = t;
-      }
-      vv[imax] = vv[j];
-    }
-    index[j] = imax;
-    if (A[j * n + j] == 0.0) A[j * n + j] = 1.0e-20;
-    const double dum = 1.0 / A[j * n + j];
-    for (int i = j + 1; i < n; ++i) A[i * n + j] *= dum;
-  }
-  for (int pass = 0; pass < 2; ++pass) {
-    double* x = pass ? res : bvec;
-    if (pass)
-      for (int i = 0; i < n; ++i) {
-        res[i] = bc[i];
-        for (int j = 0; j < n; ++j) res[i] -= Ac[i * n + j] * bvec[j];
-      }
-    int ii = -1;
-    for (int i = 0; i < n; ++i) {
-      const int ip = index[i];
-      double sum = x[ip];
-      x[ip] = x[i];
-      if (ii >= 0) for (int j = ii; j < i; ++j) sum -= A[i * n + j] * x[j];
-      else if (sum != 0.0) ii = i;
-      x[i] = sum;
-    }
-    for (int i = n - 1; i >= 0; --i) {
-      double sum = x[i];
-      for (int j = i + 1; j < n; ++j) sum -= A[i * n + j] * x[j];
-      x[i] = sum / A[i * n + i];
-    }
-  }
-  for (int i = 0; i < n; ++i) bvec[i] += res[i];
-}
-
 template <typename R>
 __global__ void nlte_stateq_kernel(NlteArgs A) {
   const pyrh_nlte_batch& b = A.b;
@@ -994,7 +931,7 @@ __global__ void nlte_stateq_kernel(NlteArgs A) {
     }
     x[ie] = b.ntotal[doff + k];
     for (int j = 0; j < nl; ++j) M[ie * nl + j] = 1.0;
-    lu_solve(nl, M, x);
+    lu_solve<PYRH_NLTE_MAX_LEVELS>(nl, M, x);
     for (int i = 0; i < nl; ++i) b.n[(int64_t)i * b.total_depth + doff + k] = x[i];
   }
 }
@@ -1089,7 +1026,7 @@ __global__ void nlte_ng_kernel(NlteArgs A, int init) {
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) lu_solve(No, Ab, Ab + No * No);
+    if (threadIdx.x == 0) lu_solve<PYRH_NLTE_MAX_LEVELS>(No, Ab, Ab + No * No);
     __syncthreads();
     const int i0 = (count - 1) % np2;
     for (int e = threadIdx.x; e < N; e += blockDim.x) {

@@ -54,6 +54,9 @@ Fixtures (npz, float64):
                   potentials, abundances) as the reference parsed them,
                   LTEpops_elem() of every element and Solve_ne() for three
                   atmospheres, one with abundance overrides
+  chem            ChemicalEquilibrium() of the molecules of tests/molecules.input
+                  (their files' text kept) on three atmospheres: the neutral
+                  fractions it starts from and the densities it leaves
 
 stokes_ref comes from the reference as setup.py builds it on x86 (-DSIMDON,
 SSE reciprocal-estimate 4x4 inverse); stokes_ref_portable from the same
@@ -535,12 +538,47 @@ def make_ltepops(ref, wd):
           f"{os.path.getsize(path) / 1e3:.0f} kB")
 
 
+def make_chem(ref, wd):
+    """ChemicalEquilibrium() with the molecules of tests/molecules.input
+    (the reference's molecule files, their text kept here) on the C0
+    atmosphere and on two cooler ones (T - 1000 K and T - 2000 K above log
+    tau 0, at least 2200 K), each with its own hse() densities: the neutral
+    fractions it starts from, the molecule and H- densities and the model
+    atoms' totals it leaves."""
+    mol_list = [ln.split()[0] for ln in open(os.path.join(rr.REF_ROOT, "tests", "molecules.input"))
+                if ln.strip() and not ln.lstrip().startswith("#") and ".molecule" in ln]
+    texts = [open(os.path.join(rr.REF_ROOT, "rh", "Molecules", m)).read() for m in mol_list]
+    cases = []
+    for shift in (0.0, 1000.0, 2000.0):
+        logtau = wl.logtau_grid(71)
+        T = wl.base_temperature(logtau)
+        T = np.where(logtau < 0.0, np.maximum(T - shift, 2200.0), T)
+        w = rr.scratch_dir()
+        rr.write_inputs(w, None)
+        ne, nH = ref.hse(w, logtau, T)
+        atm = wl.atmosphere_rows(logtau, T, ne / 1e6, nH / 1e6)
+        outdir = os.path.join(w, "chem")
+        ref.dump_chem(w, atm, outdir)
+        cases.append(rr.read_chem_dump(outdir))
+        shutil.rmtree(w, ignore_errors=True)
+    out = {"molecule_files": np.array(mol_list), "molecule_text": np.array(texts),
+           "nuclei": cases[0]["nuclei"], "nuc_model": cases[0]["nuc_model"]}
+    for c in cases[1:]:
+        assert np.array_equal(c["nuclei"], out["nuclei"])
+    for k in ("T", "ne", "nHtot", "fn0", "nmol", "nHmin", "ntot_model"):
+        out[k] = np.stack([c[k] for c in cases])
+    path = os.path.join(HERE, "chem.npz")
+    np.savez_compressed(path, **out)
+    print(f"chem: {len(mol_list)} molecules, nuclei {out['nuclei']}, "
+          f"{os.path.getsize(path) / 1e3:.0f} kB")
+
+
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
           "lte_static": make_lte_static, "lte_broadening": make_lte_broadening,
           "nlte": make_nlte, "nlte_static": make_nlte_static, "kurucz": make_kurucz,
-          "background": make_background, "ltepops": make_ltepops}
+          "background": make_background, "ltepops": make_ltepops, "chem": make_chem}
 
 
 def main():
