@@ -355,6 +355,74 @@ def background_measure(natm, local, stream, steps, warmup):
     return out
 
 
+def setup_measure(natm, local, stream, steps, warmup):
+    """The per-depth set-up on the GPU at the batched synthesis' shape (natm
+    atmospheres x 71 depths, the three atmospheres of the chemistry fixture
+    repeated): the two lines' stage densities and ln U (pyrh_line_pops), the
+    electron density from scratch (pyrh_solve_ne) and the chemical
+    equilibrium of the twelve molecules (pyrh_chem_equil), CUDA events; each
+    against the reference's own LTEpops_elem / Solve_ne / ChemicalEquilibrium
+    output on the fixtures' atmospheres."""
+    import torch
+    from pyrh_gb300 import chem as CH
+    from pyrh_gb300 import ltepops as LP
+    g = lambda n: dict(np.load(os.path.join(HERE, "tests", "golden", n + ".npz")))
+    lp, ch, c0 = g("ltepops"), g("chem"), g("lte_c0")
+    meta = lp["el_meta"][0]
+    ns = meta[:, 0].astype(np.int32)
+    tab = LP.ElementTables(lp["Tpf"], meta[:, 2].copy(), meta[:, 1].astype(np.int32), ns,
+                           np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32),
+                           lp["el_pf"], lp["el_ionpot"])
+    dev = LP.DeviceTables(tab, device=f"cuda:{local}")
+    mols = [CH.read_molecule(str(t), tab.abundance_set) for t in ch["molecule_text"]]
+    npt = natm * 71
+    rep = -(-npt // ch["T"].size)
+    T, ne, nH = (torch.from_numpy(np.tile(ch[k].ravel(), rep)[:npt]).to(f"cuda:{local}")
+                 for k in ("T", "ne", "nHtot"))
+    elem = c0["line_const"][:, 1].astype(np.int32) - 1
+    stage = c0["line_const"][:, 2].astype(np.int32)
+    legs = {"line_pops": lambda: LP.line_pops(dev, T, ne, nH, elem, stage),
+            "solve_ne": lambda: LP.solve_ne(dev, T, nH),
+            "chem_equil": lambda: CH.chem_equil(dev, mols, T, ne, nH)}
+    out = {"workload": f"{natm} atmospheres x 71 depths ({npt} points); 2 Fe I lines; "
+                       "99 elements; 12 molecules (H, C, N, O nuclei, partition-function "
+                       "neutral fractions)"}
+    with torch.cuda.stream(stream):
+        for name, fn in legs.items():
+            for _ in range(warmup):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(steps):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / steps
+            out[name] = {"ms": ms, "value": npt / (ms / 1e3), "unit": "depth points/s"}
+    # errors against the reference on the fixtures
+    err = {}
+    r = LP.line_pops(dev, c0["T"], c0["ne"], c0["nHtot"], elem, stage).cpu().numpy()
+    err["line_pops_vs_reference"] = float(np.abs(r / c0["line_pops"] - 1).max())
+    e_ne, e_ch = 0.0, 0.0
+    for c in range(2):     # the ltepops fixture's atmospheres with the file's own abundances
+        v = LP.solve_ne(dev, lp["T"][c], lp["nHtot"][c]).cpu().numpy()
+        e_ne = max(e_ne, float(np.abs(v / lp["ne_solved"][c] - 1).max()))
+    for c in range(3):
+        fn0 = {int(e): ch["fn0"][c][i] for i, e in enumerate(ch["nuclei"]) if ch["nuc_model"][i]}
+        nm, nh, nn, _ = CH.chem_equil(dev, mols, ch["T"][c], ch["ne"][c], ch["nHtot"][c], fn0)
+        ref = ch["nmol"][c]
+        m = ref != 0
+        e_ch = max(e_ch, float(np.abs(nm.cpu().numpy()[m] / ref[m] - 1).max()),
+                   float(np.abs(nh.cpu().numpy() / ch["nHmin"][c] - 1).max()))
+    err["solve_ne_vs_reference"] = e_ne
+    err["chem_equil_vs_reference"] = e_ch
+    out["accuracy"] = err
+    out["error_metric"] = ("max relative error against the reference's LTEpops_elem / "
+                           "Solve_ne / ChemicalEquilibrium output (fixtures lte_c0, ltepops, chem)")
+    return out
+
+
 def nlte_measure(natm, local, nsample=32):
     """Batched uneven NLTE (the six-level atom, five rays, Ng order 2 every 5
     iterations after 5): natm atmospheres with 50..150 depths and 700..1100
@@ -645,6 +713,10 @@ def main():
     if rank == 0 and not args.skip_background:
         extra["background"] = background_measure(args.natm, local, stream,
                                                  max(2, min(args.steps, 5)), args.warmup)
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.skip_background:
+        extra["setup"] = setup_measure(args.natm, local, stream, max(2, min(args.steps, 5)),
+                                       args.warmup)
         torch.cuda.empty_cache()
 
     cpu = None

@@ -147,29 +147,44 @@ __global__ void line_pops_kernel(DevTables t, int64_t npoint, const double* T, c
   }
 }
 
+// The factor of getfjk's stage recursion that does not depend on n_e,
+// exp(ln U_{j+1} - ln U_j - chi_j / kT), for every element and stage j >= 1
+// at one point: row stage_off[e] + j of E.  Solve_ne's iterations reuse it.
+constexpr int kMaxRows = PYRH_NELEM * PYRH_PF_MAX_STAGES;
+
+__device__ __forceinline__ void stage_factors(const DevTables& t, const PfAt& at, double T,
+                                              double* E) {
+  for (int e = 0; e < t.nelem; ++e) {
+    const int ns = t.nstage[e], off = t.stage_off[e];
+    const double* lnpf = t.lnpf + (int64_t)off * t.npf;
+    const double* ion = t.ionpot + off;
+    double Uk = pf_eval(lnpf, at);
+    for (int j = 1; j < ns; ++j) {
+      const double Ukp1 = pf_eval(lnpf + (int64_t)j * t.npf, at);
+      E[off + j] = exp(Ukp1 - Uk - ion[j - 1] / (kK * T));
+      Uk = Ukp1;
+    }
+  }
+}
+
 // getfjk (LTE branch) for element e at n_e = ne: the stage fractions and
 // their n_e derivatives, accumulated straight into Solve_ne's error and sum.
-__device__ __forceinline__ void add_element(const DevTables& t, int e, const PfAt& at, double T,
+__device__ __forceinline__ void add_element(const DevTables& t, int e, const double* E,
                                             double ne, double CT_ne_ref, double& error,
                                             double& sum, double PhiHmin) {
-  const int ns = t.nstage[e];
-  const double* lnpf = t.lnpf + (int64_t)t.stage_off[e] * t.npf;
-  const double* ion = t.ionpot + t.stage_off[e];
+  const int ns = t.nstage[e], off = t.stage_off[e];
   const double CT_ne = CT_ne_ref / ne;
   double f[PYRH_PF_MAX_STAGES], df[PYRH_PF_MAX_STAGES];
   double sum1 = 1.0, sum2 = 0.0;
   f[0] = 1.0;
   df[0] = 0.0;
-  double Uk = pf_eval(lnpf, at);
 #pragma unroll
   for (int j = 1; j < PYRH_PF_MAX_STAGES; ++j) {
     if (j < ns) {
-      const double Ukp1 = pf_eval(lnpf + (int64_t)j * t.npf, at);
-      f[j] = f[j - 1] * CT_ne * exp(Ukp1 - Uk - ion[j - 1] / (kK * T));
+      f[j] = f[j - 1] * CT_ne * E[off + j];
       df[j] = -j * f[j] / ne;
       sum1 += f[j];
       sum2 += df[j];
-      Uk = Ukp1;
     }
   }
 #pragma unroll
@@ -212,12 +227,14 @@ __global__ void solve_ne_kernel(DevTables t, int64_t npoint, const double* T,
   }
   const double CT_ne_ref = 2.0 * pow(kC1 / Tk, -1.5);
   const double PhiHmin = 0.25 * pow(kC1 / Tk, 1.5) * exp(0.754 * kEV / (kK * Tk));
+  double E[kMaxRows];
+  stage_factors(t, at, Tk, E);
   double ne_new = ne_old, dne = 0.0;
   int niter = 0;
   while (niter < kMaxElectronIter) {
     double error = ne_old / nH;
     double sum = 0.0;
-    for (int e = 0; e < t.nelem; ++e) add_element(t, e, at, Tk, ne_old, CT_ne_ref, error, sum, PhiHmin);
+    for (int e = 0; e < t.nelem; ++e) add_element(t, e, E, ne_old, CT_ne_ref, error, sum, PhiHmin);
     ne_new = ne_old - nH * error / (1.0 - nH * sum);
     dne = fabs((ne_new - ne_old) / ne_old);
     ne_old = ne_new;
