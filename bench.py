@@ -417,10 +417,91 @@ def setup_measure(natm, local, stream, steps, warmup):
                    float(np.abs(nh.cpu().numpy() / ch["nHmin"][c] - 1).max()))
     err["solve_ne_vs_reference"] = e_ne
     err["chem_equil_vs_reference"] = e_ch
+    out["hse"], err["hse_vs_reference"] = hse_measure(natm, local, tab, lp, ch)
     out["accuracy"] = err
     out["error_metric"] = ("max relative error against the reference's LTEpops_elem / "
-                           "Solve_ne / ChemicalEquilibrium output (fixtures lte_c0, ltepops, chem)")
+                           "Solve_ne / ChemicalEquilibrium / hse output (fixtures lte_c0, "
+                           "ltepops, chem, hse)")
     return out
+
+
+def hse_measure(natm, local, tab, lp, ch):
+    """Hydrostatic equilibrium (pyrh_hse) of natm atmospheres x 71 layers on
+    log tau500 (the hse fixture's first two atmospheres alternating), one
+    timed call after one untimed, CUDA events; the oracle's time for one
+    atmosphere on one host core beside it; the largest relative error of ne,
+    nHtot, rho and pg against the reference's hse() on the fixture's five
+    atmospheres."""
+    import torch
+    from pyrh_gb300 import chem as CH
+    from pyrh_gb300 import grid as G
+    from pyrh_gb300 import hse as H
+    from pyrh_gb300 import ltepops as LP
+    g = lambda n: dict(np.load(os.path.join(HERE, "tests", "golden", n + ".npz")))
+    h, bg = g("hse"), g("background")
+    atoms = [G.read_atom(str(t)) for t in h["atom_text"]]
+    dev = f"cuda:{local}"
+
+    def model(case):
+        ti = 2 if case == int(h["ab_case"]) else 0
+        meta = lp["el_meta"][ti]
+        ns = meta[:, 0].astype(np.int32)
+        t = LP.ElementTables(lp["Tpf"], meta[:, 2].copy(), meta[:, 1].astype(np.int32), ns,
+                             np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32),
+                             lp["el_pf"], lp["el_ionpot"])
+        mols = [CH.read_molecule(str(x), t.abundance_set) for x in ch["molecule_text"]]
+        fudge = (h["fudge_wave"], h["fudge_value"]) if case == int(h["fudge_case"]) else None
+        return H.HseModel.build(t, atoms, mols, float(bg["misc"][0]), fudge, device=dev)
+
+    m0 = model(0)
+    sel = np.arange(natm) % 2
+    scale, T, pg_top = h["scale"][sel], h["T"][sel], h["pg_top"][sel]
+    H.hse_batch(m0, 0, scale, T, pg_top)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s = torch.cuda.current_stream()
+    e0.record(s)
+    H.hse_batch(m0, 0, scale, T, pg_top)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    from pyrh_gb300 import _lib as L
+    launches = int(L.lib().pyrh_last_launch_count())
+    err = 0.0
+    for c in range(len(h["T"])):
+        m = m0 if c in (0, 1, 2) else model(c)
+        got = H.hse_batch(m, int(h["atm_scale"][c]), h["scale"][c][None], h["T"][c][None],
+                          float(h["pg_top"][c]))
+        for x, k in zip(got, ("ne", "nHtot", "rho", "pg")):
+            err = max(err, float(np.abs(x[0] / h[k][c] - 1).max()))
+    # the oracle (numpy restatement, one core) on the first atmosphere
+    from oracle import chem as OC
+    from oracle import hse as OH
+    otab = {"Tpf": lp["Tpf"], "el_meta": lp["el_meta"][0], "el_pf": lp["el_pf"],
+            "el_ionpot": lp["el_ionpot"]}
+    elems = [H.element_index(a) for a in atoms]
+    meta = bg["atoms_meta"]
+    lo = np.concatenate([[0], np.cumsum(meta[:, 0])])
+    co = np.concatenate([[0], np.cumsum(meta[:, 1])])
+    li = np.concatenate([[0], np.cumsum(meta[:, 2])])
+    oatoms = [dict(elem=elems[m], E=bg["atoms_lev"][lo[m]:lo[m + 1], 0],
+                   g=bg["atoms_lev"][lo[m]:lo[m + 1], 1],
+                   stage=bg["atoms_lev"][lo[m]:lo[m + 1], 2].astype(int),
+                   cont=bg["atoms_cont"][co[m]:co[m + 1]], lines=bg["atoms_line"][li[m]:li[m + 1]],
+                   tab=bg["atoms_tab"]) for m in range(len(meta))]
+    omols = [OC.read_molecule(str(x), lp["el_meta"][0][:, 1].astype(np.int32))
+             for x in ch["molecule_text"]]
+    t0 = time.perf_counter()
+    OH.hse(otab, oatoms, omols, [x["id"] for x in omols], 0, h["scale"][0][None],
+           h["T"][0][None], float(h["pg_top"][0]))
+    cpu_s = time.perf_counter() - t0
+    return {"workload": f"{natm} atmospheres x 71 layers, log tau500, 11 passive atoms, "
+                        "12 molecules, 500 nm background", "ms": ms,
+            "value": natm / (ms / 1e3), "unit": "atmospheres/s",
+            "launches": launches,
+            "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "atmospheres/s", "cores": 1,
+                             "kind": "port", "sample": "one atmosphere of 71 layers"}}, err
+
 
 
 def nlte_measure(natm, local, nsample=32):

@@ -738,6 +738,14 @@ typedef struct {
 pyrh_status pyrh_abundance_parse(const char *text, int32_t nabun, const int32_t *ab_id,
                                  const double *ab_val, double metallicity, double *abund,
                                  int32_t *abundance_set);
+/* atmos.totalAbund and atmos.wght_per_H (abundance.c:168-221): the sums, in
+   element order over the elements with an abundance, of the abundances and
+   of abundance x atomic weight [amu] (the reference's weight table). */
+pyrh_status pyrh_abundance_totals(const double *abund, const int32_t *abundance_set,
+                                  double *total_abund, double *wght_per_H);
+/* Element index (atomic number - 1) of a model atom's ID as readAtom matches
+   it (readatom.c:109-126); -1 if no element matches. */
+int32_t pyrh_element_index(const char *id);
 /* The partition-function file (XDR: Npf, Tpf[Npf], then per element its
    atomic number, Nstage, U[Nstage][Npf] and ionisation potentials in cm^-1;
    abundance.c:151-220).  With lnpf == NULL only *npf and *nrows (sum of
@@ -766,8 +774,10 @@ pyrh_status pyrh_line_pops(const pyrh_elem_tables *tables, int64_t npoint, const
                            const int32_t *elem, const int32_t *stage, double *line_pops,
                            void *stream);
 /* Electron density by Solve_ne's Newton iteration (at most 10 steps, to a
-   relative change of 1e-2), from hydrogen's ionisation alone when
-   fromscratch, else from the values in ne; ne is overwritten.  niter
+   relative change of 1e-2), from the values in ne (fromscratch 0), from
+   hydrogen's ionisation alone with its partition function (1, Solve_ne) or
+   with U = 1 (2, get_ne of rh/rhf1d/pyrh_background.c:459-540, which the
+   hydrostatic equilibrium calls); ne is overwritten.  niter
    (device [npoint], or NULL) receives the steps taken, -1 where the
    iteration did not reach its limit (the reference warns and goes on). */
 pyrh_status pyrh_solve_ne(const pyrh_elem_tables *tables, int64_t npoint, const double *T,
@@ -830,6 +840,62 @@ pyrh_status pyrh_chem_equil(const pyrh_elem_tables *tables, const pyrh_molecule 
                             int32_t nmol, int64_t npoint, const double *T, const double *ne,
                             const double *nHtot, const double *const *fn0_model, double *nmol_out,
                             double *nHmin, double *nnuc, int32_t *niter, void *stream);
+
+/* -------------------------------------------------- hydrostatic equilibrium --
+ * pyrh's hse() (rh/rhf1d/pyrh_hse.c:67-399, pyrh.pyx:427-487) for a batch of
+ * atmospheres with the same number of depth points, all on the device.  Layer
+ * by layer from the top, each atmosphere iterates until its hydrogen density
+ * changes by at most eta_limit (relative) or nmax_iter passes are done; a
+ * pass takes the electron density (get_ne: Solve_ne from hydrogen's
+ * ionisation with U = 1), the model atoms' LTE populations (LTEpops without
+ * Debye lowering, rh/ltepops.c:33-109), chemical equilibrium with the
+ * model atoms' neutral fractions and their populations scaled by the
+ * molecules' share (chemequil.c:213-345), the continuum opacity at 500 nm
+ * (pyrh_Background, rh/rhf1d/pyrh_background.c:144-457: the background
+ * without the metals' bound-free continua, scattering included), and the
+ * gas pressure by the trapezoid in log tau500 (or in height) and from it the
+ * hydrogen density.  Atoms, molecules and the background model are what the
+ * run's atoms.input / molecules.input name, all passive (LTE). */
+#define PYRH_HSE_MAX_ATOMS 24
+
+typedef struct {
+  int32_t natom;
+  int32_t elem[PYRH_HSE_MAX_ATOMS];         /* element index of each model atom */
+  int32_t lev_off[PYRH_HSE_MAX_ATOMS + 1];  /* its levels are rows lev_off[m] .. lev_off[m+1]-1
+                                               of the background model's populations */
+  const double *E, *g;                      /* device [lev_off[natom]]: J, statistical weight */
+  const int32_t *stage;                     /* device [lev_off[natom]] */
+} pyrh_hse_atoms;
+
+typedef struct {
+  double gravity;        /* m s^-2 (MULTIatmos: 10^4.4 cm s^-2) */
+  double total_abund;    /* atmos.totalAbund (pyrh_abundance_totals) */
+  double wght_per_H;     /* atmos.wght_per_H, amu */
+  int32_t scale;         /* 0: log10 tau500, 2: height in km (the reference's
+                            column-mass branch leaves its pressure step unset) */
+  int32_t nmax_iter;     /* NMAX_HSE_ITER, 50 */
+  double eta_limit;      /* 1e-2 */
+} pyrh_hse_config;
+
+typedef struct {
+  int32_t natm, ndep;    /* natm <= 65535 per call */
+  /* device arrays [ndep][natm], depth point k of atmosphere a at k * natm + a */
+  const double *scale;   /* log10 tau500 or height [km] */
+  const double *T;       /* K */
+  const double *pg_top;  /* device [natm]: gas pressure of the top layer, Pa */
+  double *ne, *nHtot;    /* out, m^-3 */
+  double *rho, *pg;      /* out, kg m^-3 and Pa */
+  double *opacity;       /* out or NULL: the 500 nm opacity of each layer, m^-1 */
+  int32_t *niter;        /* out or NULL: passes per layer (-1: nmax_iter reached first) */
+} pyrh_hse_batch;
+
+/* bg: a model prepared by pyrh_background_prepare whose population rows are
+   the atoms' levels (npop == atoms->lev_off[natom]; FP64); mol: as for
+   pyrh_chem_equil, with H2 / OH / CH (when present) giving the background's
+   molecule densities. */
+pyrh_status pyrh_hse(const pyrh_elem_tables *tables, const pyrh_molecule *mol, int32_t nmol,
+                     const pyrh_bg_model *bg, const pyrh_hse_atoms *atoms,
+                     const pyrh_hse_config *cfg, const pyrh_hse_batch *batch, void *stream);
 
 /* Number of kernel launches the last pyrh_lte_stokes / pyrh_nlte_* call issued. */
 int32_t pyrh_last_launch_count(void);

@@ -215,11 +215,13 @@ def rayleigh(lam, atom, vmicro_char):
     return sigma_e * fomega
 
 
-def background(fx: dict, a: int = 0, add_scatter: bool = False, fudge=None):
+def background(fx: dict, a: int = 0, add_scatter: bool = False, fudge=None, metals=True):
     """(chi, eta, sca) [nspect, ndep] of atmosphere a, and the per-process
     contributions [13, 2, nspect, ndep] in the order of NAMES (opacity, then
     emissivity or scattering opacity).  fudge = (lambda [N], [3, N]) applies
-    the reference's H-minus, scattering and metal fudge factors."""
+    the reference's H-minus, scattering and metal fudge factors; metals
+    False leaves Metal_bf out (the hydrostatic equilibrium's background,
+    rh/rhf1d/pyrh_background.c:144-457)."""
     lam_all = fx["lambda"]
     T, ne = fx["T"][a], fx["ne"][a]
     nHmin, nH2, nOH, nCH = fx["nHmin"][a], fx["nH2"][a], fx["nOH"][a], fx["nCH"][a]
@@ -345,7 +347,7 @@ def background(fx: dict, a: int = 0, add_scatter: bool = False, fudge=None):
                                    frac_index(th, THETA0 / T[k]), li)
                     c[11, 0, k] = (nH2[k] * 1.0E-29) * (ne[k] * KBOLTZMANN * T[k]) * kap
         # metals (every atom after the first that is not active)
-        for m in range(1, at.n_atoms):
+        for m in range(1, at.n_atoms if metals else 1):
             A = at.atoms[m]
             if A["active"]:
                 continue

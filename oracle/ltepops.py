@@ -94,10 +94,11 @@ def _fjk(tab, e, ne, T):
     return f, df
 
 
-def solve_ne(tab, T, nHtot, ne0=None):
+def solve_ne(tab, T, nHtot, ne0=None, unit_hydrogen_pf=False):
     """Solve_ne at every point: from hydrogen's ionisation (ne0 None, H in
     LTE) or from ne0.  Returns (ne, steps) with steps -1 where it did not
-    reach its limit."""
+    reach its limit.  unit_hydrogen_pf starts from U_H = 1 instead, as get_ne
+    does (rh/rhf1d/pyrh_background.c:485-492)."""
     T = np.asarray(T, np.float64)
     nHtot = np.asarray(nHtot, np.float64)
     nelem = tab["el_meta"].shape[0]
@@ -106,7 +107,7 @@ def solve_ne(tab, T, nHtot, ne0=None):
     for k in range(len(T)):
         if ne0 is None:
             off, _ = _rows(tab, 0)
-            Uk = linear(tab["Tpf"], tab["el_pf"][off], T[k])[0]
+            Uk = 0.0 if unit_hydrogen_pf else linear(tab["Tpf"], tab["el_pf"][off], T[k])[0]
             PhiH = 0.5 * (C1 / T[k]) ** 1.5 * np.exp(Uk + tab["el_ionpot"][off] / (KBOLTZMANN * T[k]))
             ne_old = (np.sqrt(1.0 + 4.0 * nHtot[k] * PhiH) - 1.0) / (2.0 * PhiH)
         else:

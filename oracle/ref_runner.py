@@ -149,6 +149,33 @@ def _hse_job(args):
     return ne, nH
 
 
+def _hse_full_job(args):
+    """hse() with every argument of pyrh.hse (pyrh.pyx:427-487): the depth
+    scale type, pg_top, fudge factors and abundance overrides; returns ne,
+    nHtot, rho, pg (SI)."""
+    workdir, pyrh_path, atm_scale, scale, T, pg_top, fudge_wave, fudge_value, ab_id, ab_val = args
+    lib = _lib(pyrh_path)
+    n = len(scale)
+    scale = np.ascontiguousarray(scale, dtype=np.float64)
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    ne, nH, rho, pg = (np.zeros(n) for _ in range(4))
+    pg[0] = pg_top
+    nf, fw, fv = 0, None, None
+    if fudge_wave is not None:
+        fudge_wave = np.ascontiguousarray(fudge_wave, dtype=np.float64)
+        fudge_value = np.ascontiguousarray(fudge_value, dtype=np.float64)
+        nf, fw, fv = len(fudge_wave), _p(fudge_wave), _p(fudge_value)
+    na, ai, av = 0, None, None
+    if ab_id is not None:
+        ab_id = np.ascontiguousarray(ab_id, dtype=np.int32)
+        ab_val = np.ascontiguousarray(ab_val, dtype=np.float64)
+        na, ai, av = len(ab_id), ab_id.ctypes.data_as(C.POINTER(C.c_int)), _p(ab_val)
+    lib.hse.restype = None
+    lib.hse(workdir.encode(), n, _p(scale), _p(T), _p(ne), _p(nH), _p(rho), _p(pg),
+            int(atm_scale), nf, fw, fv, na, ai, av)
+    return ne, nH, rho, pg
+
+
 def _synth_job(args):
     workdir, pyrh_path, mu, atm, wave = args
     lib = _lib(pyrh_path)
@@ -324,6 +351,11 @@ class Reference:
 
     def hse(self, workdir, logtau, T):
         return self._run(_hse_job, (workdir, self.pyrh_path, logtau, T))
+
+    def hse_full(self, workdir, atm_scale, scale, T, pg_top=0.1, fudge_wave=None,
+                 fudge_value=None, ab_id=None, ab_val=None):
+        return self._run(_hse_full_job, (workdir, self.pyrh_path, atm_scale, scale, T, pg_top,
+                                         fudge_wave, fudge_value, ab_id, ab_val))
 
     def synth(self, workdir, mu, atm, wave):
         return self._run(_synth_job, (workdir, self.pyrh_path, mu, atm, wave))

@@ -110,7 +110,7 @@ class Model:
     molecules: tuple              # (H2, OH, CH) present
 
 
-def model_from_setup(s: dict, lte: bool = True) -> Model:
+def model_from_setup(s: dict, lte: bool = True, metals: bool = True) -> Model:
     """The model of a set-up (see the module docstring): continua of
     hydrogen (hydrogen.c:176-200) and of the passive metals (metal.c:
     103-140, every atom after the first), Rayleigh lines of hydrogen and
@@ -118,7 +118,9 @@ def model_from_setup(s: dict, lte: bool = True) -> Model:
     atoms is row l of nstar; with lte=False the populations n come first
     (row l) and nstar follows (row nlev + l).  With lte the populations are
     the LTE ones (the passive atoms of LTE_POPULATIONS, HYDROGEN_LTE), as
-    Metal_bf and Hydrogen_bf then read them (metal.c:110, the same array)."""
+    Metal_bf and Hydrogen_bf then read them (metal.c:110, the same array).
+    metals=False leaves the metals' continua out, as the hydrostatic
+    equilibrium's background does (rh/rhf1d/pyrh_background.c:144-457)."""
     meta = np.asarray(s["atoms_meta"])
     lev = np.asarray(s["atoms_lev"])
     cont = np.asarray(s["atoms_cont"])
@@ -165,7 +167,7 @@ def model_from_setup(s: dict, lte: bool = True) -> Model:
     for r in cont[co[h]:co[h + 1]]:
         add(h, r, True)
     ncont_h = len(out)
-    for m in range(1, len(meta)):
+    for m in range(1, len(meta) if metals else 1):
         if meta[m, 3]:
             continue
         for r in cont[co[m]:co[m + 1]]:

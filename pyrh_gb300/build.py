@@ -16,7 +16,7 @@ LIB = os.path.join(HERE, "libpyrh_gb300.so")
 UNITS = ["capi.cu", "lte_stokes.cu", "lte_rf.cu"] + \
     [f"lte_rf_fp{p}_{m}.cu" for p in ("32", "64") for m in ("rf", "chi2", "vjp")] + \
     ["nlte.cu", "nlte_capi.cu", "nlte_setup.cu", "setup_host.cpp", "background.cu",
-     "ltepops.cu", "elements_host.cpp", "chem.cu"]
+     "ltepops.cu", "elements_host.cpp", "chem.cu", "hse.cu"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

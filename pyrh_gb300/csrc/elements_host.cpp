@@ -46,6 +46,20 @@ const char* const kElementID[PYRH_NELEM] = {
     "OS", "IR", "PT", "AU", "HG", "TL", "PB", "BI", "PO", "AT", "RN", "FR", "RA", "AC", "TH",
     "PA", "U ", "NP", "PU", "AM", "CM", "BK", "CF", "ES"};
 
+// Atomic weights [amu] of the same 99 elements as the reference tabulates
+// them (rh/atomweights.h); the mean weight per hydrogen atom sums them.
+const double kElementWeight[PYRH_NELEM] = {
+    1.008,   4.003,   6.939,   9.013,   10.810,  12.010,  14.010,  16.000,  19.000,  20.180,
+    22.990,  24.310,  26.980,  28.090,  30.980,  32.070,  35.450,  39.950,  39.100,  40.080,
+    44.960,  47.900,  50.940,  52.000,  54.940,  55.850,  58.940,  58.710,  63.550,  65.370,
+    69.720,  72.600,  74.920,  78.960,  79.910,  83.800,  85.480,  87.630,  88.910,  91.220,
+    92.910,  95.950,  99.000,  101.100, 102.900, 106.400, 107.900, 112.400, 114.800, 118.700,
+    121.800, 127.600, 126.900, 131.300, 132.900, 137.400, 138.900, 140.100, 140.900, 144.300,
+    147.000, 150.400, 152.000, 157.300, 158.900, 162.500, 164.900, 167.300, 168.900, 173.000,
+    175.000, 178.500, 181.000, 183.900, 186.300, 190.200, 192.200, 195.100, 197.000, 200.600,
+    204.400, 207.200, 209.000, 210.000, 211.000, 222.000, 223.000, 226.100, 227.100, 232.000,
+    231.000, 238.000, 237.000, 244.000, 243.000, 247.000, 247.000, 251.000, 254.000};
+
 pyrh_status fail(pyrh_status s, const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -130,6 +144,36 @@ extern "C" pyrh_status pyrh_abundance_parse(const char* text, int32_t nabun,
     if (metal != 1.0 && n != 0) abund[n] *= metal;
   }
   return PYRH_OK;
+}
+
+extern "C" pyrh_status pyrh_abundance_totals(const double* abund, const int32_t* abundance_set,
+                                             double* total_abund, double* wght_per_H) {
+  if (!abund || !abundance_set || !total_abund || !wght_per_H)
+    return fail(PYRH_ERR_ARG, "abundance totals: NULL argument");
+  // rh/abundance.c:168-221: sums in element order over the elements with an
+  // abundance
+  double total = 0.0, weight = 0.0;
+  for (int n = 0; n < PYRH_NELEM; ++n) {
+    if (!abundance_set[n]) continue;
+    total += abund[n];
+    weight += abund[n] * kElementWeight[n];
+  }
+  *total_abund = total;
+  *wght_per_H = weight;
+  return PYRH_OK;
+}
+
+extern "C" int32_t pyrh_element_index(const char* id) {
+  // readAtom (rh/readatom.c:109-126): the first two characters, upper case,
+  // one-letter symbols padded with a blank, matched as a substring of the
+  // table's symbols
+  if (!id || !id[0]) return -1;
+  char a[3] = {(char)toupper((unsigned char)id[0]),
+               id[1] ? (char)toupper((unsigned char)id[1]) : ' ', 0};
+  if (a[1] == 0) a[1] = ' ';
+  for (int n = 0; n < PYRH_NELEM; ++n)
+    if (strstr(kElementID[n], a)) return n;
+  return -1;
 }
 
 extern "C" pyrh_status pyrh_pf_parse(const unsigned char* bytes, size_t nbytes,

@@ -218,8 +218,12 @@ __global__ void solve_ne_kernel(DevTables t, int64_t npoint, const double* T,
   const PfAt at = pf_at(t.Tpf, t.npf, Tk);
   double ne_old;
   if (fromscratch) {
-    // ionisation of hydrogen alone (H in LTE)
-    const double Uk = pf_eval(t.lnpf + (int64_t)t.stage_off[0] * t.npf, at);
+    // ionisation of hydrogen alone (H in LTE), with hydrogen's neutral
+    // partition function (Solve_ne, solvene.c:80-86) or with U = 1 (get_ne,
+    // rh/rhf1d/pyrh_background.c:485-492, the start of the hydrostatic
+    // equilibrium's electron densities)
+    const double Uk =
+        fromscratch == 2 ? 0.0 : pf_eval(t.lnpf + (int64_t)t.stage_off[0] * t.npf, at);
     const double PhiH = 0.5 * pow(kC1 / Tk, 1.5) * exp(Uk + t.ionpot[t.stage_off[0]] / (kK * Tk));
     ne_old = (sqrt(1.0 + 4.0 * nH * PhiH) - 1.0) / (2.0 * PhiH);
   } else {
@@ -379,12 +383,13 @@ extern "C" pyrh_status pyrh_solve_ne(const pyrh_elem_tables* tables, int64_t npo
   if (npoint < 0) return fail(PYRH_ERR_ARG, "solve ne: npoint < 0");
   if (npoint == 0) return PYRH_OK;
   if (!T || !nHtot || !ne) return fail(PYRH_ERR_ARG, "solve ne: NULL array");
+  if (fromscratch < 0 || fromscratch > 2) return fail(PYRH_ERR_ARG, "solve ne: fromscratch not 0, 1 or 2");
   cudaStream_t st = (cudaStream_t)stream;
   DevTables d;
   std::vector<int32_t> ns, off;
   pyrh_status s = load_tables(tables, st, d, ns, off);
   if (s != PYRH_OK) return s;
   solve_ne_kernel<<<grid_for(npoint), kThreads, 0, st>>>(d, npoint, T, nHtot, ne,
-                                                          fromscratch ? 1 : 0, niter);
+                                                          fromscratch, niter);
   return finish(cudaGetLastError(), 1);
 }

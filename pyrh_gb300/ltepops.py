@@ -207,8 +207,11 @@ def line_pops(dev: DeviceTables, T, ne, nHtot, elem, stage):
     return out
 
 
-def solve_ne(dev: DeviceTables, T, nHtot, ne_start=None, return_iterations=False):
-    """Solve_ne: from hydrogen's ionisation (ne_start None) or from ne_start."""
+def solve_ne(dev: DeviceTables, T, nHtot, ne_start=None, return_iterations=False,
+             unit_hydrogen_pf=False):
+    """Solve_ne: from hydrogen's ionisation (ne_start None) or from ne_start.
+    With unit_hydrogen_pf the start takes hydrogen's partition function as 1,
+    as the hydrostatic equilibrium's get_ne does."""
     import torch
     T, nHtot = _dev(T, dev.device), _dev(nHtot, dev.device)
     if ne_start is None:
@@ -217,7 +220,8 @@ def solve_ne(dev: DeviceTables, T, nHtot, ne_start=None, return_iterations=False
         ne = _dev(ne_start, dev.device).clone()
     it = torch.zeros(T.numel(), dtype=torch.int32, device=dev.device)
     L.check(_lib().pyrh_solve_ne(C.byref(dev.struct), T.numel(), T.data_ptr(), nHtot.data_ptr(),
-                                 ne.data_ptr(), int(ne_start is None), it.data_ptr(),
+                                 ne.data_ptr(), 0 if ne_start is not None else
+                                 (2 if unit_hydrogen_pf else 1), it.data_ptr(),
                                  _stream()))
     return (ne, it) if return_iterations else ne
 

@@ -111,3 +111,39 @@ def delo_wavelengths(fx) -> np.ndarray:
     for l0 in fx["line_const"][:, 0]:
         win |= np.abs(lam - l0) <= lam * 20 * fx["vmicro_char"] / 2.99792458e8
     return np.nonzero(win)[0]
+
+
+# elements of the passive atoms the hse fixture's run reads (H_6, He, C, N,
+# O, S, Fe, Si, Al, Na, Mg), as readAtom matches their IDs
+HSE_ATOM_ELEMENTS = [0, 1, 5, 6, 7, 15, 25, 13, 12, 10, 11]
+
+
+def hse_oracle_inputs(golden, case: int):
+    """(tab, atoms, mols, ids) for oracle.hse: the element tables the case
+    reads (the ltepops fixture's; its third case carries the same abundance
+    overrides), the atoms as the reference parsed them (background fixture),
+    the molecules of the chem fixture."""
+    from oracle import chem as OC
+    lp, bg, ch, h = golden("ltepops"), golden("background"), golden("chem"), golden("hse")
+    ti = 2 if case == int(h["ab_case"]) else 0
+    tab = {"Tpf": lp["Tpf"], "el_meta": lp["el_meta"][ti], "el_pf": lp["el_pf"],
+           "el_ionpot": lp["el_ionpot"]}
+    meta = bg["atoms_meta"]
+    lo, co, li = (np.concatenate([[0], np.cumsum(meta[:, c])]) for c in (0, 1, 2))
+    atoms = []
+    for m in range(len(meta)):
+        lev = bg["atoms_lev"][lo[m]:lo[m + 1]]
+        atoms.append(dict(elem=HSE_ATOM_ELEMENTS[m], E=lev[:, 0], g=lev[:, 1],
+                          stage=lev[:, 2].astype(int), cont=bg["atoms_cont"][co[m]:co[m + 1]],
+                          lines=bg["atoms_line"][li[m]:li[m + 1]], tab=bg["atoms_tab"]))
+    aset = lp["el_meta"][ti][:, 1].astype(np.int32)
+    mols = [OC.read_molecule(str(t), aset) for t in ch["molecule_text"]]
+    ids = [m["id"] for m in mols]
+    return tab, atoms, mols, ids
+
+
+def hse_fudge(golden, case: int):
+    h = golden("hse")
+    if case != int(h["fudge_case"]):
+        return None
+    return h["fudge_wave"], h["fudge_value"]

@@ -57,6 +57,10 @@ Fixtures (npz, float64):
   chem            ChemicalEquilibrium() of the molecules of tests/molecules.input
                   (their files' text kept) on three atmospheres: the neutral
                   fractions it starts from and the densities it leaves
+  hse             pyrh.hse() (ne, nHtot, rho, pg) on five atmospheres: C0 on
+                  its log tau500 scale, a cooler one with another top
+                  pressure, a height scale, abundance overrides, and opacity
+                  fudge factors; the text of the model atoms it reads
 
 stokes_ref comes from the reference as setup.py builds it on x86 (-DSIMDON,
 SSE reciprocal-estimate 4x4 inverse); stokes_ref_portable from the same
@@ -573,12 +577,56 @@ def make_chem(ref, wd):
           f"{os.path.getsize(path) / 1e3:.0f} kB")
 
 
+def make_hse(ref, wd):
+    """hse() with the run's passive atoms and molecules, cases: C0 (log
+    tau500, pg_top 0.1 Pa); T - 1500 K above log tau 0 (at least 2600 K),
+    pg_top 0.3 Pa; C0's temperatures on heights from 2000 to -100 km; C0 with
+    the abundance overrides of the ltepops fixture (records 1 and 26); C0
+    with H-minus and scattering fudge factors.  Keeps the atom files' text
+    (the background fixture keeps the arrays the reference made of them)."""
+    logtau = wl.logtau_grid(71)
+    T0 = wl.base_temperature(logtau)
+    Tc = np.where(logtau < 0.0, np.maximum(T0 - 1500.0, 2600.0), T0)
+    height = np.linspace(2000.0, -100.0, 71)
+    fw = np.array([300.0, 450.0, 700.0])
+    fv = np.array([[1.30, 1.20, 1.10], [1.05, 1.10, 1.00], [1.0, 1.0, 1.0]])
+    cases = [dict(atm_scale=0, scale=logtau, T=T0, pg_top=0.1),
+             dict(atm_scale=0, scale=logtau, T=Tc, pg_top=0.3),
+             dict(atm_scale=2, scale=height, T=T0, pg_top=0.1),
+             dict(atm_scale=0, scale=logtau, T=T0, pg_top=0.1, ab_id=[1, 26], ab_val=[12.0, 7.10]),
+             dict(atm_scale=0, scale=logtau, T=T0, pg_top=0.1, fudge_wave=fw, fudge_value=fv)]
+    out = {k: [] for k in ("atm_scale", "scale", "T", "pg_top", "ne", "nHtot", "rho", "pg")}
+    for c in cases:
+        w = rr.scratch_dir()
+        rr.write_inputs(w, None)
+        ne, nH, rho, pg = ref.hse_full(w, c["atm_scale"], c["scale"], c["T"], c["pg_top"],
+                                       c.get("fudge_wave"), c.get("fudge_value"),
+                                       c.get("ab_id"), c.get("ab_val"))
+        shutil.rmtree(w, ignore_errors=True)
+        for k, v in (("atm_scale", c["atm_scale"]), ("scale", c["scale"]), ("T", c["T"]),
+                     ("pg_top", c["pg_top"]), ("ne", ne), ("nHtot", nH), ("rho", rho),
+                     ("pg", pg)):
+            out[k].append(v)
+    out = {k: np.array(v) for k, v in out.items()}
+    out["ab_case"] = np.array(3)
+    out["ab_id"], out["ab_val"] = np.array([1, 26], np.int32), np.array([12.0, 7.10])
+    out["fudge_case"] = np.array(4)
+    out["fudge_wave"], out["fudge_value"] = fw, fv
+    out["atom_files"] = np.array(rr.PASSIVE_ATOMS)
+    out["atom_text"] = np.array([open(os.path.join(rr.REF_ROOT, "rh", "Atoms", a)).read()
+                                 for a in rr.PASSIVE_ATOMS])
+    path = os.path.join(HERE, "hse.npz")
+    np.savez_compressed(path, **out)
+    print(f"hse: {len(cases)} atmospheres, {os.path.getsize(path) / 1e3:.0f} kB")
+
+
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
           "lte_static": make_lte_static, "lte_broadening": make_lte_broadening,
           "nlte": make_nlte, "nlte_static": make_nlte_static, "kurucz": make_kurucz,
-          "background": make_background, "ltepops": make_ltepops, "chem": make_chem}
+          "background": make_background, "ltepops": make_ltepops, "chem": make_chem,
+          "hse": make_hse}
 
 
 def main():

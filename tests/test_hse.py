@@ -1,0 +1,73 @@
+"""Hydrostatic equilibrium on the CPU: the oracle's restatement of pyrh's
+hse() (oracle/hse.py) against the reference's own output (fixture hse:
+log tau500 and height scales, another top pressure and a cooler
+atmosphere, abundance overrides, fudge factors), and the host pieces of
+the GPU path -- the model atoms' data as pyrh_atom_read and
+pyrh_gb300.hse.setup_from_atoms give them against the reference's parse,
+the abundance totals and the element lookup."""
+import numpy as np
+import pytest
+
+from conftest import HSE_ATOM_ELEMENTS, hse_fudge, hse_oracle_inputs
+from oracle import hse as OH
+from pyrh_gb300 import grid as G
+from pyrh_gb300 import hse as H
+from pyrh_gb300 import ltepops as LP
+
+
+@pytest.mark.parametrize("case", range(5))
+def test_oracle_hse_matches_reference(golden, case):
+    h = golden("hse")
+    tab, atoms, mols, ids = hse_oracle_inputs(golden, case)
+    ne, nH, rho, pg, passes = OH.hse(tab, atoms, mols, ids, int(h["atm_scale"][case]),
+                                     h["scale"][case][None], h["T"][case][None],
+                                     float(h["pg_top"][case]), fudge=hse_fudge(golden, case))
+    for got, key in ((ne, "ne"), (nH, "nHtot"), (rho, "rho"), (pg, "pg")):
+        np.testing.assert_allclose(got[0], h[key][case], rtol=1e-13, atol=0, err_msg=key)
+    assert np.all(passes >= 1)
+
+
+def test_setup_from_atoms_matches_reference_parse(golden):
+    """The atom files' levels, continua and lines as the GPU path reads them
+    equal the arrays the reference made of the same files."""
+    h, bg = golden("hse"), golden("background")
+    atoms = [G.read_atom(str(t)) for t in h["atom_text"]]
+    elems = [H.element_index(a) for a in atoms]
+    assert elems == HSE_ATOM_ELEMENTS
+    s = H.setup_from_atoms(atoms, elems, float(bg["misc"][0]), bg["mol_present"])
+    assert np.array_equal(s["atoms_meta"][:, :3], bg["atoms_meta"][:, :3])
+    np.testing.assert_array_equal(s["atoms_lev"], bg["atoms_lev"])
+    np.testing.assert_array_equal(s["atoms_line"], bg["atoms_line"])
+    np.testing.assert_array_equal(s["atoms_cont"][:, :7], bg["atoms_cont"][:, :7])
+    assert np.array_equal(s["misc"][:4], bg["misc"][:4])
+    # the explicit cross-section tables, row for row
+    for r, q in zip(s["atoms_cont"], bg["atoms_cont"]):
+        if not int(r[4]):
+            n = int(r[6])
+            np.testing.assert_array_equal(s["atoms_tab"][int(r[7]):int(r[7]) + n],
+                                          bg["atoms_tab"][int(q[7]):int(q[7]) + n])
+
+
+@pytest.mark.parametrize("ti", [0, 2])
+def test_abundance_totals_match_oracle(golden, ti):
+    lp = golden("ltepops")
+    meta = lp["el_meta"][ti]
+    ns = meta[:, 0].astype(np.int32)
+    tab = LP.ElementTables(lp["Tpf"], meta[:, 2].copy(), meta[:, 1].astype(np.int32), ns,
+                           np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32),
+                           lp["el_pf"], lp["el_ionpot"])
+    got = H.abundance_totals(tab)
+    want = OH.totals({"el_meta": meta})
+    assert got == want
+
+
+def test_element_index():
+    lib = H._lib()
+    for s, e in ((b"H ", 0), (b"H", 0), (b"HE", 1), (b"C ", 5), (b"FE", 25), (b"ES", 98),
+                 (b"he", 1), (b"XX", -1)):
+        assert lib.pyrh_element_index(s) == e, s
+
+
+def test_hse_rejects_the_column_mass_scale():
+    with pytest.raises(ValueError, match="column-mass"):
+        H.hse_batch(None, 1, np.zeros((1, 3)), np.ones((1, 3)))

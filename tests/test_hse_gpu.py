@@ -1,0 +1,66 @@
+"""Hydrostatic equilibrium on the GPU (pyrh_hse through the C ABI) against
+the reference's own hse() output (fixture hse): log tau500 and height
+scales, another top pressure on a cooler atmosphere, abundance overrides
+and opacity fudge factors; a batch of atmospheres in one call equals the
+atmospheres run alone, and the passes per layer equal the oracle's."""
+import numpy as np
+import pytest
+
+from conftest import hse_fudge, hse_oracle_inputs
+from oracle import hse as OH
+from pyrh_gb300 import _lib as L
+from pyrh_gb300 import chem as CH
+from pyrh_gb300 import grid as G
+from pyrh_gb300 import hse as H
+from pyrh_gb300 import ltepops as LP
+
+pytestmark = pytest.mark.gpu
+
+# the 71 layers each add the rounding of their pressure step; CUDA's exp,
+# log and pow differ from the host's by an ulp or so
+RTOL = 1e-11
+
+
+def _model(golden, case):
+    h, lp, ch, bg = golden("hse"), golden("ltepops"), golden("chem"), golden("background")
+    ti = 2 if case == int(h["ab_case"]) else 0
+    meta = lp["el_meta"][ti]
+    ns = meta[:, 0].astype(np.int32)
+    tab = LP.ElementTables(lp["Tpf"], meta[:, 2].copy(), meta[:, 1].astype(np.int32), ns,
+                           np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32),
+                           lp["el_pf"], lp["el_ionpot"])
+    atoms = [G.read_atom(str(t)) for t in h["atom_text"]]
+    mols = [CH.read_molecule(str(t), tab.abundance_set) for t in ch["molecule_text"]]
+    return H.HseModel.build(tab, atoms, mols, float(bg["misc"][0]), hse_fudge(golden, case))
+
+
+@pytest.mark.parametrize("case", range(5))
+def test_hse_matches_reference(golden, case):
+    h = golden("hse")
+    model = _model(golden, case)
+    ne, nH, rho, pg = H.hse_batch(model, int(h["atm_scale"][case]), h["scale"][case][None],
+                                  h["T"][case][None], float(h["pg_top"][case]))
+    assert L.lib().pyrh_last_launch_count() > 0
+    for got, key in ((ne, "ne"), (nH, "nHtot"), (rho, "rho"), (pg, "pg")):
+        np.testing.assert_allclose(got[0], h[key][case], rtol=RTOL, atol=0, err_msg=key)
+
+
+def test_hse_batch_equals_single_atmospheres_and_oracle_passes(golden):
+    """Cases 0 and 1 and case 0 again with case 1's top pressure, in one
+    call: each equals its own run, and every layer took the oracle's number
+    of passes."""
+    h = golden("hse")
+    model = _model(golden, 0)
+    scale = np.stack([h["scale"][0], h["scale"][1], h["scale"][0]])
+    T = np.stack([h["T"][0], h["T"][1], h["T"][0]])
+    pg_top = np.array([h["pg_top"][0], h["pg_top"][1], h["pg_top"][1]])
+    ne, nH, rho, pg, passes = H.hse_batch(model, 0, scale, T, pg_top, iterations=True)
+    for a in range(3):
+        one = H.hse_batch(model, 0, scale[a:a + 1], T[a:a + 1], pg_top[a])
+        for got, solo in zip((ne, nH, rho, pg), one):
+            assert np.array_equal(got[a], solo[0])
+    for a, c in ((0, 0), (1, 1)):
+        np.testing.assert_allclose(nH[a], h["nHtot"][c], rtol=RTOL, atol=0)
+    tab, atoms, mols, ids = hse_oracle_inputs(golden, 0)
+    *_, opasses = OH.hse(tab, atoms, mols, ids, 0, scale, T, pg_top)
+    assert np.array_equal(passes, opasses)
