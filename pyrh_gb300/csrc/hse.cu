@@ -311,7 +311,11 @@ extern "C" pyrh_status pyrh_hse(const pyrh_elem_tables* tables, const pyrh_molec
     B.opacity = op_tmp;
   }
   int32_t* still_h = nullptr;
-  cudaMallocHost(&still_h, sizeof(int32_t));
+  if (cudaMallocHost(&still_h, sizeof(int32_t)) != cudaSuccess) {
+    if (op_tmp) cudaFree(op_tmp);
+    cudaFree(S.base);
+    return fail(PYRH_ERR_CUDA, "hse: pinned host allocation");
+  }
 
   AtomsDev A;
   A.natom = atoms->natom;
