@@ -435,6 +435,7 @@ def hse_measure(natm, local, tab, lp, ch):
     import torch
     from pyrh_gb300 import chem as CH
     from pyrh_gb300 import grid as G
+    from pyrh_gb300 import equilibria as EQ
     from pyrh_gb300 import hse as H
     from pyrh_gb300 import ltepops as LP
     g = lambda n: dict(np.load(os.path.join(HERE, "tests", "golden", n + ".npz")))
@@ -450,8 +451,7 @@ def hse_measure(natm, local, tab, lp, ch):
                              np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32),
                              lp["el_pf"], lp["el_ionpot"])
         mols = [CH.read_molecule(str(x), t.abundance_set) for x in ch["molecule_text"]]
-        fudge = (h["fudge_wave"], h["fudge_value"]) if case == int(h["fudge_case"]) else None
-        return H.HseModel.build(t, atoms, mols, float(bg["misc"][0]), fudge, device=dev)
+        return EQ.AtomsModel.build(t, atoms, mols, float(bg["misc"][0]), device=dev)
 
     m0 = model(0)
     sel = np.arange(natm) % 2
@@ -469,9 +469,10 @@ def hse_measure(natm, local, tab, lp, ch):
     launches = int(L.lib().pyrh_last_launch_count())
     err = 0.0
     for c in range(len(h["T"])):
-        m = m0 if c in (0, 1, 2) else model(c)
+        m = model(c) if c == int(h["ab_case"]) else m0
+        fudge = (h["fudge_wave"], h["fudge_value"]) if c == int(h["fudge_case"]) else None
         got = H.hse_batch(m, int(h["atm_scale"][c]), h["scale"][c][None], h["T"][c][None],
-                          float(h["pg_top"][c]))
+                          float(h["pg_top"][c]), fudge)
         for x, k in zip(got, ("ne", "nHtot", "rho", "pg")):
             err = max(err, float(np.abs(x[0] / h[k][c] - 1).max()))
     # the oracle (numpy restatement, one core) on the first atmosphere
@@ -479,7 +480,7 @@ def hse_measure(natm, local, tab, lp, ch):
     from oracle import hse as OH
     otab = {"Tpf": lp["Tpf"], "el_meta": lp["el_meta"][0], "el_pf": lp["el_pf"],
             "el_ionpot": lp["el_ionpot"]}
-    elems = [H.element_index(a) for a in atoms]
+    elems = [EQ.element_index(a) for a in atoms]
     meta = bg["atoms_meta"]
     lo = np.concatenate([[0], np.cumsum(meta[:, 0])])
     co = np.concatenate([[0], np.cumsum(meta[:, 1])])

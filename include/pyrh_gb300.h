@@ -841,32 +841,65 @@ pyrh_status pyrh_chem_equil(const pyrh_elem_tables *tables, const pyrh_molecule 
                             const double *nHtot, const double *const *fn0_model, double *nmol_out,
                             double *nHmin, double *nnuc, int32_t *niter, void *stream);
 
+/* ------------------------------------- passive atoms, equilibria, depth scales --
+ * The model atoms of a run's atoms.input, all passive (LTE), as the
+ * background and the equilibria read them: levels of every atom as rows of
+ * one population array [level][npoint] (device), atoms in the list's order. */
+#define PYRH_MAX_PASSIVE_ATOMS 24
+
+typedef struct {
+  int32_t natom;
+  int32_t elem[PYRH_MAX_PASSIVE_ATOMS];         /* element index of each model atom */
+  int32_t lev_off[PYRH_MAX_PASSIVE_ATOMS + 1];  /* its levels are rows lev_off[m] ..
+                                                   lev_off[m+1]-1 of the populations */
+  const double *E, *g;                          /* device [lev_off[natom]]: J, statistical weight */
+  const int32_t *stage;                         /* device [lev_off[natom]] */
+} pyrh_passive_atoms;
+
+/* The equilibria of Background() (background.c:155-170 with SOLVE_NE NONE)
+   at npoint depth points for the given electron density: every atom's LTE
+   populations (LTEpops without Debye lowering, rh/ltepops.c:33-109), the
+   chemical equilibrium of the molecules (pyrh_chem_equil) from the model
+   atoms' neutral fractions, and the populations of the atoms bound in
+   molecules scaled by the share of their nuclei left atomic
+   (chemequil.c:219-238, 330-339).  Outputs (device): pops [nlevel][npoint],
+   nmol [nmol][npoint], nHmin [npoint]. */
+pyrh_status pyrh_equilibria(const pyrh_elem_tables *tables, const pyrh_molecule *mol,
+                            int32_t nmol, const pyrh_passive_atoms *atoms, int64_t npoint,
+                            const double *T, const double *ne, const double *nHtot, double *pops,
+                            double *nmol_out, double *nHmin, void *stream);
+
+/* The depth scales of convertScales (rh/rhf1d/multiatmos.c:100-177) for
+   natm atmospheres from the continuum opacity at the reference wavelength:
+   given log10 tau_ref (scale 0), log10 column mass [g cm^-2] (1) or height
+   [km] (2) -- converted as the reference does, pyrh_compute1dray.c:229-245 --
+   the other two follow by the trapezoid rule, and on the tau and
+   column-mass scales the heights are shifted to zero where tau_ref = 1. */
+typedef struct {
+  int32_t natm, ndep;    /* ndep >= 2 */
+  int32_t scale;         /* 0 tau_ref, 1 column mass, 2 height */
+  double gravity;        /* m s^-2 */
+  double total_abund, wght_per_H;
+  /* device arrays [ndep][natm] */
+  const double *scale_in;        /* the given scale, in the reference's input units */
+  const double *T, *ne, *nHtot;  /* K, m^-3 */
+  const double *chi_ref;         /* continuum opacity at lambda_ref, m^-1 */
+  double *tau_ref, *cmass, *height;   /* out: 1, kg m^-2, m */
+} pyrh_scales_batch;
+
+pyrh_status pyrh_convert_scales(const pyrh_scales_batch *batch, void *stream);
+
 /* -------------------------------------------------- hydrostatic equilibrium --
  * pyrh's hse() (rh/rhf1d/pyrh_hse.c:67-399, pyrh.pyx:427-487) for a batch of
  * atmospheres with the same number of depth points, all on the device.  Layer
  * by layer from the top, each atmosphere iterates until its hydrogen density
  * changes by at most eta_limit (relative) or nmax_iter passes are done; a
  * pass takes the electron density (get_ne: Solve_ne from hydrogen's
- * ionisation with U = 1), the model atoms' LTE populations (LTEpops without
- * Debye lowering, rh/ltepops.c:33-109), chemical equilibrium with the
- * model atoms' neutral fractions and their populations scaled by the
- * molecules' share (chemequil.c:213-345), the continuum opacity at 500 nm
- * (pyrh_Background, rh/rhf1d/pyrh_background.c:144-457: the background
- * without the metals' bound-free continua, scattering included), and the
- * gas pressure by the trapezoid in log tau500 (or in height) and from it the
- * hydrogen density.  Atoms, molecules and the background model are what the
- * run's atoms.input / molecules.input name, all passive (LTE). */
-#define PYRH_HSE_MAX_ATOMS 24
-
-typedef struct {
-  int32_t natom;
-  int32_t elem[PYRH_HSE_MAX_ATOMS];         /* element index of each model atom */
-  int32_t lev_off[PYRH_HSE_MAX_ATOMS + 1];  /* its levels are rows lev_off[m] .. lev_off[m+1]-1
-                                               of the background model's populations */
-  const double *E, *g;                      /* device [lev_off[natom]]: J, statistical weight */
-  const int32_t *stage;                     /* device [lev_off[natom]] */
-} pyrh_hse_atoms;
-
+ * ionisation with U = 1), the equilibria (pyrh_equilibria), the continuum
+ * opacity at 500 nm (pyrh_Background, rh/rhf1d/pyrh_background.c:144-457:
+ * the background without the metals' bound-free continua, scattering
+ * included), and the gas pressure by the trapezoid in log tau500 (or in
+ * height) and from it the hydrogen density. */
 typedef struct {
   double gravity;        /* m s^-2 (MULTIatmos: 10^4.4 cm s^-2) */
   double total_abund;    /* atmos.totalAbund (pyrh_abundance_totals) */
@@ -894,7 +927,7 @@ typedef struct {
    pyrh_chem_equil, with H2 / OH / CH (when present) giving the background's
    molecule densities. */
 pyrh_status pyrh_hse(const pyrh_elem_tables *tables, const pyrh_molecule *mol, int32_t nmol,
-                     const pyrh_bg_model *bg, const pyrh_hse_atoms *atoms,
+                     const pyrh_bg_model *bg, const pyrh_passive_atoms *atoms,
                      const pyrh_hse_config *cfg, const pyrh_hse_batch *batch, void *stream);
 
 /* Number of kernel launches the last pyrh_lte_stokes / pyrh_nlte_* call issued. */

@@ -14,6 +14,12 @@ per pass of a layer:
                                                            added)
     totals            rh/abundance.c:168-221              (totalAbund, wght_per_H)
 
+and the same pieces for a run's set-up and pyrh's get_scales:
+    equilibria(...)   SetLTEQuantities + ChemicalEquilibrium (background.c:155-170)
+    continuum(...)    Background() at given wavelengths (passive atoms, SOLVE_NE NONE)
+    convert_scales(...) convertScales, rh/rhf1d/multiatmos.c:100-177
+    get_scales(...)   rh/rhf1d/pyrh_hse.c:402-554
+
 `tab` has the layout of oracle.ltepops (tests/golden/ltepops.npz); `atoms`
 is a list of dicts (elem, E, g, stage, cont rows, line rows, tab rows as
 the background fixture keeps them), hydrogen among them; `mols` are
@@ -117,9 +123,10 @@ def _layer_fixture(atoms, pops, T, ne, nHmin, nmol_by_id, vmicro_char, mol_prese
             "misc": np.array([vmicro_char, he, h, len(atoms)], np.float64)}
 
 
-def layer_pass(tab, atoms, mols, mol_ids, T, nH, vmicro_char, fudge=None):
-    """One pass at a layer: (ne, opacity at 500 nm) at every point."""
-    ne, _ = OL.solve_ne(tab, T, nH, unit_hydrogen_pf=True)
+def equilibria(tab, atoms, mols, T, ne, nH):
+    """SetLTEQuantities and ChemicalEquilibrium at every point: the atoms'
+    populations (list of [nlevel, npoint], scaled for the nuclei bound in
+    molecules), the molecule densities [nmol, npoint] and nHmin [npoint]."""
     ntot = [tab["el_meta"][a["elem"], 2] * nH for a in atoms]
     pops = [lte_pops(a, T, ne, nt) for a, nt in zip(atoms, ntot)]
     fn0 = {a["elem"]: neutral_fraction(a, p, nt) for a, p, nt in zip(atoms, pops, ntot)}
@@ -129,10 +136,74 @@ def layer_pass(tab, atoms, mols, mol_ids, T, nH, vmicro_char, fudge=None):
         for m, a in enumerate(atoms):
             if a["elem"] == e:
                 pops[m] = pops[m] * (nnuc[i] / ntot[m])
+    return pops, nmol, nHmin
+
+
+def continuum(tab, atoms, mols, mol_ids, lam, T, ne, nH, vmicro_char=5.0e3, fudge=None,
+              hse=False):
+    """Background() at the wavelengths lam (or, with hse, pyrh_Background:
+    no metals, scattering added): chi, eta [nlam, npoint] and the protons."""
+    pops, nmol, nHmin = equilibria(tab, atoms, mols, T, ne, nH)
     by_id = {mol_ids[i]: nmol[i] for i in range(len(mols))}
     present = [x in by_id for x in ("H2", "OH", "CH")]
     fx = _layer_fixture(atoms, pops, T, ne, nHmin, by_id, vmicro_char, present)
-    chi, _, _, _ = OB.background(fx, 0, add_scatter=True, fudge=fudge, metals=False)
+    fx["lambda"] = np.atleast_1d(np.asarray(lam, np.float64))
+    chi, eta, _, _ = OB.background(fx, 0, add_scatter=hse, fudge=fudge, metals=not hse)
+    h = [a["elem"] for a in atoms].index(0)
+    return chi, eta, pops[h][-1]
+
+
+def convert_scales(atm_scale, scale, T, ne, nH, chi, total_abund, wght, gravity=GRAVITY):
+    """convertScales (rh/rhf1d/multiatmos.c:100-177) of one atmosphere:
+    tau_ref, cmass [kg m^-2], height [m] from the given scale (log10 tau,
+    log10 g cm^-2 or km) and the opacity at lambda_ref."""
+    nd = len(T)
+    rho = (AMU * wght) * np.asarray(nH)
+    tau, cm, h = np.zeros(nd), np.zeros(nd), np.zeros(nd)
+    if atm_scale == 0:
+        tau = np.exp(LG10 * np.asarray(scale))
+        cm[0] = (tau[0] / chi[0]) * rho[0]
+        for k in range(1, nd):
+            h[k] = h[k - 1] - 2.0 * (tau[k] - tau[k - 1]) / (chi[k - 1] + chi[k])
+            cm[k] = cm[k - 1] + 0.5 * (rho[k - 1] + rho[k]) * (h[k - 1] - h[k])
+    elif atm_scale == 1:
+        cm = np.exp(LG10 * np.asarray(scale)) * (1.0E-03 / (1.0E-02 * 1.0E-02))
+        tau[0] = chi[0] / rho[0] * cm[0]
+        for k in range(1, nd):
+            h[k] = h[k - 1] - 2.0 * (cm[k] - cm[k - 1]) / (rho[k - 1] + rho[k])
+            tau[k] = tau[k - 1] + 0.5 * (chi[k - 1] + chi[k]) * (h[k - 1] - h[k])
+    else:
+        h = np.asarray(scale) * KM_TO_M
+        cm[0] = (nH[0] * total_abund + ne[0]) * (KBOLTZMANN * T[0] / gravity)
+        tau[0] = 0.5 * chi[0] * (h[0] - h[1])
+        if tau[0] > 1.0:
+            tau[0] = 0.0
+        for k in range(1, nd):
+            cm[k] = cm[k - 1] + 0.5 * (rho[k - 1] + rho[k]) * (h[k - 1] - h[k])
+            tau[k] = tau[k - 1] + 0.5 * (chi[k - 1] + chi[k]) * (h[k - 1] - h[k])
+    if atm_scale in (0, 1):
+        if tau[1] > tau[0]:
+            h0 = OL.linear(tau, h, 1.0)[0]
+        else:
+            h0 = OL.linear(tau[::-1], h[::-1], 1.0)[0]
+        h = h - h0
+    return tau, cm, h
+
+
+def get_scales(tab, atoms, mols, mol_ids, atm_scale, scale, atm, lam_ref, vmicro_char=5.0e3):
+    """pyrh.get_scales of an atmosphere [9, ndep] (compute1d's rows)."""
+    cube = 1.0E-02 * 1.0E-02 * 1.0E-02
+    T, ne, nH = atm[1], atm[2] / cube, atm[8] / cube
+    chi, _, _ = continuum(tab, atoms, mols, mol_ids, [lam_ref], T, ne, nH, vmicro_char)
+    tA, wght = totals(tab)
+    return convert_scales(atm_scale, scale, T, ne, nH, chi[0], tA, wght)
+
+
+def layer_pass(tab, atoms, mols, mol_ids, T, nH, vmicro_char, fudge=None):
+    """One pass at a layer: (ne, opacity at 500 nm) at every point."""
+    ne, _ = OL.solve_ne(tab, T, nH, unit_hydrogen_pf=True)
+    chi, _, _ = continuum(tab, atoms, mols, mol_ids, [500.0], T, ne, nH, vmicro_char, fudge,
+                          hse=True)
     return ne, chi[0]
 
 

@@ -176,6 +176,27 @@ def _hse_full_job(args):
     return ne, nH, rho, pg
 
 
+def _scales_job(args):
+    """get_scales() (pyrh.pyx:491-533): tau, height, cmass of an atmosphere
+    [9, ndep] (compute1d's rows) on its scale."""
+    workdir, pyrh_path, atm_scale, scale, atm, lam_ref, ab_id, ab_val = args
+    lib = _lib(pyrh_path)
+    atm = np.array(atm, dtype=np.float64, order="C")
+    n = atm.shape[1]
+    scale = np.ascontiguousarray(scale, dtype=np.float64)
+    tau, height, cmass = (np.zeros(n) for _ in range(3))
+    na, ai, av = 0, None, None
+    if ab_id is not None:
+        ab_id = np.ascontiguousarray(ab_id, dtype=np.int32)
+        ab_val = np.ascontiguousarray(ab_val, dtype=np.float64)
+        na, ai, av = len(ab_id), ab_id.ctypes.data_as(C.POINTER(C.c_int)), _p(ab_val)
+    rows = [np.ascontiguousarray(atm[r]) for r in (1, 2, 3, 4, 8)]
+    lib.get_scales.restype = None
+    lib.get_scales(workdir.encode(), n, _p(scale), *[_p(r) for r in rows], int(atm_scale),
+                   C.c_double(lam_ref), _p(tau), _p(height), _p(cmass), na, ai, av)
+    return tau, height, cmass
+
+
 def _synth_job(args):
     workdir, pyrh_path, mu, atm, wave = args
     lib = _lib(pyrh_path)
@@ -356,6 +377,10 @@ class Reference:
                  fudge_value=None, ab_id=None, ab_val=None):
         return self._run(_hse_full_job, (workdir, self.pyrh_path, atm_scale, scale, T, pg_top,
                                          fudge_wave, fudge_value, ab_id, ab_val))
+
+    def get_scales(self, workdir, atm_scale, scale, atm, lam_ref, ab_id=None, ab_val=None):
+        return self._run(_scales_job, (workdir, self.pyrh_path, atm_scale, scale, atm, lam_ref,
+                                       ab_id, ab_val))
 
     def synth(self, workdir, mu, atm, wave):
         return self._run(_synth_job, (workdir, self.pyrh_path, mu, atm, wave))

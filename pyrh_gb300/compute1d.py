@@ -100,17 +100,24 @@ class LteSetup:
     pyrh_gb300.lte.make_lines).  With line_pops None, compute1d forms them
     on the device from the atmosphere (pyrh_line_pops) and the element
     tables: `elements` (a pyrh_gb300.ltepops.ElementTables), else the
-    abundance and partition-function files the run in cwd names."""
+    abundance and partition-function files the run in cwd names.  With
+    chi_c, eta_c, height and np None, compute1d forms them on the device as
+    the reference's Background() and convertScales do: LTE populations and
+    chemical equilibrium of the run's passive atoms and molecules
+    (`atoms_model`, a pyrh_gb300.equilibria.AtomsModel, else the files the
+    run in cwd names), the continuum on the grid, the heights from the
+    opacity at LAMBDA_REF."""
     lam: np.ndarray
-    chi_c: np.ndarray
-    eta_c: np.ndarray
-    height: np.ndarray
-    np: np.ndarray
+    chi_c: np.ndarray | None
+    eta_c: np.ndarray | None
+    height: np.ndarray | None
+    np: np.ndarray | None
     line_pops: np.ndarray | None
     line_const: np.ndarray
     zeeman: np.ndarray
     zeeman_n: np.ndarray
     elements: object = None
+    atoms_model: object = None
 
 
 def _line_constants(setup: LteSetup, loggf_ids, loggf_values) -> np.ndarray:
@@ -144,10 +151,24 @@ def compute1d(cwd, mu, atm_scale, atmosphere, wave, loggf_ids=None, loggf_values
     import torch
     if lam_ids is not None or lam_values is not None:
         raise NotImplementedError("lam_ids / lam_values change the line list's wavelengths")
+    continuum_here = all(x is None for x in (setup.chi_c, setup.eta_c, setup.height, setup.np))
+    if not continuum_here and any(x is None for x in (setup.chi_c, setup.eta_c, setup.height,
+                                                      setup.np)):
+        raise ValueError("chi_c, eta_c, height and np are given together or not at all")
+    fudge = None
     if fudge_wave is not None or fudge_value is not None:
-        raise NotImplementedError("fudge_wave / fudge_value change the background opacity")
-    if atomic_number is not None or atomic_abundance is not None:
-        raise NotImplementedError("atomic_number / atomic_abundance change the set-up")
+        if not continuum_here:
+            raise NotImplementedError("fudge_wave / fudge_value change the background opacity "
+                                      "the caller's set-up holds")
+        fudge = (np.asarray(fudge_wave, np.float64),
+                 np.asarray(fudge_value, np.float64).reshape(3, -1))
+    if (atomic_number is None) != (atomic_abundance is None):
+        atomic_number = atomic_abundance = None   # the reference reads neither then
+    if atomic_number is not None:
+        if not continuum_here or setup.line_pops is not None or setup.elements is not None \
+                or setup.atoms_model is not None:
+            raise NotImplementedError("atomic_number / atomic_abundance change the set-up the "
+                                      "caller holds")
     atmosphere = np.asarray(atmosphere, np.float64)
     if atmosphere.ndim != 2 or atmosphere.shape[0] != 9:
         raise ValueError("atmosphere must be [9, ndep]")
@@ -176,16 +197,32 @@ def compute1d(cwd, mu, atm_scale, atmosphere, wave, loggf_ids=None, loggf_values
         raise ValueError("the set-up's wavelength grid is not the one these wavelengths make")
     lc = _line_constants(setup, loggf_ids, loggf_values)
     lines, nline = lte.make_lines(lc, setup.zeeman, setup.zeeman_n)
+    model = None
+    if continuum_here:
+        from . import equilibria as EQ
+        model = setup.atoms_model if setup.atoms_model is not None else \
+            EQ.AtomsModel.from_cwd(cwd, atomic_number, atomic_abundance, device)
+        chi_c, eta_c, np_ = EQ.continuum(model, g.lam, T, ne, nH, fudge)
+        iref = int(np.searchsorted(g.lam, lambda_ref))
+        _, _, height = EQ.convert_scales(model, atm_scale, atmosphere[0], T, ne, nH, chi_c[iref])
+        height = height[0]
+    else:
+        chi_c, eta_c, np_, height = setup.chi_c, setup.eta_c, setup.np, setup.height
     line_pops = setup.line_pops
     if line_pops is None:
         from . import ltepops as LP
-        tab = setup.elements if setup.elements is not None else LP.tables_from_files(cwd)
+        if setup.elements is not None:
+            tab = setup.elements
+        elif model is not None:
+            tab = model.tables
+        else:
+            tab = LP.tables_from_files(cwd)
         line_pops = LP.line_pops(LP.DeviceTables(tab, device), T, ne, nH,
                                  lc[:, 1].astype(np.int32) - 1,
                                  lc[:, 2].astype(np.int32)).cpu().numpy()
-    atm = dict(height=setup.height, T=T, ne=ne, nHtot=nH, np=setup.np, vturb=vturb, vel=vel,
+    atm = dict(height=height, T=T, ne=ne, nHtot=nH, np=np_, vturb=vturb, vel=vel,
                B=B, gamma_B=gam, chi_B=chi, line_pops=line_pops, lam=g.lam,
-               chi_c=setup.chi_c, eta_c=setup.eta_c)
+               chi_c=chi_c, eta_c=eta_c)
     pk = lte.pack([atm], nline, precision)
     dev = lte.DeviceBatch(pk, lines, nline, device=device)
     cfg = lte.make_config(precision=precision, mu=mu, vmicro_char=vmicro_char,

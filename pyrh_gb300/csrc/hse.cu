@@ -14,6 +14,9 @@
 //                    the Newton iteration)
 //   pyrh_Background  rh/rhf1d/pyrh_background.c:144-457 (pyrh_background with
 //                    a model without the metals' continua, scattering added)
+//   convertScales    rh/rhf1d/multiatmos.c:100-177 (pyrh_convert_scales), with
+//                    Linear (rh/linear.c:22-51) and Locate (rh/hunt.c:92-117)
+//                    for the height where tau_ref = 1
 //
 // Work layout: a layer k of every atmosphere is one vector of natm points
 // (the batch is [ndep][natm]); each pass is six launches over those points
@@ -41,6 +44,8 @@ constexpr double kMe = 9.1093897E-31;
 constexpr double kPi = 3.14159265358979;
 constexpr double kAMU = 1.6605402E-27;
 constexpr double kKM_TO_M = 1.0E+03;
+constexpr double kG_TO_KG = 1.0E-03;
+constexpr double kCM_TO_M = 1.0E-02;
 constexpr double kLG10 = 2.30258509299404568402;   // ln 10 (rh.h POW10)
 constexpr double kC1 = (kH / (2.0 * kPi * kMe)) * (kH / kK);
 constexpr int kThreads = 128;
@@ -49,8 +54,8 @@ __device__ __forceinline__ double pow10r(double x) { return exp(kLG10 * (x)); }
 
 struct AtomsDev {
   int natom;
-  int elem[PYRH_HSE_MAX_ATOMS];
-  int lev_off[PYRH_HSE_MAX_ATOMS + 1];
+  int elem[PYRH_MAX_PASSIVE_ATOMS];
+  int lev_off[PYRH_MAX_PASSIVE_ATOMS + 1];
   const double *E, *g;
   const int32_t* stage;
   const double* abund;   // element tables
@@ -226,10 +231,217 @@ int find_molecule(const pyrh_molecule* mol, int nmol, const char* id) {
   return -1;
 }
 
+pyrh_status check_atoms(const pyrh_passive_atoms* atoms) {
+  if (atoms->natom < 1 || atoms->natom > PYRH_MAX_PASSIVE_ATOMS || !atoms->E || !atoms->g ||
+      !atoms->stage || atoms->lev_off[0] != 0)
+    return fail(PYRH_ERR_ARG, "passive atoms: count, arrays or first offset");
+  for (int m = 0; m < atoms->natom; ++m) {
+    if (atoms->lev_off[m + 1] <= atoms->lev_off[m] || atoms->elem[m] < 0 ||
+        atoms->elem[m] >= PYRH_NELEM)
+      return fail(PYRH_ERR_ARG, "passive atoms: levels or element");
+    for (int q = 0; q < m; ++q)
+      if (atoms->elem[q] == atoms->elem[m])
+        return fail(PYRH_ERR_ARG, "passive atoms: two atoms of one element");
+  }
+  return PYRH_OK;
+}
+
+// The nuclei (elements bound in some molecule, in element order, as
+// pyrh_chem_equil numbers them) and the model atom of each (-1: none);
+// -1 when there are more than PYRH_CHEM_MAX_NUCLEI.
+int nuclei_atoms(const pyrh_molecule* mol, int nmol, const pyrh_passive_atoms* atoms,
+                 int* nuc_atom) {
+  bool bound[PYRH_NELEM] = {false};
+  for (int i = 0; i < nmol; ++i)
+    for (int j = 0; j < mol[i].nelement && j < PYRH_MOL_MAX_ELEMENTS; ++j)
+      if (mol[i].pt_index[j] >= 0 && mol[i].pt_index[j] < PYRH_NELEM) bound[mol[i].pt_index[j]] = true;
+  int nnuc = 0;
+  for (int e = 0; e < PYRH_NELEM; ++e) {
+    if (!bound[e]) continue;
+    if (nnuc == PYRH_CHEM_MAX_NUCLEI) return -1;
+    nuc_atom[nnuc] = -1;
+    for (int m = 0; m < atoms->natom; ++m)
+      if (atoms->elem[m] == e) nuc_atom[nnuc] = m;
+    ++nnuc;
+  }
+  return nnuc;
+}
+
+AtomsDev atoms_dev(const pyrh_passive_atoms* atoms, const double* abund) {
+  AtomsDev A;
+  A.natom = atoms->natom;
+  for (int m = 0; m < A.natom; ++m) A.elem[m] = atoms->elem[m];
+  for (int m = 0; m <= A.natom; ++m) A.lev_off[m] = atoms->lev_off[m];
+  A.E = atoms->E;
+  A.g = atoms->g;
+  A.stage = atoms->stage;
+  A.abund = abund;
+  return A;
+}
+
+// LTE populations, chemical equilibrium and the scaled populations at
+// npoint points (three launches and pyrh_chem_equil's one); fn0 [natom]
+// [npoint] and nnuc_d [nnuc][npoint] are scratch, nuc_atom the device copy
+// of nuclei_atoms' map.
+pyrh_status equilibria_core(const pyrh_elem_tables* tables, const pyrh_molecule* mol, int nmol,
+                            const AtomsDev& A, int nnuc, const int* nuc_atom, int64_t npoint,
+                            const double* T, const double* ne, const double* nH, double* pops,
+                            double* fn0, double* nmol_out, double* nHmin, double* nnuc_d,
+                            cudaStream_t st, int& launches) {
+  const unsigned grid = (unsigned)((npoint + kThreads - 1) / kThreads);
+  const double* fn0_ptr[PYRH_NELEM];
+  for (int e = 0; e < PYRH_NELEM; ++e) fn0_ptr[e] = nullptr;
+  for (int m = 0; m < A.natom; ++m) fn0_ptr[A.elem[m]] = fn0 + (size_t)m * npoint;
+  hse_pops_kernel<<<grid, kThreads, 0, st>>>(A, npoint, T, nH, ne, pops, fn0);
+  ++launches;
+  const pyrh_status s = pyrh_chem_equil(tables, mol, nmol, npoint, T, ne, nH, fn0_ptr, nmol_out,
+                                        nHmin, nnuc_d, nullptr, st);
+  if (s != PYRH_OK) return s;
+  launches += pyrh_last_launch_count();
+  hse_scale_kernel<<<grid, kThreads, 0, st>>>(A, npoint, nnuc, nuc_atom, nH, nnuc_d, pops);
+  ++launches;
+  return PYRH_OK;
+}
+
+// convertScales for one atmosphere per thread, walking down its layers.
+__global__ void convert_scales_kernel(pyrh_scales_batch b) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= b.natm) return;
+  const int64_t n = b.natm;
+  const int nd = b.ndep;
+  auto at = [&](const double* x, int k) { return x[k * n + a]; };
+  double* tau = b.tau_ref;
+  double* cm = b.cmass;
+  double* h = b.height;
+  const double rho_c = kAMU * b.wght_per_H;
+  // the given scale in SI (pyrh_compute1dray.c:229-245)
+  for (int k = 0; k < nd; ++k) {
+    const double v = at(b.scale_in, k);
+    if (b.scale == 0) tau[k * n + a] = pow10r(v);
+    else if (b.scale == 1) cm[k * n + a] = pow10r(v) * (kG_TO_KG / (kCM_TO_M * kCM_TO_M));
+    else h[k * n + a] = v * kKM_TO_M;
+  }
+  double rho_u = rho_c * at(b.nHtot, 0), chi_u = at(b.chi_ref, 0);
+  if (b.scale == 1) {
+    h[a] = 0.0;
+    tau[a] = chi_u / rho_u * cm[a];
+  } else if (b.scale == 0) {
+    h[a] = 0.0;
+    cm[a] = (tau[a] / chi_u) * rho_u;
+  } else {
+    cm[a] = (at(b.nHtot, 0) * b.total_abund + at(b.ne, 0)) * (kK * at(b.T, 0) / b.gravity);
+    tau[a] = 0.5 * chi_u * (h[a] - h[n + a]);
+    if (tau[a] > 1.0) tau[a] = 0.0;
+  }
+  for (int k = 1; k < nd; ++k) {
+    const int64_t i = k * n + a, u = (k - 1) * n + a;
+    const double rho = rho_c * b.nHtot[i], chi = b.chi_ref[i];
+    if (b.scale == 1) {
+      h[i] = h[u] - 2.0 * (cm[i] - cm[u]) / (rho_u + rho);
+      tau[i] = tau[u] + 0.5 * (chi_u + chi) * (h[u] - h[i]);
+    } else if (b.scale == 0) {
+      h[i] = h[u] - 2.0 * (tau[i] - tau[u]) / (chi_u + chi);
+      cm[i] = cm[u] + 0.5 * (rho_u + rho) * (h[u] - h[i]);
+    } else {
+      cm[i] = cm[u] + 0.5 * (rho_u + rho) * (h[u] - h[i]);
+      tau[i] = tau[u] + 0.5 * (chi_u + chi) * (h[u] - h[i]);
+    }
+    rho_u = rho;
+    chi_u = chi;
+  }
+  if (b.scale == 0 || b.scale == 1) {
+    // Linear(Ndep, tau_ref, height, 1, &unity, &h_zero, FALSE)
+    const bool ascend = tau[n + a] > tau[a];
+    const double xmin = ascend ? tau[a] : tau[(nd - 1) * n + a];
+    const double xmax = ascend ? tau[(nd - 1) * n + a] : tau[a];
+    const double x = 1.0;
+    double h0;
+    if (x <= xmin) {
+      h0 = ascend ? h[a] : h[(nd - 1) * n + a];
+    } else if (x >= xmax) {
+      h0 = ascend ? h[(nd - 1) * n + a] : h[a];
+    } else {
+      // Locate: bisection for the interval holding x
+      const bool asc = tau[(nd - 1) * n + a] > tau[a];
+      int lo = 0, hi = nd;
+      while (hi - lo > 1) {
+        const int mid = (hi + lo) >> 1;
+        const double t = tau[mid * n + a];
+        if (asc ? (x >= t) : (x <= t)) lo = mid;
+        else hi = mid;
+      }
+      const double t0 = tau[lo * n + a], t1 = tau[(lo + 1) * n + a];
+      const double fx = (t1 - x) / (t1 - t0);
+      h0 = fx * h[lo * n + a] + (1 - fx) * h[(lo + 1) * n + a];
+    }
+    for (int k = 0; k < nd; ++k) h[k * n + a] = h[k * n + a] - h0;
+  }
+}
+
 }  // namespace
 
+extern "C" pyrh_status pyrh_equilibria(const pyrh_elem_tables* tables, const pyrh_molecule* mol,
+                                       int32_t nmol, const pyrh_passive_atoms* atoms,
+                                       int64_t npoint, const double* T, const double* ne,
+                                       const double* nHtot, double* pops, double* nmol_out,
+                                       double* nHmin, void* stream) {
+  pyrh::set_launches(0);
+  if (!tables || !mol || !atoms) return fail(PYRH_ERR_ARG, "equilibria: NULL argument");
+  if (npoint < 0 || npoint > ((int64_t)1 << 31) - kThreads)
+    return fail(PYRH_ERR_ARG, "equilibria: npoint outside [0, 2^31)");
+  if (npoint == 0) return PYRH_OK;
+  if (!T || !ne || !nHtot || !pops || !nmol_out || !nHmin)
+    return fail(PYRH_ERR_ARG, "equilibria: NULL array");
+  if (nmol < 1 || nmol > PYRH_CHEM_MAX_MOLECULES) return fail(PYRH_ERR_ARG, "equilibria: molecules");
+  const pyrh_status sa = check_atoms(atoms);
+  if (sa != PYRH_OK) return sa;
+  int nuc_atom_h[PYRH_CHEM_MAX_NUCLEI];
+  const int nnuc = nuclei_atoms(mol, nmol, atoms, nuc_atom_h);
+  if (nnuc < 0) return fail(PYRH_ERR_UNSUPPORTED, "equilibria: too many nuclei");
+  cudaStream_t st = (cudaStream_t)stream;
+  Scratch S;
+  S.size = 4 * 256 + sizeof(double) * (size_t)npoint * (atoms->natom + nnuc) +
+           sizeof(int) * PYRH_CHEM_MAX_NUCLEI;
+  if (cudaMalloc(&S.base, S.size) != cudaSuccess)
+    return fail(PYRH_ERR_CUDA, "equilibria: scratch allocation");
+  double* fn0 = S.take<double>((size_t)atoms->natom * npoint);
+  double* nnuc_d = S.take<double>((size_t)(nnuc > 0 ? nnuc : 1) * npoint);
+  int* nuc_atom = S.take<int>(PYRH_CHEM_MAX_NUCLEI);
+  cudaMemcpyAsync(nuc_atom, nuc_atom_h, sizeof(int) * nnuc, cudaMemcpyHostToDevice, st);
+  int launches = 0;
+  pyrh_status s = equilibria_core(tables, mol, nmol, atoms_dev(atoms, tables->abund), nnuc, nuc_atom,
+                                  npoint, T, ne, nHtot, pops, fn0, nmol_out, nHmin, nnuc_d, st,
+                                  launches);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (s == PYRH_OK && e != cudaSuccess) {
+    pyrh::set_error("equilibria: %s", cudaGetErrorString(e));
+    s = PYRH_ERR_CUDA;
+  }
+  cudaFree(S.base);
+  pyrh::set_launches(launches);
+  return s;
+}
+
+extern "C" pyrh_status pyrh_convert_scales(const pyrh_scales_batch* b, void* stream) {
+  pyrh::set_launches(0);
+  if (!b || b->natm < 1 || b->ndep < 2 || !b->scale_in || !b->T || !b->ne || !b->nHtot ||
+      !b->chi_ref || !b->tau_ref || !b->cmass || !b->height)
+    return fail(PYRH_ERR_ARG, "convert scales: NULL array, no atmosphere or fewer than 2 depths");
+  if (b->scale < 0 || b->scale > 2) return fail(PYRH_ERR_ARG, "convert scales: scale not 0, 1 or 2");
+  if (b->scale == 2 && !(b->gravity > 0.0)) return fail(PYRH_ERR_ARG, "convert scales: gravity");
+  const unsigned grid = (unsigned)((b->natm + kThreads - 1) / kThreads);
+  convert_scales_kernel<<<grid, kThreads, 0, (cudaStream_t)stream>>>(*b);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    pyrh::set_error("convert scales: %s", cudaGetErrorString(e));
+    return PYRH_ERR_CUDA;
+  }
+  pyrh::set_launches(1);
+  return PYRH_OK;
+}
+
 extern "C" pyrh_status pyrh_hse(const pyrh_elem_tables* tables, const pyrh_molecule* mol,
-                                int32_t nmol, const pyrh_bg_model* bg, const pyrh_hse_atoms* atoms,
+                                int32_t nmol, const pyrh_bg_model* bg, const pyrh_passive_atoms* atoms,
                                 const pyrh_hse_config* cfg, const pyrh_hse_batch* b,
                                 void* stream) {
   pyrh::set_launches(0);
@@ -244,16 +456,8 @@ extern "C" pyrh_status pyrh_hse(const pyrh_elem_tables* tables, const pyrh_molec
                 "branch leaves its pressure step unset");
   if (cfg->nmax_iter < 1 || !(cfg->total_abund > 0.0) || !(cfg->wght_per_H > 0.0))
     return fail(PYRH_ERR_ARG, "hse: config");
-  if (atoms->natom < 1 || atoms->natom > PYRH_HSE_MAX_ATOMS || !atoms->E || !atoms->g ||
-      !atoms->stage || atoms->lev_off[0] != 0)
-    return fail(PYRH_ERR_ARG, "hse: atoms");
-  for (int m = 0; m < atoms->natom; ++m) {
-    if (atoms->lev_off[m + 1] <= atoms->lev_off[m] || atoms->elem[m] < 0 ||
-        atoms->elem[m] >= PYRH_NELEM)
-      return fail(PYRH_ERR_ARG, "hse: atom levels or element");
-    for (int q = 0; q < m; ++q)
-      if (atoms->elem[q] == atoms->elem[m]) return fail(PYRH_ERR_ARG, "hse: two atoms of one element");
-  }
+  const pyrh_status sa = check_atoms(atoms);
+  if (sa != PYRH_OK) return sa;
   const int npop = atoms->lev_off[atoms->natom];
   if (bg->npop != npop) return fail(PYRH_ERR_ARG, "hse: background rows differ from the atoms' levels");
   if (nmol < 1 || nmol > PYRH_CHEM_MAX_MOLECULES) return fail(PYRH_ERR_ARG, "hse: molecules");
@@ -261,20 +465,9 @@ extern "C" pyrh_status pyrh_hse(const pyrh_elem_tables* tables, const pyrh_molec
             iCH = find_molecule(mol, nmol, "CH");
   if ((bg->has_h2 && iH2 < 0) || (bg->has_oh && iOH < 0) || (bg->has_ch && iCH < 0))
     return fail(PYRH_ERR_ARG, "hse: the background names a molecule the list lacks");
-  // nuclei in element order and the model atom of each (pyrh_chem_equil's order)
-  bool bound[PYRH_NELEM] = {false};
-  for (int i = 0; i < nmol; ++i)
-    for (int j = 0; j < mol[i].nelement && j < PYRH_MOL_MAX_ELEMENTS; ++j)
-      if (mol[i].pt_index[j] >= 0 && mol[i].pt_index[j] < PYRH_NELEM) bound[mol[i].pt_index[j]] = true;
-  int nuc_atom_h[PYRH_CHEM_MAX_NUCLEI], nnuc = 0;
-  for (int e = 0; e < PYRH_NELEM; ++e) {
-    if (!bound[e]) continue;
-    if (nnuc == PYRH_CHEM_MAX_NUCLEI) return fail(PYRH_ERR_UNSUPPORTED, "hse: too many nuclei");
-    nuc_atom_h[nnuc] = -1;
-    for (int m = 0; m < atoms->natom; ++m)
-      if (atoms->elem[m] == e) nuc_atom_h[nnuc] = m;
-    ++nnuc;
-  }
+  int nuc_atom_h[PYRH_CHEM_MAX_NUCLEI];
+  const int nnuc = nuclei_atoms(mol, nmol, atoms, nuc_atom_h);
+  if (nnuc < 0) return fail(PYRH_ERR_UNSUPPORTED, "hse: too many nuclei");
 
   cudaStream_t st = (cudaStream_t)stream;
   const int natm = b->natm;
@@ -317,18 +510,7 @@ extern "C" pyrh_status pyrh_hse(const pyrh_elem_tables* tables, const pyrh_molec
     return fail(PYRH_ERR_CUDA, "hse: pinned host allocation");
   }
 
-  AtomsDev A;
-  A.natom = atoms->natom;
-  for (int m = 0; m < A.natom; ++m) A.elem[m] = atoms->elem[m];
-  for (int m = 0; m <= A.natom; ++m) A.lev_off[m] = atoms->lev_off[m];
-  A.E = atoms->E;
-  A.g = atoms->g;
-  A.stage = atoms->stage;
-  A.abund = tables->abund;
-
-  const double* fn0_ptr[PYRH_NELEM];
-  for (int e = 0; e < PYRH_NELEM; ++e) fn0_ptr[e] = nullptr;
-  for (int m = 0; m < A.natom; ++m) fn0_ptr[A.elem[m]] = fn0 + (size_t)m * natm;
+  const AtomsDev A = atoms_dev(atoms, tables->abund);
 
   pyrh_bg_batch bb;
   memset(&bb, 0, sizeof bb);
@@ -370,14 +552,9 @@ extern "C" pyrh_status pyrh_hse(const pyrh_elem_tables* tables, const pyrh_molec
       s = pyrh_solve_ne(tables, natm, Tl, nHl, ne_c, 2, nullptr, stream);
       if (s != PYRH_OK) break;
       launches += pyrh_last_launch_count();
-      hse_pops_kernel<<<grid, kThreads, 0, st>>>(A, natm, Tl, nHl, ne_c, pops, fn0);
-      ++launches;
-      s = pyrh_chem_equil(tables, mol, nmol, natm, Tl, ne_c, nHl, fn0_ptr, nmol_d, nHmin, nnuc_d,
-                          nullptr, stream);
+      s = equilibria_core(tables, mol, nmol, A, nnuc, nuc_atom, natm, Tl, ne_c, nHl, pops, fn0,
+                          nmol_d, nHmin, nnuc_d, st, launches);
       if (s != PYRH_OK) break;
-      launches += pyrh_last_launch_count();
-      hse_scale_kernel<<<grid, kThreads, 0, st>>>(A, natm, nnuc, nuc_atom, nHl, nnuc_d, pops);
-      ++launches;
       s = pyrh_background(bg, &bb, stream);
       if (s != PYRH_OK) break;
       launches += pyrh_last_launch_count();

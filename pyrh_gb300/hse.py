@@ -1,6 +1,6 @@
 """Hydrostatic equilibrium on the GPU through the C ABI (pyrh_hse, hse.cu).
 
-    model = HseModel.from_cwd(cwd)                     # the run's atoms, molecules, tables
+    model = equilibria.AtomsModel.from_cwd(cwd)        # the run's atoms, molecules, tables
     ne, nHtot, rho, pg = hse_batch(model, 0, logtau, T, pg_top)   # [natm, ndep] SI
     ne, nHtot = hse(cwd, 0, logtau, T)                 # pyrh.hse's call
 
@@ -16,28 +16,17 @@ reference returns them.
 from __future__ import annotations
 
 import ctypes as C
-import math
-import os
-from dataclasses import dataclass
 
 import numpy as np
 
 from . import _lib as L
 from . import background as BG
 from . import chem as CH
-from . import grid as G
+from . import equilibria as EQ
 from . import ltepops as LP
 
-MAX_ATOMS = 24
-GRAVITY = math.exp(2.30258509299404568402 * 4.4) * 1.0e-2  # MULTIatmos: 10^4.4 cm s^-2 -> m s^-2
 NMAX_ITER = 50                                           # NMAX_HSE_ITER, pyrh_hse.c:61
 ETA_LIMIT = 1.0e-2                                       # pyrh_hse.c:214, 337
-
-
-class HseAtoms(C.Structure):
-    _fields_ = [("natom", C.c_int32), ("elem", C.c_int32 * MAX_ATOMS),
-                ("lev_off", C.c_int32 * (MAX_ATOMS + 1)), ("E", C.c_void_p), ("g", C.c_void_p),
-                ("stage", C.c_void_p)]
 
 
 class HseConfig(C.Structure):
@@ -53,148 +42,20 @@ class HseBatch(C.Structure):
 
 def _lib():
     lib = L.lib()
-    lib.pyrh_abundance_totals.restype = C.c_int
-    lib.pyrh_abundance_totals.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_double),
-                                          C.POINTER(C.c_double)]
-    lib.pyrh_element_index.restype = C.c_int32
-    lib.pyrh_element_index.argtypes = [C.c_char_p]
     lib.pyrh_hse.restype = C.c_int
     lib.pyrh_hse.argtypes = [C.POINTER(LP.ElemTables), C.POINTER(CH.Molecule), C.c_int32,
-                             C.POINTER(BG.BgModel), C.POINTER(HseAtoms), C.POINTER(HseConfig),
-                             C.POINTER(HseBatch), C.c_void_p]
+                             C.POINTER(BG.BgModel), C.POINTER(EQ.PassiveAtoms),
+                             C.POINTER(HseConfig), C.POINTER(HseBatch), C.c_void_p]
     return lib
 
 
-def abundance_totals(tab: LP.ElementTables) -> tuple[float, float]:
-    """(atmos.totalAbund, atmos.wght_per_H) of the element tables."""
-    ab = np.ascontiguousarray(tab.abund, np.float64)
-    aset = np.ascontiguousarray(tab.abundance_set, np.int32)
-    t, w = C.c_double(), C.c_double()
-    L.check(_lib().pyrh_abundance_totals(ab.ctypes.data, aset.ctypes.data, C.byref(t), C.byref(w)))
-    return t.value, w.value
-
-
-def element_index(atom: G.Atom) -> int:
-    e = _lib().pyrh_element_index(bytes(atom.id))
-    if e < 0:
-        raise ValueError(f"atom {atom.id!r}: no element of that symbol")
-    return e
-
-
-def setup_from_atoms(atoms: list, elems: list[int], vmicro_char: float, mol_present) -> dict:
-    """The atomic data the background model reads (the keys
-    background.model_from_setup takes) from parsed model atoms, all passive;
-    vmicro_char in m/s."""
-    meta, lev, cont, tab, line = [], [], [], [], []
-    for a in atoms:
-        meta.append((a.nlevel, a.ncont, a.nline, 0))
-        lev += [(a.level[i].E, a.level[i].g, a.level[i].stage) for i in range(a.nlevel)]
-        for kr in range(a.ncont):
-            c = a.cont[kr]
-            off = len(tab)
-            if c.hydrogenic:
-                lmin = c.lambda_min
-            else:
-                rows = range(c.table_off, c.table_off + c.nlambda)
-                tab += [(a.table_lambda[r], a.table_alpha[r]) for r in rows]
-                lmin = a.table_lambda[c.table_off]
-            cont.append((c.i, c.j, c.lambda0, lmin, c.hydrogenic, c.alpha0, c.nlambda, off))
-        line += [(a.line[kr].i, a.line[kr].j, a.line[kr].lambda0, a.line[kr].qwing,
-                  a.line[kr].Aji) for kr in range(a.nline)]
-    he = elems.index(1) if 1 in elems else -1
-    h = elems.index(0)
-    return {"atoms_meta": np.array(meta, np.int32).reshape(-1, 4),
-            "atoms_lev": np.array(lev, np.float64).reshape(-1, 3),
-            "atoms_cont": np.array(cont, np.float64).reshape(-1, 8),
-            "atoms_tab": np.array(tab, np.float64).reshape(-1, 2),
-            "atoms_line": np.array(line, np.float64).reshape(-1, 5),
-            "misc": np.array([vmicro_char, he, h, len(atoms)], np.float64),
-            "mol_present": np.asarray(mol_present, np.int32)}
-
-
-@dataclass
-class HseModel:
-    """Everything hse() reads besides the atmosphere, in device memory."""
-    tables: LP.ElementTables
-    dev_tables: LP.DeviceTables
-    molecules: list
-    background: BG.DeviceBackground
-    atoms: HseAtoms
-    config: HseConfig
-    keep: tuple
-
-    @classmethod
-    def build(cls, tables: LP.ElementTables, atoms: list, molecules: list,
-              vmicro_char: float = 5.0e3, fudge=None, device="cuda") -> "HseModel":
-        """tables: element tables; atoms: parsed model atoms (pyrh_gb300.grid
-        .read_atom), hydrogen among them; molecules: parsed molecules
-        (pyrh_gb300.chem.read_molecule), H2 first; fudge: (lambda [nm],
-        values [3, n]) as hse's fudge_wave / fudge_value."""
-        import torch
-        if not 0 < len(atoms) <= MAX_ATOMS:
-            raise ValueError(f"{len(atoms)} atoms (1..{MAX_ATOMS})")
-        elems = [element_index(a) for a in atoms]
-        if 0 not in elems:
-            raise ValueError("hydrogen's model atom is missing")
-        ids = [bytes(m.id).split(b"\0")[0] for m in molecules]
-        present = [x in ids for x in (b"H2", b"OH", b"CH")]
-        s = setup_from_atoms(atoms, elems, vmicro_char, present)
-        model = BG.model_from_setup(s, lte=True, metals=False)
-        bg = BG.DeviceBackground(model, add_scatter=True, fudge=fudge, device=device)
-        lev = s["atoms_lev"]
-        E = torch.from_numpy(np.ascontiguousarray(lev[:, 0])).to(device)
-        g = torch.from_numpy(np.ascontiguousarray(lev[:, 1])).to(device)
-        st = torch.from_numpy(np.ascontiguousarray(lev[:, 2], np.int32)).to(device)
-        A = HseAtoms()
-        A.natom = len(atoms)
-        off = np.concatenate([[0], np.cumsum([a.nlevel for a in atoms])])
-        for m, e in enumerate(elems):
-            A.elem[m] = e
-        for m, o in enumerate(off):
-            A.lev_off[m] = int(o)
-        A.E, A.g, A.stage = E.data_ptr(), g.data_ptr(), st.data_ptr()
-        total, wght = abundance_totals(tables)
-        cfg = HseConfig(gravity=GRAVITY, total_abund=total, wght_per_H=wght, scale=0,
-                        nmax_iter=NMAX_ITER, eta_limit=ETA_LIMIT)
-        return cls(tables, LP.DeviceTables(tables, device), list(molecules), bg, A, cfg,
-                   (E, g, st))
-
-    @classmethod
-    def from_cwd(cls, cwd, atomic_number=None, atomic_abundance=None, fudge=None,
-                 device="cuda") -> "HseModel":
-        """The model the reference reads for hse() in cwd: keyword.input's
-        ATOMS_FILE and MOLECULES_FILE (relative to cwd), the atom and
-        molecule files under $PYRH_PATH/rh/Atoms and rh/Molecules, the
-        abundance and partition-function files, VMICRO_CHAR."""
-        from .compute1d import read_keyword_input
-        kw = read_keyword_input(os.path.join(str(cwd), "keyword.input"))
-        root = os.environ.get("PYRH_PATH", "")
-        tab = LP.tables_from_files(cwd, atomic_number, atomic_abundance)
-        atoms = [G.read_atom(open(os.path.join(root, "rh", "Atoms", n)).read())
-                 for n in _list_file(os.path.join(str(cwd), kw.get("ATOMS_FILE", "atoms.input")))]
-        mols = [CH.read_molecule(open(os.path.join(root, "rh", "Molecules", n)).read(),
-                                 tab.abundance_set)
-                for n in _list_file(os.path.join(str(cwd),
-                                                 kw.get("MOLECULES_FILE", "molecules.input")))]
-        vmc = float(kw.get("VMICRO_CHAR", "0.0")) * 1.0e3
-        return cls.build(tab, atoms, mols, vmc, fudge, device)
-
-
-def _list_file(path: str) -> list[str]:
-    """The file names of an atoms.input / molecules.input list (count line,
-    then one 'file MODE POPULATIONS [pops file]' record per entry)."""
-    with open(path) as f:
-        recs = [ln.split() for ln in f if ln.strip() and not ln.lstrip().startswith("#")]
-    n = int(recs[0][0])
-    return [r[0] for r in recs[1:1 + n]]
-
-
-def hse_batch(model: HseModel, atm_scale: int, scale, T, pg_top=0.1, opacity=False,
-              iterations=False):
+def hse_batch(model: EQ.AtomsModel, atm_scale: int, scale, T, pg_top=0.1, fudge=None,
+              opacity=False, iterations=False):
     """Hydrostatic equilibrium of natm atmospheres: scale and T [natm, ndep]
     (log10 tau500 or height [km]; K), pg_top [natm] or one value (Pa).
     Returns ne, nHtot [m^-3], rho [kg m^-3], pg [Pa], each [natm, ndep] (and
-    the 500 nm opacity [m^-1] and the passes per layer on request)."""
+    the 500 nm opacity [m^-1] and the passes per layer on request).  fudge:
+    (lambda [nm], values [3, n]) as hse's fudge_wave / fudge_value."""
     import torch
     if atm_scale not in (0, 2):
         raise ValueError("atm_scale must be 0 (log tau500) or 2 (height): the reference's "
@@ -212,8 +73,10 @@ def hse_batch(model: HseModel, atm_scale: int, scale, T, pg_top=0.1, opacity=Fal
     for k in ("ne", "nHtot", "rho", "pg", "opacity"):
         t[k] = torch.zeros((ndep, natm), dtype=torch.float64, device=dev)
     t["niter"] = torch.zeros((ndep, natm), dtype=torch.int32, device=dev)
-    cfg = HseConfig.from_buffer_copy(model.config)
-    cfg.scale = atm_scale
+    cfg = HseConfig(gravity=EQ.GRAVITY, total_abund=model.total_abund,
+                    wght_per_H=model.wght_per_H, scale=atm_scale, nmax_iter=NMAX_ITER,
+                    eta_limit=ETA_LIMIT)
+    bg = model.background(hse=True, fudge=fudge)
     mols = (CH.Molecule * len(model.molecules))(*model.molecules)
     out = {k: [] for k in ("ne", "nHtot", "rho", "pg", "opacity", "niter")}
     for a0 in range(0, natm, 65535):
@@ -225,7 +88,7 @@ def hse_batch(model: HseModel, atm_scale: int, scale, T, pg_top=0.1, opacity=Fal
         for k, v in sub.items():
             setattr(b, k, v.data_ptr())
         L.check(_lib().pyrh_hse(C.byref(model.dev_tables.struct), mols, len(model.molecules),
-                                C.byref(model.background.m), C.byref(model.atoms), C.byref(cfg),
+                                C.byref(bg.m), C.byref(model.atoms), C.byref(cfg),
                                 C.byref(b), LP._stream()))
         for k in out:
             out[k].append(sub[k].cpu().numpy().T)
@@ -243,15 +106,15 @@ def hse(cwd, atm_scale, scale, temp, pg_top=0.1, fudge_wave=None, fudge_value=No
     """pyrh.hse (pyrh.pyx:427-487): ne and nHtot [m^-3] of one atmosphere
     (and rho [kg m^-3], pg [Pa] with full_output).  `model` skips reading the
     run's files again."""
+    fudge = None
+    if fudge_wave is not None or fudge_value is not None:
+        fudge = (np.asarray(fudge_wave, np.float64),
+                 np.asarray(fudge_value, np.float64).reshape(3, -1))
     if model is None:
-        fudge = None
-        if fudge_wave is not None or fudge_value is not None:
-            fudge = (np.asarray(fudge_wave, np.float64),
-                     np.asarray(fudge_value, np.float64).reshape(3, -1))
         if (atomic_number is None) != (atomic_abundance is None):
             atomic_number = atomic_abundance = None   # the reference reads neither then
         elif atomic_number is not None and len(atomic_number) != len(atomic_abundance):
             raise ValueError("different number of atomic_number and atomic_abundance")
-        model = HseModel.from_cwd(cwd, atomic_number, atomic_abundance, fudge, device)
-    ne, nH, rho, pg = (x[0] for x in hse_batch(model, atm_scale, scale, temp, pg_top))
+        model = EQ.AtomsModel.from_cwd(cwd, atomic_number, atomic_abundance, device)
+    ne, nH, rho, pg = (x[0] for x in hse_batch(model, atm_scale, scale, temp, pg_top, fudge))
     return (ne, nH, rho, pg) if full_output else (ne, nH)

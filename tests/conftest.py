@@ -118,13 +118,13 @@ def delo_wavelengths(fx) -> np.ndarray:
 HSE_ATOM_ELEMENTS = [0, 1, 5, 6, 7, 15, 25, 13, 12, 10, 11]
 
 
-def hse_oracle_inputs(golden, case: int):
+def hse_oracle_inputs(golden, case: int, fixture: str = "hse"):
     """(tab, atoms, mols, ids) for oracle.hse: the element tables the case
     reads (the ltepops fixture's; its third case carries the same abundance
     overrides), the atoms as the reference parsed them (background fixture),
     the molecules of the chem fixture."""
     from oracle import chem as OC
-    lp, bg, ch, h = golden("ltepops"), golden("background"), golden("chem"), golden("hse")
+    lp, bg, ch, h = golden("ltepops"), golden("background"), golden("chem"), golden(fixture)
     ti = 2 if case == int(h["ab_case"]) else 0
     tab = {"Tpf": lp["Tpf"], "el_meta": lp["el_meta"][ti], "el_pf": lp["el_pf"],
            "el_ionpot": lp["el_ionpot"]}
@@ -147,3 +147,22 @@ def hse_fudge(golden, case: int):
     if case != int(h["fudge_case"]):
         return None
     return h["fudge_wave"], h["fudge_value"]
+
+
+def passive_model(golden, ab_overrides: bool = False, device: str = "cuda"):
+    """pyrh_gb300.equilibria.AtomsModel of the fixtures' runs (the passive
+    atoms' files, the chem fixture's molecules, the ltepops fixture's tables,
+    with its abundance overrides if asked)."""
+    from pyrh_gb300 import chem as CH
+    from pyrh_gb300 import equilibria as EQ
+    from pyrh_gb300 import grid as G
+    from pyrh_gb300 import ltepops as LP
+    h, lp, ch, bg = golden("hse"), golden("ltepops"), golden("chem"), golden("background")
+    meta = lp["el_meta"][2 if ab_overrides else 0]
+    ns = meta[:, 0].astype(np.int32)
+    tab = LP.ElementTables(lp["Tpf"], meta[:, 2].copy(), meta[:, 1].astype(np.int32), ns,
+                           np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32),
+                           lp["el_pf"], lp["el_ionpot"])
+    atoms = [G.read_atom(str(t)) for t in h["atom_text"]]
+    mols = [CH.read_molecule(str(t), tab.abundance_set) for t in ch["molecule_text"]]
+    return EQ.AtomsModel.build(tab, atoms, mols, float(bg["misc"][0]), device=device)

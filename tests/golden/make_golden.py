@@ -57,6 +57,9 @@ Fixtures (npz, float64):
   chem            ChemicalEquilibrium() of the molecules of tests/molecules.input
                   (their files' text kept) on three atmospheres: the neutral
                   fractions it starts from and the densities it leaves
+  scales          pyrh.get_scales() of the C0 atmosphere on its three depth
+                  scales, at two reference wavelengths, and with abundance
+                  overrides
   hse             pyrh.hse() (ne, nHtot, rho, pg) on five atmospheres: C0 on
                   its log tau500 scale, a cooler one with another top
                   pressure, a height scale, abundance overrides, and opacity
@@ -620,13 +623,44 @@ def make_hse(ref, wd):
     print(f"hse: {len(cases)} atmospheres, {os.path.getsize(path) / 1e3:.0f} kB")
 
 
+def make_scales(ref, wd):
+    """get_scales() on the C0 atmosphere given on its log tau500 scale, on
+    the column-mass scale and on the height scale that run returned, at
+    lambda_ref 500 nm; on log tau500 at 450 nm; and with the abundance
+    overrides of the ltepops fixture.  The run reads the two Fe I lines'
+    Kurucz list (get_scales requires one), which adds no opacity at 450 or
+    500 nm."""
+    logtau, T, ne, nH = base_c0(ref, wd)
+    atm = wl.atmosphere_rows(logtau, T, ne, nH)
+    w = rr.scratch_dir()
+    rr.write_inputs(w, wl.fe_linelist())    # get_scales reads a Kurucz list (cwd/KURUCZ_DATA)
+    tau0, h0, cm0 = ref.get_scales(w, 0, logtau, atm, 500.0)
+    g_cm2 = 1.0e-3 / (1.0e-2 * 1.0e-2)                  # G_TO_KG / SQ(CM_TO_M)
+    cases = [(0, logtau, 500.0, None, None), (1, np.log10(cm0 / g_cm2), 500.0, None, None),
+             (2, h0 / 1.0e3, 500.0, None, None), (0, logtau, 450.0, None, None),
+             (0, logtau, 500.0, [1, 26], [12.0, 7.10])]
+    out = {k: [] for k in ("atm_scale", "scale", "lam_ref", "tau", "height", "cmass")}
+    for sc, scale, lr, ai, av in cases:
+        tau, h, cm = ref.get_scales(w, sc, scale, atm, lr, ai, av)
+        for k, v in (("atm_scale", sc), ("scale", scale), ("lam_ref", lr), ("tau", tau),
+                     ("height", h), ("cmass", cm)):
+            out[k].append(v)
+    shutil.rmtree(w, ignore_errors=True)
+    out = {k: np.array(v) for k, v in out.items()}
+    out["atm"] = atm
+    out["ab_case"] = np.array(4)
+    path = os.path.join(HERE, "scales.npz")
+    np.savez_compressed(path, **out)
+    print(f"scales: {len(cases)} cases, {os.path.getsize(path) / 1e3:.0f} kB")
+
+
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
           "lte_static": make_lte_static, "lte_broadening": make_lte_broadening,
           "nlte": make_nlte, "nlte_static": make_nlte_static, "kurucz": make_kurucz,
           "background": make_background, "ltepops": make_ltepops, "chem": make_chem,
-          "hse": make_hse}
+          "hse": make_hse, "scales": make_scales}
 
 
 def main():

@@ -26,6 +26,13 @@ def test_rejects_set_up_changes_and_wrong_grids(golden, tmp_path):
     with pytest.raises(NotImplementedError):
         C1.compute1d(cwd, 1.0, 0, fx["atm"], fx["wave"], atomic_number=np.array([26], np.int32),
                      atomic_abundance=np.array([7.5]), setup=setup_of(fx))
+    with pytest.raises(NotImplementedError):   # fudge factors and the caller's continuum
+        C1.compute1d(cwd, 1.0, 0, fx["atm"], fx["wave"], fudge_wave=np.array([400.0, 700.0]),
+                     fudge_value=np.ones((3, 2)), setup=setup_of(fx))
+    part = setup_of(fx)
+    part.height = None
+    with pytest.raises(ValueError):        # continuum, heights and protons go together
+        C1.compute1d(cwd, 1.0, 0, fx["atm"], fx["wave"], setup=part)
     with pytest.raises(ValueError):        # the set-up was made for other wavelengths
         C1.compute1d(cwd, 1.0, 0, fx["atm"], fx["wave"][:-3], setup=setup_of(fx))
     with pytest.raises(ValueError):

@@ -3,7 +3,7 @@ hse() (oracle/hse.py) against the reference's own output (fixture hse:
 log tau500 and height scales, another top pressure and a cooler
 atmosphere, abundance overrides, fudge factors), and the host pieces of
 the GPU path -- the model atoms' data as pyrh_atom_read and
-pyrh_gb300.hse.setup_from_atoms give them against the reference's parse,
+pyrh_gb300.equilibria.setup_from_atoms give them against the reference's parse,
 the abundance totals and the element lookup."""
 import numpy as np
 import pytest
@@ -11,6 +11,7 @@ import pytest
 from conftest import HSE_ATOM_ELEMENTS, hse_fudge, hse_oracle_inputs
 from oracle import hse as OH
 from pyrh_gb300 import grid as G
+from pyrh_gb300 import equilibria as EQ
 from pyrh_gb300 import hse as H
 from pyrh_gb300 import ltepops as LP
 
@@ -32,9 +33,9 @@ def test_setup_from_atoms_matches_reference_parse(golden):
     equal the arrays the reference made of the same files."""
     h, bg = golden("hse"), golden("background")
     atoms = [G.read_atom(str(t)) for t in h["atom_text"]]
-    elems = [H.element_index(a) for a in atoms]
+    elems = [EQ.element_index(a) for a in atoms]
     assert elems == HSE_ATOM_ELEMENTS
-    s = H.setup_from_atoms(atoms, elems, float(bg["misc"][0]), bg["mol_present"])
+    s = EQ.setup_from_atoms(atoms, elems, float(bg["misc"][0]), bg["mol_present"])
     assert np.array_equal(s["atoms_meta"][:, :3], bg["atoms_meta"][:, :3])
     np.testing.assert_array_equal(s["atoms_lev"], bg["atoms_lev"])
     np.testing.assert_array_equal(s["atoms_line"], bg["atoms_line"])
@@ -56,13 +57,13 @@ def test_abundance_totals_match_oracle(golden, ti):
     tab = LP.ElementTables(lp["Tpf"], meta[:, 2].copy(), meta[:, 1].astype(np.int32), ns,
                            np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32),
                            lp["el_pf"], lp["el_ionpot"])
-    got = H.abundance_totals(tab)
+    got = EQ.abundance_totals(tab)
     want = OH.totals({"el_meta": meta})
     assert got == want
 
 
 def test_element_index():
-    lib = H._lib()
+    lib = EQ._lib()
     for s, e in ((b"H ", 0), (b"H", 0), (b"HE", 1), (b"C ", 5), (b"FE", 25), (b"ES", 98),
                  (b"he", 1), (b"XX", -1)):
         assert lib.pyrh_element_index(s) == e, s
@@ -71,3 +72,34 @@ def test_element_index():
 def test_hse_rejects_the_column_mass_scale():
     with pytest.raises(ValueError, match="column-mass"):
         H.hse_batch(None, 1, np.zeros((1, 3)), np.ones((1, 3)))
+
+
+@pytest.mark.parametrize("case", range(5))
+def test_oracle_get_scales_matches_reference(golden, case):
+    """The two scales get_scales derives (the given one it leaves unset)."""
+    d = golden("scales")
+    tab, atoms, mols, ids = hse_oracle_inputs(golden, case, "scales")
+    sc = int(d["atm_scale"][case])
+    tau, cm, h = OH.get_scales(tab, atoms, mols, ids, sc, d["scale"][case], d["atm"],
+                               float(d["lam_ref"][case]))
+    got = {"tau": tau, "cmass": cm, "height": h}
+    for key in [("cmass", "height"), ("tau", "height"), ("tau", "cmass")][sc]:
+        np.testing.assert_allclose(got[key], d[key][case], rtol=1e-13, atol=1e-9, err_msg=key)
+
+
+def test_oracle_setup_matches_reference_lte_setup(golden):
+    """The set-up of a synthesis from the atmosphere alone -- continuum on
+    the whole wavelength grid, protons, heights from tau500 -- against the
+    reference's own set-up of the lte_c0 run."""
+    fx = golden("lte_c0")
+    tab, atoms, mols, ids = hse_oracle_inputs(golden, 0)
+    chi, eta, npr = OH.continuum(tab, atoms, mols, ids, fx["lam"], fx["T"], fx["ne"],
+                                 fx["nHtot"])
+    np.testing.assert_allclose(chi, fx["chi_c"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(eta, fx["eta_c"], rtol=1e-12, atol=0)
+    np.testing.assert_allclose(npr, fx["np"], rtol=1e-13, atol=0)
+    iref = int(np.searchsorted(fx["lam"], float(fx["lambda_ref"])))
+    assert fx["lam"][iref] == fx["lambda_ref"]
+    tA, w = OH.totals(tab)
+    _, _, h = OH.convert_scales(0, fx["atm"][0], fx["T"], fx["ne"], fx["nHtot"], chi[iref], tA, w)
+    np.testing.assert_allclose(h, fx["height"], rtol=1e-12, atol=1e-6)
