@@ -66,7 +66,7 @@ def hse_batch(model: EQ.AtomsModel, atm_scale: int, scale, T, pg_top=0.1, fudge=
         raise ValueError("scale and T differ in shape")
     natm, ndep = T.shape
     dev = model.dev_tables.device
-    pg0 = np.broadcast_to(np.asarray(pg_top, np.float64), (natm,))
+    pg0 = np.array(np.broadcast_to(np.asarray(pg_top, np.float64), (natm,)))
     lay = lambda x: torch.from_numpy(np.ascontiguousarray(x.T)).to(dev)
     t = {"scale": lay(scale), "T": lay(T),
          "pg_top": torch.from_numpy(np.ascontiguousarray(pg0)).to(dev)}
