@@ -5,6 +5,7 @@
     python -m pyrh_gb300.profile_case rf   --natm 512  --reps 2
     python -m pyrh_gb300.profile_case nlte --natm 64   --reps 1
     python -m pyrh_gb300.profile_case background --natm 1024 --reps 3
+    python -m pyrh_gb300.profile_case hse  --natm 1024 --reps 2
 
 lte:  pyrh_lte_stokes (FP32) over natm perturbed atmospheres, 71 depths,
       2 x 112 wavelengths (the batched synthesis workload at a smaller size).
@@ -14,6 +15,9 @@ nlte: pyrh_nlte_solve (FP32 formal solution) over natm atmospheres cycled
       from the three NLTE fixtures of tests/golden.
 background: pyrh_background (FP32) for natm copies of the C0 atmosphere of
       the background fixture on 224 wavelengths at 630.0-630.35 nm.
+hse:  pyrh_hse (FP64) for natm atmospheres of 71 layers on log tau500 (the
+      hse fixture's first two atmospheres alternating), with the passive
+      atoms, molecules and element tables of the fixtures' runs.
 Prints one line per case with the time of the last repetition (CUDA events).
 """
 from __future__ import annotations
@@ -39,7 +43,7 @@ def _time(fn, reps):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["lte", "grad", "rf", "nlte", "background"])
+    ap.add_argument("case", choices=["lte", "grad", "rf", "nlte", "background", "hse"])
     ap.add_argument("--natm", type=int, default=2048)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--fp64", action="store_true")
@@ -48,7 +52,28 @@ def main(argv=None):
     from . import _lib as L
     from . import lte, nlte, rf as RF, workload
     prec = L.PYRH_FP64 if a.fp64 else L.PYRH_FP32
-    if a.case == "background":
+    if a.case == "hse":
+        from . import chem as CH
+        from . import equilibria as EQ
+        from . import grid as G
+        from . import hse as H
+        from . import ltepops as LP
+        here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+        g = lambda n: dict(np.load(os.path.join(here, "tests", "golden", n + ".npz")))
+        h, lp, ch, bg = g("hse"), g("ltepops"), g("chem"), g("background")
+        meta = lp["el_meta"][0]
+        ns = meta[:, 0].astype(np.int32)
+        tab = LP.ElementTables(lp["Tpf"], meta[:, 2].copy(), meta[:, 1].astype(np.int32), ns,
+                               np.concatenate([[0], np.cumsum(ns)[:-1]]).astype(np.int32),
+                               lp["el_pf"], lp["el_ionpot"])
+        model = EQ.AtomsModel.build(tab, [G.read_atom(str(t)) for t in h["atom_text"]],
+                                    [CH.read_molecule(str(t), tab.abundance_set)
+                                     for t in ch["molecule_text"]], float(bg["misc"][0]))
+        sel = np.arange(a.natm) % 2
+
+        def run():
+            H.hse_batch(model, 0, h["scale"][sel], h["T"][sel], h["pg_top"][sel])
+    elif a.case == "background":
         from . import background as BGR
         here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
         fx = dict(np.load(os.path.join(here, "tests", "golden", "background.npz")))
