@@ -6,7 +6,9 @@
 //                    the gas pressure from the layer above, then passes of
 //                    electron density, LTE populations, chemical equilibrium
 //                    and 500 nm opacity until the hydrogen density settles)
-//   get_ne           rh/rhf1d/pyrh_background.c:459-540 (pyrh_solve_ne mode 2)
+//   get_ne           rh/rhf1d/pyrh_background.c:459-540 (Solve_ne's iteration,
+//                    fromscratch mode 2, with a warp per atmosphere: the
+//                    layers are too few points to fill the GPU otherwise)
 //   LTEpops          rh/ltepops.c:33-109 (Saha-Boltzmann; the Debye lowering
 //                    is switched off there, ltepops.c:53)
 //   ChemicalEquilibrium's neutral fractions and population scaling
@@ -34,6 +36,9 @@
 namespace pyrh {
 void set_error(const char* fmt, ...);
 void set_launches(int n);
+pyrh_status solve_ne_warp(const pyrh_elem_tables* tables, int64_t npoint, const double* T,
+                          const double* nHtot, double* ne, int32_t fromscratch, int32_t* niter,
+                          cudaStream_t st);
 }
 
 namespace {
@@ -549,7 +554,7 @@ extern "C" pyrh_status pyrh_hse(const pyrh_elem_tables* tables, const pyrh_molec
     ++launches;
     bb.T = Tl;
     for (int pass = 0; pass < cfg->nmax_iter; ++pass) {
-      s = pyrh_solve_ne(tables, natm, Tl, nHl, ne_c, 2, nullptr, stream);
+      s = pyrh::solve_ne_warp(tables, natm, Tl, nHl, ne_c, 2, nullptr, st);
       if (s != PYRH_OK) break;
       launches += pyrh_last_launch_count();
       s = equilibria_core(tables, mol, nmol, A, nnuc, nuc_atom, natm, Tl, ne_c, nHl, pops, fn0,

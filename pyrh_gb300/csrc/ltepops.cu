@@ -249,6 +249,121 @@ __global__ void solve_ne_kernel(DevTables t, int64_t npoint, const double* T,
   if (niter_out) niter_out[k] = dne > kMaxElectronError ? -1 : niter + 1;
 }
 
+// Solve_ne with the work of one point spread over a warp, for batches too
+// small to fill the GPU with one point per thread (the hydrostatic
+// equilibrium's layers): lane l takes elements l, l + 32, l + 64, l + 96 and
+// keeps their stage factors in registers; each Newton step adds the lanes'
+// error and derivative terms by a butterfly, so every lane holds the same
+// totals and the same n_e.  The terms are those of the reference; only their
+// summation order differs (the results agree with it to rounding).
+constexpr int kWarpElems = (PYRH_NELEM + 31) / 32;
+
+__device__ __forceinline__ void add_element_r(const DevTables& t, int e,
+                                              const double (&Er)[PYRH_PF_MAX_STAGES], double ne,
+                                              double CT_ne_ref, double& error, double& sum,
+                                              double PhiHmin) {
+  const int ns = t.nstage[e];
+  const double CT_ne = CT_ne_ref / ne;
+  double f[PYRH_PF_MAX_STAGES], df[PYRH_PF_MAX_STAGES];
+  double sum1 = 1.0, sum2 = 0.0;
+  f[0] = 1.0;
+  df[0] = 0.0;
+#pragma unroll
+  for (int j = 1; j < PYRH_PF_MAX_STAGES; ++j) {
+    if (j < ns) {
+      f[j] = f[j - 1] * CT_ne * Er[j];
+      df[j] = -j * f[j] / ne;
+      sum1 += f[j];
+      sum2 += df[j];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < PYRH_PF_MAX_STAGES; ++j) {
+    if (j < ns) {
+      f[j] /= sum1;
+      df[j] = (df[j] - f[j] * sum2) / sum1;
+    }
+  }
+  if (e == 0) {
+    error += ne * f[0] * PhiHmin;
+    sum -= (f[0] + ne * df[0]) * PhiHmin;
+  }
+  const double ab = t.abund[e];
+#pragma unroll
+  for (int j = 1; j < PYRH_PF_MAX_STAGES; ++j) {
+    if (j < ns) {
+      const double akj = ab * j;
+      error -= akj * f[j];
+      sum += akj * df[j];
+    }
+  }
+}
+
+__global__ void solve_ne_warp_kernel(DevTables t, int64_t npoint, const double* T,
+                                     const double* nHtot, double* ne, int fromscratch,
+                                     int32_t* niter_out) {
+  const int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= npoint) return;   // k is the same for the whole warp
+  const double Tk = T[k], nH = nHtot[k];
+  const PfAt at = pf_at(t.Tpf, t.npf, Tk);
+  double ne_old;
+  if (fromscratch) {
+    const double Uk =
+        fromscratch == 2 ? 0.0 : pf_eval(t.lnpf + (int64_t)t.stage_off[0] * t.npf, at);
+    const double PhiH = 0.5 * pow(kC1 / Tk, 1.5) * exp(Uk + t.ionpot[t.stage_off[0]] / (kK * Tk));
+    ne_old = (sqrt(1.0 + 4.0 * nH * PhiH) - 1.0) / (2.0 * PhiH);
+  } else {
+    ne_old = ne[k];
+  }
+  const double CT_ne_ref = 2.0 * pow(kC1 / Tk, -1.5);
+  const double PhiHmin = 0.25 * pow(kC1 / Tk, 1.5) * exp(0.754 * kEV / (kK * Tk));
+  double E[kWarpElems][PYRH_PF_MAX_STAGES];
+#pragma unroll
+  for (int q = 0; q < kWarpElems; ++q) {
+    const int e = lane + 32 * q;
+#pragma unroll
+    for (int j = 0; j < PYRH_PF_MAX_STAGES; ++j) E[q][j] = 0.0;
+    if (e >= t.nelem) continue;
+    const int ns = t.nstage[e], off = t.stage_off[e];
+    const double* lnpf = t.lnpf + (int64_t)off * t.npf;
+    double Uk = pf_eval(lnpf, at);
+#pragma unroll
+    for (int j = 1; j < PYRH_PF_MAX_STAGES; ++j) {
+      if (j < ns) {
+        const double Ukp1 = pf_eval(lnpf + (int64_t)j * t.npf, at);
+        E[q][j] = exp(Ukp1 - Uk - t.ionpot[off + j - 1] / (kK * Tk));
+        Uk = Ukp1;
+      }
+    }
+  }
+  double ne_new = ne_old, dne = 0.0;
+  int niter = 0;
+  while (niter < kMaxElectronIter) {
+    double err = 0.0, sm = 0.0;
+#pragma unroll
+    for (int q = 0; q < kWarpElems; ++q) {
+      const int e = lane + 32 * q;
+      if (e < t.nelem) add_element_r(t, e, E[q], ne_old, CT_ne_ref, err, sm, PhiHmin);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      err += __shfl_xor_sync(0xffffffffu, err, o);
+      sm += __shfl_xor_sync(0xffffffffu, sm, o);
+    }
+    const double error = ne_old / nH + err;
+    ne_new = ne_old - nH * error / (1.0 - nH * sm);
+    dne = fabs((ne_new - ne_old) / ne_old);
+    ne_old = ne_new;
+    if (dne <= kMaxElectronError) break;
+    niter++;
+  }
+  if (lane == 0) {
+    ne[k] = ne_new;
+    if (niter_out) niter_out[k] = dne > kMaxElectronError ? -1 : niter + 1;
+  }
+}
+
 pyrh_status fail(pyrh_status s, const char* msg) {
   pyrh::set_error("%s", msg);
   return s;
@@ -375,6 +490,26 @@ extern "C" pyrh_status pyrh_line_pops(const pyrh_elem_tables* tables, int64_t np
   }
   return finish(e, launches);
 }
+
+namespace pyrh {
+// pyrh_solve_ne's iteration with a warp per point (see solve_ne_warp_kernel);
+// launches one kernel on the stream.
+pyrh_status solve_ne_warp(const pyrh_elem_tables* tables, int64_t npoint, const double* T,
+                          const double* nHtot, double* ne, int32_t fromscratch, int32_t* niter,
+                          cudaStream_t st) {
+  if (npoint < 0 || npoint > ((int64_t)1 << 26)) return fail(PYRH_ERR_ARG, "solve ne: npoint");
+  if (npoint == 0) return PYRH_OK;
+  if (!T || !nHtot || !ne) return fail(PYRH_ERR_ARG, "solve ne: NULL array");
+  if (fromscratch < 0 || fromscratch > 2) return fail(PYRH_ERR_ARG, "solve ne: fromscratch not 0, 1 or 2");
+  DevTables d;
+  std::vector<int32_t> ns, off;
+  pyrh_status s = load_tables(tables, st, d, ns, off);
+  if (s != PYRH_OK) return s;
+  solve_ne_warp_kernel<<<(unsigned)((npoint * 32 + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+      d, npoint, T, nHtot, ne, fromscratch, niter);
+  return finish(cudaGetLastError(), 1);
+}
+}  // namespace pyrh
 
 extern "C" pyrh_status pyrh_solve_ne(const pyrh_elem_tables* tables, int64_t npoint,
                                      const double* T, const double* nHtot, double* ne,
