@@ -202,6 +202,193 @@ __global__ void chem_kernel(const __grid_constant__ ChemArgs A, int64_t npoint, 
   if (niter_out) niter_out[k] = dnmax > kIterLimit ? -1 : (niter > kMaxIter ? kMaxIter : niter);
 }
 
+// Chemical equilibrium with a warp per point, for batches too small to fill
+// the GPU one point per thread (the layers of the hydrostatic equilibrium, a
+// single atmosphere's set-up): lane i owns equation i, its row of the
+// Jacobian in shared memory.  Rows are filled in the reference's order.  The
+// factorisation is the right-looking form of the reference's Crout
+// elimination with the same implicit pivoting: every entry receives the same
+// updates, with the same multipliers, in the same order.  The forward
+// substitution runs column by column in the reference's order, the back
+// substitution column by column from the last (another summation order);
+// the results agree with the reference to rounding.
+constexpr int kChemWarps = 2;
+
+__device__ __forceinline__ void warp_lu_substitute(int Neq, const double* M, const int* piv,
+                                                   double* x, int lane) {
+  // the row interchanges in order (ludcmp.c LUbacksubst), then L y = P b
+  if (lane == 0)
+    for (int i = 0; i < Neq; ++i) {
+      const int ip = piv[i];
+      const double t = x[ip];
+      x[ip] = x[i];
+      x[i] = t;
+    }
+  __syncwarp();
+  double xl = lane < Neq ? x[lane] : 0.0;
+  for (int i = 0; i < Neq; ++i) {
+    const double xi = __shfl_sync(0xffffffffu, xl, i);
+    if (lane > i && lane < Neq) xl -= M[lane * Neq + i] * xi;
+  }
+  for (int i = Neq - 1; i >= 0; --i) {
+    if (lane == i) xl = xl / M[i * Neq + i];
+    const double xi = __shfl_sync(0xffffffffu, xl, i);
+    if (lane < i) xl -= M[lane * Neq + i] * xi;
+  }
+  __syncwarp();
+  if (lane < Neq) x[lane] = xl;
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * kChemWarps)
+    chem_warp_kernel(const __grid_constant__ ChemArgs A, int64_t npoint, const double* Tv,
+                     const double* nev, const double* nHv, double* nmol_out, double* nHmin_out,
+                     double* nnuc_out, int32_t* niter_out) {
+  __shared__ double sM[kChemWarps][kMaxEq * kMaxEq];
+  __shared__ double sMc[kChemWarps][kMaxEq * kMaxEq];
+  __shared__ double sx[kChemWarps][kMaxEq], sr[kChemWarps][kMaxEq], sn[kChemWarps][kMaxEq];
+  __shared__ int spiv[kChemWarps][kMaxEq];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t k = blockIdx.x * (int64_t)kChemWarps + w;
+  if (k >= npoint) return;   // the same for the whole warp
+  double* M = sM[w];
+  double* Mc = sMc[w];
+  double* x = sx[w];
+  double* r = sr[w];
+  double* nS = sn[w];
+  int* piv = spiv[w];
+  const unsigned full = 0xffffffffu;
+  const double T = Tv[k], ne = nev[k], nHtot = nHv[k];
+  const int Nn = A.nnuc, Nm = A.nmol, Neq = Nn + Nm;
+  double fl0 = 0.0, al = 0.0;
+  if (lane < Nn) {
+    const int e = A.nuc_elem[lane];
+    fl0 = A.fn0[lane] ? A.fn0[lane][k] : neutral_fraction(A, e, ne, T);
+    al = A.abund[e] * nHtot;
+  }
+  double fn0[PYRH_CHEM_MAX_NUCLEI];
+#pragma unroll
+  for (int i = 0; i < PYRH_CHEM_MAX_NUCLEI; ++i) fn0[i] = __shfl_sync(full, fl0, i);
+  const double PhiHmin = 0.25 * pow(kCI / T, 1.5) * exp(0.754 * kEV / (kK * T));
+  const double fHmin = ne * fn0[0] * PhiHmin;
+  const bool mol_row = lane >= Nn && lane < Neq;
+  const double Phi = mol_row ? equilconstant(A.mol[lane - Nn], T) : 0.0;
+  double nl = lane < Nn ? al : 0.0;
+  double prev = nl;
+  double dnmax = 0.0;
+  int niter = 1;
+  while (niter <= kMaxIter) {
+    nS[lane] = nl;
+    __syncwarp();
+    double fl = 0.0;
+    if (lane < Neq) {
+      double* row = M + lane * Neq;
+      for (int j = 0; j < Neq; ++j) row[j] = 0.0;
+      row[lane] = 1.0;
+      fl = nl - al;
+      if (lane == 0) {
+        fl += fHmin * nl;
+        row[0] += fHmin;
+      }
+      if (lane < Nn) {
+        for (int i = 0; i < Nm; ++i) {
+          const pyrh_molecule& m = A.mol[i];
+          for (int j = 0; j < m.nelement; ++j)
+            if (A.nucl_index[i][j] == lane) {
+              fl += m.pt_count[j] * nS[Nn + i];
+              row[Nn + i] += m.pt_count[j];
+            }
+        }
+      } else {
+        const pyrh_molecule& m = A.mol[lane - Nn];
+        double saha = Phi;
+        for (int j = 0; j < m.nelement; ++j) {
+          const int nu = A.nucl_index[lane - Nn][j];
+          saha *= pow(fn0[nu] * nS[nu], (double)m.pt_count[j]);
+        }
+        saha /= pow(ne, (double)m.charge);
+        fl -= saha;
+        for (int j = 0; j < m.nelement; ++j) {
+          const int nu = A.nucl_index[lane - Nn][j];
+          row[nu] = -saha * (m.pt_count[j] / nS[nu]);
+        }
+      }
+      x[lane] = fl;
+    }
+    __syncwarp();
+    for (int i = lane; i < Neq * Neq; i += 32) Mc[i] = M[i];
+    // implicit scaling of each row (ludcmp.c LUdecomp)
+    double vv = 0.0;
+    if (lane < Neq) {
+      double big = 0.0;
+      for (int j = 0; j < Neq; ++j) big = fmax(big, fabs(M[lane * Neq + j]));
+      vv = big == 0.0 ? 0.0 : 1.0 / big;
+    }
+    __syncwarp();
+    for (int j = 0; j < Neq; ++j) {
+      // pivot: the largest scaled |A[i][j]| of rows i >= j, the last of equals
+      double best = (lane >= j && lane < Neq) ? vv * fabs(M[lane * Neq + j]) : -1.0;
+      int imax = lane;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(full, best, o);
+        const int oi = __shfl_xor_sync(full, imax, o);
+        if (ob > best || (ob == best && oi > imax)) {
+          best = ob;
+          imax = oi;
+        }
+      }
+      if (imax != j) {
+        if (lane < Neq) {
+          const double t = M[imax * Neq + lane];
+          M[imax * Neq + lane] = M[j * Neq + lane];
+          M[j * Neq + lane] = t;
+        }
+        const double vj = __shfl_sync(full, vv, j);
+        if (lane == imax) vv = vj;
+      }
+      if (lane == 0) piv[j] = imax;
+      __syncwarp();
+      if (lane == 0 && M[j * Neq + j] == 0.0) M[j * Neq + j] = 1.0e-20;
+      __syncwarp();
+      const double dum = 1.0 / M[j * Neq + j];
+      if (lane > j && lane < Neq) {
+        double* row = M + lane * Neq;
+        const double l = row[j] * dum;
+        row[j] = l;
+        for (int c = j + 1; c < Neq; ++c) row[c] -= l * M[j * Neq + c];
+      }
+      __syncwarp();
+    }
+    // solve, then one improvement with the residual of the original system
+    warp_lu_substitute(Neq, M, piv, x, lane);
+    if (lane < Neq) {
+      double res = fl;
+      for (int j = 0; j < Neq; ++j) res -= Mc[lane * Neq + j] * x[j];
+      r[lane] = res;
+    }
+    __syncwarp();
+    warp_lu_substitute(Neq, M, piv, r, lane);
+    if (lane < Neq) nl -= x[lane] + r[lane];
+    // MaxChange with NG_CHEM_ORDER 0: the last two iterates
+    double d = 0.0;
+    if (lane < Neq && nl) d = fabs((nl - prev) / nl);
+    prev = nl;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d = fmax(d, __shfl_xor_sync(full, d, o));
+    dnmax = d;
+    if (dnmax <= kIterLimit) break;
+    niter++;
+  }
+  if (mol_row) nmol_out[(int64_t)(lane - Nn) * npoint + k] = nl;
+  const double n0 = __shfl_sync(full, nl, 0);
+  if (lane == 0) {
+    nHmin_out[k] = ne * (n0 * PhiHmin);
+    if (niter_out) niter_out[k] = dnmax > kIterLimit ? -1 : (niter > kMaxIter ? kMaxIter : niter);
+  }
+  if (nnuc_out && lane < Nn) nnuc_out[(int64_t)lane * npoint + k] = nl;
+}
+
 pyrh_status fail(pyrh_status s, const char* msg) {
   pyrh::set_error("%s", msg);
   return s;
@@ -209,12 +396,11 @@ pyrh_status fail(pyrh_status s, const char* msg) {
 
 }  // namespace
 
-extern "C" pyrh_status pyrh_chem_equil(const pyrh_elem_tables* tables, const pyrh_molecule* mol,
-                                       int32_t nmol, int64_t npoint, const double* T,
-                                       const double* ne, const double* nHtot,
-                                       const double* const* fn0_model, double* nmol_out,
-                                       double* nHmin, double* nnuc, int32_t* niter,
-                                       void* stream) {
+namespace {
+pyrh_status chem_launch(const pyrh_elem_tables* tables, const pyrh_molecule* mol, int32_t nmol,
+                        int64_t npoint, const double* T, const double* ne, const double* nHtot,
+                        const double* const* fn0_model, double* nmol_out, double* nHmin,
+                        double* nnuc, int32_t* niter, void* stream, bool warp) {
   pyrh::set_launches(0);
   if (!tables || !mol || nmol < 1 || nmol > PYRH_CHEM_MAX_MOLECULES || npoint < 0)
     return fail(PYRH_ERR_ARG, "chem: bad arguments");
@@ -263,9 +449,14 @@ extern "C" pyrh_status pyrh_chem_equil(const pyrh_elem_tables* tables, const pyr
   A.nstage = tables->nstage;
   A.stage_off = tables->stage_off;
   cudaStream_t st = (cudaStream_t)stream;
-  const int threads = 64;
-  chem_kernel<<<(unsigned)((npoint + threads - 1) / threads), threads, 0, st>>>(
-      A, npoint, T, ne, nHtot, nmol_out, nHmin, nnuc, niter);
+  if (warp) {
+    chem_warp_kernel<<<(unsigned)((npoint + kChemWarps - 1) / kChemWarps), 32 * kChemWarps, 0,
+                       st>>>(A, npoint, T, ne, nHtot, nmol_out, nHmin, nnuc, niter);
+  } else {
+    const int threads = 64;
+    chem_kernel<<<(unsigned)((npoint + threads - 1) / threads), threads, 0, st>>>(
+        A, npoint, T, ne, nHtot, nmol_out, nHmin, nnuc, niter);
+  }
   const cudaError_t e = cudaGetLastError();
   pyrh::set_launches(1);
   if (e != cudaSuccess) {
@@ -274,3 +465,29 @@ extern "C" pyrh_status pyrh_chem_equil(const pyrh_elem_tables* tables, const pyr
   }
   return PYRH_OK;
 }
+}  // namespace
+
+extern "C" pyrh_status pyrh_chem_equil(const pyrh_elem_tables* tables, const pyrh_molecule* mol,
+                                       int32_t nmol, int64_t npoint, const double* T,
+                                       const double* ne, const double* nHtot,
+                                       const double* const* fn0_model, double* nmol_out,
+                                       double* nHmin, double* nnuc, int32_t* niter,
+                                       void* stream) {
+  return chem_launch(tables, mol, nmol, npoint, T, ne, nHtot, fn0_model, nmol_out, nHmin, nnuc,
+                     niter, stream, false);
+}
+
+namespace pyrh {
+// pyrh_chem_equil with a warp per point (chem_warp_kernel).
+pyrh_status chem_equil_warp(const pyrh_elem_tables* tables, const pyrh_molecule* mol,
+                            int32_t nmol, int64_t npoint, const double* T, const double* ne,
+                            const double* nHtot, const double* const* fn0_model, double* nmol_out,
+                            double* nHmin, double* nnuc, int32_t* niter, void* stream) {
+  if (npoint > ((int64_t)1 << 31) - kChemWarps) {
+    pyrh::set_error("chem: npoint too large for a warp per point");
+    return PYRH_ERR_ARG;
+  }
+  return chem_launch(tables, mol, nmol, npoint, T, ne, nHtot, fn0_model, nmol_out, nHmin, nnuc,
+                     niter, stream, true);
+}
+}  // namespace pyrh

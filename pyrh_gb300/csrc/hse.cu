@@ -39,6 +39,10 @@ void set_launches(int n);
 pyrh_status solve_ne_warp(const pyrh_elem_tables* tables, int64_t npoint, const double* T,
                           const double* nHtot, double* ne, int32_t fromscratch, int32_t* niter,
                           cudaStream_t st);
+pyrh_status chem_equil_warp(const pyrh_elem_tables* tables, const pyrh_molecule* mol,
+                            int32_t nmol, int64_t npoint, const double* T, const double* ne,
+                            const double* nHtot, const double* const* fn0_model, double* nmol_out,
+                            double* nHmin, double* nnuc, int32_t* niter, void* stream);
 }
 
 namespace {
@@ -284,8 +288,8 @@ AtomsDev atoms_dev(const pyrh_passive_atoms* atoms, const double* abund) {
   return A;
 }
 
-// LTE populations, chemical equilibrium and the scaled populations at
-// npoint points (three launches and pyrh_chem_equil's one); fn0 [natom]
+// LTE populations, chemical equilibrium (a warp per point) and the scaled
+// populations at npoint points (three launches); fn0 [natom]
 // [npoint] and nnuc_d [nnuc][npoint] are scratch, nuc_atom the device copy
 // of nuclei_atoms' map.
 pyrh_status equilibria_core(const pyrh_elem_tables* tables, const pyrh_molecule* mol, int nmol,
@@ -299,8 +303,8 @@ pyrh_status equilibria_core(const pyrh_elem_tables* tables, const pyrh_molecule*
   for (int m = 0; m < A.natom; ++m) fn0_ptr[A.elem[m]] = fn0 + (size_t)m * npoint;
   hse_pops_kernel<<<grid, kThreads, 0, st>>>(A, npoint, T, nH, ne, pops, fn0);
   ++launches;
-  const pyrh_status s = pyrh_chem_equil(tables, mol, nmol, npoint, T, ne, nH, fn0_ptr, nmol_out,
-                                        nHmin, nnuc_d, nullptr, st);
+  const pyrh_status s = pyrh::chem_equil_warp(tables, mol, nmol, npoint, T, ne, nH, fn0_ptr,
+                                               nmol_out, nHmin, nnuc_d, nullptr, st);
   if (s != PYRH_OK) return s;
   launches += pyrh_last_launch_count();
   hse_scale_kernel<<<grid, kThreads, 0, st>>>(A, npoint, nnuc, nuc_atom, nH, nnuc_d, pops);

@@ -254,16 +254,19 @@ __global__ void solve_ne_kernel(DevTables t, int64_t npoint, const double* T,
 // equilibrium's layers): lane l takes elements l, l + 32, l + 64, l + 96 and
 // keeps their stage factors in registers; each Newton step adds the lanes'
 // error and derivative terms by a butterfly, so every lane holds the same
-// totals and the same n_e.  The terms are those of the reference; only their
-// summation order differs (the results agree with it to rounding).
+// totals and the same n_e.  The terms are those of the reference; their
+// summation order differs, and the divisions by n_e and by each element's
+// stage sum are multiplications by the reciprocal (FP64 divisions dominate
+// the work on this part's FP64 pipe): the results agree with the
+// reference's to rounding.
 constexpr int kWarpElems = (PYRH_NELEM + 31) / 32;
 
 __device__ __forceinline__ void add_element_r(const DevTables& t, int e,
                                               const double (&Er)[PYRH_PF_MAX_STAGES], double ne,
-                                              double CT_ne_ref, double& error, double& sum,
-                                              double PhiHmin) {
+                                              double inv_ne, double CT_ne_ref, double& error,
+                                              double& sum, double PhiHmin) {
   const int ns = t.nstage[e];
-  const double CT_ne = CT_ne_ref / ne;
+  const double CT_ne = CT_ne_ref * inv_ne;
   double f[PYRH_PF_MAX_STAGES], df[PYRH_PF_MAX_STAGES];
   double sum1 = 1.0, sum2 = 0.0;
   f[0] = 1.0;
@@ -272,16 +275,17 @@ __device__ __forceinline__ void add_element_r(const DevTables& t, int e,
   for (int j = 1; j < PYRH_PF_MAX_STAGES; ++j) {
     if (j < ns) {
       f[j] = f[j - 1] * CT_ne * Er[j];
-      df[j] = -j * f[j] / ne;
+      df[j] = -j * f[j] * inv_ne;
       sum1 += f[j];
       sum2 += df[j];
     }
   }
+  const double inv_sum1 = 1.0 / sum1;
 #pragma unroll
   for (int j = 0; j < PYRH_PF_MAX_STAGES; ++j) {
     if (j < ns) {
-      f[j] /= sum1;
-      df[j] = (df[j] - f[j] * sum2) / sum1;
+      f[j] *= inv_sum1;
+      df[j] = (df[j] - f[j] * sum2) * inv_sum1;
     }
   }
   if (e == 0) {
@@ -341,10 +345,11 @@ __global__ void solve_ne_warp_kernel(DevTables t, int64_t npoint, const double* 
   int niter = 0;
   while (niter < kMaxElectronIter) {
     double err = 0.0, sm = 0.0;
+    const double inv_ne = 1.0 / ne_old;
 #pragma unroll
     for (int q = 0; q < kWarpElems; ++q) {
       const int e = lane + 32 * q;
-      if (e < t.nelem) add_element_r(t, e, E[q], ne_old, CT_ne_ref, err, sm, PhiHmin);
+      if (e < t.nelem) add_element_r(t, e, E[q], ne_old, inv_ne, CT_ne_ref, err, sm, PhiHmin);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {

@@ -84,3 +84,23 @@ def test_compute1d_with_the_setup_from_the_atmosphere(golden, tmp_path, model, n
     for s in range(4):
         assert np.abs(got[s] - base[s]).max() < 1e-9 * ic
         assert np.abs(got[s] - fx["stokes_ref_portable"][s]).max() < 1e-5 * ic
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_equilibria_match_reference_chemistry(golden, model, case):
+    """pyrh_equilibria from T, n_e and nHtot alone -- the passive atoms' LTE
+    populations and their neutral fractions, then the chemistry (a warp per
+    point) -- against the reference's SetLTEQuantities + ChemicalEquilibrium
+    (fixture chem, down to 2900 K)."""
+    d = golden("chem")
+    pops, nmol, nHmin = EQ.equilibria(model, d["T"][case], d["ne"][case], d["nHtot"][case])
+    ref = d["nmol"][case]
+    np.testing.assert_allclose(nmol.cpu().numpy(), ref, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(nHmin.cpu().numpy(), d["nHmin"][case], rtol=1e-12, atol=0)
+    # the model atoms of the nuclei keep their atomic share (rows of H, C, N, O)
+    p = pops.cpu().numpy()
+    for i, e in enumerate(d["nuclei"]):
+        m = [model.atoms.elem[q] for q in range(model.atoms.natom)].index(int(e))
+        lo, hi = model.atoms.lev_off[m], model.atoms.lev_off[m + 1]
+        np.testing.assert_allclose(p[lo:hi].sum(axis=0), d["ntot_model"][case][i], rtol=1e-12,
+                                   atol=0)
