@@ -7,8 +7,8 @@
 //                    electron density, LTE populations, chemical equilibrium
 //                    and 500 nm opacity until the hydrogen density settles)
 //   get_ne           rh/rhf1d/pyrh_background.c:459-540 (Solve_ne's iteration,
-//                    fromscratch mode 2, with a warp per atmosphere: the
-//                    layers are too few points to fill the GPU otherwise)
+//                    fromscratch mode 2; a warp per atmosphere for batches
+//                    too small to fill the GPU one atmosphere per thread)
 //   LTEpops          rh/ltepops.c:33-109 (Saha-Boltzmann; the Debye lowering
 //                    is switched off there, ltepops.c:53)
 //   ChemicalEquilibrium's neutral fractions and population scaling
@@ -288,8 +288,15 @@ AtomsDev atoms_dev(const pyrh_passive_atoms* atoms, const double* abund) {
   return A;
 }
 
-// LTE populations, chemical equilibrium (a warp per point) and the scaled
-// populations at npoint points (three launches); fn0 [natom]
+// Up to this many points a call takes the warp-per-point forms of Solve_ne
+// and of the chemistry (the one-point-per-thread forms leave most of the GPU
+// idle and are bound by one thread's latency; above it they are faster:
+// 1024 atmospheres of hse 122 against 487 ms, 16384 875 against 598 ms).
+constexpr int64_t kSmallBatch = 8192;
+bool small_batch(int64_t npoint) { return npoint <= kSmallBatch; }
+
+// LTE populations, chemical equilibrium and the scaled populations at
+// npoint points (three launches); fn0 [natom]
 // [npoint] and nnuc_d [nnuc][npoint] are scratch, nuc_atom the device copy
 // of nuclei_atoms' map.
 pyrh_status equilibria_core(const pyrh_elem_tables* tables, const pyrh_molecule* mol, int nmol,
@@ -303,8 +310,12 @@ pyrh_status equilibria_core(const pyrh_elem_tables* tables, const pyrh_molecule*
   for (int m = 0; m < A.natom; ++m) fn0_ptr[A.elem[m]] = fn0 + (size_t)m * npoint;
   hse_pops_kernel<<<grid, kThreads, 0, st>>>(A, npoint, T, nH, ne, pops, fn0);
   ++launches;
-  const pyrh_status s = pyrh::chem_equil_warp(tables, mol, nmol, npoint, T, ne, nH, fn0_ptr,
-                                               nmol_out, nHmin, nnuc_d, nullptr, st);
+  const pyrh_status s =
+      small_batch(npoint)
+          ? pyrh::chem_equil_warp(tables, mol, nmol, npoint, T, ne, nH, fn0_ptr, nmol_out, nHmin,
+                                  nnuc_d, nullptr, st)
+          : pyrh_chem_equil(tables, mol, nmol, npoint, T, ne, nH, fn0_ptr, nmol_out, nHmin,
+                            nnuc_d, nullptr, st);
   if (s != PYRH_OK) return s;
   launches += pyrh_last_launch_count();
   hse_scale_kernel<<<grid, kThreads, 0, st>>>(A, npoint, nnuc, nuc_atom, nH, nnuc_d, pops);
@@ -558,7 +569,8 @@ extern "C" pyrh_status pyrh_hse(const pyrh_elem_tables* tables, const pyrh_molec
     ++launches;
     bb.T = Tl;
     for (int pass = 0; pass < cfg->nmax_iter; ++pass) {
-      s = pyrh::solve_ne_warp(tables, natm, Tl, nHl, ne_c, 2, nullptr, st);
+      s = small_batch(natm) ? pyrh::solve_ne_warp(tables, natm, Tl, nHl, ne_c, 2, nullptr, st)
+                            : pyrh_solve_ne(tables, natm, Tl, nHl, ne_c, 2, nullptr, st);
       if (s != PYRH_OK) break;
       launches += pyrh_last_launch_count();
       s = equilibria_core(tables, mol, nmol, A, nnuc, nuc_atom, natm, Tl, ne_c, nHl, pops, fn0,
