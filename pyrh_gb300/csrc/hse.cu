@@ -103,15 +103,17 @@ __global__ void hse_start_kernel(pyrh_hse_config c, pyrh_hse_batch b, int k, int
 
 // LTE populations of every model atom at the pass's electron density
 // (rows [level][natm] of pops) and the neutral fraction of each (fn0
-// [atom][natm]).
+// [atom][natm]); one thread per (atom, point), the points of an atom
+// consecutive.
 __global__ void hse_pops_kernel(AtomsDev A, int natm, const double* __restrict__ Tl,
                                 const double* __restrict__ nHl, const double* __restrict__ ne_c,
                                 double* __restrict__ pops, double* __restrict__ fn0) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= natm) return;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)natm * A.natom) return;
+  const int a = (int)(t % natm), m = (int)(t / natm);
   const double T = Tl[a], nH = nHl[a], ne = ne_c[a];
   const double cNe_T = 0.5 * ne * pow(kC1 / T, 1.5);
-  for (int m = 0; m < A.natom; ++m) {
+  {
     const int o = A.lev_off[m], nl = A.lev_off[m + 1] - o;
     const double ntotal = A.abund[A.elem[m]] * nH;
     const double E0 = A.E[o], g0 = A.g[o];
@@ -305,10 +307,11 @@ pyrh_status equilibria_core(const pyrh_elem_tables* tables, const pyrh_molecule*
                             double* fn0, double* nmol_out, double* nHmin, double* nnuc_d,
                             cudaStream_t st, int& launches) {
   const unsigned grid = (unsigned)((npoint + kThreads - 1) / kThreads);
+  const unsigned grid_atoms = (unsigned)((npoint * A.natom + kThreads - 1) / kThreads);
   const double* fn0_ptr[PYRH_NELEM];
   for (int e = 0; e < PYRH_NELEM; ++e) fn0_ptr[e] = nullptr;
   for (int m = 0; m < A.natom; ++m) fn0_ptr[A.elem[m]] = fn0 + (size_t)m * npoint;
-  hse_pops_kernel<<<grid, kThreads, 0, st>>>(A, npoint, T, nH, ne, pops, fn0);
+  hse_pops_kernel<<<grid_atoms, kThreads, 0, st>>>(A, npoint, T, nH, ne, pops, fn0);
   ++launches;
   const pyrh_status s =
       small_batch(npoint)
