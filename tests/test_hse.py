@@ -103,3 +103,71 @@ def test_oracle_setup_matches_reference_lte_setup(golden):
     tA, w = OH.totals(tab)
     _, _, h = OH.convert_scales(0, fx["atm"][0], fx["T"], fx["ne"], fx["nHtot"], chi[iref], tA, w)
     np.testing.assert_allclose(h, fx["height"], rtol=1e-12, atol=1e-6)
+
+
+def test_hse_structs_match_compiled_header(tmp_path):
+    """sizeof/offsetof of the passive-atom, depth-scale and hse structs as a
+    C compiler lays them out from include/pyrh_gb300.h, against the ctypes
+    mirrors."""
+    import ctypes as C
+    import os
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "pyrh_gb300.h"\n'
+        'int main(void) { printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", '
+        'sizeof(pyrh_passive_atoms), offsetof(pyrh_passive_atoms, E), '
+        'sizeof(pyrh_scales_batch), offsetof(pyrh_scales_batch, scale_in), '
+        'sizeof(pyrh_hse_config), offsetof(pyrh_hse_config, eta_limit), '
+        'sizeof(pyrh_hse_batch), offsetof(pyrh_hse_batch, niter)); return 0; }\n')
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", inc, str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True,
+                                          text=True).stdout.split()]
+    assert got == [C.sizeof(EQ.PassiveAtoms), EQ.PassiveAtoms.E.offset,
+                   C.sizeof(EQ.ScalesBatch), EQ.ScalesBatch.scale_in.offset,
+                   C.sizeof(H.HseConfig), H.HseConfig.eta_limit.offset,
+                   C.sizeof(H.HseBatch), H.HseBatch.niter.offset]
+
+
+def test_argument_checks_before_any_device_work():
+    """The entry points refuse bad arguments with a status and a message,
+    before they touch the device (so these run without a GPU)."""
+    import ctypes as C
+    from pyrh_gb300 import _lib as L
+    lib = EQ._lib()
+    H._lib()
+    b = EQ.ScalesBatch(natm=1, ndep=1, scale=0)           # fewer than 2 depth points
+    assert lib.pyrh_convert_scales(C.byref(b), None) == L.PYRH_ERR_ARG
+    assert b"convert scales" in lib.pyrh_last_error()
+    b = EQ.ScalesBatch(natm=1, ndep=4, scale=3)
+    for f in ("scale_in", "T", "ne", "nHtot", "chi_ref", "tau_ref", "cmass", "height"):
+        setattr(b, f, 8)
+    assert lib.pyrh_convert_scales(C.byref(b), None) == L.PYRH_ERR_ARG
+    assert b"scale" in lib.pyrh_last_error()
+    # no atoms, no molecules: refused before any allocation
+    tabs = LP.ElemTables()
+    atoms = EQ.PassiveAtoms()
+    assert lib.pyrh_equilibria(C.byref(tabs), None, 0, C.byref(atoms), 4, *([None] * 7)) == \
+        L.PYRH_ERR_ARG
+    assert lib.pyrh_equilibria(C.byref(tabs), None, 0, C.byref(atoms), 0, *([None] * 7)) == \
+        L.PYRH_ERR_ARG
+    cfg = H.HseConfig(scale=1, nmax_iter=50, total_abund=1.1, wght_per_H=1.4)
+    hb = H.HseBatch(natm=2, ndep=3)
+    for f in ("scale", "T", "pg_top", "ne", "nHtot", "rho", "pg"):
+        setattr(hb, f, 8)
+    from pyrh_gb300 import background as BG
+    from pyrh_gb300 import chem as CH
+    mols = (CH.Molecule * 1)()
+    st = lib.pyrh_hse(C.byref(tabs), mols, 1, C.byref(BG.BgModel()), C.byref(atoms),
+                      C.byref(cfg), C.byref(hb), None)
+    assert st == L.PYRH_ERR_UNSUPPORTED and b"column-mass" in lib.pyrh_last_error()
+    hb.natm = 0
+    st = lib.pyrh_hse(C.byref(tabs), mols, 1, C.byref(BG.BgModel()), C.byref(atoms),
+                      C.byref(cfg), C.byref(hb), None)
+    assert st == L.PYRH_ERR_ARG
