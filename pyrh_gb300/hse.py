@@ -65,8 +65,8 @@ def hse_batch(model: EQ.AtomsModel, atm_scale: int, scale, T, pg_top=0.1, fudge=
     if scale.shape != T.shape:
         raise ValueError("scale and T differ in shape")
     natm, ndep = T.shape
-    if natm < 1 or ndep < 2:
-        raise ValueError(f"{natm} atmospheres of {ndep} layers: need at least one of two")
+    if natm < 1 or ndep < 1:
+        raise ValueError(f"{natm} atmospheres of {ndep} layers")
     dev = model.dev_tables.device
     pg0 = np.array(np.broadcast_to(np.asarray(pg_top, np.float64), (natm,)))
     lay = lambda x: torch.from_numpy(np.ascontiguousarray(x.T)).to(dev)
