@@ -198,7 +198,8 @@ def _scales_job(args):
 
 
 def _synth_job(args):
-    workdir, pyrh_path, mu, atm, wave = args
+    workdir, pyrh_path, mu, atm, wave = args[:5]
+    atm_scale = args[5] if len(args) > 5 else 0
     lib = _lib(pyrh_path)
     atm = np.ascontiguousarray(atm, dtype=np.float64)
     wave = np.ascontiguousarray(wave, dtype=np.float64)
@@ -207,7 +208,7 @@ def _synth_job(args):
     flag = C.c_int(0)
     lib.harness_synth.restype = C.c_int
     n = lib.harness_synth(workdir.encode(), C.c_double(mu), atm.shape[1],
-                          _p(atm), 0, len(wave), _p(wave), cap,
+                          _p(atm), int(atm_scale), len(wave), _p(wave), cap,
                           *[_p(o) for o in out], C.byref(flag))
     if n < 0:
         raise RuntimeError("reference output larger than capacity")
@@ -382,8 +383,8 @@ class Reference:
         return self._run(_scales_job, (workdir, self.pyrh_path, atm_scale, scale, atm, lam_ref,
                                        ab_id, ab_val))
 
-    def synth(self, workdir, mu, atm, wave):
-        return self._run(_synth_job, (workdir, self.pyrh_path, mu, atm, wave))
+    def synth(self, workdir, mu, atm, wave, atm_scale=0):
+        return self._run(_synth_job, (workdir, self.pyrh_path, mu, atm, wave, atm_scale))
 
     def synth_loggf(self, workdir, mu, atm, wave, ids, vals, get_rfs=True):
         return self._run(_loggf_job, (workdir, self.pyrh_path, mu, atm, wave, ids, vals, get_rfs))

@@ -60,6 +60,7 @@ Fixtures (npz, float64):
   scales          pyrh.get_scales() of the C0 atmosphere on its three depth
                   scales, at two reference wavelengths, and with abundance
                   overrides
+  lte_scales      compute1d of C0 given on the column-mass and height scales
   hse             pyrh.hse() (ne, nHtot, rho, pg) on five atmospheres: C0 on
                   its log tau500 scale, a cooler one with another top
                   pressure, a height scale, abundance overrides, and opacity
@@ -654,13 +655,37 @@ def make_scales(ref, wd):
     print(f"scales: {len(cases)} cases, {os.path.getsize(path) / 1e3:.0f} kB")
 
 
+def make_lte_scales(ref, wd):
+    """compute1d of the C0 atmosphere and its two Fe I lines given on the
+    column-mass scale (log10 g cm^-2) and on the height scale (km) that
+    get_scales made of it (fixture scales), by both reference builds."""
+    d = np.load(os.path.join(HERE, "scales.npz"))
+    atm0 = d["atm"]
+    wave = wl.line_wavelengths(201, 0.05)
+    g_cm2 = 1.0e-3 / (1.0e-2 * 1.0e-2)
+    out = {"wave": wave}
+    for sc, row in ((1, np.log10(d["cmass"][0] / g_cm2)), (2, d["height"][0] / 1.0e3)):
+        atm = atm0.copy()
+        atm[0] = row
+        w = rr.scratch_dir()
+        rr.write_inputs(w, wl.fe_linelist())
+        lam_out, stokes, _ = ref.synth(w, 1.0, atm, wave, atm_scale=sc)
+        _, stokes_p, _ = PORTABLE.synth(w, 1.0, atm, wave, atm_scale=sc)
+        shutil.rmtree(w, ignore_errors=True)
+        out[f"atm_{sc}"], out[f"stokes_ref_{sc}"] = atm, stokes
+        out[f"stokes_ref_portable_{sc}"], out["lam_out"] = stokes_p, lam_out
+    path = os.path.join(HERE, "lte_scales.npz")
+    np.savez_compressed(path, **out)
+    print(f"lte_scales: {os.path.getsize(path) / 1e3:.0f} kB")
+
+
 MAKERS = {"lte_c0": make_lte_c0, "base_model": make_base_model, "lte_edge": make_lte_edge,
           "lte_b0": make_lte_b0, "lte_batch": make_lte_batch, "lte_dT": make_lte_dT,
           "lte_modes": make_lte_modes, "lte_loggf": make_lte_loggf,
           "lte_static": make_lte_static, "lte_broadening": make_lte_broadening,
           "nlte": make_nlte, "nlte_static": make_nlte_static, "kurucz": make_kurucz,
           "background": make_background, "ltepops": make_ltepops, "chem": make_chem,
-          "hse": make_hse, "scales": make_scales}
+          "hse": make_hse, "scales": make_scales, "lte_scales": make_lte_scales}
 
 
 def main():

@@ -104,3 +104,22 @@ def test_equilibria_match_reference_chemistry(golden, model, case):
         lo, hi = model.atoms.lev_off[m], model.atoms.lev_off[m + 1]
         np.testing.assert_allclose(p[lo:hi].sum(axis=0), d["ntot_model"][case][i], rtol=1e-12,
                                    atol=0)
+
+
+@pytest.mark.parametrize("atm_scale", [1, 2])
+def test_compute1d_on_column_mass_and_height_scales(golden, tmp_path, model, atm_scale):
+    """compute1d of C0 given on the column-mass or the height scale, its
+    heights from the device's convertScales: the reference's spectra of the
+    same calls (fixture lte_scales)."""
+    fx, d = golden("lte_c0"), golden("lte_scales")
+    cwd = keyword_dir(tmp_path, fx, "FULL_STOKES")
+    su = setup_of(fx)
+    su.chi_c = su.eta_c = su.height = su.np = None
+    su.line_pops, su.atoms_model = None, model
+    atm = np.ascontiguousarray(d[f"atm_{atm_scale}"])
+    got = C1.compute1d(cwd, 1.0, atm_scale, atm, d["wave"], setup=su)
+    ref = d[f"stokes_ref_portable_{atm_scale}"]
+    ic = ref[0].max()
+    assert np.array_equal(got[4], d["lam_out"])
+    for s in range(4):
+        assert np.abs(got[s] - ref[s]).max() < 1e-5 * ic
