@@ -214,30 +214,26 @@ pyrh_status launch_rf(const pyrh_lte_batch* b, const pyrh_line* d_lines, int nli
 }
 
 // Workspace of the host-buffer entry point: device buffers cached between
-// calls, and five streams (two for host-to-device copies, so that two copy
-// engines share the upload, two for kernels, one for device-to-host copies)
-// with per-chunk events for the pipelined upload.
+// calls, and four streams (host-to-device copies, two for kernels,
+// device-to-host copies) with per-chunk events for the pipelined upload.
 struct HostWs {
   std::mutex mu;
-  cudaStream_t stream = nullptr;      // host-to-device copies: everything but eta_c
-  cudaStream_t stream2 = nullptr;     // host-to-device copies: eta_c
+  cudaStream_t stream = nullptr;      // host-to-device copies
   cudaStream_t kstream[2] = {};       // kernels of even and odd chunks
   cudaStream_t ostream = nullptr;     // device-to-host copies
-  std::vector<cudaEvent_t> ev_in, ev_in2, ev_k;
+  std::vector<cudaEvent_t> ev_in, ev_k;
   std::vector<void*> bufs;
   std::vector<size_t> caps;
   cudaError_t init(int nchunk) {
     cudaError_t e = cudaSuccess;
-    for (cudaStream_t* s : {&stream, &stream2, &kstream[0], &kstream[1], &ostream})
+    for (cudaStream_t* s : {&stream, &kstream[0], &kstream[1], &ostream})
       if (!*s && (e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking)) != cudaSuccess) return e;
     while ((int)ev_in.size() < nchunk) {
-      cudaEvent_t a, b, c;
+      cudaEvent_t a, b;
       if ((e = cudaEventCreateWithFlags(&a, cudaEventDisableTiming)) != cudaSuccess) return e;
       if ((e = cudaEventCreateWithFlags(&b, cudaEventDisableTiming)) != cudaSuccess) return e;
-      if ((e = cudaEventCreateWithFlags(&c, cudaEventDisableTiming)) != cudaSuccess) return e;
       ev_in.push_back(a);
       ev_k.push_back(b);
-      ev_in2.push_back(c);
     }
     return e;
   }
@@ -581,13 +577,10 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host
                    sizeof(double) * (d1 - d0)));
     CUDA_TRY(h2d(db.lambda + l0, hb->lambda + l0, sizeof(double) * (l1 - l0)));
     CUDA_TRY(h2d(d_chi + real * c0, h_chi + real * c0, real * (c1 - c0)));
-    CUDA_TRY(cudaMemcpyAsync(d_eta + real * c0, h_eta + real * c0, real * (c1 - c0),
-                             cudaMemcpyHostToDevice, g_ws.stream2));
+    CUDA_TRY(h2d(d_eta + real * c0, h_eta + real * c0, real * (c1 - c0)));
     CUDA_TRY(cudaEventRecord(g_ws.ev_in[c], g_ws.stream));
-    CUDA_TRY(cudaEventRecord(g_ws.ev_in2[c], g_ws.stream2));
     cudaStream_t ks = g_ws.kstream[c & 1];
     CUDA_TRY(cudaStreamWaitEvent(ks, g_ws.ev_in[c], 0));
-    CUDA_TRY(cudaStreamWaitEvent(ks, g_ws.ev_in2[c], 0));
     pyrh_lte_batch cb = db;   // atmospheres [p0, p1): offsets stay absolute
     cb.natm = p1 - p0;
     cb.ndep = db.ndep + p0;
@@ -608,7 +601,6 @@ pyrh_status pyrh_lte_stokes_host(const pyrh_lte_batch* hb, const pyrh_line* host
   CUDA_TRY(cudaStreamSynchronize(g_ws.kstream[0]));
   CUDA_TRY(cudaStreamSynchronize(g_ws.kstream[1]));
   CUDA_TRY(cudaStreamSynchronize(g_ws.stream));
-  CUDA_TRY(cudaStreamSynchronize(g_ws.stream2));
   g_last_launches = nchunk;
   return PYRH_OK;
 }
