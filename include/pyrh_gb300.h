@@ -2,10 +2,12 @@
  *
  * Drop-in boundary for the polarized LTE synthesis that the reference runs
  * per atmosphere through rhf1d() (rh/rhf1d/pyrh_compute1dray.h:26-36, bound
- * to Python by pyrh.compute1d, pyrh.pyx:537-668).  The set-up that rhf1d()
- * does on the host before its hot loop -- reading *.input files, LTE stage
- * densities, background continuum, tau500 -> height -- is the caller's; this
- * library takes its results as arrays and runs, on one GB300:
+ * to Python by pyrh.compute1d, pyrh.pyx:537-668).  The synthesis takes the
+ * set-up that rhf1d() does before its hot loop -- LTE stage densities,
+ * background continuum, tau500 -> height -- as arrays, from the caller or
+ * from the set-up entry points further down (readers of the input files,
+ * element tables, LTE populations, n_e, chemical equilibrium, background,
+ * depth scales, hydrostatic equilibrium); it runs, on one GB300:
  *   - the Kurucz-line Zeeman/Voigt opacity of rlk_opacity()/RLKProfile()
  *     (rh/kurucz.c:511-827, Humlicek 1982 Voigt, rh/humlicek.c:28-118),
  *   - the formal solution of Formal() (rh/rhf1d/formal.c:44-346): DELO-Bezier3
