@@ -740,7 +740,9 @@ pyrh_status pyrh_background(const pyrh_bg_model* model, const pyrh_bg_batch* b, 
     return f32 ? pyrh::bg_smem_bytes<float>(b->max_ndep, bs, model->nonlte)
                : pyrh::bg_smem_bytes<double>(b->max_ndep, bs, model->nonlte);
   };
+  // a block's threads are its wavelengths: short spectra take narrower blocks
   int bs = pyrh::kBlock;
+  if (b->max_nspect < bs) bs = ((b->max_nspect + 31) / 32) * 32;
   while (bs > 32 && smem_of(bs) > 160 * 1024) bs -= 32;
   const size_t smem = smem_of(bs);
   if (smem > 220 * 1024) {
@@ -753,6 +755,9 @@ pyrh_status pyrh_background(const pyrh_bg_model* model, const pyrh_bg_batch* b, 
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int group = (int)(((int64_t)b->natm * ntile) / (4 * (int64_t)nsm));
   group = group < 1 ? 1 : (group > pyrh::kGroup ? pyrh::kGroup : group);
+  // fewer than 32 wavelengths leave most of a block's lanes idle; then a
+  // block per atmosphere spreads the atmospheres over the SMs instead
+  if (b->max_nspect < 32) group = 1;
   dim3 g(ntile, (b->natm + group - 1) / group);
   cudaError_t ea;
   if (f32) {
