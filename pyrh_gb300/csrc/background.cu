@@ -755,9 +755,6 @@ pyrh_status pyrh_background(const pyrh_bg_model* model, const pyrh_bg_batch* b, 
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int group = (int)(((int64_t)b->natm * ntile) / (4 * (int64_t)nsm));
   group = group < 1 ? 1 : (group > pyrh::kGroup ? pyrh::kGroup : group);
-  // fewer than 32 wavelengths leave most of a block's lanes idle; then a
-  // block per atmosphere spreads the atmospheres over the SMs instead
-  if (b->max_nspect < 32) group = 1;
   dim3 g(ntile, (b->natm + group - 1) / group);
   cudaError_t ea;
   if (f32) {
