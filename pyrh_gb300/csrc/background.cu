@@ -740,9 +740,7 @@ pyrh_status pyrh_background(const pyrh_bg_model* model, const pyrh_bg_batch* b, 
     return f32 ? pyrh::bg_smem_bytes<float>(b->max_ndep, bs, model->nonlte)
                : pyrh::bg_smem_bytes<double>(b->max_ndep, bs, model->nonlte);
   };
-  // a block's threads are its wavelengths: short spectra take narrower blocks
   int bs = pyrh::kBlock;
-  if (b->max_nspect < bs) bs = ((b->max_nspect + 31) / 32) * 32;
   while (bs > 32 && smem_of(bs) > 160 * 1024) bs -= 32;
   const size_t smem = smem_of(bs);
   if (smem > 220 * 1024) {
